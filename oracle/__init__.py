@@ -1,0 +1,169 @@
+"""Python access to the CPU checkers -- TEST INFRASTRUCTURE ONLY.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` use this package, always as the checker and never as the thing
+measured or shipped.
+
+* :class:`Oracle` wraps ``liboracle.so`` (the C++ restatement in
+  ``sdl_oracle.cc``; built by ``make -C oracle oracle``).
+* :func:`run_reference` runs ``_ref/ref_driver`` (the unmodified reference,
+  built by ``make -C oracle ref`` only where the reference sources exist).
+* :func:`canon` / :func:`digest` put stage outputs (hit-index tuples) in a
+  canonical multiset order so two implementations can be compared.
+"""
+from __future__ import annotations
+
+import ctypes
+import hashlib
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+STAGES = ("MD", "SG", "TL", "TP", "TC")
+WIDTH = (2, 4, 8, 8, 16)
+
+_i64, _i32, _u32, _f32 = ctypes.c_int64, ctypes.c_int32, ctypes.c_uint32, ctypes.c_float
+_vp = ctypes.c_void_p
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+def build(ref: bool = False) -> None:
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    if ref and os.path.isdir(os.environ.get("SDL_REFDIR", "/root/reference")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "-j8",
+                        "REFDIR=" + os.environ.get("SDL_REFDIR", "/root/reference")], check=True)
+
+
+_LIB = None
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = ctypes.CDLL(path)
+        L.sdlo_geometry_create.restype = _vp
+        L.sdlo_geometry_create.argtypes = [_i64, _vp, _vp, _i64, _vp, _vp, _i64, _vp, _vp, _vp]
+        L.sdlo_geometry_free.argtypes = [_vp]
+        L.sdlo_run.restype = _vp
+        L.sdlo_run.argtypes = [_vp, _i64, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int]
+        L.sdlo_count.restype = _i64
+        L.sdlo_count.argtypes = [_vp, ctypes.c_int]
+        L.sdlo_copy.argtypes = [_vp, ctypes.c_int, _vp]
+        L.sdlo_counters.argtypes = [_vp, _vp]
+        L.sdlo_times.argtypes = [_vp, _vp]
+        L.sdlo_free.argtypes = [_vp]
+        L.sdlo_run_many.restype = _i64
+        L.sdlo_run_many.argtypes = [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int]
+        _LIB = L
+    return _LIB
+
+
+class Oracle:
+    """The restated chain bound to one detector geometry."""
+
+    def __init__(self, det):
+        L = lib()
+        t_id, t_val, e_id, e_val, keys, off, dst = det.tables()
+        self._keep = [np.ascontiguousarray(a) for a in (t_id, t_val, e_id, e_val, keys, off, dst)]
+        t_id, t_val, e_id, e_val, keys, off, dst = self._keep
+        self.h = L.sdlo_geometry_create(len(t_id), t_id.ctypes.data, t_val.ctypes.data, len(e_id),
+                                        e_id.ctypes.data, e_val.ctypes.data, len(keys), keys.ctypes.data,
+                                        off.ctypes.data, dst.ctypes.data)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().sdlo_geometry_free(self.h)
+            self.h = None
+
+    def run(self, ev, mode: int = 0, stop_after: int = 4):
+        """Returns (tuples per stage, counters[110], seconds[5])."""
+        L = lib()
+        arrs = [np.ascontiguousarray(a) for a in (ev.x, ev.y, ev.z, ev.idx, ev.detid)]
+        r = L.sdlo_run(self.h, len(arrs[0]), *[a.ctypes.data for a in arrs], mode, stop_after)
+        try:
+            out = []
+            for s in range(5):
+                n = L.sdlo_count(r, s)
+                a = np.empty((n, WIDTH[s]), dtype=np.int32)
+                if n:
+                    L.sdlo_copy(r, s, a.ctypes.data)
+                out.append(a)
+            cnt = np.empty(110, dtype=np.uint32)
+            L.sdlo_counters(r, cnt.ctypes.data)
+            sec = np.empty(5, dtype=np.float64)
+            L.sdlo_times(r, sec.ctypes.data)
+        finally:
+            L.sdlo_free(r)
+        return out, cnt, sec
+
+    def run_many(self, events, n_threads: int, mode: int = 0) -> int:
+        """Runs whole chains on independent events in parallel threads;
+        returns the total track-candidate count."""
+        off = np.zeros(len(events) + 1, dtype=np.int64)
+        off[1:] = np.cumsum([len(e) for e in events])
+        cat = [np.ascontiguousarray(np.concatenate([getattr(e, k) for e in events]))
+               for k in ("x", "y", "z", "idx", "detid")]
+        return int(lib().sdlo_run_many(self.h, len(events), off.ctypes.data, *[a.ctypes.data for a in cat],
+                                       mode, n_threads))
+
+
+def read_dump(path):
+    """Reads a dump written by ref_driver (same layout as Oracle.run)."""
+    with open(path, "rb") as f:
+        data = f.read()
+    pos = 0
+    out = []
+    for s in range(5):
+        n, w = np.frombuffer(data, dtype=np.int64, count=2, offset=pos)
+        pos += 16
+        a = np.frombuffer(data, dtype=np.int32, count=int(n * w), offset=pos).reshape(int(n), int(w))
+        pos += int(n * w) * 4
+        out.append(a.copy())
+    cnt = np.frombuffer(data, dtype=np.uint32, count=110, offset=pos).copy()
+    pos += 440
+    sec = np.frombuffer(data, dtype=np.float64, count=5, offset=pos).copy()
+    return out, cnt, sec
+
+
+def run_reference(det, ev, mode: str = "map", workdir: str | None = None):
+    """Runs the compiled reference (oracle/_ref/ref_driver) on one event."""
+    exe = os.path.join(HERE, "_ref", "ref_driver")
+    if not os.path.exists(exe):
+        raise FileNotFoundError("reference driver not built (make -C oracle ref)")
+    with tempfile.TemporaryDirectory(dir=workdir) as d:
+        paths = det.write_files(d)
+        hb = os.path.join(d, "hits.bin")
+        ob = os.path.join(d, "out.bin")
+        ev.write_bin(hb)
+        subprocess.run([exe, *paths, hb, ob, mode], check=True, capture_output=True)
+        return read_dump(ob)
+
+
+def canon(t: np.ndarray) -> np.ndarray:
+    """Rows sorted lexicographically: the canonical form of a tuple multiset."""
+    t = np.ascontiguousarray(t, dtype=np.int32)
+    if t.shape[0] == 0:
+        return t
+    order = np.lexsort(t.T[::-1])
+    return t[order]
+
+
+def digest(t: np.ndarray) -> str:
+    return hashlib.sha256(canon(t).tobytes()).hexdigest()[:24]
+
+
+def multiset_diff(a: np.ndarray, b: np.ndarray):
+    """(rows in a not in b, rows in b not in a), multiplicity-aware."""
+    from collections import Counter
+    ca = Counter(map(tuple, np.asarray(a).tolist()))
+    cb = Counter(map(tuple, np.asarray(b).tolist()))
+    return list((ca - cb).elements()), list((cb - ca).elements())

@@ -1,0 +1,57 @@
+/*
+ * CPU restatement of the reference segment-linking chain -- TEST
+ * INFRASTRUCTURE ONLY.  Nothing in the product links this; the GPU parity
+ * tests, smoke() and the benchmark's CPU-baseline leg use it as the checker.
+ *
+ * It restates, in the reference's precision and operation order, the live
+ * code of Hit.cc:68-183, MathUtil.cc:3-27, GeometryUtil.cc:3-23,
+ * Module.cc:159-358, MiniDoublet.cc:60-81,228-684,741-810,989-1209,1242-1332,
+ * Segment.cc:337-994, Tracklet.cc:144-301,902-2665,3181-3331,
+ * Triplet.cc:50-122, TrackCandidate.cc:143-226 and the stage drivers of
+ * Event.cc:120-139,245-305,432-872.  It is pinned against the compiled
+ * reference (oracle/_ref) on the committed golden fixtures.
+ *
+ * Output: per stage (0 MD, 1 SG, 2 TL, 3 TP, 4 TC) a list of hit-index tuples
+ * of width 2, 4, 8, 8, 16, and the reference's per-layer counters
+ * (5 stages x {candidates, objects} x {barrel[6], endcap[5]}).
+ */
+#pragma once
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Geometry: tilted rows (detid, drdz, slope); endcap rows (detid, 8 values in
+ * file column order: avgr2 yl sl yh sh c7 c8 cz); connection map as CSR
+ * (keys[nk], off[nk+1], dst[off[nk]]). Later rows win for repeated keys, as
+ * the reference's load() does. */
+void* sdlo_geometry_create(int64_t n_tilted, const uint32_t* t_detid, const float* t_vals,
+                           int64_t n_endcap, const uint32_t* e_detid, const float* e_vals,
+                           int64_t n_keys, const uint32_t* keys, const int64_t* off,
+                           const uint32_t* dst);
+void sdlo_geometry_free(void* geo);
+
+/* mode bit 0: layer-pair segments (createSegments) instead of module map;
+ * bit 1: layer-pair tracklets (createTracklets) instead of module map;
+ * bit 2: DefaultNm1 tracklet algorithm (no deltaBeta rejection).
+ * stop_after: last stage to run (0 MD .. 4 TC). */
+void* sdlo_run(const void* geo, int64_t n, const float* x, const float* y, const float* z,
+               const int32_t* idx, const uint32_t* detid, int mode, int stop_after);
+int64_t sdlo_count(const void* res, int stage);
+int sdlo_width(int stage);
+void sdlo_copy(const void* res, int stage, int32_t* out);
+void sdlo_counters(const void* res, uint32_t* out110);
+void sdlo_times(const void* res, double* out5);
+void sdlo_free(void* res);
+
+/* Thread-parallel helper for the CPU baseline: runs n_events independent
+ * events (CSR over the concatenated hit arrays) on n_threads threads and
+ * returns the total number of track candidates. */
+int64_t sdlo_run_many(const void* geo, int64_t n_events, const int64_t* ev_off, const float* x,
+                      const float* y, const float* z, const int32_t* idx, const uint32_t* detid,
+                      int mode, int n_threads);
+
+#ifdef __cplusplus
+}
+#endif
