@@ -1,0 +1,128 @@
+/*
+ * sdl_gpu.h - C ABI of the GB300 segment-linking chain (libsdlgpu.so).
+ *
+ * The reference library (bsathian/SDL) is a C++ class library with no FFI of
+ * its own; a caller loads three geometry singletons, adds hits to an
+ * SDL::Event and calls the create* stages.  Each entry point below replaces
+ * one step of that call sequence (file:line of the reference interface in
+ * brackets) with plain pointers and sizes, so it can be bound from C, C++
+ * (see sdl_event.hpp), Python ctypes, or any other FFI.
+ *
+ * Conventions: every function returns SDLG_OK (0) or a negative SDLG_ERR_*
+ * code and never throws; sdlg_last_error() describes the last failure of a
+ * context.  A context owns one CUDA stream and all of its device memory; the
+ * functions of one context must not be called concurrently.  Host buffers
+ * are caller-owned and only read/written during the call.
+ *
+ * Objects are reported as hit-index tuples (the idx the caller gave each hit):
+ *   mini-doublet (lower, upper)                               width 2
+ *   segment      (inner MD, outer MD)                         width 4
+ *   tracklet / triplet (inner segment, outer segment)         width 8
+ *   track candidate (inner tracklet, outer tracklet)          width 16
+ * which is the identity the reference's isIdxMatched() uses
+ * (Hit.cc:175-182, MiniDoublet.cc:686-693, Segment.cc:868-875).
+ */
+#ifndef SDL_GPU_H
+#define SDL_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SDLG_OK 0
+#define SDLG_ERR_ARG (-1)          /* invalid argument */
+#define SDLG_ERR_CUDA (-2)         /* CUDA runtime error (message in sdlg_last_error) */
+#define SDLG_ERR_NO_GEOMETRY (-3)  /* sdlg_geometry_* not called yet */
+#define SDLG_ERR_NO_EVENTS (-4)    /* sdlg_set_events not called yet */
+#define SDLG_ERR_IO (-5)           /* geometry file unreadable */
+#define SDLG_ERR_DETID (-6)        /* detId that does not decode to a barrel/endcap module */
+#define SDLG_ERR_CAPACITY (-7)     /* object capacity could not be grown (device memory) */
+#define SDLG_ERR_DUP_IDX (-8)      /* reserved */
+#define SDLG_ERR_NO_DEVICE (-9)    /* no CUDA device */
+
+/* stages (create* order) */
+#define SDLG_STAGE_MD 0
+#define SDLG_STAGE_SG 1
+#define SDLG_STAGE_TL 2
+#define SDLG_STAGE_TP 3
+#define SDLG_STAGE_TC 4
+
+/* run flags */
+#define SDLG_FLAG_TL_NM1 4   /* tracklets with DefaultNm1_TLAlgo (Algo.h:23-28) */
+#define SDLG_FLAG_NO_GRAPH 8 /* launch stage by stage instead of replaying a CUDA graph */
+
+typedef struct sdlg_ctx sdlg_ctx;
+
+/* Create a context on CUDA device `device` (new SDL::Event's device state). */
+int sdlg_create(sdlg_ctx** out, int device);
+int sdlg_destroy(sdlg_ctx* ctx);
+const char* sdlg_last_error(const sdlg_ctx* ctx);
+
+/* Load the three geometry text files in the reference's formats:
+ * replaces SDL::tiltedGeometry.load (TiltedGeometry.cc:18-41),
+ * SDL::endcapGeometry.load (EndcapGeometry.cc:18-61; the 7th column is the
+ * centroid phi) and SDL::moduleConnectionMap.load (ModuleConnectionMap.cc:18-47).
+ * Any path may be NULL (empty table, as an unloaded singleton). */
+int sdlg_geometry_load_files(sdlg_ctx* ctx, const char* tilted_path, const char* endcap_path,
+                             const char* map_path);
+
+/* Same tables as arrays: tilted rows (detid, drdz, slope); endcap rows
+ * (detid, 8 floats in file column order avgr2 yl sl yh sh c7 c8 cz); the map
+ * as CSR keys[n_keys], off[n_keys+1], dst[off[n_keys]].  Later rows win for
+ * repeated keys, as in the reference's load(). */
+int sdlg_geometry_upload(sdlg_ctx* ctx, int64_t n_tilted, const uint32_t* t_detid, const float* t_vals,
+                         int64_t n_endcap, const uint32_t* e_detid, const float* e_vals, int64_t n_keys,
+                         const uint32_t* keys, const int64_t* off, const uint32_t* dst);
+
+/* Number of modules in the device module table. */
+int64_t sdlg_num_modules(const sdlg_ctx* ctx);
+
+/* Set the hits of a batch of n_events events (replaces
+ * SDL::Event::addHitToModule, Event.cc:120-139, for every hit).  Event e owns
+ * hits [ev_off[e], ev_off[e+1]) of the concatenated arrays.  Host buffers; the
+ * copy to the device is issued on the context stream (pinned buffers from
+ * sdlg_host_alloc are copied directly, others through a pinned staging
+ * buffer).  Hit idx values must be unique within an event. */
+int sdlg_set_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, const float* x, const float* y,
+                    const float* z, const int32_t* idx, const uint32_t* detid);
+
+/* Run the chain createMiniDoublets -> createSegmentsWithModuleMap ->
+ * createTrackletsWithModuleMap -> createTriplets -> createTrackCandidates
+ * (Event.cc:245-305, 445-522, 611-693, 524-597, 823-872) on every event of
+ * the batch, up to and including stage `stop_after`.  Synchronous: returns
+ * when the results are on the device.  Object capacities grow automatically. */
+int sdlg_run(sdlg_ctx* ctx, int stop_after, int flags);
+
+/* Enqueue the same chain on the context stream without waiting (for callers
+ * that overlap work or time the device); sdlg_sync() waits and resolves
+ * capacity overflows by re-running. */
+int sdlg_run_async(sdlg_ctx* ctx, int stop_after, int flags);
+int sdlg_sync(sdlg_ctx* ctx);
+
+/* Objects per stage for event `event` (or the whole batch when event < 0):
+ * out5[stage] (getNumberOfMiniDoublets ... getNumberOfTrackCandidates,
+ * Event.h:302-311). */
+int sdlg_get_counts(sdlg_ctx* ctx, int64_t event, int64_t* out5);
+
+/* Copy the hit-index tuples of one stage of one event (event < 0: all) into
+ * out (capacity `cap` tuples); *n_out receives the number of tuples. */
+int sdlg_get_objects(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int64_t cap, int64_t* n_out);
+
+/* The reference's per-layer counters for one event (Event.cc:1064-1344):
+ * 5 stages x {candidates, objects} x {barrel layers 1-6, endcap layers 1-5}. */
+int sdlg_get_counters(sdlg_ctx* ctx, int64_t event, uint32_t* out110);
+
+/* Device time of the last run: [0] ingest, [1..5] MD..TC stages, [6] total (ms). */
+int sdlg_last_times(sdlg_ctx* ctx, float* out7);
+
+/* Pinned host memory for zero-staging transfers. */
+int sdlg_host_alloc(sdlg_ctx* ctx, int64_t bytes, void** out);
+int sdlg_host_free(sdlg_ctx* ctx, void* p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SDL_GPU_H */

@@ -1,0 +1,185 @@
+"""GB300 segment-linking chain: Python binding of libsdlgpu.so (C ABI in
+include/sdl_gpu.h).
+
+The classes mirror the reference's user-facing calls:
+
+* :class:`Geometry`-loading methods replace ``SDL::tiltedGeometry.load``,
+  ``SDL::endcapGeometry.load`` and ``SDL::moduleConnectionMap.load``;
+* :meth:`Chain.set_events` replaces ``SDL::Event::addHitToModule`` for every
+  hit of a batch of events;
+* :meth:`Chain.run` replaces ``createMiniDoublets ->
+  createSegmentsWithModuleMap -> createTrackletsWithModuleMap ->
+  createTriplets -> createTrackCandidates``;
+* :meth:`Chain.objects` / :meth:`Chain.counts` / :meth:`Chain.counters`
+  replace the object lists and ``getNumberOf*`` counters.
+
+There is no CPU fallback: a missing library or CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsdlgpu.so")
+
+STAGES = ("MD", "SG", "TL", "TP", "TC")
+WIDTH = (2, 4, 8, 8, 16)
+FLAG_TL_NM1 = 4
+FLAG_NO_GRAPH = 8
+
+
+class SDLError(RuntimeError):
+    pass
+
+
+_LIB = None
+
+
+def lib():
+    """Load libsdlgpu.so (raises if it is missing: there is no fallback)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise SDLError("libsdlgpu.so is not built (run __graft_entry__.build() or sdl_gb300/build.py)")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+        L.sdlg_create.argtypes = [ctypes.POINTER(vp), i32]
+        L.sdlg_destroy.argtypes = [vp]
+        L.sdlg_last_error.argtypes = [vp]
+        L.sdlg_last_error.restype = ctypes.c_char_p
+        L.sdlg_geometry_load_files.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
+        L.sdlg_geometry_upload.argtypes = [vp, i64, vp, vp, i64, vp, vp, i64, vp, vp, vp]
+        L.sdlg_num_modules.argtypes = [vp]
+        L.sdlg_num_modules.restype = i64
+        L.sdlg_set_events.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp]
+        L.sdlg_run.argtypes = [vp, i32, i32]
+        L.sdlg_run_async.argtypes = [vp, i32, i32]
+        L.sdlg_sync.argtypes = [vp]
+        L.sdlg_get_counts.argtypes = [vp, i64, vp]
+        L.sdlg_get_objects.argtypes = [vp, i32, i64, vp, i64, vp]
+        L.sdlg_get_counters.argtypes = [vp, i64, vp]
+        L.sdlg_last_times.argtypes = [vp, vp]
+        L.sdlg_host_alloc.argtypes = [vp, i64, ctypes.POINTER(vp)]
+        L.sdlg_host_free.argtypes = [vp, vp]
+        _LIB = L
+    return _LIB
+
+
+class Chain:
+    """One device context: geometry, a batch of events and their results."""
+
+    def __init__(self, device: int = 0):
+        L = lib()
+        h = ctypes.c_void_p()
+        rc = L.sdlg_create(ctypes.byref(h), device)
+        if rc != 0:
+            raise SDLError("sdlg_create failed (%d): no usable CUDA device %d" % (rc, device))
+        self.h = h
+        self._pinned = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            for p in self._pinned:
+                lib().sdlg_host_free(self.h, p)
+            self._pinned = []
+            lib().sdlg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ck(self, rc):
+        if rc != 0:
+            raise SDLError("%d: %s" % (rc, lib().sdlg_last_error(self.h).decode()))
+
+    # geometry -------------------------------------------------------------
+    def load_files(self, tilted=None, endcap=None, cmap=None):
+        enc = lambda p: p.encode() if p else None
+        self._ck(lib().sdlg_geometry_load_files(self.h, enc(tilted), enc(endcap), enc(cmap)))
+
+    def upload_tables(self, t_id, t_val, e_id, e_val, keys, off, dst):
+        arrs = [np.ascontiguousarray(a, dtype=d) for a, d in
+                ((t_id, np.uint32), (t_val, np.float32), (e_id, np.uint32), (e_val, np.float32),
+                 (keys, np.uint32), (off, np.int64), (dst, np.uint32))]
+        t_id, t_val, e_id, e_val, keys, off, dst = arrs
+        self._ck(lib().sdlg_geometry_upload(self.h, len(t_id), t_id.ctypes.data, t_val.ctypes.data, len(e_id),
+                                            e_id.ctypes.data, e_val.ctypes.data, len(keys), keys.ctypes.data,
+                                            off.ctypes.data, dst.ctypes.data))
+
+    def upload_detector(self, det):
+        """Geometry tables of a :class:`sdl_gb300.synth.Detector`."""
+        self.upload_tables(*det.tables())
+
+    @property
+    def num_modules(self) -> int:
+        return int(lib().sdlg_num_modules(self.h))
+
+    # events -----------------------------------------------------------------
+    def pinned(self, nbytes: int) -> np.ndarray:
+        """A pinned host byte buffer owned by this context."""
+        p = ctypes.c_void_p()
+        self._ck(lib().sdlg_host_alloc(self.h, nbytes, ctypes.byref(p)))
+        self._pinned.append(p)
+        return np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(p.value))
+
+    def set_events(self, events=None, *, ev_off=None, x=None, y=None, z=None, idx=None, detid=None):
+        """Either a list of objects with x/y/z/idx/detid arrays, or the
+        concatenated arrays with ev_off (int64, n_events + 1)."""
+        if events is not None:
+            ev_off = np.zeros(len(events) + 1, dtype=np.int64)
+            ev_off[1:] = np.cumsum([len(e.x) for e in events])
+            x = np.concatenate([e.x for e in events])
+            y = np.concatenate([e.y for e in events])
+            z = np.concatenate([e.z for e in events])
+            idx = np.concatenate([e.idx for e in events])
+            detid = np.concatenate([e.detid for e in events])
+        ev_off = np.ascontiguousarray(ev_off, dtype=np.int64)
+        arrs = [np.ascontiguousarray(a, dtype=d) for a, d in
+                ((x, np.float32), (y, np.float32), (z, np.float32), (idx, np.int32), (detid, np.uint32))]
+        self._ck(lib().sdlg_set_events(self.h, len(ev_off) - 1, ev_off.ctypes.data, *[a.ctypes.data for a in arrs]))
+        self.n_events = len(ev_off) - 1
+
+    def set_events_raw(self, n_events, ev_off_ptr, x_ptr, y_ptr, z_ptr, idx_ptr, det_ptr):
+        self._ck(lib().sdlg_set_events(self.h, n_events, ev_off_ptr, x_ptr, y_ptr, z_ptr, idx_ptr, det_ptr))
+        self.n_events = n_events
+
+    # running ----------------------------------------------------------------
+    def run(self, stop_after: int = 4, flags: int = 0):
+        self._ck(lib().sdlg_run(self.h, stop_after, flags))
+
+    def run_async(self, stop_after: int = 4, flags: int = 0):
+        self._ck(lib().sdlg_run_async(self.h, stop_after, flags))
+
+    def sync(self):
+        self._ck(lib().sdlg_sync(self.h))
+
+    # results ----------------------------------------------------------------
+    def counts(self, event: int = -1) -> np.ndarray:
+        out = np.zeros(5, dtype=np.int64)
+        self._ck(lib().sdlg_get_counts(self.h, event, out.ctypes.data))
+        return out
+
+    def objects(self, stage: int, event: int = -1) -> np.ndarray:
+        n = ctypes.c_int64()
+        self._ck(lib().sdlg_get_objects(self.h, stage, event, None, 0, ctypes.byref(n)))
+        out = np.empty((n.value, WIDTH[stage]), dtype=np.int32)
+        if n.value:
+            self._ck(lib().sdlg_get_objects(self.h, stage, event, out.ctypes.data, n.value, ctypes.byref(n)))
+        return out
+
+    def counters(self, event: int = 0) -> np.ndarray:
+        out = np.zeros(110, dtype=np.uint32)
+        self._ck(lib().sdlg_get_counters(self.h, event, out.ctypes.data))
+        return out
+
+    def times(self) -> np.ndarray:
+        """Device ms of the last run: ingest, MD, SG, TL, TP, TC, total."""
+        out = np.zeros(7, dtype=np.float32)
+        self._ck(lib().sdlg_last_times(self.h, out.ctypes.data))
+        return out

@@ -1,0 +1,756 @@
+// Host side of the GB300 segment-linking chain: context, geometry tables,
+// device buffers and the C ABI declared in include/sdl_gpu.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/sdl_gpu.h"
+#include "sdl_kernels.h"
+
+using namespace sdlg;
+
+namespace {
+
+// ------------------------------------------------------------------ detId decoding (Module.cc:159-358)
+struct Decoded {
+    uint16_t subdet, side, layer, rod, ring, module;
+    bool lower, inverted;
+    uint8_t type, ltype;
+    uint32_t partner;
+};
+
+Decoded decode(uint32_t d) {
+    Decoded m{};
+    m.subdet = (d >> 25) & 7;
+    const bool ec = m.subdet == kEndcap, br = m.subdet == kBarrel;
+    m.side = ec ? (d >> 23) & 3 : br ? (d >> 18) & 3 : 0;
+    m.layer = ec ? (d >> 18) & 7 : br ? (d >> 20) & 7 : 0;
+    m.rod = br ? (d >> 10) & 127 : 0;
+    m.ring = ec ? (d >> 12) & 15 : 0;
+    m.module = (d >> 2) & 127;
+    bool inv = false;
+    if (ec) inv = m.side == kNegZ ? (m.module % 2 == 1) : m.side == kPosZ ? (m.module % 2 == 0) : false;
+    else if (br) {
+        if (m.side == kCenter) inv = m.layer <= 3 ? (m.module % 2 == 1) : (m.module % 2 == 0);
+        else if (m.side == kNegZ || m.side == kPosZ) inv = m.layer <= 2 ? (m.module % 2 == 1) : m.layer == 3 ? (m.module % 2 == 0) : false;
+    }
+    m.inverted = inv;
+    m.lower = inv ? !(d & 1) : (d & 1);
+    m.partner = m.lower ? (inv ? d - 1 : d + 1) : (inv ? d + 1 : d - 1);
+    if (br) m.type = m.layer <= 3 ? kPS : kTwoS;
+    else m.type = (m.layer <= 2 ? m.ring <= 10 : m.ring <= 7) ? kPS : kTwoS;
+    m.ltype = m.type == kTwoS ? kStrip : (inv ? (m.lower ? kStrip : kPixel) : (m.lower ? kPixel : kStrip));
+    return m;
+}
+
+bool valid_module(const Decoded& m) {
+    if (m.subdet == kBarrel) return m.layer >= 1 && m.layer <= 6;
+    if (m.subdet == kEndcap) return m.layer >= 1 && m.layer <= 5 && m.ring >= 1 && m.ring <= 15;
+    return false;
+}
+
+// MiniDoublet.cc:1242-1332 (sensor gap of a module)
+float gap_size(const Decoded& m) {
+    const bool b = m.subdet == kBarrel;
+    const bool tighter = (b && m.side != kCenter && m.layer == 3) || (b && m.side == kNegZ && m.layer == 2 && m.rod > 5) ||
+                         (b && m.side == kPosZ && m.layer == 2 && m.rod < 8) || (b && m.side == kNegZ && m.layer == 1 && m.rod > 9) ||
+                         (b && m.side == kPosZ && m.layer == 1 && m.rod < 4);
+    static const float flat[6] = {0.26f, 0.16f, 0.16f, 0.18f, 0.18f, 0.18f};
+    const int iL = m.layer - 1;
+    if (b && m.side == kCenter) return flat[iL];
+    if (tighter) return 0.26f;
+    if (m.subdet == kEndcap) {
+        const int lim = iL <= 1 ? 10 : iL <= 3 ? 8 : 9;
+        return (m.ring - 1) < lim ? 0.4f : 0.18f;
+    }
+    return 0.4f;
+}
+
+struct HostGeometry {
+    std::map<uint32_t, std::pair<float, float>> tilted;  // drdz, slope
+    std::map<uint32_t, std::pair<float, float>> endcap;  // slope lower, centroid phi (7th column)
+    std::map<uint32_t, std::vector<uint32_t>> conn;
+};
+
+template <class T>
+struct DevBuf {
+    T* p = nullptr;
+    int64_t n = 0;
+};
+
+}  // namespace
+
+struct sdlg_ctx {
+    int device = 0;
+    int n_sm = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    bool have_geo = false;
+    HostGeometry hg;
+    std::vector<uint32_t> detids;  // sorted module table
+    std::vector<ModDev> mods;
+    std::vector<int32_t> conn_off, conn_idx;
+    // device geometry
+    uint32_t* d_detid = nullptr;
+    ModDev* d_mod = nullptr;
+    int32_t* d_conn_off = nullptr;
+    int32_t* d_conn_idx = nullptr;
+    // batch
+    int64_t n_ev = 0, n_hit = 0;
+    std::vector<int64_t> ev_off;
+    BatchDev b{};
+    std::vector<void*> allocs;  // batch allocations
+    int64_t cap_hit = 0, cap_ev = 0;
+    int64_t cap_obj[kNumStages] = {0, 0, 0, 0, 0};
+    bool buffers_ok = false;
+    // pinned staging
+    void* pinned = nullptr;
+    int64_t pinned_bytes = 0;
+    int64_t* h_small = nullptr;   // pinned: n_rec[5], status
+    // graph
+    cudaGraphExec_t graph = nullptr;
+    int graph_stop = -1, graph_flags = -1;
+    // timing
+    cudaEvent_t ev[8];
+    int last_stop = -1, last_flags = 0;
+    bool ran = false;
+};
+
+namespace {
+
+int fail(sdlg_ctx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+void free_batch(sdlg_ctx* ctx) {
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
+    for (void* p : ctx->allocs) cudaFree(p);
+    ctx->allocs.clear();
+    ctx->buffers_ok = false;
+}
+
+template <class T>
+int dalloc(sdlg_ctx* ctx, T** p, int64_t n) {
+    void* q = nullptr;
+    const size_t bytes = (size_t)std::max<int64_t>(n, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CAPACITY, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    ctx->allocs.push_back(q);
+    *p = static_cast<T*>(q);
+    return SDLG_OK;
+}
+
+int build_module_table(sdlg_ctx* ctx, const std::vector<uint32_t>& extra) {
+    std::vector<uint32_t> ids;
+    for (auto& kv : ctx->hg.tilted) ids.push_back(kv.first);
+    for (auto& kv : ctx->hg.endcap) ids.push_back(kv.first);
+    for (auto& kv : ctx->hg.conn) {
+        ids.push_back(kv.first);
+        for (uint32_t d : kv.second) ids.push_back(d);
+    }
+    ids.insert(ids.end(), ctx->detids.begin(), ctx->detids.end());
+    ids.insert(ids.end(), extra.begin(), extra.end());
+    std::vector<uint32_t> valid;
+    for (uint32_t d : ids) {
+        const Decoded m = decode(d);
+        if (!valid_module(m)) continue;
+        valid.push_back(d);
+        valid.push_back(m.partner);
+    }
+    std::sort(valid.begin(), valid.end());
+    valid.erase(std::unique(valid.begin(), valid.end()), valid.end());
+    ctx->detids = valid;
+    const int n = (int)valid.size();
+    auto index_of = [&](uint32_t d) -> int {
+        auto it = std::lower_bound(valid.begin(), valid.end(), d);
+        return (it != valid.end() && *it == d) ? (int)(it - valid.begin()) : -1;
+    };
+    auto tget = [&](uint32_t d, int k) -> float {
+        auto it = ctx->hg.tilted.find(d);
+        return it == ctx->hg.tilted.end() ? 0.f : (k ? it->second.second : it->second.first);
+    };
+    auto eget = [&](uint32_t d, int k) -> float {
+        auto it = ctx->hg.endcap.find(d);
+        return it == ctx->hg.endcap.end() ? 0.f : (k ? it->second.second : it->second.first);
+    };
+    ctx->mods.assign(n, ModDev{});
+    for (int i = 0; i < n; ++i) {
+        const uint32_t d = valid[i];
+        const Decoded m = decode(d);
+        ModDev& o = ctx->mods[i];
+        o.detid = d;
+        o.partner = index_of(m.partner);
+        o.subdet = (uint8_t)m.subdet; o.side = (uint8_t)m.side; o.layer = (uint8_t)m.layer; o.ring = (uint8_t)m.ring;
+        o.rod = (uint8_t)m.rod; o.module = (uint8_t)m.module; o.lower = m.lower; o.inverted = m.inverted;
+        o.type = m.type; o.ltype = m.ltype;
+        o.layer_slot = (uint8_t)(m.subdet == kBarrel ? m.layer - 1 : 6 + m.layer - 1);
+        o.gap = gap_size(m);
+        // the strip sensor of the pair keys the tilted / endcap lookups (MiniDoublet.cc:781,1040-1053)
+        const uint32_t strip = m.ltype == kPixel ? m.partner : d;
+        o.drdz_s = tget(strip, 0);
+        o.slope_s = m.subdet == kEndcap ? eget(strip, 0) : tget(strip, 1);
+        // GeometryUtil.cc:12-16: the edge offset along this sensor's centroid phi
+        const float phi = eget(d, 1);
+        o.edge_x = (float)(2.5 * std::cos((double)phi));
+        o.edge_y = (float)(2.5 * std::sin((double)phi));
+    }
+    ctx->conn_off.assign(n + 1, 0);
+    ctx->conn_idx.clear();
+    for (int i = 0; i < n; ++i) {
+        auto it = ctx->hg.conn.find(valid[i]);
+        if (it != ctx->hg.conn.end())
+            for (uint32_t d : it->second) {
+                const int k = index_of(d);
+                if (k >= 0) ctx->conn_idx.push_back(k);
+            }
+        ctx->conn_off[i + 1] = (int32_t)ctx->conn_idx.size();
+    }
+    // upload
+    free_batch(ctx);
+    cudaFree(ctx->d_detid); cudaFree(ctx->d_mod); cudaFree(ctx->d_conn_off); cudaFree(ctx->d_conn_idx);
+    ctx->d_detid = nullptr; ctx->d_mod = nullptr; ctx->d_conn_off = nullptr; ctx->d_conn_idx = nullptr;
+    CK(cudaMalloc(&ctx->d_detid, std::max(1, n) * sizeof(uint32_t)));
+    CK(cudaMalloc(&ctx->d_mod, std::max(1, n) * sizeof(ModDev)));
+    CK(cudaMalloc(&ctx->d_conn_off, (n + 1) * sizeof(int32_t)));
+    CK(cudaMalloc(&ctx->d_conn_idx, std::max<size_t>(1, ctx->conn_idx.size()) * sizeof(int32_t)));
+    CK(cudaMemcpy(ctx->d_detid, valid.data(), n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_mod, ctx->mods.data(), n * sizeof(ModDev), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_conn_off, ctx->conn_off.data(), (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice));
+    if (!ctx->conn_idx.empty())
+        CK(cudaMemcpy(ctx->d_conn_idx, ctx->conn_idx.data(), ctx->conn_idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    ctx->have_geo = true;
+    return SDLG_OK;
+}
+
+// (re)allocate the batch buffers for the current event sizes and capacities
+int ensure_buffers(sdlg_ctx* ctx) {
+    const int n_mod = (int)ctx->detids.size();
+    const int64_t n_gm = ctx->n_ev * n_mod;
+    if (ctx->buffers_ok && ctx->n_hit <= ctx->cap_hit && ctx->n_ev == ctx->cap_ev) return SDLG_OK;
+    free_batch(ctx);
+    ctx->cap_hit = std::max<int64_t>(ctx->n_hit, ctx->cap_hit);
+    ctx->cap_ev = ctx->n_ev;
+    const int64_t H = std::max<int64_t>(ctx->cap_hit, 1024);
+    const int64_t mult[kNumStages] = {1, 2, 3, 4, 2};
+    for (int s = 0; s < kNumStages; ++s) ctx->cap_obj[s] = std::max<int64_t>(ctx->cap_obj[s], H * mult[s] + 4096);
+    BatchDev& b = ctx->b;
+    b = BatchDev{};
+    b.geo.n_mod = n_mod;
+    b.geo.n_conn = (int)ctx->conn_idx.size();
+    b.geo.detid = ctx->d_detid;
+    b.geo.mod = ctx->d_mod;
+    b.geo.conn_off = ctx->d_conn_off;
+    b.geo.conn_idx = ctx->d_conn_idx;
+    b.n_ev = (int)ctx->n_ev;
+    b.n_gm = (int)n_gm;
+    b.n_hit_cap = H;
+    b.n_sm = ctx->n_sm;
+    int rc;
+#define AL(ptr, n) if ((rc = dalloc(ctx, &(ptr), (n))) != SDLG_OK) return rc
+    int64_t* small;
+    AL(small, 2 + kNumStages);
+    b.n_hit = small;
+    b.n_gm_dev = small + 1;
+    b.n_rec = small + 2;
+    float* fx; float* fy; float* fz; int32_t* fi; uint32_t* fd; int64_t* eo;
+    AL(fx, H); AL(fy, H); AL(fz, H); AL(fi, H); AL(fd, H); AL(eo, ctx->n_ev + 1);
+    b.in_x = fx; b.in_y = fy; b.in_z = fz; b.in_idx = fi; b.in_det = fd; b.ev_off = eo;
+    AL(b.hit_gm, H); AL(b.hit_rank, H); AL(b.mod_hit, n_gm + 1);
+    AL(b.hx, H); AL(b.hy, H); AL(b.hz, H); AL(b.hrt, H); AL(b.hphi, H); AL(b.hr3, H);
+    AL(b.ha1, H); AL(b.htf, H); AL(b.htd, H); AL(b.ha3, H); AL(b.hidx, H); AL(b.hgm, H);
+    const int nf[kNumStages] = {4, 6, 0, 0, 0};
+    for (int s = 0; s < kNumStages; ++s) {
+        const int64_t C = ctx->cap_obj[s];
+        Objs& O = b.obj[s];
+        Recs& R = b.rec[s];
+        O.cap = C; O.nf = nf[s]; R.nf = nf[s];
+        AL(O.i, C); AL(O.j, C); AL(O.g, C); AL(O.f, C * std::max(1, nf[s])); AL(O.mod_cnt, n_gm + 1);
+        AL(R.i, C); AL(R.j, C); AL(R.g, C); AL(R.rank, C); AL(R.f, C * std::max(1, nf[s]));
+    }
+    b.cand_cap[kMD] = n_gm;
+    b.cand_cap[kSG] = ctx->cap_obj[kMD];
+    b.cand_cap[kTL] = ctx->cap_obj[kSG];
+    b.cand_cap[kTP] = ctx->cap_obj[kSG];
+    b.cand_cap[kTC] = ctx->cap_obj[kTL];
+    for (int s = 0; s < kNumStages; ++s) AL(b.cand[s], b.cand_cap[s] + 1);
+    AL(b.conn_pref, std::max<int64_t>(1, ctx->n_ev * (int64_t)ctx->conn_idx.size()));
+    AL(b.conn_sum, n_gm);
+    AL(b.counters, ctx->n_ev * 110);
+    AL(b.status, 1);
+    AL(b.task, kNumStages);
+    AL(b.dbg, 8);
+    int64_t mx = n_gm;
+    for (int s = 0; s < kNumStages; ++s) mx = std::max(mx, ctx->cap_obj[s]);
+    b.scan_tmp_cap = mx / 4096 + 16;
+    AL(b.scan_tmp, b.scan_tmp_cap);
+#undef AL
+    CK(cudaMemcpyAsync(b.n_gm_dev, &n_gm, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->buffers_ok = true;
+    return SDLG_OK;
+}
+
+// events recorded while a stream is captured must become graph nodes
+inline void record(cudaEvent_t e, cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &st);
+    if (st == cudaStreamCaptureStatusActive) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+    else cudaEventRecord(e, s);
+}
+
+// the full chain, enqueued on the context stream (also the body of the CUDA graph)
+void enqueue_chain(sdlg_ctx* ctx, int stop_after) {
+    BatchDev& b = ctx->b;
+    cudaStream_t s = ctx->stream;
+    const int64_t n_gm = b.n_gm;
+    record(ctx->ev[0], s);
+    cudaMemsetAsync(b.status, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(b.dbg, 0, 8 * sizeof(unsigned long long), s);
+    cudaMemsetAsync(b.n_rec, 0, kNumStages * sizeof(int64_t), s);
+    cudaMemsetAsync(b.task, 0, kNumStages * sizeof(unsigned long long), s);
+    cudaMemsetAsync(b.counters, 0, b.n_ev * 110 * sizeof(uint32_t), s);
+    cudaMemsetAsync(b.mod_hit, 0, (n_gm + 1) * sizeof(int64_t), s);
+    for (int st = 0; st < kNumStages; ++st) cudaMemsetAsync(b.obj[st].mod_cnt, 0, (n_gm + 1) * sizeof(int64_t), s);
+    launch_ingest(b, s);
+    record(ctx->ev[1], s);
+    if (stop_after >= kMD) launch_md(b, s);
+    record(ctx->ev[2], s);
+    if (stop_after >= kSG) launch_sg(b, s);
+    record(ctx->ev[3], s);
+    if (stop_after >= kTL) launch_tl(b, s);
+    record(ctx->ev[4], s);
+    if (stop_after >= kTP) launch_tp(b, s);
+    record(ctx->ev[5], s);
+    if (stop_after >= kTC) launch_tc(b, s);
+    record(ctx->ev[6], s);
+    // status word and attempted appends for the host's overflow check
+    cudaMemcpyAsync(ctx->h_small, b.n_rec, kNumStages * sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(ctx->h_small + kNumStages, b.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+}
+
+#ifdef SDL_DEVICE_CHECKS
+// debug builds: run stage by stage, synchronising after each, and report the
+// first out-of-bounds index the device checks recorded
+int check_stage(sdlg_ctx* ctx, const char* what) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    unsigned long long d[4];
+    CK(cudaMemcpy(d, ctx->b.dbg, sizeof(d), cudaMemcpyDeviceToHost));
+    if (d[0]) return fail(ctx, SDLG_ERR_CUDA, "%s: %llu bad indices, first at sdl_kernels.cu:%llu index %lld limit %lld", what,
+                          d[0], d[1], (long long)d[2], (long long)d[3]);
+    return SDLG_OK;
+}
+
+int launch_checked(sdlg_ctx* ctx, int stop_after) {
+    BatchDev& b = ctx->b;
+    cudaStream_t s = ctx->stream;
+    const int64_t n_gm = b.n_gm;
+    cudaMemsetAsync(b.status, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(b.dbg, 0, 8 * sizeof(unsigned long long), s);
+    cudaMemsetAsync(b.n_rec, 0, kNumStages * sizeof(int64_t), s);
+    cudaMemsetAsync(b.task, 0, kNumStages * sizeof(unsigned long long), s);
+    cudaMemsetAsync(b.counters, 0, b.n_ev * 110 * sizeof(uint32_t), s);
+    cudaMemsetAsync(b.mod_hit, 0, (n_gm + 1) * sizeof(int64_t), s);
+    for (int st = 0; st < kNumStages; ++st) cudaMemsetAsync(b.obj[st].mod_cnt, 0, (n_gm + 1) * sizeof(int64_t), s);
+    int rc;
+    record(ctx->ev[0], s);
+    launch_ingest(b, s);
+    if ((rc = check_stage(ctx, "ingest"))) return rc;
+    record(ctx->ev[1], s);
+    void (*fns[5])(const BatchDev&, cudaStream_t) = {launch_md, launch_sg, launch_tl, launch_tp, launch_tc};
+    static const char* names[5] = {"MD", "SG", "TL", "TP", "TC"};
+    for (int st = 0; st < 5; ++st) {
+        if (stop_after >= st) fns[st](b, s);
+        if ((rc = check_stage(ctx, names[st]))) return rc;
+        record(ctx->ev[2 + st], s);
+    }
+    cudaMemcpyAsync(ctx->h_small, b.n_rec, kNumStages * sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(ctx->h_small + kNumStages, b.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    return SDLG_OK;
+}
+#endif
+
+int launch(sdlg_ctx* ctx, int stop_after, int flags) {
+    ctx->b.flags = flags;
+    ctx->ran = true;
+#ifdef SDL_DEVICE_CHECKS
+    return launch_checked(ctx, stop_after);
+#endif
+    const bool use_graph = !(flags & SDLG_FLAG_NO_GRAPH);
+    if (!use_graph) {
+        enqueue_chain(ctx, stop_after);
+        CK(cudaGetLastError());
+        return SDLG_OK;
+    }
+    if (!ctx->graph || ctx->graph_stop != stop_after || ctx->graph_flags != flags) {
+        if (ctx->graph) {
+            cudaGraphExecDestroy(ctx->graph);
+            ctx->graph = nullptr;
+        }
+        cudaGraph_t g;
+        CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_chain(ctx, stop_after);
+        CK(cudaStreamEndCapture(ctx->stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&ctx->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+        ctx->graph_stop = stop_after;
+        ctx->graph_flags = flags;
+    }
+    CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+    return SDLG_OK;
+}
+
+// wait for a run; grow overflowing capacities and re-run until clean
+int finish(sdlg_ctx* ctx) {
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        const uint32_t status = (uint32_t)(ctx->h_small[kNumStages] & 0xffffffffu);
+        if (status & kStatusUnknownModule) {
+            // new detIds: extend the module table and re-run (modules created on
+            // demand, Event.cc:54-78)
+            std::vector<uint32_t> hd(ctx->n_hit);
+            CK(cudaMemcpy(hd.data(), ctx->b.in_det, ctx->n_hit * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+            std::vector<float> keep[3];
+            std::vector<int32_t> ki(ctx->n_hit);
+            for (int k = 0; k < 3; ++k) keep[k].resize(ctx->n_hit);
+            CK(cudaMemcpy(keep[0].data(), ctx->b.in_x, ctx->n_hit * 4, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(keep[1].data(), ctx->b.in_y, ctx->n_hit * 4, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(keep[2].data(), ctx->b.in_z, ctx->n_hit * 4, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(ki.data(), ctx->b.in_idx, ctx->n_hit * 4, cudaMemcpyDeviceToHost));
+            for (uint32_t d : hd)
+                if (!valid_module(decode(d))) return fail(ctx, SDLG_ERR_DETID, "detId %u is not a barrel or endcap module", d);
+            const std::vector<int64_t> off = ctx->ev_off;
+            int rc = build_module_table(ctx, hd);
+            if (rc) return rc;
+            rc = sdlg_set_events(ctx, ctx->n_ev, off.data(), keep[0].data(), keep[1].data(), keep[2].data(), ki.data(), hd.data());
+            if (rc) return rc;
+            rc = launch(ctx, ctx->last_stop, ctx->last_flags);
+            if (rc) return rc;
+            continue;
+        }
+        if (!(status & 0x1fu)) return SDLG_OK;
+        // grow every stage that overflowed (the attempted-append counters hold
+        // the exact need of the first overflowing stage)
+        bool grew = false;
+        for (int s = 0; s < kNumStages; ++s) {
+            if (status & (1u << s)) {
+                ctx->cap_obj[s] = std::max<int64_t>(ctx->cap_obj[s] * 2, ctx->h_small[s] + ctx->h_small[s] / 4 + 4096);
+                grew = true;
+            }
+        }
+        if (!grew) return fail(ctx, SDLG_ERR_CAPACITY, "inconsistent status %u", status);
+        ctx->buffers_ok = false;
+        const std::vector<int64_t> off = ctx->ev_off;
+        // keep the inputs: copy them back, reallocate, upload again
+        std::vector<float> x(ctx->n_hit), y(ctx->n_hit), z(ctx->n_hit);
+        std::vector<int32_t> idx(ctx->n_hit);
+        std::vector<uint32_t> det(ctx->n_hit);
+        CK(cudaMemcpy(x.data(), ctx->b.in_x, ctx->n_hit * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(y.data(), ctx->b.in_y, ctx->n_hit * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(z.data(), ctx->b.in_z, ctx->n_hit * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(idx.data(), ctx->b.in_idx, ctx->n_hit * 4, cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(det.data(), ctx->b.in_det, ctx->n_hit * 4, cudaMemcpyDeviceToHost));
+        int rc = sdlg_set_events(ctx, ctx->n_ev, off.data(), x.data(), y.data(), z.data(), idx.data(), det.data());
+        if (rc) return rc;
+        rc = launch(ctx, ctx->last_stop, ctx->last_flags);
+        if (rc) return rc;
+    }
+    return fail(ctx, SDLG_ERR_CAPACITY, "capacity did not converge");
+}
+
+int parse_file(const char* path, int kind, HostGeometry& hg) {
+    std::ifstream f(path);
+    if (!f.is_open()) return SDLG_ERR_IO;
+    std::string line;
+    while (std::getline(f, line)) {
+        std::stringstream ss(line);
+        unsigned int d;
+        if (kind == 0) {  // TiltedGeometry.cc:28-40
+            float drdz, slope;
+            ss >> d >> drdz >> slope;
+            hg.tilted[d] = {drdz, slope};
+        } else if (kind == 1) {  // EndcapGeometry.cc:36-59
+            float avgr2, yl, sl, yh, sh, c7, c8, cz;
+            ss >> d >> avgr2 >> yl >> sl >> yh >> sh >> c7 >> c8 >> cz;
+            hg.endcap[d] = {sl, c7};
+        } else {  // ModuleConnectionMap.cc:28-45
+            int n;
+            ss >> d >> n;
+            std::vector<uint32_t> v;
+            for (int k = 0; k < n; ++k) {
+                unsigned int e;
+                ss >> e;
+                v.push_back(e);
+            }
+            hg.conn[d] = v;
+        }
+    }
+    return SDLG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sdlg_create(sdlg_ctx** out, int device) {
+    if (!out) return SDLG_ERR_ARG;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return SDLG_ERR_NO_DEVICE;
+    if (device < 0 || device >= n) return SDLG_ERR_ARG;
+    sdlg_ctx* ctx = new sdlg_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&ctx->ev[k]);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_small, 16 * sizeof(int64_t));
+    if (e != cudaSuccess) {
+        delete ctx;
+        return SDLG_ERR_CUDA;
+    }
+    *out = ctx;
+    return SDLG_OK;
+}
+
+int sdlg_destroy(sdlg_ctx* ctx) {
+    if (!ctx) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_batch(ctx);
+    cudaFree(ctx->d_detid); cudaFree(ctx->d_mod); cudaFree(ctx->d_conn_off); cudaFree(ctx->d_conn_idx);
+    if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->h_small) cudaFreeHost(ctx->h_small);
+    for (int k = 0; k < 8; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return SDLG_OK;
+}
+
+const char* sdlg_last_error(const sdlg_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int sdlg_geometry_load_files(sdlg_ctx* ctx, const char* tilted_path, const char* endcap_path, const char* map_path) {
+    if (!ctx) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    HostGeometry hg;
+    const char* paths[3] = {tilted_path, endcap_path, map_path};
+    for (int k = 0; k < 3; ++k)
+        if (paths[k] && parse_file(paths[k], k, hg) != SDLG_OK) return fail(ctx, SDLG_ERR_IO, "cannot read %s", paths[k]);
+    ctx->hg = hg;
+    ctx->detids.clear();
+    return build_module_table(ctx, {});
+}
+
+int sdlg_geometry_upload(sdlg_ctx* ctx, int64_t n_tilted, const uint32_t* t_detid, const float* t_vals, int64_t n_endcap,
+                         const uint32_t* e_detid, const float* e_vals, int64_t n_keys, const uint32_t* keys,
+                         const int64_t* off, const uint32_t* dst) {
+    if (!ctx || n_tilted < 0 || n_endcap < 0 || n_keys < 0) return SDLG_ERR_ARG;
+    if ((n_tilted && (!t_detid || !t_vals)) || (n_endcap && (!e_detid || !e_vals)) || (n_keys && (!keys || !off)))
+        return fail(ctx, SDLG_ERR_ARG, "null table pointer");
+    cudaSetDevice(ctx->device);
+    HostGeometry hg;
+    for (int64_t i = 0; i < n_tilted; ++i) hg.tilted[t_detid[i]] = {t_vals[2 * i], t_vals[2 * i + 1]};
+    for (int64_t i = 0; i < n_endcap; ++i) hg.endcap[e_detid[i]] = {e_vals[8 * i + 2], e_vals[8 * i + 5]};
+    for (int64_t k = 0; k < n_keys; ++k) {
+        if (off[k + 1] < off[k]) return fail(ctx, SDLG_ERR_ARG, "map offsets not monotone");
+        hg.conn[keys[k]] = std::vector<uint32_t>(dst + off[k], dst + off[k + 1]);
+    }
+    ctx->hg = hg;
+    ctx->detids.clear();
+    return build_module_table(ctx, {});
+}
+
+int64_t sdlg_num_modules(const sdlg_ctx* ctx) { return ctx ? (int64_t)ctx->detids.size() : -1; }
+
+int sdlg_set_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, const float* x, const float* y, const float* z,
+                    const int32_t* idx, const uint32_t* detid) {
+    if (!ctx || n_events <= 0 || !ev_off) return SDLG_ERR_ARG;
+    if (!ctx->have_geo) return fail(ctx, SDLG_ERR_NO_GEOMETRY, "no geometry loaded");
+    cudaSetDevice(ctx->device);
+    if (ev_off[0] != 0) return fail(ctx, SDLG_ERR_ARG, "ev_off[0] must be 0");
+    for (int64_t e = 0; e < n_events; ++e)
+        if (ev_off[e + 1] < ev_off[e]) return fail(ctx, SDLG_ERR_ARG, "event offsets not monotone");
+    const int64_t n = ev_off[n_events];
+    if (n > 0 && (!x || !y || !z || !idx || !detid)) return fail(ctx, SDLG_ERR_ARG, "null hit array");
+    if (n > INT32_MAX / 4) return fail(ctx, SDLG_ERR_ARG, "too many hits in one batch");
+    // wait for any run still reading the inputs
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->n_ev = n_events;
+    ctx->n_hit = n;
+    ctx->ev_off.assign(ev_off, ev_off + n_events + 1);
+    int rc = ensure_buffers(ctx);
+    if (rc) return rc;
+    BatchDev& b = ctx->b;
+    cudaStream_t s = ctx->stream;
+    const void* src[5] = {x, y, z, idx, detid};
+    void* dstp[5] = {(void*)b.in_x, (void*)b.in_y, (void*)b.in_z, (void*)b.in_idx, (void*)b.in_det};
+    const size_t bytes = (size_t)n * 4;
+    // pinned callers are copied directly; others through the pinned staging buffer
+    bool all_pinned = true;
+    for (int k = 0; k < 5 && n > 0; ++k) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, src[k]) != cudaSuccess || a.type != cudaMemoryTypeHost) {
+            cudaGetLastError();
+            all_pinned = false;
+        }
+    }
+    if (n > 0 && all_pinned) {
+        for (int k = 0; k < 5; ++k) CK(cudaMemcpyAsync(dstp[k], src[k], bytes, cudaMemcpyHostToDevice, s));
+    } else if (n > 0) {
+        if (ctx->pinned_bytes < (int64_t)(bytes * 5)) {
+            if (ctx->pinned) cudaFreeHost(ctx->pinned);
+            ctx->pinned = nullptr;
+            ctx->pinned_bytes = 0;
+            CK(cudaMallocHost(&ctx->pinned, bytes * 5));
+            ctx->pinned_bytes = (int64_t)bytes * 5;
+        }
+        char* p = static_cast<char*>(ctx->pinned);
+        for (int k = 0; k < 5; ++k) {
+            std::memcpy(p + k * bytes, src[k], bytes);
+            CK(cudaMemcpyAsync(dstp[k], p + k * bytes, bytes, cudaMemcpyHostToDevice, s));
+        }
+    }
+    int64_t* hsm = ctx->h_small + 8;
+    hsm[0] = n;
+    CK(cudaMemcpyAsync(const_cast<int64_t*>(b.n_hit), hsm, sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(const_cast<int64_t*>(b.ev_off), ev_off, (n_events + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, s));
+    // the host offsets may be pageable: make the copy complete before returning
+    CK(cudaStreamSynchronize(s));
+    ctx->ran = false;
+    return SDLG_OK;
+}
+
+int sdlg_run_async(sdlg_ctx* ctx, int stop_after, int flags) {
+    if (!ctx) return SDLG_ERR_ARG;
+    if (!ctx->have_geo) return fail(ctx, SDLG_ERR_NO_GEOMETRY, "no geometry loaded");
+    if (!ctx->buffers_ok || ctx->n_ev <= 0) return fail(ctx, SDLG_ERR_NO_EVENTS, "no events set");
+    if (stop_after < 0 || stop_after > 4) return fail(ctx, SDLG_ERR_ARG, "stop_after out of range");
+    cudaSetDevice(ctx->device);
+    ctx->last_stop = stop_after;
+    ctx->last_flags = flags;
+    ctx->ran = true;
+    return launch(ctx, stop_after, flags);
+}
+
+int sdlg_sync(sdlg_ctx* ctx) {
+    if (!ctx) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    return finish(ctx);
+}
+
+int sdlg_run(sdlg_ctx* ctx, int stop_after, int flags) {
+    int rc = sdlg_run_async(ctx, stop_after, flags);
+    if (rc) return rc;
+    return sdlg_sync(ctx);
+}
+
+static int event_range(sdlg_ctx* ctx, int stage, int64_t event, int64_t* first, int64_t* n) {
+    if (!ctx->ran) return fail(ctx, SDLG_ERR_NO_EVENTS, "chain not run");
+    if (stage < 0 || stage > ctx->last_stop) return fail(ctx, SDLG_ERR_ARG, "stage %d not run", stage);
+    if (event >= ctx->n_ev) return fail(ctx, SDLG_ERR_ARG, "event out of range");
+    const int64_t n_mod = (int64_t)ctx->detids.size();
+    const int64_t a = event < 0 ? 0 : event * n_mod;
+    const int64_t z = event < 0 ? ctx->n_ev * n_mod : (event + 1) * n_mod;
+    int64_t v[2];
+    CK(cudaMemcpyAsync(&v[0], ctx->b.obj[stage].mod_cnt + a, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(&v[1], ctx->b.obj[stage].mod_cnt + z, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    *first = v[0];
+    *n = v[1] - v[0];
+    return SDLG_OK;
+}
+
+int sdlg_get_counts(sdlg_ctx* ctx, int64_t event, int64_t* out5) {
+    if (!ctx || !out5) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    for (int s = 0; s < 5; ++s) {
+        out5[s] = 0;
+        if (s > ctx->last_stop) continue;
+        int64_t f, n;
+        int rc = event_range(ctx, s, event, &f, &n);
+        if (rc) return rc;
+        out5[s] = n;
+    }
+    return SDLG_OK;
+}
+
+int sdlg_get_objects(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int64_t cap, int64_t* n_out) {
+    if (!ctx || !n_out || cap < 0) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    int64_t first, n;
+    int rc = event_range(ctx, stage, event, &first, &n);
+    if (rc) return rc;
+    *n_out = n;
+    if (n == 0 || !out) return SDLG_OK;  // a NULL out is a size query
+    if (cap < n) return fail(ctx, SDLG_ERR_ARG, "output capacity %lld < %lld tuples", (long long)cap, (long long)n);
+    static const int width[5] = {2, 4, 8, 8, 16};
+    const size_t bytes = (size_t)n * width[stage] * 4;
+    // materialise into the (then unused) staging records of the stage
+    int32_t* tmp = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&tmp, bytes, ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "cudaMallocAsync: %s", cudaGetErrorString(e));
+    launch_materialize(ctx->b, stage, first, n, tmp, ctx->stream);
+    CK(cudaMemcpyAsync(out, tmp, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(tmp, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SDLG_OK;
+}
+
+int sdlg_get_counters(sdlg_ctx* ctx, int64_t event, uint32_t* out110) {
+    if (!ctx || !out110 || event < 0 || event >= ctx->n_ev) return SDLG_ERR_ARG;
+    if (!ctx->ran) return fail(ctx, SDLG_ERR_NO_EVENTS, "chain not run");
+    cudaSetDevice(ctx->device);
+    CK(cudaMemcpyAsync(out110, ctx->b.counters + event * 110, 110 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SDLG_OK;
+}
+
+int sdlg_last_times(sdlg_ctx* ctx, float* out7) {
+    if (!ctx || !out7) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    CK(cudaEventSynchronize(ctx->ev[6]));
+    for (int k = 0; k < 6; ++k) CK(cudaEventElapsedTime(&out7[k], ctx->ev[k], ctx->ev[k + 1]));
+    CK(cudaEventElapsedTime(&out7[6], ctx->ev[0], ctx->ev[6]));
+    return SDLG_OK;
+}
+
+int sdlg_host_alloc(sdlg_ctx* ctx, int64_t bytes, void** out) {
+    if (!ctx || !out || bytes <= 0) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    CK(cudaMallocHost(out, (size_t)bytes));
+    return SDLG_OK;
+}
+
+int sdlg_host_free(sdlg_ctx* ctx, void* p) {
+    if (!ctx) return SDLG_ERR_ARG;
+    CK(cudaFreeHost(p));
+    return SDLG_OK;
+}
+
+}  // extern "C"

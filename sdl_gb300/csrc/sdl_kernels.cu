@@ -1,0 +1,767 @@
+// Segment-linking kernels for sm_103a.
+//
+// Every stage follows the same pattern, batched over all events:
+//   count  - per inner object, the number of candidate pairs the reference's
+//            loop would test (Event.cc:257-301, 472-521, 635-691, ...);
+//   scan   - exclusive prefix sum -> a flat candidate space [0, total);
+//   enum   - a persistent, work-stealing grid: each warp takes 256
+//            consecutive candidates, maps them back to (inner, outer) objects,
+//            applies the reference's cuts and appends the survivors with a
+//            warp-aggregated atomic, ranking each survivor inside its inner
+//            module;
+//   group  - per-module counts are scanned and the survivors scattered into
+//            dense arrays grouped by inner module (objects of one event stay
+//            contiguous).
+// Triplets and track candidates are exact equi-joins on the shared
+// mini-doublet / segment instead of the reference's all-pairs loops.
+#include <cstdio>
+
+#include "sdl_kernels.h"
+
+namespace sdlg {
+
+namespace {
+
+// Bounds checks of every global-memory index (debug builds with
+// -DSDL_DEVICE_CHECKS): a bad index is recorded in b.dbg (count, source line,
+// index, limit) and the access is redirected to element 0 instead of faulting.
+#ifdef SDL_DEVICE_CHECKS
+__device__ __forceinline__ int64_t checked_idx(int64_t i, int64_t lim, int line, unsigned long long* dbg) {
+    if (i >= 0 && i < lim) return i;
+    if (atomicAdd(dbg, 1ull) == 0ull) {
+        dbg[1] = (unsigned long long)line;
+        dbg[2] = (unsigned long long)i;
+        dbg[3] = (unsigned long long)lim;
+    }
+    return 0;
+}
+#define IX(i, lim) checked_idx((int64_t)(i), (int64_t)(lim), __LINE__, b.dbg)
+#else
+#define IX(i, lim) (i)
+#endif
+#define AT(arr, i, lim) (arr)[IX(i, lim)]
+
+constexpr int kWarp = 32;
+constexpr int kEnumThreads = 256;
+constexpr int kTask = 256;  // candidates per warp task
+constexpr int kScanThreads = 512;
+constexpr int kScanItems = 8;
+constexpr int kScanBlock = kScanThreads * kScanItems;
+
+__device__ __forceinline__ bool halted(const BatchDev& b) { return (*b.status & 0x1fu) != 0; }
+
+// add v to *addr with one atomic per group of lanes sharing the address;
+// every lane of the warp must call it
+__device__ __forceinline__ void warp_add(uint32_t* addr, uint32_t v, bool active) {
+    const unsigned act = __ballot_sync(0xffffffffu, active);
+    if (!active) return;
+    const unsigned peers = __match_any_sync(act, (unsigned long long)(uintptr_t)addr);
+    const uint32_t sum = __reduce_add_sync(peers, v);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(addr, sum);
+}
+
+// largest i in [lo, hi] with off[i] <= c (off has `lim` entries)
+__device__ __forceinline__ int find_obj(const BatchDev& b, const int64_t* off, int64_t lim, int lo, int hi, int64_t c) {
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (AT(off, mid, lim) <= c) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ------------------------------------------------------------------ scan
+struct ScanArgs {
+    int64_t* data;      // cap + 1 entries
+    const int64_t* n_ptr;
+    int64_t cap;
+    int64_t* blk;
+    int64_t blk_cap;
+    unsigned long long* dbg;
+};
+
+__global__ void k_scan_reduce(ScanArgs b) {
+    const int64_t n = min(*b.n_ptr, b.cap);
+    const int64_t base = (int64_t)blockIdx.x * kScanBlock;
+    if (base >= n) return;
+    int64_t s = 0;
+    for (int k = 0; k < kScanItems; ++k) {
+        const int64_t i = base + (int64_t)k * kScanThreads + threadIdx.x;
+        if (i < n) s += AT(b.data, i, b.cap + 1);
+    }
+    for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    __shared__ int64_t ws[32];  // one slot per lane of warp 0
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        int64_t v = threadIdx.x < kScanThreads / 32 ? ws[threadIdx.x] : 0;
+        for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) AT(b.blk, blockIdx.x, b.blk_cap) = v;
+    }
+}
+
+__global__ void k_scan_blocks(ScanArgs b) {
+    const int64_t n = min(*b.n_ptr, b.cap);
+    const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
+    __shared__ int64_t carry;
+    __shared__ int64_t ws[32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t base = 0; base < nb; base += blockDim.x) {
+        const int64_t i = base + threadIdx.x;
+        const int64_t v = i < nb ? AT(b.blk, i, b.blk_cap) : 0;
+        int64_t x = v;
+        const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) ws[w] = x;
+        __syncthreads();
+        if (w == 0) {
+            int64_t t = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int64_t y = __shfl_up_sync(0xffffffffu, t, o);
+                if (lane >= o) t += y;
+            }
+            ws[lane] = t;
+        }
+        __syncthreads();
+        const int64_t incl = x + (w ? ws[w - 1] : 0);
+        if (i < nb) AT(b.blk, i, b.blk_cap) = carry + incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) AT(b.data, n, b.cap + 1) = carry;
+}
+
+__global__ void k_scan_apply(ScanArgs b) {
+    const int64_t n = min(*b.n_ptr, b.cap);
+    const int64_t base = (int64_t)blockIdx.x * kScanBlock;
+    if (base >= n) return;
+    // each thread owns kScanItems consecutive elements
+    int64_t v[kScanItems];
+    int64_t s = 0;
+    const int64_t my = base + (int64_t)threadIdx.x * kScanItems;
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = (my + k < n) ? AT(b.data, my + k, b.cap + 1) : 0;
+        s += v[k];
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int64_t x = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    __shared__ int64_t ws[32];  // one slot per lane of warp 0
+    if (lane == 31) ws[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int64_t t = lane < kScanThreads / 32 ? ws[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < kScanThreads / 32) ws[lane] = t;
+    }
+    __syncthreads();
+    int64_t run = AT(b.blk, blockIdx.x, b.blk_cap) + x - s + (w ? ws[w - 1] : 0);
+    for (int k = 0; k < kScanItems; ++k) {
+        if (my + k < n) AT(b.data, my + k, b.cap + 1) = run;
+        run += v[k];
+    }
+}
+
+void scan(const BatchDev& bd, int64_t* data, const int64_t* n_ptr, int64_t cap, cudaStream_t s) {
+    const int64_t nb = (cap + kScanBlock - 1) / kScanBlock;
+    if (nb <= 0) return;
+    ScanArgs a{data, n_ptr, cap, bd.scan_tmp, bd.scan_tmp_cap, bd.dbg};
+    k_scan_reduce<<<(unsigned)nb, kScanThreads, 0, s>>>(a);
+    k_scan_blocks<<<1, 1024, 0, s>>>(a);
+    k_scan_apply<<<(unsigned)nb, kScanThreads, 0, s>>>(a);
+}
+
+// array sizes
+__device__ __forceinline__ int64_t H(const BatchDev& b) { return b.n_hit_cap; }
+__device__ __forceinline__ int64_t NG1(const BatchDev& b) { return (int64_t)b.n_gm + 1; }
+__device__ __forceinline__ int64_t NM(const BatchDev& b) { return b.geo.n_mod; }
+__device__ __forceinline__ int64_t NC(const BatchDev& b) { return b.geo.n_conn > 0 ? b.geo.n_conn : 1; }
+__device__ __forceinline__ int64_t NCP(const BatchDev& b) {
+    const int64_t v = (int64_t)b.n_ev * b.geo.n_conn;
+    return v > 0 ? v : 1;
+}
+__device__ __forceinline__ const ModDev& MOD(const BatchDev& b, int64_t m) { return AT(b.geo.mod, m, NM(b)); }
+
+// ------------------------------------------------------------------ ingest
+__global__ void k_hit_map(BatchDev b) {
+    const int64_t n = *b.n_hit;
+    for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < n; h += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = b.n_ev;  // event: largest e with ev_off[e] <= h
+        while (hi - lo > 1) {
+            const int mid = (lo + hi) >> 1;
+            if (AT(b.ev_off, mid, b.n_ev + 1) <= h) lo = mid;
+            else hi = mid;
+        }
+        const int ev = lo;
+        const uint32_t d = AT(b.in_det, h, H(b));
+        int a = 0, c = b.geo.n_mod;  // first module with detid >= d
+        while (a < c) {
+            const int mid = (a + c) >> 1;
+            if (AT(b.geo.detid, mid, NM(b)) < d) a = mid + 1;
+            else c = mid;
+        }
+        int gm = -1, rank = 0;
+        if (a < b.geo.n_mod && AT(b.geo.detid, a, NM(b)) == d) {
+            gm = ev * b.geo.n_mod + a;
+            rank = (int)atomicAdd((unsigned long long*)&AT(b.mod_hit, gm, NG1(b)), 1ull);
+        } else {
+            atomicOr(b.status, kStatusUnknownModule);
+        }
+        AT(b.hit_gm, h, H(b)) = gm;
+        AT(b.hit_rank, h, H(b)) = rank;
+    }
+}
+
+__global__ void k_hit_scatter(BatchDev b) {
+    const int64_t n = *b.n_hit;
+    for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < n; h += (int64_t)gridDim.x * blockDim.x) {
+        const int gm = AT(b.hit_gm, h, H(b));
+        if (gm < 0) continue;
+        const int64_t pos = AT(b.mod_hit, gm, NG1(b)) + AT(b.hit_rank, h, H(b));
+        const float x = AT(b.in_x, h, H(b)), y = AT(b.in_y, h, H(b)), z = AT(b.in_z, h, H(b));
+        const P3 p = mk(x, y, z);
+        AT(b.hx, pos, H(b)) = x; AT(b.hy, pos, H(b)) = y; AT(b.hz, pos, H(b)) = z;
+        AT(b.hrt, pos, H(b)) = p.rt; AT(b.hphi, pos, H(b)) = p.phi; AT(b.hr3, pos, H(b)) = p.r3;
+        const float a1 = f_asin(fmin_ref(p.rt * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
+        AT(b.ha1, pos, H(b)) = a1;
+        AT(b.htf, pos, H(b)) = f_tan(a1);
+        AT(b.htd, pos, H(b)) = (float)(tan((double)a1) / (double)a1);
+        AT(b.ha3, pos, H(b)) = f_asin(fmin_ref(p.rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax));
+        AT(b.hidx, pos, H(b)) = AT(b.in_idx, h, H(b));
+        AT(b.hgm, pos, H(b)) = gm;
+    }
+}
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ P3 hit(const BatchDev& b, int64_t k) {
+    P3 p;
+    p.x = AT(b.hx, k, H(b)); p.y = AT(b.hy, k, H(b)); p.z = AT(b.hz, k, H(b));
+    p.rt = AT(b.hrt, k, H(b)); p.phi = AT(b.hphi, k, H(b)); p.r3 = AT(b.hr3, k, H(b));
+    return p;
+}
+
+__device__ __forceinline__ int md_anchor(const ModDev& lm, int lo, int up) {
+    return (lm.type == kPS && lm.ltype != kPixel) ? up : lo;  // MiniDoublet.cc:60-81
+}
+
+// object arrays of stage st
+__device__ __forceinline__ int OI(const BatchDev& b, int st, int64_t k) { return AT(b.obj[st].i, k, b.obj[st].cap); }
+__device__ __forceinline__ int OJ(const BatchDev& b, int st, int64_t k) { return AT(b.obj[st].j, k, b.obj[st].cap); }
+__device__ __forceinline__ int OG(const BatchDev& b, int st, int64_t k) { return AT(b.obj[st].g, k, b.obj[st].cap); }
+__device__ __forceinline__ float OF(const BatchDev& b, int st, int f, int64_t k) {
+    const Objs& O = b.obj[st];
+    return AT(O.f, (int64_t)f * O.cap + k, O.cap * (O.nf > 0 ? O.nf : 1));
+}
+__device__ __forceinline__ int64_t OFF(const BatchDev& b, int st, int64_t g) { return AT(b.obj[st].mod_cnt, g, NG1(b)); }
+
+__device__ __forceinline__ MDView md_view(const BatchDev& b, int a) {
+    const int gm = OG(b, kMD, a);
+    const ModDev* lm = &MOD(b, gm % b.geo.n_mod);
+    MDView v;
+    v.m = lm;
+    v.a = hit(b, md_anchor(*lm, OI(b, kMD, a), OJ(b, kMD, a)));
+    v.dz = OF(b, kMD, 0, a);
+    v.shiftedDz = OF(b, kMD, 1, a);
+    v.dphi = OF(b, kMD, 2, a);
+    v.dphichange = OF(b, kMD, 3, a);
+    return v;
+}
+
+__device__ __forceinline__ AnchorView anchor_view(const BatchDev& b, int64_t k) {
+    AnchorView a;
+    a.p = hit(b, k);
+    a.asin1 = AT(b.ha1, k, H(b));
+    a.tand1 = AT(b.htd, k, H(b));
+    a.asin3 = AT(b.ha3, k, H(b));
+    a.m = &MOD(b, AT(b.hgm, k, H(b)) % b.geo.n_mod);
+    return a;
+}
+
+__device__ __forceinline__ SGView sg_view(const BatchDev& b, int s) {
+    SGView v;
+    const int im = OI(b, kSG, s), om = OJ(b, kSG, s);
+    const ModDev& ilm = MOD(b, OG(b, kMD, im) % b.geo.n_mod);
+    const ModDev& olm = MOD(b, OG(b, kMD, om) % b.geo.n_mod);
+    v.lo = anchor_view(b, md_anchor(ilm, OI(b, kMD, im), OJ(b, kMD, im)));
+    v.up = anchor_view(b, md_anchor(olm, OI(b, kMD, om), OJ(b, kMD, om)));
+    v.dphi = OF(b, kSG, 0, s);
+    v.dphimin = OF(b, kSG, 1, s);
+    v.dphimax = OF(b, kSG, 2, s);
+    v.dphichange = OF(b, kSG, 3, s);
+    v.dphiminchange = OF(b, kSG, 4, s);
+    v.dphimaxchange = OF(b, kSG, 5, s);
+    return v;
+}
+
+// ------------------------------------------------------------------ stage functors
+struct MDStage {
+    static constexpr int kSt = kMD;
+    __device__ static bool eval(const BatchDev& b, int gm, int64_t q, int& oi, int& oj, float* fv) {
+        const int n_mod = b.geo.n_mod;
+        const int ev = gm / n_mod;
+        const ModDev lm = MOD(b, gm - ev * n_mod);
+        const int pg = ev * n_mod + lm.partner;
+        const int64_t nu = AT(b.mod_hit, pg + 1, NG1(b)) - AT(b.mod_hit, pg, NG1(b));
+        if (nu <= 0) {
+#ifdef SDL_DEVICE_CHECKS
+            IX(-1, 0);
+#endif
+            return false;
+        }
+        const int64_t i = q / nu, j = q - i * nu;
+        const int64_t lo = AT(b.mod_hit, gm, NG1(b)) + i, up = AT(b.mod_hit, pg, NG1(b)) + j;
+        const P3 L = hit(b, lo), U = hit(b, up);
+        const float pixAsin = lm.ltype == kPixel ? AT(b.ha1, lo, H(b)) : AT(b.ha1, up, H(b));
+        MDVals v;
+        v.dz = 0.f; v.shiftedDz = 0.f; v.dphi = 0.f; v.dphichange = 0.f;
+        const bool pass = lm.subdet == kBarrel ? md_barrel(L, U, pixAsin, lm, v) : md_endcap(L, U, pixAsin, lm, v);
+        oi = (int)lo; oj = (int)up;
+        fv[0] = v.dz; fv[1] = v.shiftedDz; fv[2] = v.dphi; fv[3] = v.dphichange;
+        return pass;
+    }
+    __device__ static int group_of(const BatchDev& b, int gm) { return gm; }
+};
+
+// conn entry k of module m for the flat index q, given per-entry exclusive prefixes
+__device__ __forceinline__ int conn_entry(const BatchDev& b, int ev, int m, int64_t q, int& pref) {
+    const int k0 = AT(b.geo.conn_off, m, NM(b) + 1), k1 = AT(b.geo.conn_off, m + 1, NM(b) + 1);
+    const int64_t base = (int64_t)ev * b.geo.n_conn;
+    int lo = k0, hi = k1 - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (AT(b.conn_pref, base + mid, NCP(b)) <= q) lo = mid;
+        else hi = mid - 1;
+    }
+    pref = AT(b.conn_pref, base + lo, NCP(b));
+    return lo;
+}
+
+struct SGStage {
+    static constexpr int kSt = kSG;
+    __device__ static bool eval(const BatchDev& b, int a, int64_t q, int& oi, int& oj, float* fv) {
+        const int n_mod = b.geo.n_mod;
+        const int g1 = OG(b, kMD, a);
+        const int ev = g1 / n_mod, m1 = g1 - ev * n_mod;
+        int pref;
+        const int k = conn_entry(b, ev, m1, q, pref);
+        const int g2 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
+        const int bmd = (int)(OFF(b, kMD, g2) + (q - pref));
+        const MDView im = md_view(b, a);
+        const MDView om = md_view(b, bmd);
+        const int oanc = md_anchor(*om.m, OI(b, kMD, bmd), OJ(b, kMD, bmd));
+        SGVals v;
+        v.dphi = v.dphimin = v.dphimax = v.dphichange = v.dphiminchange = v.dphimaxchange = 0.f;
+        bool pass;
+        const bool ob = om.m->subdet == kBarrel;
+        if (ob) {
+            pass = sg_barrel(im, om, AT(b.ha1, oanc, H(b)), AT(b.htf, oanc, H(b)), v);
+        } else {
+            P3 oHi = om.a, oLo = om.a;
+            if (om.m->type == kTwoS && om.m->subdet == kEndcap) {
+                const ModDev& am = MOD(b, AT(b.hgm, oanc, H(b)) % n_mod);
+                oHi = strip_edge(om.a, am, true);
+                oLo = strip_edge(om.a, am, false);
+            }
+            pass = sg_endcap(im, om, AT(b.ha1, oanc, H(b)), AT(b.htf, oanc, H(b)), true, oHi, oLo, v);
+        }
+        oi = a; oj = bmd;
+        fv[0] = v.dphi; fv[1] = v.dphimin; fv[2] = v.dphimax;
+        fv[3] = v.dphichange; fv[4] = v.dphiminchange; fv[5] = v.dphimaxchange;
+        return pass;
+    }
+    __device__ static int group_of(const BatchDev& b, int a) { return OG(b, kMD, a); }
+};
+
+struct TLStage {
+    static constexpr int kSt = kTL;
+    __device__ static bool eval(const BatchDev& b, int s, int64_t q, int& oi, int& oj, float* fv) {
+        const int n_mod = b.geo.n_mod;
+        const int g2 = OG(b, kMD, OJ(b, kSG, s));
+        const int ev = g2 / n_mod, m2 = g2 - ev * n_mod;
+        int pref;
+        const int k = conn_entry(b, ev, m2, q, pref);
+        const int g3 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
+        const int t = (int)(OFF(b, kSG, g3) + (q - pref));
+        const SGView A = sg_view(b, s);
+        const SGView B = sg_view(b, t);
+        oi = s; oj = t;
+        (void)fv;
+        return tl_dispatch(A, B, (b.flags & 4) != 0);
+    }
+    __device__ static int group_of(const BatchDev& b, int s) { return OG(b, kSG, s); }
+};
+
+struct TPStage {
+    static constexpr int kSt = kTP;
+    __device__ static bool eval(const BatchDev& b, int s1, int64_t q, int& oi, int& oj, float* fv) {
+        const int omd = OJ(b, kSG, s1);
+        const int g2 = OG(b, kMD, omd);
+        const int64_t n2 = OFF(b, kSG, g2 + 1) - OFF(b, kSG, g2);
+        if (n2 <= 0) {
+#ifdef SDL_DEVICE_CHECKS
+            IX(-2, 0);
+#endif
+            return false;
+        }
+        const int s2 = (int)(OFF(b, kSG, g2) + q % n2);
+        oi = s1; oj = s2;
+        (void)fv;
+        return OI(b, kSG, s2) == omd;  // Triplet.cc:55 via Segment.cc:861-866
+    }
+    __device__ static int group_of(const BatchDev& b, int s) { return OG(b, kSG, s); }
+};
+
+struct TCStage {
+    static constexpr int kSt = kTC;
+    __device__ static bool eval(const BatchDev& b, int t1, int64_t q, int& oi, int& oj, float* fv) {
+        const int sB = OJ(b, kTL, t1);
+        const int g3 = OG(b, kSG, sB);
+        const int t2 = (int)(OFF(b, kTL, g3) + q);
+        const int sC = OI(b, kTL, t2);
+        oi = t1; oj = t2;
+        (void)fv;
+        return OI(b, kSG, sC) == OI(b, kSG, sB) && OJ(b, kSG, sC) == OJ(b, kSG, sB);  // TrackCandidate.cc:161
+    }
+    __device__ static int group_of(const BatchDev& b, int t) { return OG(b, kTL, t); }
+};
+
+// inner-object count of a stage (device), clamped to the inner capacity
+__device__ __forceinline__ int64_t n_inner(const BatchDev& b, int st) {
+    switch (st) {
+        case kMD: return b.n_gm;
+        case kSG: return min(OFF(b, kMD, b.n_gm), b.obj[kMD].cap);
+        case kTL:
+        case kTP: return min(OFF(b, kSG, b.n_gm), b.obj[kSG].cap);
+        default: return min(OFF(b, kTL, b.n_gm), b.obj[kTL].cap);
+    }
+}
+
+template <class F>
+__global__ void __launch_bounds__(kEnumThreads) k_enum(BatchDev b) {
+    constexpr int st = F::kSt;
+    if (halted(b)) return;
+    const int64_t nobj = n_inner(b, st);
+    if (nobj <= 0) return;
+    const int64_t* off = b.cand[st];
+    const int64_t offlim = b.cand_cap[st] + 1;
+    const int64_t total = AT(off, nobj, offlim);
+    const int64_t ntask = (total + kTask - 1) / kTask;
+    const int lane = threadIdx.x & 31;
+    const Recs& R = b.rec[st];
+    const Objs& O = b.obj[st];
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(b.task + st, 1ull);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if ((int64_t)t >= ntask) break;
+        const int64_t base = (int64_t)t * kTask;
+        const int64_t end = min(base + kTask, total);
+        int ilo = 0;
+        if (lane < 2) ilo = find_obj(b, off, offlim, 0, (int)nobj - 1, lane == 0 ? base : end - 1);
+        const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
+        const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
+        for (int r = 0; r < kTask / kWarp; ++r) {
+            const int64_t c = base + r * kWarp + lane;
+            const bool valid = c < end;
+            int oi = 0, oj = 0, g = 0;
+            float fv[6];
+            bool pass = false;
+            if (valid) {
+                const int i = (i0 == i1) ? i0 : find_obj(b, off, offlim, i0, i1, c);
+                pass = F::eval(b, i, c - AT(off, i, offlim), oi, oj, fv);
+                if (pass) g = F::group_of(b, i);
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, pass);
+            if (m) {
+                const int leader = __ffs(m) - 1;
+                unsigned long long p0 = 0;
+                if (lane == leader) p0 = atomicAdd((unsigned long long*)(b.n_rec + st), (unsigned long long)__popc(m));
+                p0 = __shfl_sync(0xffffffffu, p0, leader);
+                if (pass) {
+                    const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));
+                    if (pos < O.cap) {
+                        AT(R.i, pos, O.cap) = oi;
+                        AT(R.j, pos, O.cap) = oj;
+                        AT(R.g, pos, O.cap) = g;
+                        AT(R.rank, pos, O.cap) = (int)atomicAdd((unsigned long long*)&AT(O.mod_cnt, g, NG1(b)), 1ull);
+                        for (int k = 0; k < R.nf; ++k) AT(R.f, (int64_t)k * O.cap + pos, O.cap * R.nf) = fv[k];
+                    } else {
+                        atomicOr(b.status, 1u << st);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// per-module object counts of a stage -> layer counters (before the scan)
+__global__ void k_obj_counters(BatchDev b, int st) {
+    if (halted(b)) return;
+    const int n_mod = b.geo.n_mod;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g - threadIdx.x < b.n_gm; g += (int64_t)gridDim.x * blockDim.x) {
+        const bool in = g < b.n_gm;
+        uint32_t v = 0;
+        int ev = 0, slot = 0;
+        if (in) {
+            v = (uint32_t)OFF(b, st, g);
+            ev = (int)(g / n_mod);
+            slot = MOD(b, g - (int64_t)ev * n_mod).layer_slot;
+        }
+        const bool act = in && v != 0;
+        warp_add(act ? &AT(b.counters, (int64_t)ev * 110 + st * 22 + 11 + slot, (int64_t)b.n_ev * 110) : b.counters, v, act);
+    }
+}
+
+__global__ void k_scatter(BatchDev b, int st) {
+    if (halted(b)) return;
+    const Recs& R = b.rec[st];
+    const Objs& O = b.obj[st];
+    const int64_t n = min(b.n_rec[st], O.cap);
+    const int64_t flim = O.cap * (O.nf > 0 ? O.nf : 1);
+    for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const int g = AT(R.g, r, O.cap);
+        const int64_t pos = OFF(b, st, g) + AT(R.rank, r, O.cap);
+        if (pos >= O.cap) continue;
+        AT(O.i, pos, O.cap) = AT(R.i, r, O.cap);
+        AT(O.j, pos, O.cap) = AT(R.j, r, O.cap);
+        AT(O.g, pos, O.cap) = g;
+        for (int k = 0; k < O.nf; ++k) AT(O.f, (int64_t)k * O.cap + pos, flim) = AT(R.f, (int64_t)k * O.cap + r, flim);
+    }
+}
+
+// ------------------------------------------------------------------ counts
+__device__ __forceinline__ uint32_t* counter_at(const BatchDev& b, int ev, int st, int kind, int slot) {
+    return &AT(b.counters, (int64_t)ev * 110 + st * 22 + kind * 11 + slot, (int64_t)b.n_ev * 110);
+}
+
+__global__ void k_md_count(BatchDev b) {
+    const int n_mod = b.geo.n_mod;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g - threadIdx.x < b.n_gm; g += (int64_t)gridDim.x * blockDim.x) {
+        const bool in = g < b.n_gm;
+        int64_t c = 0;
+        int ev = 0, slot = 0;
+        if (in) {
+            ev = (int)(g / n_mod);
+            const ModDev& m = MOD(b, g - (int64_t)ev * n_mod);
+            if (m.lower && m.partner >= 0) {
+                const int64_t pg = (int64_t)ev * n_mod + m.partner;
+                c = (AT(b.mod_hit, g + 1, NG1(b)) - AT(b.mod_hit, g, NG1(b))) *
+                    (AT(b.mod_hit, pg + 1, NG1(b)) - AT(b.mod_hit, pg, NG1(b)));
+            }
+            slot = m.layer_slot;
+            AT(b.cand[kMD], g, b.cand_cap[kMD] + 1) = c;
+        }
+        const bool act = in && c != 0;
+        warp_add(act ? counter_at(b, ev, kMD, 0, slot) : b.counters, (uint32_t)c, act);
+    }
+}
+
+// per lower module: running sums of the object counts of its connected
+// modules (stage src) -> conn_pref per entry and conn_sum per module; the
+// reference's candidate counters of stage cst get n_obj(g) * conn_sum(g).
+__global__ void k_conn_sum(BatchDev b, int src, int cst) {
+    if (halted(b)) return;
+    const int n_mod = b.geo.n_mod;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g - threadIdx.x < b.n_gm; g += (int64_t)gridDim.x * blockDim.x) {
+        const bool in = g < b.n_gm;
+        int64_t sum = 0, cand = 0;
+        int ev = 0, slot = 0;
+        if (in) {
+            ev = (int)(g / n_mod);
+            const int m = (int)(g - (int64_t)ev * n_mod);
+            const int k0 = AT(b.geo.conn_off, m, NM(b) + 1), k1 = AT(b.geo.conn_off, m + 1, NM(b) + 1);
+            const int64_t pbase = (int64_t)ev * b.geo.n_conn;
+            const int64_t ebase = (int64_t)ev * n_mod;
+            for (int k = k0; k < k1; ++k) {
+                AT(b.conn_pref, pbase + k, NCP(b)) = (int32_t)sum;
+                const int64_t g2 = ebase + AT(b.geo.conn_idx, k, NC(b));
+                sum += OFF(b, src, g2 + 1) - OFF(b, src, g2);
+            }
+            AT(b.conn_sum, g, b.n_gm) = sum;
+            cand = (OFF(b, src, g + 1) - OFF(b, src, g)) * sum;
+            slot = MOD(b, m).layer_slot;
+        }
+        const bool act = in && cand != 0 && cst >= 0;
+        warp_add(act ? counter_at(b, ev, cst, 0, slot) : b.counters, (uint32_t)cand, act);
+    }
+}
+
+__global__ void k_sg_count(BatchDev b) {
+    if (halted(b)) return;
+    const int64_t n = n_inner(b, kSG);
+    for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x)
+        AT(b.cand[kSG], a, b.cand_cap[kSG] + 1) = AT(b.conn_sum, OG(b, kMD, a), b.n_gm);
+}
+
+__global__ void k_tl_count(BatchDev b) {
+    if (halted(b)) return;
+    const int n_mod = b.geo.n_mod;
+    const int64_t n = n_inner(b, kTL);
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s - threadIdx.x < n; s += (int64_t)gridDim.x * blockDim.x) {
+        const bool in = s < n;
+        int64_t c = 0;
+        int ev = 0, slot = 0;
+        if (in) {
+            const int g2 = OG(b, kMD, OJ(b, kSG, s));
+            c = AT(b.conn_sum, g2, b.n_gm);
+            AT(b.cand[kTL], s, b.cand_cap[kTL] + 1) = c;
+            const int g1 = OG(b, kSG, s);
+            ev = g1 / n_mod;
+            slot = MOD(b, g1 - ev * n_mod).layer_slot;
+        }
+        const bool act = in && c != 0;
+        warp_add(act ? counter_at(b, ev, kTL, 0, slot) : b.counters, (uint32_t)c, act);
+    }
+}
+
+__global__ void k_tp_count(BatchDev b) {
+    if (halted(b)) return;
+    const int n_mod = b.geo.n_mod;
+    const int64_t n = n_inner(b, kTP);
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        const int g1 = OG(b, kSG, s);
+        const int ev = g1 / n_mod, m1 = g1 - ev * n_mod;
+        const int g2 = OG(b, kMD, OJ(b, kSG, s));
+        const int m2 = g2 - ev * n_mod;
+        int mult = 0;
+        const int k0 = AT(b.geo.conn_off, m1, NM(b) + 1), k1 = AT(b.geo.conn_off, m1 + 1, NM(b) + 1);
+        for (int k = k0; k < k1; ++k) mult += AT(b.geo.conn_idx, k, NC(b)) == m2;
+        AT(b.cand[kTP], s, b.cand_cap[kTP] + 1) = (int64_t)mult * (OFF(b, kSG, g2 + 1) - OFF(b, kSG, g2));
+    }
+}
+
+__global__ void k_tc_count(BatchDev b) {
+    if (halted(b)) return;
+    const int n_mod = b.geo.n_mod;
+    const int64_t n = n_inner(b, kTC);
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+        int64_t c = 0;
+        const int g1 = OG(b, kTL, t);
+        const ModDev& m1 = MOD(b, g1 % n_mod);
+        if (m1.subdet == kBarrel && m1.layer == 1) {
+            const int g3 = OG(b, kSG, OJ(b, kTL, t));
+            const ModDev& m3 = MOD(b, g3 % n_mod);
+            if (m3.subdet == kBarrel && m3.layer == 3) c = OFF(b, kTL, g3 + 1) - OFF(b, kTL, g3);
+        }
+        AT(b.cand[kTC], t, b.cand_cap[kTC] + 1) = c;
+    }
+}
+
+// Event.cc:835: track-candidate candidates are barrel-layer-1 x barrel-layer-3 tracklets
+__global__ void k_tc_cand_counter(BatchDev b) {
+    for (int ev = blockIdx.x * blockDim.x + threadIdx.x; ev < b.n_ev; ev += gridDim.x * blockDim.x) {
+        const uint32_t n1 = *counter_at(b, ev, kTL, 1, 0), n3 = *counter_at(b, ev, kTL, 1, 2);
+        *counter_at(b, ev, kTC, 0, 0) += n1 * n3;
+    }
+}
+
+// ------------------------------------------------------------------ output
+__device__ __forceinline__ void put_md(const BatchDev& b, int a, int32_t* o) {
+    o[0] = AT(b.hidx, OI(b, kMD, a), H(b));
+    o[1] = AT(b.hidx, OJ(b, kMD, a), H(b));
+}
+__device__ __forceinline__ void put_sg(const BatchDev& b, int s, int32_t* o) {
+    put_md(b, OI(b, kSG, s), o);
+    put_md(b, OJ(b, kSG, s), o + 2);
+}
+__device__ __forceinline__ void put_tl(const BatchDev& b, int st, int t, int32_t* o) {
+    put_sg(b, OI(b, st, t), o);
+    put_sg(b, OJ(b, st, t), o + 4);
+}
+
+__global__ void k_materialize(BatchDev b, int st, int64_t first, int64_t n, int32_t* out) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int o = (int)(first + k);
+        switch (st) {
+            case kMD: put_md(b, o, out + 2 * k); break;
+            case kSG: put_sg(b, o, out + 4 * k); break;
+            case kTL: put_tl(b, kTL, o, out + 8 * k); break;
+            case kTP: put_tl(b, kTP, o, out + 8 * k); break;
+            default:
+                put_tl(b, kTL, OI(b, kTC, o), out + 16 * k);
+                put_tl(b, kTL, OJ(b, kTC, o), out + 16 * k + 8);
+        }
+    }
+}
+
+unsigned grid_for(int64_t n, int threads, int cap_blocks) {
+    int64_t g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > cap_blocks) g = cap_blocks;
+    return (unsigned)g;
+}
+
+template <class F>
+void enum_and_group(const BatchDev& b, cudaStream_t s) {
+    constexpr int st = F::kSt;
+    const int64_t* ninner_ptr = nullptr;
+    switch (st) {
+        case kMD: ninner_ptr = b.n_gm_dev; break;
+        case kSG: ninner_ptr = b.obj[kMD].mod_cnt + b.n_gm; break;
+        case kTL:
+        case kTP: ninner_ptr = b.obj[kSG].mod_cnt + b.n_gm; break;
+        default: ninner_ptr = b.obj[kTL].mod_cnt + b.n_gm;
+    }
+    scan(b, b.cand[st], ninner_ptr, b.cand_cap[st], s);
+    k_enum<F><<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
+    k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, st);
+    scan(b, b.obj[st].mod_cnt, b.n_gm_dev, b.n_gm, s);
+    k_scatter<<<b.n_sm * 8, 256, 0, s>>>(b, st);
+}
+
+}  // namespace
+
+void launch_ingest(const BatchDev& b, cudaStream_t s) {
+    const unsigned g = grid_for(b.n_hit_cap, 256, b.n_sm * 16);
+    k_hit_map<<<g, 256, 0, s>>>(b);
+    scan(b, b.mod_hit, b.n_gm_dev, b.n_gm, s);
+    k_hit_scatter<<<g, 256, 0, s>>>(b);
+}
+
+void launch_md(const BatchDev& b, cudaStream_t s) {
+    k_md_count<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b);
+    enum_and_group<MDStage>(b, s);
+}
+
+void launch_sg(const BatchDev& b, cudaStream_t s) {
+    k_conn_sum<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kMD, kSG);
+    k_sg_count<<<b.n_sm * 8, 256, 0, s>>>(b);
+    enum_and_group<SGStage>(b, s);
+}
+
+void launch_tl(const BatchDev& b, cudaStream_t s) {
+    // conn sums over segment counts serve the tracklet enumeration and the
+    // triplet candidate counters (Event.cc:547-596 loops over the same lists)
+    k_conn_sum<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kSG, kTP);
+    k_tl_count<<<b.n_sm * 8, 256, 0, s>>>(b);
+    enum_and_group<TLStage>(b, s);
+}
+
+void launch_tp(const BatchDev& b, cudaStream_t s) {
+    k_tp_count<<<b.n_sm * 8, 256, 0, s>>>(b);
+    enum_and_group<TPStage>(b, s);
+}
+
+void launch_tc(const BatchDev& b, cudaStream_t s) {
+    k_tc_count<<<b.n_sm * 8, 256, 0, s>>>(b);
+    k_tc_cand_counter<<<grid_for(b.n_ev, 128, 1024), 128, 0, s>>>(b);
+    enum_and_group<TCStage>(b, s);
+}
+
+void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s) {
+    if (n <= 0) return;
+    k_materialize<<<grid_for(n, 256, b.n_sm * 16), 256, 0, s>>>(b, st, first, n, out);
+}
+
+}  // namespace sdlg

@@ -1,0 +1,58 @@
+// Launchers for the segment-linking kernels (sm_103a).  The host code in
+// sdl_capi.cu owns the buffers and calls these in stage order on one stream.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sdl_types.h"
+
+namespace sdlg {
+
+struct BatchDev {
+    Geometry geo;
+    int n_ev;
+    int n_gm;          // n_ev * n_mod
+    int64_t n_hit_cap;
+    const int64_t* n_hit;   // device scalar
+    // inputs (concatenated events)
+    const float *in_x, *in_y, *in_z;
+    const int32_t* in_idx;
+    const uint32_t* in_det;
+    const int64_t* ev_off;   // n_ev + 1
+    // ingest
+    int32_t* hit_gm;
+    int32_t* hit_rank;
+    int64_t* mod_hit;        // n_gm + 1: counts -> offsets
+    // sorted hits (SoA)
+    float *hx, *hy, *hz, *hrt, *hphi, *hr3, *ha1, *htf, *htd, *ha3;
+    int32_t *hidx, *hgm;
+    // stages
+    Objs obj[kNumStages];
+    Recs rec[kNumStages];
+    int64_t* cand[kNumStages];     // per inner object candidate counts -> offsets (cap_inner + 1)
+    int64_t cand_cap[kNumStages];
+    int64_t* n_rec;                // kNumStages attempted appends
+    int64_t* n_gm_dev;             // device scalar = n_gm
+    // connection-list prefix sums of per-module object counts
+    int32_t* conn_pref;            // n_ev * n_conn
+    int64_t* conn_sum;             // n_gm
+    uint32_t* counters;            // n_ev * 110
+    uint32_t* status;
+    unsigned long long* task;      // kNumStages work counters
+    int64_t* scan_tmp;
+    int64_t scan_tmp_cap;
+    int flags;                     // bit2: DefaultNm1 tracklets
+    int n_sm;
+    unsigned long long* dbg;       // bounds-check record (debug builds): count, line, index, limit
+};
+
+// stage launchers (each enqueues its kernels on stream s)
+void launch_ingest(const BatchDev& b, cudaStream_t s);
+void launch_md(const BatchDev& b, cudaStream_t s);
+void launch_sg(const BatchDev& b, cudaStream_t s);
+void launch_tl(const BatchDev& b, cudaStream_t s);
+void launch_tp(const BatchDev& b, cudaStream_t s);
+void launch_tc(const BatchDev& b, cudaStream_t s);
+// hit-index tuples of stage st for objects [first, first + n) into out (width 2/4/8/8/16)
+void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s);
+
+}  // namespace sdlg

@@ -1,0 +1,57 @@
+// Device buffer layout of one batch of events (host-visible struct of device
+// pointers).  All per-module arrays are indexed by the global module index
+// gm = event * n_mod + module, so every stage runs over all events of the
+// batch in one launch and the objects of one event stay contiguous.
+#pragma once
+#include <cstdint>
+
+#include "sdl_device.cuh"
+
+namespace sdlg {
+
+enum Stage { kMD = 0, kSG = 1, kTL = 2, kTP = 3, kTC = 4, kNumStages = 5 };
+
+// staging records of one stage: the candidate (inner object i, outer object
+// j), the inner object's module and the rank inside that module, plus the
+// floats the next stages read.
+struct Recs {
+    int32_t* i;
+    int32_t* j;
+    int32_t* g;
+    int32_t* rank;
+    float* f;      // nf floats per record, SoA: f[k * cap + r]
+    int nf;
+};
+
+// Dense object arrays grouped by inner module.
+struct Objs {
+    int32_t* i;    // MD: lower hit | SG: inner MD | TL/TP: inner SG | TC: inner TL
+    int32_t* j;    // MD: upper hit | SG: outer MD | TL/TP: outer SG | TC: outer TL
+    int32_t* g;    // inner module (gm)
+    float* f;      // nf floats SoA (cap stride)
+    int nf;
+    int64_t* mod_cnt;  // n_gm + 1 counts, scanned in place to offsets
+    int64_t cap;
+};
+
+struct Geometry {
+    int n_mod;
+    int n_conn;
+    const uint32_t* detid;   // sorted
+    const ModDev* mod;
+    const int32_t* conn_off; // n_mod + 1
+    const int32_t* conn_idx;
+};
+
+// Per-stage status word bits
+enum : uint32_t {
+    kStatusOverflowMD = 1u << 0,
+    kStatusOverflowSG = 1u << 1,
+    kStatusOverflowTL = 1u << 2,
+    kStatusOverflowTP = 1u << 3,
+    kStatusOverflowTC = 1u << 4,
+    kStatusUnknownModule = 1u << 8,
+    kStatusPhiLoop = 1u << 9,
+};
+
+}  // namespace sdlg
