@@ -117,6 +117,12 @@ int sdlg_get_counters(sdlg_ctx* ctx, int64_t event, uint32_t* out110);
 /* Device time of the last run: [0] ingest, [1..5] MD..TC stages, [6] total (ms). */
 int sdlg_last_times(sdlg_ctx* ctx, float* out7);
 
+/* Device time of each stage's candidate-evaluation kernel in the last run (ms). */
+int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5);
+
+/* Number of kernels one run of the chain launches (as last enqueued). */
+int64_t sdlg_last_launches(const sdlg_ctx* ctx);
+
 /* Pinned host memory for zero-staging transfers. */
 int sdlg_host_alloc(sdlg_ctx* ctx, int64_t bytes, void** out);
 int sdlg_host_free(sdlg_ctx* ctx, void* p);

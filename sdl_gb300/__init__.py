@@ -62,6 +62,9 @@ def lib():
         L.sdlg_get_objects.argtypes = [vp, i32, i64, vp, i64, vp]
         L.sdlg_get_counters.argtypes = [vp, i64, vp]
         L.sdlg_last_times.argtypes = [vp, vp]
+        L.sdlg_last_kernel_times.argtypes = [vp, vp]
+        L.sdlg_last_launches.argtypes = [vp]
+        L.sdlg_last_launches.restype = i64
         L.sdlg_host_alloc.argtypes = [vp, i64, ctypes.POINTER(vp)]
         L.sdlg_host_free.argtypes = [vp, vp]
         _LIB = L
@@ -177,6 +180,17 @@ class Chain:
         out = np.zeros(110, dtype=np.uint32)
         self._ck(lib().sdlg_get_counters(self.h, event, out.ctypes.data))
         return out
+
+    def kernel_times(self) -> np.ndarray:
+        """Device ms of each stage's candidate-evaluation kernel in the last run."""
+        out = np.zeros(5, dtype=np.float32)
+        self._ck(lib().sdlg_last_kernel_times(self.h, out.ctypes.data))
+        return out
+
+    @property
+    def launches(self) -> int:
+        """Kernels one run of the chain launches."""
+        return int(lib().sdlg_last_launches(self.h))
 
     def times(self) -> np.ndarray:
         """Device ms of the last run: ingest, MD, SG, TL, TP, TC, total."""

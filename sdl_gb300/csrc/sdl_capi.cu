@@ -122,6 +122,8 @@ struct sdlg_ctx {
     int graph_stop = -1, graph_flags = -1;
     // timing
     cudaEvent_t ev[8];
+    Hooks hooks;
+    int launches_per_run = 0;
     int last_stop = -1, last_flags = 0;
     bool ran = false;
 };
@@ -336,18 +338,22 @@ void enqueue_chain(sdlg_ctx* ctx, int stop_after) {
     cudaMemsetAsync(b.counters, 0, b.n_ev * 110 * sizeof(uint32_t), s);
     cudaMemsetAsync(b.mod_hit, 0, (n_gm + 1) * sizeof(int64_t), s);
     for (int st = 0; st < kNumStages; ++st) cudaMemsetAsync(b.obj[st].mod_cnt, 0, (n_gm + 1) * sizeof(int64_t), s);
-    launch_ingest(b, s);
+    Hooks* h = &ctx->hooks;
+    h->timed = true;
+    h->launches = 0;
+    launch_ingest(b, s, h);
     record(ctx->ev[1], s);
-    if (stop_after >= kMD) launch_md(b, s);
+    if (stop_after >= kMD) launch_md(b, s, h);
     record(ctx->ev[2], s);
-    if (stop_after >= kSG) launch_sg(b, s);
+    if (stop_after >= kSG) launch_sg(b, s, h);
     record(ctx->ev[3], s);
-    if (stop_after >= kTL) launch_tl(b, s);
+    if (stop_after >= kTL) launch_tl(b, s, h);
     record(ctx->ev[4], s);
-    if (stop_after >= kTP) launch_tp(b, s);
+    if (stop_after >= kTP) launch_tp(b, s, h);
     record(ctx->ev[5], s);
-    if (stop_after >= kTC) launch_tc(b, s);
+    if (stop_after >= kTC) launch_tc(b, s, h);
     record(ctx->ev[6], s);
+    ctx->launches_per_run = h->launches;
     // status word and attempted appends for the host's overflow check
     cudaMemcpyAsync(ctx->h_small, b.n_rec, kNumStages * sizeof(int64_t), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(ctx->h_small + kNumStages, b.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
@@ -379,13 +385,16 @@ int launch_checked(sdlg_ctx* ctx, int stop_after) {
     for (int st = 0; st < kNumStages; ++st) cudaMemsetAsync(b.obj[st].mod_cnt, 0, (n_gm + 1) * sizeof(int64_t), s);
     int rc;
     record(ctx->ev[0], s);
-    launch_ingest(b, s);
+    Hooks* h = &ctx->hooks;
+    h->timed = true;
+    h->launches = 0;
+    launch_ingest(b, s, h);
     if ((rc = check_stage(ctx, "ingest"))) return rc;
     record(ctx->ev[1], s);
-    void (*fns[5])(const BatchDev&, cudaStream_t) = {launch_md, launch_sg, launch_tl, launch_tp, launch_tc};
+    void (*fns[5])(const BatchDev&, cudaStream_t, Hooks*) = {launch_md, launch_sg, launch_tl, launch_tp, launch_tc};
     static const char* names[5] = {"MD", "SG", "TL", "TP", "TC"};
     for (int st = 0; st < 5; ++st) {
-        if (stop_after >= st) fns[st](b, s);
+        if (stop_after >= st) fns[st](b, s, h);
         if ((rc = check_stage(ctx, names[st]))) return rc;
         record(ctx->ev[2 + st], s);
     }
@@ -530,6 +539,10 @@ int sdlg_create(sdlg_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&ctx->ev[k]);
+    for (int k = 0; k < kNumStages && e == cudaSuccess; ++k) {
+        e = cudaEventCreate(&ctx->hooks.enum_start[k]);
+        if (e == cudaSuccess) e = cudaEventCreate(&ctx->hooks.enum_stop[k]);
+    }
     if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_small, 16 * sizeof(int64_t));
     if (e != cudaSuccess) {
         delete ctx;
@@ -548,6 +561,10 @@ int sdlg_destroy(sdlg_ctx* ctx) {
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     for (int k = 0; k < 8; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
+    for (int k = 0; k < kNumStages; ++k) {
+        if (ctx->hooks.enum_start[k]) cudaEventDestroy(ctx->hooks.enum_start[k]);
+        if (ctx->hooks.enum_stop[k]) cudaEventDestroy(ctx->hooks.enum_stop[k]);
+    }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SDLG_OK;
@@ -739,6 +756,21 @@ int sdlg_last_times(sdlg_ctx* ctx, float* out7) {
     CK(cudaEventElapsedTime(&out7[6], ctx->ev[0], ctx->ev[6]));
     return SDLG_OK;
 }
+
+int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5) {
+    if (!ctx || !out5) return SDLG_ERR_ARG;
+    if (!ctx->ran) return fail(ctx, SDLG_ERR_NO_EVENTS, "chain not run");
+    cudaSetDevice(ctx->device);
+    for (int k = 0; k < kNumStages; ++k) {
+        out5[k] = 0.f;
+        if (k > ctx->last_stop) continue;
+        CK(cudaEventSynchronize(ctx->hooks.enum_stop[k]));
+        CK(cudaEventElapsedTime(&out5[k], ctx->hooks.enum_start[k], ctx->hooks.enum_stop[k]));
+    }
+    return SDLG_OK;
+}
+
+int64_t sdlg_last_launches(const sdlg_ctx* ctx) { return ctx ? ctx->launches_per_run : -1; }
 
 int sdlg_host_alloc(sdlg_ctx* ctx, int64_t bytes, void** out) {
     if (!ctx || !out || bytes <= 0) return SDLG_ERR_ARG;

@@ -702,8 +702,20 @@ unsigned grid_for(int64_t n, int threads, int cap_blocks) {
     return (unsigned)g;
 }
 
+inline void rec_event(cudaEvent_t e, cudaStream_t s) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(s, &st);
+    if (st == cudaStreamCaptureStatusActive) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+    else cudaEventRecord(e, s);
+}
+
+void scan_h(const BatchDev& b, int64_t* data, const int64_t* n_ptr, int64_t cap, cudaStream_t s, Hooks* h) {
+    scan(b, data, n_ptr, cap, s);
+    if (h) h->launches += 3;
+}
+
 template <class F>
-void enum_and_group(const BatchDev& b, cudaStream_t s) {
+void enum_and_group(const BatchDev& b, cudaStream_t s, Hooks* h) {
     constexpr int st = F::kSt;
     const int64_t* ninner_ptr = nullptr;
     switch (st) {
@@ -713,50 +725,59 @@ void enum_and_group(const BatchDev& b, cudaStream_t s) {
         case kTP: ninner_ptr = b.obj[kSG].mod_cnt + b.n_gm; break;
         default: ninner_ptr = b.obj[kTL].mod_cnt + b.n_gm;
     }
-    scan(b, b.cand[st], ninner_ptr, b.cand_cap[st], s);
+    scan_h(b, b.cand[st], ninner_ptr, b.cand_cap[st], s, h);
+    if (h && h->timed) rec_event(h->enum_start[st], s);
     k_enum<F><<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
+    if (h && h->timed) rec_event(h->enum_stop[st], s);
     k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, st);
-    scan(b, b.obj[st].mod_cnt, b.n_gm_dev, b.n_gm, s);
+    scan_h(b, b.obj[st].mod_cnt, b.n_gm_dev, b.n_gm, s, h);
     k_scatter<<<b.n_sm * 8, 256, 0, s>>>(b, st);
+    if (h) h->launches += 3;
 }
 
 }  // namespace
 
-void launch_ingest(const BatchDev& b, cudaStream_t s) {
+void launch_ingest(const BatchDev& b, cudaStream_t s, Hooks* h) {
     const unsigned g = grid_for(b.n_hit_cap, 256, b.n_sm * 16);
     k_hit_map<<<g, 256, 0, s>>>(b);
-    scan(b, b.mod_hit, b.n_gm_dev, b.n_gm, s);
+    scan_h(b, b.mod_hit, b.n_gm_dev, b.n_gm, s, h);
     k_hit_scatter<<<g, 256, 0, s>>>(b);
+    if (h) h->launches += 2;
 }
 
-void launch_md(const BatchDev& b, cudaStream_t s) {
+void launch_md(const BatchDev& b, cudaStream_t s, Hooks* h) {
     k_md_count<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b);
-    enum_and_group<MDStage>(b, s);
+    if (h) h->launches += 1;
+    enum_and_group<MDStage>(b, s, h);
 }
 
-void launch_sg(const BatchDev& b, cudaStream_t s) {
+void launch_sg(const BatchDev& b, cudaStream_t s, Hooks* h) {
     k_conn_sum<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kMD, kSG);
     k_sg_count<<<b.n_sm * 8, 256, 0, s>>>(b);
-    enum_and_group<SGStage>(b, s);
+    if (h) h->launches += 2;
+    enum_and_group<SGStage>(b, s, h);
 }
 
-void launch_tl(const BatchDev& b, cudaStream_t s) {
+void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     // conn sums over segment counts serve the tracklet enumeration and the
     // triplet candidate counters (Event.cc:547-596 loops over the same lists)
     k_conn_sum<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kSG, kTP);
     k_tl_count<<<b.n_sm * 8, 256, 0, s>>>(b);
-    enum_and_group<TLStage>(b, s);
+    if (h) h->launches += 2;
+    enum_and_group<TLStage>(b, s, h);
 }
 
-void launch_tp(const BatchDev& b, cudaStream_t s) {
+void launch_tp(const BatchDev& b, cudaStream_t s, Hooks* h) {
     k_tp_count<<<b.n_sm * 8, 256, 0, s>>>(b);
-    enum_and_group<TPStage>(b, s);
+    if (h) h->launches += 1;
+    enum_and_group<TPStage>(b, s, h);
 }
 
-void launch_tc(const BatchDev& b, cudaStream_t s) {
+void launch_tc(const BatchDev& b, cudaStream_t s, Hooks* h) {
     k_tc_count<<<b.n_sm * 8, 256, 0, s>>>(b);
     k_tc_cand_counter<<<grid_for(b.n_ev, 128, 1024), 128, 0, s>>>(b);
-    enum_and_group<TCStage>(b, s);
+    if (h) h->launches += 2;
+    enum_and_group<TCStage>(b, s, h);
 }
 
 void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s) {

@@ -45,13 +45,22 @@ struct BatchDev {
     unsigned long long* dbg;       // bounds-check record (debug builds): count, line, index, limit
 };
 
+// Host-side instrumentation of the launches: events around each stage's
+// candidate-evaluation kernel and a count of kernels launched.
+struct Hooks {
+    cudaEvent_t enum_start[kNumStages];
+    cudaEvent_t enum_stop[kNumStages];
+    bool timed = false;
+    int launches = 0;
+};
+
 // stage launchers (each enqueues its kernels on stream s)
-void launch_ingest(const BatchDev& b, cudaStream_t s);
-void launch_md(const BatchDev& b, cudaStream_t s);
-void launch_sg(const BatchDev& b, cudaStream_t s);
-void launch_tl(const BatchDev& b, cudaStream_t s);
-void launch_tp(const BatchDev& b, cudaStream_t s);
-void launch_tc(const BatchDev& b, cudaStream_t s);
+void launch_ingest(const BatchDev& b, cudaStream_t s, Hooks* h);
+void launch_md(const BatchDev& b, cudaStream_t s, Hooks* h);
+void launch_sg(const BatchDev& b, cudaStream_t s, Hooks* h);
+void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h);
+void launch_tp(const BatchDev& b, cudaStream_t s, Hooks* h);
+void launch_tc(const BatchDev& b, cudaStream_t s, Hooks* h);
 // hit-index tuples of stage st for objects [first, first + n) into out (width 2/4/8/8/16)
 void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s);
 

@@ -433,26 +433,25 @@ def _inside(det, rows, p):
     return np.where(kd == KIND_EC, ok_e, ok_b)
 
 
-def _row_lookup(det):
-    if not hasattr(det, "_rowmap"):
-        det._rowmap = {int(d): i for i, d in enumerate(det.detid)}
-    return det._rowmap
+def _rows_of(det, ids):
+    """Sensor rows of detIds (vectorised; every id must exist)."""
+    if not hasattr(det, "_order"):
+        det._order = np.argsort(det.detid, kind="stable")
+        det._sorted = det.detid[det._order]
+    ids = np.asarray(ids, dtype=np.uint32)
+    pos = np.searchsorted(det._sorted, ids)
+    return det._order[pos]
 
 
 def _partner_row(det, lower_rows):
-    rm = _row_lookup(det)
-    out = np.empty(len(lower_rows), dtype=np.int64)
-    for j, r in enumerate(lower_rows):
-        d = int(det.detid[r])
-        out[j] = rm[d + 1] if (d & 3) == 1 else rm[d - 1]
-    return out
+    d = det.detid[lower_rows].astype(np.int64)
+    part = np.where((d & 3) == 1, d + 1, d - 1)
+    return _rows_of(det, part)
 
 
 def _track_hits(det, tr, rng):
     """All sensor crossings of the helices in tr; returns (rows, points)."""
     R, h, phi0, cot, z0 = tr
-    ntrk = R.shape[0]
-    rm = _row_lookup(det)
     rows_all, pts_all = [], []
     # barrel layers
     for layer, branch in [(L, b) for L in range(1, 7) for b in (0, 1)]:
@@ -485,7 +484,7 @@ def _track_hits(det, tr, rng):
             if not np.any(valid):
                 continue
             sel = np.nonzero(valid)[0]
-            low_rows = np.array([rm[int(v)] for v in ids[sel]])
+            low_rows = _rows_of(det, ids[sel])
             up_rows = _partner_row(det, low_rows)
             sub = tuple(p[trk[sel]] for p in tr)
             for s, rows in ((0, low_rows), (1, up_rows)):
@@ -525,7 +524,7 @@ def _track_hits(det, tr, rng):
                 good = ids != 0
                 if not np.any(good):
                     continue
-                low_rows = np.array([rm[int(v)] for v in ids[good]])
+                low_rows = _rows_of(det, ids[good])
                 rows = low_rows if s == 0 else _partner_row(det, low_rows)
                 p = np.stack([px[good], py[good], pz[good]], axis=1)
                 rows_all.append(rows)
