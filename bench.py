@@ -338,8 +338,10 @@ def main():
     achieved = alg_bytes / (tl_mean * 1e-3) / 1e9
     tr = ncu_traffic()
     traffic = None
-    if tr and tr.get("bytes_per_event"):
-        traffic = int(tr["bytes_per_event"])
+    if tr and tr.get("traffic_per_algorithmic_byte"):
+        # DRAM bytes of one ncu capture of this kernel, scaled to this launch
+        # by the algorithmic bytes (segments read, tracklets written)
+        traffic = int(alg_bytes * float(tr["traffic_per_algorithmic_byte"]))
     roofline = {"bound": "hbm", "achieved": round(achieved, 3), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 6), "traffic": traffic, "peak_source": src,
                 "kernel": "k_enum<TLStage> (tracklet cuts)", "kernel_ms": round(tl_mean, 4),

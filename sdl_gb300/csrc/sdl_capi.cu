@@ -302,6 +302,7 @@ int ensure_buffers(sdlg_ctx* ctx) {
     for (int s = 0; s < kNumStages; ++s) AL(b.cand[s], b.cand_cap[s] + 1);
     AL(b.conn_pref, std::max<int64_t>(1, ctx->n_ev * (int64_t)ctx->conn_idx.size()));
     AL(b.conn_sum, n_gm);
+    AL(b.sgpack, ctx->cap_obj[kSG] * PK_N);
     AL(b.counters, ctx->n_ev * 110);
     AL(b.status, 1);
     AL(b.task, kNumStages);

@@ -42,11 +42,15 @@ struct ModDev {
 };
 
 // ------------------------------------------------------------------ math
-__device__ __forceinline__ float f_asin(float x) { return (float)asin((double)x); }
-__device__ __forceinline__ float f_atan(float x) { return (float)atan((double)x); }
-__device__ __forceinline__ float f_sin(float x) { return (float)sin((double)x); }
-__device__ __forceinline__ float f_cos(float x) { return (float)cos((double)x); }
-__device__ __forceinline__ float f_tan(float x) { return (float)tan((double)x); }
+// The double-precision math routines are kept out of line: one copy of each
+// in the binary instead of one per call site keeps the cut kernels small
+// enough for the instruction caches.
+static __device__ __noinline__ float f_asin(float x) { return (float)asin((double)x); }
+static __device__ __noinline__ float f_atan(float x) { return (float)atan((double)x); }
+static __device__ __noinline__ float f_sin(float x) { return (float)sin((double)x); }
+static __device__ __noinline__ float f_cos(float x) { return (float)cos((double)x); }
+static __device__ __noinline__ float f_tan(float x) { return (float)tan((double)x); }
+static __device__ __noinline__ double d_sin(double x) { return sin(x); }
 __device__ __forceinline__ float fmin_ref(float a, float b) { return (b < a) ? b : a; }  // std::min
 __device__ __forceinline__ float fmax_ref(float a, float b) { return (a < b) ? b : a; }  // std::max
 __device__ __forceinline__ int trunc_i32(float f) {
@@ -72,7 +76,7 @@ __device__ __forceinline__ float atan2_ref(float y, float x) {
     if (y > 0) return (float)(kPi / 2);
     return (float)(-kPi / 2);
 }
-__device__ __forceinline__ float phi_of(float x, float y) {
+static __device__ __noinline__ float phi_of(float x, float y) {
     return phi_mpi_pi((float)(kPi + (double)atan2_ref(-y, -x)));
 }
 
@@ -364,42 +368,89 @@ __device__ __forceinline__ bool sg_endcap(const MDView& im, const MDView& om, fl
 }
 
 // ------------------------------------------------------------------ tracklets
-struct AnchorView {
-    P3 p;
-    float asin1;   // asin(min(rt*k, .95))
-    float tand1;   // (float)(tan((double)asin1) / asin1)
-    float asin3;   // asin(min(rt*k/3, .95))
-    const ModDev* m;
+// The tracklet stage reads each segment through a packed 128-byte record
+// built once per segment (k_sg_pack): both anchor hits with their derived
+// quantities, the segment's angles and the per-segment sub-expressions of
+// the tracklet algorithms (all evaluated exactly as in the per-candidate
+// formulas, so the results do not change).
+enum SGPackField : int {
+    PK_LX, PK_LY, PK_LZ, PK_LRT,            // inner-MD anchor
+    PK_LPHI, PK_LR3, PK_LA1, PK_LTD,        //   phi, r3, asin(min(rt*k,.95)), (float)(tan(a1)/a1)
+    PK_LA3, PK_LR3Z, PK_UX, PK_UY,          //   asin(min(rt*k/3,.95)), sqrt(z*z+rt*rt); outer-MD anchor x, y
+    PK_UZ, PK_URT, PK_UPHI, PK_UR3,         //   outer-MD anchor
+    PK_DPC, PK_DPMIN, PK_DPMAX, PK_DPMINC,  // segment dPhiChange, dPhiMin, dPhiMax, dPhiMinChange
+    PK_DPMAXC, PK_RTSEG, PK_ALPHAUP, PK_DPHILU,  // dPhiMaxChange, rt of (up - lo), dphi(up, up - lo), dphi(lo, up)
+    PK_EX, PK_EY, PK_FLAGS, PK_G2,          // outer anchor module's strip-edge offset; flags; module of the outer MD
+    PK_S0, PK_S1, PK_S2, PK_S3,
+    PK_N
 };
-struct SGView {
-    AnchorView lo, up;
-    float dphi, dphimin, dphimax, dphichange, dphiminchange, dphimaxchange;
+enum : uint32_t {
+    F_LO_B = 1u, F_LO_E = 2u, F_LO_PS = 4u,
+    F_UP_B = 8u, F_UP_E = 16u, F_UP_PS = 32u, F_UP_2S = 64u,
 };
 
-// Tracklet.cc:3181-3324
+struct SGV {
+    float lx, ly, lz, lrt, lphi, lr3, la1, ltd, la3, lr3z;
+    float ux, uy, uz, urt, uphi, ur3;
+    float dpc, dpmin, dpmax, dpminc, dpmaxc, rtseg, alphaup, dphilu, ex, ey;
+    uint32_t flags;
+    __device__ P3 lo() const { P3 p; p.x = lx; p.y = ly; p.z = lz; p.rt = lrt; p.phi = lphi; p.r3 = lr3; return p; }
+    __device__ P3 up() const { P3 p; p.x = ux; p.y = uy; p.z = uz; p.rt = urt; p.phi = uphi; p.r3 = ur3; return p; }
+};
+
+__device__ __forceinline__ SGV load_sgv(const float* __restrict__ pack, int64_t s) {
+    const float4* q = reinterpret_cast<const float4*>(pack + s * PK_N);
+    const float4 a = __ldg(q + 0), c = __ldg(q + 1), d = __ldg(q + 2), e = __ldg(q + 3);
+    const float4 f = __ldg(q + 4), g = __ldg(q + 5), h = __ldg(q + 6);
+    SGV v;
+    v.lx = a.x; v.ly = a.y; v.lz = a.z; v.lrt = a.w;
+    v.lphi = c.x; v.lr3 = c.y; v.la1 = c.z; v.ltd = c.w;
+    v.la3 = d.x; v.lr3z = d.y; v.ux = d.z; v.uy = d.w;
+    v.uz = e.x; v.urt = e.y; v.uphi = e.z; v.ur3 = e.w;
+    v.dpc = f.x; v.dpmin = f.y; v.dpmax = f.z; v.dpminc = f.w;
+    v.dpmaxc = g.x; v.rtseg = g.y; v.alphaup = g.z; v.dphilu = g.w;
+    v.ex = h.x; v.ey = h.y; v.flags = __float_as_uint(h.z);
+    return v;
+}
+
+// strip-edge point of a 2S endcap hit (GeometryUtil.cc:3-23) from the edge offset
+__device__ __forceinline__ P3 edge_point(float x, float y, float z, float ex, float ey, bool up) {
+    float px = up ? ex : -ex, py = up ? ey : -ey, pz = 0.f;
+    px += x; py += y; pz += z;
+    return mk2(px, py, pz);
+}
+__device__ __forceinline__ float edge_rt(float x, float y, float ex, float ey, bool up) {
+    float px = up ? ex : -ex, py = up ? ey : -ey;
+    px += x; py += y;
+    return __fsqrt_rn(__fadd_rn(__fmul_rn(px, px), __fmul_rn(py, py)));
+}
+
+// Tracklet.cc:3181-3324.  The reference adds the double copysign term to a
+// float and rounds to float; a double sum of two floats rounded to float
+// equals the float sum (53 >= 2*24+2), so the additions are done in float.
 __device__ __forceinline__ void delta_beta_iterations(float& betaIn, float& betaOut, float& betaAv, float& pt_beta, float sdIn_dr,
                                                       float sdOut_dr, float dr, int lIn, float pt_betaMax) {
     const float sinAlphaMax = 0.95f;
     if (betaIn * betaOut > 0.f &&
         (fabsf(pt_beta) < 4.f * pt_betaMax || (lIn >= 11 && fabsf(pt_beta) < 8.f * pt_betaMax))) {
-        const float betaInUpd = (float)((double)betaIn + copysign((double)f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), (double)betaIn));
-        const float betaOutUpd = (float)((double)betaOut + copysign((double)f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), (double)betaOut));
+        const float betaInUpd = betaIn + copysignf(f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
+        const float betaOutUpd = betaOut + copysignf(f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaOut);
         betaAv = 0.5f * (betaInUpd + betaOutUpd);
-        pt_beta = (float)((double)(dr * k2Rinv1GeVf) / sin((double)betaAv));
-        betaIn = (float)((double)betaIn + copysign((double)f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), (double)betaIn));
-        betaOut = (float)((double)betaOut + copysign((double)f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), (double)betaOut));
+        pt_beta = (float)((double)(dr * k2Rinv1GeVf) / d_sin((double)betaAv));
+        betaIn = betaIn + copysignf(f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
+        betaOut = betaOut + copysignf(f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaOut);
         betaAv = 0.5f * (betaIn + betaOut);
-        pt_beta = (float)((double)(dr * k2Rinv1GeVf) / sin((double)betaAv));
+        pt_beta = (float)((double)(dr * k2Rinv1GeVf) / d_sin((double)betaAv));
     } else if (lIn < 11 && (double)fabsf(betaOut) < 0.2 * (double)fabsf(betaIn) && fabsf(pt_beta) < 12.f * pt_betaMax) {
-        const float pt_betaIn = (float)((double)(dr * k2Rinv1GeVf) / sin((double)betaIn));
-        const float betaInUpd = (float)((double)betaIn + copysign((double)f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), (double)betaIn));
-        const float betaOutUpd = (float)((double)betaOut + copysign((double)f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), (double)betaIn));
+        const float pt_betaIn = (float)((double)(dr * k2Rinv1GeVf) / d_sin((double)betaIn));
+        const float betaInUpd = betaIn + copysignf(f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), betaIn);
+        const float betaOutUpd = betaOut + copysignf(f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), betaIn);
         betaAv = (fabsf(betaOut) > 0.2f * fabsf(betaIn)) ? (0.5f * (betaInUpd + betaOutUpd)) : betaInUpd;
-        pt_beta = (float)((double)(dr * k2Rinv1GeVf) / sin((double)betaAv));
-        betaIn = (float)((double)betaIn + copysign((double)f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), (double)betaIn));
-        betaOut = (float)((double)betaOut + copysign((double)f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), (double)betaIn));
+        pt_beta = (float)((double)(dr * k2Rinv1GeVf) / d_sin((double)betaAv));
+        betaIn = betaIn + copysignf(f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
+        betaOut = betaOut + copysignf(f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
         betaAv = 0.5f * (betaIn + betaOut);
-        pt_beta = (float)((double)(dr * k2Rinv1GeVf) / sin((double)betaAv));
+        pt_beta = (float)((double)(dr * k2Rinv1GeVf) / d_sin((double)betaAv));
     }
 }
 
@@ -411,283 +462,222 @@ __device__ __forceinline__ float dbeta_cut2(float dBetaRes, float dBetaMuls, flo
     return (float)((double)head + 0.25 * (t * t));
 }
 
-// Tracklet.cc:902-1538
-__device__ __forceinline__ bool tl_bbbb(const SGView& S, const SGView& T, bool nm1) {
-    const float pt_betaMax = 7.0f;
-    const AnchorView& InLo = S.lo;
-    const AnchorView& InUp = S.up;
-    const AnchorView& OutLo = T.lo;
-    const AnchorView& OutUp = T.up;
-    const float zpitch_InLo = InLo.m->type == kPS ? kPixelPSZpitch : kStrip2SZpitch;
-    const float zpitch_OutLo = OutLo.m->type == kPS ? kPixelPSZpitch : kStrip2SZpitch;
-    const float rt_InLo = InLo.p.rt, rt_OutLo = OutLo.p.rt, z_InLo = InLo.p.z, z_OutLo = OutLo.p.z;
-    const float alpha1GeV_OutLo = OutLo.asin1;
-    const float rtRatio = rt_OutLo / rt_InLo;
-    const float dzDrtScale = OutLo.tand1;
-    const float zHi = z_InLo + (z_InLo + kDeltaZLum) * (rtRatio - 1.f) * (z_InLo < 0.f ? 1.f : dzDrtScale) + (zpitch_InLo + zpitch_OutLo);
-    const float zLo = z_InLo + (z_InLo - kDeltaZLum) * (rtRatio - 1.f) * (z_InLo > 0.f ? 1.f : dzDrtScale) - (zpitch_InLo + zpitch_OutLo);
-    if (!(z_OutLo >= zLo && z_OutLo <= zHi)) return false;
-    const float drt_OutLo_InLo = rt_OutLo - rt_InLo;
-    const float drt_InSeg = InUp.p.rt - InLo.p.rt;
-    const float dz_InSeg = InUp.p.z - InLo.p.z;
-    const float dr3_InSeg = InUp.p.r3 - InLo.p.r3;
-    const float coshEta = dr3_InSeg / drt_InSeg;
-    const float r3_InLo = __fsqrt_rn(z_InLo * z_InLo + rt_InLo * rt_InLo);
-    const float sdlThetaMulsF = (float)((double)0.015f * sqrt((double)0.1f + 0.2 * (double)(rt_OutLo - rt_InLo) / (double)50.f) * sqrt((double)(r3_InLo / rt_InLo)));
-    const float sdlMuls = sdlThetaMulsF * 3.f / kPtCut * 4.f;
-    const float sdlPVoff = 0.1f / rt_OutLo;
-    const float sdlCut = (float)((double)alpha1GeV_OutLo + sqrt((double)(sdlMuls * sdlMuls + sdlPVoff * sdlPVoff)));
-    // cut #3 (independent of cut #2; evaluated first because it is cheaper)
-    if (!(fabsf(dphi(InUp.p, OutUp.p)) <= sdlCut)) return false;
-    float dzErr = (zpitch_InLo + zpitch_OutLo) * (zpitch_InLo + zpitch_OutLo) * 2.f;
-    dzErr += sdlMuls * sdlMuls * drt_OutLo_InLo * drt_OutLo_InLo / 3.f * coshEta * coshEta;
-    dzErr = __fsqrt_rn(dzErr);
-    const float dzMean = dz_InSeg / drt_InSeg * drt_OutLo_InLo;
-    const float zWindow = dzErr / drt_InSeg * drt_OutLo_InLo + (zpitch_InLo + zpitch_OutLo);
-    const float zLoPointed = z_InLo + dzMean * (z_InLo > 0.f ? 1.f : dzDrtScale) - zWindow;
-    const float zHiPointed = z_InLo + dzMean * (z_InLo < 0.f ? 1.f : dzDrtScale) + zWindow;
-    if (!(z_OutLo >= zLoPointed && z_OutLo <= zHiPointed)) return false;
-    const P3 mid = midpoint(InLo.p, OutLo.p);
-    const float dPhi = dphi(mid, sub(OutLo.p, InLo.p));
-    if (!(fabsf(dPhi) <= sdlCut)) return false;
-    const float alpha_InLo = S.dphichange;
-    const bool isEC_lastLayer = OutUp.m->subdet == kEndcap && OutUp.m->type == kTwoS;
-    const P3 tl_axis = sub(OutUp.p, InLo.p);
-    const float drt_tl_axis = tl_axis.rt;
-    const float rt_InSeg = rt_of_diff(InUp.p, InLo.p);
-    float betaIn = alpha_InLo - dphi(InLo.p, tl_axis);
-    const float betaIn_cut = f_asin(fmin_ref((-rt_InSeg * 1.f + drt_tl_axis) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / drt_InSeg);
-    float betaInRHmin = betaIn, betaInRHmax = betaIn;
-    if (!(fabsf(betaInRHmin) < betaIn_cut)) return false;
-    const float alpha_OutUp = dphi(OutUp.p, sub(OutUp.p, OutLo.p));
-    float betaOut = -alpha_OutUp + dphi(OutUp.p, tl_axis);
-    float betaOutRHmin, betaOutRHmax;
-    P3 hiE = OutUp.p, loE = OutUp.p;
-    if (isEC_lastLayer) {
-        hiE = strip_edge(OutUp.p, *OutUp.m, true);
-        loE = strip_edge(OutUp.p, *OutUp.m, false);
-        const float alpha_hi = dphi(hiE, sub(hiE, OutLo.p));
-        const float alpha_lo = dphi(loE, sub(loE, OutLo.p));
-        betaOutRHmin = -alpha_hi + dphi(hiE, sub(hiE, InLo.p));
-        betaOutRHmax = -alpha_lo + dphi(loE, sub(loE, InLo.p));
-    } else {
-        betaOutRHmin = betaOut;
-        betaOutRHmax = betaOut;
+// (float)(x + sqrt(y)) with the sum in double, as the reference writes it
+__device__ __forceinline__ float add_dsqrt(float x, float y) { return (float)((double)x + sqrt((double)y)); }
+
+// Tracklet algorithm ids carried between the two phases
+enum : int { kAlgoNone = 0, kAlgoBBBB = 1, kAlgoBBEE = 2, kAlgoEEEE = 3 };
+
+// ---- phase A: dispatch (Tracklet.cc:144-296) and the cuts that need only
+// float arithmetic and square roots.  Returns the algorithm or kAlgoNone,
+// and the two quantities phase B reuses.
+__device__ __forceinline__ int tl_phaseA(const SGV& S, const SGV& T, float& sdlCut, float& mulsF) {
+    const uint32_t fs = S.flags, ft = T.flags;
+    const bool b1 = fs & F_LO_B, b2 = fs & F_UP_B, b3 = ft & F_LO_B, b4 = ft & F_UP_B;
+    const bool e1 = fs & F_LO_E, e2 = fs & F_UP_E, e3 = ft & F_LO_E, e4 = ft & F_UP_E;
+    const float rtIn = S.lrt, rtOut = T.lrt, zIn = S.lz, zOut = T.lz;
+    if (b1 && b2 && b3 && (b4 || e4)) {
+        // Tracklet.cc:902-1132 (cuts 1, 3 and 2)
+        const float zpitch_InLo = (fs & F_LO_PS) ? kPixelPSZpitch : kStrip2SZpitch;
+        const float zpitch_OutLo = (ft & F_LO_PS) ? kPixelPSZpitch : kStrip2SZpitch;
+        const float rtRatio = rtOut / rtIn;
+        const float dzDrtScale = T.ltd;
+        const float zHi = zIn + (zIn + kDeltaZLum) * (rtRatio - 1.f) * (zIn < 0.f ? 1.f : dzDrtScale) + (zpitch_InLo + zpitch_OutLo);
+        const float zLo = zIn + (zIn - kDeltaZLum) * (rtRatio - 1.f) * (zIn > 0.f ? 1.f : dzDrtScale) - (zpitch_InLo + zpitch_OutLo);
+        if (!(zOut >= zLo && zOut <= zHi)) return kAlgoNone;
+        mulsF = (float)((double)0.015f * sqrt((double)0.1f + 0.2 * (double)(rtOut - rtIn) / (double)50.f) * sqrt((double)(S.lr3z / rtIn)));
+        const float sdlMuls = mulsF * 3.f / kPtCut * 4.f;
+        const float sdlPVoff = 0.1f / rtOut;
+        sdlCut = add_dsqrt(T.la1, sdlMuls * sdlMuls + sdlPVoff * sdlPVoff);
+        if (!(fabsf(phi_mpi_pi(T.uphi - S.uphi)) <= sdlCut)) return kAlgoNone;
+        const float drt_OutLo_InLo = rtOut - rtIn;
+        const float drt_InSeg = S.urt - S.lrt;
+        const float dz_InSeg = S.uz - S.lz;
+        const float coshEta = (S.ur3 - S.lr3) / drt_InSeg;
+        float dzErr = (zpitch_InLo + zpitch_OutLo) * (zpitch_InLo + zpitch_OutLo) * 2.f;
+        dzErr += sdlMuls * sdlMuls * drt_OutLo_InLo * drt_OutLo_InLo / 3.f * coshEta * coshEta;
+        dzErr = __fsqrt_rn(dzErr);
+        const float dzMean = dz_InSeg / drt_InSeg * drt_OutLo_InLo;
+        const float zWindow = dzErr / drt_InSeg * drt_OutLo_InLo + (zpitch_InLo + zpitch_OutLo);
+        const float zLoPointed = zIn + dzMean * (zIn > 0.f ? 1.f : dzDrtScale) - zWindow;
+        const float zHiPointed = zIn + dzMean * (zIn < 0.f ? 1.f : dzDrtScale) + zWindow;
+        if (!(zOut >= zLoPointed && zOut <= zHiPointed)) return kAlgoNone;
+        return kAlgoBBBB;
     }
-    float betaAv = 0.5f * (betaIn + betaOut);
-    float pt_beta = (float)((double)(drt_tl_axis * k2Rinv1GeVf) / sin((double)betaAv));
-    const int lIn = 5;
-    const int lOut = isEC_lastLayer ? 11 : 5;
-    const float sdOut_dr = rt_of_diff(OutUp.p, OutLo.p);
-    const float sdOut_d = OutUp.p.rt - OutLo.p.rt;
-    delta_beta_iterations(betaIn, betaOut, betaAv, pt_beta, rt_InSeg, sdOut_dr, drt_tl_axis, lIn, pt_betaMax);
-    const float betaInMMSF = (fabsf(betaInRHmin + betaInRHmax) > 0) ? (2.f * betaIn / fabsf(betaInRHmin + betaInRHmax)) : 0.f;
-    const float betaOutMMSF = (fabsf(betaOutRHmin + betaOutRHmax) > 0) ? (2.f * betaOut / fabsf(betaOutRHmin + betaOutRHmax)) : 0.f;
-    betaInRHmin *= betaInMMSF; betaInRHmax *= betaInMMSF;
-    betaOutRHmin *= betaOutMMSF; betaOutRHmax *= betaOutMMSF;
-    const float dBetaMuls = sdlThetaMulsF * 4.f / fmin_ref(fabsf(pt_beta), pt_betaMax);
-    const float alpha_OutLo = T.dphichange;
-    const float alphaInAbsReg = fmax_ref(fabsf(alpha_InLo), InLo.asin3);
-    const float alphaOutAbsReg = fmax_ref(fabsf(alpha_OutLo), OutLo.asin3);
-    const float dBetaInLum = lIn < 11 ? 0.0f : fabsf(alphaInAbsReg * kDeltaZLum / InLo.p.z);
-    const float dBetaOutLum = lOut < 11 ? 0.0f : fabsf(alphaOutAbsReg * kDeltaZLum / OutLo.p.z);
-    const float dBetaLum2 = (dBetaInLum + dBetaOutLum) * (dBetaInLum + dBetaOutLum);
-    const float sinDPhi = f_sin(dPhi);
-    const double rr = (double)((hiE.rt - loE.rt) * sinDPhi / drt_tl_axis);
-    const float dBetaROut2 = (float)(rr * rr);
-    const float betaOut_cut = (float)((double)(f_asin(fmin_ref(drt_tl_axis * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d)) + sqrt((double)(dBetaLum2 + dBetaMuls * dBetaMuls)));
-    if (!(fabsf(betaOut) < betaOut_cut)) return false;
-    const float dBetaRes = 0.02f / fmin_ref(sdOut_d, drt_InSeg);
-    const float dBetaCut2 = dbeta_cut2(dBetaRes, dBetaMuls, dBetaLum2, dBetaROut2, betaInRHmin, betaInRHmax, betaOutRHmin, betaOutRHmax);
-    const float dBeta = betaIn - betaOut;
-    return (dBeta * dBeta <= dBetaCut2) || nm1;
+    if (b1 && e3 && e4 && (b2 || e2)) {
+        // Tracklet.cc:1540-1720
+        const float zGeom = ((fs & F_LO_PS) ? kPixelPSZpitch : kStrip2SZpitch) + ((ft & F_LO_PS) ? kPixelPSZpitch : kStrip2SZpitch);
+        const float dzDrtScale = T.ltd;
+        if (!(zIn * zOut > 0)) return kAlgoNone;
+        const float dLum = f_copysign(kDeltaZLum, zIn);
+        const float rtGeom1 = (ft & F_LO_PS) ? kPixelPSZpitch : kStrip2SZpitch;
+        const float zGeom1 = f_copysign(zGeom, zIn);
+        const float rtLo = rtIn * (1.f + (zOut - zIn - zGeom1) / (zIn + zGeom1 + dLum) / dzDrtScale) - rtGeom1;
+        if (!(rtOut >= rtLo)) return kAlgoNone;
+        float zInForHi = zIn - zGeom1 - dLum;
+        if (zInForHi * zIn < 0) zInForHi = f_copysign(0.1f, zIn);
+        const float rtHi = rtIn * (1.f + (zOut - zIn + zGeom1) / zInForHi) + rtGeom1;
+        if (!(rtOut >= rtLo && rtOut <= rtHi)) return kAlgoNone;
+        const float kZ = (zOut - zIn) / (S.uz - S.lz);
+        if (!(kZ >= 0)) return kAlgoNone;
+        mulsF = (float)((double)0.015f * sqrt((double)0.1f + 0.2 * (double)(rtOut - rtIn) / (double)50.f) * sqrt((double)(S.lr3z / rtIn)));
+        const float sdlMuls = mulsF * 3.f / kPtCut * 4.f;
+        const float sdlPVoff = 0.1f / rtOut;
+        sdlCut = add_dsqrt(T.la1, sdlMuls * sdlMuls + sdlPVoff * sdlPVoff);
+        if (!(fabsf(phi_mpi_pi(T.uphi - S.uphi)) <= sdlCut)) return kAlgoNone;
+        return kAlgoBBEE;
+    }
+    if (e1 && e2 && e3 && e4) {
+        // Tracklet.cc:2018-2218
+        const float dzDrtScale = T.ltd;
+        if (!(zIn * zOut > 0)) return kAlgoNone;
+        const float dLum = f_copysign(kDeltaZLum, zIn);
+        const bool inPS = fs & F_LO_PS, outPS = ft & F_LO_PS;
+        const float rtGeom = (inPS && outPS) ? 2.f * kPixelPSZpitch : (inPS || outPS) ? (kPixelPSZpitch + kStrip2SZpitch) : 2.f * kStrip2SZpitch;
+        const float dz = zOut - zIn;
+        const float rtLo = rtIn * (1.f + dz / (zIn + dLum) / dzDrtScale) - rtGeom;
+        if (!(rtOut >= rtLo)) return kAlgoNone;
+        const float rtHi = rtIn * (1.f + dz / (zIn - dLum)) + rtGeom;
+        if (!(rtOut >= rtLo && rtOut <= rtHi)) return kAlgoNone;
+        mulsF = (float)((double)0.015f * sqrt((double)0.1f + 0.2 * (double)(rtOut - rtIn) / (double)50.f));
+        const float sdlMuls = mulsF * 3.f / kPtCut * 4.f;
+        const float sdlPVoff = 0.1f / rtOut;
+        sdlCut = add_dsqrt(T.la1, sdlMuls * sdlMuls + sdlPVoff * sdlPVoff);
+        if (!(fabsf(phi_mpi_pi(T.uphi - S.uphi)) <= sdlCut)) return kAlgoNone;
+        if (inPS && (fs & F_UP_PS)) {
+            const float drtSDIn = S.urt - S.lrt;
+            const float dzSDIn = S.uz - S.lz;
+            const float coshEta = (S.ur3 - S.lr3) / drtSDIn;
+            const float dzOutInAbs = fabsf(zOut - zIn);
+            const float multDzDr = dzOutInAbs * coshEta / (coshEta * coshEta - 1.f);
+            const float kZ = (zOut - zIn) / dzSDIn;
+            float drtErr = kPixelPSZpitch * kPixelPSZpitch * 2.f / dzSDIn / dzSDIn * dzOutInAbs * dzOutInAbs;
+            drtErr += sdlMuls * sdlMuls * multDzDr * multDzDr / 3.f * coshEta * coshEta;
+            drtErr = __fsqrt_rn(drtErr);
+            const float drtMean = drtSDIn * dzOutInAbs / fabsf(dzSDIn);
+            const float rtWindow = drtErr + rtGeom;
+            const float rtLo_point = rtIn + drtMean / dzDrtScale - rtWindow;
+            const float rtHi_point = rtIn + drtMean + rtWindow;
+            if (!(kZ >= 0 && rtOut >= rtLo_point && rtOut <= rtHi_point)) return kAlgoNone;
+        }
+        return kAlgoEEEE;
+    }
+    return kAlgoNone;
 }
 
-// Tracklet.cc:1540-2016
-__device__ __forceinline__ bool tl_bbee(const SGView& S, const SGView& T, bool nm1) {
+// ---- phase B: the remaining cuts (mid-point direction, betaIn, the
+// deltaBeta iterations, betaOut and the deltaBeta cut)
+static __device__ __noinline__ bool tl_phaseB(int algo, const SGV& S, const SGV& T, float sdlCut, float mulsF, bool nm1) {
     const float pt_betaMax = 7.0f;
-    const AnchorView& InLo = S.lo;
-    const AnchorView& InUp = S.up;
-    const AnchorView& OutLo = T.lo;
-    const AnchorView& OutUp = T.up;
-    const float zGeom = (InLo.m->type == kPS ? kPixelPSZpitch : kStrip2SZpitch) + (OutLo.m->type == kPS ? kPixelPSZpitch : kStrip2SZpitch);
-    const float rtIn = InLo.p.rt, rtOut = OutLo.p.rt, zIn = InLo.p.z, zOut = OutLo.p.z;
-    const float sdlSlope = OutLo.asin1;
-    const float dzDrtScale = OutLo.tand1;
-    if (!(zIn * zOut > 0)) return false;
-    const float dLum = f_copysign(kDeltaZLum, zIn);
-    const float rtGeom1 = OutLo.m->type == kPS ? kPixelPSZpitch : kStrip2SZpitch;
-    const float zGeom1 = f_copysign(zGeom, zIn);
-    const float rtLo = rtIn * (1.f + (zOut - zIn - zGeom1) / (zIn + zGeom1 + dLum) / dzDrtScale) - rtGeom1;
-    if (!(rtOut >= rtLo)) return false;
-    float zInForHi = zIn - zGeom1 - dLum;
-    if (zInForHi * zIn < 0) zInForHi = f_copysign(0.1f, zIn);
-    const float rtHi = rtIn * (1.f + (zOut - zIn + zGeom1) / zInForHi) + rtGeom1;
-    if (!(rtOut >= rtLo && rtOut <= rtHi)) return false;
-    const float dzSDIn = InUp.p.z - InLo.p.z;
-    const float kZ = (zOut - zIn) / dzSDIn;
-    if (!(kZ >= 0)) return false;
-    const float rIn = __fsqrt_rn(zIn * zIn + rtIn * rtIn);
-    const float sdlThetaMulsF = (float)((double)0.015f * sqrt((double)0.1f + 0.2 * (double)(rtOut - rtIn) / (double)50.f) * sqrt((double)(rIn / rtIn)));
-    const float sdlMuls = sdlThetaMulsF * 3.f / kPtCut * 4.f;
-    const float sdlPVoff = 0.1f / rtOut;
-    const float sdlCut = (float)((double)sdlSlope + sqrt((double)(sdlMuls * sdlMuls + sdlPVoff * sdlPVoff)));
-    if (!(fabsf(dphi(InUp.p, OutUp.p)) <= sdlCut)) return false;
-    const P3 mid = midpoint(InLo.p, OutLo.p);
-    const float dPhi = dphi(mid, sub(OutLo.p, InLo.p));
+    const P3 InLo = S.lo(), InUp = S.up(), OutLo = T.lo(), OutUp = T.up();
+    const P3 mid = midpoint(InLo, OutLo);
+    const float dPhi = dphi(mid, sub(OutLo, InLo));
     if (!(fabsf(dPhi) <= sdlCut)) return false;
-    const float sdIn_alpha = S.dphichange;
-    const float sdOut_alpha = S.dphichange;  // (sic) Tracklet.cc:1790
-    const float sdOut_alphaOut = dphi(OutUp.p, sub(OutUp.p, OutLo.p));
-    const float sdOut_alphaOut_min = phi_mpi_pi(T.dphiminchange - T.dphimin);
-    const float sdOut_alphaOut_max = phi_mpi_pi(T.dphimaxchange - T.dphimax);
-    const P3 dr3 = sub(OutUp.p, InLo.p);
-    float betaIn = sdIn_alpha - dphi(InLo.p, dr3);
-    float betaOut = -sdOut_alphaOut + dphi(OutUp.p, dr3);
-    float betaInRHmin = betaIn, betaInRHmax = betaIn;  // isEC_secondLayer is always false (Tracklet.cc:1798)
-    float betaOutRHmin = betaOut - sdOut_alphaOut_min + sdOut_alphaOut;
-    float betaOutRHmax = betaOut - sdOut_alphaOut_max + sdOut_alphaOut;
-    if (fabsf(betaOutRHmin) > fabsf(betaOutRHmax)) { float t = betaOutRHmin; betaOutRHmin = betaOutRHmax; betaOutRHmax = t; }
-    const float sdIn_dr = rt_of_diff(InUp.p, InLo.p);
-    const float sdIn_d = InUp.p.rt - InLo.p.rt;
-    const float dr = dr3.rt;
-    const float betaIn_cut = f_asin(fmin_ref((-sdIn_dr * 1.f + dr) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdIn_d);
-    if (!(fabsf(betaInRHmin) < betaIn_cut)) return false;
-    float betaAv = 0.5f * (betaIn + betaOut);
-    float pt_beta = (float)((double)(dr * k2Rinv1GeVf) / sin((double)betaAv));
-    const int lIn = 5, lOut = 11;
-    const float sdOut_dr = rt_of_diff(OutUp.p, OutLo.p);
-    const float sdOut_d = OutUp.p.rt - OutLo.p.rt;
-    delta_beta_iterations(betaIn, betaOut, betaAv, pt_beta, sdIn_dr, sdOut_dr, dr, lIn, pt_betaMax);
-    const float betaInMMSF = (fabsf(betaInRHmin + betaInRHmax) > 0) ? 2.f * betaIn / fabsf(betaInRHmin + betaInRHmax) : 0.f;
-    const float betaOutMMSF = (fabsf(betaOutRHmin + betaOutRHmax) > 0) ? 2.f * betaOut / fabsf(betaOutRHmin + betaOutRHmax) : 0.f;
-    betaInRHmin *= betaInMMSF; betaInRHmax *= betaInMMSF;
-    betaOutRHmin *= betaOutMMSF; betaOutRHmax *= betaOutMMSF;
-    const float dBetaMuls = sdlThetaMulsF * 4.f / fmin_ref(fabsf(pt_beta), pt_betaMax);
-    const float alphaInAbsReg = fmax_ref(fabsf(sdIn_alpha), InLo.asin3);
-    const float alphaOutAbsReg = fmax_ref(fabsf(sdOut_alpha), OutLo.asin3);
-    const float dBetaInLum = lIn < 11 ? 0.0f : fabsf(alphaInAbsReg * kDeltaZLum / InLo.p.z);
-    const float dBetaOutLum = lOut < 11 ? 0.0f : fabsf(alphaOutAbsReg * kDeltaZLum / OutLo.p.z);
-    const float dBetaLum2 = (dBetaInLum + dBetaOutLum) * (dBetaInLum + dBetaOutLum);
-    const float sinDPhi = f_sin(dPhi);
+    const P3 axis = sub(OutUp, InLo);  // tl_axis (BBBB) / dr3 (BBEE, EEEE)
+    const float dr = axis.rt;
+    const float sdIn_dr = S.rtseg;
+    const float sdIn_d = InUp.rt - InLo.rt;
+    const float sdOut_dr = T.rtseg;
+    const float sdOut_d = OutUp.rt - OutLo.rt;
+    float betaIn, betaOut, betaInRHmin, betaInRHmax, betaOutRHmin, betaOutRHmax;
+    float alphaIn, alphaOutReg;
+    int lIn, lOut;
     float dBetaROut2 = 0.f;
-    if (OutUp.m->type == kTwoS) {
-        const P3 hiE = strip_edge(OutUp.p, *OutUp.m, true);
-        const P3 loE = strip_edge(OutUp.p, *OutUp.m, false);
-        const double rr = (double)((hiE.rt - loE.rt) * sinDPhi / dr);
-        dBetaROut2 = (float)(rr * rr);
+    if (algo == kAlgoBBBB) {
+        // Tracklet.cc:1205-1538
+        alphaIn = S.dpc;
+        betaIn = alphaIn - dphi(InLo, axis);
+        const float betaIn_cut = f_asin(fmin_ref((-sdIn_dr * 1.f + dr) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdIn_d);
+        betaInRHmin = betaIn; betaInRHmax = betaIn;
+        if (!(fabsf(betaInRHmin) < betaIn_cut)) return false;
+        betaOut = -T.alphaup + dphi(OutUp, axis);
+        const bool ec2s = (T.flags & F_UP_E) && (T.flags & F_UP_2S);
+        if (ec2s) {
+            const P3 hiE = edge_point(OutUp.x, OutUp.y, OutUp.z, T.ex, T.ey, true);
+            const P3 loE = edge_point(OutUp.x, OutUp.y, OutUp.z, T.ex, T.ey, false);
+            betaOutRHmin = -dphi(hiE, sub(hiE, OutLo)) + dphi(hiE, sub(hiE, InLo));
+            betaOutRHmax = -dphi(loE, sub(loE, OutLo)) + dphi(loE, sub(loE, InLo));
+            const float sinDPhi = f_sin(dPhi);
+            const double rr = (double)((hiE.rt - loE.rt) * sinDPhi / dr);
+            dBetaROut2 = (float)(rr * rr);
+        } else {
+            // (rt - rt) * sin(dPhi) / dr squared: sin(dPhi) is finite here
+            // (|dPhi| <= sdlCut), so the product is a signed zero and only
+            // its square matters
+            betaOutRHmin = betaOut; betaOutRHmax = betaOut;
+            const double rr = (double)((OutUp.rt - OutUp.rt) * 0.f / dr);
+            dBetaROut2 = (float)(rr * rr);
+        }
+        alphaOutReg = T.dpc;
+        lIn = 5;
+        lOut = ec2s ? 11 : 5;
+    } else if (algo == kAlgoBBEE) {
+        // Tracklet.cc:1765-2016
+        alphaIn = S.dpc;
+        const float sdOut_alphaOut = T.alphaup;
+        const float sdOut_alphaOut_min = phi_mpi_pi(T.dpminc - T.dpmin);
+        const float sdOut_alphaOut_max = phi_mpi_pi(T.dpmaxc - T.dpmax);
+        betaIn = alphaIn - dphi(InLo, axis);
+        betaOut = -sdOut_alphaOut + dphi(OutUp, axis);
+        betaInRHmin = betaIn; betaInRHmax = betaIn;  // isEC_secondLayer is always false (Tracklet.cc:1798)
+        betaOutRHmin = betaOut - sdOut_alphaOut_min + sdOut_alphaOut;
+        betaOutRHmax = betaOut - sdOut_alphaOut_max + sdOut_alphaOut;
+        if (fabsf(betaOutRHmin) > fabsf(betaOutRHmax)) { const float t = betaOutRHmin; betaOutRHmin = betaOutRHmax; betaOutRHmax = t; }
+        const float betaIn_cut = f_asin(fmin_ref((-sdIn_dr * 1.f + dr) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdIn_d);
+        if (!(fabsf(betaInRHmin) < betaIn_cut)) return false;
+        if (T.flags & F_UP_2S) {
+            const float sinDPhi = f_sin(dPhi);
+            const float hrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, true);
+            const float lrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, false);
+            const double rr = (double)((hrt - lrt) * sinDPhi / dr);
+            dBetaROut2 = (float)(rr * rr);
+        } else {
+            const double rr = (double)((OutUp.rt - OutUp.rt) * 0.f / dr);  // see the BBBB branch
+            dBetaROut2 = (float)(rr * rr);
+        }
+        alphaOutReg = S.dpc;  // sdOut_alpha is the inner segment's (Tracklet.cc:1790)
+        lIn = 5;
+        lOut = 11;
     } else {
-        const double rr = (double)((OutUp.p.rt - OutUp.p.rt) * sinDPhi / dr);
-        dBetaROut2 = (float)(rr * rr);
+        // Tracklet.cc:2220-2665
+        alphaIn = S.dpc;
+        const float sdOut_dPhiPos = T.dphilu;
+        const float sdOut_alphaOutRHmin = phi_mpi_pi(T.dpminc - sdOut_dPhiPos);
+        const float sdOut_alphaOutRHmax = phi_mpi_pi(T.dpmaxc - sdOut_dPhiPos);
+        const float sdOut_alphaOut = phi_mpi_pi(T.dpc - sdOut_dPhiPos);
+        betaIn = alphaIn - dphi(InLo, axis);
+        betaOut = -sdOut_alphaOut + dphi(OutUp, axis);
+        betaInRHmin = betaIn + S.dpminc - alphaIn;
+        betaInRHmax = betaIn + S.dpmaxc - alphaIn;
+        if (fabsf(betaInRHmin) > fabsf(betaInRHmax)) { const float t = betaInRHmin; betaInRHmin = betaInRHmax; betaInRHmax = t; }
+        betaOutRHmin = betaOut - sdOut_alphaOutRHmin + sdOut_alphaOut;
+        betaOutRHmax = betaOut - sdOut_alphaOutRHmax + sdOut_alphaOut;
+        if (fabsf(betaOutRHmin) > fabsf(betaOutRHmax)) { const float t = betaOutRHmin; betaOutRHmin = betaOutRHmax; betaOutRHmax = t; }
+        // cut #6 never rejects here (Tracklet.cc:2327-2336)
+        alphaOutReg = S.dpc;  // (sic)
+        lIn = 11;
+        lOut = 13;
     }
-    const float betaOut_cut = (float)((double)(f_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d)) + sqrt((double)(dBetaLum2 + dBetaMuls * dBetaMuls)));
-    if (!(fabsf(betaOut) < betaOut_cut)) return false;
-    const float dBetaRes = 0.02f / fmin_ref(sdOut_d, sdIn_d);
-    const float dBetaCut2 = dbeta_cut2(dBetaRes, dBetaMuls, dBetaLum2, dBetaROut2, betaInRHmin, betaInRHmax, betaOutRHmin, betaOutRHmax);
-    const float dBeta = betaIn - betaOut;
-    return (dBeta * dBeta <= dBetaCut2) || nm1;
-}
-
-// Tracklet.cc:2018-2665
-__device__ __forceinline__ bool tl_eeee(const SGView& S, const SGView& T, bool nm1) {
-    const float pt_betaMax = 7.0f;
-    const AnchorView& InLo = S.lo;
-    const AnchorView& InUp = S.up;
-    const AnchorView& OutLo = T.lo;
-    const AnchorView& OutUp = T.up;
-    const float rtIn = InLo.p.rt, rtOut = OutLo.p.rt, zIn = InLo.p.z, zOut = OutLo.p.z;
-    const float sdlSlope = OutLo.asin1;
-    const float dzDrtScale = OutLo.tand1;
-    if (!(zIn * zOut > 0)) return false;
-    const float dLum = f_copysign(kDeltaZLum, zIn);
-    const bool isOutSgInnerMDPS = OutLo.m->type == kPS;
-    const bool isInSgInnerMDPS = InLo.m->type == kPS;
-    const float rtGeom = (isInSgInnerMDPS && isOutSgInnerMDPS) ? 2.f * kPixelPSZpitch
-                       : (isInSgInnerMDPS || isOutSgInnerMDPS) ? (kPixelPSZpitch + kStrip2SZpitch) : 2.f * kStrip2SZpitch;
-    const float dz = zOut - zIn;
-    const float rtLo = rtIn * (1.f + dz / (zIn + dLum) / dzDrtScale) - rtGeom;
-    if (!(rtOut >= rtLo)) return false;
-    const float rtHi = rtIn * (1.f + dz / (zIn - dLum)) + rtGeom;
-    if (!(rtOut >= rtLo && rtOut <= rtHi)) return false;
-    const float sdlThetaMulsF = (float)((double)0.015f * sqrt((double)0.1f + 0.2 * (double)(rtOut - rtIn) / (double)50.f));
-    const float sdlMuls = sdlThetaMulsF * 3.f / kPtCut * 4.f;
-    const float sdlPVoff = 0.1f / rtOut;
-    const float sdlCut = (float)((double)sdlSlope + sqrt((double)(sdlMuls * sdlMuls + sdlPVoff * sdlPVoff)));
-    if (!(fabsf(dphi(InUp.p, OutUp.p)) <= sdlCut)) return false;
-    const bool isInSgOuterMDPS = InUp.m->type == kPS;
-    const float drtSDIn = InUp.p.rt - InLo.p.rt;
-    const float dzSDIn = InUp.p.z - InLo.p.z;
-    if (isInSgInnerMDPS && isInSgOuterMDPS) {
-        const float dr3SDIn = InUp.p.r3 - InLo.p.r3;
-        const float coshEta = dr3SDIn / drtSDIn;
-        const float dzOutInAbs = fabsf(zOut - zIn);
-        const float multDzDr = dzOutInAbs * coshEta / (coshEta * coshEta - 1.f);
-        const float kZ = (zOut - zIn) / dzSDIn;
-        float drtErr = kPixelPSZpitch * kPixelPSZpitch * 2.f / dzSDIn / dzSDIn * dzOutInAbs * dzOutInAbs;
-        drtErr += sdlMuls * sdlMuls * multDzDr * multDzDr / 3.f * coshEta * coshEta;
-        drtErr = __fsqrt_rn(drtErr);
-        const float drtMean = drtSDIn * dzOutInAbs / fabsf(dzSDIn);
-        const float rtWindow = drtErr + rtGeom;
-        const float rtLo_point = rtIn + drtMean / dzDrtScale - rtWindow;
-        const float rtHi_point = rtIn + drtMean + rtWindow;
-        if (!(kZ >= 0 && rtOut >= rtLo_point && rtOut <= rtHi_point)) return false;
-    }
-    const P3 mid = midpoint(InLo.p, OutLo.p);
-    const float dPhi = dphi(mid, sub(OutLo.p, InLo.p));
-    if (!(fabsf(dPhi) <= sdlCut)) return false;
-    const float sdIn_alpha = S.dphichange;
-    const float sdOut_alpha = S.dphichange;  // (sic)
-    const float sdOut_dPhiPos = dphi(OutLo.p, OutUp.p);
-    const float sdOut_alphaOutRHmin = phi_mpi_pi(T.dphiminchange - sdOut_dPhiPos);
-    const float sdOut_alphaOutRHmax = phi_mpi_pi(T.dphimaxchange - sdOut_dPhiPos);
-    const float sdOut_alphaOut = phi_mpi_pi(T.dphichange - sdOut_dPhiPos);
-    const P3 dr3 = sub(OutUp.p, InLo.p);
-    float betaIn = sdIn_alpha - dphi(InLo.p, dr3);
-    float betaOut = -sdOut_alphaOut + dphi(OutUp.p, dr3);
-    float betaInRHmin = betaIn + S.dphiminchange - sdIn_alpha;
-    float betaInRHmax = betaIn + S.dphimaxchange - sdIn_alpha;
-    if (fabsf(betaInRHmin) > fabsf(betaInRHmax)) { float t = betaInRHmin; betaInRHmin = betaInRHmax; betaInRHmax = t; }
-    float betaOutRHmin = betaOut - sdOut_alphaOutRHmin + sdOut_alphaOut;
-    float betaOutRHmax = betaOut - sdOut_alphaOutRHmax + sdOut_alphaOut;
-    if (fabsf(betaOutRHmin) > fabsf(betaOutRHmax)) { float t = betaOutRHmin; betaOutRHmin = betaOutRHmax; betaOutRHmax = t; }
-    const float sdIn_dr = rt_of_diff(InUp.p, InLo.p);
-    const float sdIn_d = InUp.p.rt - InLo.p.rt;
-    const float dr = dr3.rt;
-    // cut #6 never rejects here (Tracklet.cc:2327-2336)
     float betaAv = 0.5f * (betaIn + betaOut);
-    float pt_beta = (float)((double)(dr * k2Rinv1GeVf) / sin((double)betaAv));
-    const int lIn = 11, lOut = 13;
-    const float sdOut_dr = rt_of_diff(OutUp.p, OutLo.p);
-    const float sdOut_d = OutUp.p.rt - OutLo.p.rt;
+    float pt_beta = (float)((double)(dr * k2Rinv1GeVf) / d_sin((double)betaAv));
     delta_beta_iterations(betaIn, betaOut, betaAv, pt_beta, sdIn_dr, sdOut_dr, dr, lIn, pt_betaMax);
     const float betaInMMSF = (fabsf(betaInRHmin + betaInRHmax) > 0) ? (2.f * betaIn / fabsf(betaInRHmin + betaInRHmax)) : 0.f;
     const float betaOutMMSF = (fabsf(betaOutRHmin + betaOutRHmax) > 0) ? (2.f * betaOut / fabsf(betaOutRHmin + betaOutRHmax)) : 0.f;
     betaInRHmin *= betaInMMSF; betaInRHmax *= betaInMMSF;
     betaOutRHmin *= betaOutMMSF; betaOutRHmax *= betaOutMMSF;
-    const float dBetaMuls = sdlThetaMulsF * 4.f / fmin_ref(fabsf(pt_beta), pt_betaMax);
-    const float alphaInAbsReg = fmax_ref(fabsf(sdIn_alpha), InLo.asin3);
-    const float alphaOutAbsReg = fmax_ref(fabsf(sdOut_alpha), OutLo.asin3);
-    const float dBetaInLum = lIn < 11 ? 0.0f : fabsf(alphaInAbsReg * kDeltaZLum / InLo.p.z);
-    const float dBetaOutLum = lOut < 11 ? 0.0f : fabsf(alphaOutAbsReg * kDeltaZLum / OutLo.p.z);
+    const float dBetaMuls = mulsF * 4.f / fmin_ref(fabsf(pt_beta), pt_betaMax);
+    const float alphaInAbsReg = fmax_ref(fabsf(alphaIn), S.la3);
+    const float alphaOutAbsReg = fmax_ref(fabsf(alphaOutReg), T.la3);
+    const float dBetaInLum = lIn < 11 ? 0.0f : fabsf(alphaInAbsReg * kDeltaZLum / InLo.z);
+    const float dBetaOutLum = lOut < 11 ? 0.0f : fabsf(alphaOutAbsReg * kDeltaZLum / OutLo.z);
     const float dBetaLum2 = (dBetaInLum + dBetaOutLum) * (dBetaInLum + dBetaOutLum);
-    const float betaOut_cut = (float)((double)(f_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d)) + sqrt((double)(dBetaLum2 + dBetaMuls * dBetaMuls)));
+    const float betaOut_cut = add_dsqrt(f_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d),
+                                        dBetaLum2 + dBetaMuls * dBetaMuls);
     if (!(fabsf(betaOut) < betaOut_cut)) return false;
     const float dBetaRes = 0.02f / fmin_ref(sdOut_d, sdIn_d);
-    const float dBetaCut2 = dbeta_cut2(dBetaRes, dBetaMuls, dBetaLum2, 0.f, betaInRHmin, betaInRHmax, betaOutRHmin, betaOutRHmax);
+    const float dBetaCut2 = dbeta_cut2(dBetaRes, dBetaMuls, dBetaLum2, dBetaROut2, betaInRHmin, betaInRHmax, betaOutRHmin, betaOutRHmax);
     const float dBeta = betaIn - betaOut;
     return (dBeta * dBeta <= dBetaCut2) || nm1;
-}
-
-// Tracklet.cc:144-296
-__device__ __forceinline__ bool tl_dispatch(const SGView& S, const SGView& T, bool nm1) {
-    const bool b1 = S.lo.m->subdet == kBarrel, b2 = S.up.m->subdet == kBarrel;
-    const bool b3 = T.lo.m->subdet == kBarrel, b4 = T.up.m->subdet == kBarrel;
-    const bool e1 = S.lo.m->subdet == kEndcap, e2 = S.up.m->subdet == kEndcap;
-    const bool e3 = T.lo.m->subdet == kEndcap, e4 = T.up.m->subdet == kEndcap;
-    if (b1 && b2 && b3 && (b4 || e4)) return tl_bbbb(S, T, nm1);
-    if (b1 && ((b2 && e3) || (e2 && e3)) && e4) return tl_bbee(S, T, nm1);
-    if (e1 && e2 && e3 && e4) return tl_eeee(S, T, nm1);
-    return false;
 }
 
 }  // namespace sdlg

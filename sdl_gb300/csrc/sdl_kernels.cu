@@ -278,32 +278,6 @@ __device__ __forceinline__ MDView md_view(const BatchDev& b, int a) {
     return v;
 }
 
-__device__ __forceinline__ AnchorView anchor_view(const BatchDev& b, int64_t k) {
-    AnchorView a;
-    a.p = hit(b, k);
-    a.asin1 = AT(b.ha1, k, H(b));
-    a.tand1 = AT(b.htd, k, H(b));
-    a.asin3 = AT(b.ha3, k, H(b));
-    a.m = &MOD(b, AT(b.hgm, k, H(b)) % b.geo.n_mod);
-    return a;
-}
-
-__device__ __forceinline__ SGView sg_view(const BatchDev& b, int s) {
-    SGView v;
-    const int im = OI(b, kSG, s), om = OJ(b, kSG, s);
-    const ModDev& ilm = MOD(b, OG(b, kMD, im) % b.geo.n_mod);
-    const ModDev& olm = MOD(b, OG(b, kMD, om) % b.geo.n_mod);
-    v.lo = anchor_view(b, md_anchor(ilm, OI(b, kMD, im), OJ(b, kMD, im)));
-    v.up = anchor_view(b, md_anchor(olm, OI(b, kMD, om), OJ(b, kMD, om)));
-    v.dphi = OF(b, kSG, 0, s);
-    v.dphimin = OF(b, kSG, 1, s);
-    v.dphimax = OF(b, kSG, 2, s);
-    v.dphichange = OF(b, kSG, 3, s);
-    v.dphiminchange = OF(b, kSG, 4, s);
-    v.dphimaxchange = OF(b, kSG, 5, s);
-    return v;
-}
-
 // ------------------------------------------------------------------ stage functors
 struct MDStage {
     static constexpr int kSt = kMD;
@@ -383,24 +357,16 @@ struct SGStage {
     __device__ static int group_of(const BatchDev& b, int a) { return OG(b, kMD, a); }
 };
 
-struct TLStage {
-    static constexpr int kSt = kTL;
-    __device__ static bool eval(const BatchDev& b, int s, int64_t q, int& oi, int& oj, float* fv) {
-        const int n_mod = b.geo.n_mod;
-        const int g2 = OG(b, kMD, OJ(b, kSG, s));
-        const int ev = g2 / n_mod, m2 = g2 - ev * n_mod;
-        int pref;
-        const int k = conn_entry(b, ev, m2, q, pref);
-        const int g3 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
-        const int t = (int)(OFF(b, kSG, g3) + (q - pref));
-        const SGView A = sg_view(b, s);
-        const SGView B = sg_view(b, t);
-        oi = s; oj = t;
-        (void)fv;
-        return tl_dispatch(A, B, (b.flags & 4) != 0);
-    }
-    __device__ static int group_of(const BatchDev& b, int s) { return OG(b, kSG, s); }
-};
+// tracklet candidate q of inner segment s -> outer segment (Event.cc:635-663)
+__device__ __forceinline__ int tl_outer(const BatchDev& b, int s, int64_t q) {
+    const int n_mod = b.geo.n_mod;
+    const int g2 = OG(b, kMD, OJ(b, kSG, s));
+    const int ev = g2 / n_mod, m2 = g2 - ev * n_mod;
+    int pref;
+    const int k = conn_entry(b, ev, m2, q, pref);
+    const int g3 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
+    return (int)(OFF(b, kSG, g3) + (q - pref));
+}
 
 struct TPStage {
     static constexpr int kSt = kTP;
@@ -502,6 +468,163 @@ __global__ void __launch_bounds__(kEnumThreads) k_enum(BatchDev b) {
                 }
             }
         }
+    }
+}
+
+// warp-aggregated append of a survivor of stage st (inner object i, outer j)
+__device__ __forceinline__ void append_rec(const BatchDev& b, int st, bool pass, int oi, int oj, int g, const float* fv) {
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(0xffffffffu, pass);
+    if (!m) return;
+    const Recs& R = b.rec[st];
+    const Objs& O = b.obj[st];
+    const int leader = __ffs(m) - 1;
+    unsigned long long p0 = 0;
+    if (lane == leader) p0 = atomicAdd((unsigned long long*)(b.n_rec + st), (unsigned long long)__popc(m));
+    p0 = __shfl_sync(0xffffffffu, p0, leader);
+    if (!pass) return;
+    const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));
+    if (pos < O.cap) {
+        AT(R.i, pos, O.cap) = oi;
+        AT(R.j, pos, O.cap) = oj;
+        AT(R.g, pos, O.cap) = g;
+        AT(R.rank, pos, O.cap) = (int)atomicAdd((unsigned long long*)&AT(O.mod_cnt, g, NG1(b)), 1ull);
+        for (int k = 0; k < R.nf; ++k) AT(R.f, (int64_t)k * O.cap + pos, O.cap * R.nf) = fv[k];
+    } else {
+        atomicOr(b.status, 1u << st);
+    }
+}
+
+// One packed record per segment for the tracklet stage (the anchors of both
+// mini-doublets, the segment's angles and the per-segment sub-expressions of
+// Tracklet.cc that depend on one segment only).
+__global__ void k_sg_pack(BatchDev b) {
+    if (halted(b)) return;
+    const int n_mod = b.geo.n_mod;
+    const int64_t n = n_inner(b, kTL);
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        const int im = OI(b, kSG, s), om = OJ(b, kSG, s);
+        const ModDev& ilm = MOD(b, OG(b, kMD, im) % n_mod);
+        const ModDev& olm = MOD(b, OG(b, kMD, om) % n_mod);
+        const int la = md_anchor(ilm, OI(b, kMD, im), OJ(b, kMD, im));
+        const int ua = md_anchor(olm, OI(b, kMD, om), OJ(b, kMD, om));
+        const P3 lo = hit(b, la), up = hit(b, ua);
+        const ModDev& lam = MOD(b, AT(b.hgm, la, H(b)) % n_mod);
+        const ModDev& uam = MOD(b, AT(b.hgm, ua, H(b)) % n_mod);
+        uint32_t fl = 0;
+        fl |= lam.subdet == kBarrel ? F_LO_B : 0u;
+        fl |= lam.subdet == kEndcap ? F_LO_E : 0u;
+        fl |= lam.type == kPS ? F_LO_PS : 0u;
+        fl |= uam.subdet == kBarrel ? F_UP_B : 0u;
+        fl |= uam.subdet == kEndcap ? F_UP_E : 0u;
+        fl |= uam.type == kPS ? F_UP_PS : 0u;
+        fl |= uam.type == kTwoS ? F_UP_2S : 0u;
+        float v[PK_N];
+        v[PK_LX] = lo.x; v[PK_LY] = lo.y; v[PK_LZ] = lo.z; v[PK_LRT] = lo.rt;
+        v[PK_LPHI] = lo.phi; v[PK_LR3] = lo.r3; v[PK_LA1] = AT(b.ha1, la, H(b)); v[PK_LTD] = AT(b.htd, la, H(b));
+        v[PK_LA3] = AT(b.ha3, la, H(b));
+        v[PK_LR3Z] = __fsqrt_rn(lo.z * lo.z + lo.rt * lo.rt);
+        v[PK_UX] = up.x; v[PK_UY] = up.y; v[PK_UZ] = up.z; v[PK_URT] = up.rt; v[PK_UPHI] = up.phi; v[PK_UR3] = up.r3;
+        v[PK_DPC] = OF(b, kSG, 3, s); v[PK_DPMIN] = OF(b, kSG, 1, s); v[PK_DPMAX] = OF(b, kSG, 2, s);
+        v[PK_DPMINC] = OF(b, kSG, 4, s); v[PK_DPMAXC] = OF(b, kSG, 5, s);
+        v[PK_RTSEG] = rt_of_diff(up, lo);
+        v[PK_ALPHAUP] = dphi(up, sub(up, lo));
+        v[PK_DPHILU] = dphi(lo, up);
+        v[PK_EX] = uam.edge_x; v[PK_EY] = uam.edge_y;
+        v[PK_FLAGS] = __uint_as_float(fl);
+        v[PK_G2] = __int_as_float(OG(b, kMD, om));
+        v[PK_S0] = v[PK_S1] = v[PK_S2] = v[PK_S3] = 0.f;
+        float4* dst = reinterpret_cast<float4*>(&AT(b.sgpack, s * PK_N, b.obj[kSG].cap * PK_N));
+        for (int k = 0; k < PK_N / 4; ++k) dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    }
+}
+
+constexpr int kTLQueue = 64;  // per-warp queue of candidates that passed phase A
+
+// Tracklet candidates (Event.cc:611-693 with Tracklet.cc:144-2665).  Phase A
+// (float cuts) runs on every candidate; its survivors go to a per-warp queue
+// in shared memory and phase B (the double-precision part) runs on full warps
+// of queued candidates.
+__global__ void __launch_bounds__(kEnumThreads) k_tl_enum(BatchDev b) {
+    if (halted(b)) return;
+    const int64_t nobj = n_inner(b, kTL);
+    if (nobj <= 0) return;
+    const int64_t* off = b.cand[kTL];
+    const int64_t offlim = b.cand_cap[kTL] + 1;
+    const int64_t total = AT(off, nobj, offlim);
+    const int64_t ntask = (total + kTask - 1) / kTask;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const bool nm1 = (b.flags & 4) != 0;
+    __shared__ int qs[kEnumThreads / 32][kTLQueue];
+    __shared__ int qt[kEnumThreads / 32][kTLQueue];
+    __shared__ float qc[kEnumThreads / 32][kTLQueue];
+    __shared__ float qm[kEnumThreads / 32][kTLQueue];
+    __shared__ int qa[kEnumThreads / 32][kTLQueue];
+    int qn = 0;  // warp-uniform queue length
+    bool more = true;
+    while (more || qn > 0) {
+        if (more) {
+            unsigned long long t = 0;
+            if (lane == 0) t = atomicAdd(b.task + kTL, 1ull);
+            t = __shfl_sync(0xffffffffu, t, 0);
+            if ((int64_t)t >= ntask) {
+                more = false;
+            } else {
+                const int64_t base = (int64_t)t * kTask;
+                const int64_t end = min(base + kTask, total);
+                int ilo = 0;
+                if (lane < 2) ilo = find_obj(b, off, offlim, 0, (int)nobj - 1, lane == 0 ? base : end - 1);
+                const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
+                const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
+                for (int r = 0; r < kTask / kWarp; ++r) {
+                    const int64_t c = base + r * kWarp + lane;
+                    int algo = kAlgoNone, s = 0, tt = 0;
+                    float cut = 0.f, muls = 0.f;
+                    if (c < end) {
+                        s = (i0 == i1) ? i0 : find_obj(b, off, offlim, i0, i1, c);
+                        tt = tl_outer(b, s, c - AT(off, s, offlim));
+                        (void)IX(s, b.obj[kSG].cap);
+                        (void)IX(tt, b.obj[kSG].cap);
+                        const SGV S = load_sgv(b.sgpack, s);
+                        const SGV T = load_sgv(b.sgpack, tt);
+                        algo = tl_phaseA(S, T, cut, muls);
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, algo != kAlgoNone);
+                    if (algo != kAlgoNone) {
+                        const int p = qn + __popc(m & ((1u << lane) - 1u));
+                        qs[w][p] = s; qt[w][p] = tt; qc[w][p] = cut; qm[w][p] = muls; qa[w][p] = algo;
+                    }
+                    qn += __popc(m);
+                    __syncwarp();
+                    if (qn >= kWarp) {
+                        // phase B on the last 32 queued candidates
+                        const int k = qn - kWarp + lane;
+                        const int qs_ = qs[w][k], qt_ = qt[w][k], qa_ = qa[w][k];
+                        const float qc_ = qc[w][k], qm_ = qm[w][k];
+                        __syncwarp();
+                        qn -= kWarp;
+                        const SGV S = load_sgv(b.sgpack, qs_);
+                        const SGV T = load_sgv(b.sgpack, qt_);
+                        const bool pass = tl_phaseB(qa_, S, T, qc_, qm_, nm1);
+                        append_rec(b, kTL, pass, qs_, qt_, OG(b, kSG, qs_), nullptr);
+                    }
+                }
+                continue;
+            }
+        }
+        // drain: fewer than 32 queued candidates left
+        bool pass = false;
+        int qs_ = 0, qt_ = 0;
+        if (lane < qn) {
+            qs_ = qs[w][lane];
+            qt_ = qt[w][lane];
+            const SGV S = load_sgv(b.sgpack, qs_);
+            const SGV T = load_sgv(b.sgpack, qt_);
+            pass = tl_phaseB(qa[w][lane], S, T, qc[w][lane], qm[w][lane], nm1);
+        }
+        __syncwarp();
+        append_rec(b, kTL, pass, qs_, qt_, pass ? OG(b, kSG, qs_) : 0, nullptr);
+        qn = 0;
     }
 }
 
@@ -761,10 +884,18 @@ void launch_sg(const BatchDev& b, cudaStream_t s, Hooks* h) {
 void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     // conn sums over segment counts serve the tracklet enumeration and the
     // triplet candidate counters (Event.cc:547-596 loops over the same lists)
+    k_sg_pack<<<b.n_sm * 8, 256, 0, s>>>(b);
     k_conn_sum<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kSG, kTP);
     k_tl_count<<<b.n_sm * 8, 256, 0, s>>>(b);
-    if (h) h->launches += 2;
-    enum_and_group<TLStage>(b, s, h);
+    if (h) h->launches += 3;
+    scan_h(b, b.cand[kTL], b.obj[kSG].mod_cnt + b.n_gm, b.cand_cap[kTL], s, h);
+    if (h && h->timed) rec_event(h->enum_start[kTL], s);
+    k_tl_enum<<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
+    if (h && h->timed) rec_event(h->enum_stop[kTL], s);
+    k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kTL);
+    scan_h(b, b.obj[kTL].mod_cnt, b.n_gm_dev, b.n_gm, s, h);
+    k_scatter<<<b.n_sm * 8, 256, 0, s>>>(b, kTL);
+    if (h) h->launches += 3;
 }
 
 void launch_tp(const BatchDev& b, cudaStream_t s, Hooks* h) {

@@ -35,6 +35,7 @@ struct BatchDev {
     // connection-list prefix sums of per-module object counts
     int32_t* conn_pref;            // n_ev * n_conn
     int64_t* conn_sum;             // n_gm
+    float* sgpack;                 // segment cap * PK_N packed records for the tracklet stage
     uint32_t* counters;            // n_ev * 110
     uint32_t* status;
     unsigned long long* task;      // kNumStages work counters
