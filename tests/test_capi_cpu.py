@@ -32,3 +32,27 @@ def test_create_without_device_reports_error():
         L.sdlg_destroy(h)
     else:
         assert rc in (-9, -2)
+
+
+def build_cpp_demo(tmpdir):
+    """Compiles tests/cpp_event_api.cc against include/sdl_event.hpp and the library."""
+    import subprocess
+    from sdl_gb300 import build
+    lib = build.build()
+    exe = os.path.join(str(tmpdir), "cpp_event_api")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp_event_api.cc"), "-o", exe, lib,
+                    "-Wl,-rpath," + os.path.dirname(lib)], check=True)
+    return exe
+
+
+def test_cpp_event_api_builds_and_reports_missing_device(tmp_path):
+    import subprocess
+    from sdl_gb300 import synth
+    exe = build_cpp_demo(tmp_path)
+    det, ev = synth.workload_event("barrel_flat", 0)
+    paths = det.write_files(str(tmp_path))
+    hb = os.path.join(str(tmp_path), "hits.bin")
+    ev.write_bin(hb)
+    r = subprocess.run([exe, *paths, hb], capture_output=True, text=True)
+    assert r.returncode in (0, 3), r.stderr

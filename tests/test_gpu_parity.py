@@ -129,3 +129,21 @@ def test_unknown_module_extends_table(gpu, oracle_lib):
     ref, _, _ = oracle_lib.Oracle(det).run(cat)
     for s in range(5):
         assert oracle_lib.digest(gpu.objects(s, 0)) == oracle_lib.digest(ref[s])
+
+
+def test_cpp_event_api_matches_golden(tmp_path, oracle_lib):
+    """The reference's call sequence through include/sdl_event.hpp."""
+    import os
+    import subprocess
+    from conftest import ROOT
+    from test_capi_cpu import build_cpp_demo
+    meta = golden_meta("flat_s0")
+    det, ev = regenerate(meta)
+    exe = build_cpp_demo(tmp_path)
+    paths = det.write_files(str(tmp_path))
+    hb = os.path.join(str(tmp_path), "hits.bin")
+    ev.write_bin(hb)
+    r = subprocess.run([exe, *paths, hb], capture_output=True, text=True, check=True)
+    nums = [int(v) for v in r.stdout.split("\n")[0].split()]
+    assert nums[0] == len(ev)
+    assert nums[1:] == meta["counts"]
