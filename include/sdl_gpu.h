@@ -123,6 +123,34 @@ int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5);
 /* Number of kernels one run of the chain launches (as last enqueued). */
 int64_t sdlg_last_launches(const sdlg_ctx* ctx);
 
+/* Mini-doublets of one event with no device allocation (no counterpart in
+ * the reference, whose only interface is the host class library).  It is for
+ * callers that may not allocate device memory while they process events:
+ * frameworks that hand out all device memory from their own pool at start-up,
+ * code whose stream is being captured into a CUDA graph, plugins whose host
+ * owns the allocator.  Inputs (n_hits hits: x, y, z, idx, detid) and outputs
+ * are the caller's DEVICE buffers; the stage's working memory is a fixed
+ * array inside the library (about 17 MiB, held on every GPU that loads the
+ * library until the process exits).  Results: d_pairs receives up to
+ * pair_cap (lower idx, upper idx) pairs, *d_count the number of
+ * mini-doublets (or, if the array's capacity overflowed, the number needed)
+ * and *d_status the device status word (0 = clean; bit 0 = more than
+ * SDLG_STATIC_MAX_MINI_DOUBLETS mini-doublets, nothing written; bit 8 = hits
+ * in modules the geometry does not list, which are skipped).  Asynchronous on
+ * `stream` (NULL: the context's stream); the geometry must be loaded.
+ * Limits: n_hits <= SDLG_STATIC_MAX_HITS and at most SDLG_STATIC_MAX_MODULES
+ * modules, else SDLG_ERR_CAPACITY.  The first call on a device looks up the
+ * array's device address; make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (different
+ * streams, contexts or threads without ordering) race and corrupt each
+ * other's results. */
+#define SDLG_STATIC_MAX_HITS 131072
+#define SDLG_STATIC_MAX_MODULES 65536
+#define SDLG_STATIC_MAX_MINI_DOUBLETS 131072
+int sdlg_mini_doublets_static(sdlg_ctx* ctx, int64_t n_hits, const float* d_x, const float* d_y, const float* d_z,
+                              const int32_t* d_idx, const uint32_t* d_detid, int32_t* d_pairs, int64_t pair_cap,
+                              int64_t* d_count, uint32_t* d_status, void* stream);
+
 /* Pinned host memory for zero-staging transfers. */
 int sdlg_host_alloc(sdlg_ctx* ctx, int64_t bytes, void** out);
 int sdlg_host_free(sdlg_ctx* ctx, void* p);

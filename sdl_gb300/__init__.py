@@ -65,6 +65,7 @@ def lib():
         L.sdlg_last_kernel_times.argtypes = [vp, vp]
         L.sdlg_last_launches.argtypes = [vp]
         L.sdlg_last_launches.restype = i64
+        L.sdlg_mini_doublets_static.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
         L.sdlg_host_alloc.argtypes = [vp, i64, ctypes.POINTER(vp)]
         L.sdlg_host_free.argtypes = [vp, vp]
         _LIB = L
@@ -191,6 +192,14 @@ class Chain:
     def launches(self) -> int:
         """Kernels one run of the chain launches."""
         return int(lib().sdlg_last_launches(self.h))
+
+    def mini_doublets_static(self, n_hits, d_x, d_y, d_z, d_idx, d_detid, d_pairs, pair_cap, d_count, d_status,
+                             stream=None):
+        """Allocation-free mini-doublets of one event (device pointers in and
+        out, working memory in the library's fixed array); see
+        sdlg_mini_doublets_static in include/sdl_gpu.h."""
+        self._ck(lib().sdlg_mini_doublets_static(self.h, n_hits, d_x, d_y, d_z, d_idx, d_detid, d_pairs, pair_cap,
+                                                 d_count, d_status, stream))
 
     def times(self) -> np.ndarray:
         """Device ms of the last run: ingest, MD, SG, TL, TP, TC, total."""

@@ -773,6 +773,30 @@ int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5) {
 
 int64_t sdlg_last_launches(const sdlg_ctx* ctx) { return ctx ? ctx->launches_per_run : -1; }
 
+}  // extern "C"
+
+// read-only views of a context for sdl_static.cu
+namespace sdlg {
+bool ctx_geometry(const sdlg_ctx* ctx, Geometry* g, int* device, int* n_sm) {
+    if (!ctx || !ctx->have_geo) return false;
+    g->n_mod = (int)ctx->detids.size();
+    g->n_conn = (int)ctx->conn_idx.size();
+    g->detid = ctx->d_detid;
+    g->mod = ctx->d_mod;
+    g->conn_off = ctx->d_conn_off;
+    g->conn_idx = ctx->d_conn_idx;
+    *device = ctx->device;
+    *n_sm = ctx->n_sm;
+    return true;
+}
+void* ctx_stream(const sdlg_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+void ctx_set_error(sdlg_ctx* ctx, const char* msg) {
+    if (ctx) ctx->err = msg;
+}
+}  // namespace sdlg
+
+extern "C" {
+
 int sdlg_host_alloc(sdlg_ctx* ctx, int64_t bytes, void** out) {
     if (!ctx || !out || bytes <= 0) return SDLG_ERR_ARG;
     cudaSetDevice(ctx->device);
