@@ -344,7 +344,7 @@ def main():
         traffic = int(alg_bytes * float(tr["traffic_per_algorithmic_byte"]))
     roofline = {"bound": "hbm", "achieved": round(achieved, 3), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 6), "traffic": traffic, "peak_source": src,
-                "kernel": "k_enum<TLStage> (tracklet cuts)", "kernel_ms": round(tl_mean, 4),
+                "kernel": "k_tl_enum (tracklet cuts)", "kernel_ms": round(tl_mean, 4),
                 "algorithmic_bytes": alg_bytes,
                 "note": "latency/FP64-bound candidate evaluation; HBM bytes are small by construction"}
 

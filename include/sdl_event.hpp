@@ -95,10 +95,26 @@ class Event {
 
     // Event.cc:245-305, 445-522, 611-693, 524-597, 823-872
     void createMiniDoublets(MDAlgo algo = Default_MDAlgo) { require(algo == Default_MDAlgo); run(SDLG_STAGE_MD); }
-    void createSegmentsWithModuleMap(SGAlgo algo = Default_SGAlgo) { require(algo == Default_SGAlgo); run(SDLG_STAGE_SG); }
+    void createSegmentsWithModuleMap(SGAlgo algo = Default_SGAlgo) {
+        require(algo == Default_SGAlgo);
+        sg_flags_ = 0;
+        run(SDLG_STAGE_SG);
+    }
+    // Event.cc:432-443: segments from the layer pairs of Layer.cc:32-50
+    void createSegments(SGAlgo algo = Default_SGAlgo) {
+        require(algo == Default_SGAlgo);
+        sg_flags_ = SDLG_FLAG_SG_LAYERS;
+        run(SDLG_STAGE_SG);
+    }
     void createTrackletsWithModuleMap(TLAlgo algo = Default_TLAlgo) {
         require(algo == Default_TLAlgo || algo == DefaultNm1_TLAlgo);
-        flags_ = algo == DefaultNm1_TLAlgo ? SDLG_FLAG_TL_NM1 : 0;
+        tl_flags_ = algo == DefaultNm1_TLAlgo ? SDLG_FLAG_TL_NM1 : 0;
+        run(SDLG_STAGE_TL);
+    }
+    // Event.cc:599-609: tracklets from the layer pairs of Layer.cc:3-30
+    void createTracklets(TLAlgo algo = Default_TLAlgo) {
+        require(algo == Default_TLAlgo || algo == DefaultNm1_TLAlgo);
+        tl_flags_ = SDLG_FLAG_TL_LAYERS | (algo == DefaultNm1_TLAlgo ? SDLG_FLAG_TL_NM1 : 0);
         run(SDLG_STAGE_TL);
     }
     void createTriplets(TPAlgo algo = Default_TPAlgo) { require(algo == Default_TPAlgo); run(SDLG_STAGE_TP); }
@@ -161,7 +177,8 @@ class Event {
             check(sdlg_set_events(ctx_, 1, off, x_.data(), y_.data(), z_.data(), idx_.data(), det_.data()), "set_events");
             dirty_ = false;
         }
-        check(sdlg_run(ctx_, stage, flags_), "run");
+        // each call re-runs the chain up to `stage` with the variants chosen so far
+        check(sdlg_run(ctx_, stage, sg_flags_ | tl_flags_), "run");
         ran_ = stage;
         stage_ = stage;
     }
@@ -193,7 +210,7 @@ class Event {
     std::vector<int32_t> idx_;
     std::vector<uint32_t> det_;
     bool dirty_ = false;
-    int flags_ = 0;
+    int sg_flags_ = 0, tl_flags_ = 0;
     int ran_ = -1;
     int stage_ = -1;
 };

@@ -50,6 +50,10 @@ extern "C" {
 #define SDLG_STAGE_TC 4
 
 /* run flags */
+#define SDLG_FLAG_SG_LAYERS 1 /* segments by layer pairs: Event::createSegments (Event.cc:432-443,793-821;
+                                 pair table Layer.cc:32-50) instead of createSegmentsWithModuleMap */
+#define SDLG_FLAG_TL_LAYERS 2 /* tracklets by layer pairs: Event::createTracklets (Event.cc:599-609,755-790;
+                                 pair table Layer.cc:3-30) instead of createTrackletsWithModuleMap */
 #define SDLG_FLAG_TL_NM1 4   /* tracklets with DefaultNm1_TLAlgo (Algo.h:23-28) */
 #define SDLG_FLAG_NO_GRAPH 8 /* launch stage by stage instead of replaying a CUDA graph */
 
@@ -92,7 +96,12 @@ int sdlg_set_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, cons
  * createTrackletsWithModuleMap -> createTriplets -> createTrackCandidates
  * (Event.cc:245-305, 445-522, 611-693, 524-597, 823-872) on every event of
  * the batch, up to and including stage `stop_after`.  Synchronous: returns
- * when the results are on the device.  Object capacities grow automatically. */
+ * when the results are on the device.  Object capacities grow automatically.
+ * `flags` selects the variants: SDLG_FLAG_SG_LAYERS / SDLG_FLAG_TL_LAYERS
+ * replace the module-map segment / tracklet steps by the layer-pair ones
+ * (createSegments / createTracklets; these count no segment candidates or
+ * segments in the per-layer counters, as in the reference), SDLG_FLAG_TL_NM1
+ * selects DefaultNm1_TLAlgo, SDLG_FLAG_NO_GRAPH launches without a graph. */
 int sdlg_run(sdlg_ctx* ctx, int stop_after, int flags);
 
 /* Enqueue the same chain on the context stream without waiting (for callers

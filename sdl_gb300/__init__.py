@@ -27,6 +27,8 @@ LIB_PATH = os.path.join(HERE, "libsdlgpu.so")
 
 STAGES = ("MD", "SG", "TL", "TP", "TC")
 WIDTH = (2, 4, 8, 8, 16)
+FLAG_SG_LAYERS = 1   # Event::createSegments (layer pairs) instead of createSegmentsWithModuleMap
+FLAG_TL_LAYERS = 2   # Event::createTracklets (layer pairs) instead of createTrackletsWithModuleMap
 FLAG_TL_NM1 = 4
 FLAG_NO_GRAPH = 8
 

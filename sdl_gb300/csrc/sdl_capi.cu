@@ -105,6 +105,8 @@ struct sdlg_ctx {
     ModDev* d_mod = nullptr;
     int32_t* d_conn_off = nullptr;
     int32_t* d_conn_idx = nullptr;
+    std::vector<int32_t> slot_run;
+    int32_t* d_slot_run = nullptr;
     // batch
     int64_t n_ev = 0, n_hit = 0;
     std::vector<int64_t> ev_off;
@@ -232,10 +234,22 @@ int build_module_table(sdlg_ctx* ctx, const std::vector<uint32_t>& extra) {
             }
         ctx->conn_off[i + 1] = (int32_t)ctx->conn_idx.size();
     }
+    // layers as runs of consecutive module indices (Layer.cc:3-50 pairs layers)
+    std::vector<std::vector<int32_t>> runs(kNumSlots);
+    for (int i = 0; i < n; ++i) {
+        auto& r = runs[ctx->mods[i].layer_slot];
+        if (!r.empty() && r.back() == i) r.back() = i + 1;
+        else { r.push_back(i); r.push_back(i + 1); }
+    }
+    ctx->slot_run.assign(kNumSlots + 1, 0);
+    for (int sl = 0; sl < kNumSlots; ++sl) ctx->slot_run[sl + 1] = ctx->slot_run[sl] + (int32_t)runs[sl].size() / 2;
+    for (int sl = 0; sl < kNumSlots; ++sl) ctx->slot_run.insert(ctx->slot_run.end(), runs[sl].begin(), runs[sl].end());
     // upload
     free_batch(ctx);
     cudaFree(ctx->d_detid); cudaFree(ctx->d_mod); cudaFree(ctx->d_conn_off); cudaFree(ctx->d_conn_idx);
+    cudaFree(ctx->d_slot_run);
     ctx->d_detid = nullptr; ctx->d_mod = nullptr; ctx->d_conn_off = nullptr; ctx->d_conn_idx = nullptr;
+    ctx->d_slot_run = nullptr;
     CK(cudaMalloc(&ctx->d_detid, std::max(1, n) * sizeof(uint32_t)));
     CK(cudaMalloc(&ctx->d_mod, std::max(1, n) * sizeof(ModDev)));
     CK(cudaMalloc(&ctx->d_conn_off, (n + 1) * sizeof(int32_t)));
@@ -245,6 +259,8 @@ int build_module_table(sdlg_ctx* ctx, const std::vector<uint32_t>& extra) {
     CK(cudaMemcpy(ctx->d_conn_off, ctx->conn_off.data(), (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice));
     if (!ctx->conn_idx.empty())
         CK(cudaMemcpy(ctx->d_conn_idx, ctx->conn_idx.data(), ctx->conn_idx.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&ctx->d_slot_run, ctx->slot_run.size() * sizeof(int32_t)));
+    CK(cudaMemcpy(ctx->d_slot_run, ctx->slot_run.data(), ctx->slot_run.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
     ctx->have_geo = true;
     return SDLG_OK;
 }
@@ -268,6 +284,8 @@ int ensure_buffers(sdlg_ctx* ctx) {
     b.geo.mod = ctx->d_mod;
     b.geo.conn_off = ctx->d_conn_off;
     b.geo.conn_idx = ctx->d_conn_idx;
+    b.geo.slot_run = ctx->d_slot_run;
+    b.geo.n_slot_run = (int)ctx->slot_run.size();
     b.n_ev = (int)ctx->n_ev;
     b.n_gm = (int)n_gm;
     b.n_hit_cap = H;
@@ -559,6 +577,7 @@ int sdlg_destroy(sdlg_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_batch(ctx);
     cudaFree(ctx->d_detid); cudaFree(ctx->d_mod); cudaFree(ctx->d_conn_off); cudaFree(ctx->d_conn_idx);
+    cudaFree(ctx->d_slot_run);
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     for (int k = 0; k < 8; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
@@ -785,6 +804,8 @@ bool ctx_geometry(const sdlg_ctx* ctx, Geometry* g, int* device, int* n_sm) {
     g->mod = ctx->d_mod;
     g->conn_off = ctx->d_conn_off;
     g->conn_idx = ctx->d_conn_idx;
+    g->slot_run = ctx->d_slot_run;
+    g->n_slot_run = (int)ctx->slot_run.size();
     *device = ctx->device;
     *n_sm = ctx->n_sm;
     return true;

@@ -321,6 +321,36 @@ __device__ __forceinline__ int conn_entry(const BatchDev& b, int ev, int m, int6
     return lo;
 }
 
+// segment algorithm on inner MD a and outer MD bmd (Segment.cc:337-859);
+// `connected`: the outer MD's module is in the inner module's connection list
+// (the endcap algorithm's first requirement, Segment.cc:613-633)
+__device__ __forceinline__ bool sg_pair(const BatchDev& b, int a, int bmd, bool connected, float* fv) {
+    const int n_mod = b.geo.n_mod;
+    const MDView im = md_view(b, a);
+    const MDView om = md_view(b, bmd);
+    const int oanc = md_anchor(*om.m, OI(b, kMD, bmd), OJ(b, kMD, bmd));
+    SGVals v;
+    v.dphi = v.dphimin = v.dphimax = v.dphichange = v.dphiminchange = v.dphimaxchange = 0.f;
+    bool pass;
+    const bool ob = om.m->subdet == kBarrel;
+    if (ob) {
+        pass = sg_barrel(im, om, AT(b.ha1, oanc, H(b)), AT(b.htf, oanc, H(b)), v);
+    } else {
+        P3 oHi = om.a, oLo = om.a;
+        if (om.m->type == kTwoS && om.m->subdet == kEndcap) {
+            const ModDev& am = MOD(b, AT(b.hgm, oanc, H(b)) % n_mod);
+            oHi = strip_edge(om.a, am, true);
+            oLo = strip_edge(om.a, am, false);
+        }
+        pass = sg_endcap(im, om, AT(b.ha1, oanc, H(b)), AT(b.htf, oanc, H(b)), connected, oHi, oLo, v);
+    }
+    fv[0] = v.dphi; fv[1] = v.dphimin; fv[2] = v.dphimax;
+    fv[3] = v.dphichange; fv[4] = v.dphiminchange; fv[5] = v.dphimaxchange;
+    return pass;
+}
+
+// segment candidates along the module map (Event.cc:445-522): candidate q of
+// inner MD a is an MD of a connected module, in connection-list order
 struct SGStage {
     static constexpr int kSt = kSG;
     __device__ static bool eval(const BatchDev& b, int a, int64_t q, int& oi, int& oj, float* fv) {
@@ -331,28 +361,87 @@ struct SGStage {
         const int k = conn_entry(b, ev, m1, q, pref);
         const int g2 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
         const int bmd = (int)(OFF(b, kMD, g2) + (q - pref));
-        const MDView im = md_view(b, a);
-        const MDView om = md_view(b, bmd);
-        const int oanc = md_anchor(*om.m, OI(b, kMD, bmd), OJ(b, kMD, bmd));
-        SGVals v;
-        v.dphi = v.dphimin = v.dphimax = v.dphichange = v.dphiminchange = v.dphimaxchange = 0.f;
-        bool pass;
-        const bool ob = om.m->subdet == kBarrel;
-        if (ob) {
-            pass = sg_barrel(im, om, AT(b.ha1, oanc, H(b)), AT(b.htf, oanc, H(b)), v);
-        } else {
-            P3 oHi = om.a, oLo = om.a;
-            if (om.m->type == kTwoS && om.m->subdet == kEndcap) {
-                const ModDev& am = MOD(b, AT(b.hgm, oanc, H(b)) % n_mod);
-                oHi = strip_edge(om.a, am, true);
-                oLo = strip_edge(om.a, am, false);
+        oi = a; oj = bmd;
+        return sg_pair(b, a, bmd, true, fv);
+    }
+    __device__ static int group_of(const BatchDev& b, int a) { return OG(b, kMD, a); }
+};
+
+// ------------------------------------------------------------------ layer pairs
+// Layer.cc:32-50: the outer layer slots paired with inner slot si (barrel
+// layers 1-5 -> the next barrel layer and endcap layer 1; endcap 1 -> 2;
+// endcap 2 -> 3, 4, 5; endcap 3 -> 4; endcap 4 -> 5); -1 past the last
+__device__ __forceinline__ int sg_layer_outer(int si, int k) {
+    if (si <= 4) return k == 0 ? si + 1 : (k == 1 ? 6 : -1);
+    if (si == 6) return k == 0 ? 7 : -1;
+    if (si == 7) return k < 3 ? 8 + k : -1;
+    if (si == 8 || si == 9) return k == 0 ? si + 1 : -1;
+    return -1;
+}
+
+// Layer.cc:19-24: tracklet layer pairs are barrel (1,3), (2,4), (3,5)
+__device__ __forceinline__ int tl_layer_outer(int si) { return si <= 2 ? si + 2 : -1; }
+
+__device__ __forceinline__ int SR(const BatchDev& b, int k) { return AT(b.geo.slot_run, k, b.geo.n_slot_run); }
+
+// objects of stage st in layer slot sl of event ev
+__device__ __forceinline__ int64_t layer_count(const BatchDev& b, int st, int ev, int sl) {
+    const int64_t base = (int64_t)ev * b.geo.n_mod;
+    int64_t n = 0;
+    for (int r = SR(b, sl); r < SR(b, sl + 1); ++r)
+        n += OFF(b, st, base + SR(b, kNumSlots + 2 + 2 * r)) - OFF(b, st, base + SR(b, kNumSlots + 1 + 2 * r));
+    return n;
+}
+
+// the q-th object of stage st in layer slot sl of event ev (q < layer_count)
+__device__ __forceinline__ int layer_object(const BatchDev& b, int st, int ev, int sl, int64_t q) {
+    const int64_t base = (int64_t)ev * b.geo.n_mod;
+    for (int r = SR(b, sl); r < SR(b, sl + 1); ++r) {
+        const int64_t o0 = OFF(b, st, base + SR(b, kNumSlots + 1 + 2 * r));
+        const int64_t n = OFF(b, st, base + SR(b, kNumSlots + 2 + 2 * r)) - o0;
+        if (q < n) return (int)(o0 + q);
+        q -= n;
+    }
+#ifdef SDL_DEVICE_CHECKS
+    (void)IX(-3, 0);
+#endif
+    return 0;
+}
+
+// segment candidates by layer pairs (Event.cc:432-443, 793-821): candidate q
+// of inner MD a runs over the MDs of the paired outer layers, in table order
+struct SGLayerStage {
+    static constexpr int kSt = kSG;
+    __device__ static bool eval(const BatchDev& b, int a, int64_t q, int& oi, int& oj, float* fv) {
+        const int n_mod = b.geo.n_mod;
+        const int g1 = OG(b, kMD, a);
+        const int ev = g1 / n_mod, m1 = g1 - ev * n_mod;
+        const int si = MOD(b, m1).layer_slot;
+        int bmd = -1;
+        for (int k = 0; k < 3; ++k) {
+            const int so = sg_layer_outer(si, k);
+            if (so < 0) break;
+            const int64_t n = layer_count(b, kMD, ev, so);
+            if (q < n) {
+                bmd = layer_object(b, kMD, ev, so, q);
+                break;
             }
-            pass = sg_endcap(im, om, AT(b.ha1, oanc, H(b)), AT(b.htf, oanc, H(b)), true, oHi, oLo, v);
+            q -= n;
         }
         oi = a; oj = bmd;
-        fv[0] = v.dphi; fv[1] = v.dphimin; fv[2] = v.dphimax;
-        fv[3] = v.dphichange; fv[4] = v.dphiminchange; fv[5] = v.dphimaxchange;
-        return pass;
+        if (bmd < 0) {
+#ifdef SDL_DEVICE_CHECKS
+            (void)IX(-4, 0);
+#endif
+            return false;
+        }
+        const int m2 = OG(b, kMD, bmd) - ev * n_mod;
+        bool connected = false;
+        if (MOD(b, m2).subdet == kEndcap) {
+            const int k0 = AT(b.geo.conn_off, m1, NM(b) + 1), k1 = AT(b.geo.conn_off, m1 + 1, NM(b) + 1);
+            for (int k = k0; k < k1 && !connected; ++k) connected = AT(b.geo.conn_idx, k, NC(b)) == m2;
+        }
+        return sg_pair(b, a, bmd, connected, fv);
     }
     __device__ static int group_of(const BatchDev& b, int a) { return OG(b, kMD, a); }
 };
@@ -366,6 +455,15 @@ __device__ __forceinline__ int tl_outer(const BatchDev& b, int s, int64_t q) {
     const int k = conn_entry(b, ev, m2, q, pref);
     const int g3 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
     return (int)(OFF(b, kSG, g3) + (q - pref));
+}
+
+// tracklet candidate q of inner segment s by layer pairs (Event.cc:755-790):
+// the q-th segment of the paired outer barrel layer
+__device__ __forceinline__ int tl_outer_layer(const BatchDev& b, int s, int64_t q) {
+    const int n_mod = b.geo.n_mod;
+    const int g1 = OG(b, kSG, s);
+    const int ev = g1 / n_mod;
+    return layer_object(b, kSG, ev, tl_layer_outer(MOD(b, g1 - ev * n_mod).layer_slot), q);
 }
 
 struct TPStage {
@@ -554,7 +652,8 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum(BatchDev b) {
     const int64_t total = AT(off, nobj, offlim);
     const int64_t ntask = (total + kTask - 1) / kTask;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const bool nm1 = (b.flags & 4) != 0;
+    const bool nm1 = (b.flags & kFlagTLNm1) != 0;
+    const bool lay = (b.flags & kFlagTLLayers) != 0;
     __shared__ int qs[kEnumThreads / 32][kTLQueue];
     __shared__ int qt[kEnumThreads / 32][kTLQueue];
     __shared__ float qc[kEnumThreads / 32][kTLQueue];
@@ -582,7 +681,7 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum(BatchDev b) {
                     float cut = 0.f, muls = 0.f;
                     if (c < end) {
                         s = (i0 == i1) ? i0 : find_obj(b, off, offlim, i0, i1, c);
-                        tt = tl_outer(b, s, c - AT(off, s, offlim));
+                        tt = lay ? tl_outer_layer(b, s, c - AT(off, s, offlim)) : tl_outer(b, s, c - AT(off, s, offlim));
                         (void)IX(s, b.obj[kSG].cap);
                         (void)IX(tt, b.obj[kSG].cap);
                         const SGV S = load_sgv(b.sgpack, s);
@@ -748,6 +847,49 @@ __global__ void k_tl_count(BatchDev b) {
     }
 }
 
+// layer-pair segment candidates of every MD (Event.cc:805-818 loops over
+// inner-layer MDs x outer-layer MDs); the reference counts none of them
+__global__ void k_sg_count_layers(BatchDev b) {
+    if (halted(b)) return;
+    const int n_mod = b.geo.n_mod;
+    const int64_t n = n_inner(b, kSG);
+    for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+        const int g1 = OG(b, kMD, a);
+        const int ev = g1 / n_mod;
+        const int si = MOD(b, g1 - ev * n_mod).layer_slot;
+        int64_t c = 0;
+        for (int k = 0; k < 3; ++k) {
+            const int so = sg_layer_outer(si, k);
+            if (so < 0) break;
+            c += layer_count(b, kMD, ev, so);
+        }
+        AT(b.cand[kSG], a, b.cand_cap[kSG] + 1) = c;
+    }
+}
+
+// layer-pair tracklet candidates of every segment (Event.cc:762-787), counted
+// per inner layer like the module-map variant
+__global__ void k_tl_count_layers(BatchDev b) {
+    if (halted(b)) return;
+    const int n_mod = b.geo.n_mod;
+    const int64_t n = n_inner(b, kTL);
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s - threadIdx.x < n; s += (int64_t)gridDim.x * blockDim.x) {
+        const bool in = s < n;
+        int64_t c = 0;
+        int ev = 0, slot = 0;
+        if (in) {
+            const int g1 = OG(b, kSG, s);
+            ev = g1 / n_mod;
+            slot = MOD(b, g1 - ev * n_mod).layer_slot;
+            const int so = tl_layer_outer(slot);
+            c = so >= 0 ? layer_count(b, kSG, ev, so) : 0;
+            AT(b.cand[kTL], s, b.cand_cap[kTL] + 1) = c;
+        }
+        const bool act = in && c != 0;
+        warp_add(act ? counter_at(b, ev, kTL, 0, slot) : b.counters, (uint32_t)c, act);
+    }
+}
+
 __global__ void k_tp_count(BatchDev b) {
     if (halted(b)) return;
     const int n_mod = b.geo.n_mod;
@@ -838,7 +980,7 @@ void scan_h(const BatchDev& b, int64_t* data, const int64_t* n_ptr, int64_t cap,
 }
 
 template <class F>
-void enum_and_group(const BatchDev& b, cudaStream_t s, Hooks* h) {
+void enum_and_group(const BatchDev& b, cudaStream_t s, Hooks* h, bool layer_counters = true) {
     constexpr int st = F::kSt;
     const int64_t* ninner_ptr = nullptr;
     switch (st) {
@@ -852,10 +994,10 @@ void enum_and_group(const BatchDev& b, cudaStream_t s, Hooks* h) {
     if (h && h->timed) rec_event(h->enum_start[st], s);
     k_enum<F><<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
     if (h && h->timed) rec_event(h->enum_stop[st], s);
-    k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, st);
+    if (layer_counters) k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, st);
     scan_h(b, b.obj[st].mod_cnt, b.n_gm_dev, b.n_gm, s, h);
     k_scatter<<<b.n_sm * 8, 256, 0, s>>>(b, st);
-    if (h) h->launches += 3;
+    if (h) h->launches += layer_counters ? 3 : 2;
 }
 
 }  // namespace
@@ -875,6 +1017,13 @@ void launch_md(const BatchDev& b, cudaStream_t s, Hooks* h) {
 }
 
 void launch_sg(const BatchDev& b, cudaStream_t s, Hooks* h) {
+    if (b.flags & kFlagSGLayers) {
+        // Event.cc:793-821 increments no per-layer counter
+        k_sg_count_layers<<<b.n_sm * 8, 256, 0, s>>>(b);
+        if (h) h->launches += 1;
+        enum_and_group<SGLayerStage>(b, s, h, false);
+        return;
+    }
     k_conn_sum<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kMD, kSG);
     k_sg_count<<<b.n_sm * 8, 256, 0, s>>>(b);
     if (h) h->launches += 2;
@@ -886,7 +1035,8 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     // triplet candidate counters (Event.cc:547-596 loops over the same lists)
     k_sg_pack<<<b.n_sm * 8, 256, 0, s>>>(b);
     k_conn_sum<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kSG, kTP);
-    k_tl_count<<<b.n_sm * 8, 256, 0, s>>>(b);
+    if (b.flags & kFlagTLLayers) k_tl_count_layers<<<b.n_sm * 8, 256, 0, s>>>(b);
+    else k_tl_count<<<b.n_sm * 8, 256, 0, s>>>(b);
     if (h) h->launches += 3;
     scan_h(b, b.cand[kTL], b.obj[kSG].mod_cnt + b.n_gm, b.cand_cap[kTL], s, h);
     if (h && h->timed) rec_event(h->enum_start[kTL], s);

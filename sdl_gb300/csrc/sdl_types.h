@@ -41,6 +41,22 @@ struct Geometry {
     const ModDev* mod;
     const int32_t* conn_off; // n_mod + 1
     const int32_t* conn_idx;
+    // Layers as module-index runs, for the layer-pair variants (Layer.cc:3-50):
+    // slot_run[s] .. slot_run[s + 1] are the runs of layer slot s (0-5 barrel
+    // layers 1-6, 6-10 endcap layers 1-5); run r spans module indices
+    // [slot_run[kNumSlots + 1 + 2r], slot_run[kNumSlots + 2 + 2r]).  Barrel
+    // layers are one run of the sorted detIds, endcap layers one run per side.
+    const int32_t* slot_run;
+    int n_slot_run;          // entries of slot_run
+};
+
+constexpr int kNumSlots = 11;
+
+// Chain flags (the SDLG_FLAG_* values of the C ABI)
+enum : int {
+    kFlagSGLayers = 1,   // createSegments: layer-pair segments
+    kFlagTLLayers = 2,   // createTracklets: layer-pair tracklets
+    kFlagTLNm1 = 4,      // DefaultNm1_TLAlgo
 };
 
 // Per-stage status word bits

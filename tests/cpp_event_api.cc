@@ -1,9 +1,12 @@
 // Drives the chain through include/sdl_event.hpp exactly as a caller of the
 // reference's SDL::Event would, and prints the object counts per stage.
-//   cpp_event_api <tilted> <endcap> <map> <hits.bin>
+//   cpp_event_api <tilted> <endcap> <map> <hits.bin> [layer]
+// "layer" selects createSegments / createTracklets (layer pairs) instead of
+// the module-map variants.
 // hits.bin: int64 n, float32 x[n], y[n], z[n], int32 idx[n], uint32 detid[n].
 // Exit code 3 when no CUDA device is available.
 #include <cstdio>
+#include <string>
 #include <vector>
 
 #include "sdl_event.hpp"
@@ -28,8 +31,11 @@ int main(int argc, char** argv) {
         SDL::Event ev;
         for (int64_t i = 0; i < n; ++i) ev.addHitToModule(SDL::Hit(x[i], y[i], z[i], idx[i]), det[i]);
         ev.createMiniDoublets();
-        ev.createSegmentsWithModuleMap();
-        ev.createTrackletsWithModuleMap();
+        const bool layer = argc > 5 && std::string(argv[5]) == "layer";
+        if (layer) ev.createSegments();
+        else ev.createSegmentsWithModuleMap();
+        if (layer) ev.createTracklets();
+        else ev.createTrackletsWithModuleMap();
         ev.createTriplets();
         ev.createTrackCandidates();
         std::printf("%u %u %u %u %u %u\n", ev.getNumberOfHits(), ev.getNumberOfMiniDoublets(), ev.getNumberOfSegments(),

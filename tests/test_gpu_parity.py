@@ -28,14 +28,16 @@ def run_gpu(gpu, det, events, flags=0):
     return gpu
 
 
-MAP_NAMES = [n for n in golden_names() if not n.endswith("_layer")]
+# fixture mode -> chain flags: "layer" fixtures were made with the
+# reference's createSegments + createTracklets (layer pairs)
+FLAGS = {"map": 0, "layer": 3}
 
 
-@pytest.mark.parametrize("name", MAP_NAMES)
+@pytest.mark.parametrize("name", golden_names())
 def test_gpu_matches_reference_golden(name, gpu, oracle_lib):
     meta = golden_meta(name)
     det, ev = regenerate(meta)
-    run_gpu(gpu, det, [ev])
+    run_gpu(gpu, det, [ev], FLAGS[meta["mode"]])
     full = golden_tuples(name)
     for s in range(5):
         got = gpu.objects(s, 0)
@@ -70,6 +72,26 @@ def test_gpu_matches_oracle_batch_uneven(gpu, oracle_lib):
         assert np.array_equal(gpu.counters(e), cnt)
     tot = gpu.counts(-1)
     assert tot[4] == sum(len(orc.run(ev)[0][4]) for ev in events)
+
+
+@pytest.mark.parametrize("flags", [1, 2, 3, 3 | 4])
+def test_layer_pair_variants_match_oracle(flags, gpu, oracle_lib):
+    """createSegments / createTracklets (layer pairs), alone and together, on
+    a batch with barrel, tilted and endcap hits and an empty event, against
+    the CPU restatement (mode bits = chain flag bits), counters included."""
+    from sdl_gb300 import synth
+    det = synth.detector("full")
+    events = [synth.make_event(det, 940, "full", n_pu=350),
+              synth.make_event(det, 941, "full", n_pu=0, n_signal=0, noise_frac=0.0),
+              synth.make_event(det, 942, "full", n_pu=1050)]
+    run_gpu(gpu, det, events, flags)
+    orc = oracle_lib.Oracle(det)
+    for e, ev in enumerate(events):
+        ref, cnt, _ = orc.run(ev, mode=flags)
+        for s in range(5):
+            got = gpu.objects(s, e)
+            assert oracle_lib.digest(got) == oracle_lib.digest(ref[s]), describe(oracle_lib, got, ref[s], s)
+        assert np.array_equal(gpu.counters(e), cnt)
 
 
 def test_graph_and_direct_launch_agree(gpu, oracle_lib):
@@ -131,19 +153,19 @@ def test_unknown_module_extends_table(gpu, oracle_lib):
         assert oracle_lib.digest(gpu.objects(s, 0)) == oracle_lib.digest(ref[s])
 
 
-def test_cpp_event_api_matches_golden(tmp_path, oracle_lib):
+@pytest.mark.parametrize("name", ["flat_s0", "flat_s0_layer"])
+def test_cpp_event_api_matches_golden(name, tmp_path, oracle_lib):
     """The reference's call sequence through include/sdl_event.hpp."""
     import os
     import subprocess
-    from conftest import ROOT
     from test_capi_cpu import build_cpp_demo
-    meta = golden_meta("flat_s0")
+    meta = golden_meta(name)
     det, ev = regenerate(meta)
     exe = build_cpp_demo(tmp_path)
     paths = det.write_files(str(tmp_path))
     hb = os.path.join(str(tmp_path), "hits.bin")
     ev.write_bin(hb)
-    r = subprocess.run([exe, *paths, hb], capture_output=True, text=True, check=True)
+    r = subprocess.run([exe, *paths, hb, meta["mode"]], capture_output=True, text=True, check=True)
     nums = [int(v) for v in r.stdout.split("\n")[0].split()]
     assert nums[0] == len(ev)
     assert nums[1:] == meta["counts"]
