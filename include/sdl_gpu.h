@@ -56,6 +56,7 @@ extern "C" {
                                  pair table Layer.cc:3-30) instead of createTrackletsWithModuleMap */
 #define SDLG_FLAG_TL_NM1 4   /* tracklets with DefaultNm1_TLAlgo (Algo.h:23-28) */
 #define SDLG_FLAG_NO_GRAPH 8 /* launch stage by stage instead of replaying a CUDA graph */
+#define SDLG_FLAG_MLP 16     /* learned pre-filter ahead of the tracklet cuts (no counterpart in the reference) */
 
 typedef struct sdlg_ctx sdlg_ctx;
 
@@ -159,6 +160,48 @@ int64_t sdlg_last_launches(const sdlg_ctx* ctx);
 int sdlg_mini_doublets_static(sdlg_ctx* ctx, int64_t n_hits, const float* d_x, const float* d_y, const float* d_z,
                               const int32_t* d_idx, const uint32_t* d_detid, int32_t* d_pairs, int64_t pair_cap,
                               int64_t* d_count, uint32_t* d_status, void* stream);
+
+/* ---- Learned tracklet pre-filter (no counterpart in the reference) ----
+ * A 12-64-64-1 perceptron (ReLU, BF16 weights and first hidden layer, FP32
+ * accumulation) scores every tracklet candidate (inner segment, outer
+ * segment) from 12 float features; with SDLG_FLAG_MLP a candidate whose logit
+ * is below the threshold is dropped before the reference's tracklet cuts,
+ * which still judge every other candidate.  The pruned chain's tracklets,
+ * triplets and track candidates are therefore subsets of the plain chain's.
+ * Inference runs on the tensor cores inside the tracklet kernel; training
+ * runs on the GPU with this library's kernels on samples labelled by the
+ * plain chain's tracklet cuts.
+ * Parameter vector (SDLG_MLP_PARAMS floats): W1[64][12], b1[64], W2[64][64],
+ * b2[64], w3[64], b3; logit = b3 + w3 . relu(W2 relu(W1 x + b1) + b2). */
+#define SDLG_MLP_FEATURES 12
+#define SDLG_MLP_PARAMS 5057
+int sdlg_mlp_set_params(sdlg_ctx* ctx, const float* params, float threshold);
+int sdlg_mlp_get_params(sdlg_ctx* ctx, float* params, float* threshold);
+int sdlg_mlp_set_threshold(sdlg_ctx* ctx, float threshold);
+/* uniform fan-in initialisation from `seed`, zero biases, threshold 0 */
+int sdlg_mlp_init(sdlg_ctx* ctx, uint64_t seed);
+/* After a run through the tracklet stage without SDLG_FLAG_MLP: append the
+ * features of every tracklet candidate that passes the float cuts to the
+ * context's training set, labelled 1 if the tracklet cuts accept it and 0
+ * otherwise; rejected candidates are kept with probability neg_keep (a
+ * deterministic hash of the candidate and `seed`).  *n_total: samples held. */
+int sdlg_mlp_collect(sdlg_ctx* ctx, float neg_keep, uint64_t seed, int64_t* n_total);
+int sdlg_mlp_add_samples(sdlg_ctx* ctx, int64_t n, const float* x, const float* y);
+int sdlg_mlp_num_samples(sdlg_ctx* ctx, int64_t* n);
+int sdlg_mlp_get_samples(sdlg_ctx* ctx, float* x, float* y, int64_t cap, int64_t* n);
+int sdlg_mlp_clear_samples(sdlg_ctx* ctx);
+/* Adam (beta 0.9, 0.999) on the weighted logistic loss, positives weighted
+ * pos_weight, mini-batches of `batch` in a fresh shuffle per epoch;
+ * epoch_loss[e] (optional) receives each epoch's mean loss. */
+int sdlg_mlp_train(sdlg_ctx* ctx, int epochs, int batch, float lr, float pos_weight, uint64_t seed, float* epoch_loss);
+/* Gradient of mean_i w_i * (softplus(z_i) - y_i z_i) at the current
+ * parameters over n samples (the training kernels), and the loss. */
+int sdlg_mlp_gradient(sdlg_ctx* ctx, int64_t n, const float* x, const float* y, const float* w, float* grad, double* loss);
+/* logits of n feature rows (n x 12) through the tensor-core kernel */
+int sdlg_mlp_score(sdlg_ctx* ctx, int64_t n, const float* x, float* logits);
+/* counts of the last run with SDLG_FLAG_MLP: candidates scored, kept,
+ * kept and through the float cuts, tensor-core waits that gave up */
+int sdlg_mlp_stats(sdlg_ctx* ctx, int64_t* out4);
 
 /* Pinned host memory for zero-staging transfers. */
 int sdlg_host_alloc(sdlg_ctx* ctx, int64_t bytes, void** out);

@@ -31,6 +31,9 @@ FLAG_SG_LAYERS = 1   # Event::createSegments (layer pairs) instead of createSegm
 FLAG_TL_LAYERS = 2   # Event::createTracklets (layer pairs) instead of createTrackletsWithModuleMap
 FLAG_TL_NM1 = 4
 FLAG_NO_GRAPH = 8
+FLAG_MLP = 16        # learned pre-filter ahead of the tracklet cuts
+MLP_FEATURES = 12
+MLP_PARAMS = 5057
 
 
 class SDLError(RuntimeError):
@@ -70,6 +73,20 @@ def lib():
         L.sdlg_mini_doublets_static.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
         L.sdlg_host_alloc.argtypes = [vp, i64, ctypes.POINTER(vp)]
         L.sdlg_host_free.argtypes = [vp, vp]
+        u64, f32 = ctypes.c_uint64, ctypes.c_float
+        L.sdlg_mlp_set_params.argtypes = [vp, vp, f32]
+        L.sdlg_mlp_get_params.argtypes = [vp, vp, vp]
+        L.sdlg_mlp_set_threshold.argtypes = [vp, f32]
+        L.sdlg_mlp_init.argtypes = [vp, u64]
+        L.sdlg_mlp_collect.argtypes = [vp, f32, u64, vp]
+        L.sdlg_mlp_add_samples.argtypes = [vp, i64, vp, vp]
+        L.sdlg_mlp_num_samples.argtypes = [vp, vp]
+        L.sdlg_mlp_get_samples.argtypes = [vp, vp, vp, i64, vp]
+        L.sdlg_mlp_clear_samples.argtypes = [vp]
+        L.sdlg_mlp_train.argtypes = [vp, i32, i32, f32, f32, u64, vp]
+        L.sdlg_mlp_gradient.argtypes = [vp, i64, vp, vp, vp, vp, vp]
+        L.sdlg_mlp_score.argtypes = [vp, i64, vp, vp]
+        L.sdlg_mlp_stats.argtypes = [vp, vp]
         _LIB = L
     return _LIB
 
@@ -208,3 +225,86 @@ class Chain:
         out = np.zeros(7, dtype=np.float32)
         self._ck(lib().sdlg_last_times(self.h, out.ctypes.data))
         return out
+
+    # ---------------------------------------------------------------- pre-filter
+    def mlp_set_params(self, params, threshold: float = 0.0):
+        """Load the pre-filter's FP32 parameter vector (MLP_PARAMS floats) and
+        logit threshold."""
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.size != MLP_PARAMS:
+            raise SDLError("expected %d parameters, got %d" % (MLP_PARAMS, p.size))
+        self._ck(lib().sdlg_mlp_set_params(self.h, p.ctypes.data, float(threshold)))
+
+    def mlp_params(self):
+        """(parameters, threshold)"""
+        p = np.empty(MLP_PARAMS, dtype=np.float32)
+        t = ctypes.c_float()
+        self._ck(lib().sdlg_mlp_get_params(self.h, p.ctypes.data, ctypes.addressof(t)))
+        return p, float(t.value)
+
+    def mlp_set_threshold(self, threshold: float):
+        self._ck(lib().sdlg_mlp_set_threshold(self.h, float(threshold)))
+
+    def mlp_init(self, seed: int = 0):
+        self._ck(lib().sdlg_mlp_init(self.h, int(seed)))
+
+    def mlp_collect(self, neg_keep: float = 1.0, seed: int = 0) -> int:
+        """Append training samples from the last run's tracklet candidates;
+        returns the number of samples held."""
+        n = ctypes.c_int64()
+        self._ck(lib().sdlg_mlp_collect(self.h, float(neg_keep), int(seed), ctypes.addressof(n)))
+        return int(n.value)
+
+    def mlp_add_samples(self, x, y):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, MLP_FEATURES)
+        y = np.ascontiguousarray(y, dtype=np.float32).reshape(-1)
+        self._ck(lib().sdlg_mlp_add_samples(self.h, len(y), x.ctypes.data, y.ctypes.data))
+
+    def mlp_num_samples(self) -> int:
+        n = ctypes.c_int64()
+        self._ck(lib().sdlg_mlp_num_samples(self.h, ctypes.addressof(n)))
+        return int(n.value)
+
+    def mlp_samples(self):
+        """(features n x 12, labels n) of the training set"""
+        n = self.mlp_num_samples()
+        x = np.empty((n, MLP_FEATURES), dtype=np.float32)
+        y = np.empty(n, dtype=np.float32)
+        m = ctypes.c_int64()
+        self._ck(lib().sdlg_mlp_get_samples(self.h, x.ctypes.data, y.ctypes.data, n, ctypes.addressof(m)))
+        return x, y
+
+    def mlp_clear_samples(self):
+        self._ck(lib().sdlg_mlp_clear_samples(self.h))
+
+    def mlp_train(self, epochs: int, batch: int = 4096, lr: float = 2e-3, pos_weight: float = 4.0, seed: int = 0):
+        """Train on the GPU (the library's forward / backward / Adam kernels);
+        returns the mean loss of each epoch."""
+        out = np.zeros(max(epochs, 1), dtype=np.float32)
+        self._ck(lib().sdlg_mlp_train(self.h, int(epochs), int(batch), float(lr), float(pos_weight), int(seed),
+                                      out.ctypes.data))
+        return out[:epochs]
+
+    def mlp_gradient(self, x, y, w):
+        """(gradient, loss) of mean_i w_i * logistic loss at the current parameters"""
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, MLP_FEATURES)
+        y = np.ascontiguousarray(y, dtype=np.float32).reshape(-1)
+        w = np.ascontiguousarray(w, dtype=np.float32).reshape(-1)
+        g = np.empty(MLP_PARAMS, dtype=np.float32)
+        loss = ctypes.c_double()
+        self._ck(lib().sdlg_mlp_gradient(self.h, len(y), x.ctypes.data, y.ctypes.data, w.ctypes.data, g.ctypes.data,
+                                         ctypes.addressof(loss)))
+        return g, float(loss.value)
+
+    def mlp_score(self, x) -> np.ndarray:
+        """Logits of feature rows through the tensor-core kernel."""
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(-1, MLP_FEATURES)
+        z = np.empty(len(x), dtype=np.float32)
+        self._ck(lib().sdlg_mlp_score(self.h, len(x), x.ctypes.data, z.ctypes.data))
+        return z
+
+    def mlp_stats(self) -> dict:
+        """Pre-filter counts of the last run with FLAG_MLP."""
+        out = np.zeros(4, dtype=np.int64)
+        self._ck(lib().sdlg_mlp_stats(self.h, out.ctypes.data))
+        return {"scored": int(out[0]), "kept": int(out[1]), "passed_float_cuts": int(out[2]), "timeouts": int(out[3])}

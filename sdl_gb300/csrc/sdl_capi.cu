@@ -16,6 +16,7 @@
 
 #include "../../include/sdl_gpu.h"
 #include "sdl_kernels.h"
+#include "sdl_mlp.h"
 
 using namespace sdlg;
 
@@ -107,6 +108,23 @@ struct sdlg_ctx {
     int32_t* d_conn_idx = nullptr;
     std::vector<int32_t> slot_run;
     int32_t* d_slot_run = nullptr;
+    // learned tracklet pre-filter: parameters, packed weights, training state
+    struct {
+        float* params = nullptr;        // FP32 master parameters (kMlpParams)
+        unsigned char* pack = nullptr;  // packed inference weights + threshold (kPackBytes)
+        MlpStats* stats = nullptr;
+        float *grad = nullptr, *m = nullptr, *v = nullptr;
+        double* loss = nullptr;
+        unsigned int* status = nullptr;
+        unsigned long long* found = nullptr;
+        int64_t adam_t = 0;
+        float thr = 0.f;
+        bool have = false;
+        float *x = nullptr, *y = nullptr;  // training samples
+        int64_t n = 0, cap = 0;
+        int32_t* order = nullptr;
+        int64_t order_cap = 0;
+    } mlp;
     // batch
     int64_t n_ev = 0, n_hit = 0;
     std::vector<int64_t> ev_off;
@@ -290,6 +308,8 @@ int ensure_buffers(sdlg_ctx* ctx) {
     b.n_gm = (int)n_gm;
     b.n_hit_cap = H;
     b.n_sm = ctx->n_sm;
+    b.mlp_pack = ctx->mlp.pack;
+    b.mlp_stats = ctx->mlp.stats;
     int rc;
 #define AL(ptr, n) if ((rc = dalloc(ctx, &(ptr), (n))) != SDLG_OK) return rc
     int64_t* small;
@@ -357,6 +377,7 @@ void enqueue_chain(sdlg_ctx* ctx, int stop_after) {
     cudaMemsetAsync(b.counters, 0, b.n_ev * 110 * sizeof(uint32_t), s);
     cudaMemsetAsync(b.mod_hit, 0, (n_gm + 1) * sizeof(int64_t), s);
     for (int st = 0; st < kNumStages; ++st) cudaMemsetAsync(b.obj[st].mod_cnt, 0, (n_gm + 1) * sizeof(int64_t), s);
+    cudaMemsetAsync(b.mlp_stats, 0, sizeof(MlpStats), s);
     Hooks* h = &ctx->hooks;
     h->timed = true;
     h->launches = 0;
@@ -402,6 +423,7 @@ int launch_checked(sdlg_ctx* ctx, int stop_after) {
     cudaMemsetAsync(b.counters, 0, b.n_ev * 110 * sizeof(uint32_t), s);
     cudaMemsetAsync(b.mod_hit, 0, (n_gm + 1) * sizeof(int64_t), s);
     for (int st = 0; st < kNumStages; ++st) cudaMemsetAsync(b.obj[st].mod_cnt, 0, (n_gm + 1) * sizeof(int64_t), s);
+    cudaMemsetAsync(b.mlp_stats, 0, sizeof(MlpStats), s);
     int rc;
     record(ctx->ev[0], s);
     Hooks* h = &ctx->hooks;
@@ -482,6 +504,8 @@ int finish(sdlg_ctx* ctx) {
             if (rc) return rc;
             continue;
         }
+        if (status & kStatusMlpTimeout)
+            return fail(ctx, SDLG_ERR_CUDA, "tracklet pre-filter: a tensor-core wait gave up; results discarded");
         if (!(status & 0x1fu)) return SDLG_OK;
         // grow every stage that overflowed (the attempted-append counters hold
         // the exact need of the first overflowing stage)
@@ -544,6 +568,57 @@ int parse_file(const char* path, int kind, HostGeometry& hg) {
 
 }  // namespace
 
+namespace {
+
+// ------------------------------------------------------------------ pre-filter
+uint64_t splitmix64(uint64_t& state) {
+    uint64_t z = (state += 0x9E3779B97F4A7C15ull);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+int mlp_repack(sdlg_ctx* ctx) {
+    launch_mlp_pack(ctx->mlp.params, ctx->mlp.pack, ctx->mlp.thr, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SDLG_OK;
+}
+
+// grow the training-sample buffers to hold `need` samples, keeping the first n
+int mlp_reserve(sdlg_ctx* ctx, int64_t need) {
+    auto& M = ctx->mlp;
+    if (need <= M.cap) return SDLG_OK;
+    const int64_t cap = std::max<int64_t>(need, M.cap * 2 + 65536);
+    float *x = nullptr, *y = nullptr;
+    CK(cudaMalloc(&x, cap * kMlpIn * sizeof(float)));
+    if (cudaMalloc(&y, cap * sizeof(float)) != cudaSuccess) {
+        cudaFree(x);
+        return fail(ctx, SDLG_ERR_CAPACITY, "no device memory for %lld training samples", (long long)cap);
+    }
+    if (M.n) {
+        CK(cudaMemcpy(x, M.x, M.n * kMlpIn * sizeof(float), cudaMemcpyDeviceToDevice));
+        CK(cudaMemcpy(y, M.y, M.n * sizeof(float), cudaMemcpyDeviceToDevice));
+    }
+    cudaFree(M.x);
+    cudaFree(M.y);
+    M.x = x;
+    M.y = y;
+    M.cap = cap;
+    return SDLG_OK;
+}
+
+// device copy of a host array (caller frees)
+template <class T>
+int to_device(sdlg_ctx* ctx, const T* h, int64_t n, T** d) {
+    *d = nullptr;
+    CK(cudaMalloc(d, std::max<int64_t>(n, 1) * sizeof(T)));
+    if (n) CK(cudaMemcpy(*d, h, n * sizeof(T), cudaMemcpyHostToDevice));
+    return SDLG_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int sdlg_create(sdlg_ctx** out, int device) {
@@ -563,7 +638,24 @@ int sdlg_create(sdlg_ctx** out, int device) {
         if (e == cudaSuccess) e = cudaEventCreate(&ctx->hooks.enum_stop[k]);
     }
     if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_small, 16 * sizeof(int64_t));
+    // pre-filter state is small and allocated once, so device pointers captured
+    // in the launch graph never change
+    auto& M = ctx->mlp;
+    if (e == cudaSuccess) e = cudaMalloc(&M.params, kMlpParams * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&M.grad, kMlpParams * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&M.m, kMlpParams * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&M.v, kMlpParams * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&M.pack, kPackBytes);
+    if (e == cudaSuccess) e = cudaMalloc(&M.stats, sizeof(MlpStats));
+    if (e == cudaSuccess) e = cudaMalloc(&M.loss, sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&M.status, sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMalloc(&M.found, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(M.grad, 0, kMlpParams * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(M.pack, 0, kPackBytes);
+    if (e == cudaSuccess) e = cudaMemset(M.stats, 0, sizeof(MlpStats));
     if (e != cudaSuccess) {
+        void* ps[] = {M.params, M.pack, M.stats, M.grad, M.m, M.v, M.loss, M.status, M.found};
+        for (void* p : ps) cudaFree(p);
         delete ctx;
         return SDLG_ERR_CUDA;
     }
@@ -578,6 +670,11 @@ int sdlg_destroy(sdlg_ctx* ctx) {
     free_batch(ctx);
     cudaFree(ctx->d_detid); cudaFree(ctx->d_mod); cudaFree(ctx->d_conn_off); cudaFree(ctx->d_conn_idx);
     cudaFree(ctx->d_slot_run);
+    {
+        auto& M = ctx->mlp;
+        void* ps[] = {M.params, M.pack, M.stats, M.grad, M.m, M.v, M.loss, M.status, M.found, M.x, M.y, M.order};
+        for (void* p : ps) cudaFree(p);
+    }
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     for (int k = 0; k < 8; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
@@ -688,6 +785,7 @@ int sdlg_run_async(sdlg_ctx* ctx, int stop_after, int flags) {
     if (!ctx->have_geo) return fail(ctx, SDLG_ERR_NO_GEOMETRY, "no geometry loaded");
     if (!ctx->buffers_ok || ctx->n_ev <= 0) return fail(ctx, SDLG_ERR_NO_EVENTS, "no events set");
     if (stop_after < 0 || stop_after > 4) return fail(ctx, SDLG_ERR_ARG, "stop_after out of range");
+    if ((flags & SDLG_FLAG_MLP) && !ctx->mlp.have) return fail(ctx, SDLG_ERR_ARG, "SDLG_FLAG_MLP without pre-filter parameters");
     cudaSetDevice(ctx->device);
     ctx->last_stop = stop_after;
     ctx->last_flags = flags;
@@ -791,6 +889,229 @@ int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5) {
 }
 
 int64_t sdlg_last_launches(const sdlg_ctx* ctx) { return ctx ? ctx->launches_per_run : -1; }
+
+// ------------------------------------------------------------------ pre-filter
+int sdlg_mlp_set_params(sdlg_ctx* ctx, const float* params, float threshold) {
+    if (!ctx || !params) return SDLG_ERR_ARG;
+    for (int k = 0; k < kMlpParams; ++k)
+        if (!std::isfinite(params[k])) return fail(ctx, SDLG_ERR_ARG, "parameter %d is not finite", k);
+    cudaSetDevice(ctx->device);
+    auto& M = ctx->mlp;
+    CK(cudaMemcpy(M.params, params, kMlpParams * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemset(M.m, 0, kMlpParams * sizeof(float)));
+    CK(cudaMemset(M.v, 0, kMlpParams * sizeof(float)));
+    CK(cudaMemset(M.grad, 0, kMlpParams * sizeof(float)));
+    M.adam_t = 0;
+    M.thr = threshold;
+    M.have = true;
+    return mlp_repack(ctx);
+}
+
+int sdlg_mlp_get_params(sdlg_ctx* ctx, float* params, float* threshold) {
+    if (!ctx) return SDLG_ERR_ARG;
+    if (!ctx->mlp.have) return fail(ctx, SDLG_ERR_ARG, "no pre-filter parameters");
+    cudaSetDevice(ctx->device);
+    if (params) CK(cudaMemcpy(params, ctx->mlp.params, kMlpParams * sizeof(float), cudaMemcpyDeviceToHost));
+    if (threshold) *threshold = ctx->mlp.thr;
+    return SDLG_OK;
+}
+
+int sdlg_mlp_set_threshold(sdlg_ctx* ctx, float threshold) {
+    if (!ctx) return SDLG_ERR_ARG;
+    if (!ctx->mlp.have) return fail(ctx, SDLG_ERR_ARG, "no pre-filter parameters");
+    cudaSetDevice(ctx->device);
+    ctx->mlp.thr = threshold;
+    return mlp_repack(ctx);
+}
+
+int sdlg_mlp_init(sdlg_ctx* ctx, uint64_t seed) {
+    if (!ctx) return SDLG_ERR_ARG;
+    // uniform fan-in initialisation (He et al. 2015), zero biases
+    std::vector<float> p(kMlpParams, 0.f);
+    uint64_t st = seed;
+    auto u = [&]() { return (double)(splitmix64(st) >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0; };
+    const double a1 = std::sqrt(6.0 / kMlpIn), a2 = std::sqrt(6.0 / kMlpHid);
+    for (int k = 0; k < kMlpHid * kMlpIn; ++k) p[kMlpW1 + k] = (float)(a1 * u());
+    for (int k = 0; k < kMlpHid * kMlpHid; ++k) p[kMlpW2 + k] = (float)(a2 * u());
+    for (int k = 0; k < kMlpHid; ++k) p[kMlpW3 + k] = (float)(a2 * u());
+    return sdlg_mlp_set_params(ctx, p.data(), 0.f);
+}
+
+int sdlg_mlp_collect(sdlg_ctx* ctx, float neg_keep, uint64_t seed, int64_t* n_total) {
+    if (!ctx || !(neg_keep >= 0.f && neg_keep <= 1.f)) return SDLG_ERR_ARG;
+    if (!ctx->ran || ctx->last_stop < kTL) return fail(ctx, SDLG_ERR_ARG, "run the chain through the tracklet stage first");
+    if (ctx->last_flags & SDLG_FLAG_MLP) return fail(ctx, SDLG_ERR_ARG, "collect after a run without SDLG_FLAG_MLP");
+    cudaSetDevice(ctx->device);
+    auto& M = ctx->mlp;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        int rc = mlp_reserve(ctx, M.n + 1);
+        if (rc) return rc;
+        CK(cudaMemsetAsync(M.found, 0, sizeof(unsigned long long), ctx->stream));
+        MlpCollect c;
+        c.x = M.x + M.n * kMlpIn;
+        c.y = M.y + M.n;
+        c.cap = M.cap - M.n;
+        c.n = M.found;
+        c.neg_keep = neg_keep;
+        c.seed = seed;
+        launch_tl_collect(ctx->b, c, ctx->stream);
+        CK(cudaGetLastError());
+        unsigned long long found = 0;
+        CK(cudaMemcpyAsync(&found, M.found, sizeof(found), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        if ((int64_t)found <= c.cap) {
+            M.n += (int64_t)found;
+            if (n_total) *n_total = M.n;
+            return SDLG_OK;
+        }
+        rc = mlp_reserve(ctx, M.n + (int64_t)found);  // the sampling is deterministic: collect again
+        if (rc) return rc;
+    }
+    return fail(ctx, SDLG_ERR_CAPACITY, "sample collection did not fit");
+}
+
+int sdlg_mlp_add_samples(sdlg_ctx* ctx, int64_t n, const float* x, const float* y) {
+    if (!ctx || n < 0 || (n && (!x || !y))) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    auto& M = ctx->mlp;
+    int rc = mlp_reserve(ctx, M.n + n);
+    if (rc) return rc;
+    if (n) {
+        CK(cudaMemcpy(M.x + M.n * kMlpIn, x, n * kMlpIn * sizeof(float), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(M.y + M.n, y, n * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    M.n += n;
+    return SDLG_OK;
+}
+
+int sdlg_mlp_num_samples(sdlg_ctx* ctx, int64_t* n) {
+    if (!ctx || !n) return SDLG_ERR_ARG;
+    *n = ctx->mlp.n;
+    return SDLG_OK;
+}
+
+int sdlg_mlp_get_samples(sdlg_ctx* ctx, float* x, float* y, int64_t cap, int64_t* n) {
+    if (!ctx || cap < 0) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    const int64_t k = std::min(cap, ctx->mlp.n);
+    if (k && x) CK(cudaMemcpy(x, ctx->mlp.x, k * kMlpIn * sizeof(float), cudaMemcpyDeviceToHost));
+    if (k && y) CK(cudaMemcpy(y, ctx->mlp.y, k * sizeof(float), cudaMemcpyDeviceToHost));
+    if (n) *n = ctx->mlp.n;
+    return SDLG_OK;
+}
+
+int sdlg_mlp_clear_samples(sdlg_ctx* ctx) {
+    if (!ctx) return SDLG_ERR_ARG;
+    ctx->mlp.n = 0;
+    return SDLG_OK;
+}
+
+int sdlg_mlp_train(sdlg_ctx* ctx, int epochs, int batch, float lr, float pos_weight, uint64_t seed, float* epoch_loss) {
+    if (!ctx || epochs < 0 || batch <= 0 || !(lr > 0.f) || !(pos_weight > 0.f)) return SDLG_ERR_ARG;
+    auto& M = ctx->mlp;
+    if (!M.have) return fail(ctx, SDLG_ERR_ARG, "no pre-filter parameters (sdlg_mlp_init or sdlg_mlp_set_params)");
+    if (M.n <= 0) return fail(ctx, SDLG_ERR_ARG, "no training samples");
+    if (M.n > INT32_MAX) return fail(ctx, SDLG_ERR_ARG, "too many training samples");
+    cudaSetDevice(ctx->device);
+    cudaStream_t s = ctx->stream;
+    if (M.order_cap < M.n) {
+        cudaFree(M.order);
+        M.order = nullptr;
+        CK(cudaMalloc(&M.order, M.n * sizeof(int32_t)));
+        M.order_cap = M.n;
+    }
+    std::vector<int32_t> order(M.n);
+    for (int64_t i = 0; i < M.n; ++i) order[i] = (int32_t)i;
+    uint64_t st = seed;
+    for (int ep = 0; ep < epochs; ++ep) {
+        for (int64_t i = M.n - 1; i > 0; --i) std::swap(order[i], order[splitmix64(st) % (uint64_t)(i + 1)]);
+        CK(cudaMemcpyAsync(M.order, order.data(), M.n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+        CK(cudaMemsetAsync(M.loss, 0, sizeof(double), s));
+        for (int64_t start = 0; start < M.n; start += batch) {
+            const int64_t count = std::min<int64_t>(batch, M.n - start);
+            cudaError_t e = launch_mlp_fwd_bwd(M.x, M.y, nullptr, M.order, start, count, pos_weight, 1.f / (float)count,
+                                               M.params, M.grad, M.loss, s);
+            if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "training step: %s", cudaGetErrorString(e));
+            ++M.adam_t;
+            const float c1 = (float)(1.0 - std::pow(0.9, (double)M.adam_t));
+            const float c2 = (float)(1.0 - std::pow(0.999, (double)M.adam_t));
+            launch_mlp_adam(M.params, M.grad, M.m, M.v, lr, c1, c2, s);
+        }
+        double loss = 0.0;
+        CK(cudaMemcpyAsync(&loss, M.loss, sizeof(double), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));  // the host order buffer is reused next epoch
+        if (epoch_loss) epoch_loss[ep] = (float)(loss / (double)M.n);
+    }
+    CK(cudaGetLastError());
+    return mlp_repack(ctx);
+}
+
+int sdlg_mlp_gradient(sdlg_ctx* ctx, int64_t n, const float* x, const float* y, const float* w, float* grad, double* loss) {
+    if (!ctx || n <= 0 || !x || !y || !w || !grad) return SDLG_ERR_ARG;
+    if (!ctx->mlp.have) return fail(ctx, SDLG_ERR_ARG, "no pre-filter parameters");
+    cudaSetDevice(ctx->device);
+    auto& M = ctx->mlp;
+    float *dx = nullptr, *dy = nullptr, *dw = nullptr;
+    int rc = to_device(ctx, x, n * kMlpIn, &dx);
+    if (!rc) rc = to_device(ctx, y, n, &dy);
+    if (!rc) rc = to_device(ctx, w, n, &dw);
+    cudaError_t e = cudaSuccess;
+    double l = 0.0;
+    if (!rc) {
+        cudaMemsetAsync(M.grad, 0, kMlpParams * sizeof(float), ctx->stream);
+        cudaMemsetAsync(M.loss, 0, sizeof(double), ctx->stream);
+        e = launch_mlp_fwd_bwd(dx, dy, dw, nullptr, 0, n, 1.f, 1.f / (float)n, M.params, M.grad, M.loss, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(grad, M.grad, kMlpParams * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&l, M.loss, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(M.grad, 0, kMlpParams * sizeof(float), ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    }
+    cudaFree(dx);
+    cudaFree(dy);
+    cudaFree(dw);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "gradient: %s", cudaGetErrorString(e));
+    if (loss) *loss = l / (double)n;
+    return SDLG_OK;
+}
+
+int sdlg_mlp_score(sdlg_ctx* ctx, int64_t n, const float* x, float* logits) {
+    if (!ctx || n < 0 || (n && (!x || !logits))) return SDLG_ERR_ARG;
+    if (!ctx->mlp.have) return fail(ctx, SDLG_ERR_ARG, "no pre-filter parameters");
+    if (!n) return SDLG_OK;
+    cudaSetDevice(ctx->device);
+    float *dx = nullptr, *dz = nullptr;
+    int rc = to_device(ctx, x, n * kMlpIn, &dx);
+    if (!rc && cudaMalloc(&dz, n * sizeof(float)) != cudaSuccess) rc = fail(ctx, SDLG_ERR_CUDA, "cudaMalloc");
+    cudaError_t e = cudaSuccess;
+    unsigned int st = 0;
+    if (!rc) {
+        cudaMemsetAsync(ctx->mlp.status, 0, sizeof(unsigned int), ctx->stream);
+        launch_mlp_score(dx, n, ctx->mlp.pack, dz, ctx->mlp.status, ctx->n_sm, ctx->stream);
+        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(logits, dz, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&st, ctx->mlp.status, sizeof(st), cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    }
+    cudaFree(dx);
+    cudaFree(dz);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "score: %s", cudaGetErrorString(e));
+    if (st) return fail(ctx, SDLG_ERR_CUDA, "score: a tensor-core wait gave up");
+    return SDLG_OK;
+}
+
+int sdlg_mlp_stats(sdlg_ctx* ctx, int64_t* out4) {
+    if (!ctx || !out4) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    MlpStats h;
+    CK(cudaMemcpy(&h, ctx->mlp.stats, sizeof(h), cudaMemcpyDeviceToHost));
+    out4[0] = (int64_t)h.scored;
+    out4[1] = (int64_t)h.kept;
+    out4[2] = (int64_t)h.passA;
+    out4[3] = (int64_t)h.timeouts;
+    return SDLG_OK;
+}
 
 }  // extern "C"
 

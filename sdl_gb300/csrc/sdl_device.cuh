@@ -413,6 +413,44 @@ __device__ __forceinline__ SGV load_sgv(const float* __restrict__ pack, int64_t 
     return v;
 }
 
+// Features of a tracklet candidate for the learned pre-filter (float
+// arithmetic only, no counterpart in the reference): anchor radii and z of
+// the innermost and outermost mini-doublets, the azimuthal opening between
+// them, the two segments' direction angles, float estimates of the betaIn /
+// betaOut angles the exact cuts test (Tracklet.cc:1205-1260), the rz
+// pointing residual of the outer anchor against the inner segment, a signed
+// 1/pT estimate from the mean beta, and a code of the anchor module types.
+// Every feature is scaled to O(1) and clamped to [-16, 16].
+__device__ __forceinline__ float wrap_pi_f(float x) { return x - 6.28318531f * rintf(x * 0.159154943f); }
+__device__ __forceinline__ void tl_features(const SGV& S, const SGV& T, float* f) {
+    const float ax = T.ux - S.lx, ay = T.uy - S.ly;
+    const float dr = sqrtf(ax * ax + ay * ay);
+    const float phiAxis = atan2f(ay, ax);
+    const float betaIn = S.dpc - wrap_pi_f(phiAxis - S.lphi);
+    const float betaOut = -T.alphaup + wrap_pi_f(phiAxis - T.uphi);
+    const float drIn = S.urt - S.lrt;
+    const float slope = (S.uz - S.lz) / (fabsf(drIn) > 1e-3f ? drIn : copysignf(1e-3f, drIn));
+    const float zRes = T.uz - (S.lz + slope * (T.urt - S.lrt));
+    const float invPt = __sinf(0.5f * (betaIn + betaOut)) / (fmaxf(dr, 1e-3f) * k2Rinv1GeVf);
+    const uint32_t fs = S.flags, ft = T.flags;
+    float v[12];
+    v[0] = S.lrt * 0.01f;
+    v[1] = S.lz * 0.01f;
+    v[2] = T.urt * 0.01f;
+    v[3] = T.uz * 0.01f;
+    v[4] = wrap_pi_f(T.uphi - S.lphi) * 10.f;
+    v[5] = S.dpc * 10.f;
+    v[6] = T.alphaup * 10.f;
+    v[7] = betaIn * 10.f;
+    v[8] = betaOut * 10.f;
+    v[9] = zRes * 0.1f;
+    v[10] = invPt;
+    v[11] = ((fs & F_LO_E) ? 1.f : 0.f) + ((ft & F_UP_E) ? 0.5f : 0.f) + ((fs & F_LO_PS) ? 0.25f : 0.f) +
+            ((ft & F_UP_2S) ? 0.125f : 0.f);
+#pragma unroll
+    for (int k = 0; k < 12; ++k) f[k] = fmaxf(fminf(v[k], 16.f), -16.f);
+}
+
 // strip-edge point of a 2S endcap hit (GeometryUtil.cc:3-23) from the edge offset
 __device__ __forceinline__ P3 edge_point(float x, float y, float z, float ex, float ey, bool up) {
     float px = up ? ex : -ex, py = up ? ey : -ey, pz = 0.f;

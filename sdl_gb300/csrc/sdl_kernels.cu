@@ -639,6 +639,63 @@ __global__ void k_sg_pack(BatchDev b) {
 
 constexpr int kTLQueue = 64;  // per-warp queue of candidates that passed phase A
 
+// one warp's queue of tracklet candidates that passed phase A
+struct TLQueue {
+    int* s;
+    int* t;
+    float* cut;
+    float* muls;
+    int* algo;
+};
+
+// queue the lanes' phase-A survivors; once a full warp is queued, run phase
+// B on 32 of them and append the accepted ones (every lane calls it)
+__device__ __forceinline__ void tl_queue_push(const BatchDev& b, const TLQueue& q, int& qn, int algo, int s, int tt, float cut,
+                                              float muls, bool nm1) {
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(0xffffffffu, algo != kAlgoNone);
+    if (algo != kAlgoNone) {
+        const int p = qn + __popc(m & ((1u << lane) - 1u));
+        q.s[p] = s; q.t[p] = tt; q.cut[p] = cut; q.muls[p] = muls; q.algo[p] = algo;
+    }
+    qn += __popc(m);
+    __syncwarp();
+    if (qn >= kWarp) {
+        // phase B on the last 32 queued candidates
+        const int k = qn - kWarp + lane;
+        const int qs_ = q.s[k], qt_ = q.t[k], qa_ = q.algo[k];
+        const float qc_ = q.cut[k], qm_ = q.muls[k];
+        __syncwarp();
+        qn -= kWarp;
+        const SGV S = load_sgv(b.sgpack, qs_);
+        const SGV T = load_sgv(b.sgpack, qt_);
+        const bool pass = tl_phaseB(qa_, S, T, qc_, qm_, nm1);
+        append_rec(b, kTL, pass, qs_, qt_, OG(b, kSG, qs_), nullptr);
+    }
+}
+
+// phase B on the fewer than 32 candidates left in the queue
+__device__ __forceinline__ void tl_queue_drain(const BatchDev& b, const TLQueue& q, int& qn, bool nm1) {
+    const int lane = threadIdx.x & 31;
+    bool pass = false;
+    int qs_ = 0, qt_ = 0;
+    if (lane < qn) {
+        qs_ = q.s[lane];
+        qt_ = q.t[lane];
+        const SGV S = load_sgv(b.sgpack, qs_);
+        const SGV T = load_sgv(b.sgpack, qt_);
+        pass = tl_phaseB(q.algo[lane], S, T, q.cut[lane], q.muls[lane], nm1);
+    }
+    __syncwarp();
+    append_rec(b, kTL, pass, qs_, qt_, pass ? OG(b, kSG, qs_) : 0, nullptr);
+    qn = 0;
+}
+
+// outer segment of flat tracklet candidate c of inner segment s
+__device__ __forceinline__ int tl_outer_of(const BatchDev& b, bool lay, int s, int64_t q) {
+    return lay ? tl_outer_layer(b, s, q) : tl_outer(b, s, q);
+}
+
 // Tracklet candidates (Event.cc:611-693 with Tracklet.cc:144-2665).  Phase A
 // (float cuts) runs on every candidate; its survivors go to a per-warp queue
 // in shared memory and phase B (the double-precision part) runs on full warps
@@ -659,71 +716,176 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum(BatchDev b) {
     __shared__ float qc[kEnumThreads / 32][kTLQueue];
     __shared__ float qm[kEnumThreads / 32][kTLQueue];
     __shared__ int qa[kEnumThreads / 32][kTLQueue];
+    const TLQueue q{qs[w], qt[w], qc[w], qm[w], qa[w]};
     int qn = 0;  // warp-uniform queue length
-    bool more = true;
-    while (more || qn > 0) {
-        if (more) {
-            unsigned long long t = 0;
-            if (lane == 0) t = atomicAdd(b.task + kTL, 1ull);
-            t = __shfl_sync(0xffffffffu, t, 0);
-            if ((int64_t)t >= ntask) {
-                more = false;
-            } else {
-                const int64_t base = (int64_t)t * kTask;
-                const int64_t end = min(base + kTask, total);
-                int ilo = 0;
-                if (lane < 2) ilo = find_obj(b, off, offlim, 0, (int)nobj - 1, lane == 0 ? base : end - 1);
-                const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
-                const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
-                for (int r = 0; r < kTask / kWarp; ++r) {
-                    const int64_t c = base + r * kWarp + lane;
-                    int algo = kAlgoNone, s = 0, tt = 0;
-                    float cut = 0.f, muls = 0.f;
-                    if (c < end) {
-                        s = (i0 == i1) ? i0 : find_obj(b, off, offlim, i0, i1, c);
-                        tt = lay ? tl_outer_layer(b, s, c - AT(off, s, offlim)) : tl_outer(b, s, c - AT(off, s, offlim));
-                        (void)IX(s, b.obj[kSG].cap);
-                        (void)IX(tt, b.obj[kSG].cap);
-                        const SGV S = load_sgv(b.sgpack, s);
-                        const SGV T = load_sgv(b.sgpack, tt);
-                        algo = tl_phaseA(S, T, cut, muls);
-                    }
-                    const unsigned m = __ballot_sync(0xffffffffu, algo != kAlgoNone);
-                    if (algo != kAlgoNone) {
-                        const int p = qn + __popc(m & ((1u << lane) - 1u));
-                        qs[w][p] = s; qt[w][p] = tt; qc[w][p] = cut; qm[w][p] = muls; qa[w][p] = algo;
-                    }
-                    qn += __popc(m);
-                    __syncwarp();
-                    if (qn >= kWarp) {
-                        // phase B on the last 32 queued candidates
-                        const int k = qn - kWarp + lane;
-                        const int qs_ = qs[w][k], qt_ = qt[w][k], qa_ = qa[w][k];
-                        const float qc_ = qc[w][k], qm_ = qm[w][k];
-                        __syncwarp();
-                        qn -= kWarp;
-                        const SGV S = load_sgv(b.sgpack, qs_);
-                        const SGV T = load_sgv(b.sgpack, qt_);
-                        const bool pass = tl_phaseB(qa_, S, T, qc_, qm_, nm1);
-                        append_rec(b, kTL, pass, qs_, qt_, OG(b, kSG, qs_), nullptr);
-                    }
-                }
-                continue;
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(b.task + kTL, 1ull);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if ((int64_t)t >= ntask) break;
+        const int64_t base = (int64_t)t * kTask;
+        const int64_t end = min(base + kTask, total);
+        int ilo = 0;
+        if (lane < 2) ilo = find_obj(b, off, offlim, 0, (int)nobj - 1, lane == 0 ? base : end - 1);
+        const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
+        const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
+        for (int r = 0; r < kTask / kWarp; ++r) {
+            const int64_t c = base + r * kWarp + lane;
+            int algo = kAlgoNone, s = 0, tt = 0;
+            float cut = 0.f, muls = 0.f;
+            if (c < end) {
+                s = (i0 == i1) ? i0 : find_obj(b, off, offlim, i0, i1, c);
+                tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
+                (void)IX(s, b.obj[kSG].cap);
+                (void)IX(tt, b.obj[kSG].cap);
+                const SGV S = load_sgv(b.sgpack, s);
+                const SGV T = load_sgv(b.sgpack, tt);
+                algo = tl_phaseA(S, T, cut, muls);
+            }
+            tl_queue_push(b, q, qn, algo, s, tt, cut, muls, nm1);
+        }
+    }
+    tl_queue_drain(b, q, qn, nm1);
+}
+
+constexpr int kMlpWarps = kMlpTile / 32;
+
+// Tracklet candidates behind the learned pre-filter (no counterpart in the
+// reference).  The CTA takes 128 consecutive candidates at a time and scores
+// them as one tensor-core tile; a candidate whose logit reaches the threshold
+// goes through phase A and phase B exactly as in k_tl_enum, the others are
+// dropped.  Control flow around the tile is uniform over the CTA.
+__global__ void __launch_bounds__(kMlpTile) k_tl_enum_mlp(BatchDev b) {
+    __shared__ MlpSmem sm;
+    __shared__ int qs[kMlpWarps][kTLQueue];
+    __shared__ int qt[kMlpWarps][kTLQueue];
+    __shared__ float qc[kMlpWarps][kTLQueue];
+    __shared__ float qm[kMlpWarps][kTLQueue];
+    __shared__ int qa[kMlpWarps][kTLQueue];
+    __shared__ long long s_task;
+    __shared__ int s_go;
+    if (threadIdx.x == 0) s_go = !halted(b) && n_inner(b, kTL) > 0;
+    __syncthreads();
+    if (!s_go) return;
+    const int64_t nobj = n_inner(b, kTL);
+    const int64_t* off = b.cand[kTL];
+    const int64_t offlim = b.cand_cap[kTL] + 1;
+    const int64_t total = AT(off, nobj, offlim);
+    const int64_t ntask = (total + kMlpTile - 1) / kMlpTile;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const bool nm1 = (b.flags & kFlagTLNm1) != 0;
+    const bool lay = (b.flags & kFlagTLLayers) != 0;
+    const TLQueue q{qs[w], qt[w], qc[w], qm[w], qa[w]};
+    mlp_setup(sm, b.mlp_pack);
+    const float thr = reinterpret_cast<const float*>(sm.w + kPackB3)[1];
+    MlpThread st;
+    int qn = 0;
+    unsigned n_scored = 0, n_kept = 0, n_passA = 0;
+    for (;;) {
+        if (threadIdx.x == 0) s_task = (long long)atomicAdd(b.task + kTL, 1ull);
+        __syncthreads();
+        const int64_t t = s_task;
+        if (t >= ntask) break;
+        const int64_t base = t * kMlpTile;
+        const int64_t end = min(base + kMlpTile, total);
+        const int64_t wbase = base + kWarp * w;
+        int ilo = 0;
+        if (lane < 2 && wbase < end) ilo = find_obj(b, off, offlim, 0, (int)nobj - 1, lane == 0 ? wbase : min(wbase + kWarp, end) - 1);
+        const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
+        const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
+        const int64_t c = wbase + lane;
+        const bool valid = c < end;
+        int s = 0, tt = 0;
+        float f[kMlpIn];
+        if (valid) {
+            s = (i0 == i1) ? i0 : find_obj(b, off, offlim, i0, i1, c);
+            tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
+            (void)IX(s, b.obj[kSG].cap);
+            (void)IX(tt, b.obj[kSG].cap);
+            tl_features(load_sgv(b.sgpack, s), load_sgv(b.sgpack, tt), f);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kMlpIn; ++k) f[k] = 0.f;
+        }
+        const float z = mlp_tile(sm, f, st);
+        const bool keep = valid && z >= thr;
+        int algo = kAlgoNone;
+        float cut = 0.f, muls = 0.f;
+        if (keep) algo = tl_phaseA(load_sgv(b.sgpack, s), load_sgv(b.sgpack, tt), cut, muls);
+        n_scored += valid;
+        n_kept += keep;
+        n_passA += algo != kAlgoNone;
+        tl_queue_push(b, q, qn, algo, s, tt, cut, muls, nm1);
+    }
+    tl_queue_drain(b, q, qn, nm1);
+    n_scored = __reduce_add_sync(0xffffffffu, n_scored);
+    n_kept = __reduce_add_sync(0xffffffffu, n_kept);
+    n_passA = __reduce_add_sync(0xffffffffu, n_passA);
+    if (lane == 0) {
+        atomicAdd(&b.mlp_stats->scored, (unsigned long long)n_scored);
+        atomicAdd(&b.mlp_stats->kept, (unsigned long long)n_kept);
+        atomicAdd(&b.mlp_stats->passA, (unsigned long long)n_passA);
+    }
+    if (st.abort && threadIdx.x == 0) {
+        atomicAdd(&b.mlp_stats->timeouts, 1ull);
+        atomicOr(b.status, kStatusMlpTimeout);
+    }
+    mlp_teardown(sm, st);
+}
+
+__device__ __forceinline__ float hash_unit(unsigned long long c, unsigned long long seed) {
+    // splitmix64 finaliser (Steele, Lea, Flood 2014)
+    unsigned long long z = c + seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (float)(z >> 40) * (1.0f / 16777216.0f);
+}
+
+// Training samples for the learned pre-filter: the features of every
+// tracklet candidate of the last run that passes phase A, labelled by phase
+// B (the plain chain's accept / reject); rejected ones are kept with
+// probability neg_keep.
+__global__ void k_tl_collect(BatchDev b, MlpCollect col) {
+    if (halted(b)) return;
+    const int64_t nobj = n_inner(b, kTL);
+    if (nobj <= 0) return;
+    const int64_t* off = b.cand[kTL];
+    const int64_t offlim = b.cand_cap[kTL] + 1;
+    const int64_t total = AT(off, nobj, offlim);
+    const bool lay = (b.flags & kFlagTLLayers) != 0;
+    const int lane = threadIdx.x & 31;
+    for (int64_t c0 = (int64_t)blockIdx.x * blockDim.x; c0 < total; c0 += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = c0 + threadIdx.x;
+        bool keep = false;
+        float label = 0.f;
+        float f[kMlpIn];
+        if (c < total) {
+            const int s = find_obj(b, off, offlim, 0, (int)nobj - 1, c);
+            const int tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
+            const SGV S = load_sgv(b.sgpack, s);
+            const SGV T = load_sgv(b.sgpack, tt);
+            float cut = 0.f, muls = 0.f;
+            const int algo = tl_phaseA(S, T, cut, muls);
+            if (algo != kAlgoNone) {
+                const bool pass = tl_phaseB(algo, S, T, cut, muls, false);
+                label = pass ? 1.f : 0.f;
+                keep = pass || hash_unit((unsigned long long)c, col.seed) < col.neg_keep;
+                if (keep) tl_features(S, T, f);
             }
         }
-        // drain: fewer than 32 queued candidates left
-        bool pass = false;
-        int qs_ = 0, qt_ = 0;
-        if (lane < qn) {
-            qs_ = qs[w][lane];
-            qt_ = qt[w][lane];
-            const SGV S = load_sgv(b.sgpack, qs_);
-            const SGV T = load_sgv(b.sgpack, qt_);
-            pass = tl_phaseB(qa[w][lane], S, T, qc[w][lane], qm[w][lane], nm1);
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (!m) continue;
+        const int leader = __ffs(m) - 1;
+        unsigned long long p0 = 0;
+        if (lane == leader) p0 = atomicAdd(col.n, (unsigned long long)__popc(m));
+        p0 = __shfl_sync(0xffffffffu, p0, leader);
+        const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));
+        if (keep && pos < col.cap) {
+#pragma unroll
+            for (int k = 0; k < kMlpIn; ++k) col.x[pos * kMlpIn + k] = f[k];
+            col.y[pos] = label;
         }
-        __syncwarp();
-        append_rec(b, kTL, pass, qs_, qt_, pass ? OG(b, kSG, qs_) : 0, nullptr);
-        qn = 0;
     }
 }
 
@@ -1040,7 +1202,8 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     if (h) h->launches += 3;
     scan_h(b, b.cand[kTL], b.obj[kSG].mod_cnt + b.n_gm, b.cand_cap[kTL], s, h);
     if (h && h->timed) rec_event(h->enum_start[kTL], s);
-    k_tl_enum<<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
+    if (b.flags & kFlagMLP) k_tl_enum_mlp<<<b.n_sm * 8, kMlpTile, 0, s>>>(b);
+    else k_tl_enum<<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
     if (h && h->timed) rec_event(h->enum_stop[kTL], s);
     k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kTL);
     scan_h(b, b.obj[kTL].mod_cnt, b.n_gm_dev, b.n_gm, s, h);
@@ -1059,6 +1222,10 @@ void launch_tc(const BatchDev& b, cudaStream_t s, Hooks* h) {
     k_tc_cand_counter<<<grid_for(b.n_ev, 128, 1024), 128, 0, s>>>(b);
     if (h) h->launches += 2;
     enum_and_group<TCStage>(b, s, h);
+}
+
+void launch_tl_collect(const BatchDev& b, const MlpCollect& c, cudaStream_t s) {
+    k_tl_collect<<<b.n_sm * 8, 256, 0, s>>>(b, c);
 }
 
 void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s) {

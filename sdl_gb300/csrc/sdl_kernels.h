@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "sdl_mlp.cuh"
 #include "sdl_types.h"
 
 namespace sdlg {
@@ -41,7 +42,9 @@ struct BatchDev {
     unsigned long long* task;      // kNumStages work counters
     int64_t* scan_tmp;
     int64_t scan_tmp_cap;
-    int flags;                     // bit2: DefaultNm1 tracklets
+    int flags;                     // kFlag* bits
+    const unsigned char* mlp_pack; // packed pre-filter weights and threshold (kPackBytes)
+    MlpStats* mlp_stats;           // pre-filter counts of the last run
     int n_sm;
     unsigned long long* dbg;       // bounds-check record (debug builds): count, line, index, limit
 };
@@ -62,6 +65,16 @@ void launch_sg(const BatchDev& b, cudaStream_t s, Hooks* h);
 void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h);
 void launch_tp(const BatchDev& b, cudaStream_t s, Hooks* h);
 void launch_tc(const BatchDev& b, cudaStream_t s, Hooks* h);
+// Training samples for the pre-filter from the last run's tracklet step
+struct MlpCollect {
+    float* x;                  // cap x kMlpIn features
+    float* y;                  // cap labels (1: the tracklet cuts accept)
+    int64_t cap;
+    unsigned long long* n;     // samples found (can exceed cap; nothing past cap is written)
+    float neg_keep;            // probability of keeping a rejected candidate
+    unsigned long long seed;
+};
+void launch_tl_collect(const BatchDev& b, const MlpCollect& c, cudaStream_t s);
 // hit-index tuples of stage st for objects [first, first + n) into out (width 2/4/8/8/16)
 void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s);
 

@@ -1,0 +1,280 @@
+// Learned pre-filter for tracklet candidates (no counterpart in the
+// reference).  A 12-64-64-1 perceptron with ReLU hidden layers scores each
+// (inner segment, outer segment) candidate of the tracklet step before the
+// reference's cuts; a candidate whose logit is below the threshold is dropped
+// and every other one is judged by the exact cuts as before, so the pruned
+// chain's tracklets are a subset of the plain chain's.
+//
+// Numerics (shared by inference and training): features, weights and the
+// first hidden layer are rounded to BF16; every sum accumulates in FP32;
+// the output layer runs in FP32 on BF16-rounded weights.  Inference uses the
+// tensor cores (tcgen05.mma kind::f16, one 128-candidate tile per MMA, FP32
+// accumulators in tensor memory); training uses CUDA-core kernels.
+#pragma once
+#include <cstdint>
+#include <cstring>
+
+namespace sdlg {
+
+constexpr int kMlpIn = 12;      // features per candidate
+constexpr int kMlpK1 = 16;      // first-layer K, padded to the MMA's K
+constexpr int kMlpHid = 64;     // units per hidden layer (the MMAs' N)
+constexpr int kMlpTile = 128;   // candidates per tile (the MMAs' M)
+
+// FP32 parameter vector: W1[64][12], b1[64], W2[64][64], b2[64], w3[64], b3
+constexpr int kMlpW1 = 0;
+constexpr int kMlpB1 = kMlpW1 + kMlpHid * kMlpIn;
+constexpr int kMlpW2 = kMlpB1 + kMlpHid;
+constexpr int kMlpB2 = kMlpW2 + kMlpHid * kMlpHid;
+constexpr int kMlpW3 = kMlpB2 + kMlpHid;
+constexpr int kMlpB3 = kMlpW3 + kMlpHid;
+constexpr int kMlpParams = kMlpB3 + 1;  // 5057
+
+// Packed inference weights, copied into shared memory by every CTA: W1 and
+// W2 in BF16 in the tensor cores' K-major core-matrix layout, then b1, b2,
+// the BF16-rounded w3 and b3 in FP32.
+constexpr int kPackW1 = 0;                                  // 64 x 16 bf16
+constexpr int kPackW2 = kPackW1 + kMlpHid * kMlpK1 * 2;     // 64 x 64 bf16
+constexpr int kPackB1 = kPackW2 + kMlpHid * kMlpHid * 2;
+constexpr int kPackB2 = kPackB1 + kMlpHid * 4;
+constexpr int kPackW3 = kPackB2 + kMlpHid * 4;
+constexpr int kPackB3 = kPackW3 + kMlpHid * 4;
+constexpr int kPackBytes = kPackB3 + 16;                    // 11024, a multiple of 16
+
+// Byte offset of element (row, k) of a K-major BF16 tile without swizzling:
+// 8-row x 16-byte core matrices, `kgroups` of them along K per 8-row group
+// (so the byte stride between core matrices along K is 128 and between 8-row
+// groups kgroups * 128).
+__host__ __device__ constexpr uint32_t cm_offset(int row, int k, int kgroups) {
+    return (uint32_t)((row >> 3) * (kgroups * 128) + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// round-to-nearest-even FP32 -> BF16 bits (finite inputs)
+__host__ __device__ inline uint16_t bf16_bits(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+__host__ __device__ inline float bf16_round(float f) {
+    uint32_t u = (uint32_t)bf16_bits(f) << 16;
+    float r;
+    memcpy(&r, &u, 4);
+    return r;
+}
+
+struct MlpStats {
+    unsigned long long scored;   // candidates scored
+    unsigned long long kept;     // logit >= threshold
+    unsigned long long passA;    // kept and through the float cuts (phase B load)
+    unsigned long long timeouts; // tensor-core waits that gave up
+};
+
+#if defined(__CUDACC__)
+
+// ------------------------------------------------------------------ PTX
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared memory matrix descriptor: start address, byte offset between core
+// matrices along K (lbo) and along M/N (sbo), descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+           (1ull << 46);
+}
+
+// instruction descriptor, kind::f16: FP32 accumulator (bits 4-5 = 1), BF16 A
+// and B (bits 7-9, 10-12 = 1), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
+constexpr uint32_t kIdescBf16M128N64 = (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void tc_alloc(uint32_t* dst, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(dst)), "r"(ncols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tc_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// generic-proxy shared-memory writes -> visible to the tensor cores
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* mbar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(mbar))
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_init(uint64_t* mbar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(mbar)), "r"(1u) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// wait for the mbarrier phase of the given parity, at most ~0.25 s
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
+    const uint32_t a = smem_addr(mbar);
+    uint64_t t0 = 0;
+    for (uint32_t it = 0; it < (1u << 24); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (it == 0) t0 = global_ns();
+        else if ((it & 63u) == 0 && global_ns() - t0 > 250000000ull) return false;
+    }
+    return false;
+}
+// 16 consecutive FP32 columns of this thread's tensor-memory lane
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// ------------------------------------------------------------------ tile
+// Shared memory of one CTA running the tensor-core MLP (128 threads, thread
+// t owns tile row t).
+struct __align__(128) MlpSmem {
+    alignas(128) unsigned char w[kPackBytes];
+    alignas(128) unsigned char a1[kMlpTile * kMlpK1 * 2];    // features, BF16, 2 k-groups
+    alignas(128) unsigned char a2[kMlpTile * kMlpHid * 2];   // hidden layer 1, BF16, 8 k-groups
+    alignas(8) uint64_t mbar;
+    uint32_t tmem;       // base address of 64 tensor-memory columns (both layers' accumulators)
+};
+
+// Per-thread state of the tile loop.  `phase` is the parity of the next
+// mbarrier phase; `abort` turns true (on every thread at the next barrier)
+// once a tensor-core wait gave up, after which no MMA is issued.
+struct MlpThread {
+    uint32_t phase = 0;
+    bool abort = false;
+    bool pending = false;  // an MMA whose completion was not seen may still run
+};
+
+// copy the packed weights, set up the mbarrier and tensor memory (all 128 threads)
+__device__ __forceinline__ void mlp_setup(MlpSmem& sm, const unsigned char* __restrict__ pack) {
+    const uint4* src = reinterpret_cast<const uint4*>(pack);
+    uint4* dst = reinterpret_cast<uint4*>(sm.w);
+    for (int k = threadIdx.x; k < kPackBytes / 16; k += blockDim.x) dst[k] = __ldg(src + k);
+    if (threadIdx.x == 0) mbar_init(&sm.mbar);
+    if (threadIdx.x < 32) tc_alloc(&sm.tmem, 64);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+}
+
+// release tensor memory (all 128 threads; after the last tile), after one
+// more bounded wait for an MMA whose completion was not seen
+__device__ __forceinline__ void mlp_teardown(MlpSmem& sm, MlpThread& st) {
+    if (st.pending) (void)mbar_wait(&sm.mbar, st.phase);
+    tc_fence_before();
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        tc_fence_after();
+        tc_dealloc(sm.tmem, 64);
+    }
+}
+
+// make this thread's shared-memory tile rows visible, issue the MMAs of one
+// layer from thread 0 and wait for them (all threads, uniform control flow).
+// Both layers accumulate into the same 64 columns: the barrier orders every
+// thread's reads of the previous accumulator before the next MMA.
+__device__ __forceinline__ void mlp_layer_sync(MlpSmem& sm, int layer, MlpThread& st) {
+    fence_async_smem();
+    tc_fence_before();
+    if (__syncthreads_or(st.abort ? 1 : 0)) {
+        st.abort = true;
+        return;
+    }
+    if (threadIdx.x == 0) {
+        tc_fence_after();
+        const uint32_t w = smem_addr(sm.w);
+        if (layer == 0) {
+            tc_mma(sm.tmem, smem_desc(smem_addr(sm.a1), 128, 256), smem_desc(w + kPackW1, 128, 256), kIdescBf16M128N64, 0);
+        } else {
+            const uint32_t a2 = smem_addr(sm.a2);
+#pragma unroll
+            for (int kc = 0; kc < 4; ++kc)
+                tc_mma(sm.tmem, smem_desc(a2 + 256 * kc, 128, 1024), smem_desc(w + kPackW2 + 256 * kc, 128, 1024),
+                       kIdescBf16M128N64, kc > 0 ? 1u : 0u);
+        }
+        tc_commit(&sm.mbar);
+    }
+    if (mbar_wait(&sm.mbar, st.phase)) {
+        st.phase ^= 1u;
+    } else {
+        st.abort = true;
+        st.pending = true;
+    }
+    tc_fence_after();
+}
+
+// One tile: thread t scores the features x of its candidate (rounded to
+// BF16 here) and gets the logit.  Every thread of the 128-thread CTA calls
+// it.  After an abort the logit is meaningless.
+__device__ __forceinline__ float mlp_tile(MlpSmem& sm, const float* x, MlpThread& st) {
+    const int t = threadIdx.x;
+    {
+        uint32_t q[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float lo = 2 * j < kMlpIn ? x[2 * j] : 0.f;
+            const float hi = 2 * j + 1 < kMlpIn ? x[2 * j + 1] : 0.f;
+            q[j] = (uint32_t)bf16_bits(lo) | ((uint32_t)bf16_bits(hi) << 16);
+        }
+        *reinterpret_cast<uint4*>(sm.a1 + cm_offset(t, 0, 2)) = make_uint4(q[0], q[1], q[2], q[3]);
+        *reinterpret_cast<uint4*>(sm.a1 + cm_offset(t, 8, 2)) = make_uint4(q[4], q[5], q[6], q[7]);
+    }
+    mlp_layer_sync(sm, 0, st);
+    const uint32_t lane_base = sm.tmem + ((uint32_t)(t & ~31) << 16);
+    const float* b1 = reinterpret_cast<const float*>(sm.w + kPackB1);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        float v[16];
+        tc_ld16(lane_base + 16 * c, v);
+        uint32_t q[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float h0 = fmaxf(__fadd_rn(v[2 * j], b1[16 * c + 2 * j]), 0.f);
+            const float h1 = fmaxf(__fadd_rn(v[2 * j + 1], b1[16 * c + 2 * j + 1]), 0.f);
+            q[j] = (uint32_t)bf16_bits(h0) | ((uint32_t)bf16_bits(h1) << 16);
+        }
+        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c, 8)) = make_uint4(q[0], q[1], q[2], q[3]);
+        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c + 8, 8)) = make_uint4(q[4], q[5], q[6], q[7]);
+    }
+    mlp_layer_sync(sm, 1, st);
+    const float* b2 = reinterpret_cast<const float*>(sm.w + kPackB2);
+    const float* w3 = reinterpret_cast<const float*>(sm.w + kPackW3);
+    float z = *reinterpret_cast<const float*>(sm.w + kPackB3);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+        float v[16];
+        tc_ld16(lane_base + 16 * c, v);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) z = __fmaf_rn(w3[16 * c + j], fmaxf(__fadd_rn(v[j], b2[16 * c + j]), 0.f), z);
+    }
+    return z;
+}
+
+#endif  // __CUDACC__
+
+}  // namespace sdlg

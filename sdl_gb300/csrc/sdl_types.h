@@ -57,6 +57,7 @@ enum : int {
     kFlagSGLayers = 1,   // createSegments: layer-pair segments
     kFlagTLLayers = 2,   // createTracklets: layer-pair tracklets
     kFlagTLNm1 = 4,      // DefaultNm1_TLAlgo
+    kFlagMLP = 16,       // learned pre-filter ahead of the tracklet cuts
 };
 
 // Per-stage status word bits
@@ -68,6 +69,7 @@ enum : uint32_t {
     kStatusOverflowTC = 1u << 4,
     kStatusUnknownModule = 1u << 8,
     kStatusPhiLoop = 1u << 9,
+    kStatusMlpTimeout = 1u << 10,  // a tensor-core wait of the pre-filter gave up
 };
 
 }  // namespace sdlg
