@@ -3,13 +3,18 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-Workload (the configuration the events/s metric is quoted on): the plain
-chain createMiniDoublets -> createSegmentsWithModuleMap ->
-createTrackletsWithModuleMap -> createTriplets -> createTrackCandidates on
-one PU200-like event per step (full synthetic geometry: barrel with tilted
-layers 1-3 and 5 endcap disks per side; 7,000 helices pT = 0.6 + Exp(0.7) GeV
-plus 20 signal helices, |eta| < 2.5, 2 % noise hits).  The batched form
-(64 events of PU 50-250 in one launch sequence) is reported beside it.
+Headline workload (events/s): the batched chain with the learned tracklet
+pre-filter on 128 events of uneven size, PU drawn uniformly in 150-300, full
+synthetic geometry (barrel with tilted layers 1-3, 5 endcap disks per side;
+per PU unit 35 helices pT = 0.6 + Exp(0.7) GeV, plus 20 signal helices,
+|eta| < 2.5, 2 % noise hits), all events in one launch sequence per stage
+replayed from a CUDA graph: createMiniDoublets -> createSegmentsWithModuleMap
+-> createTrackletsWithModuleMap (pre-filter + exact cuts) -> createTriplets
+-> createTrackCandidates.  In the same line: the plain batched chain on the
+same events (no pre-filter) and the track-candidate recall of the pruned
+chain against it, and the plain chain on one PU200-like event per step (the
+configuration whose object sets are checked bit for bit against the
+reference).
 
 One JSON line is printed by rank 0.  Under torchrun every rank runs its own
 events (weak scaling, no collective on the data path); the barrier and the
@@ -17,7 +22,8 @@ max over ranks use gloo on the host.
 
 --impl reference times the reference algorithm on the host cores: the CPU
 restatement in oracle/ (the reference's own sources cannot be built on the
-GPU host), run on all host threads, one bounded sample of events per step.
+GPU host), run on all host threads, one bounded sample of events of the
+headline workload per step.
 """
 from __future__ import annotations
 
@@ -35,10 +41,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "events/s at PU200-like density, plain vs batched+MLP-pruned at ≥99.5% TC recall"
-WORKLOAD = ("plain chain, 1 PU200-like event per step: full synthetic geometry (tilted barrel L1-3, "
-            "5 endcap disks/side), 7,000 helices pT=0.6+Exp(0.7) GeV + 20 signal, |eta|<2.5, 2% noise")
-BATCH_WORKLOAD = "batched plain chain: 64 events of PU uniform in 50-250, one launch sequence per stage"
+WORKLOAD = ("batched + MLP-pruned chain: 128 events of PU uniform in 150-300 (full synthetic geometry: tilted "
+            "barrel L1-3, 5 endcap disks/side; 35 helices per PU unit pT=0.6+Exp(0.7) GeV + 20 signal, |eta|<2.5, "
+            "2% noise), one launch sequence per stage from a CUDA graph, learned pre-filter ahead of the tracklet cuts")
+SINGLE_WORKLOAD = ("plain chain, 1 PU200-like event per step (7,000 helices + 20 signal, 2% noise), "
+                   "object sets identical to the reference")
+MLP_WEIGHTS = os.path.join(ROOT, "sdl_gb300", "weights", "tl_mlp_pu.npz")
 FALLBACK_HBM_GBS = 6800.0
+FALLBACK_BF16_TFLOPS = 1900.0
+MLP_FLOPS_PER_CANDIDATE = 2 * (16 * 64 + 64 * 64 + 64)  # the two MMAs (K padded to 16) and the output layer
 
 
 def dist():
@@ -160,23 +171,30 @@ class L2Flush:
 
 
 def peaks():
+    """(HBM GB/s, bf16 TFLOP/s sustained, source)"""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
         with open(path) as f:
             d = json.load(f)
-        return float(d["hbm_gbs"]), "measured"
+        tf = float(d.get("bf16_tflops_sustained") or d.get("bf16_tflops") or FALLBACK_BF16_TFLOPS)
+        return float(d["hbm_gbs"]), tf, "measured"
     except Exception:
-        return FALLBACK_HBM_GBS, "fallback"
+        return FALLBACK_HBM_GBS, FALLBACK_BF16_TFLOPS, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per event of the tracklet kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "tl_kernel_traffic.json")
+def ncu_traffic(name):
+    """DRAM bytes per algorithmic byte of a kernel from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
     try:
         with open(path) as f:
             return json.load(f)
     except Exception:
         return None
+
+
+def headline_pus(rank, n):
+    import numpy as np
+    return np.random.default_rng(4242 + rank).uniform(150.0, 300.0, size=n)
 
 
 def cpu_sample(events, threads):
@@ -196,7 +214,9 @@ def run_reference_arm(a, rank, world, pg):
     import oracle
     oracle.build()
     n_ev = max(1, threads)
-    events = make_events([(5000 + k, 200.0) for k in range(n_ev)], threads)
+    # the first events of the headline workload (same seeds and PU draws)
+    pus = headline_pus(0, 128)
+    events = make_events([(1000 + 500 + k, float(pus[k])) for k in range(n_ev)], threads)
     for _ in range(a.warmup):
         cpu_sample(events[: max(1, threads // 4)], threads)
     rates, secs = [], []
@@ -206,7 +226,8 @@ def run_reference_arm(a, rank, world, pg):
         secs.append(dt)
     total = sum(secs)
     value = a.steps * n_ev / total
-    sample = "%d PU200-like events per step (seeds 5000-%d), whole chain per event, %d host threads" % (n_ev, 5000 + n_ev - 1, threads)
+    sample = ("%d events of the headline workload per step (PU 150-300), plain chain per event (the reference has "
+              "no pre-filter), %d host threads" % (n_ev, threads))
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "events/s", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1e3 * total / a.steps, 3), "higher_is_better": True,
@@ -218,13 +239,26 @@ def run_reference_arm(a, rank, world, pg):
     print(json.dumps(line), flush=True)
 
 
+def timed_runs(ch, flags, steps, flush):
+    """device ms per run (CUDA events around the chain on its stream)"""
+    out, stage, tl = [], [], []
+    for _ in range(steps):
+        flush()
+        ch.run(4, flags)
+        t = ch.times()
+        out.append(float(t[6]))
+        stage.append(t[:6].copy())
+        tl.append(float(ch.kernel_times()[2]))
+    return out, stage, tl
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
-    ap.add_argument("--batch-events", type=int, default=64)
+    ap.add_argument("--batch-events", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
@@ -238,114 +272,117 @@ def main():
     threads = os.cpu_count() or 1
     # ---- inputs (generated before any CUDA call) ----------------------------
     base = 1000 + 997 * rank
-    n_e2e = 8
-    single = make_events([(base + k, 200.0) for k in range(n_e2e)], threads)
-    rng = np.random.default_rng(4242 + rank)
-    batch_pus = rng.uniform(50.0, 250.0, size=a.batch_events) if a.batch_events > 0 else []
-    batch = make_events([(base + 500 + k, float(p)) for k, p in enumerate(batch_pus)], threads)
+    pus = headline_pus(rank, a.batch_events)
+    batch = make_events([(base + 500 + k, float(p)) for k, p in enumerate(pus)], threads)
+    single = make_events([(base + k, 200.0) for k in range(4)], threads)
     cpu_events = []
     if rank == 0 and not a.no_cpu_baseline:
-        cpu_events = make_events([(7000 + k, 200.0) for k in range(max(1, threads))], threads)
+        cpu_events = batch[:max(1, threads)]
 
     from __graft_entry__ import build
     build()
-    from sdl_gb300 import Chain
+    from sdl_gb300 import FLAG_MLP, Chain, mlp
+    if not os.path.exists(MLP_WEIGHTS):
+        raise SystemExit("missing pre-filter parameters: %s" % MLP_WEIGHTS)
+    params, thr, meta = mlp.load(MLP_WEIGHTS)
     det = synth.detector("full")
     ch = Chain(local)
     ch.upload_detector(det)
+    ch.mlp_set_params(params, thr)
     flush = L2Flush(local)
 
-    # ---- device-resident plain chain: 1 event per step ----------------------
-    ev = single[0]
-    ch.set_events([ev])
+    # ---- headline: batched + pre-filter, device-resident inputs --------------
+    ch.set_events(batch)
     for _ in range(a.warmup):
-        ch.run(4)
-    counts = ch.counts(0)
+        ch.run(4, FLAG_MLP)
+    n_pruned = ch.counts(-1)
+    mstats = ch.mlp_stats()
     clocks = Clocks(local)
     barrier(pg)
-    step_ms, tl_ms, stage_ms = [], [], []
     t_wall0 = time.perf_counter()
-    for _ in range(a.steps):
-        flush()
-        ch.run(4)
-        t = ch.times()
-        step_ms.append(float(t[6]))
-        stage_ms.append(t[:6].copy())
-        tl_ms.append(float(ch.kernel_times()[2]))
+    step_ms, stage_ms, tl_ms = timed_runs(ch, FLAG_MLP, a.steps, flush)
     wall = time.perf_counter() - t_wall0
     barrier(pg)
     clk = clocks.stop()
     launches = ch.launches
     mean_ms = allmax(pg, statistics.fmean(step_ms))
-    value = allsum(pg, 1.0) * 1e3 / mean_ms  # every rank processes one event per step
+    value = allsum(pg, len(batch)) * 1e3 / mean_ms
+    hl_stage = np.mean(np.array(stage_ms), axis=0)
 
-    # ---- end to end through the C ABI: host buffers in, track candidates out --
-    n_max = max(len(e) for e in single)
-    pin = ch.pinned(n_max * 20 + 64)
-    evoff = np.zeros(2, dtype=np.int64)
+    # ---- the plain batched chain on the same events --------------------------
+    for _ in range(2):
+        ch.run(4, 0)
+    n_plain = ch.counts(-1)
+    p_ms, p_stage, p_tl = timed_runs(ch, 0, max(3, a.steps // 4), flush)
+    p_mean = allmax(pg, statistics.fmean(p_ms))
+    tc_rec = float(n_pruned[4]) / max(1.0, float(n_plain[4]))
+    tl_rec = float(n_pruned[2]) / max(1.0, float(n_plain[2]))
+    plain_batched = {"value": round(allsum(pg, len(batch)) * 1e3 / p_mean, 3), "unit": "events/s",
+                     "ms_per_step": round(p_mean, 3), "objects_per_step": [int(v) for v in n_plain],
+                     "stage_ms": [round(float(v), 3) for v in np.mean(np.array(p_stage), axis=0)],
+                     "tl_kernel_ms": round(statistics.fmean(p_tl), 3)}
 
-    def stage_host(e):
-        n = len(e)
-        views = []
-        for k, (arr, dt) in enumerate(((e.x, np.float32), (e.y, np.float32), (e.z, np.float32), (e.idx, np.int32),
-                                       (e.detid, np.uint32))):
-            v = pin[k * n * 4:(k + 1) * n * 4].view(dt)
-            v[:] = arr
-            views.append(v)
-        return views
-
-    e2e_ms, h2d, d2h = [], [], []
+    # ---- end to end through the C ABI: pinned host buffers in, track
+    # candidates out, for the whole batch each step -----------------------------
+    n_hit = int(sum(len(e) for e in batch))
+    pin = ch.pinned(n_hit * 20 + 64)
+    evoff = np.zeros(len(batch) + 1, dtype=np.int64)
+    evoff[1:] = np.cumsum([len(e) for e in batch])
+    views = []
+    for k, (attr, dt) in enumerate((("x", np.float32), ("y", np.float32), ("z", np.float32), ("idx", np.int32),
+                                    ("detid", np.uint32))):
+        v = pin[k * n_hit * 4:(k + 1) * n_hit * 4].view(dt)
+        v[:] = np.concatenate([getattr(e, attr) for e in batch])
+        views.append(v)
+    e2e_ms, d2h = [], []
     for k in range(a.warmup + a.steps):
-        e = single[k % n_e2e]
-        views = stage_host(e)  # host-side preparation of the caller's pinned buffers (not timed)
-        evoff[1] = len(e)
         flush()
         t0 = time.perf_counter()
-        ch.set_events_raw(1, evoff.ctypes.data, *[v.ctypes.data for v in views])
-        ch.run(4)
-        tc = ch.objects(4, 0)
+        ch.set_events_raw(len(batch), evoff.ctypes.data, *[v.ctypes.data for v in views])
+        ch.run(4, FLAG_MLP)
+        tc = ch.objects(4, -1)
         t1 = time.perf_counter()
         if k >= a.warmup:
             e2e_ms.append((t1 - t0) * 1e3)
-            h2d.append(len(e) * 20 + 16)
             d2h.append(tc.nbytes + 8 * 2)
     e2e_mean = allmax(pg, statistics.fmean(e2e_ms))
-    e2e_value = allsum(pg, 1.0) * 1e3 / e2e_mean
+    e2e_value = allsum(pg, len(batch)) * 1e3 / e2e_mean
 
-    # ---- batched chain ---------------------------------------------------------
-    batched = None
-    if batch:
-        ch.set_events(batch)
-        for _ in range(a.warmup):
-            ch.run(4)
-        bms = []
-        for _ in range(max(3, a.steps // 2)):
-            flush()
-            ch.run(4)
-            bms.append(float(ch.times()[6]))
-        bmean = allmax(pg, statistics.fmean(bms))
-        btot = ch.counts(-1)
-        batched = {"value": round(allsum(pg, len(batch)) * 1e3 / bmean, 2), "unit": "events/s",
-                   "ms_per_step": round(bmean, 3), "events_per_step": len(batch), "workload": BATCH_WORKLOAD,
-                   "hits_per_step": int(sum(len(e) for e in batch)), "objects_per_step": [int(v) for v in btot],
-                   "stage_ms": [round(float(v), 3) for v in ch.times()[:6]]}
+    # ---- plain chain, one PU200-like event per step --------------------------
+    ev = single[0]
+    ch.set_events([ev])
+    for _ in range(a.warmup):
+        ch.run(4, 0)
+    s_counts = ch.counts(0)
+    s_ms, s_stage, s_tl = timed_runs(ch, 0, a.steps, flush)
+    s_mean = allmax(pg, statistics.fmean(s_ms))
+    s_st = np.mean(np.array(s_stage), axis=0)
+    plain_single = {"value": round(allsum(pg, 1.0) * 1e3 / s_mean, 3), "unit": "events/s", "ms_per_step": round(s_mean, 4),
+                    "workload": SINGLE_WORKLOAD, "hits_per_event": len(ev),
+                    "objects_per_event": [int(v) for v in s_counts],
+                    "stage_ms": {k: round(float(v), 4) for k, v in zip(("ingest", "MD", "SG", "TL", "TP", "TC"), s_st)},
+                    "tl_kernel_ms": round(statistics.fmean(s_tl), 4)}
 
-    # ---- roofline of the dominant kernel (tracklet candidate evaluation) -----
-    hbm, src = peaks()
+    # ---- roofline of the dominant kernel of the headline run -----------------
+    # k_tl_enum_mlp: algorithmic bytes = segments read once (28 B) + tracklets
+    # written once (8 B); tensor work = the pre-filter's MMAs per candidate
+    hbm, tflops, src = peaks()
     tl_mean = statistics.fmean(tl_ms)
-    n_sg, n_tl = int(counts[1]), int(counts[2])
-    alg_bytes = 28 * n_sg + 8 * n_tl  # segments read once (28 B) + tracklets written once (8 B)
+    n_sg, n_tl = int(n_pruned[1]), int(n_pruned[2])
+    alg_bytes = 28 * n_sg + 8 * n_tl
     achieved = alg_bytes / (tl_mean * 1e-3) / 1e9
-    tr = ncu_traffic()
+    tr = ncu_traffic("tl_mlp_kernel_traffic.json")
     traffic = None
     if tr and tr.get("traffic_per_algorithmic_byte"):
-        # DRAM bytes of one ncu capture of this kernel, scaled to this launch
-        # by the algorithmic bytes (segments read, tracklets written)
         traffic = int(alg_bytes * float(tr["traffic_per_algorithmic_byte"]))
+    mma_tflops = mstats["scored"] * MLP_FLOPS_PER_CANDIDATE / (tl_mean * 1e-3) / 1e12
     roofline = {"bound": "hbm", "achieved": round(achieved, 3), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 6), "traffic": traffic, "peak_source": src,
-                "kernel": "k_tl_enum (tracklet cuts)", "kernel_ms": round(tl_mean, 4),
+                "kernel": "k_tl_enum_mlp (pre-filter + tracklet cuts)", "kernel_ms": round(tl_mean, 3),
                 "algorithmic_bytes": alg_bytes,
+                "tensor": {"achieved": round(mma_tflops, 2), "peak": tflops, "unit": "TFLOP/s",
+                           "frac": round(mma_tflops / tflops, 5), "flops_per_candidate": MLP_FLOPS_PER_CANDIDATE,
+                           "candidates": mstats["scored"]},
                 "note": "latency/FP64-bound candidate evaluation; HBM bytes are small by construction"}
 
     # ---- CPU baseline (rank 0) -----------------------------------------------
@@ -353,26 +390,31 @@ def main():
     if rank == 0 and cpu_events:
         r, dt, _ = cpu_sample(cpu_events, threads)
         cpu = {"value": round(r, 4), "unit": "events/s", "cores": threads, "kind": "port",
-               "sample": "%d PU200-like events through the CPU restatement of the reference chain on %d threads (%.1f s)"
-                         % (len(cpu_events), threads, dt)}
+               "sample": "the first %d events of the headline workload (PU 150-300) through the CPU restatement of "
+                         "the reference chain on %d threads (%.1f s)" % (len(cpu_events), threads, dt)}
 
     if rank == 0:
-        stage = np.mean(np.array(stage_ms), axis=0)
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "events/s", "n_gpus": world, "steps": a.steps,
-            "warmup": a.warmup, "ms_per_step": round(mean_ms, 4), "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "events_per_step": 1, "hits_per_event": len(ev),
-                       "objects_per_event": [int(v) for v in counts], "l2": "flushed between steps (512 MiB memset)",
-                       "stage_ms": {"ingest": round(float(stage[0]), 4), "MD": round(float(stage[1]), 4),
-                                    "SG": round(float(stage[2]), 4), "TL": round(float(stage[3]), 4),
-                                    "TP": round(float(stage[4]), 4), "TC": round(float(stage[5]), 4)},
+            "warmup": a.warmup, "ms_per_step": round(mean_ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64 cuts, bf16 pre-filter", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "events_per_step": len(batch), "hits_per_step": n_hit,
+                       "objects_per_step": [int(v) for v in n_pruned],
+                       "l2": "flushed between steps (512 MiB memset); inputs > L2",
+                       "stage_ms": {k: round(float(v), 3) for k, v in zip(("ingest", "MD", "SG", "TL", "TP", "TC"), hl_stage)},
+                       "prefilter": {"weights": "sdl_gb300/weights/tl_mlp_pu.npz", "threshold": thr,
+                                     "trained_on": "%d events, PU 100-300 (seeds 100000+)" % meta.get("train_events", 0),
+                                     "candidates": mstats["scored"], "kept": mstats["kept"],
+                                     "pruned_fraction": round(1.0 - mstats["kept"] / max(1, mstats["scored"]), 4),
+                                     "passed_float_cuts": mstats["passed_float_cuts"]},
                        "wall_s": round(wall, 3)},
-            "e2e": {"value": round(e2e_value, 3), "unit": "events/s", "ms_per_step": round(e2e_mean, 4),
-                    "h2d_bytes_per_step": int(statistics.fmean(h2d)), "d2h_bytes_per_step": int(statistics.fmean(d2h)),
-                    "path": "sdlg_set_events (pinned host) + sdlg_run + sdlg_get_objects(TC)"},
+            "tc_recall": round(tc_rec, 5), "tl_recall": round(tl_rec, 5),
+            "plain_batched": plain_batched, "plain_single": plain_single,
+            "e2e": {"value": round(e2e_value, 3), "unit": "events/s", "ms_per_step": round(e2e_mean, 3),
+                    "h2d_bytes_per_step": n_hit * 20 + 8 * (len(batch) + 1), "d2h_bytes_per_step": int(statistics.fmean(d2h)),
+                    "path": "sdlg_set_events (pinned host) + sdlg_run(SDLG_FLAG_MLP) + sdlg_get_objects(TC)"},
             "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-            "gpu_launches": int(launches * a.steps), "batched": batched,
+            "gpu_launches": int(launches * a.steps),
         }
         print(json.dumps(line), flush=True)
     ch.close()

@@ -274,6 +274,14 @@ class Chain:
         self._ck(lib().sdlg_mlp_get_samples(self.h, x.ctypes.data, y.ctypes.data, n, ctypes.addressof(m)))
         return x, y
 
+    def mlp_labels(self) -> np.ndarray:
+        """labels of the training set (1: accepted by the tracklet cuts)"""
+        n = self.mlp_num_samples()
+        y = np.empty(n, dtype=np.float32)
+        m = ctypes.c_int64()
+        self._ck(lib().sdlg_mlp_get_samples(self.h, None, y.ctypes.data, n, ctypes.addressof(m)))
+        return y
+
     def mlp_clear_samples(self):
         self._ck(lib().sdlg_mlp_clear_samples(self.h))
 
