@@ -132,6 +132,7 @@ struct sdlg_ctx {
     std::vector<void*> allocs;  // batch allocations
     int64_t cap_hit = 0, cap_ev = 0;
     int64_t cap_obj[kNumStages] = {0, 0, 0, 0, 0};
+    int64_t cap_kept = 0;  // tracklet candidates the pre-filter may keep per run
     bool buffers_ok = false;
     // pinned staging
     void* pinned = nullptr;
@@ -294,6 +295,7 @@ int ensure_buffers(sdlg_ctx* ctx) {
     const int64_t H = std::max<int64_t>(ctx->cap_hit, 1024);
     const int64_t mult[kNumStages] = {1, 2, 3, 4, 2};
     for (int s = 0; s < kNumStages; ++s) ctx->cap_obj[s] = std::max<int64_t>(ctx->cap_obj[s], H * mult[s] + 4096);
+    ctx->cap_kept = std::max<int64_t>(ctx->cap_kept, 8 * H + 4096);
     BatchDev& b = ctx->b;
     b = BatchDev{};
     b.geo.n_mod = n_mod;
@@ -340,6 +342,11 @@ int ensure_buffers(sdlg_ctx* ctx) {
     for (int s = 0; s < kNumStages; ++s) AL(b.cand[s], b.cand_cap[s] + 1);
     AL(b.conn_pref, std::max<int64_t>(1, ctx->n_ev * (int64_t)ctx->conn_idx.size()));
     AL(b.conn_sum, n_gm);
+    b.bucket_cap = (int64_t)1 << 24;  // covers 2^32 candidates of one stage
+    AL(b.bucket, b.bucket_cap);
+    b.kept_cap = ctx->cap_kept;
+    AL(b.kept, b.kept_cap);
+    AL(b.n_kept, 1);
     AL(b.sgpack, ctx->cap_obj[kSG] * PK_N);
     AL(b.counters, ctx->n_ev * 110);
     AL(b.status, 1);
@@ -397,6 +404,7 @@ void enqueue_chain(sdlg_ctx* ctx, int stop_after) {
     // status word and attempted appends for the host's overflow check
     cudaMemcpyAsync(ctx->h_small, b.n_rec, kNumStages * sizeof(int64_t), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(ctx->h_small + kNumStages, b.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(ctx->h_small + kNumStages + 1, b.n_kept, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
 }
 
 #ifdef SDL_DEVICE_CHECKS
@@ -441,6 +449,7 @@ int launch_checked(sdlg_ctx* ctx, int stop_after) {
     }
     cudaMemcpyAsync(ctx->h_small, b.n_rec, kNumStages * sizeof(int64_t), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(ctx->h_small + kNumStages, b.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(ctx->h_small + kNumStages + 1, b.n_kept, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
     return SDLG_OK;
 }
 #endif
@@ -506,7 +515,7 @@ int finish(sdlg_ctx* ctx) {
         }
         if (status & kStatusMlpTimeout)
             return fail(ctx, SDLG_ERR_CUDA, "tracklet pre-filter: a tensor-core wait gave up; results discarded");
-        if (!(status & 0x1fu)) return SDLG_OK;
+        if (!(status & kStatusHalt)) return SDLG_OK;
         // grow every stage that overflowed (the attempted-append counters hold
         // the exact need of the first overflowing stage)
         bool grew = false;
@@ -515,6 +524,11 @@ int finish(sdlg_ctx* ctx) {
                 ctx->cap_obj[s] = std::max<int64_t>(ctx->cap_obj[s] * 2, ctx->h_small[s] + ctx->h_small[s] / 4 + 4096);
                 grew = true;
             }
+        }
+        if (status & kStatusOverflowKept) {
+            const int64_t need = ctx->h_small[kNumStages + 1];
+            ctx->cap_kept = std::max<int64_t>(ctx->cap_kept * 2, need + need / 4 + 4096);
+            grew = true;
         }
         if (!grew) return fail(ctx, SDLG_ERR_CAPACITY, "inconsistent status %u", status);
         ctx->buffers_ok = false;

@@ -48,7 +48,7 @@ constexpr int kScanThreads = 512;
 constexpr int kScanItems = 8;
 constexpr int kScanBlock = kScanThreads * kScanItems;
 
-__device__ __forceinline__ bool halted(const BatchDev& b) { return (*b.status & 0x1fu) != 0; }
+__device__ __forceinline__ bool halted(const BatchDev& b) { return (*b.status & kStatusHalt) != 0; }
 
 // add v to *addr with one atomic per group of lanes sharing the address;
 // every lane of the warp must call it
@@ -68,6 +68,30 @@ __device__ __forceinline__ int find_obj(const BatchDev& b, const int64_t* off, i
         else hi = mid - 1;
     }
     return lo;
+}
+
+// Bucket table of a stage's flat candidate space: bucket[k] is the inner
+// object that holds candidate k * 2^kBucketShift, plus a last entry nobj - 1.
+// A candidate c then lies in an inner object between bucket[c >> shift] and
+// bucket[(c >> shift) + 1], so the enumerators search a few objects instead
+// of all of them.  A table too small for the candidate space is not built
+// and the search covers the whole range.
+constexpr int kBucketShift = 8;
+
+__device__ __forceinline__ bool buckets_ok(const BatchDev& b, int64_t total) {
+    return ((total + (1ll << kBucketShift) - 1) >> kBucketShift) + 1 <= b.bucket_cap;
+}
+
+// search bounds of the inner objects of candidates c0 <= c1
+__device__ __forceinline__ void obj_bounds(const BatchDev& b, int64_t nobj, int64_t total, int64_t c0, int64_t c1, int& lo,
+                                           int& hi) {
+    if (buckets_ok(b, total)) {
+        lo = AT(b.bucket, c0 >> kBucketShift, b.bucket_cap);
+        hi = AT(b.bucket, (c1 >> kBucketShift) + 1, b.bucket_cap);
+    } else {
+        lo = 0;
+        hi = (int)nobj - 1;
+    }
 }
 
 // ------------------------------------------------------------------ scan
@@ -449,7 +473,8 @@ struct SGLayerStage {
 // tracklet candidate q of inner segment s -> outer segment (Event.cc:635-663)
 __device__ __forceinline__ int tl_outer(const BatchDev& b, int s, int64_t q) {
     const int n_mod = b.geo.n_mod;
-    const int g2 = OG(b, kMD, OJ(b, kSG, s));
+    // module of the outer mini-doublet, from the packed segment record
+    const int g2 = __float_as_int(AT(b.sgpack, (int64_t)s * PK_N + PK_G2, b.obj[kSG].cap * PK_N));
     const int ev = g2 / n_mod, m2 = g2 - ev * n_mod;
     int pref;
     const int k = conn_entry(b, ev, m2, q, pref);
@@ -511,6 +536,25 @@ __device__ __forceinline__ int64_t n_inner(const BatchDev& b, int st) {
     }
 }
 
+// bucket table of stage st's scanned candidate offsets
+__global__ void k_cand_buckets(BatchDev b, int st) {
+    if (halted(b)) return;
+    const int64_t nobj = n_inner(b, st);
+    if (nobj <= 0) return;
+    const int64_t* off = b.cand[st];
+    const int64_t offlim = b.cand_cap[st] + 1;
+    const int64_t total = AT(off, nobj, offlim);
+    if (!buckets_ok(b, total)) return;
+    const int64_t nb = (total + (1ll << kBucketShift) - 1) >> kBucketShift;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tid == 0) AT(b.bucket, nb, b.bucket_cap) = (int)(nobj - 1);
+    for (int64_t s = tid; s < nobj; s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t lo = AT(off, s, offlim), hi = AT(off, s + 1, offlim);
+        for (int64_t k = (lo + (1ll << kBucketShift) - 1) >> kBucketShift; (k << kBucketShift) < hi; ++k)
+            AT(b.bucket, k, b.bucket_cap) = (int)s;
+    }
+}
+
 template <class F>
 __global__ void __launch_bounds__(kEnumThreads) k_enum(BatchDev b) {
     constexpr int st = F::kSt;
@@ -532,7 +576,11 @@ __global__ void __launch_bounds__(kEnumThreads) k_enum(BatchDev b) {
         const int64_t base = (int64_t)t * kTask;
         const int64_t end = min(base + kTask, total);
         int ilo = 0;
-        if (lane < 2) ilo = find_obj(b, off, offlim, 0, (int)nobj - 1, lane == 0 ? base : end - 1);
+        if (lane < 2) {
+            int lo, hi;
+            obj_bounds(b, nobj, total, base, end - 1, lo, hi);
+            ilo = find_obj(b, off, offlim, lo, hi, lane == 0 ? base : end - 1);
+        }
         const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
         const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
         for (int r = 0; r < kTask / kWarp; ++r) {
@@ -726,7 +774,11 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum(BatchDev b) {
         const int64_t base = (int64_t)t * kTask;
         const int64_t end = min(base + kTask, total);
         int ilo = 0;
-        if (lane < 2) ilo = find_obj(b, off, offlim, 0, (int)nobj - 1, lane == 0 ? base : end - 1);
+        if (lane < 2) {
+            int lo, hi;
+            obj_bounds(b, nobj, total, base, end - 1, lo, hi);
+            ilo = find_obj(b, off, offlim, lo, hi, lane == 0 ? base : end - 1);
+        }
         const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
         const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
         for (int r = 0; r < kTask / kWarp; ++r) {
@@ -750,18 +802,14 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum(BatchDev b) {
 
 constexpr int kMlpWarps = kMlpTile / 32;
 
-// Tracklet candidates behind the learned pre-filter (no counterpart in the
+// Learned pre-filter of the tracklet candidates (no counterpart in the
 // reference).  The CTA takes 128 consecutive candidates at a time and scores
-// them as one tensor-core tile; a candidate whose logit reaches the threshold
-// goes through phase A and phase B exactly as in k_tl_enum, the others are
-// dropped.  Control flow around the tile is uniform over the CTA.
-__global__ void __launch_bounds__(kMlpTile) k_tl_enum_mlp(BatchDev b) {
+// them as one tensor-core tile; the (inner, outer) segments of every
+// candidate whose logit reaches the threshold are appended to the kept list,
+// which k_tl_exact judges with the reference's cuts.  Control flow around the
+// tile is uniform over the CTA.
+__global__ void __launch_bounds__(kMlpTile) k_tl_prefilter(BatchDev b) {
     __shared__ MlpSmem sm;
-    __shared__ int qs[kMlpWarps][kTLQueue];
-    __shared__ int qt[kMlpWarps][kTLQueue];
-    __shared__ float qc[kMlpWarps][kTLQueue];
-    __shared__ float qm[kMlpWarps][kTLQueue];
-    __shared__ int qa[kMlpWarps][kTLQueue];
     __shared__ long long s_task;
     __shared__ int s_go;
     if (threadIdx.x == 0) s_go = !halted(b) && n_inner(b, kTL) > 0;
@@ -773,14 +821,11 @@ __global__ void __launch_bounds__(kMlpTile) k_tl_enum_mlp(BatchDev b) {
     const int64_t total = AT(off, nobj, offlim);
     const int64_t ntask = (total + kMlpTile - 1) / kMlpTile;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const bool nm1 = (b.flags & kFlagTLNm1) != 0;
     const bool lay = (b.flags & kFlagTLLayers) != 0;
-    const TLQueue q{qs[w], qt[w], qc[w], qm[w], qa[w]};
     mlp_setup(sm, b.mlp_pack);
     const float thr = reinterpret_cast<const float*>(sm.w + kPackB3)[1];
     MlpThread st;
-    int qn = 0;
-    unsigned n_scored = 0, n_kept = 0, n_passA = 0;
+    unsigned n_scored = 0, n_kept = 0;
     for (;;) {
         if (threadIdx.x == 0) s_task = (long long)atomicAdd(b.task + kTL, 1ull);
         __syncthreads();
@@ -790,7 +835,12 @@ __global__ void __launch_bounds__(kMlpTile) k_tl_enum_mlp(BatchDev b) {
         const int64_t end = min(base + kMlpTile, total);
         const int64_t wbase = base + kWarp * w;
         int ilo = 0;
-        if (lane < 2 && wbase < end) ilo = find_obj(b, off, offlim, 0, (int)nobj - 1, lane == 0 ? wbase : min(wbase + kWarp, end) - 1);
+        if (lane < 2 && wbase < end) {
+            const int64_t wlast = min(wbase + kWarp, end) - 1;
+            int lo, hi;
+            obj_bounds(b, nobj, total, wbase, wlast, lo, hi);
+            ilo = find_obj(b, off, offlim, lo, hi, lane == 0 ? wbase : wlast);
+        }
         const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
         const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
         const int64_t c = wbase + lane;
@@ -802,35 +852,74 @@ __global__ void __launch_bounds__(kMlpTile) k_tl_enum_mlp(BatchDev b) {
             tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
             (void)IX(s, b.obj[kSG].cap);
             (void)IX(tt, b.obj[kSG].cap);
-            tl_features(load_sgv(b.sgpack, s), load_sgv(b.sgpack, tt), f);
+            tl_features(feat_in(b.sgpack, s, tt), f);
         } else {
 #pragma unroll
             for (int k = 0; k < kMlpIn; ++k) f[k] = 0.f;
         }
         const float z = mlp_tile(sm, f, st);
         const bool keep = valid && z >= thr;
-        int algo = kAlgoNone;
-        float cut = 0.f, muls = 0.f;
-        if (keep) algo = tl_phaseA(load_sgv(b.sgpack, s), load_sgv(b.sgpack, tt), cut, muls);
         n_scored += valid;
         n_kept += keep;
-        n_passA += algo != kAlgoNone;
-        tl_queue_push(b, q, qn, algo, s, tt, cut, muls, nm1);
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            unsigned long long p0 = 0;
+            if (lane == leader) p0 = atomicAdd(b.n_kept, (unsigned long long)__popc(m));
+            p0 = __shfl_sync(0xffffffffu, p0, leader);
+            const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));
+            if (keep) {
+                if (pos < b.kept_cap) AT(b.kept, pos, b.kept_cap) = make_int2(s, tt);
+                else atomicOr(b.status, kStatusOverflowKept);
+            }
+        }
     }
-    tl_queue_drain(b, q, qn, nm1);
     n_scored = __reduce_add_sync(0xffffffffu, n_scored);
     n_kept = __reduce_add_sync(0xffffffffu, n_kept);
-    n_passA = __reduce_add_sync(0xffffffffu, n_passA);
     if (lane == 0) {
         atomicAdd(&b.mlp_stats->scored, (unsigned long long)n_scored);
         atomicAdd(&b.mlp_stats->kept, (unsigned long long)n_kept);
-        atomicAdd(&b.mlp_stats->passA, (unsigned long long)n_passA);
     }
     if (st.abort && threadIdx.x == 0) {
         atomicAdd(&b.mlp_stats->timeouts, 1ull);
         atomicOr(b.status, kStatusMlpTimeout);
     }
     mlp_teardown(sm, st);
+}
+
+// The reference's tracklet cuts on the candidates the pre-filter kept:
+// phase A on every one, phase B on full warps of its survivors, exactly as
+// k_tl_enum does for all candidates.
+__global__ void __launch_bounds__(kEnumThreads) k_tl_exact(BatchDev b) {
+    if (halted(b)) return;
+    const int64_t n = min((int64_t)*b.n_kept, b.kept_cap);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const bool nm1 = (b.flags & kFlagTLNm1) != 0;
+    __shared__ int qs[kEnumThreads / 32][kTLQueue];
+    __shared__ int qt[kEnumThreads / 32][kTLQueue];
+    __shared__ float qc[kEnumThreads / 32][kTLQueue];
+    __shared__ float qm[kEnumThreads / 32][kTLQueue];
+    __shared__ int qa[kEnumThreads / 32][kTLQueue];
+    const TLQueue q{qs[w], qt[w], qc[w], qm[w], qa[w]};
+    int qn = 0;
+    unsigned n_passA = 0;
+    const int64_t nwarp = (int64_t)gridDim.x * (kEnumThreads / 32);
+    for (int64_t base = ((int64_t)blockIdx.x * (kEnumThreads / 32) + w) * kWarp; base < n; base += nwarp * kWarp) {
+        const int64_t i = base + lane;
+        int algo = kAlgoNone, s = 0, tt = 0;
+        float cut = 0.f, muls = 0.f;
+        if (i < n) {
+            const int2 p = AT(b.kept, i, b.kept_cap);
+            s = p.x;
+            tt = p.y;
+            algo = tl_phaseA(load_sgv(b.sgpack, s), load_sgv(b.sgpack, tt), cut, muls);
+        }
+        n_passA += algo != kAlgoNone;
+        tl_queue_push(b, q, qn, algo, s, tt, cut, muls, nm1);
+    }
+    tl_queue_drain(b, q, qn, nm1);
+    n_passA = __reduce_add_sync(0xffffffffu, n_passA);
+    if (lane == 0 && n_passA) atomicAdd(&b.mlp_stats->passA, (unsigned long long)n_passA);
 }
 
 __device__ __forceinline__ float hash_unit(unsigned long long c, unsigned long long seed) {
@@ -861,7 +950,9 @@ __global__ void k_tl_collect(BatchDev b, MlpCollect col) {
         float label = 0.f;
         float f[kMlpIn];
         if (c < total) {
-            const int s = find_obj(b, off, offlim, 0, (int)nobj - 1, c);
+            int lo, hi;
+            obj_bounds(b, nobj, total, c, c, lo, hi);
+            const int s = find_obj(b, off, offlim, lo, hi, c);
             const int tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
             const SGV S = load_sgv(b.sgpack, s);
             const SGV T = load_sgv(b.sgpack, tt);
@@ -871,7 +962,7 @@ __global__ void k_tl_collect(BatchDev b, MlpCollect col) {
                 const bool pass = tl_phaseB(algo, S, T, cut, muls, false);
                 label = pass ? 1.f : 0.f;
                 keep = pass || hash_unit((unsigned long long)c, col.seed) < col.neg_keep;
-                if (keep) tl_features(S, T, f);
+                if (keep) tl_features(feat_in(S, T), f);
             }
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);
@@ -1153,6 +1244,8 @@ void enum_and_group(const BatchDev& b, cudaStream_t s, Hooks* h, bool layer_coun
         default: ninner_ptr = b.obj[kTL].mod_cnt + b.n_gm;
     }
     scan_h(b, b.cand[st], ninner_ptr, b.cand_cap[st], s, h);
+    k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, st);
+    if (h) h->launches += 1;
     if (h && h->timed) rec_event(h->enum_start[st], s);
     k_enum<F><<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
     if (h && h->timed) rec_event(h->enum_stop[st], s);
@@ -1201,9 +1294,17 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     else k_tl_count<<<b.n_sm * 8, 256, 0, s>>>(b);
     if (h) h->launches += 3;
     scan_h(b, b.cand[kTL], b.obj[kSG].mod_cnt + b.n_gm, b.cand_cap[kTL], s, h);
+    k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, kTL);
+    if (h) h->launches += 1;
     if (h && h->timed) rec_event(h->enum_start[kTL], s);
-    if (b.flags & kFlagMLP) k_tl_enum_mlp<<<b.n_sm * 8, kMlpTile, 0, s>>>(b);
-    else k_tl_enum<<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
+    if (b.flags & kFlagMLP) {
+        cudaMemsetAsync(b.n_kept, 0, sizeof(unsigned long long), s);
+        k_tl_prefilter<<<b.n_sm * 8, kMlpTile, 0, s>>>(b);
+        k_tl_exact<<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
+        if (h) h->launches += 1;
+    } else {
+        k_tl_enum<<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
+    }
     if (h && h->timed) rec_event(h->enum_stop[kTL], s);
     k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kTL);
     scan_h(b, b.obj[kTL].mod_cnt, b.n_gm_dev, b.n_gm, s, h);
@@ -1225,6 +1326,8 @@ void launch_tc(const BatchDev& b, cudaStream_t s, Hooks* h) {
 }
 
 void launch_tl_collect(const BatchDev& b, const MlpCollect& c, cudaStream_t s) {
+    // the bucket table holds the last stage that ran: rebuild the tracklet one
+    k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, kTL);
     k_tl_collect<<<b.n_sm * 8, 256, 0, s>>>(b, c);
 }
 

@@ -42,9 +42,14 @@ struct BatchDev {
     unsigned long long* task;      // kNumStages work counters
     int64_t* scan_tmp;
     int64_t scan_tmp_cap;
+    int32_t* bucket;               // first inner object of every 256 consecutive candidates of the running stage
+    int64_t bucket_cap;
     int flags;                     // kFlag* bits
     const unsigned char* mlp_pack; // packed pre-filter weights and threshold (kPackBytes)
     MlpStats* mlp_stats;           // pre-filter counts of the last run
+    int2* kept;                    // (inner, outer) segments of the tracklet candidates the pre-filter kept
+    int64_t kept_cap;
+    unsigned long long* n_kept;    // kept candidates found (can exceed kept_cap: overflow)
     int n_sm;
     unsigned long long* dbg;       // bounds-check record (debug builds): count, line, index, limit
 };

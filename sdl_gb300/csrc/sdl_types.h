@@ -70,6 +70,8 @@ enum : uint32_t {
     kStatusUnknownModule = 1u << 8,
     kStatusPhiLoop = 1u << 9,
     kStatusMlpTimeout = 1u << 10,  // a tensor-core wait of the pre-filter gave up
+    kStatusOverflowKept = 1u << 11,  // the pre-filter's list of kept candidates overflowed
+    kStatusHalt = 0x1fu | kStatusOverflowKept,  // bits that stop the remaining kernels of a run
 };
 
 }  // namespace sdlg
