@@ -240,8 +240,9 @@ def run_reference_arm(a, rank, world, pg):
 
 
 def timed_runs(ch, flags, steps, flush):
-    """device ms per run (CUDA events around the chain on its stream)"""
-    out, stage, tl = [], [], []
+    """device ms per run (CUDA events around the chain on its stream), per
+    stage, of the tracklet kernels, and of the pre-filter kernel alone"""
+    out, stage, tl, pf = [], [], [], []
     for _ in range(steps):
         flush()
         ch.run(4, flags)
@@ -249,7 +250,8 @@ def timed_runs(ch, flags, steps, flush):
         out.append(float(t[6]))
         stage.append(t[:6].copy())
         tl.append(float(ch.kernel_times()[2]))
-    return out, stage, tl
+        pf.append(ch.prefilter_times().copy())
+    return out, stage, tl, pf
 
 
 def main():
@@ -300,7 +302,7 @@ def main():
     clocks = Clocks(local)
     barrier(pg)
     t_wall0 = time.perf_counter()
-    step_ms, stage_ms, tl_ms = timed_runs(ch, FLAG_MLP, a.steps, flush)
+    step_ms, stage_ms, tl_ms, pf_ms = timed_runs(ch, FLAG_MLP, a.steps, flush)
     wall = time.perf_counter() - t_wall0
     barrier(pg)
     clk = clocks.stop()
@@ -313,7 +315,7 @@ def main():
     for _ in range(2):
         ch.run(4, 0)
     n_plain = ch.counts(-1)
-    p_ms, p_stage, p_tl = timed_runs(ch, 0, max(3, a.steps // 4), flush)
+    p_ms, p_stage, p_tl, _ = timed_runs(ch, 0, max(3, a.steps // 4), flush)
     p_mean = allmax(pg, statistics.fmean(p_ms))
     tc_rec = float(n_pruned[4]) / max(1.0, float(n_plain[4]))
     tl_rec = float(n_pruned[2]) / max(1.0, float(n_plain[2]))
@@ -354,7 +356,7 @@ def main():
     for _ in range(a.warmup):
         ch.run(4, 0)
     s_counts = ch.counts(0)
-    s_ms, s_stage, s_tl = timed_runs(ch, 0, a.steps, flush)
+    s_ms, s_stage, s_tl, _ = timed_runs(ch, 0, a.steps, flush)
     s_mean = allmax(pg, statistics.fmean(s_ms))
     s_st = np.mean(np.array(s_stage), axis=0)
     plain_single = {"value": round(allsum(pg, 1.0) * 1e3 / s_mean, 3), "unit": "events/s", "ms_per_step": round(s_mean, 4),
@@ -364,22 +366,25 @@ def main():
                     "tl_kernel_ms": round(statistics.fmean(s_tl), 4)}
 
     # ---- roofline of the dominant kernel of the headline run -----------------
-    # k_tl_enum_mlp: algorithmic bytes = segments read once (28 B) + tracklets
-    # written once (8 B); tensor work = the pre-filter's MMAs per candidate
+    # k_tl_prefilter: algorithmic bytes = segment records read once (28 B per
+    # segment) + kept candidate pairs written once (8 B each); tensor work =
+    # the pre-filter's MMAs per scored candidate
     hbm, tflops, src = peaks()
-    tl_mean = statistics.fmean(tl_ms)
-    n_sg, n_tl = int(n_pruned[1]), int(n_pruned[2])
-    alg_bytes = 28 * n_sg + 8 * n_tl
-    achieved = alg_bytes / (tl_mean * 1e-3) / 1e9
-    tr = ncu_traffic("tl_mlp_kernel_traffic.json")
+    pf = np.mean(np.array(pf_ms), axis=0)
+    pf_mean, ex_mean = float(pf[0]), float(pf[1])
+    n_sg = int(n_pruned[1])
+    alg_bytes = 28 * n_sg + 8 * mstats["kept"]
+    achieved = alg_bytes / (pf_mean * 1e-3) / 1e9
+    tr = ncu_traffic("tl_prefilter_traffic.json")
     traffic = None
     if tr and tr.get("traffic_per_algorithmic_byte"):
         traffic = int(alg_bytes * float(tr["traffic_per_algorithmic_byte"]))
-    mma_tflops = mstats["scored"] * MLP_FLOPS_PER_CANDIDATE / (tl_mean * 1e-3) / 1e12
+    mma_tflops = mstats["scored"] * MLP_FLOPS_PER_CANDIDATE / (pf_mean * 1e-3) / 1e12
     roofline = {"bound": "hbm", "achieved": round(achieved, 3), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 6), "traffic": traffic, "peak_source": src,
-                "kernel": "k_tl_enum_mlp (pre-filter + tracklet cuts)", "kernel_ms": round(tl_mean, 3),
-                "algorithmic_bytes": alg_bytes,
+                "kernel": "k_tl_prefilter (tensor-core pre-filter of the tracklet candidates)",
+                "kernel_ms": round(pf_mean, 3), "algorithmic_bytes": alg_bytes,
+                "exact_cuts_kernel_ms": round(ex_mean, 3),
                 "tensor": {"achieved": round(mma_tflops, 2), "peak": tflops, "unit": "TFLOP/s",
                            "frac": round(mma_tflops / tflops, 5), "flops_per_candidate": MLP_FLOPS_PER_CANDIDATE,
                            "candidates": mstats["scored"]},

@@ -130,6 +130,11 @@ int sdlg_last_times(sdlg_ctx* ctx, float* out7);
 /* Device time of each stage's candidate-evaluation kernel in the last run (ms). */
 int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5);
 
+/* For a run with SDLG_FLAG_MLP: device time (ms) of the pre-filter kernel and
+ * of the exact tracklet cuts on the candidates it kept (no counterpart in the
+ * reference); zeros otherwise. */
+int sdlg_last_prefilter_times(sdlg_ctx* ctx, float* out2);
+
 /* Number of kernels one run of the chain launches (as last enqueued). */
 int64_t sdlg_last_launches(const sdlg_ctx* ctx);
 

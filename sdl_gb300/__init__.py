@@ -68,6 +68,7 @@ def lib():
         L.sdlg_get_counters.argtypes = [vp, i64, vp]
         L.sdlg_last_times.argtypes = [vp, vp]
         L.sdlg_last_kernel_times.argtypes = [vp, vp]
+        L.sdlg_last_prefilter_times.argtypes = [vp, vp]
         L.sdlg_last_launches.argtypes = [vp]
         L.sdlg_last_launches.restype = i64
         L.sdlg_mini_doublets_static.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
@@ -310,6 +311,12 @@ class Chain:
         z = np.empty(len(x), dtype=np.float32)
         self._ck(lib().sdlg_mlp_score(self.h, len(x), x.ctypes.data, z.ctypes.data))
         return z
+
+    def prefilter_times(self) -> np.ndarray:
+        """Device ms of the last FLAG_MLP run's pre-filter kernel and exact tracklet cuts."""
+        out = np.zeros(2, dtype=np.float32)
+        self._ck(lib().sdlg_last_prefilter_times(self.h, out.ctypes.data))
+        return out
 
     def mlp_stats(self) -> dict:
         """Pre-filter counts of the last run with FLAG_MLP."""

@@ -651,6 +651,7 @@ int sdlg_create(sdlg_ctx** out, int device) {
         e = cudaEventCreate(&ctx->hooks.enum_start[k]);
         if (e == cudaSuccess) e = cudaEventCreate(&ctx->hooks.enum_stop[k]);
     }
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->hooks.tl_mid);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_small, 16 * sizeof(int64_t));
     // pre-filter state is small and allocated once, so device pointers captured
     // in the launch graph never change
@@ -696,6 +697,7 @@ int sdlg_destroy(sdlg_ctx* ctx) {
         if (ctx->hooks.enum_start[k]) cudaEventDestroy(ctx->hooks.enum_start[k]);
         if (ctx->hooks.enum_stop[k]) cudaEventDestroy(ctx->hooks.enum_stop[k]);
     }
+    if (ctx->hooks.tl_mid) cudaEventDestroy(ctx->hooks.tl_mid);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SDLG_OK;
@@ -899,6 +901,18 @@ int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5) {
         CK(cudaEventSynchronize(ctx->hooks.enum_stop[k]));
         CK(cudaEventElapsedTime(&out5[k], ctx->hooks.enum_start[k], ctx->hooks.enum_stop[k]));
     }
+    return SDLG_OK;
+}
+
+int sdlg_last_prefilter_times(sdlg_ctx* ctx, float* out2) {
+    if (!ctx || !out2) return SDLG_ERR_ARG;
+    if (!ctx->ran) return fail(ctx, SDLG_ERR_NO_EVENTS, "chain not run");
+    out2[0] = out2[1] = 0.f;
+    if (!(ctx->last_flags & SDLG_FLAG_MLP) || ctx->last_stop < kTL) return SDLG_OK;
+    cudaSetDevice(ctx->device);
+    CK(cudaEventSynchronize(ctx->hooks.enum_stop[kTL]));
+    CK(cudaEventElapsedTime(&out2[0], ctx->hooks.enum_start[kTL], ctx->hooks.tl_mid));
+    CK(cudaEventElapsedTime(&out2[1], ctx->hooks.tl_mid, ctx->hooks.enum_stop[kTL]));
     return SDLG_OK;
 }
 

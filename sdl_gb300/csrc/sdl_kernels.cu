@@ -1300,6 +1300,7 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     if (b.flags & kFlagMLP) {
         cudaMemsetAsync(b.n_kept, 0, sizeof(unsigned long long), s);
         k_tl_prefilter<<<b.n_sm * 8, kMlpTile, 0, s>>>(b);
+        if (h && h->timed) rec_event(h->tl_mid, s);
         k_tl_exact<<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
         if (h) h->launches += 1;
     } else {

@@ -59,6 +59,7 @@ struct BatchDev {
 struct Hooks {
     cudaEvent_t enum_start[kNumStages];
     cudaEvent_t enum_stop[kNumStages];
+    cudaEvent_t tl_mid;  // between the pre-filter and the exact tracklet cuts
     bool timed = false;
     int launches = 0;
 };
