@@ -136,6 +136,19 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
     }
     return false;
 }
+// two floats rounded to BF16 (to nearest, ties to even) and packed, lo in
+// the low half; the .relu form first clamps negative values to zero
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi) {
+    uint32_t d;
+    asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
+}
+__device__ __forceinline__ uint32_t pack_bf16x2_relu(float lo, float hi) {
+    uint32_t d;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+    return d;
+}
+
 // 16 consecutive FP32 columns of this thread's tensor-memory lane
 __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
     uint32_t r[16];
@@ -239,7 +252,7 @@ __device__ __forceinline__ float mlp_tile(MlpSmem& sm, const float* x, MlpThread
         for (int j = 0; j < 8; ++j) {
             const float lo = 2 * j < kMlpIn ? x[2 * j] : 0.f;
             const float hi = 2 * j + 1 < kMlpIn ? x[2 * j + 1] : 0.f;
-            q[j] = (uint32_t)bf16_bits(lo) | ((uint32_t)bf16_bits(hi) << 16);
+            q[j] = pack_bf16x2(lo, hi);
         }
         *reinterpret_cast<uint4*>(sm.a1 + cm_offset(t, 0, 2)) = make_uint4(q[0], q[1], q[2], q[3]);
         *reinterpret_cast<uint4*>(sm.a1 + cm_offset(t, 8, 2)) = make_uint4(q[4], q[5], q[6], q[7]);
@@ -253,11 +266,8 @@ __device__ __forceinline__ float mlp_tile(MlpSmem& sm, const float* x, MlpThread
         tc_ld16(lane_base + 16 * c, v);
         uint32_t q[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const float h0 = fmaxf(__fadd_rn(v[2 * j], b1[16 * c + 2 * j]), 0.f);
-            const float h1 = fmaxf(__fadd_rn(v[2 * j + 1], b1[16 * c + 2 * j + 1]), 0.f);
-            q[j] = (uint32_t)bf16_bits(h0) | ((uint32_t)bf16_bits(h1) << 16);
-        }
+        for (int j = 0; j < 8; ++j)
+            q[j] = pack_bf16x2_relu(__fadd_rn(v[2 * j], b1[16 * c + 2 * j]), __fadd_rn(v[2 * j + 1], b1[16 * c + 2 * j + 1]));
         *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c, 8)) = make_uint4(q[0], q[1], q[2], q[3]);
         *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c + 8, 8)) = make_uint4(q[4], q[5], q[6], q[7]);
     }
