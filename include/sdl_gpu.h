@@ -135,6 +135,16 @@ int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5);
  * reference); zeros otherwise. */
 int sdlg_last_prefilter_times(sdlg_ctx* ctx, float* out2);
 
+/* Self-check of the float-float evaluations that stand for the reference's
+ * double sub-expressions (no counterpart in the reference).  Function fn
+ * (0 asin, 1 atan2, 2 hit phi, 3 x + sqrt(y), 4 s + sqrt(a^2+b^2+c^2),
+ * 5 Phi_mpi_pi, 6 M_PI + x) is evaluated on n inputs: the float bit patterns
+ * start .. start+n-1 (exhaustive != 0, unary functions) or hashed pseudo-random
+ * inputs from `seed`.  out8: inputs where the fast path answered, of those
+ * the ones whose float differs from the double evaluation's (must be 0), a
+ * flag, and the first differing inputs and results as bit patterns. */
+int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64_t n, uint64_t seed, uint64_t* out8);
+
 /* Number of kernels one run of the chain launches (as last enqueued). */
 int64_t sdlg_last_launches(const sdlg_ctx* ctx);
 

@@ -69,6 +69,7 @@ def lib():
         L.sdlg_last_times.argtypes = [vp, vp]
         L.sdlg_last_kernel_times.argtypes = [vp, vp]
         L.sdlg_last_prefilter_times.argtypes = [vp, vp]
+        L.sdlg_math_check.argtypes = [vp, i32, i32, ctypes.c_uint64, i64, ctypes.c_uint64, vp]
         L.sdlg_last_launches.argtypes = [vp]
         L.sdlg_last_launches.restype = i64
         L.sdlg_mini_doublets_static.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
@@ -317,6 +318,14 @@ class Chain:
         out = np.zeros(2, dtype=np.float32)
         self._ck(lib().sdlg_last_prefilter_times(self.h, out.ctypes.data))
         return out
+
+    def math_check(self, fn: int, n: int, *, start: int = 0, exhaustive: bool = False, seed: int = 0) -> dict:
+        """Self-check of a float-float fast path against the double evaluation."""
+        out = np.zeros(8, dtype=np.uint64)
+        self._ck(lib().sdlg_math_check(self.h, int(fn), 1 if exhaustive else 0, int(start), int(n), int(seed),
+                                       out.ctypes.data))
+        return {"answered": int(out[0]), "mismatches": int(out[1]),
+                "first": [int(v) for v in out[3:8]] if out[2] else None}
 
     def mlp_stats(self) -> dict:
         """Pre-filter counts of the last run with FLAG_MLP."""

@@ -10,11 +10,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libsdlgpu.so")
 SOURCES = ("sdl_kernels.cu", "sdl_capi.cu", "sdl_static.cu", "sdl_mlp.cu")
-# -fmad=false: no multiply-add contraction, the cut arithmetic must round like
-# the reference CPU build; IEEE division and square root are nvcc's defaults.
+# -fmad=false (device) and -ffp-contract=off (host): no multiply-add
+# contraction, the cut arithmetic must round like the reference CPU build;
+# IEEE division and square root are nvcc's defaults.
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
-              "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off"]
 
 
 def nvcc() -> str:

@@ -241,6 +241,10 @@ int build_module_table(sdlg_ctx* ctx, const std::vector<uint32_t>& extra) {
         const float phi = eget(d, 1);
         o.edge_x = (float)(2.5 * std::cos((double)phi));
         o.edge_y = (float)(2.5 * std::sin((double)phi));
+        // MiniDoublet.cc:781-783 / Segment.cc:920-928: the tilt term depends on the module only
+        const float half_pitch_drdz = 0.5f * 0.15f * o.drdz_s;
+        const float one_plus = 1.f + o.drdz_s * o.drdz_s;
+        o.tilt = (float)((double)half_pitch_drdz / std::sqrt((double)one_plus) / (double)o.gap);
     }
     ctx->conn_off.assign(n + 1, 0);
     ctx->conn_idx.clear();
@@ -917,6 +921,24 @@ int sdlg_last_prefilter_times(sdlg_ctx* ctx, float* out2) {
 }
 
 int64_t sdlg_last_launches(const sdlg_ctx* ctx) { return ctx ? ctx->launches_per_run : -1; }
+
+int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64_t n, uint64_t seed, uint64_t* out8) {
+    if (!ctx || !out8 || n < 0 || fn < 0 || fn > 6) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    unsigned long long* d = nullptr;
+    CK(cudaMalloc(&d, 8 * sizeof(unsigned long long)));
+    cudaError_t e = cudaMemsetAsync(d, 0, 8 * sizeof(unsigned long long), ctx->stream);
+    if (e == cudaSuccess) {
+        launch_math_check(fn, exhaustive, (unsigned long long)start, (long long)n, (unsigned long long)seed, d, ctx->n_sm,
+                          ctx->stream);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out8, d, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "math check: %s", cudaGetErrorString(e));
+    return SDLG_OK;
+}
 
 // ------------------------------------------------------------------ pre-filter
 int sdlg_mlp_set_params(sdlg_ctx* ctx, const float* params, float threshold) {

@@ -16,6 +16,8 @@
 #pragma once
 #include <cstdint>
 
+#include "sdl_ffmath.cuh"
+
 namespace sdlg {
 
 constexpr double kPi = 3.14159265358979323846;
@@ -39,13 +41,14 @@ struct ModDev {
     float drdz_s;        // tilted drdz of the strip sensor of the pair
     float slope_s;       // strip-direction slope of the strip sensor of the pair
     float edge_x, edge_y;  // (float)(2.5*cos(phi_c)), (float)(2.5*sin(phi_c)) of this sensor
+    float tilt;          // (float)((double)(0.5f*pitchPS*drdz_s) / sqrt((double)(1.f + drdz_s*drdz_s)) / (double)gap)
 };
 
 // ------------------------------------------------------------------ math
 // The double-precision math routines are kept out of line: one copy of each
 // in the binary instead of one per call site keeps the cut kernels small
 // enough for the instruction caches.
-static __device__ __noinline__ float f_asin(float x) { return (float)asin((double)x); }
+static __device__ __noinline__ float f_asin_d(float x) { return (float)asin((double)x); }
 static __device__ __noinline__ float f_atan(float x) { return (float)atan((double)x); }
 static __device__ __noinline__ float f_sin(float x) { return (float)sin((double)x); }
 static __device__ __noinline__ float f_cos(float x) { return (float)cos((double)x); }
@@ -60,8 +63,54 @@ __device__ __forceinline__ int trunc_i32(float f) {
 __device__ __forceinline__ int iabs(int v) { return v < 0 ? (int)(0u - (unsigned)v) : v; }
 __device__ __forceinline__ float f_copysign(float a, float b) { return copysignf(a, b); }
 
-// MathUtil.cc:3-19; the loop is bounded (|x| stays within a few pi here)
-__device__ __forceinline__ float phi_mpi_pi(float x) {
+// Each function below returns the float the double evaluation gives: the
+// float-float evaluation of sdl_ffmath.cuh when its rounding is certain, the
+// double evaluation otherwise.
+
+// (float)asin((double)x) (std::asin of a float)
+__device__ __forceinline__ bool f_asin_fast(float x, float& r) {
+    if (x == 0.f) {
+        r = x;
+        return true;
+    }
+    return fabsf(x) <= 0.95f && ffm::round_unique_rel(ffm::asin_ff(x), r);
+}
+static __device__ __noinline__ float f_asin(float x) {
+    float r;
+    return f_asin_fast(x, r) ? r : f_asin_d(x);
+}
+
+// (float)((double)x + sqrt((double)y)), the reference's float + double sqrt of a float
+static __device__ __noinline__ float add_dsqrt_d(float x, float y) { return (float)((double)x + sqrt((double)y)); }
+__device__ __forceinline__ bool add_dsqrt_fast(float x, float y, float& r) {
+    if (!(y > 0x1p-100f && y < 0x1p100f)) return false;
+    const ffm::ff s = ffm::sqrt_ff(ffm::ff{y, 0.f});
+    return ffm::round_unique(ffm::add(s, x), __fmul_rn(__fadd_rn(fabsf(x), s.hi), 0x1p-40f), r);
+}
+static __device__ __noinline__ float add_dsqrt(float x, float y) {
+    float r;
+    return add_dsqrt_fast(x, y, r) ? r : add_dsqrt_d(x, y);
+}
+// (float)(s + sqrt(a*a + b*b + c*c)) with a, b, c floats promoted to double
+static __device__ __noinline__ float add_dsqrt3_d(float s, float a, float b, float c) {
+    const double da = a, db = b, dc = c;
+    return (float)((double)s + sqrt(da * da + db * db + dc * dc));
+}
+__device__ __forceinline__ bool add_dsqrt3_fast(float s, float a, float b, float c, float& r) {
+    const float m = fmaxf(fabsf(a), fmaxf(fabsf(b), fabsf(c)));
+    if (!(m > 0x1p-50f && m < 0x1p50f)) return false;
+    const ffm::ff q = ffm::add(ffm::add(ffm::two_prod(a, a), ffm::two_prod(b, b)), ffm::two_prod(c, c));
+    const ffm::ff r0 = ffm::sqrt_ff(q);
+    return ffm::round_unique(ffm::add(r0, s), __fmul_rn(__fadd_rn(fabsf(s), r0.hi), 0x1p-40f), r);
+}
+static __device__ __noinline__ float add_dsqrt3(float s, float a, float b, float c) {
+    float r;
+    return add_dsqrt3_fast(s, a, b, c, r) ? r : add_dsqrt3_d(s, a, b, c);
+}
+
+// MathUtil.cc:3-19; the loop is bounded (|x| stays within a few pi here).
+// 0x1.921fb6p+1f is the float just above pi: |x| below it is in [-pi, pi).
+static __device__ __noinline__ float phi_mpi_pi_d(float x) {
     if (isnan(x)) return x;
 #pragma unroll 1
     for (int it = 0; it < 64 && (double)x >= kPi; ++it) x = (float)((double)x - 2. * kPi);
@@ -69,15 +118,55 @@ __device__ __forceinline__ float phi_mpi_pi(float x) {
     for (int it = 0; it < 64 && (double)x < -kPi; ++it) x = (float)((double)x + 2. * kPi);
     return x;
 }
+// one step of the loop, (float)((double)x -+ 2 M_PI), when it is enough
+// (2 M_PI as hi + lo is 7.1e-15 off; the sum's error is below 1e-13)
+__device__ __forceinline__ bool phi_mpi_pi_fast(float x, float& r) {
+    const float ax = fabsf(x);
+    if (ax < 0x1.921fb6p+1f) {
+        r = x;
+        return true;
+    }
+    if (!(ax < 9.f)) return false;
+    const ffm::ff tp = x > 0.f ? ffm::ff{-0x1.921fb6p+2f, 0x1.777a5cp-23f} : ffm::ff{0x1.921fb6p+2f, -0x1.777a5cp-23f};
+    return ffm::round_unique(ffm::add(tp, x), 2e-13f, r) && fabsf(r) < 0x1.921fb6p+1f;
+}
+static __device__ __noinline__ float phi_mpi_pi_slow(float x) {
+    float r;
+    return phi_mpi_pi_fast(x, r) ? r : phi_mpi_pi_d(x);
+}
+__device__ __forceinline__ float phi_mpi_pi(float x) {
+    if (fabsf(x) < 0x1.921fb6p+1f) return x;
+    return phi_mpi_pi_slow(x);
+}
 // MathUtil.cc:21-27
+static __device__ __noinline__ float atan2_d(float y, float x) { return (float)atan2((double)y, (double)x); }
+__device__ __forceinline__ bool atan2_fast(float y, float x, float& r) {
+    ffm::ff a;
+    return y != 0.f && x != 0.f && ffm::atan2_ff(ffm::ff{y, 0.f}, ffm::ff{x, 0.f}, a) && ffm::round_unique_rel(a, r);
+}
 __device__ __forceinline__ float atan2_ref(float y, float x) {
-    if (x != 0) return (float)atan2((double)y, (double)x);
+    if (x != 0) {
+        float r;
+        return atan2_fast(y, x, r) ? r : atan2_d(y, x);
+    }
     if (y == 0) return 0.f;
     if (y > 0) return (float)(kPi / 2);
     return (float)(-kPi / 2);
 }
+// phi of a point (Hit.cc:68-83 via MathUtil.cc): Phi_mpi_pi(M_PI + ATan2(-y, -x))
+static __device__ __noinline__ float phi_of_d(float x, float y) {
+    const float a = x != 0 ? atan2_d(-y, -x) : atan2_ref(-y, -x);
+    return phi_mpi_pi_d((float)(kPi + (double)a));
+}
+// (float)(M_PI + (double)a): M_PI as hi + lo is 3.6e-15 off; error below 1e-13
+__device__ __forceinline__ bool add_pi_fast(float a, float& p) {
+    return ffm::round_unique(ffm::add(ffm::ff{0x1.921fb6p+1f, -0x1.777a5cp-24f}, a), 1e-13f, p);
+}
 static __device__ __noinline__ float phi_of(float x, float y) {
-    return phi_mpi_pi((float)(kPi + (double)atan2_ref(-y, -x)));
+    const float a = atan2_ref(-y, -x);
+    float p;
+    if (!add_pi_fast(a, p)) p = (float)(kPi + (double)a);
+    return phi_mpi_pi(p);
 }
 
 // A point with the derived quantities (Hit.cc:68-83).
@@ -145,21 +234,12 @@ __device__ __forceinline__ float dphi_threshold(float rt, float asin_rt1, const 
     (void)rt;
     const bool barrel = m.subdet == kBarrel;
     const float rLay = barrel ? rB[iL] : rE[iL];
-    const float miniPVoff = (float)(0.1 / (double)rLay);
+    const float miniPVoff = (float)(0.1 / (double)rLay);  // a double division of constants (one per layer)
     const float miniMuls = barrel ? mulsB[iL] * 3.f / kPtCut : 0.006f * 3.f / kPtCut;
-    if (barrel && m.side == kCenter) {
-        const double a = miniMuls, b = miniPVoff;
-        return (float)((double)miniSlope + sqrt(a * a + b * b));
-    }
-    if (barrel) {
-        const float drdz = m.drdz_s;
-        const float miniTilt = (float)((double)(0.5f * kPixelPSZpitch * drdz) / sqrt((double)(1.f + drdz * drdz)) / (double)m.gap);
-        const double a = miniMuls, b = miniPVoff, c = miniTilt * miniSlope;
-        return (float)((double)miniSlope + sqrt(a * a + b * b + c * c));
-    }
+    if (barrel && m.side == kCenter) return add_dsqrt3(miniSlope, miniMuls, miniPVoff, 0.f);
+    if (barrel) return add_dsqrt3(miniSlope, miniMuls, miniPVoff, m.tilt * miniSlope);
     const float miniLum = (float)iabs(trunc_i32(dPhi * kDeltaZLum / dz));
-    const double a = miniMuls, b = miniPVoff, c = miniLum;
-    return (float)((double)miniSlope + sqrt(a * a + b * b + c * c));
+    return add_dsqrt3(miniSlope, miniMuls, miniPVoff, miniLum);
 }
 
 // MiniDoublet.cc:989-1209.  pix/str are the anchoring and the shifted hit.
@@ -276,8 +356,8 @@ __device__ __forceinline__ void dalpha_threshold(const MDView& im, const MDView&
     const float dAlpha_Bfield = f_asin(fmin_ref(segmentDr * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
     const bool inTilt = I.subdet == kBarrel && I.side != kCenter;
     const bool outTilt = O.subdet == kBarrel && O.side != kCenter;
-    const float iTilt = inTilt ? (float)((double)(0.5f * kPixelPSZpitch * I.drdz_s) / sqrt((double)(1.f + I.drdz_s * I.drdz_s)) / (double)I.gap) : 0.f;
-    const float oTilt = outTilt ? (float)((double)(0.5f * kPixelPSZpitch * O.drdz_s) / sqrt((double)(1.f + O.drdz_s * O.drdz_s)) / (double)O.gap) : 0.f;
+    const float iTilt = inTilt ? I.tilt : 0.f;
+    const float oTilt = outTilt ? O.tilt : 0.f;
     const float miniDelta = I.gap;
     float lumIn, lumOut;
     if (I.subdet == kBarrel) lumIn = iTilt * dAlpha_Bfield;
@@ -288,13 +368,10 @@ __device__ __forceinline__ void dalpha_threshold(const MDView& im, const MDView&
     else lumOut = (float)((double)om.dphi * 15.0 / (double)om.dz);
     const float resIn = 0.02f / miniDelta * (I.subdet == kBarrel ? 1.0f : fabsf(im.a.z / im.a.rt));
     const float resOut = 0.02f / miniDelta * (O.subdet == kBarrel ? 1.0f : fabsf(om.a.z / om.a.rt));
-    const double res = (double)(resIn + resOut);
-    const double mu = sdMuls;
-    const double base = res * res + mu * mu;
-    const double li = lumIn, lo = lumOut;
-    th[0] = (I.subdet == kBarrel && I.side == kCenter) ? (float)((double)dAlpha_Bfield + sqrt(base)) : (float)((double)dAlpha_Bfield + sqrt(base + li * li));
-    th[1] = (O.subdet == kBarrel && O.side == kCenter) ? (float)((double)dAlpha_Bfield + sqrt(base)) : (float)((double)dAlpha_Bfield + sqrt(base + lo * lo));
-    th[2] = (float)((double)dAlpha_Bfield + sqrt(base));
+    const float res = resIn + resOut;
+    th[0] = add_dsqrt3(dAlpha_Bfield, res, sdMuls, (I.subdet == kBarrel && I.side == kCenter) ? 0.f : lumIn);
+    th[1] = add_dsqrt3(dAlpha_Bfield, res, sdMuls, (O.subdet == kBarrel && O.side == kCenter) ? 0.f : lumOut);
+    th[2] = add_dsqrt3(dAlpha_Bfield, res, sdMuls, 0.f);
 }
 
 __device__ __forceinline__ bool dalpha_cuts(const MDView& im, const MDView& om, float sg_alpha) {
@@ -322,7 +399,7 @@ __device__ __forceinline__ bool sg_barrel(const MDView& im, const MDView& om, fl
     const float zLo = zIn + (zIn - kDeltaZLum) * (rtOut / rtIn - 1.f) * (zIn > 0.f ? 1.f : dzDrtScale) - zGeom;
     const float zHi = zIn + (zIn + kDeltaZLum) * (rtOut / rtIn - 1.f) * (zIn < 0.f ? 1.f : dzDrtScale) + zGeom;
     if (!(zOut >= zLo && zOut <= zHi)) return false;
-    const float sdCut = (float)((double)sdSlope + sqrt((double)(sdMuls * sdMuls + sdPVoff * sdPVoff)));
+    const float sdCut = add_dsqrt(sdSlope, sdMuls * sdMuls + sdPVoff * sdPVoff);
     const float deltaPhi = dphi(im.a, om.a);
     if (!(fabsf(deltaPhi) <= sdCut)) return false;
     v.dphichange = dphichange(im.a, om.a);
@@ -527,8 +604,6 @@ __device__ __forceinline__ float dbeta_cut2(float dBetaRes, float dBetaMuls, flo
     return (float)((double)head + 0.25 * (t * t));
 }
 
-// (float)(x + sqrt(y)) with the sum in double, as the reference writes it
-__device__ __forceinline__ float add_dsqrt(float x, float y) { return (float)((double)x + sqrt((double)y)); }
 
 // Tracklet algorithm ids carried between the two phases
 enum : int { kAlgoNone = 0, kAlgoBBBB = 1, kAlgoBBEE = 2, kAlgoEEEE = 3 };

@@ -1,0 +1,174 @@
+// Float-float evaluation of the double-precision sub-expressions of the cut
+// arithmetic, with a rounding test and a double-precision fallback.
+//
+// The reference computes many float results through double intermediates
+// (unqualified sqrt/atan2/sin on promoted floats, double constants); the
+// device reproduces them exactly.  GB300 runs FP64 at a small fraction of its
+// FP32 rate, so each such result is first evaluated here in float-float
+// arithmetic (pairs hi + lo of floats, about 44 significant bits) together
+// with a bound on its distance to the value the double evaluation produces.
+// If no float rounding boundary lies within that bound, the float the double
+// evaluation rounds to is known: it is returned.  Otherwise (a fraction of
+// about 2^-15 of the inputs) the caller evaluates the expression in double as
+// before.  The results are therefore identical to the double evaluation's.
+//
+// Published methods used: Dekker's and Knuth's error-free transformations
+// (TwoSum, FastTwoSum, TwoProd via fused multiply-add), Dekker's double-length
+// division and square root, argument reduction of atan by a 33-entry table of
+// atan(k/32) and its Taylor series on |u| <= 1/64, and Ziv's rounding test.
+// Table and constants were computed with mpmath at 200 bits.
+#pragma once
+
+namespace sdlg {
+namespace ffm {
+
+struct ff {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+// |a| >= |b| or a == 0
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ ff neg(ff a) { return {-a.hi, -a.lo}; }
+__device__ __forceinline__ ff fabs_ff(ff a) { return a.hi < 0.f ? neg(a) : a; }
+__device__ __forceinline__ ff add(ff a, ff b) {
+    ff s = two_sum(a.hi, b.hi);
+    const ff t = two_sum(a.lo, b.lo);
+    s.lo = __fadd_rn(s.lo, t.hi);
+    s = fast_two_sum(s.hi, s.lo);
+    s.lo = __fadd_rn(s.lo, t.lo);
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ ff add(ff a, float b) {
+    ff s = two_sum(a.hi, b);
+    s.lo = __fadd_rn(s.lo, a.lo);
+    return fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ ff sub(ff a, ff b) { return add(a, neg(b)); }
+__device__ __forceinline__ ff mul(ff a, ff b) {
+    ff p = two_prod(a.hi, b.hi);
+    p.lo = __fadd_rn(p.lo, __fadd_rn(__fmul_rn(a.hi, b.lo), __fmul_rn(a.lo, b.hi)));
+    return fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ ff mul(ff a, float b) {
+    ff p = two_prod(a.hi, b);
+    p.lo = __fadd_rn(p.lo, __fmul_rn(a.lo, b));
+    return fast_two_sum(p.hi, p.lo);
+}
+// a / b (b.hi != 0): relative error below 2^-44
+__device__ __forceinline__ ff div(ff a, ff b) {
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const ff r = sub(a, mul(b, q1));
+    const float q2 = __fdiv_rn(r.hi, b.hi);
+    return fast_two_sum(q1, q2);
+}
+// sqrt(a) (a.hi > 0, normal): relative error below 2^-45
+__device__ __forceinline__ ff sqrt_ff(ff a) {
+    const float s0 = __fsqrt_rn(a.hi);
+    const ff p = two_prod(s0, s0);
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p.hi), p.lo), a.lo);
+    return fast_two_sum(s0, __fdiv_rn(r, __fmul_rn(2.f, s0)));
+}
+
+// Ziv's rounding test.  If every real number within err of v rounds to the
+// same float, store it in out and return true.  Zero, subnormal, very small,
+// very large and non-finite values return false.
+__device__ __forceinline__ bool round_unique(ff v, float err, float& out) {
+    const float r = __fadd_rn(v.hi, v.lo);
+    const uint32_t ur = __float_as_uint(r) & 0x7fffffffu;
+    const uint32_t e = ur >> 23;
+    if (e < 40u || e > 215u) return false;
+    float h = __uint_as_float((e - 24u) << 23);  // half an ulp of r
+    if ((ur & 0x7fffffu) == 0u) h = __fmul_rn(h, 0.5f);  // below a power of two the gap halves
+    // v - r (hi - r is exact; the sum and the test below round by at most
+    // 2^-24 relative, which the factor on h covers)
+    const float d = __fadd_rn(__fsub_rn(v.hi, r), v.lo);
+    if (!(__fadd_rn(fabsf(d), err) < __fmul_rn(0.99999f, h))) return false;
+    out = r;
+    return true;
+}
+// the same with err = |v| * 2^-40 (results with relative error below 2^-42)
+__device__ __forceinline__ bool round_unique_rel(ff v, float& out) {
+    return round_unique(v, __fmul_rn(fabsf(v.hi), 0x1p-40f), out);
+}
+
+// atan(k/32), k = 0..32, as hi + lo
+__device__ constexpr float kAtanTabHi[33] = {
+    0x0.0p+0f, 0x1.ffd55cp-6f, 0x1.ff55bcp-5f, 0x1.7ee182p-4f, 0x1.fd5baap-4f, 0x1.3d6eeep-3f, 0x1.7b97b4p-3f,
+    0x1.b90d76p-3f, 0x1.f5b760p-3f, 0x1.18bf5ap-2f, 0x1.362774p-2f, 0x1.530adap-2f, 0x1.6f6194p-2f, 0x1.8b24d4p-2f,
+    0x1.a64eecp-2f, 0x1.c0db4cp-2f, 0x1.dac670p-2f, 0x1.f40dd0p-2f, 0x1.0657eap-1f, 0x1.1255dap-1f, 0x1.1e00bap-1f,
+    0x1.2958e6p-1f, 0x1.345f02p-1f, 0x1.3f13fcp-1f, 0x1.4978fap-1f, 0x1.538f58p-1f, 0x1.5d5898p-1f, 0x1.66d664p-1f,
+    0x1.700a7cp-1f, 0x1.78f6bcp-1f, 0x1.819d0cp-1f, 0x1.89ff60p-1f, 0x1.921fb6p-1f};
+__device__ constexpr float kAtanTabLo[33] = {
+    0x0.0p+0f, -0x1.15a276p-32f, -0x1.1a6042p-30f, 0x1.80bc44p-30f, -0x1.54f424p-30f, 0x1.18cc4ep-28f,
+    0x1.79cb60p-28f, -0x1.adb3ecp-28f, -0x1.b4dfc8p-29f, 0x1.85f8bcp-29f, -0x1.1f0286p-27f, -0x1.ab8caep-28f,
+    0x1.e4def0p-30f, -0x1.ad7936p-28f, 0x1.e611fep-29f, 0x1.29d93ep-27f, 0x1.586ed4p-28f, 0x1.6a8282p-27f,
+    -0x1.6499e6p-26f, -0x1.010b56p-27f, 0x1.7bdfd6p-26f, -0x1.b3dc74p-27f, -0x1.98e422p-28f, -0x1.d85a42p-27f,
+    0x1.934f70p-28f, -0x1.1dbe78p-27f, 0x1.c5a6c6p-27f, -0x1.b707dep-27f, 0x1.5e118cp-27f, -0x1.516750p-28f,
+    -0x1.1d4eb6p-26f, -0x1.501c10p-30f, -0x1.777a5cp-26f};
+__device__ constexpr ff kPiFF = {0x1.921fb6p+1f, -0x1.777a5cp-24f};
+__device__ constexpr ff kPi2FF = {0x1.921fb6p+0f, -0x1.777a5cp-25f};
+__device__ constexpr ff kThirdFF = {0x1.555556p-2f, -0x1.555556p-27f};
+
+// atan(u) for |u| <= 1/64 + 2^-20: u + u P(u^2), P = -u^2/3 + u^4/5 - u^6/7 + u^8/9;
+// the truncation error is below |u| u^10/11 < |u| 2^-63, the rounding error
+// below |u| 2^-44
+__device__ __forceinline__ ff atan_small(ff u) {
+    const ff u2 = add(two_prod(u.hi, u.hi), __fmul_rn(__fmul_rn(2.f, u.hi), u.lo));
+    const float z = u2.hi;
+    const float tail = __fmul_rn(__fmul_rn(z, z), __fsub_rn(0.2f, __fmul_rn(z, __fsub_rn(0x1.249249p-3f, __fmul_rn(z, 0x1.c71c72p-4f)))));
+    const ff p = add(neg(mul(u2, kThirdFF)), tail);
+    return add(u, mul(u, p));
+}
+
+// atan(t) for t >= 0 (t.hi normal, below 2^60): relative error below 2^-42
+__device__ __forceinline__ ff atan_ff(ff t) {
+    const bool inv = t.hi > 1.f;
+    if (inv) t = div(ff{1.f, 0.f}, t);
+    const int k = __float2int_rn(__fmul_rn(t.hi, 32.f));  // 0..32
+    const float c = __fmul_rn((float)k, 0.03125f);
+    const ff num = add(t, -c);
+    const ff den = add(mul(t, c), 1.f);
+    const ff a = add(ff{kAtanTabHi[k], kAtanTabLo[k]}, atan_small(div(num, den)));
+    return inv ? sub(kPi2FF, a) : a;
+}
+
+// atan2(y, x) for nonzero, normal x and y with |y/x| and |x/y| above 2^-60:
+// relative error below 2^-42.  Returns false when the arguments are outside
+// that range.
+__device__ __forceinline__ bool atan2_ff(ff y, ff x, ff& out) {
+    const float ax = fabsf(x.hi), ay = fabsf(y.hi);
+    if (!(ax > 0x1p-60f && ax < 0x1p60f && ay > 0x1p-60f && ay < 0x1p60f)) return false;
+    const bool swap = ay > ax;
+    const ff t = swap ? div(fabs_ff(x), fabs_ff(y)) : div(fabs_ff(y), fabs_ff(x));
+    if (!(t.hi > 0x1p-60f)) return false;
+    ff a = atan_ff(t);
+    if (swap) a = sub(kPi2FF, a);
+    if (x.hi < 0.f) a = sub(kPiFF, a);
+    if (y.hi < 0.f) a = neg(a);
+    out = a;
+    return true;
+}
+
+// asin(x) for 0 < |x| <= 0.95 as atan(x / sqrt(1 - x^2)): relative error below 2^-42
+__device__ __forceinline__ ff asin_ff(float x) {
+    const ff w = add(neg(two_prod(x, x)), 1.f);
+    const ff t = div(ff{fabsf(x), 0.f}, sqrt_ff(w));
+    const ff a = atan_ff(t);
+    return x < 0.f ? neg(a) : a;
+}
+
+}  // namespace ffm
+}  // namespace sdlg

@@ -1326,6 +1326,94 @@ void launch_tc(const BatchDev& b, cudaStream_t s, Hooks* h) {
     enum_and_group<TCStage>(b, s, h);
 }
 
+// ------------------------------------------------------------------ self-check
+// The float-float fast paths of the cut arithmetic against the double
+// evaluation they stand for: every input whose fast path succeeds must give
+// the same float bit for bit.  Inputs are either all float bit patterns of a
+// range (unary functions) or hashed pseudo-random values.
+__device__ __forceinline__ float hash_log(unsigned long long h, float lo_exp, float hi_exp) {
+    const float u = (float)((h >> 11) & 0xffffffull) * (1.f / 16777216.f);
+    const float m = 1.f + (float)((h >> 35) & 0x7fffffull) * (1.f / 8388608.f);
+    return ldexpf(m, (int)floorf(lo_exp + u * (hi_exp - lo_exp)));
+}
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_math_check(int fn, int exhaustive, unsigned long long start, long long n, unsigned long long seed,
+                             unsigned long long* out) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float a = 0.f, b = 0.f, c = 0.f, d = 0.f;
+        if (exhaustive) {
+            a = __uint_as_float((unsigned)(start + (unsigned long long)i));
+        } else {
+            const unsigned long long h1 = mix64(seed * 0x9E3779B97F4A7C15ull + (unsigned long long)i);
+            const unsigned long long h2 = mix64(h1 + 0x632BE59BD9B4E019ull);
+            const unsigned long long h3 = mix64(h2 + 0x632BE59BD9B4E019ull);
+            const unsigned long long h4 = mix64(h3 + 0x632BE59BD9B4E019ull);
+            const float sa = (h1 & 1) ? -1.f : 1.f, sb = (h2 & 1) ? -1.f : 1.f;
+            switch (fn) {
+                case 1: case 2:  // coordinates: magnitudes 2^-12..2^9, a fraction on axes and diagonals
+                    a = sa * hash_log(h1, -12.f, 9.f);
+                    b = sb * hash_log(h2, -12.f, 9.f);
+                    if ((h3 & 15) == 0) b = sb * fabsf(a) * (1.f + (float)((h4 >> 40) & 0xff) * 0x1p-20f);
+                    if ((h3 & 15) == 1) b = a * 0x1p-20f;
+                    break;
+                case 3:
+                    a = sa * hash_log(h1, -20.f, 4.f);
+                    b = hash_log(h2, -40.f, 6.f);
+                    break;
+                case 4:
+                    a = hash_log(h1, -10.f, 1.f);
+                    b = hash_log(h2, -14.f, 1.f);
+                    c = hash_log(h3, -14.f, 1.f);
+                    d = (h4 & 3) == 0 ? 0.f : hash_log(h4, -14.f, 3.f);
+                    break;
+                default:
+                    a = sa * hash_log(h1, -30.f, 0.f);
+            }
+        }
+        float f = 0.f, ref = 0.f;
+        bool ok = false;
+        switch (fn) {
+            case 0: ok = f_asin_fast(a, f); if (ok) ref = f_asin_d(a); break;
+            case 1: ok = atan2_fast(a, b, f); if (ok) ref = atan2_d(a, b); break;
+            case 2: {
+                f = phi_of(a, b);
+                ref = phi_of_d(a, b);
+                ok = true;
+                break;
+            }
+            case 3: ok = add_dsqrt_fast(a, b, f); if (ok) ref = add_dsqrt_d(a, b); break;
+            case 4: ok = add_dsqrt3_fast(a, b, c, d, f); if (ok) ref = add_dsqrt3_d(a, b, c, d); break;
+            case 5: ok = phi_mpi_pi_fast(a, f); if (ok) ref = phi_mpi_pi_d(a); break;
+            case 6: ok = add_pi_fast(a, f); if (ok) ref = (float)(kPi + (double)a); break;
+            default: break;
+        }
+        const bool bad = ok && __float_as_uint(f) != __float_as_uint(ref) && !(isnan(f) && isnan(ref));
+        const unsigned m_ok = __ballot_sync(__activemask(), ok);
+        const unsigned m_bad = __ballot_sync(__activemask(), bad);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(out + 0, (unsigned long long)__popc(m_ok));
+            if (m_bad) atomicAdd(out + 1, (unsigned long long)__popc(m_bad));
+        }
+        if (bad && atomicCAS(out + 2, 0ull, 1ull) == 0ull) {
+            out[3] = __float_as_uint(a);
+            out[4] = __float_as_uint(b);
+            out[5] = __float_as_uint(c);
+            out[6] = __float_as_uint(f);
+            out[7] = __float_as_uint(ref);
+        }
+    }
+}
+
+void launch_math_check(int fn, int exhaustive, unsigned long long start, long long n, unsigned long long seed,
+                       unsigned long long* out, int n_sm, cudaStream_t s) {
+    k_math_check<<<n_sm * 16, 256, 0, s>>>(fn, exhaustive, start, n, seed, out);
+}
+
 void launch_tl_collect(const BatchDev& b, const MlpCollect& c, cudaStream_t s) {
     // the bucket table holds the last stage that ran: rebuild the tracklet one
     k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, kTL);

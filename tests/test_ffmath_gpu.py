@@ -1,0 +1,44 @@
+"""The float-float evaluations that stand for the reference's double
+sub-expressions must give the double evaluation's float bit for bit whenever
+their rounding test lets them answer (otherwise the double path runs).
+Unary functions are checked on every float of their working range, the
+others on 2^27-2^28 hashed inputs each; the fast paths must answer almost
+always."""
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+ASIN, ATAN2, PHI, ADD_SQRT, ADD_SQRT3, PHI_MPI_PI, ADD_PI = range(7)
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from sdl_gb300 import Chain, build
+    build.build()
+    return Chain(0)
+
+
+def _bits(x):
+    import struct
+    return struct.unpack("<I", struct.pack("<f", x))[0]
+
+
+@pytest.mark.parametrize("fn,lo,hi,min_answered", [
+    (ASIN, 2.0 ** -30, 0.95, 0.999),        # every float of the std::asin arguments
+    (PHI_MPI_PI, 3.1415927, 9.0, 0.999),    # every float the loop's first step handles
+    (ADD_PI, 2.0 ** -20, 3.1415925, 0.99),  # M_PI + atan2 result
+])
+def test_unary_exhaustive(gpu, fn, lo, hi, min_answered):
+    n = _bits(hi) - _bits(lo) + 1
+    for sign in (0, 0x80000000):
+        r = gpu.math_check(fn, n, start=sign | _bits(lo), exhaustive=True)
+        assert r["mismatches"] == 0, r
+        assert r["answered"] >= min_answered * n, (r["answered"], n)
+
+
+@pytest.mark.parametrize("fn,n,min_answered", [
+    (ATAN2, 1 << 28, 0.99), (PHI, 1 << 27, 1.0), (ADD_SQRT, 1 << 27, 0.99), (ADD_SQRT3, 1 << 27, 0.99)])
+def test_random_inputs(gpu, fn, n, min_answered):
+    r = gpu.math_check(fn, n, seed=12345)
+    assert r["mismatches"] == 0, r
+    assert r["answered"] >= min_answered * n, (r["answered"], n)
