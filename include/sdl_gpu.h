@@ -138,7 +138,10 @@ int sdlg_last_prefilter_times(sdlg_ctx* ctx, float* out2);
 /* Self-check of the float-float evaluations that stand for the reference's
  * double sub-expressions (no counterpart in the reference).  Function fn
  * (0 asin, 1 atan2, 2 hit phi, 3 x + sqrt(y), 4 s + sqrt(a^2+b^2+c^2),
- * 5 Phi_mpi_pi, 6 M_PI + x) is evaluated on n inputs: the float bit patterns
+ * 5 Phi_mpi_pi, 6 M_PI + x, 7 a / sin(b), 8 and 15 the tracklets' multiple
+ * scattering factor with and without its second square root, 9 a + b^2/4,
+ * 10 sin, 11 cos, 12 atan, 13 sqrt(a^2 + b^2), 14 15 a / b) is evaluated on
+ * n inputs: the float bit patterns
  * start .. start+n-1 (exhaustive != 0, unary functions) or hashed pseudo-random
  * inputs from `seed`.  out8: inputs where the fast path answered, of those
  * the ones whose float differs from the double evaluation's (must be 0), a

@@ -923,7 +923,7 @@ int sdlg_last_prefilter_times(sdlg_ctx* ctx, float* out2) {
 int64_t sdlg_last_launches(const sdlg_ctx* ctx) { return ctx ? ctx->launches_per_run : -1; }
 
 int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64_t n, uint64_t seed, uint64_t* out8) {
-    if (!ctx || !out8 || n < 0 || fn < 0 || fn > 6) return SDLG_ERR_ARG;
+    if (!ctx || !out8 || n < 0 || fn < 0 || fn > 15) return SDLG_ERR_ARG;
     cudaSetDevice(ctx->device);
     unsigned long long* d = nullptr;
     CK(cudaMalloc(&d, 8 * sizeof(unsigned long long)));

@@ -49,9 +49,9 @@ struct ModDev {
 // in the binary instead of one per call site keeps the cut kernels small
 // enough for the instruction caches.
 static __device__ __noinline__ float f_asin_d(float x) { return (float)asin((double)x); }
-static __device__ __noinline__ float f_atan(float x) { return (float)atan((double)x); }
-static __device__ __noinline__ float f_sin(float x) { return (float)sin((double)x); }
-static __device__ __noinline__ float f_cos(float x) { return (float)cos((double)x); }
+static __device__ __noinline__ float f_atan_d(float x) { return (float)atan((double)x); }
+static __device__ __noinline__ float f_sin_d(float x) { return (float)sin((double)x); }
+static __device__ __noinline__ float f_cos_d(float x) { return (float)cos((double)x); }
 static __device__ __noinline__ float f_tan(float x) { return (float)tan((double)x); }
 static __device__ __noinline__ double d_sin(double x) { return sin(x); }
 __device__ __forceinline__ float fmin_ref(float a, float b) { return (b < a) ? b : a; }  // std::min
@@ -78,6 +78,128 @@ __device__ __forceinline__ bool f_asin_fast(float x, float& r) {
 static __device__ __noinline__ float f_asin(float x) {
     float r;
     return f_asin_fast(x, r) ? r : f_asin_d(x);
+}
+
+// (float)atan((double)x), (float)sin((double)x), (float)cos((double)x)
+__device__ __forceinline__ bool f_atan_fast(float x, float& r) {
+    if (x == 0.f) {
+        r = x;
+        return true;
+    }
+    const float ax = fabsf(x);
+    if (!(ax > 0x1p-60f && ax < 0x1p60f)) return false;
+    const ffm::ff a = ffm::atan_ff(ffm::ff{ax, 0.f});
+    return ffm::round_unique_rel(x < 0.f ? ffm::neg(a) : a, r);
+}
+static __device__ __noinline__ float f_atan(float x) {
+    float r;
+    return f_atan_fast(x, r) ? r : f_atan_d(x);
+}
+__device__ __forceinline__ bool f_sincos_fast(float x, int shift, float& r) {
+    if (shift == 0 && x == 0.f) {
+        r = x;
+        return true;
+    }
+    if (!(fabsf(x) > 0x1p-60f)) return false;
+    ffm::ff v;
+    return ffm::sincos_ff(x, shift, v) && ffm::round_unique_rel(v, r);
+}
+static __device__ __noinline__ float f_sin(float x) {
+    float r;
+    return f_sincos_fast(x, 0, r) ? r : f_sin_d(x);
+}
+static __device__ __noinline__ float f_cos(float x) {
+    float r;
+    return f_sincos_fast(x, 1, r) ? r : f_cos_d(x);
+}
+
+// (float)(c + (double)a) for the double constants c = M_PI and 2 M_PI (as
+// hi + lo they are 3.6e-15 and 7.1e-15 off; the sum's error is below 2e-13)
+__device__ __forceinline__ bool add_dconst_fast(ffm::ff c, float a, float& r) {
+    return ffm::round_unique(ffm::add(c, a), 2e-13f, r);
+}
+static __device__ __noinline__ float pi_plus(float a) {
+    float r;
+    if (add_dconst_fast(ffm::ff{0x1.921fb6p+1f, -0x1.777a5cp-24f}, a, r)) return r;
+    return (float)(kPi + (double)a);
+}
+static __device__ __noinline__ float two_pi_plus(float a) {
+    float r;
+    if (add_dconst_fast(ffm::ff{0x1.921fb6p+2f, -0x1.777a5cp-23f}, a, r)) return r;
+    return (float)(2 * kPi + (double)a);
+}
+
+// (float)sqrt((double)a*a + (double)b*b)
+static __device__ __noinline__ float hypot_d(float a, float b) {
+    const double da = a, db = b;
+    return (float)sqrt(da * da + db * db);
+}
+__device__ __forceinline__ bool hypot_fast(float a, float b, float& r) {
+    const float m = fmaxf(fabsf(a), fabsf(b));
+    if (!(m > 0x1p-50f && m < 0x1p50f)) return false;
+    return ffm::round_unique_rel(ffm::sqrt_ff(ffm::add(ffm::two_prod(a, a), ffm::two_prod(b, b))), r);
+}
+static __device__ __noinline__ float hypot_ref(float a, float b) {
+    float r;
+    return hypot_fast(a, b, r) ? r : hypot_d(a, b);
+}
+// (float)((double)a * 15.0 / (double)b): the product is exact in double
+static __device__ __noinline__ float times15_over_d(float a, float b) { return (float)((double)a * 15.0 / (double)b); }
+__device__ __forceinline__ bool times15_over_fast(float a, float b, float& r) {
+    if (!(fabsf(a) > 0x1p-60f && fabsf(a) < 0x1p60f && fabsf(b) > 0x1p-60f && fabsf(b) < 0x1p60f)) return false;
+    return ffm::round_unique_rel(ffm::div(ffm::two_prod(a, 15.f), ffm::ff{b, 0.f}), r);
+}
+static __device__ __noinline__ float times15_over(float a, float b) {
+    float r;
+    return times15_over_fast(a, b, r) ? r : times15_over_d(a, b);
+}
+
+// (float)((double)num / sin((double)beta)), the tracklets' pT from a turning angle
+static __device__ __noinline__ float pt_from_d(float num, float beta) { return (float)((double)num / d_sin((double)beta)); }
+__device__ __forceinline__ bool pt_from_fast(float num, float beta, float& r) {
+    const float ab = fabsf(beta);
+    if (!(ab > 0x1p-30f && ab <= 0.8f && fabsf(num) > 0x1p-60f && fabsf(num) < 0x1p60f)) return false;
+    return ffm::round_unique_rel(ffm::div(ffm::ff{num, 0.f}, ffm::sin_small_ff(beta)), r);
+}
+static __device__ __noinline__ float pt_from(float num, float beta) {
+    float r;
+    return pt_from_fast(num, beta, r) ? r : pt_from_d(num, beta);
+}
+
+// Tracklet.cc multiple-scattering factor
+// (float)((double)0.015f * sqrt((double)0.1f + 0.2 * (double)d / (double)50.f) [* sqrt((double)q)])
+static __device__ __noinline__ float muls_d(float d, float q, bool two) {
+    const double m = (double)0.015f * sqrt((double)0.1f + 0.2 * (double)d / (double)50.f);
+    return two ? (float)(m * sqrt((double)q)) : (float)m;
+}
+__device__ __forceinline__ bool muls_fast(float d, float q, bool two, float& r) {
+    if (!(d >= 0.f && d < 1e4f)) return false;  // no cancellation in 0.1 + 0.004 d
+    if (two && !(q > 0x1p-60f && q < 0x1p60f)) return false;
+    // the double 0.2 as hi + lo is 5.6e-17 off
+    const ffm::ff t = ffm::div(ffm::mul(ffm::ff{0x1.99999ap-3f, -0x1.99999ap-29f}, d), ffm::ff{50.f, 0.f});
+    ffm::ff m = ffm::mul(ffm::sqrt_ff(ffm::add(t, 0.1f)), 0.015f);
+    if (two) m = ffm::mul(m, ffm::sqrt_ff(ffm::ff{q, 0.f}));
+    return ffm::round_unique_rel(m, r);
+}
+static __device__ __noinline__ float muls(float d, float q, bool two) {
+    float r;
+    return muls_fast(d, q, two, r) ? r : muls_d(d, q, two);
+}
+
+// (float)((double)head + 0.25 * ((double)t * (double)t)): the square is exact in double
+static __device__ __noinline__ float add_quarter_sq_d(float head, float t) {
+    const double dt = t;
+    return (float)((double)head + 0.25 * (dt * dt));
+}
+__device__ __forceinline__ bool add_quarter_sq_fast(float head, float t, float& r) {
+    if (!(fabsf(t) < 0x1p50f && fabsf(head) < 0x1p100f)) return false;
+    const ffm::ff q = ffm::two_prod(t, t);
+    const ffm::ff v = ffm::add(ffm::ff{__fmul_rn(q.hi, 0.25f), __fmul_rn(q.lo, 0.25f)}, head);
+    return ffm::round_unique(v, __fmul_rn(__fadd_rn(fabsf(head), __fmul_rn(q.hi, 0.25f)), 0x1p-44f), r);
+}
+static __device__ __noinline__ float add_quarter_sq(float head, float t) {
+    float r;
+    return add_quarter_sq_fast(head, t, r) ? r : add_quarter_sq_d(head, t);
 }
 
 // (float)((double)x + sqrt((double)y)), the reference's float + double sqrt of a float
@@ -227,14 +349,17 @@ __device__ constexpr float kDeltaZLum = 15.f;
 // MiniDoublet.cc:741-810
 __device__ __forceinline__ float dphi_threshold(float rt, float asin_rt1, const ModDev& m, float dPhi, float dz) {
     const float mulsB[6] = {0.0052f, 0.0038f, 0.0034f, 0.0034f, 0.0032f, 0.0034f};
-    const float rB[6] = {21.8f, 34.6f, 49.6f, 67.4f, 87.6f, 106.8f};
-    const float rE[5] = {131.4f, 156.2f, 185.6f, 220.3f, 261.5f};
     const unsigned iL = m.layer - 1;
     const float miniSlope = asin_rt1;  // asin(min(rt * k2Rinv1GeVf / 1, 0.95))
     (void)rt;
     const bool barrel = m.subdet == kBarrel;
-    const float rLay = barrel ? rB[iL] : rE[iL];
-    const float miniPVoff = (float)(0.1 / (double)rLay);  // a double division of constants (one per layer)
+    // (float)(0.1 / (double)rLay) for the layer radii 21.8 ... 106.8 (barrel) and
+    // 131.4 ... 261.5 (endcap) of MiniDoublet.cc:763-767: constant per layer
+    constexpr float pvB[6] = {(float)(0.1 / (double)21.8f), (float)(0.1 / (double)34.6f), (float)(0.1 / (double)49.6f),
+                              (float)(0.1 / (double)67.4f), (float)(0.1 / (double)87.6f), (float)(0.1 / (double)106.8f)};
+    constexpr float pvE[5] = {(float)(0.1 / (double)131.4f), (float)(0.1 / (double)156.2f), (float)(0.1 / (double)185.6f),
+                              (float)(0.1 / (double)220.3f), (float)(0.1 / (double)261.5f)};
+    const float miniPVoff = barrel ? pvB[iL] : pvE[iL];
     const float miniMuls = barrel ? mulsB[iL] * 3.f / kPtCut : 0.006f * 3.f / kPtCut;
     if (barrel && m.side == kCenter) return add_dsqrt3(miniSlope, miniMuls, miniPVoff, 0.f);
     if (barrel) return add_dsqrt3(miniSlope, miniMuls, miniPVoff, m.tilt * miniSlope);
@@ -249,20 +374,20 @@ __device__ __forceinline__ void shift_strip(const P3& lo, const P3& up, const Mo
     const P3& pix = (ps && !pixLower) ? up : lo;
     const P3& str = (ps && !pixLower) ? lo : up;
     const bool isEndcap = lm.subdet == kEndcap;
-    const float angleA = (float)fabs((double)f_atan(pix.rt / pix.z));
+    const float angleA = fabsf(f_atan(pix.rt / pix.z));
     const float angleB = isEndcap ? (float)(kPi / 2.) : f_atan(lm.drdz_s);
     float sep = lm.gap;
     if (ps && !pixLower) sep *= -1;
     const float sAB = f_sin(angleA + angleB);
     const float drprime = (sep / sAB) * f_sin(angleA);
     const float slope = lm.slope_s;
-    const float absArctanSlope = (slope != kSdlInf) ? (float)fabs((double)f_atan(slope)) : (float)(kPi / 2);
+    const float absArctanSlope = (slope != kSdlInf) ? fabsf(f_atan(slope)) : (float)(kPi / 2);
     const float xp = pix.x, yp = pix.y;
     float angleM;
     if (xp > 0 && yp > 0) angleM = absArctanSlope;
-    else if (xp > 0 && yp < 0) angleM = (float)(kPi - (double)absArctanSlope);
-    else if (xp < 0 && yp < 0) angleM = (float)(kPi + (double)absArctanSlope);
-    else angleM = (float)(2 * kPi - (double)absArctanSlope);
+    else if (xp > 0 && yp < 0) angleM = pi_plus(-absArctanSlope);  // (float)(kPi - (double)a)
+    else if (xp < 0 && yp < 0) angleM = pi_plus(absArctanSlope);
+    else angleM = two_pi_plus(-absArctanSlope);
     const float dx = drprime * f_sin(angleM);
     const float dy = drprime * f_cos(angleM);
     const float xa = xp + dx, ya = yp + dy;
@@ -275,8 +400,9 @@ __device__ __forceinline__ void shift_strip(const P3& lo, const P3& up, const Mo
     }
     const float absdzprime = fabsf(sep / sAB * f_cos(angleA));
     float abszn;
-    if (pixLower) abszn = (float)(fabs((double)pix.z) + (double)absdzprime);
-    else abszn = (float)(fabs((double)pix.z) - (double)absdzprime);
+    // one double operation on two floats rounded to float: the float operation
+    if (pixLower) abszn = fabsf(pix.z) + absdzprime;
+    else abszn = fabsf(pix.z) - absdzprime;
     zn = abszn * ((pix.z > 0) ? 1 : -1);
 }
 
@@ -333,7 +459,7 @@ __device__ __forceinline__ bool md_endcap(const P3& lo, const P3& up, float pixA
     }
     const float miniCut = dphi_threshold(0.f, pixAsin, lm, v.dphi, dz);
     if (!(fabsf(v.dphi) < miniCut)) return false;
-    const float dzFrac = (float)((double)fabsf(dz) / fabs((double)lo.z));
+    const float dzFrac = fabsf(dz) / fabsf(lo.z);  // a double division of two floats rounded to float
     v.dphichange = v.dphi / dzFrac * (1.f + dzFrac);
     return fabsf(v.dphichange) < miniCut;
 }
@@ -351,8 +477,7 @@ __device__ __forceinline__ void dalpha_threshold(const MDView& im, const MDView&
     const ModDev& I = *im.m;
     const ModDev& O = *om.m;
     const float sdMuls = I.subdet == kBarrel ? mulsB[I.layer - 1] * 3.f / kPtCut : 0.006f * 3.f / kPtCut;
-    const double dyy = (double)(om.a.y - im.a.y), dxx = (double)(om.a.x - im.a.x);
-    const float segmentDr = (float)sqrt(dyy * dyy + dxx * dxx);
+    const float segmentDr = hypot_ref(om.a.y - im.a.y, om.a.x - im.a.x);
     const float dAlpha_Bfield = f_asin(fmin_ref(segmentDr * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
     const bool inTilt = I.subdet == kBarrel && I.side != kCenter;
     const bool outTilt = O.subdet == kBarrel && O.side != kCenter;
@@ -361,11 +486,11 @@ __device__ __forceinline__ void dalpha_threshold(const MDView& im, const MDView&
     const float miniDelta = I.gap;
     float lumIn, lumOut;
     if (I.subdet == kBarrel) lumIn = iTilt * dAlpha_Bfield;
-    else if (I.type == kPS) lumIn = (float)((double)im.dphi * 15.0 / (double)im.shiftedDz);
-    else lumIn = (float)((double)im.dphi * 15.0 / (double)im.dz);
+    else if (I.type == kPS) lumIn = times15_over(im.dphi, im.shiftedDz);
+    else lumIn = times15_over(im.dphi, im.dz);
     if (O.subdet == kBarrel) lumOut = oTilt * dAlpha_Bfield;
-    else if (O.type == kPS) lumOut = (float)((double)om.dphi * 15.0 / (double)om.shiftedDz);
-    else lumOut = (float)((double)om.dphi * 15.0 / (double)om.dz);
+    else if (O.type == kPS) lumOut = times15_over(om.dphi, om.shiftedDz);
+    else lumOut = times15_over(om.dphi, om.dz);
     const float resIn = 0.02f / miniDelta * (I.subdet == kBarrel ? 1.0f : fabsf(im.a.z / im.a.rt));
     const float resOut = 0.02f / miniDelta * (O.subdet == kBarrel ? 1.0f : fabsf(om.a.z / om.a.rt));
     const float res = resIn + resOut;
@@ -578,21 +703,21 @@ __device__ __forceinline__ void delta_beta_iterations(float& betaIn, float& beta
         const float betaInUpd = betaIn + copysignf(f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
         const float betaOutUpd = betaOut + copysignf(f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaOut);
         betaAv = 0.5f * (betaInUpd + betaOutUpd);
-        pt_beta = (float)((double)(dr * k2Rinv1GeVf) / d_sin((double)betaAv));
+        pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
         betaIn = betaIn + copysignf(f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
         betaOut = betaOut + copysignf(f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaOut);
         betaAv = 0.5f * (betaIn + betaOut);
-        pt_beta = (float)((double)(dr * k2Rinv1GeVf) / d_sin((double)betaAv));
+        pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
     } else if (lIn < 11 && (double)fabsf(betaOut) < 0.2 * (double)fabsf(betaIn) && fabsf(pt_beta) < 12.f * pt_betaMax) {
-        const float pt_betaIn = (float)((double)(dr * k2Rinv1GeVf) / d_sin((double)betaIn));
+        const float pt_betaIn = pt_from(dr * k2Rinv1GeVf, betaIn);
         const float betaInUpd = betaIn + copysignf(f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), betaIn);
         const float betaOutUpd = betaOut + copysignf(f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), betaIn);
         betaAv = (fabsf(betaOut) > 0.2f * fabsf(betaIn)) ? (0.5f * (betaInUpd + betaOutUpd)) : betaInUpd;
-        pt_beta = (float)((double)(dr * k2Rinv1GeVf) / d_sin((double)betaAv));
+        pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
         betaIn = betaIn + copysignf(f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
         betaOut = betaOut + copysignf(f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
         betaAv = 0.5f * (betaIn + betaOut);
-        pt_beta = (float)((double)(dr * k2Rinv1GeVf) / d_sin((double)betaAv));
+        pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
     }
 }
 
@@ -600,8 +725,7 @@ __device__ __forceinline__ float dbeta_cut2(float dBetaRes, float dBetaMuls, flo
                                             float inMax, float outMin, float outMax) {
     const float dBetaRIn2 = 0;
     const float head = dBetaRes * dBetaRes * 2.0f + dBetaMuls * dBetaMuls + dBetaLum2 + dBetaRIn2 + dBetaROut2;
-    const double t = (double)(fabsf(inMin - inMax) + fabsf(outMin - outMax));
-    return (float)((double)head + 0.25 * (t * t));
+    return add_quarter_sq(head, fabsf(inMin - inMax) + fabsf(outMin - outMax));
 }
 
 
@@ -625,7 +749,7 @@ __device__ __forceinline__ int tl_phaseA(const SGV& S, const SGV& T, float& sdlC
         const float zHi = zIn + (zIn + kDeltaZLum) * (rtRatio - 1.f) * (zIn < 0.f ? 1.f : dzDrtScale) + (zpitch_InLo + zpitch_OutLo);
         const float zLo = zIn + (zIn - kDeltaZLum) * (rtRatio - 1.f) * (zIn > 0.f ? 1.f : dzDrtScale) - (zpitch_InLo + zpitch_OutLo);
         if (!(zOut >= zLo && zOut <= zHi)) return kAlgoNone;
-        mulsF = (float)((double)0.015f * sqrt((double)0.1f + 0.2 * (double)(rtOut - rtIn) / (double)50.f) * sqrt((double)(S.lr3z / rtIn)));
+        mulsF = muls(rtOut - rtIn, S.lr3z / rtIn, true);
         const float sdlMuls = mulsF * 3.f / kPtCut * 4.f;
         const float sdlPVoff = 0.1f / rtOut;
         sdlCut = add_dsqrt(T.la1, sdlMuls * sdlMuls + sdlPVoff * sdlPVoff);
@@ -660,7 +784,7 @@ __device__ __forceinline__ int tl_phaseA(const SGV& S, const SGV& T, float& sdlC
         if (!(rtOut >= rtLo && rtOut <= rtHi)) return kAlgoNone;
         const float kZ = (zOut - zIn) / (S.uz - S.lz);
         if (!(kZ >= 0)) return kAlgoNone;
-        mulsF = (float)((double)0.015f * sqrt((double)0.1f + 0.2 * (double)(rtOut - rtIn) / (double)50.f) * sqrt((double)(S.lr3z / rtIn)));
+        mulsF = muls(rtOut - rtIn, S.lr3z / rtIn, true);
         const float sdlMuls = mulsF * 3.f / kPtCut * 4.f;
         const float sdlPVoff = 0.1f / rtOut;
         sdlCut = add_dsqrt(T.la1, sdlMuls * sdlMuls + sdlPVoff * sdlPVoff);
@@ -679,7 +803,7 @@ __device__ __forceinline__ int tl_phaseA(const SGV& S, const SGV& T, float& sdlC
         if (!(rtOut >= rtLo)) return kAlgoNone;
         const float rtHi = rtIn * (1.f + dz / (zIn - dLum)) + rtGeom;
         if (!(rtOut >= rtLo && rtOut <= rtHi)) return kAlgoNone;
-        mulsF = (float)((double)0.015f * sqrt((double)0.1f + 0.2 * (double)(rtOut - rtIn) / (double)50.f));
+        mulsF = muls(rtOut - rtIn, 0.f, false);
         const float sdlMuls = mulsF * 3.f / kPtCut * 4.f;
         const float sdlPVoff = 0.1f / rtOut;
         sdlCut = add_dsqrt(T.la1, sdlMuls * sdlMuls + sdlPVoff * sdlPVoff);
@@ -738,15 +862,15 @@ static __device__ __noinline__ bool tl_phaseB(int algo, const SGV& S, const SGV&
             betaOutRHmin = -dphi(hiE, sub(hiE, OutLo)) + dphi(hiE, sub(hiE, InLo));
             betaOutRHmax = -dphi(loE, sub(loE, OutLo)) + dphi(loE, sub(loE, InLo));
             const float sinDPhi = f_sin(dPhi);
-            const double rr = (double)((hiE.rt - loE.rt) * sinDPhi / dr);
-            dBetaROut2 = (float)(rr * rr);
+            const float rr = (hiE.rt - loE.rt) * sinDPhi / dr;
+            dBetaROut2 = rr * rr;  // the double square of a float is exact: one rounding to float
         } else {
             // (rt - rt) * sin(dPhi) / dr squared: sin(dPhi) is finite here
             // (|dPhi| <= sdlCut), so the product is a signed zero and only
             // its square matters
             betaOutRHmin = betaOut; betaOutRHmax = betaOut;
-            const double rr = (double)((OutUp.rt - OutUp.rt) * 0.f / dr);
-            dBetaROut2 = (float)(rr * rr);
+            const float rr = (OutUp.rt - OutUp.rt) * 0.f / dr;
+            dBetaROut2 = rr * rr;
         }
         alphaOutReg = T.dpc;
         lIn = 5;
@@ -769,11 +893,11 @@ static __device__ __noinline__ bool tl_phaseB(int algo, const SGV& S, const SGV&
             const float sinDPhi = f_sin(dPhi);
             const float hrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, true);
             const float lrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, false);
-            const double rr = (double)((hrt - lrt) * sinDPhi / dr);
-            dBetaROut2 = (float)(rr * rr);
+            const float rr = (hrt - lrt) * sinDPhi / dr;
+            dBetaROut2 = rr * rr;
         } else {
-            const double rr = (double)((OutUp.rt - OutUp.rt) * 0.f / dr);  // see the BBBB branch
-            dBetaROut2 = (float)(rr * rr);
+            const float rr = (OutUp.rt - OutUp.rt) * 0.f / dr;  // see the BBBB branch
+            dBetaROut2 = rr * rr;
         }
         alphaOutReg = S.dpc;  // sdOut_alpha is the inner segment's (Tracklet.cc:1790)
         lIn = 5;
@@ -799,7 +923,7 @@ static __device__ __noinline__ bool tl_phaseB(int algo, const SGV& S, const SGV&
         lOut = 13;
     }
     float betaAv = 0.5f * (betaIn + betaOut);
-    float pt_beta = (float)((double)(dr * k2Rinv1GeVf) / d_sin((double)betaAv));
+    float pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
     delta_beta_iterations(betaIn, betaOut, betaAv, pt_beta, sdIn_dr, sdOut_dr, dr, lIn, pt_betaMax);
     const float betaInMMSF = (fabsf(betaInRHmin + betaInRHmax) > 0) ? (2.f * betaIn / fabsf(betaInRHmin + betaInRHmax)) : 0.f;
     const float betaOutMMSF = (fabsf(betaOutRHmin + betaOutRHmax) > 0) ? (2.f * betaOut / fabsf(betaOutRHmin + betaOutRHmax)) : 0.f;

@@ -170,5 +170,66 @@ __device__ __forceinline__ ff asin_ff(float x) {
     return x < 0.f ? neg(a) : a;
 }
 
+// sin(x) for |x| <= 0.8: x + x P(x^2) with the Taylor series to x^13 (the
+// truncation error is below |x| 2^-45); the x^2..x^6 terms in float-float,
+// the rest in float.  Relative error below 2^-42.
+__device__ __forceinline__ ff sin_small_ff(float x) {
+    const ff x2 = two_prod(x, x);
+    const float z = x2.hi;
+    const float t = __fadd_rn(0x1.71de3ap-19f, __fmul_rn(z, __fsub_rn(__fmul_rn(z, 0x1.612462p-33f), 0x1.ae6456p-26f)));
+    ff h = add(ff{-0x1.a01a02p-13f, 0x1.7f97fap-39f}, __fmul_rn(z, t));
+    h = add(ff{0x1.111112p-7f, -0x1.dddddep-32f}, mul(x2, h));
+    h = add(ff{-0x1.555556p-3f, 0x1.555556p-28f}, mul(x2, h));
+    return add(mul(mul(x2, h), x), x);
+}
+
+// cos(x) for |x| <= 0.8: Taylor series to x^14 (truncation below 2^-49),
+// the x^2..x^8 terms in float-float.  Relative error below 2^-43.
+__device__ __forceinline__ ff cos_small_ff(float x) {
+    const ff x2 = two_prod(x, x);
+    const float z = x2.hi;
+    const float t = __fsub_rn(__fmul_rn(z, __fsub_rn(0x1.1eed8ep-29f, __fmul_rn(z, 0x1.93974ap-37f))), 0x1.27e4fcp-22f);
+    ff h = add(ff{0x1.a01a02p-16f, -0x1.7f97fap-42f}, __fmul_rn(z, t));
+    h = add(ff{-0x1.6c16c2p-10f, 0x1.27d27ep-35f}, mul(x2, h));
+    h = add(ff{0x1.555556p-5f, -0x1.555556p-30f}, mul(x2, h));
+    h = add(ff{-0.5f, 0.f}, mul(x2, h));
+    return add(mul(x2, h), 1.f);
+}
+
+// sin(x) (cosine: shift = 1) for |x| <= 8: x = r + k pi/2 with pi/2 split in
+// three parts (the first two with at most 20 significant bits, so k times
+// them is exact; the split is 2e-21 off), then the series on |r| <= pi/4.
+// Relative error below 2^-42; false when |r| < 2^-16 after a reduction
+// (a result near a zero of the function).
+__device__ __forceinline__ bool sincos_ff(float x, int shift, ff& out) {
+    if (!(fabsf(x) <= 8.f)) return false;
+    const int k = __float2int_rn(__fmul_rn(x, 0x1.45f306p-1f));
+    ff s, c;
+    if (k == 0) {
+        if (shift == 0) {
+            out = sin_small_ff(x);
+            return true;
+        }
+        s = sin_small_ff(x);
+        c = cos_small_ff(x);
+    } else {
+        const float fk = (float)k;
+        const float r1 = __fsub_rn(x, __fmul_rn(fk, 0x1.921fc0p+0f));
+        ff r = two_sum(r1, -__fmul_rn(fk, -0x1.5777a0p-21f));
+        r = add(r, -__fmul_rn(fk, -0x1.73dcb4p-43f));
+        if (!(fabsf(r.hi) > 0x1p-16f)) return false;
+        const ff s0 = sin_small_ff(r.hi), c0 = cos_small_ff(r.hi);
+        s = add(s0, __fmul_rn(c0.hi, r.lo));  // sin(hi + lo) = sin hi + lo cos hi + O(lo^2)
+        c = add(c0, -__fmul_rn(s0.hi, r.lo));
+    }
+    switch ((k + shift) & 3) {
+        case 0: out = s; break;
+        case 1: out = c; break;
+        case 2: out = neg(s); break;
+        default: out = neg(c);
+    }
+    return true;
+}
+
 }  // namespace ffm
 }  // namespace sdlg

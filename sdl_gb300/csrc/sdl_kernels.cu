@@ -1365,6 +1365,26 @@ __global__ void k_math_check(int fn, int exhaustive, unsigned long long start, l
                     a = sa * hash_log(h1, -20.f, 4.f);
                     b = hash_log(h2, -40.f, 6.f);
                     break;
+                case 7:  // (dr k, beta): |beta| below 0.5
+                    a = hash_log(h1, -8.f, 1.f);
+                    b = sa * hash_log(h2, -24.f, -1.f);
+                    break;
+                case 8: case 15:  // (rtOut - rtIn, r3/rt)
+                    a = hash_log(h1, -10.f, 8.f);
+                    b = 1.f + hash_log(h2, -12.f, 2.f);
+                    break;
+                case 9:  // (head, t)
+                    a = hash_log(h1, -30.f, 2.f);
+                    b = hash_log(h2, -16.f, 2.f);
+                    break;
+                case 13:  // coordinate differences
+                    a = sa * hash_log(h1, -12.f, 8.f);
+                    b = sb * hash_log(h2, -12.f, 8.f);
+                    break;
+                case 14:  // (dphi, dz)
+                    a = sa * hash_log(h1, -24.f, 1.f);
+                    b = sb * hash_log(h2, -8.f, 4.f);
+                    break;
                 case 4:
                     a = hash_log(h1, -10.f, 1.f);
                     b = hash_log(h2, -14.f, 1.f);
@@ -1390,6 +1410,15 @@ __global__ void k_math_check(int fn, int exhaustive, unsigned long long start, l
             case 4: ok = add_dsqrt3_fast(a, b, c, d, f); if (ok) ref = add_dsqrt3_d(a, b, c, d); break;
             case 5: ok = phi_mpi_pi_fast(a, f); if (ok) ref = phi_mpi_pi_d(a); break;
             case 6: ok = add_pi_fast(a, f); if (ok) ref = (float)(kPi + (double)a); break;
+            case 7: ok = pt_from_fast(a, b, f); if (ok) ref = pt_from_d(a, b); break;
+            case 8: ok = muls_fast(a, b, true, f); if (ok) ref = muls_d(a, b, true); break;
+            case 9: ok = add_quarter_sq_fast(a, b, f); if (ok) ref = add_quarter_sq_d(a, b); break;
+            case 10: ok = f_sincos_fast(a, 0, f); if (ok) ref = f_sin_d(a); break;
+            case 11: ok = f_sincos_fast(a, 1, f); if (ok) ref = f_cos_d(a); break;
+            case 12: ok = f_atan_fast(a, f); if (ok) ref = f_atan_d(a); break;
+            case 13: ok = hypot_fast(a, b, f); if (ok) ref = hypot_d(a, b); break;
+            case 14: ok = times15_over_fast(a, b, f); if (ok) ref = times15_over_d(a, b); break;
+            case 15: ok = muls_fast(a, b, false, f); if (ok) ref = muls_d(a, b, false); break;
             default: break;
         }
         const bool bad = ok && __float_as_uint(f) != __float_as_uint(ref) && !(isnan(f) && isnan(ref));

@@ -8,7 +8,7 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-ASIN, ATAN2, PHI, ADD_SQRT, ADD_SQRT3, PHI_MPI_PI, ADD_PI = range(7)
+ASIN, ATAN2, PHI, ADD_SQRT, ADD_SQRT3, PHI_MPI_PI, ADD_PI, PT, MULS, QSQ, SIN, COS, ATAN, HYPOT, T15, MULS1 = range(16)
 
 
 @pytest.fixture(scope="module")
@@ -27,6 +27,9 @@ def _bits(x):
     (ASIN, 2.0 ** -30, 0.95, 0.999),        # every float of the std::asin arguments
     (PHI_MPI_PI, 3.1415927, 9.0, 0.999),    # every float the loop's first step handles
     (ADD_PI, 2.0 ** -20, 3.1415925, 0.99),  # M_PI + atan2 result
+    (SIN, 2.0 ** -30, 8.0, 0.999),          # every float of the angles the strip shift uses
+    (COS, 2.0 ** -30, 8.0, 0.999),
+    (ATAN, 2.0 ** -40, 2.0 ** 40, 0.999),
 ])
 def test_unary_exhaustive(gpu, fn, lo, hi, min_answered):
     n = _bits(hi) - _bits(lo) + 1
@@ -37,7 +40,9 @@ def test_unary_exhaustive(gpu, fn, lo, hi, min_answered):
 
 
 @pytest.mark.parametrize("fn,n,min_answered", [
-    (ATAN2, 1 << 28, 0.99), (PHI, 1 << 27, 1.0), (ADD_SQRT, 1 << 27, 0.99), (ADD_SQRT3, 1 << 27, 0.99)])
+    (ATAN2, 1 << 28, 0.99), (PHI, 1 << 27, 1.0), (ADD_SQRT, 1 << 27, 0.99), (ADD_SQRT3, 1 << 27, 0.99),
+    (PT, 1 << 27, 0.99), (MULS, 1 << 27, 0.99), (MULS1, 1 << 27, 0.99), (QSQ, 1 << 27, 0.99),
+    (HYPOT, 1 << 27, 0.99), (T15, 1 << 27, 0.99)])
 def test_random_inputs(gpu, fn, n, min_answered):
     r = gpu.math_check(fn, n, seed=12345)
     assert r["mismatches"] == 0, r
