@@ -831,7 +831,12 @@ __device__ __forceinline__ int tl_phaseA(const SGV& S, const SGV& T, float& sdlC
 
 // ---- phase B: the remaining cuts (mid-point direction, betaIn, the
 // deltaBeta iterations, betaOut and the deltaBeta cut)
-static __device__ __noinline__ bool tl_phaseB(int algo, const SGV& S, const SGV& T, float sdlCut, float mulsF, bool nm1) {
+// (The records are loaded here from their indices: passing them by reference
+// to this out-of-line function would put them on the stack.)
+static __device__ __noinline__ bool tl_phaseB(int algo, const float* __restrict__ pack, int s, int t, float sdlCut,
+                                               float mulsF, bool nm1) {
+    const SGV S = load_sgv(pack, s);
+    const SGV T = load_sgv(pack, t);
     const float pt_betaMax = 7.0f;
     const P3 InLo = S.lo(), InUp = S.up(), OutLo = T.lo(), OutUp = T.up();
     const P3 mid = midpoint(InLo, OutLo);

@@ -715,9 +715,7 @@ __device__ __forceinline__ void tl_queue_push(const BatchDev& b, const TLQueue& 
         const float qc_ = q.cut[k], qm_ = q.muls[k];
         __syncwarp();
         qn -= kWarp;
-        const SGV S = load_sgv(b.sgpack, qs_);
-        const SGV T = load_sgv(b.sgpack, qt_);
-        const bool pass = tl_phaseB(qa_, S, T, qc_, qm_, nm1);
+        const bool pass = tl_phaseB(qa_, b.sgpack, qs_, qt_, qc_, qm_, nm1);
         append_rec(b, kTL, pass, qs_, qt_, OG(b, kSG, qs_), nullptr);
     }
 }
@@ -730,9 +728,7 @@ __device__ __forceinline__ void tl_queue_drain(const BatchDev& b, const TLQueue&
     if (lane < qn) {
         qs_ = q.s[lane];
         qt_ = q.t[lane];
-        const SGV S = load_sgv(b.sgpack, qs_);
-        const SGV T = load_sgv(b.sgpack, qt_);
-        pass = tl_phaseB(q.algo[lane], S, T, q.cut[lane], q.muls[lane], nm1);
+        pass = tl_phaseB(q.algo[lane], b.sgpack, qs_, qt_, q.cut[lane], q.muls[lane], nm1);
     }
     __syncwarp();
     append_rec(b, kTL, pass, qs_, qt_, pass ? OG(b, kSG, qs_) : 0, nullptr);
@@ -748,7 +744,7 @@ __device__ __forceinline__ int tl_outer_of(const BatchDev& b, bool lay, int s, i
 // (float cuts) runs on every candidate; its survivors go to a per-warp queue
 // in shared memory and phase B (the double-precision part) runs on full warps
 // of queued candidates.
-__global__ void __launch_bounds__(kEnumThreads) k_tl_enum(BatchDev b) {
+__global__ void __launch_bounds__(kEnumThreads, 3) k_tl_enum(BatchDev b) {
     if (halted(b)) return;
     const int64_t nobj = n_inner(b, kTL);
     if (nobj <= 0) return;
@@ -890,7 +886,7 @@ __global__ void __launch_bounds__(kMlpTile) k_tl_prefilter(BatchDev b) {
 // The reference's tracklet cuts on the candidates the pre-filter kept:
 // phase A on every one, phase B on full warps of its survivors, exactly as
 // k_tl_enum does for all candidates.
-__global__ void __launch_bounds__(kEnumThreads) k_tl_exact(BatchDev b) {
+__global__ void __launch_bounds__(kEnumThreads, 3) k_tl_exact(BatchDev b) {
     if (halted(b)) return;
     const int64_t n = min((int64_t)*b.n_kept, b.kept_cap);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -959,7 +955,7 @@ __global__ void k_tl_collect(BatchDev b, MlpCollect col) {
             float cut = 0.f, muls = 0.f;
             const int algo = tl_phaseA(S, T, cut, muls);
             if (algo != kAlgoNone) {
-                const bool pass = tl_phaseB(algo, S, T, cut, muls, false);
+                const bool pass = tl_phaseB(algo, b.sgpack, s, tt, cut, muls, false);
                 label = pass ? 1.f : 0.f;
                 keep = pass || hash_unit((unsigned long long)c, col.seed) < col.neg_keep;
                 if (keep) tl_features(feat_in(S, T), f);
