@@ -6,9 +6,9 @@ tensor-core inference kernel (logits) and the training kernels (loss and
 gradient) can be checked against it:
 
     x1 = bf16(x)                      12 features
-    h1 = bf16(relu(W1' x1 + b1))      W1' = bf16(W1), 64 units
-    h2 = relu(W2' h1 + b2)            W2' = bf16(W2), 64 units
-    z  = b3 + w3' . h2                w3' = bf16(w3)
+    h1 = bf16(relu(W1' x1 + b1'))     W1' = bf16(W1), b1' = bf16(b1), 64 units
+    h2 = relu(W2' h1 + b2')           W2' = bf16(W2), b2' = bf16(b2), 64 units
+    z  = b3 + w3' . h2                w3' = bf16(w3), b3 FP32
 
 loss_i = w_i * (softplus(z_i) - y_i z_i); the gradient is taken with the
 BF16 roundings treated as the identity (as the training kernels do).
@@ -46,9 +46,9 @@ def forward(p, x, exact: bool = False):
     r = (lambda a: np.asarray(a, np.float64)) if exact else (lambda a: bf16(np.asarray(a, np.float32)).astype(np.float64))
     w1, b1, w2, b2, w3, b3 = unpack(p)
     x1 = r(np.asarray(x, np.float64 if exact else np.float32).reshape(-1, N_IN))
-    a1 = x1 @ r(w1).T + np.asarray(b1, np.float64)
+    a1 = x1 @ r(w1).T + r(b1)
     h1 = np.maximum(a1, 0.0) if exact else bf16(np.maximum(a1, 0.0).astype(np.float32)).astype(np.float64)
-    a2 = h1 @ r(w2).T + np.asarray(b2, np.float64)
+    a2 = h1 @ r(w2).T + r(b2)
     h2 = np.maximum(a2, 0.0)
     z = h2 @ r(w3) + float(b3)
     return z, (x1, h1, h2)

@@ -352,6 +352,7 @@ int ensure_buffers(sdlg_ctx* ctx) {
     AL(b.kept, b.kept_cap);
     AL(b.n_kept, 1);
     AL(b.sgpack, ctx->cap_obj[kSG] * PK_N);
+    AL(b.sgfeat, ctx->cap_obj[kSG] * kFeatN);
     AL(b.counters, ctx->n_ev * 110);
     AL(b.status, 1);
     AL(b.task, kNumStages);

@@ -622,60 +622,48 @@ __device__ __forceinline__ SGV load_sgv(const float* __restrict__ pack, int64_t 
 // betaOut angles the exact cuts test (Tracklet.cc:1205-1260), the rz
 // pointing residual of the outer anchor against the inner segment, a signed
 // 1/pT estimate from the mean beta, and a code of the anchor module types.
-// Every feature is scaled to O(1) and clamped to [-16, 16].
+// Every feature is scaled to O(1) and clamped to [-16, 16].  They read one
+// 32-byte record of each segment (k_sg_pack): the inner segment's in its
+// inner role, the outer segment's in its outer role.
 __device__ __forceinline__ float wrap_pi_f(float x) { return x - 6.28318531f * rintf(x * 0.159154943f); }
-// the packed-record fields the features read (inner segment S, outer T)
-struct FeatIn {
-    float slx, sly, slz, slrt, slphi, suz, surt, sdpc;
-    float tux, tuy, tuz, turt, tuphi, talphaup;
-    uint32_t sflags, tflags;
+constexpr int kFeatN = 16;  // floats per segment: inner-role record, outer-role record
+struct FeatS {               // a segment as the inner one
+    float lx, ly, lz, lrt, lphi, dpc, slope, code;  // lower anchor; dPhiChange; rz slope; module code
 };
-__device__ __forceinline__ FeatIn feat_in(const SGV& S, const SGV& T) {
-    FeatIn in;
-    in.slx = S.lx; in.sly = S.ly; in.slz = S.lz; in.slrt = S.lrt; in.slphi = S.lphi;
-    in.suz = S.uz; in.surt = S.urt; in.sdpc = S.dpc; in.sflags = S.flags;
-    in.tux = T.ux; in.tuy = T.uy; in.tuz = T.uz; in.turt = T.urt; in.tuphi = T.uphi; in.talphaup = T.alphaup;
-    in.tflags = T.flags;
-    return in;
+struct FeatT {               // a segment as the outer one
+    float ux, uy, uz, urt, uphi, alphaup, code, pad;  // upper anchor; direction angle; module code
+};
+__device__ __forceinline__ FeatS feat_s(const float* __restrict__ f, int64_t s) {
+    const float4* q = reinterpret_cast<const float4*>(f + s * kFeatN);
+    const float4 a = __ldg(q), b = __ldg(q + 1);
+    return FeatS{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 }
-// the same fields straight from the packed records (9 of their 14 float4s)
-__device__ __forceinline__ FeatIn feat_in(const float* __restrict__ pack, int64_t s, int64_t t) {
-    const float4* a = reinterpret_cast<const float4*>(pack + s * PK_N);
-    const float4* b = reinterpret_cast<const float4*>(pack + t * PK_N);
-    const float4 a0 = __ldg(a + 0), a1 = __ldg(a + 1), a3 = __ldg(a + 3), a4 = __ldg(a + 4), a6 = __ldg(a + 6);
-    const float4 b2 = __ldg(b + 2), b3 = __ldg(b + 3), b5 = __ldg(b + 5), b6 = __ldg(b + 6);
-    FeatIn in;
-    in.slx = a0.x; in.sly = a0.y; in.slz = a0.z; in.slrt = a0.w; in.slphi = a1.x;
-    in.suz = a3.x; in.surt = a3.y; in.sdpc = a4.x; in.sflags = __float_as_uint(a6.z);
-    in.tux = b2.z; in.tuy = b2.w; in.tuz = b3.x; in.turt = b3.y; in.tuphi = b3.z; in.talphaup = b5.z;
-    in.tflags = __float_as_uint(b6.z);
-    return in;
+__device__ __forceinline__ FeatT feat_t(const float* __restrict__ f, int64_t t) {
+    const float4* q = reinterpret_cast<const float4*>(f + t * kFeatN + 8);
+    const float4 a = __ldg(q), b = __ldg(q + 1);
+    return FeatT{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
 }
-__device__ __forceinline__ void tl_features(const FeatIn& in, float* f) {
-    const float ax = in.tux - in.slx, ay = in.tuy - in.sly;
+__device__ __forceinline__ void tl_features(const FeatS& S, const FeatT& T, float* f) {
+    const float ax = T.ux - S.lx, ay = T.uy - S.ly;
     const float dr = sqrtf(ax * ax + ay * ay);
     const float phiAxis = atan2f(ay, ax);
-    const float betaIn = in.sdpc - wrap_pi_f(phiAxis - in.slphi);
-    const float betaOut = -in.talphaup + wrap_pi_f(phiAxis - in.tuphi);
-    const float drIn = in.surt - in.slrt;
-    const float slope = (in.suz - in.slz) / (fabsf(drIn) > 1e-3f ? drIn : copysignf(1e-3f, drIn));
-    const float zRes = in.tuz - (in.slz + slope * (in.turt - in.slrt));
-    const float invPt = __sinf(0.5f * (betaIn + betaOut)) / (fmaxf(dr, 1e-3f) * k2Rinv1GeVf);
-    const uint32_t fs = in.sflags, ft = in.tflags;
+    const float betaIn = S.dpc - wrap_pi_f(phiAxis - S.lphi);
+    const float betaOut = -T.alphaup + wrap_pi_f(phiAxis - T.uphi);
+    const float zRes = T.uz - (S.lz + S.slope * (T.urt - S.lrt));
+    const float invPt = __fdividef(__sinf(0.5f * (betaIn + betaOut)), fmaxf(dr, 1e-3f) * k2Rinv1GeVf);
     float v[12];
-    v[0] = in.slrt * 0.01f;
-    v[1] = in.slz * 0.01f;
-    v[2] = in.turt * 0.01f;
-    v[3] = in.tuz * 0.01f;
-    v[4] = wrap_pi_f(in.tuphi - in.slphi) * 10.f;
-    v[5] = in.sdpc * 10.f;
-    v[6] = in.talphaup * 10.f;
+    v[0] = S.lrt * 0.01f;
+    v[1] = S.lz * 0.01f;
+    v[2] = T.urt * 0.01f;
+    v[3] = T.uz * 0.01f;
+    v[4] = wrap_pi_f(T.uphi - S.lphi) * 10.f;
+    v[5] = S.dpc * 10.f;
+    v[6] = T.alphaup * 10.f;
     v[7] = betaIn * 10.f;
     v[8] = betaOut * 10.f;
     v[9] = zRes * 0.1f;
     v[10] = invPt;
-    v[11] = ((fs & F_LO_E) ? 1.f : 0.f) + ((ft & F_UP_E) ? 0.5f : 0.f) + ((fs & F_LO_PS) ? 0.25f : 0.f) +
-            ((ft & F_UP_2S) ? 0.125f : 0.f);
+    v[11] = S.code + T.code;
 #pragma unroll
     for (int k = 0; k < 12; ++k) f[k] = fmaxf(fminf(v[k], 16.f), -16.f);
 }

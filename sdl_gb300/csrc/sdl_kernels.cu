@@ -682,6 +682,16 @@ __global__ void k_sg_pack(BatchDev b) {
         v[PK_S0] = v[PK_S1] = v[PK_S2] = v[PK_S3] = 0.f;
         float4* dst = reinterpret_cast<float4*>(&AT(b.sgpack, s * PK_N, b.obj[kSG].cap * PK_N));
         for (int k = 0; k < PK_N / 4; ++k) dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+        // the pre-filter's feature records (inner role, outer role)
+        const float drIn = up.rt - lo.rt;
+        const float slope = (up.z - lo.z) / (fabsf(drIn) > 1e-3f ? drIn : copysignf(1e-3f, drIn));
+        const float scode = ((fl & F_LO_E) ? 1.f : 0.f) + ((fl & F_LO_PS) ? 0.25f : 0.f);
+        const float tcode = ((fl & F_UP_E) ? 0.5f : 0.f) + ((fl & F_UP_2S) ? 0.125f : 0.f);
+        float4* fd = reinterpret_cast<float4*>(&AT(b.sgfeat, s * kFeatN, b.obj[kSG].cap * kFeatN));
+        fd[0] = make_float4(lo.x, lo.y, lo.z, lo.rt);
+        fd[1] = make_float4(lo.phi, v[PK_DPC], slope, scode);
+        fd[2] = make_float4(up.x, up.y, up.z, up.rt);
+        fd[3] = make_float4(up.phi, v[PK_ALPHAUP], tcode, 0.f);
     }
 }
 
@@ -848,7 +858,7 @@ __global__ void __launch_bounds__(kMlpTile) k_tl_prefilter(BatchDev b) {
             tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
             (void)IX(s, b.obj[kSG].cap);
             (void)IX(tt, b.obj[kSG].cap);
-            tl_features(feat_in(b.sgpack, s, tt), f);
+            tl_features(feat_s(b.sgfeat, s), feat_t(b.sgfeat, tt), f);
         } else {
 #pragma unroll
             for (int k = 0; k < kMlpIn; ++k) f[k] = 0.f;
@@ -958,7 +968,7 @@ __global__ void k_tl_collect(BatchDev b, MlpCollect col) {
                 const bool pass = tl_phaseB(algo, b.sgpack, s, tt, cut, muls, false);
                 label = pass ? 1.f : 0.f;
                 keep = pass || hash_unit((unsigned long long)c, col.seed) < col.neg_keep;
-                if (keep) tl_features(feat_in(S, T), f);
+                if (keep) tl_features(feat_s(b.sgfeat, s), feat_t(b.sgfeat, tt), f);
             }
         }
         const unsigned m = __ballot_sync(0xffffffffu, keep);

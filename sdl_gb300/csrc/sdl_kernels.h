@@ -37,6 +37,7 @@ struct BatchDev {
     int32_t* conn_pref;            // n_ev * n_conn
     int64_t* conn_sum;             // n_gm
     float* sgpack;                 // segment cap * PK_N packed records for the tracklet stage
+    float* sgfeat;                 // segment cap * kFeatN: the pre-filter's per-segment feature records
     uint32_t* counters;            // n_ev * 110
     uint32_t* status;
     unsigned long long* task;      // kNumStages work counters

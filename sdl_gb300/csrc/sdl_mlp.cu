@@ -9,22 +9,21 @@ namespace sdlg {
 
 namespace {
 
-// FP32 parameters -> packed BF16 tiles + FP32 vectors; `thr` is stored after b3
+// FP32 parameters -> packed BF16 tiles [W1 b1], [W2 b2] and the FP32 tail
+// (BF16-rounded w3, b3, threshold)
 __global__ void k_mlp_pack(const float* __restrict__ p, unsigned char* __restrict__ pack, float thr) {
     for (int e = threadIdx.x; e < kMlpHid * kMlpK1; e += blockDim.x) {
         const int n = e / kMlpK1, k = e % kMlpK1;
-        const float w = k < kMlpIn ? p[kMlpW1 + n * kMlpIn + k] : 0.f;
+        const float w = k < kMlpIn ? p[kMlpW1 + n * kMlpIn + k] : (k == kMlpIn ? p[kMlpB1 + n] : 0.f);
         *reinterpret_cast<uint16_t*>(pack + kPackW1 + cm_offset(n, k, 2)) = bf16_bits(w);
     }
-    for (int e = threadIdx.x; e < kMlpHid * kMlpHid; e += blockDim.x) {
-        const int n = e / kMlpHid, k = e % kMlpHid;
-        *reinterpret_cast<uint16_t*>(pack + kPackW2 + cm_offset(n, k, 8)) = bf16_bits(p[kMlpW2 + e]);
+    for (int e = threadIdx.x; e < kMlpHid * kMlpK2; e += blockDim.x) {
+        const int n = e / kMlpK2, k = e % kMlpK2;
+        const float w = k < kMlpHid ? p[kMlpW2 + n * kMlpHid + k] : (k == kMlpHid ? p[kMlpB2 + n] : 0.f);
+        *reinterpret_cast<uint16_t*>(pack + kPackW2 + cm_offset(n, k, 10)) = bf16_bits(w);
     }
-    for (int n = threadIdx.x; n < kMlpHid; n += blockDim.x) {
-        reinterpret_cast<float*>(pack + kPackB1)[n] = p[kMlpB1 + n];
-        reinterpret_cast<float*>(pack + kPackB2)[n] = p[kMlpB2 + n];
+    for (int n = threadIdx.x; n < kMlpHid; n += blockDim.x)
         reinterpret_cast<float*>(pack + kPackW3)[n] = bf16_round(p[kMlpW3 + n]);
-    }
     if (threadIdx.x == 0) {
         float* tail = reinterpret_cast<float*>(pack + kPackB3);
         tail[0] = p[kMlpB3];
@@ -59,7 +58,7 @@ constexpr int kTrainRows = 128;   // samples per block
 constexpr int kLd = kMlpHid + 1;  // padded row stride of the per-sample hidden arrays
 
 struct TrainSmem {
-    float w[kMlpParams];          // BF16-rounded weights (FP32 biases)
+    float w[kMlpParams];          // BF16-rounded weights and biases (b3 FP32)
     float x[kTrainRows][kMlpIn];  // BF16-rounded features
     float h1[kTrainRows][kLd];    // BF16-rounded ReLU outputs of layer 1
     float h2[kTrainRows][kLd];    // layer-2 ReLU outputs, then dLoss/da2
@@ -90,8 +89,7 @@ __global__ void __launch_bounds__(kTrainRows) k_mlp_fwd_bwd(const float* __restr
     const int t = threadIdx.x;
     for (int e = t; e < kMlpParams; e += blockDim.x) {
         const float v = params[e];
-        const bool bias = (e >= kMlpB1 && e < kMlpW2) || (e >= kMlpB2 && e < kMlpW3) || e == kMlpB3;
-        sm.w[e] = bias ? v : bf16_round(v);
+        sm.w[e] = e == kMlpB3 ? v : bf16_round(v);
     }
     const int64_t i = (int64_t)blockIdx.x * kTrainRows + t;
     const bool valid = i < count;

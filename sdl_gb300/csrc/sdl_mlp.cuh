@@ -5,11 +5,13 @@
 // and every other one is judged by the exact cuts as before, so the pruned
 // chain's tracklets are a subset of the plain chain's.
 //
-// Numerics (shared by inference and training): features, weights and the
-// first hidden layer are rounded to BF16; every sum accumulates in FP32;
-// the output layer runs in FP32 on BF16-rounded weights.  Inference uses the
-// tensor cores (tcgen05.mma kind::f16, one 128-candidate tile per MMA, FP32
-// accumulators in tensor memory); training uses CUDA-core kernels.
+// Numerics (shared by inference and training): features, W1, b1, W2, b2,
+// w3 and the first hidden layer are rounded to BF16; every sum accumulates in
+// FP32; b3 and the output layer's sum are FP32.  The biases b1 and b2 ride in
+// the MMAs: a constant 1 is the 13th input and the 65th first-layer output,
+// with the bias as its weight.  Inference uses the tensor cores
+// (tcgen05.mma kind::f16, one 128-candidate tile per MMA, FP32 accumulators
+// in tensor memory); training uses CUDA-core kernels.
 #pragma once
 #include <cstdint>
 #include <cstring>
@@ -17,8 +19,9 @@
 namespace sdlg {
 
 constexpr int kMlpIn = 12;      // features per candidate
-constexpr int kMlpK1 = 16;      // first-layer K, padded to the MMA's K
+constexpr int kMlpK1 = 16;      // first-layer K: 12 features, the constant 1, padding
 constexpr int kMlpHid = 64;     // units per hidden layer (the MMAs' N)
+constexpr int kMlpK2 = 80;      // second-layer K: 64 units, the constant 1, padding
 constexpr int kMlpTile = 128;   // candidates per tile (the MMAs' M)
 
 // FP32 parameter vector: W1[64][12], b1[64], W2[64][64], b2[64], w3[64], b3
@@ -30,16 +33,14 @@ constexpr int kMlpW3 = kMlpB2 + kMlpHid;
 constexpr int kMlpB3 = kMlpW3 + kMlpHid;
 constexpr int kMlpParams = kMlpB3 + 1;  // 5057
 
-// Packed inference weights, copied into shared memory by every CTA: W1 and
-// W2 in BF16 in the tensor cores' K-major core-matrix layout, then b1, b2,
-// the BF16-rounded w3 and b3 in FP32.
+// Packed inference weights, copied into shared memory by every CTA: [W1 b1]
+// (64 x 16) and [W2 b2] (64 x 80) in BF16 in the tensor cores' K-major
+// core-matrix layout, the BF16-rounded w3 and b3 in FP32, then the threshold.
 constexpr int kPackW1 = 0;                                  // 64 x 16 bf16
-constexpr int kPackW2 = kPackW1 + kMlpHid * kMlpK1 * 2;     // 64 x 64 bf16
-constexpr int kPackB1 = kPackW2 + kMlpHid * kMlpHid * 2;
-constexpr int kPackB2 = kPackB1 + kMlpHid * 4;
-constexpr int kPackW3 = kPackB2 + kMlpHid * 4;
+constexpr int kPackW2 = kPackW1 + kMlpHid * kMlpK1 * 2;     // 64 x 80 bf16
+constexpr int kPackW3 = kPackW2 + kMlpHid * kMlpK2 * 2;
 constexpr int kPackB3 = kPackW3 + kMlpHid * 4;
-constexpr int kPackBytes = kPackB3 + 16;                    // 11024, a multiple of 16
+constexpr int kPackBytes = kPackB3 + 16;                    // 12560, a multiple of 16
 
 // Byte offset of element (row, k) of a K-major BF16 tile without swizzling:
 // 8-row x 16-byte core matrices, `kgroups` of them along K per 8-row group
@@ -168,7 +169,7 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
 struct __align__(128) MlpSmem {
     alignas(128) unsigned char w[kPackBytes];
     alignas(128) unsigned char a1[kMlpTile * kMlpK1 * 2];    // features, BF16, 2 k-groups
-    alignas(128) unsigned char a2[kMlpTile * kMlpHid * 2];   // hidden layer 1, BF16, 8 k-groups
+    alignas(128) unsigned char a2[kMlpTile * kMlpK2 * 2];    // hidden layer 1 + the constant 1, BF16, 10 k-groups
     alignas(8) uint64_t mbar;
     uint32_t tmem;       // base address of 64 tensor-memory columns (both layers' accumulators)
 };
@@ -188,6 +189,9 @@ __device__ __forceinline__ void mlp_setup(MlpSmem& sm, const unsigned char* __re
     uint4* dst = reinterpret_cast<uint4*>(sm.w);
     for (int k = threadIdx.x; k < kPackBytes / 16; k += blockDim.x) dst[k] = __ldg(src + k);
     if (threadIdx.x == 0) mbar_init(&sm.mbar);
+    // the constant part of this thread's second-layer row: 1 at k = 64, zeros after
+    *reinterpret_cast<uint4*>(sm.a2 + cm_offset(threadIdx.x, 64, 10)) = make_uint4(0x3f80u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4*>(sm.a2 + cm_offset(threadIdx.x, 72, 10)) = make_uint4(0u, 0u, 0u, 0u);
     if (threadIdx.x < 32) tc_alloc(&sm.tmem, 64);
     fence_async_smem();
     tc_fence_before();
@@ -226,8 +230,8 @@ __device__ __forceinline__ void mlp_layer_sync(MlpSmem& sm, int layer, MlpThread
         } else {
             const uint32_t a2 = smem_addr(sm.a2);
 #pragma unroll
-            for (int kc = 0; kc < 4; ++kc)
-                tc_mma(sm.tmem, smem_desc(a2 + 256 * kc, 128, 1024), smem_desc(w + kPackW2 + 256 * kc, 128, 1024),
+            for (int kc = 0; kc < kMlpK2 / 16; ++kc)
+                tc_mma(sm.tmem, smem_desc(a2 + 256 * kc, 128, 1280), smem_desc(w + kPackW2 + 256 * kc, 128, 1280),
                        kIdescBf16M128N64, kc > 0 ? 1u : 0u);
         }
         tc_commit(&sm.mbar);
@@ -249,38 +253,39 @@ __device__ __forceinline__ float mlp_tile(MlpSmem& sm, const float* x, MlpThread
     {
         uint32_t q[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const float lo = 2 * j < kMlpIn ? x[2 * j] : 0.f;
-            const float hi = 2 * j + 1 < kMlpIn ? x[2 * j + 1] : 0.f;
-            q[j] = pack_bf16x2(lo, hi);
-        }
+        for (int j = 0; j < 6; ++j) q[j] = pack_bf16x2(x[2 * j], x[2 * j + 1]);
+        q[6] = 0x3f80u;  // the constant 1 (BF16) that carries b1, then zeros
+        q[7] = 0u;
         *reinterpret_cast<uint4*>(sm.a1 + cm_offset(t, 0, 2)) = make_uint4(q[0], q[1], q[2], q[3]);
         *reinterpret_cast<uint4*>(sm.a1 + cm_offset(t, 8, 2)) = make_uint4(q[4], q[5], q[6], q[7]);
     }
     mlp_layer_sync(sm, 0, st);
     const uint32_t lane_base = sm.tmem + ((uint32_t)(t & ~31) << 16);
-    const float* b1 = reinterpret_cast<const float*>(sm.w + kPackB1);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         float v[16];
         tc_ld16(lane_base + 16 * c, v);
         uint32_t q[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
-            q[j] = pack_bf16x2_relu(__fadd_rn(v[2 * j], b1[16 * c + 2 * j]), __fadd_rn(v[2 * j + 1], b1[16 * c + 2 * j + 1]));
-        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c, 8)) = make_uint4(q[0], q[1], q[2], q[3]);
-        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c + 8, 8)) = make_uint4(q[4], q[5], q[6], q[7]);
+        for (int j = 0; j < 8; ++j) q[j] = pack_bf16x2_relu(v[2 * j], v[2 * j + 1]);
+        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c, 10)) = make_uint4(q[0], q[1], q[2], q[3]);
+        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c + 8, 10)) = make_uint4(q[4], q[5], q[6], q[7]);
     }
     mlp_layer_sync(sm, 1, st);
-    const float* b2 = reinterpret_cast<const float*>(sm.w + kPackB2);
-    const float* w3 = reinterpret_cast<const float*>(sm.w + kPackW3);
+    const float4* w3 = reinterpret_cast<const float4*>(sm.w + kPackW3);
     float z = *reinterpret_cast<const float*>(sm.w + kPackB3);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         float v[16];
         tc_ld16(lane_base + 16 * c, v);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) z = __fmaf_rn(w3[16 * c + j], fmaxf(__fadd_rn(v[j], b2[16 * c + j]), 0.f), z);
+        for (int j = 0; j < 4; ++j) {
+            const float4 w = w3[4 * c + j];
+            z = __fmaf_rn(w.x, fmaxf(v[4 * j], 0.f), z);
+            z = __fmaf_rn(w.y, fmaxf(v[4 * j + 1], 0.f), z);
+            z = __fmaf_rn(w.z, fmaxf(v[4 * j + 2], 0.f), z);
+            z = __fmaf_rn(w.w, fmaxf(v[4 * j + 3], 0.f), z);
+        }
     }
     return z;
 }
