@@ -814,6 +814,18 @@ constexpr int kMlpWarps = kMlpTile / 32;
 // candidate whose logit reaches the threshold are appended to the kept list,
 // which k_tl_exact judges with the reference's cuts.  Control flow around the
 // tile is uniform over the CTA.
+// write a tile's kept pairs (lanes in m) at the positions its atomic, issued
+// by lane `leader` (raw value there), reserved; every lane calls it
+__device__ __forceinline__ void kept_append(const BatchDev& b, unsigned m, unsigned long long raw, int leader, int2 pair) {
+    if (m == 0u) return;
+    const unsigned long long p0 = __shfl_sync(0xffffffffu, raw, leader);
+    const int lane = threadIdx.x & 31;
+    if (!((m >> lane) & 1u)) return;
+    const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));
+    if (pos < b.kept_cap) AT(b.kept, pos, b.kept_cap) = pair;
+    else atomicOr(b.status, kStatusOverflowKept);
+}
+
 __global__ void __launch_bounds__(kMlpTile) k_tl_prefilter(BatchDev b) {
     __shared__ MlpSmem sm;
     __shared__ long long s_task;
@@ -832,11 +844,20 @@ __global__ void __launch_bounds__(kMlpTile) k_tl_prefilter(BatchDev b) {
     const float thr = reinterpret_cast<const float*>(sm.w + kPackB3)[1];
     MlpThread st;
     unsigned n_scored = 0, n_kept = 0;
+    // the kept candidates of a tile are appended at the next tile, after its
+    // decode, so that the append's atomic has returned by then
+    unsigned pend_m = 0;
+    unsigned long long pend_p0 = 0;
+    int pend_leader = 0;
+    int2 pend = make_int2(0, 0);
+    // the next task is fetched while the current one runs
+    if (threadIdx.x == 0) s_task = (long long)atomicAdd(b.task + kTL, 1ull);
+    __syncthreads();
     for (;;) {
-        if (threadIdx.x == 0) s_task = (long long)atomicAdd(b.task + kTL, 1ull);
-        __syncthreads();
         const int64_t t = s_task;
         if (t >= ntask) break;
+        unsigned long long nxt = 0;
+        if (threadIdx.x == 0) nxt = atomicAdd(b.task + kTL, 1ull);
         const int64_t base = t * kMlpTile;
         const int64_t end = min(base + kMlpTile, total);
         const int64_t wbase = base + kWarp * w;
@@ -863,23 +884,21 @@ __global__ void __launch_bounds__(kMlpTile) k_tl_prefilter(BatchDev b) {
 #pragma unroll
             for (int k = 0; k < kMlpIn; ++k) f[k] = 0.f;
         }
+        kept_append(b, pend_m, pend_p0, pend_leader, pend);
         const float z = mlp_tile(sm, f, st);
         const bool keep = valid && z >= thr;
         n_scored += valid;
         n_kept += keep;
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        if (m) {
-            const int leader = __ffs(m) - 1;
-            unsigned long long p0 = 0;
-            if (lane == leader) p0 = atomicAdd(b.n_kept, (unsigned long long)__popc(m));
-            p0 = __shfl_sync(0xffffffffu, p0, leader);
-            const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));
-            if (keep) {
-                if (pos < b.kept_cap) AT(b.kept, pos, b.kept_cap) = make_int2(s, tt);
-                else atomicOr(b.status, kStatusOverflowKept);
-            }
+        pend_m = __ballot_sync(0xffffffffu, keep);
+        if (pend_m) {
+            pend_leader = __ffs(pend_m) - 1;
+            if (lane == pend_leader) pend_p0 = atomicAdd(b.n_kept, (unsigned long long)__popc(pend_m));
         }
+        pend = make_int2(s, tt);
+        if (threadIdx.x == 0) s_task = (long long)nxt;
+        __syncthreads();
     }
+    kept_append(b, pend_m, pend_p0, pend_leader, pend);
     n_scored = __reduce_add_sync(0xffffffffu, n_scored);
     n_kept = __reduce_add_sync(0xffffffffu, n_kept);
     if (lane == 0) {

@@ -168,8 +168,12 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
 // t owns tile row t).
 struct __align__(128) MlpSmem {
     alignas(128) unsigned char w[kPackBytes];
-    alignas(128) unsigned char a1[kMlpTile * kMlpK1 * 2];    // features, BF16, 2 k-groups
-    alignas(128) unsigned char a2[kMlpTile * kMlpK2 * 2];    // hidden layer 1 + the constant 1, BF16, 10 k-groups
+    // A operand of both layers, BF16, 10 k-groups per 8-row group: columns
+    // 0-15 hold a candidate's features and the constant 1 for the first MMA,
+    // then columns 0-63 its first hidden layer and column 64 the constant 1
+    // for the second (the features are consumed before the layer overwrites
+    // them, and the layer before the next tile's features)
+    alignas(128) unsigned char a2[kMlpTile * kMlpK2 * 2];
     alignas(8) uint64_t mbar;
     uint32_t tmem;       // base address of 64 tensor-memory columns (both layers' accumulators)
 };
@@ -226,7 +230,7 @@ __device__ __forceinline__ void mlp_layer_sync(MlpSmem& sm, int layer, MlpThread
         tc_fence_after();
         const uint32_t w = smem_addr(sm.w);
         if (layer == 0) {
-            tc_mma(sm.tmem, smem_desc(smem_addr(sm.a1), 128, 256), smem_desc(w + kPackW1, 128, 256), kIdescBf16M128N64, 0);
+            tc_mma(sm.tmem, smem_desc(smem_addr(sm.a2), 128, 1280), smem_desc(w + kPackW1, 128, 256), kIdescBf16M128N64, 0);
         } else {
             const uint32_t a2 = smem_addr(sm.a2);
 #pragma unroll
@@ -256,8 +260,8 @@ __device__ __forceinline__ float mlp_tile(MlpSmem& sm, const float* x, MlpThread
         for (int j = 0; j < 6; ++j) q[j] = pack_bf16x2(x[2 * j], x[2 * j + 1]);
         q[6] = 0x3f80u;  // the constant 1 (BF16) that carries b1, then zeros
         q[7] = 0u;
-        *reinterpret_cast<uint4*>(sm.a1 + cm_offset(t, 0, 2)) = make_uint4(q[0], q[1], q[2], q[3]);
-        *reinterpret_cast<uint4*>(sm.a1 + cm_offset(t, 8, 2)) = make_uint4(q[4], q[5], q[6], q[7]);
+        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 0, 10)) = make_uint4(q[0], q[1], q[2], q[3]);
+        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 8, 10)) = make_uint4(q[4], q[5], q[6], q[7]);
     }
     mlp_layer_sync(sm, 0, st);
     const uint32_t lane_base = sm.tmem + ((uint32_t)(t & ~31) << 16);
