@@ -130,6 +130,14 @@ int sdlg_last_times(sdlg_ctx* ctx, float* out7);
 /* Device time of each stage's candidate-evaluation kernel in the last run (ms). */
 int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5);
 
+/* Autotuner (no counterpart in the reference): runs the chain on the current
+ * batch with each of a grid of launch shapes for the stages' candidate
+ * evaluation kernels (candidates per warp task 128-1024, 4-16 CTAs per SM),
+ * keeps the fastest shape per stage for later runs of this context, and
+ * returns it in out10 (tasks[5], CTAs per SM[5]; may be NULL).  Results do
+ * not depend on the shapes.  Takes about 24 runs of the chain. */
+int sdlg_autotune(sdlg_ctx* ctx, int stop_after, int flags, int32_t* out10);
+
 /* For a run with SDLG_FLAG_MLP: device time (ms) of the pre-filter kernel and
  * of the exact tracklet cuts on the candidates it kept (no counterpart in the
  * reference); zeros otherwise. */

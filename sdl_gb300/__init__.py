@@ -70,6 +70,7 @@ def lib():
         L.sdlg_last_kernel_times.argtypes = [vp, vp]
         L.sdlg_last_prefilter_times.argtypes = [vp, vp]
         L.sdlg_math_check.argtypes = [vp, i32, i32, ctypes.c_uint64, i64, ctypes.c_uint64, vp]
+        L.sdlg_autotune.argtypes = [vp, i32, i32, vp]
         L.sdlg_last_launches.argtypes = [vp]
         L.sdlg_last_launches.restype = i64
         L.sdlg_mini_doublets_static.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
@@ -318,6 +319,12 @@ class Chain:
         out = np.zeros(2, dtype=np.float32)
         self._ck(lib().sdlg_last_prefilter_times(self.h, out.ctypes.data))
         return out
+
+    def autotune(self, stop_after: int = 4, flags: int = 0) -> dict:
+        """Pick the fastest launch shape per stage on the current batch (kept for later runs)."""
+        out = np.zeros(10, dtype=np.int32)
+        self._ck(lib().sdlg_autotune(self.h, int(stop_after), int(flags), out.ctypes.data))
+        return {"task": [int(v) for v in out[:5]], "ctas_per_sm": [int(v) for v in out[5:]]}
 
     def math_check(self, fn: int, n: int, *, start: int = 0, exhaustive: bool = False, seed: int = 0) -> dict:
         """Self-check of a float-float fast path against the double evaluation."""

@@ -133,6 +133,8 @@ struct sdlg_ctx {
     int64_t cap_hit = 0, cap_ev = 0;
     int64_t cap_obj[kNumStages] = {0, 0, 0, 0, 0};
     int64_t cap_kept = 0;  // tracklet candidates the pre-filter may keep per run
+    int tune_task[kNumStages] = {0, 0, 0, 0, 0};  // tuned launch shapes (0: default)
+    int tune_grid[kNumStages] = {0, 0, 0, 0, 0};
     bool buffers_ok = false;
     // pinned staging
     void* pinned = nullptr;
@@ -316,6 +318,10 @@ int ensure_buffers(sdlg_ctx* ctx) {
     b.n_sm = ctx->n_sm;
     b.mlp_pack = ctx->mlp.pack;
     b.mlp_stats = ctx->mlp.stats;
+    for (int st = 0; st < kNumStages; ++st) {
+        b.enum_task[st] = ctx->tune_task[st];
+        b.enum_grid[st] = ctx->tune_grid[st];
+    }
     int rc;
 #define AL(ptr, n) if ((rc = dalloc(ctx, &(ptr), (n))) != SDLG_OK) return rc
     int64_t* small;
@@ -906,6 +912,55 @@ int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5) {
         CK(cudaEventSynchronize(ctx->hooks.enum_stop[k]));
         CK(cudaEventElapsedTime(&out5[k], ctx->hooks.enum_start[k], ctx->hooks.enum_stop[k]));
     }
+    return SDLG_OK;
+}
+
+int sdlg_autotune(sdlg_ctx* ctx, int stop_after, int flags, int32_t* out10) {
+    if (!ctx) return SDLG_ERR_ARG;
+    if (!ctx->have_geo) return fail(ctx, SDLG_ERR_NO_GEOMETRY, "no geometry loaded");
+    if (!ctx->buffers_ok || ctx->n_ev <= 0) return fail(ctx, SDLG_ERR_NO_EVENTS, "no events set");
+    if (stop_after < 0 || stop_after > 4) return fail(ctx, SDLG_ERR_ARG, "stop_after out of range");
+    static const int kTasks[] = {128, 256, 512, 1024};
+    static const int kGrids[] = {4, 8, 16};
+    float best[kNumStages];
+    int bt[kNumStages], bg[kNumStages];
+    for (int st = 0; st < kNumStages; ++st) {
+        best[st] = 3.4e38f;
+        bt[st] = ctx->tune_task[st];
+        bg[st] = ctx->tune_grid[st];
+    }
+    for (int task : kTasks) {
+        for (int grid : kGrids) {
+            for (int st = 0; st < kNumStages; ++st) {  // (a capacity regrow re-reads the context's values)
+                ctx->tune_task[st] = ctx->b.enum_task[st] = task;
+                ctx->tune_grid[st] = ctx->b.enum_grid[st] = grid;
+            }
+            float t[kNumStages];
+            for (int rep = 0; rep < 2; ++rep) {  // the second run is timed
+                int rc = sdlg_run(ctx, stop_after, flags | SDLG_FLAG_NO_GRAPH);
+                if (rc) return rc;
+                rc = sdlg_last_kernel_times(ctx, t);
+                if (rc) return rc;
+            }
+            for (int st = 0; st <= stop_after; ++st)
+                if (t[st] < best[st]) {
+                    best[st] = t[st];
+                    bt[st] = task;
+                    bg[st] = grid;
+                }
+        }
+    }
+    for (int st = 0; st < kNumStages; ++st) {
+        ctx->tune_task[st] = bt[st];
+        ctx->tune_grid[st] = bg[st];
+        ctx->b.enum_task[st] = bt[st];
+        ctx->b.enum_grid[st] = bg[st];
+        if (out10) {
+            out10[st] = bt[st];
+            out10[kNumStages + st] = bg[st];
+        }
+    }
+    ctx->graph_stop = -1;  // the launch graph holds the old shapes
     return SDLG_OK;
 }
 

@@ -43,7 +43,7 @@ __device__ __forceinline__ int64_t checked_idx(int64_t i, int64_t lim, int line,
 
 constexpr int kWarp = 32;
 constexpr int kEnumThreads = 256;
-constexpr int kTask = 256;  // candidates per warp task
+constexpr int kTaskDefault = 256;  // candidates per warp task unless tuned
 constexpr int kScanThreads = 512;
 constexpr int kScanItems = 8;
 constexpr int kScanBlock = kScanThreads * kScanItems;
@@ -564,7 +564,8 @@ __global__ void __launch_bounds__(kEnumThreads) k_enum(BatchDev b) {
     const int64_t* off = b.cand[st];
     const int64_t offlim = b.cand_cap[st] + 1;
     const int64_t total = AT(off, nobj, offlim);
-    const int64_t ntask = (total + kTask - 1) / kTask;
+    const int task = b.enum_task[st] > 0 ? b.enum_task[st] : kTaskDefault;
+    const int64_t ntask = (total + task - 1) / task;
     const int lane = threadIdx.x & 31;
     const Recs& R = b.rec[st];
     const Objs& O = b.obj[st];
@@ -573,8 +574,8 @@ __global__ void __launch_bounds__(kEnumThreads) k_enum(BatchDev b) {
         if (lane == 0) t = atomicAdd(b.task + st, 1ull);
         t = __shfl_sync(0xffffffffu, t, 0);
         if ((int64_t)t >= ntask) break;
-        const int64_t base = (int64_t)t * kTask;
-        const int64_t end = min(base + kTask, total);
+        const int64_t base = (int64_t)t * task;
+        const int64_t end = min(base + task, total);
         int ilo = 0;
         if (lane < 2) {
             int lo, hi;
@@ -583,8 +584,8 @@ __global__ void __launch_bounds__(kEnumThreads) k_enum(BatchDev b) {
         }
         const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
         const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
-        for (int r = 0; r < kTask / kWarp; ++r) {
-            const int64_t c = base + r * kWarp + lane;
+        for (int64_t cb = base; cb < end; cb += kWarp) {
+            const int64_t c = cb + lane;
             const bool valid = c < end;
             int oi = 0, oj = 0, g = 0;
             float fv[6];
@@ -761,7 +762,8 @@ __global__ void __launch_bounds__(kEnumThreads, 3) k_tl_enum(BatchDev b) {
     const int64_t* off = b.cand[kTL];
     const int64_t offlim = b.cand_cap[kTL] + 1;
     const int64_t total = AT(off, nobj, offlim);
-    const int64_t ntask = (total + kTask - 1) / kTask;
+    const int task = b.enum_task[kTL] > 0 ? b.enum_task[kTL] : kTaskDefault;
+    const int64_t ntask = (total + task - 1) / task;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const bool nm1 = (b.flags & kFlagTLNm1) != 0;
     const bool lay = (b.flags & kFlagTLLayers) != 0;
@@ -777,8 +779,8 @@ __global__ void __launch_bounds__(kEnumThreads, 3) k_tl_enum(BatchDev b) {
         if (lane == 0) t = atomicAdd(b.task + kTL, 1ull);
         t = __shfl_sync(0xffffffffu, t, 0);
         if ((int64_t)t >= ntask) break;
-        const int64_t base = (int64_t)t * kTask;
-        const int64_t end = min(base + kTask, total);
+        const int64_t base = (int64_t)t * task;
+        const int64_t end = min(base + task, total);
         int ilo = 0;
         if (lane < 2) {
             int lo, hi;
@@ -787,8 +789,8 @@ __global__ void __launch_bounds__(kEnumThreads, 3) k_tl_enum(BatchDev b) {
         }
         const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
         const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
-        for (int r = 0; r < kTask / kWarp; ++r) {
-            const int64_t c = base + r * kWarp + lane;
+        for (int64_t cb = base; cb < end; cb += kWarp) {
+            const int64_t c = cb + lane;
             int algo = kAlgoNone, s = 0, tt = 0;
             float cut = 0.f, muls = 0.f;
             if (c < end) {
@@ -1257,6 +1259,8 @@ void scan_h(const BatchDev& b, int64_t* data, const int64_t* n_ptr, int64_t cap,
     if (h) h->launches += 3;
 }
 
+int enum_grid(const BatchDev& b, int st) { return b.enum_grid[st] > 0 ? b.enum_grid[st] : 8; }
+
 template <class F>
 void enum_and_group(const BatchDev& b, cudaStream_t s, Hooks* h, bool layer_counters = true) {
     constexpr int st = F::kSt;
@@ -1272,7 +1276,7 @@ void enum_and_group(const BatchDev& b, cudaStream_t s, Hooks* h, bool layer_coun
     k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, st);
     if (h) h->launches += 1;
     if (h && h->timed) rec_event(h->enum_start[st], s);
-    k_enum<F><<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
+    k_enum<F><<<b.n_sm * enum_grid(b, st), kEnumThreads, 0, s>>>(b);
     if (h && h->timed) rec_event(h->enum_stop[st], s);
     if (layer_counters) k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, st);
     scan_h(b, b.obj[st].mod_cnt, b.n_gm_dev, b.n_gm, s, h);
@@ -1326,10 +1330,10 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
         cudaMemsetAsync(b.n_kept, 0, sizeof(unsigned long long), s);
         k_tl_prefilter<<<b.n_sm * 8, kMlpTile, 0, s>>>(b);
         if (h && h->timed) rec_event(h->tl_mid, s);
-        k_tl_exact<<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
+        k_tl_exact<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
         if (h) h->launches += 1;
     } else {
-        k_tl_enum<<<b.n_sm * 8, kEnumThreads, 0, s>>>(b);
+        k_tl_enum<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
     }
     if (h && h->timed) rec_event(h->enum_stop[kTL], s);
     k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kTL);

@@ -46,6 +46,10 @@ struct BatchDev {
     int32_t* bucket;               // first inner object of every 256 consecutive candidates of the running stage
     int64_t bucket_cap;
     int flags;                     // kFlag* bits
+    // launch shape of each stage's candidate-evaluation kernel (autotuned):
+    // candidates per warp task (a multiple of 32) and CTAs per SM
+    int enum_task[kNumStages];
+    int enum_grid[kNumStages];
     const unsigned char* mlp_pack; // packed pre-filter weights and threshold (kPackBytes)
     MlpStats* mlp_stats;           // pre-filter counts of the last run
     int2* kept;                    // (inner, outer) segments of the tracklet candidates the pre-filter kept
