@@ -12,6 +12,9 @@
 // about 2^-15 of the inputs) the caller evaluates the expression in double as
 // before.  The results are therefore identical to the double evaluation's.
 //
+// sincos_ff is out of line: one copy shared by the sine and the cosine keeps
+// the mini-doublet kernel's code within the instruction caches.
+//
 // Published methods used: Dekker's and Knuth's error-free transformations
 // (TwoSum, FastTwoSum, TwoProd via fused multiply-add), Dekker's double-length
 // division and square root, argument reduction of atan by a 33-entry table of
@@ -201,7 +204,7 @@ __device__ __forceinline__ ff cos_small_ff(float x) {
 // them is exact; the split is 2e-21 off), then the series on |r| <= pi/4.
 // Relative error below 2^-42; false when |r| < 2^-16 after a reduction
 // (a result near a zero of the function).
-__device__ __forceinline__ bool sincos_ff(float x, int shift, ff& out) {
+static __device__ __noinline__ bool sincos_ff(float x, int shift, ff& out) {
     if (!(fabsf(x) <= 8.f)) return false;
     const int k = __float2int_rn(__fmul_rn(x, 0x1.45f306p-1f));
     ff s, c;
