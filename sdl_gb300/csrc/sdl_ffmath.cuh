@@ -131,7 +131,7 @@ __device__ constexpr ff kThirdFF = {0x1.555556p-2f, -0x1.555556p-27f};
 __device__ __forceinline__ ff atan_small(ff u) {
     const ff u2 = add(two_prod(u.hi, u.hi), __fmul_rn(__fmul_rn(2.f, u.hi), u.lo));
     const float z = u2.hi;
-    const float tail = __fmul_rn(__fmul_rn(z, z), __fsub_rn(0.2f, __fmul_rn(z, __fsub_rn(0x1.249249p-3f, __fmul_rn(z, 0x1.c71c72p-4f)))));
+    const float tail = __fmul_rn(__fmul_rn(z, z), __fsub_rn(0.2f, __fmul_rn(z, __fsub_rn(0x1.24924ap-3f, __fmul_rn(z, 0x1.c71c72p-4f)))));
     const ff p = add(neg(mul(u2, kThirdFF)), tail);
     return add(u, mul(u, p));
 }

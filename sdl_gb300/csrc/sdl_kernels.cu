@@ -846,22 +846,18 @@ __global__ void __launch_bounds__(kMlpTile) k_tl_prefilter(BatchDev b) {
     const float thr = reinterpret_cast<const float*>(sm.w + kPackB3)[1];
     MlpThread st;
     unsigned n_scored = 0, n_kept = 0;
-    // the kept candidates of a tile are appended at the next tile, after its
-    // decode, so that the append's atomic has returned by then
+    // Software pipeline over tiles: while the tensor cores run a tile's first
+    // layer, the CTA decodes the next tile's candidates and loads their
+    // features; a tile's kept candidates are written one tile later, when
+    // the atomic that reserved their positions has returned.
     unsigned pend_m = 0;
     unsigned long long pend_p0 = 0;
     int pend_leader = 0;
     int2 pend = make_int2(0, 0);
-    // the next task is fetched while the current one runs
-    if (threadIdx.x == 0) s_task = (long long)atomicAdd(b.task + kTL, 1ull);
-    __syncthreads();
-    for (;;) {
-        const int64_t t = s_task;
-        if (t >= ntask) break;
-        unsigned long long nxt = 0;
-        if (threadIdx.x == 0) nxt = atomicAdd(b.task + kTL, 1ull);
+    // decode candidate c = t * 128 + threadIdx.x of task t and compute its features
+    auto load_tile = [&](int64_t t, bool& valid, int& s, int& tt, float* f) {
         const int64_t base = t * kMlpTile;
-        const int64_t end = min(base + kMlpTile, total);
+        const int64_t end = t < ntask ? min(base + kMlpTile, total) : base;
         const int64_t wbase = base + kWarp * w;
         int ilo = 0;
         if (lane < 2 && wbase < end) {
@@ -873,9 +869,9 @@ __global__ void __launch_bounds__(kMlpTile) k_tl_prefilter(BatchDev b) {
         const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
         const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
         const int64_t c = wbase + lane;
-        const bool valid = c < end;
-        int s = 0, tt = 0;
-        float f[kMlpIn];
+        valid = c < end;
+        s = 0;
+        tt = 0;
         if (valid) {
             s = (i0 == i1) ? i0 : find_obj(b, off, offlim, i0, i1, c);
             tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
@@ -886,8 +882,29 @@ __global__ void __launch_bounds__(kMlpTile) k_tl_prefilter(BatchDev b) {
 #pragma unroll
             for (int k = 0; k < kMlpIn; ++k) f[k] = 0.f;
         }
+    };
+    if (threadIdx.x == 0) s_task = (long long)atomicAdd(b.task + kTL, 1ull);
+    __syncthreads();
+    int64_t t = s_task;
+    bool valid;
+    int s, tt;
+    float f[kMlpIn];
+    if (t < ntask) load_tile(t, valid, s, tt, f);
+    // s_task is rewritten only after every thread passed the barrier in
+    // mlp_tile_begin, i.e. after every thread has read it
+    __syncthreads();
+    if (threadIdx.x == 0) s_task = (long long)atomicAdd(b.task + kTL, 1ull);
+    while (t < ntask) {
+        mlp_tile_begin(sm, f, st);  // its barrier publishes s_task (the next task)
+        const int64_t tn = s_task;
+        unsigned long long nxt = 0;
+        if (threadIdx.x == 0) nxt = atomicAdd(b.task + kTL, 1ull);
+        bool valid_n;
+        int s_n, tt_n;
+        float f_n[kMlpIn];
+        load_tile(tn, valid_n, s_n, tt_n, f_n);
         kept_append(b, pend_m, pend_p0, pend_leader, pend);
-        const float z = mlp_tile(sm, f, st);
+        const float z = mlp_tile_end(sm, st);
         const bool keep = valid && z >= thr;
         n_scored += valid;
         n_kept += keep;
@@ -898,7 +915,12 @@ __global__ void __launch_bounds__(kMlpTile) k_tl_prefilter(BatchDev b) {
         }
         pend = make_int2(s, tt);
         if (threadIdx.x == 0) s_task = (long long)nxt;
-        __syncthreads();
+        t = tn;
+        valid = valid_n;
+        s = s_n;
+        tt = tt_n;
+#pragma unroll
+        for (int k = 0; k < kMlpIn; ++k) f[k] = f_n[k];
     }
     kept_append(b, pend_m, pend_p0, pend_leader, pend);
     n_scored = __reduce_add_sync(0xffffffffu, n_scored);

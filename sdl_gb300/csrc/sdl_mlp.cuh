@@ -249,21 +249,46 @@ __device__ __forceinline__ void mlp_layer_sync(MlpSmem& sm, int layer, MlpThread
     tc_fence_after();
 }
 
-// One tile: thread t scores the features x of its candidate (rounded to
-// BF16 here) and gets the logit.  Every thread of the 128-thread CTA calls
-// it.  After an abort the logit is meaningless.
-__device__ __forceinline__ float mlp_tile(MlpSmem& sm, const float* x, MlpThread& st) {
+// First half of a tile: thread t writes the features x of its candidate
+// (rounded to BF16, with the constant 1) as row t and thread 0 starts the
+// first layer's MMA.  Every thread of the 128-thread CTA calls it; the CTA
+// may run other work before mlp_tile_end.
+__device__ __forceinline__ void mlp_tile_begin(MlpSmem& sm, const float* x, MlpThread& st) {
     const int t = threadIdx.x;
-    {
-        uint32_t q[8];
+    uint32_t q[8];
 #pragma unroll
-        for (int j = 0; j < 6; ++j) q[j] = pack_bf16x2(x[2 * j], x[2 * j + 1]);
-        q[6] = 0x3f80u;  // the constant 1 (BF16) that carries b1, then zeros
-        q[7] = 0u;
-        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 0, 10)) = make_uint4(q[0], q[1], q[2], q[3]);
-        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 8, 10)) = make_uint4(q[4], q[5], q[6], q[7]);
+    for (int j = 0; j < 6; ++j) q[j] = pack_bf16x2(x[2 * j], x[2 * j + 1]);
+    q[6] = 0x3f80u;  // the constant 1 (BF16) that carries b1, then zeros
+    q[7] = 0u;
+    *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 0, 10)) = make_uint4(q[0], q[1], q[2], q[3]);
+    *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 8, 10)) = make_uint4(q[4], q[5], q[6], q[7]);
+    fence_async_smem();
+    tc_fence_before();
+    if (__syncthreads_or(st.abort ? 1 : 0)) {
+        st.abort = true;
+        return;
     }
-    mlp_layer_sync(sm, 0, st);
+    if (t == 0) {
+        tc_fence_after();
+        tc_mma(sm.tmem, smem_desc(smem_addr(sm.a2), 128, 1280), smem_desc(smem_addr(sm.w) + kPackW1, 128, 256),
+               kIdescBf16M128N64, 0);
+        tc_commit(&sm.mbar);
+    }
+}
+
+// Second half: wait for the first layer, run the second and the output
+// layer, return the logit (meaningless after an abort).  Every thread calls it.
+__device__ __forceinline__ float mlp_tile_end(MlpSmem& sm, MlpThread& st) {
+    const int t = threadIdx.x;
+    if (!st.abort) {
+        if (mbar_wait(&sm.mbar, st.phase)) {
+            st.phase ^= 1u;
+        } else {
+            st.abort = true;
+            st.pending = true;
+        }
+        tc_fence_after();
+    }
     const uint32_t lane_base = sm.tmem + ((uint32_t)(t & ~31) << 16);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -292,6 +317,12 @@ __device__ __forceinline__ float mlp_tile(MlpSmem& sm, const float* x, MlpThread
         }
     }
     return z;
+}
+
+// One tile: thread t scores the features x of its candidate and gets the logit.
+__device__ __forceinline__ float mlp_tile(MlpSmem& sm, const float* x, MlpThread& st) {
+    mlp_tile_begin(sm, x, st);
+    return mlp_tile_end(sm, st);
 }
 
 #endif  // __CUDACC__
