@@ -828,7 +828,7 @@ __device__ __forceinline__ void kept_append(const BatchDev& b, unsigned m, unsig
     else atomicOr(b.status, kStatusOverflowKept);
 }
 
-__global__ void __launch_bounds__(kMlpTile) k_tl_prefilter(BatchDev b) {
+__global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
     __shared__ MlpSmem sm;
     __shared__ long long s_task;
     __shared__ int s_go;

@@ -7,9 +7,9 @@
 //
 // Numerics (shared by inference and training): features, W1, b1, W2, b2,
 // w3 and the first hidden layer are rounded to BF16; every sum accumulates in
-// FP32; b3 and the output layer's sum are FP32.  The biases b1 and b2 ride in
-// the MMAs: a constant 1 is the 13th input and the 65th first-layer output,
-// with the bias as its weight.  Inference uses the tensor cores
+// FP32; b3 and the output layer's sum are FP32.  The bias b1 rides in the
+// first MMA as the weight of a constant 13th input; b2 is added to the
+// second MMA's FP32 result.  Inference uses the tensor cores
 // (tcgen05.mma kind::f16, one 128-candidate tile per MMA, FP32 accumulators
 // in tensor memory); training uses CUDA-core kernels.
 #pragma once
@@ -21,7 +21,7 @@ namespace sdlg {
 constexpr int kMlpIn = 12;      // features per candidate
 constexpr int kMlpK1 = 16;      // first-layer K: 12 features, the constant 1, padding
 constexpr int kMlpHid = 64;     // units per hidden layer (the MMAs' N)
-constexpr int kMlpK2 = 80;      // second-layer K: 64 units, the constant 1, padding
+constexpr int kMlpK2 = 64;      // second-layer K: the 64 units
 constexpr int kMlpTile = 128;   // candidates per tile (the MMAs' M)
 
 // FP32 parameter vector: W1[64][12], b1[64], W2[64][64], b2[64], w3[64], b3
@@ -34,13 +34,15 @@ constexpr int kMlpB3 = kMlpW3 + kMlpHid;
 constexpr int kMlpParams = kMlpB3 + 1;  // 5057
 
 // Packed inference weights, copied into shared memory by every CTA: [W1 b1]
-// (64 x 16) and [W2 b2] (64 x 80) in BF16 in the tensor cores' K-major
-// core-matrix layout, the BF16-rounded w3 and b3 in FP32, then the threshold.
+// (64 x 16) and W2 (64 x 64) in BF16 in the tensor cores' K-major
+// core-matrix layout, the BF16-rounded b2 and w3 and b3 in FP32, then the
+// threshold.
 constexpr int kPackW1 = 0;                                  // 64 x 16 bf16
-constexpr int kPackW2 = kPackW1 + kMlpHid * kMlpK1 * 2;     // 64 x 80 bf16
-constexpr int kPackW3 = kPackW2 + kMlpHid * kMlpK2 * 2;
+constexpr int kPackW2 = kPackW1 + kMlpHid * kMlpK1 * 2;     // 64 x 64 bf16
+constexpr int kPackB2 = kPackW2 + kMlpHid * kMlpK2 * 2;
+constexpr int kPackW3 = kPackB2 + kMlpHid * 4;
 constexpr int kPackB3 = kPackW3 + kMlpHid * 4;
-constexpr int kPackBytes = kPackB3 + 16;                    // 12560, a multiple of 16
+constexpr int kPackBytes = kPackB3 + 16;                    // 10768, a multiple of 16
 
 // Byte offset of element (row, k) of a K-major BF16 tile without swizzling:
 // 8-row x 16-byte core matrices, `kgroups` of them along K per 8-row group
@@ -168,11 +170,11 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
 // t owns tile row t).
 struct __align__(128) MlpSmem {
     alignas(128) unsigned char w[kPackBytes];
-    // A operand of both layers, BF16, 10 k-groups per 8-row group: columns
+    // A operand of both layers, BF16, 8 k-groups per 8-row group: columns
     // 0-15 hold a candidate's features and the constant 1 for the first MMA,
-    // then columns 0-63 its first hidden layer and column 64 the constant 1
-    // for the second (the features are consumed before the layer overwrites
-    // them, and the layer before the next tile's features)
+    // then columns 0-63 its first hidden layer for the second (the features
+    // are consumed before the layer overwrites them, and the layer before the
+    // next tile's features)
     alignas(128) unsigned char a2[kMlpTile * kMlpK2 * 2];
     alignas(8) uint64_t mbar;
     uint32_t tmem;       // base address of 64 tensor-memory columns (both layers' accumulators)
@@ -193,9 +195,6 @@ __device__ __forceinline__ void mlp_setup(MlpSmem& sm, const unsigned char* __re
     uint4* dst = reinterpret_cast<uint4*>(sm.w);
     for (int k = threadIdx.x; k < kPackBytes / 16; k += blockDim.x) dst[k] = __ldg(src + k);
     if (threadIdx.x == 0) mbar_init(&sm.mbar);
-    // the constant part of this thread's second-layer row: 1 at k = 64, zeros after
-    *reinterpret_cast<uint4*>(sm.a2 + cm_offset(threadIdx.x, 64, 10)) = make_uint4(0x3f80u, 0u, 0u, 0u);
-    *reinterpret_cast<uint4*>(sm.a2 + cm_offset(threadIdx.x, 72, 10)) = make_uint4(0u, 0u, 0u, 0u);
     if (threadIdx.x < 32) tc_alloc(&sm.tmem, 64);
     fence_async_smem();
     tc_fence_before();
@@ -230,12 +229,12 @@ __device__ __forceinline__ void mlp_layer_sync(MlpSmem& sm, int layer, MlpThread
         tc_fence_after();
         const uint32_t w = smem_addr(sm.w);
         if (layer == 0) {
-            tc_mma(sm.tmem, smem_desc(smem_addr(sm.a2), 128, 1280), smem_desc(w + kPackW1, 128, 256), kIdescBf16M128N64, 0);
+            tc_mma(sm.tmem, smem_desc(smem_addr(sm.a2), 128, 1024), smem_desc(w + kPackW1, 128, 256), kIdescBf16M128N64, 0);
         } else {
             const uint32_t a2 = smem_addr(sm.a2);
 #pragma unroll
             for (int kc = 0; kc < kMlpK2 / 16; ++kc)
-                tc_mma(sm.tmem, smem_desc(a2 + 256 * kc, 128, 1280), smem_desc(w + kPackW2 + 256 * kc, 128, 1280),
+                tc_mma(sm.tmem, smem_desc(a2 + 256 * kc, 128, 1024), smem_desc(w + kPackW2 + 256 * kc, 128, 1024),
                        kIdescBf16M128N64, kc > 0 ? 1u : 0u);
         }
         tc_commit(&sm.mbar);
@@ -260,8 +259,8 @@ __device__ __forceinline__ void mlp_tile_begin(MlpSmem& sm, const float* x, MlpT
     for (int j = 0; j < 6; ++j) q[j] = pack_bf16x2(x[2 * j], x[2 * j + 1]);
     q[6] = 0x3f80u;  // the constant 1 (BF16) that carries b1, then zeros
     q[7] = 0u;
-    *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 0, 10)) = make_uint4(q[0], q[1], q[2], q[3]);
-    *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 8, 10)) = make_uint4(q[4], q[5], q[6], q[7]);
+    *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 0, 8)) = make_uint4(q[0], q[1], q[2], q[3]);
+    *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 8, 8)) = make_uint4(q[4], q[5], q[6], q[7]);
     fence_async_smem();
     tc_fence_before();
     if (__syncthreads_or(st.abort ? 1 : 0)) {
@@ -270,7 +269,7 @@ __device__ __forceinline__ void mlp_tile_begin(MlpSmem& sm, const float* x, MlpT
     }
     if (t == 0) {
         tc_fence_after();
-        tc_mma(sm.tmem, smem_desc(smem_addr(sm.a2), 128, 1280), smem_desc(smem_addr(sm.w) + kPackW1, 128, 256),
+        tc_mma(sm.tmem, smem_desc(smem_addr(sm.a2), 128, 1024), smem_desc(smem_addr(sm.w) + kPackW1, 128, 256),
                kIdescBf16M128N64, 0);
         tc_commit(&sm.mbar);
     }
@@ -297,10 +296,11 @@ __device__ __forceinline__ float mlp_tile_end(MlpSmem& sm, MlpThread& st) {
         uint32_t q[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) q[j] = pack_bf16x2_relu(v[2 * j], v[2 * j + 1]);
-        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c, 10)) = make_uint4(q[0], q[1], q[2], q[3]);
-        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c + 8, 10)) = make_uint4(q[4], q[5], q[6], q[7]);
+        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c, 8)) = make_uint4(q[0], q[1], q[2], q[3]);
+        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c + 8, 8)) = make_uint4(q[4], q[5], q[6], q[7]);
     }
     mlp_layer_sync(sm, 1, st);
+    const float4* b2 = reinterpret_cast<const float4*>(sm.w + kPackB2);
     const float4* w3 = reinterpret_cast<const float4*>(sm.w + kPackW3);
     float z = *reinterpret_cast<const float*>(sm.w + kPackB3);
 #pragma unroll
@@ -309,11 +309,11 @@ __device__ __forceinline__ float mlp_tile_end(MlpSmem& sm, MlpThread& st) {
         tc_ld16(lane_base + 16 * c, v);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float4 w = w3[4 * c + j];
-            z = __fmaf_rn(w.x, fmaxf(v[4 * j], 0.f), z);
-            z = __fmaf_rn(w.y, fmaxf(v[4 * j + 1], 0.f), z);
-            z = __fmaf_rn(w.z, fmaxf(v[4 * j + 2], 0.f), z);
-            z = __fmaf_rn(w.w, fmaxf(v[4 * j + 3], 0.f), z);
+            const float4 w = w3[4 * c + j], bb = b2[4 * c + j];
+            z = __fmaf_rn(w.x, fmaxf(__fadd_rn(v[4 * j], bb.x), 0.f), z);
+            z = __fmaf_rn(w.y, fmaxf(__fadd_rn(v[4 * j + 1], bb.y), 0.f), z);
+            z = __fmaf_rn(w.z, fmaxf(__fadd_rn(v[4 * j + 2], bb.z), 0.f), z);
+            z = __fmaf_rn(w.w, fmaxf(__fadd_rn(v[4 * j + 3], bb.w), 0.f), z);
         }
     }
     return z;
