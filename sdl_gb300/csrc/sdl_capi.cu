@@ -359,6 +359,7 @@ int ensure_buffers(sdlg_ctx* ctx) {
     AL(b.n_kept, 1);
     AL(b.sgpack, ctx->cap_obj[kSG] * PK_N);
     AL(b.sgfeat, ctx->cap_obj[kSG] * kFeatN);
+    AL(b.mdpack, ctx->cap_obj[kMD] * kMdPack);
     AL(b.counters, ctx->n_ev * 110);
     AL(b.status, 1);
     AL(b.task, kNumStages);

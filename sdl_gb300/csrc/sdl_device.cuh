@@ -470,6 +470,7 @@ struct MDView {
     float dphi, dphichange, dz, shiftedDz;
     const ModDev* m;  // lower module
 };
+constexpr int kMdPack = 16;  // floats per packed mini-doublet record
 
 // Segment.cc:886-994 (the three thresholds)
 __device__ __forceinline__ void dalpha_threshold(const MDView& im, const MDView& om, float th[3]) {

@@ -345,28 +345,63 @@ __device__ __forceinline__ int conn_entry(const BatchDev& b, int ev, int m, int6
     return lo;
 }
 
+// One 64-byte record per mini-doublet for the segment stage (k_md_pack):
+// the anchor hit with its derived quantities and asin / tan terms, the
+// mini-doublet's four floats, the lower module and the anchor's module.
+struct MDRec {
+    MDView v;
+    float a1, tf;  // asin(min(rt*k,.95)) and its float tan, of the anchor hit
+    int anc_mod;   // module of the anchor hit
+};
+__device__ __forceinline__ MDRec md_rec(const BatchDev& b, int64_t a) {
+    const float4* q = reinterpret_cast<const float4*>(&AT(b.mdpack, a * kMdPack, b.obj[kMD].cap * kMdPack));
+    const float4 r0 = __ldg(q), r1 = __ldg(q + 1), r2 = __ldg(q + 2), r3 = __ldg(q + 3);
+    MDRec r;
+    r.v.a.x = r0.x; r.v.a.y = r0.y; r.v.a.z = r0.z; r.v.a.rt = r0.w;
+    r.v.a.phi = r1.x; r.v.a.r3 = r1.y; r.a1 = r1.z; r.tf = r1.w;
+    r.v.dz = r2.x; r.v.shiftedDz = r2.y; r.v.dphi = r2.z; r.v.dphichange = r2.w;
+    r.v.m = &MOD(b, __float_as_int(r3.x));
+    r.anc_mod = __float_as_int(r3.y);
+    return r;
+}
+
+__global__ void k_md_pack(BatchDev b) {
+    if (halted(b)) return;
+    const int n_mod = b.geo.n_mod;
+    const int64_t n = min(OFF(b, kMD, b.n_gm), b.obj[kMD].cap);  // mini-doublets
+    for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
+        const int lm = OG(b, kMD, a) % n_mod;
+        const int anc = md_anchor(MOD(b, lm), OI(b, kMD, a), OJ(b, kMD, a));
+        const P3 p = hit(b, anc);
+        float4* q = reinterpret_cast<float4*>(&AT(b.mdpack, a * kMdPack, b.obj[kMD].cap * kMdPack));
+        q[0] = make_float4(p.x, p.y, p.z, p.rt);
+        q[1] = make_float4(p.phi, p.r3, AT(b.ha1, anc, H(b)), AT(b.htf, anc, H(b)));
+        q[2] = make_float4(OF(b, kMD, 0, a), OF(b, kMD, 1, a), OF(b, kMD, 2, a), OF(b, kMD, 3, a));
+        q[3] = make_float4(__int_as_float(lm), __int_as_float(AT(b.hgm, anc, H(b)) % n_mod), 0.f, 0.f);
+    }
+}
+
 // segment algorithm on inner MD a and outer MD bmd (Segment.cc:337-859);
 // `connected`: the outer MD's module is in the inner module's connection list
 // (the endcap algorithm's first requirement, Segment.cc:613-633)
 __device__ __forceinline__ bool sg_pair(const BatchDev& b, int a, int bmd, bool connected, float* fv) {
-    const int n_mod = b.geo.n_mod;
-    const MDView im = md_view(b, a);
-    const MDView om = md_view(b, bmd);
-    const int oanc = md_anchor(*om.m, OI(b, kMD, bmd), OJ(b, kMD, bmd));
+    const MDView im = md_rec(b, a).v;
+    const MDRec orec = md_rec(b, bmd);
+    const MDView& om = orec.v;
     SGVals v;
     v.dphi = v.dphimin = v.dphimax = v.dphichange = v.dphiminchange = v.dphimaxchange = 0.f;
     bool pass;
     const bool ob = om.m->subdet == kBarrel;
     if (ob) {
-        pass = sg_barrel(im, om, AT(b.ha1, oanc, H(b)), AT(b.htf, oanc, H(b)), v);
+        pass = sg_barrel(im, om, orec.a1, orec.tf, v);
     } else {
         P3 oHi = om.a, oLo = om.a;
         if (om.m->type == kTwoS && om.m->subdet == kEndcap) {
-            const ModDev& am = MOD(b, AT(b.hgm, oanc, H(b)) % n_mod);
+            const ModDev& am = MOD(b, orec.anc_mod);
             oHi = strip_edge(om.a, am, true);
             oLo = strip_edge(om.a, am, false);
         }
-        pass = sg_endcap(im, om, AT(b.ha1, oanc, H(b)), AT(b.htf, oanc, H(b)), connected, oHi, oLo, v);
+        pass = sg_endcap(im, om, orec.a1, orec.tf, connected, oHi, oLo, v);
     }
     fv[0] = v.dphi; fv[1] = v.dphimin; fv[2] = v.dphimax;
     fv[3] = v.dphichange; fv[4] = v.dphiminchange; fv[5] = v.dphimaxchange;
@@ -1323,6 +1358,8 @@ void launch_md(const BatchDev& b, cudaStream_t s, Hooks* h) {
 }
 
 void launch_sg(const BatchDev& b, cudaStream_t s, Hooks* h) {
+    k_md_pack<<<b.n_sm * 8, 256, 0, s>>>(b);
+    if (h) h->launches += 1;
     if (b.flags & kFlagSGLayers) {
         // Event.cc:793-821 increments no per-layer counter
         k_sg_count_layers<<<b.n_sm * 8, 256, 0, s>>>(b);

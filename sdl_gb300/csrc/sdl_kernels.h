@@ -38,6 +38,7 @@ struct BatchDev {
     int64_t* conn_sum;             // n_gm
     float* sgpack;                 // segment cap * PK_N packed records for the tracklet stage
     float* sgfeat;                 // segment cap * kFeatN: the pre-filter's per-segment feature records
+    float* mdpack;                 // mini-doublet cap * kMdPack: packed records for the segment stage
     uint32_t* counters;            // n_ev * 110
     uint32_t* status;
     unsigned long long* task;      // kNumStages work counters
