@@ -197,6 +197,19 @@ def headline_pus(rank, n):
     return np.random.default_rng(4242 + rank).uniform(150.0, 300.0, size=n)
 
 
+def headline_plan(rank, n):
+    """(seed, PU) of the n headline events of a rank: every rank runs its own
+    events (weak scaling); seeds of different ranks never coincide for n < 497"""
+    base = 1000 + 997 * rank
+    return [(base + 500 + k, float(p)) for k, p in enumerate(headline_pus(rank, n))]
+
+
+def single_plan(rank, n):
+    """(seed, PU) of the single-event workload of a rank"""
+    base = 1000 + 997 * rank
+    return [(base + k, 200.0) for k in range(n)]
+
+
 def cpu_sample(events, threads):
     import oracle
     from sdl_gb300 import synth
@@ -215,8 +228,7 @@ def run_reference_arm(a, rank, world, pg):
     oracle.build()
     n_ev = max(1, threads)
     # the first events of the headline workload (same seeds and PU draws)
-    pus = headline_pus(0, 128)
-    events = make_events([(1000 + 500 + k, float(pus[k])) for k in range(n_ev)], threads)
+    events = make_events(headline_plan(0, 128)[:n_ev], threads)
     for _ in range(a.warmup):
         cpu_sample(events[: max(1, threads // 4)], threads)
     rates, secs = [], []
@@ -273,10 +285,8 @@ def main():
     from sdl_gb300 import synth
     threads = os.cpu_count() or 1
     # ---- inputs (generated before any CUDA call) ----------------------------
-    base = 1000 + 997 * rank
-    pus = headline_pus(rank, a.batch_events)
-    batch = make_events([(base + 500 + k, float(p)) for k, p in enumerate(pus)], threads)
-    single = make_events([(base + k, 200.0) for k in range(4)], threads)
+    batch = make_events(headline_plan(rank, a.batch_events), threads)
+    single = make_events(single_plan(rank, 4), threads)
     cpu_events = []
     if rank == 0 and not a.no_cpu_baseline:
         cpu_events = batch[:max(1, threads)]
