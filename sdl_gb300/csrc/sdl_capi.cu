@@ -357,6 +357,9 @@ int ensure_buffers(sdlg_ctx* ctx) {
     b.kept_cap = ctx->cap_kept;
     AL(b.kept, b.kept_cap);
     AL(b.n_kept, 1);
+    AL(b.passa, b.kept_cap);
+    AL(b.passa_muls, b.kept_cap);
+    AL(b.n_passa, 1);
     AL(b.sgpack, ctx->cap_obj[kSG] * PK_N);
     AL(b.sgfeat, ctx->cap_obj[kSG] * kFeatN);
     AL(b.mdpack, ctx->cap_obj[kMD] * kMdPack);

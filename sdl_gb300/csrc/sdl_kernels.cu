@@ -849,8 +849,8 @@ constexpr int kMlpWarps = kMlpTile / 32;
 // reference).  The CTA takes 128 consecutive candidates at a time and scores
 // them as one tensor-core tile; the (inner, outer) segments of every
 // candidate whose logit reaches the threshold are appended to the kept list,
-// which k_tl_exact judges with the reference's cuts.  Control flow around the
-// tile is uniform over the CTA.
+// which k_tl_exact_a and k_tl_exact_b judge with the reference's cuts.
+// Control flow around the tile is uniform over the CTA.
 // write a tile's kept pairs (lanes in m) at the positions its atomic, issued
 // by lane `leader` (raw value there), reserved; every lane calls it
 __device__ __forceinline__ void kept_append(const BatchDev& b, unsigned m, unsigned long long raw, int leader, int2 pair) {
@@ -971,22 +971,15 @@ __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
     mlp_teardown(sm, st);
 }
 
-// The reference's tracklet cuts on the candidates the pre-filter kept:
-// phase A on every one, phase B on full warps of its survivors, exactly as
-// k_tl_enum does for all candidates.
-__global__ void __launch_bounds__(kEnumThreads, 3) k_tl_exact(BatchDev b) {
+// The reference's tracklet cuts on the candidates the pre-filter kept, in
+// two kernels so that each runs one phase's code: k_tl_exact_a runs phase A
+// on every kept candidate and lists its survivors (at most as many as kept
+// candidates), k_tl_exact_b runs phase B on the list and appends the
+// tracklets.
+__global__ void __launch_bounds__(kEnumThreads) k_tl_exact_a(BatchDev b) {
     if (halted(b)) return;
     const int64_t n = min((int64_t)*b.n_kept, b.kept_cap);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const bool nm1 = (b.flags & kFlagTLNm1) != 0;
-    __shared__ int qs[kEnumThreads / 32][kTLQueue];
-    __shared__ int qt[kEnumThreads / 32][kTLQueue];
-    __shared__ float qc[kEnumThreads / 32][kTLQueue];
-    __shared__ float qm[kEnumThreads / 32][kTLQueue];
-    __shared__ int qa[kEnumThreads / 32][kTLQueue];
-    const TLQueue q{qs[w], qt[w], qc[w], qm[w], qa[w]};
-    int qn = 0;
-    unsigned n_passA = 0;
     const int64_t nwarp = (int64_t)gridDim.x * (kEnumThreads / 32);
     for (int64_t base = ((int64_t)blockIdx.x * (kEnumThreads / 32) + w) * kWarp; base < n; base += nwarp * kWarp) {
         const int64_t i = base + lane;
@@ -998,12 +991,40 @@ __global__ void __launch_bounds__(kEnumThreads, 3) k_tl_exact(BatchDev b) {
             tt = p.y;
             algo = tl_phaseA(load_sgv(b.sgpack, s), load_sgv(b.sgpack, tt), cut, muls);
         }
-        n_passA += algo != kAlgoNone;
-        tl_queue_push(b, q, qn, algo, s, tt, cut, muls, nm1);
+        const bool pass = algo != kAlgoNone;
+        const unsigned m = __ballot_sync(0xffffffffu, pass);
+        if (!m) continue;
+        const int leader = __ffs(m) - 1;
+        unsigned long long p0 = 0;
+        if (lane == leader) p0 = atomicAdd(b.n_passa, (unsigned long long)__popc(m));
+        p0 = __shfl_sync(0xffffffffu, p0, leader);
+        if (pass) {
+            const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));  // below n <= kept_cap
+            AT(b.passa, pos, b.kept_cap) = make_int4(s, tt, algo, __float_as_int(cut));
+            AT(b.passa_muls, pos, b.kept_cap) = muls;
+        }
     }
-    tl_queue_drain(b, q, qn, nm1);
-    n_passA = __reduce_add_sync(0xffffffffu, n_passA);
-    if (lane == 0 && n_passA) atomicAdd(&b.mlp_stats->passA, (unsigned long long)n_passA);
+}
+
+__global__ void __launch_bounds__(kEnumThreads) k_tl_exact_b(BatchDev b) {
+    if (halted(b)) return;
+    const int64_t n = min((int64_t)*b.n_passa, b.kept_cap);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const bool nm1 = (b.flags & kFlagTLNm1) != 0;
+    const int64_t nwarp = (int64_t)gridDim.x * (kEnumThreads / 32);
+    for (int64_t base = ((int64_t)blockIdx.x * (kEnumThreads / 32) + w) * kWarp; base < n; base += nwarp * kWarp) {
+        const int64_t i = base + lane;
+        bool pass = false;
+        int s = 0, tt = 0;
+        if (i < n) {
+            const int4 p = AT(b.passa, i, b.kept_cap);
+            s = p.x;
+            tt = p.y;
+            pass = tl_phaseB(p.z, b.sgpack, s, tt, __int_as_float(p.w), AT(b.passa_muls, i, b.kept_cap), nm1);
+        }
+        append_rec(b, kTL, pass, s, tt, pass ? OG(b, kSG, s) : 0, nullptr);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.mlp_stats->passA, (unsigned long long)n);
 }
 
 __device__ __forceinline__ float hash_unit(unsigned long long c, unsigned long long seed) {
@@ -1387,10 +1408,12 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     if (h && h->timed) rec_event(h->enum_start[kTL], s);
     if (b.flags & kFlagMLP) {
         cudaMemsetAsync(b.n_kept, 0, sizeof(unsigned long long), s);
+        cudaMemsetAsync(b.n_passa, 0, sizeof(unsigned long long), s);
         k_tl_prefilter<<<b.n_sm * 8, kMlpTile, 0, s>>>(b);
         if (h && h->timed) rec_event(h->tl_mid, s);
-        k_tl_exact<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
-        if (h) h->launches += 1;
+        k_tl_exact_a<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
+        k_tl_exact_b<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
+        if (h) h->launches += 2;
     } else {
         k_tl_enum<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
     }

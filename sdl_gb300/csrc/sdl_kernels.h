@@ -56,6 +56,9 @@ struct BatchDev {
     int2* kept;                    // (inner, outer) segments of the tracklet candidates the pre-filter kept
     int64_t kept_cap;
     unsigned long long* n_kept;    // kept candidates found (can exceed kept_cap: overflow)
+    int4* passa;                   // kept candidates through phase A: (inner, outer, algorithm, cut bits)
+    float* passa_muls;             //   and their multiple-scattering factor (kept_cap entries)
+    unsigned long long* n_passa;
     int n_sm;
     unsigned long long* dbg;       // bounds-check record (debug builds): count, line, index, limit
 };
