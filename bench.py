@@ -274,6 +274,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--batch-events", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-only", action="store_true",
+                    help="time only the plain batched chain (a short run to profile its kernels)")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     rank, world, local, pg = dist()
@@ -303,6 +305,20 @@ def main():
     ch.mlp_set_params(params, thr)
     flush = L2Flush(local)
 
+    if a.plain_only:
+        ch.set_events(batch)
+        tuned_plain = ch.autotune(4, 0)
+        for _ in range(a.warmup):
+            ch.run(4, 0)
+        p_ms, p_stage, _, p_pass = timed_runs(ch, 0, a.steps, flush)
+        if rank == 0:
+            print(json.dumps({"workload": "plain batched chain, %d events of PU uniform in 150-300" % len(batch),
+                              "ms_per_step": round(statistics.fmean(p_ms), 3), "tuned": tuned_plain,
+                              "stage_ms": [round(float(v), 3) for v in np.mean(np.array(p_stage), axis=0)],
+                              "tl_passes_ms": [round(float(v), 3) for v in np.mean(np.array(p_pass), axis=0)]}))
+        ch.close()
+        return
+
     # ---- headline: batched + pre-filter, device-resident inputs --------------
     ch.set_events(batch)
     ch.run(4, FLAG_MLP)
@@ -328,14 +344,16 @@ def main():
     for _ in range(2):
         ch.run(4, 0)
     n_plain = ch.counts(-1)
-    p_ms, p_stage, p_tl, _ = timed_runs(ch, 0, max(3, a.steps // 4), flush)
+    p_ms, p_stage, p_tl, p_pass = timed_runs(ch, 0, max(3, a.steps // 4), flush)
     p_mean = allmax(pg, statistics.fmean(p_ms))
     tc_rec = float(n_pruned[4]) / max(1.0, float(n_plain[4]))
     tl_rec = float(n_pruned[2]) / max(1.0, float(n_plain[2]))
     plain_batched = {"value": round(allsum(pg, len(batch)) * 1e3 / p_mean, 3), "unit": "events/s", "tuned": tuned_plain,
                      "ms_per_step": round(p_mean, 3), "objects_per_step": [int(v) for v in n_plain],
                      "stage_ms": [round(float(v), 3) for v in np.mean(np.array(p_stage), axis=0)],
-                     "tl_kernel_ms": round(statistics.fmean(p_tl), 3)}
+                     "tl_kernel_ms": round(statistics.fmean(p_tl), 3),
+                     "tl_passes_ms": {"enumeration_and_float_cuts": round(float(np.mean([v[0] for v in p_pass])), 3),
+                                      "double_cuts": round(float(np.mean([v[1] for v in p_pass])), 3)}}
 
     # ---- end to end through the C ABI: pinned host buffers in, track
     # candidates out, for the whole batch each step -----------------------------

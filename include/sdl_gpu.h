@@ -138,9 +138,11 @@ int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5);
  * not depend on the shapes.  Takes about 24 runs of the chain. */
 int sdlg_autotune(sdlg_ctx* ctx, int stop_after, int flags, int32_t* out10);
 
-/* For a run with SDLG_FLAG_MLP: device time (ms) of the pre-filter kernel and
- * of the exact tracklet cuts on the candidates it kept (no counterpart in the
- * reference); zeros otherwise. */
+/* Device time (ms) of the last run's two tracklet passes (no counterpart in
+ * the reference): with SDLG_FLAG_MLP the pre-filter kernel and the exact
+ * tracklet cuts on the candidates it kept, else the enumeration with the
+ * cuts' float phase and the double-precision phase on its survivors; zeros
+ * for a run that stopped before the tracklets. */
 int sdlg_last_prefilter_times(sdlg_ctx* ctx, float* out2);
 
 /* Self-check of the float-float evaluations that stand for the reference's

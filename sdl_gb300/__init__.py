@@ -315,7 +315,8 @@ class Chain:
         return z
 
     def prefilter_times(self) -> np.ndarray:
-        """Device ms of the last FLAG_MLP run's pre-filter kernel and exact tracklet cuts."""
+        """Device ms of the last run's two tracklet passes: the pre-filter and the
+        exact cuts (FLAG_MLP), else enumeration + phase A and phase B."""
         out = np.zeros(2, dtype=np.float32)
         self._ck(lib().sdlg_last_prefilter_times(self.h, out.ctypes.data))
         return out

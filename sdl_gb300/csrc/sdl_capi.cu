@@ -360,6 +360,9 @@ int ensure_buffers(sdlg_ctx* ctx) {
     AL(b.passa, b.kept_cap);
     AL(b.passa_muls, b.kept_cap);
     AL(b.n_passa, 1);
+    AL(b.pb, b.kept_cap);
+    AL(b.pb2, b.kept_cap);
+    AL(b.n_pb, 2);
     AL(b.sgpack, ctx->cap_obj[kSG] * PK_N);
     AL(b.sgfeat, ctx->cap_obj[kSG] * kFeatN);
     AL(b.mdpack, ctx->cap_obj[kMD] * kMdPack);
@@ -972,7 +975,7 @@ int sdlg_last_prefilter_times(sdlg_ctx* ctx, float* out2) {
     if (!ctx || !out2) return SDLG_ERR_ARG;
     if (!ctx->ran) return fail(ctx, SDLG_ERR_NO_EVENTS, "chain not run");
     out2[0] = out2[1] = 0.f;
-    if (!(ctx->last_flags & SDLG_FLAG_MLP) || ctx->last_stop < kTL) return SDLG_OK;
+    if (ctx->last_stop < kTL) return SDLG_OK;
     cudaSetDevice(ctx->device);
     CK(cudaEventSynchronize(ctx->hooks.enum_stop[kTL]));
     CK(cudaEventElapsedTime(&out2[0], ctx->hooks.enum_start[kTL], ctx->hooks.tl_mid));

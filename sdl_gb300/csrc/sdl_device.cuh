@@ -818,36 +818,49 @@ __device__ __forceinline__ int tl_phaseA(const SGV& S, const SGV& T, float& sdlC
     return kAlgoNone;
 }
 
-// ---- phase B: the remaining cuts (mid-point direction, betaIn, the
-// deltaBeta iterations, betaOut and the deltaBeta cut)
+// ---- phase B1: the mid-point direction cut and the betaIn cut
+// (Tracklet.cc:1139-1222 BBBB, 1765-1819 BBEE, 2258-2292 EEEE; EEEE has no
+// betaIn cut).  Its code is the same for the three algorithms.  Returns
+// whether the candidate passes, and betaIn and dPhi, which phase B2 reuses.
 // (The records are loaded here from their indices: passing them by reference
-// to this out-of-line function would put them on the stack.)
-static __device__ __noinline__ bool tl_phaseB(int algo, const float* __restrict__ pack, int s, int t, float sdlCut,
-                                               float mulsF, bool nm1) {
+// to an out-of-line function would put them on the stack.)
+static __device__ __noinline__ bool tl_phaseB1(int algo, const float* __restrict__ pack, int s, int t, float sdlCut,
+                                                float& betaIn, float& dPhi) {
+    const SGV S = load_sgv(pack, s);
+    const SGV T = load_sgv(pack, t);
+    const P3 InLo = S.lo(), OutLo = T.lo(), OutUp = T.up();
+    dPhi = dphi(midpoint(InLo, OutLo), sub(OutLo, InLo));
+    if (!(fabsf(dPhi) <= sdlCut)) return false;
+    const P3 axis = sub(OutUp, InLo);  // tl_axis (BBBB) / dr3 (BBEE, EEEE)
+    betaIn = S.dpc - dphi(InLo, axis);  // alphaIn - dphi(InLo, axis)
+    if (algo == kAlgoEEEE) return true;
+    const float sdIn_d = S.urt - S.lrt;
+    const float betaIn_cut = f_asin(fmin_ref((-S.rtseg * 1.f + axis.rt) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdIn_d);
+    return fabsf(betaIn) < betaIn_cut;  // betaInRHmin == betaIn for BBBB and BBEE
+}
+
+// ---- phase B2: betaOut, the deltaBeta iterations, the betaOut cut and the
+// deltaBeta cut, on the candidates through phase B1
+static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict__ pack, int s, int t, float mulsF,
+                                                float betaIn, float dPhi, bool nm1) {
     const SGV S = load_sgv(pack, s);
     const SGV T = load_sgv(pack, t);
     const float pt_betaMax = 7.0f;
     const P3 InLo = S.lo(), InUp = S.up(), OutLo = T.lo(), OutUp = T.up();
-    const P3 mid = midpoint(InLo, OutLo);
-    const float dPhi = dphi(mid, sub(OutLo, InLo));
-    if (!(fabsf(dPhi) <= sdlCut)) return false;
-    const P3 axis = sub(OutUp, InLo);  // tl_axis (BBBB) / dr3 (BBEE, EEEE)
+    const P3 axis = sub(OutUp, InLo);
     const float dr = axis.rt;
     const float sdIn_dr = S.rtseg;
     const float sdIn_d = InUp.rt - InLo.rt;
     const float sdOut_dr = T.rtseg;
     const float sdOut_d = OutUp.rt - OutLo.rt;
-    float betaIn, betaOut, betaInRHmin, betaInRHmax, betaOutRHmin, betaOutRHmax;
-    float alphaIn, alphaOutReg;
+    const float alphaIn = S.dpc;
+    float betaOut, betaInRHmin, betaInRHmax, betaOutRHmin, betaOutRHmax;
+    float alphaOutReg;
     int lIn, lOut;
     float dBetaROut2 = 0.f;
     if (algo == kAlgoBBBB) {
         // Tracklet.cc:1205-1538
-        alphaIn = S.dpc;
-        betaIn = alphaIn - dphi(InLo, axis);
-        const float betaIn_cut = f_asin(fmin_ref((-sdIn_dr * 1.f + dr) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdIn_d);
         betaInRHmin = betaIn; betaInRHmax = betaIn;
-        if (!(fabsf(betaInRHmin) < betaIn_cut)) return false;
         betaOut = -T.alphaup + dphi(OutUp, axis);
         const bool ec2s = (T.flags & F_UP_E) && (T.flags & F_UP_2S);
         if (ec2s) {
@@ -871,18 +884,14 @@ static __device__ __noinline__ bool tl_phaseB(int algo, const float* __restrict_
         lOut = ec2s ? 11 : 5;
     } else if (algo == kAlgoBBEE) {
         // Tracklet.cc:1765-2016
-        alphaIn = S.dpc;
         const float sdOut_alphaOut = T.alphaup;
         const float sdOut_alphaOut_min = phi_mpi_pi(T.dpminc - T.dpmin);
         const float sdOut_alphaOut_max = phi_mpi_pi(T.dpmaxc - T.dpmax);
-        betaIn = alphaIn - dphi(InLo, axis);
         betaOut = -sdOut_alphaOut + dphi(OutUp, axis);
         betaInRHmin = betaIn; betaInRHmax = betaIn;  // isEC_secondLayer is always false (Tracklet.cc:1798)
         betaOutRHmin = betaOut - sdOut_alphaOut_min + sdOut_alphaOut;
         betaOutRHmax = betaOut - sdOut_alphaOut_max + sdOut_alphaOut;
         if (fabsf(betaOutRHmin) > fabsf(betaOutRHmax)) { const float t = betaOutRHmin; betaOutRHmin = betaOutRHmax; betaOutRHmax = t; }
-        const float betaIn_cut = f_asin(fmin_ref((-sdIn_dr * 1.f + dr) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdIn_d);
-        if (!(fabsf(betaInRHmin) < betaIn_cut)) return false;
         if (T.flags & F_UP_2S) {
             const float sinDPhi = f_sin(dPhi);
             const float hrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, true);
@@ -898,12 +907,10 @@ static __device__ __noinline__ bool tl_phaseB(int algo, const float* __restrict_
         lOut = 11;
     } else {
         // Tracklet.cc:2220-2665
-        alphaIn = S.dpc;
         const float sdOut_dPhiPos = T.dphilu;
         const float sdOut_alphaOutRHmin = phi_mpi_pi(T.dpminc - sdOut_dPhiPos);
         const float sdOut_alphaOutRHmax = phi_mpi_pi(T.dpmaxc - sdOut_dPhiPos);
         const float sdOut_alphaOut = phi_mpi_pi(T.dpc - sdOut_dPhiPos);
-        betaIn = alphaIn - dphi(InLo, axis);
         betaOut = -sdOut_alphaOut + dphi(OutUp, axis);
         betaInRHmin = betaIn + S.dpminc - alphaIn;
         betaInRHmax = betaIn + S.dpmaxc - alphaIn;
@@ -936,6 +943,13 @@ static __device__ __noinline__ bool tl_phaseB(int algo, const float* __restrict_
     const float dBetaCut2 = dbeta_cut2(dBetaRes, dBetaMuls, dBetaLum2, dBetaROut2, betaInRHmin, betaInRHmax, betaOutRHmin, betaOutRHmax);
     const float dBeta = betaIn - betaOut;
     return (dBeta * dBeta <= dBetaCut2) || nm1;
+}
+
+// phase B in one call (phase B1, then phase B2 on its survivors)
+__device__ __forceinline__ bool tl_phaseB(int algo, const float* __restrict__ pack, int s, int t, float sdlCut, float mulsF,
+                                          bool nm1) {
+    float betaIn = 0.f, dPhi = 0.f;
+    return tl_phaseB1(algo, pack, s, t, sdlCut, betaIn, dPhi) && tl_phaseB2(algo, pack, s, t, mulsF, betaIn, dPhi, nm1);
 }
 
 }  // namespace sdlg

@@ -731,66 +731,45 @@ __global__ void k_sg_pack(BatchDev b) {
     }
 }
 
-constexpr int kTLQueue = 64;  // per-warp queue of candidates that passed phase A
-
-// one warp's queue of tracklet candidates that passed phase A
-struct TLQueue {
-    int* s;
-    int* t;
-    float* cut;
-    float* muls;
-    int* algo;
-};
-
-// queue the lanes' phase-A survivors; once a full warp is queued, run phase
-// B on 32 of them and append the accepted ones (every lane calls it)
-__device__ __forceinline__ void tl_queue_push(const BatchDev& b, const TLQueue& q, int& qn, int algo, int s, int tt, float cut,
-                                              float muls, bool nm1) {
-    const int lane = threadIdx.x & 31;
-    const unsigned m = __ballot_sync(0xffffffffu, algo != kAlgoNone);
-    if (algo != kAlgoNone) {
-        const int p = qn + __popc(m & ((1u << lane) - 1u));
-        q.s[p] = s; q.t[p] = tt; q.cut[p] = cut; q.muls[p] = muls; q.algo[p] = algo;
-    }
-    qn += __popc(m);
-    __syncwarp();
-    if (qn >= kWarp) {
-        // phase B on the last 32 queued candidates
-        const int k = qn - kWarp + lane;
-        const int qs_ = q.s[k], qt_ = q.t[k], qa_ = q.algo[k];
-        const float qc_ = q.cut[k], qm_ = q.muls[k];
-        __syncwarp();
-        qn -= kWarp;
-        const bool pass = tl_phaseB(qa_, b.sgpack, qs_, qt_, qc_, qm_, nm1);
-        append_rec(b, kTL, pass, qs_, qt_, OG(b, kSG, qs_), nullptr);
-    }
-}
-
-// phase B on the fewer than 32 candidates left in the queue
-__device__ __forceinline__ void tl_queue_drain(const BatchDev& b, const TLQueue& q, int& qn, bool nm1) {
-    const int lane = threadIdx.x & 31;
-    bool pass = false;
-    int qs_ = 0, qt_ = 0;
-    if (lane < qn) {
-        qs_ = q.s[lane];
-        qt_ = q.t[lane];
-        pass = tl_phaseB(q.algo[lane], b.sgpack, qs_, qt_, q.cut[lane], q.muls[lane], nm1);
-    }
-    __syncwarp();
-    append_rec(b, kTL, pass, qs_, qt_, pass ? OG(b, kSG, qs_) : 0, nullptr);
-    qn = 0;
-}
-
 // outer segment of flat tracklet candidate c of inner segment s
 __device__ __forceinline__ int tl_outer_of(const BatchDev& b, bool lay, int s, int64_t q) {
     return lay ? tl_outer_layer(b, s, q) : tl_outer(b, s, q);
 }
 
-// Tracklet candidates (Event.cc:611-693 with Tracklet.cc:144-2665).  Phase A
-// (float cuts) runs on every candidate; its survivors go to a per-warp queue
-// in shared memory and phase B (the double-precision part) runs on full warps
-// of queued candidates.
-__global__ void __launch_bounds__(kEnumThreads, 3) k_tl_enum(BatchDev b) {
+// append the lanes' phase-A survivors to the survivor list at the positions
+// reserved on `count` (every lane calls it); positions past the list's
+// capacity are not written and flag the overflow (the count keeps growing, so
+// it holds the capacity needed)
+__device__ __forceinline__ void passa_append(const BatchDev& b, unsigned long long* count, int algo, int s, int tt,
+                                             float cut, float muls) {
+    const int lane = threadIdx.x & 31;
+    const bool pass = algo != kAlgoNone;
+    const unsigned m = __ballot_sync(0xffffffffu, pass);
+    if (!m) return;
+    const int leader = __ffs(m) - 1;
+    unsigned long long p0 = 0;
+    if (lane == leader) p0 = atomicAdd(count, (unsigned long long)__popc(m));
+    p0 = __shfl_sync(0xffffffffu, p0, leader);
+    if (!pass) return;
+    const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));
+    if (pos < b.kept_cap) {
+        AT(b.passa, pos, b.kept_cap) = make_int4(s, tt, algo, __float_as_int(cut));
+        AT(b.passa_muls, pos, b.kept_cap) = muls;
+    } else {
+        atomicOr(b.status, kStatusOverflowKept);
+    }
+}
+
+constexpr int kMlpWarps = kMlpTile / 32;
+
+// Tracklet candidates (Event.cc:611-693 with Tracklet.cc:144-2665) in three
+// kernels: k_tl_enum_a takes tasks of consecutive candidates from a shared
+// counter, runs phase A (the float cuts) on each and lists the survivors;
+// k_tl_b1 and k_tl_b2 run the two parts of phase B on compacted lists and
+// append the tracklets.  Each kernel keeps only its own phase's code
+// resident, and each phase runs on full warps.  The survivor list shares the
+// pre-filter's capacity and overflow handling (its count is n_kept).
+__global__ void __launch_bounds__(kEnumThreads) k_tl_enum_a(BatchDev b) {
     if (halted(b)) return;
     const int64_t nobj = n_inner(b, kTL);
     if (nobj <= 0) return;
@@ -799,16 +778,8 @@ __global__ void __launch_bounds__(kEnumThreads, 3) k_tl_enum(BatchDev b) {
     const int64_t total = AT(off, nobj, offlim);
     const int task = b.enum_task[kTL] > 0 ? b.enum_task[kTL] : kTaskDefault;
     const int64_t ntask = (total + task - 1) / task;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const bool nm1 = (b.flags & kFlagTLNm1) != 0;
+    const int lane = threadIdx.x & 31;
     const bool lay = (b.flags & kFlagTLLayers) != 0;
-    __shared__ int qs[kEnumThreads / 32][kTLQueue];
-    __shared__ int qt[kEnumThreads / 32][kTLQueue];
-    __shared__ float qc[kEnumThreads / 32][kTLQueue];
-    __shared__ float qm[kEnumThreads / 32][kTLQueue];
-    __shared__ int qa[kEnumThreads / 32][kTLQueue];
-    const TLQueue q{qs[w], qt[w], qc[w], qm[w], qa[w]};
-    int qn = 0;  // warp-uniform queue length
     for (;;) {
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(b.task + kTL, 1ull);
@@ -833,23 +804,18 @@ __global__ void __launch_bounds__(kEnumThreads, 3) k_tl_enum(BatchDev b) {
                 tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
                 (void)IX(s, b.obj[kSG].cap);
                 (void)IX(tt, b.obj[kSG].cap);
-                const SGV S = load_sgv(b.sgpack, s);
-                const SGV T = load_sgv(b.sgpack, tt);
-                algo = tl_phaseA(S, T, cut, muls);
+                algo = tl_phaseA(load_sgv(b.sgpack, s), load_sgv(b.sgpack, tt), cut, muls);
             }
-            tl_queue_push(b, q, qn, algo, s, tt, cut, muls, nm1);
+            passa_append(b, b.n_kept, algo, s, tt, cut, muls);
         }
     }
-    tl_queue_drain(b, q, qn, nm1);
 }
-
-constexpr int kMlpWarps = kMlpTile / 32;
 
 // Learned pre-filter of the tracklet candidates (no counterpart in the
 // reference).  The CTA takes 128 consecutive candidates at a time and scores
 // them as one tensor-core tile; the (inner, outer) segments of every
 // candidate whose logit reaches the threshold are appended to the kept list,
-// which k_tl_exact_a and k_tl_exact_b judge with the reference's cuts.
+// which k_tl_exact_a, k_tl_b1 and k_tl_b2 judge with the reference's cuts.
 // Control flow around the tile is uniform over the CTA.
 // write a tile's kept pairs (lanes in m) at the positions its atomic, issued
 // by lane `leader` (raw value there), reserved; every lane calls it
@@ -971,11 +937,10 @@ __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
     mlp_teardown(sm, st);
 }
 
-// The reference's tracklet cuts on the candidates the pre-filter kept, in
-// two kernels so that each runs one phase's code: k_tl_exact_a runs phase A
-// on every kept candidate and lists its survivors (at most as many as kept
-// candidates), k_tl_exact_b runs phase B on the list and appends the
-// tracklets.
+// The reference's tracklet cuts on the candidates the pre-filter kept:
+// k_tl_exact_a runs phase A on every kept candidate and lists its survivors
+// (at most as many as kept candidates); k_tl_b1 and k_tl_b2 then run phase B
+// on the list as for the plain chain.
 __global__ void __launch_bounds__(kEnumThreads) k_tl_exact_a(BatchDev b) {
     if (halted(b)) return;
     const int64_t n = min((int64_t)*b.n_kept, b.kept_cap);
@@ -991,24 +956,55 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_exact_a(BatchDev b) {
             tt = p.y;
             algo = tl_phaseA(load_sgv(b.sgpack, s), load_sgv(b.sgpack, tt), cut, muls);
         }
-        const bool pass = algo != kAlgoNone;
-        const unsigned m = __ballot_sync(0xffffffffu, pass);
-        if (!m) continue;
-        const int leader = __ffs(m) - 1;
-        unsigned long long p0 = 0;
-        if (lane == leader) p0 = atomicAdd(b.n_passa, (unsigned long long)__popc(m));
-        p0 = __shfl_sync(0xffffffffu, p0, leader);
-        if (pass) {
-            const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));  // below n <= kept_cap
-            AT(b.passa, pos, b.kept_cap) = make_int4(s, tt, algo, __float_as_int(cut));
-            AT(b.passa_muls, pos, b.kept_cap) = muls;
-        }
+        passa_append(b, b.n_passa, algo, s, tt, cut, muls);  // at most n <= kept_cap survivors
     }
 }
 
-__global__ void __launch_bounds__(kEnumThreads) k_tl_exact_b(BatchDev b) {
+// Phase B1 on a survivor list of phase A (count entries); the candidates
+// through it go to the phase-B2 list, BBBB ones from the front and the others
+// from the back, so that phase B2's warps mostly run one algorithm.  Front
+// and back never meet: together they hold at most count <= kept_cap entries.
+__global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const unsigned long long* count) {
     if (halted(b)) return;
-    const int64_t n = min((int64_t)*b.n_passa, b.kept_cap);
+    const int64_t n = min((int64_t)*count, b.kept_cap);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t nwarp = (int64_t)gridDim.x * (kEnumThreads / 32);
+    for (int64_t base = ((int64_t)blockIdx.x * (kEnumThreads / 32) + w) * kWarp; base < n; base += nwarp * kWarp) {
+        const int64_t i = base + lane;
+        bool pass = false;
+        int4 p = make_int4(0, 0, kAlgoNone, 0);
+        float betaIn = 0.f, dPhi = 0.f, muls = 0.f;
+        if (i < n) {
+            p = AT(b.passa, i, b.kept_cap);
+            muls = AT(b.passa_muls, i, b.kept_cap);
+            pass = tl_phaseB1(p.z, b.sgpack, p.x, p.y, __int_as_float(p.w), betaIn, dPhi);
+        }
+        const bool front = pass && p.z == kAlgoBBBB;
+        const unsigned mf = __ballot_sync(0xffffffffu, front);
+        const unsigned mb = __ballot_sync(0xffffffffu, pass && !front);
+        if (!(mf | mb)) continue;
+        unsigned long long pf = 0, pbk = 0;
+        if (lane == 0) {
+            if (mf) pf = atomicAdd(b.n_pb, (unsigned long long)__popc(mf));
+            if (mb) pbk = atomicAdd(b.n_pb + 1, (unsigned long long)__popc(mb));
+        }
+        pf = __shfl_sync(0xffffffffu, pf, 0);
+        pbk = __shfl_sync(0xffffffffu, pbk, 0);
+        if (pass) {
+            const unsigned below = (1u << lane) - 1u;
+            const int64_t pos = front ? (int64_t)pf + __popc(mf & below) : b.kept_cap - 1 - ((int64_t)pbk + __popc(mb & below));
+            AT(b.pb, pos, b.kept_cap) = make_int4(p.x, p.y, p.z, __float_as_int(muls));
+            AT(b.pb2, pos, b.kept_cap) = make_float2(betaIn, dPhi);
+        }
+    }
+    if ((b.flags & kFlagMLP) && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.mlp_stats->passA, (unsigned long long)n);
+}
+
+// Phase B2 on the phase-B2 list (front part, then back part); appends the tracklets.
+__global__ void __launch_bounds__(kEnumThreads) k_tl_b2(BatchDev b) {
+    if (halted(b)) return;
+    const int64_t nf = min((int64_t)b.n_pb[0], b.kept_cap);
+    const int64_t n = min(nf + (int64_t)b.n_pb[1], b.kept_cap);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const bool nm1 = (b.flags & kFlagTLNm1) != 0;
     const int64_t nwarp = (int64_t)gridDim.x * (kEnumThreads / 32);
@@ -1017,14 +1013,15 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_exact_b(BatchDev b) {
         bool pass = false;
         int s = 0, tt = 0;
         if (i < n) {
-            const int4 p = AT(b.passa, i, b.kept_cap);
+            const int64_t k = i < nf ? i : b.kept_cap - 1 - (i - nf);
+            const int4 p = AT(b.pb, k, b.kept_cap);
+            const float2 q = AT(b.pb2, k, b.kept_cap);
             s = p.x;
             tt = p.y;
-            pass = tl_phaseB(p.z, b.sgpack, s, tt, __int_as_float(p.w), AT(b.passa_muls, i, b.kept_cap), nm1);
+            pass = tl_phaseB2(p.z, b.sgpack, s, tt, __int_as_float(p.w), q.x, q.y, nm1);
         }
         append_rec(b, kTL, pass, s, tt, pass ? OG(b, kSG, s) : 0, nullptr);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.mlp_stats->passA, (unsigned long long)n);
 }
 
 __device__ __forceinline__ float hash_unit(unsigned long long c, unsigned long long seed) {
@@ -1412,11 +1409,15 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
         k_tl_prefilter<<<b.n_sm * 8, kMlpTile, 0, s>>>(b);
         if (h && h->timed) rec_event(h->tl_mid, s);
         k_tl_exact_a<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
-        k_tl_exact_b<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
-        if (h) h->launches += 2;
     } else {
-        k_tl_enum<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
+        cudaMemsetAsync(b.n_kept, 0, sizeof(unsigned long long), s);
+        k_tl_enum_a<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
+        if (h && h->timed) rec_event(h->tl_mid, s);
     }
+    cudaMemsetAsync(b.n_pb, 0, 2 * sizeof(unsigned long long), s);
+    k_tl_b1<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, (b.flags & kFlagMLP) ? b.n_passa : b.n_kept);
+    k_tl_b2<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
+    if (h) h->launches += (b.flags & kFlagMLP) ? 3 : 2;
     if (h && h->timed) rec_event(h->enum_stop[kTL], s);
     k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kTL);
     scan_h(b, b.obj[kTL].mod_cnt, b.n_gm_dev, b.n_gm, s, h);

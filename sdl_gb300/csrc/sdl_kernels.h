@@ -59,6 +59,9 @@ struct BatchDev {
     int4* passa;                   // kept candidates through phase A: (inner, outer, algorithm, cut bits)
     float* passa_muls;             //   and their multiple-scattering factor (kept_cap entries)
     unsigned long long* n_passa;
+    int4* pb;                      // candidates through phase B1: (inner, outer, algorithm, muls bits), BBBB
+    float2* pb2;                   //   from the front, the others from the back; and (betaIn, dPhi)
+    unsigned long long* n_pb;      // [2]: BBBB entries, other entries (kept_cap in all)
     int n_sm;
     unsigned long long* dbg;       // bounds-check record (debug builds): count, line, index, limit
 };
