@@ -253,7 +253,8 @@ def run_reference_arm(a, rank, world, pg):
 
 def timed_runs(ch, flags, steps, flush):
     """device ms per run (CUDA events around the chain on its stream), per
-    stage, of the tracklet kernels, and of the pre-filter kernel alone"""
+    stage, of the tracklet kernels, and of the tracklet passes (enumeration +
+    float cuts, pre-filter, double-precision cuts)"""
     out, stage, tl, pf = [], [], [], []
     for _ in range(steps):
         flush()
@@ -262,7 +263,7 @@ def timed_runs(ch, flags, steps, flush):
         out.append(float(t[6]))
         stage.append(t[:6].copy())
         tl.append(float(ch.kernel_times()[2]))
-        pf.append(ch.prefilter_times().copy())
+        pf.append(ch.tl_pass_times().copy())
     return out, stage, tl, pf
 
 
@@ -353,7 +354,7 @@ def main():
                      "stage_ms": [round(float(v), 3) for v in np.mean(np.array(p_stage), axis=0)],
                      "tl_kernel_ms": round(statistics.fmean(p_tl), 3),
                      "tl_passes_ms": {"enumeration_and_float_cuts": round(float(np.mean([v[0] for v in p_pass])), 3),
-                                      "double_cuts": round(float(np.mean([v[1] for v in p_pass])), 3)}}
+                                      "double_cuts": round(float(np.mean([v[2] for v in p_pass])), 3)}}
 
     # ---- end to end through the C ABI: pinned host buffers in, track
     # candidates out, for the whole batch each step -----------------------------
@@ -400,14 +401,15 @@ def main():
                     "tl_kernel_ms": round(statistics.fmean(s_tl), 4)}
 
     # ---- roofline of the dominant kernel of the headline run -----------------
-    # k_tl_prefilter: algorithmic bytes = segment records read once (28 B per
-    # segment) + kept candidate pairs written once (8 B each); tensor work =
-    # the pre-filter's MMAs per scored candidate
+    # k_tl_prefilter (the network over the phase-A survivor list): algorithmic
+    # bytes = each survivor entry read once (20 B) + each segment's feature
+    # record read once (64 B) + each kept entry written once (20 B); tensor
+    # work = the network's MMAs per scored candidate
     hbm, tflops, src = peaks()
     pf = np.mean(np.array(pf_ms), axis=0)
-    pf_mean, ex_mean = float(pf[0]), float(pf[1])
+    fc_mean, pf_mean, ex_mean = float(pf[0]), float(pf[1]), float(pf[2])
     n_sg = int(n_pruned[1])
-    alg_bytes = 28 * n_sg + 8 * mstats["kept"]
+    alg_bytes = 20 * mstats["scored"] + 64 * n_sg + 20 * mstats["kept"]
     achieved = alg_bytes / (pf_mean * 1e-3) / 1e9
     tr = ncu_traffic("tl_prefilter_traffic.json")
     traffic = None
@@ -416,9 +418,9 @@ def main():
     mma_tflops = mstats["scored"] * MLP_FLOPS_PER_CANDIDATE / (pf_mean * 1e-3) / 1e12
     roofline = {"bound": "hbm", "achieved": round(achieved, 3), "peak": hbm, "unit": "GB/s",
                 "frac": round(achieved / hbm, 6), "traffic": traffic, "peak_source": src,
-                "kernel": "k_tl_prefilter (tensor-core pre-filter of the tracklet candidates)",
+                "kernel": "k_tl_prefilter (tensor-core pre-filter of the tracklet candidates through the float cuts)",
                 "kernel_ms": round(pf_mean, 3), "algorithmic_bytes": alg_bytes,
-                "exact_cuts_kernel_ms": round(ex_mean, 3),
+                "enumeration_float_cuts_ms": round(fc_mean, 3), "double_cuts_ms": round(ex_mean, 3),
                 "tensor": {"achieved": round(mma_tflops, 2), "peak": tflops, "unit": "TFLOP/s",
                            "frac": round(mma_tflops / tflops, 5), "flops_per_candidate": MLP_FLOPS_PER_CANDIDATE,
                            "candidates": mstats["scored"]},
@@ -444,9 +446,9 @@ def main():
                        "stage_ms": {k: round(float(v), 3) for k, v in zip(("ingest", "MD", "SG", "TL", "TP", "TC"), hl_stage)},
                        "prefilter": {"weights": "sdl_gb300/weights/tl_mlp_pu.npz", "threshold": thr,
                                      "trained_on": "%d events, PU 100-300 (seeds 100000+)" % meta.get("train_events", 0),
-                                     "candidates": mstats["scored"], "kept": mstats["kept"],
-                                     "pruned_fraction": round(1.0 - mstats["kept"] / max(1, mstats["scored"]), 4),
-                                     "passed_float_cuts": mstats["passed_float_cuts"]},
+                                     "candidates": mstats["candidates"], "scored_after_float_cuts": mstats["scored"],
+                                     "kept": mstats["kept"],
+                                     "pruned_fraction": round(1.0 - mstats["kept"] / max(1, mstats["scored"]), 4)},
                        "wall_s": round(wall, 3)},
             "tc_recall": round(tc_rec, 5), "tl_recall": round(tl_rec, 5),
             "plain_batched": plain_batched, "plain_single": plain_single,

@@ -138,12 +138,11 @@ int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5);
  * not depend on the shapes.  Takes about 24 runs of the chain. */
 int sdlg_autotune(sdlg_ctx* ctx, int stop_after, int flags, int32_t* out10);
 
-/* Device time (ms) of the last run's two tracklet passes (no counterpart in
- * the reference): with SDLG_FLAG_MLP the pre-filter kernel and the exact
- * tracklet cuts on the candidates it kept, else the enumeration with the
- * cuts' float phase and the double-precision phase on its survivors; zeros
- * for a run that stopped before the tracklets. */
-int sdlg_last_prefilter_times(sdlg_ctx* ctx, float* out2);
+/* Device time (ms) of the last run's tracklet passes (no counterpart in the
+ * reference): the enumeration with the float part of the cuts, the
+ * pre-filter (0 without SDLG_FLAG_MLP), and the double-precision part of the
+ * cuts; zeros for a run that stopped before the tracklets. */
+int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3);
 
 /* Self-check of the float-float evaluations that stand for the reference's
  * double sub-expressions (no counterpart in the reference).  Function fn
@@ -192,9 +191,10 @@ int sdlg_mini_doublets_static(sdlg_ctx* ctx, int64_t n_hits, const float* d_x, c
 /* ---- Learned tracklet pre-filter (no counterpart in the reference) ----
  * A 12-64-64-1 perceptron (ReLU, BF16 weights and first hidden layer, FP32
  * accumulation) scores every tracklet candidate (inner segment, outer
- * segment) from 12 float features; with SDLG_FLAG_MLP a candidate whose logit
- * is below the threshold is dropped before the reference's tracklet cuts,
- * which still judge every other candidate.  The pruned chain's tracklets,
+ * segment) from 12 float features; with SDLG_FLAG_MLP every candidate through
+ * the float part of the reference's tracklet cuts is scored, one whose logit
+ * is below the threshold is dropped, and the rest of the cuts judge every
+ * other one.  The pruned chain's tracklets,
  * triplets and track candidates are therefore subsets of the plain chain's.
  * Inference runs on the tensor cores inside the tracklet kernel; training
  * runs on the GPU with this library's kernels on samples labelled by the
@@ -227,8 +227,9 @@ int sdlg_mlp_train(sdlg_ctx* ctx, int epochs, int batch, float lr, float pos_wei
 int sdlg_mlp_gradient(sdlg_ctx* ctx, int64_t n, const float* x, const float* y, const float* w, float* grad, double* loss);
 /* logits of n feature rows (n x 12) through the tensor-core kernel */
 int sdlg_mlp_score(sdlg_ctx* ctx, int64_t n, const float* x, float* logits);
-/* counts of the last run with SDLG_FLAG_MLP: candidates scored, kept,
- * kept and through the float cuts, tensor-core waits that gave up */
+/* counts of the last run with SDLG_FLAG_MLP: tracklet candidates, those
+ * through the float cuts (scored by the network), those kept (logit at or
+ * above the threshold), tensor-core waits that gave up */
 int sdlg_mlp_stats(sdlg_ctx* ctx, int64_t* out4);
 
 /* Pinned host memory for zero-staging transfers. */

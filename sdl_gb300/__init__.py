@@ -68,7 +68,7 @@ def lib():
         L.sdlg_get_counters.argtypes = [vp, i64, vp]
         L.sdlg_last_times.argtypes = [vp, vp]
         L.sdlg_last_kernel_times.argtypes = [vp, vp]
-        L.sdlg_last_prefilter_times.argtypes = [vp, vp]
+        L.sdlg_last_tl_pass_times.argtypes = [vp, vp]
         L.sdlg_math_check.argtypes = [vp, i32, i32, ctypes.c_uint64, i64, ctypes.c_uint64, vp]
         L.sdlg_autotune.argtypes = [vp, i32, i32, vp]
         L.sdlg_last_launches.argtypes = [vp]
@@ -314,11 +314,11 @@ class Chain:
         self._ck(lib().sdlg_mlp_score(self.h, len(x), x.ctypes.data, z.ctypes.data))
         return z
 
-    def prefilter_times(self) -> np.ndarray:
-        """Device ms of the last run's two tracklet passes: the pre-filter and the
-        exact cuts (FLAG_MLP), else enumeration + phase A and phase B."""
-        out = np.zeros(2, dtype=np.float32)
-        self._ck(lib().sdlg_last_prefilter_times(self.h, out.ctypes.data))
+    def tl_pass_times(self) -> np.ndarray:
+        """Device ms of the last run's tracklet passes: enumeration + float cuts,
+        the pre-filter (0 without FLAG_MLP), the double-precision cuts."""
+        out = np.zeros(3, dtype=np.float32)
+        self._ck(lib().sdlg_last_tl_pass_times(self.h, out.ctypes.data))
         return out
 
     def autotune(self, stop_after: int = 4, flags: int = 0) -> dict:
@@ -336,7 +336,8 @@ class Chain:
                 "first": [int(v) for v in out[3:8]] if out[2] else None}
 
     def mlp_stats(self) -> dict:
-        """Pre-filter counts of the last run with FLAG_MLP."""
+        """Pre-filter counts of the last run with FLAG_MLP: tracklet candidates,
+        those through the float cuts (scored by the network), those kept."""
         out = np.zeros(4, dtype=np.int64)
         self._ck(lib().sdlg_mlp_stats(self.h, out.ctypes.data))
-        return {"scored": int(out[0]), "kept": int(out[1]), "passed_float_cuts": int(out[2]), "timeouts": int(out[3])}
+        return {"candidates": int(out[0]), "scored": int(out[1]), "kept": int(out[2]), "timeouts": int(out[3])}

@@ -355,11 +355,12 @@ int ensure_buffers(sdlg_ctx* ctx) {
     b.bucket_cap = (int64_t)1 << 24;  // covers 2^32 candidates of one stage
     AL(b.bucket, b.bucket_cap);
     b.kept_cap = ctx->cap_kept;
-    AL(b.kept, b.kept_cap);
     AL(b.n_kept, 1);
     AL(b.passa, b.kept_cap);
     AL(b.passa_muls, b.kept_cap);
-    AL(b.n_passa, 1);
+    AL(b.kept, b.kept_cap);
+    AL(b.kept_muls, b.kept_cap);
+    AL(b.n_kept2, 1);
     AL(b.pb, b.kept_cap);
     AL(b.pb2, b.kept_cap);
     AL(b.n_pb, 2);
@@ -669,7 +670,8 @@ int sdlg_create(sdlg_ctx** out, int device) {
         e = cudaEventCreate(&ctx->hooks.enum_start[k]);
         if (e == cudaSuccess) e = cudaEventCreate(&ctx->hooks.enum_stop[k]);
     }
-    if (e == cudaSuccess) e = cudaEventCreate(&ctx->hooks.tl_mid);
+    for (int k = 0; k < 2; ++k)
+        if (e == cudaSuccess) e = cudaEventCreate(&ctx->hooks.tl_mid[k]);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_small, 16 * sizeof(int64_t));
     // pre-filter state is small and allocated once, so device pointers captured
     // in the launch graph never change
@@ -715,7 +717,8 @@ int sdlg_destroy(sdlg_ctx* ctx) {
         if (ctx->hooks.enum_start[k]) cudaEventDestroy(ctx->hooks.enum_start[k]);
         if (ctx->hooks.enum_stop[k]) cudaEventDestroy(ctx->hooks.enum_stop[k]);
     }
-    if (ctx->hooks.tl_mid) cudaEventDestroy(ctx->hooks.tl_mid);
+    for (int k = 0; k < 2; ++k)
+        if (ctx->hooks.tl_mid[k]) cudaEventDestroy(ctx->hooks.tl_mid[k]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return SDLG_OK;
@@ -971,15 +974,16 @@ int sdlg_autotune(sdlg_ctx* ctx, int stop_after, int flags, int32_t* out10) {
     return SDLG_OK;
 }
 
-int sdlg_last_prefilter_times(sdlg_ctx* ctx, float* out2) {
-    if (!ctx || !out2) return SDLG_ERR_ARG;
+int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3) {
+    if (!ctx || !out3) return SDLG_ERR_ARG;
     if (!ctx->ran) return fail(ctx, SDLG_ERR_NO_EVENTS, "chain not run");
-    out2[0] = out2[1] = 0.f;
+    out3[0] = out3[1] = out3[2] = 0.f;
     if (ctx->last_stop < kTL) return SDLG_OK;
     cudaSetDevice(ctx->device);
     CK(cudaEventSynchronize(ctx->hooks.enum_stop[kTL]));
-    CK(cudaEventElapsedTime(&out2[0], ctx->hooks.enum_start[kTL], ctx->hooks.tl_mid));
-    CK(cudaEventElapsedTime(&out2[1], ctx->hooks.tl_mid, ctx->hooks.enum_stop[kTL]));
+    CK(cudaEventElapsedTime(&out3[0], ctx->hooks.enum_start[kTL], ctx->hooks.tl_mid[0]));
+    CK(cudaEventElapsedTime(&out3[1], ctx->hooks.tl_mid[0], ctx->hooks.tl_mid[1]));
+    CK(cudaEventElapsedTime(&out3[2], ctx->hooks.tl_mid[1], ctx->hooks.enum_stop[kTL]));
     return SDLG_OK;
 }
 
@@ -1219,9 +1223,9 @@ int sdlg_mlp_stats(sdlg_ctx* ctx, int64_t* out4) {
     cudaSetDevice(ctx->device);
     MlpStats h;
     CK(cudaMemcpy(&h, ctx->mlp.stats, sizeof(h), cudaMemcpyDeviceToHost));
-    out4[0] = (int64_t)h.scored;
-    out4[1] = (int64_t)h.kept;
-    out4[2] = (int64_t)h.passA;
+    out4[0] = (int64_t)h.candidates;
+    out4[1] = (int64_t)h.scored;
+    out4[2] = (int64_t)h.kept;
     out4[3] = (int64_t)h.timeouts;
     return SDLG_OK;
 }

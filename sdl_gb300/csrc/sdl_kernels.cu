@@ -812,118 +812,94 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_a(BatchDev b) {
 }
 
 // Learned pre-filter of the tracklet candidates (no counterpart in the
-// reference).  The CTA takes 128 consecutive candidates at a time and scores
-// them as one tensor-core tile; the (inner, outer) segments of every
-// candidate whose logit reaches the threshold are appended to the kept list,
-// which k_tl_exact_a, k_tl_b1 and k_tl_b2 judge with the reference's cuts.
+// reference).  It scores the phase-A survivor list (n_kept entries) in tiles
+// of 128 entries on the tensor cores; the entries whose logit reaches the
+// threshold go to the kept list (n_kept2 entries), which k_tl_b1 and k_tl_b2
+// judge.  A candidate that fails phase A gives no tracklet, so the tracklets
+// are those of the plain chain among the candidates the network keeps; the
+// network only sees phase-A survivors, the candidates it was trained on.
+// Each CTA takes every gridDim.x-th tile; while the tensor cores run a
+// tile's first layer, the CTA loads the next tile's entries and features.
 // Control flow around the tile is uniform over the CTA.
-// write a tile's kept pairs (lanes in m) at the positions its atomic, issued
-// by lane `leader` (raw value there), reserved; every lane calls it
-__device__ __forceinline__ void kept_append(const BatchDev& b, unsigned m, unsigned long long raw, int leader, int2 pair) {
-    if (m == 0u) return;
-    const unsigned long long p0 = __shfl_sync(0xffffffffu, raw, leader);
+
+// one tile's kept entries: written once the atomic that reserved their
+// positions (issued by lane `leader`, raw value there) has returned
+struct PfPending {
+    unsigned m = 0u;
+    unsigned long long raw = 0ull;
+    int leader = 0;
+    int4 e = make_int4(0, 0, 0, 0);  // (inner, outer, algorithm, cut bits)
+    float muls = 0.f;
+};
+
+__device__ __forceinline__ void pf_flush(const BatchDev& b, const PfPending& p) {
+    if (p.m == 0u) return;
+    const unsigned long long p0 = __shfl_sync(0xffffffffu, p.raw, p.leader);
     const int lane = threadIdx.x & 31;
-    if (!((m >> lane) & 1u)) return;
-    const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));
-    if (pos < b.kept_cap) AT(b.kept, pos, b.kept_cap) = pair;
-    else atomicOr(b.status, kStatusOverflowKept);
+    if (!((p.m >> lane) & 1u)) return;
+    const int64_t pos = (int64_t)p0 + __popc(p.m & ((1u << lane) - 1u));  // below the list length <= kept_cap
+    AT(b.kept, pos, b.kept_cap) = p.e;
+    AT(b.kept_muls, pos, b.kept_cap) = p.muls;
 }
 
 __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
     __shared__ MlpSmem sm;
-    __shared__ long long s_task;
-    __shared__ int s_go;
-    if (threadIdx.x == 0) s_go = !halted(b) && n_inner(b, kTL) > 0;
-    __syncthreads();
-    if (!s_go) return;
-    const int64_t nobj = n_inner(b, kTL);
-    const int64_t* off = b.cand[kTL];
-    const int64_t offlim = b.cand_cap[kTL] + 1;
-    const int64_t total = AT(off, nobj, offlim);
-    const int64_t ntask = (total + kMlpTile - 1) / kMlpTile;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const bool lay = (b.flags & kFlagTLLayers) != 0;
+    if (halted(b)) return;
+    const int64_t n = min((int64_t)*b.n_kept, b.kept_cap);
+    const int64_t ntile = (n + kMlpTile - 1) / kMlpTile;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const int64_t nobj = n_inner(b, kTL);
+        const int64_t cand = nobj > 0 ? AT(b.cand[kTL], nobj, b.cand_cap[kTL] + 1) : 0;
+        atomicAdd(&b.mlp_stats->candidates, (unsigned long long)cand);
+    }
+    if ((int64_t)blockIdx.x >= ntile) return;
+    const int lane = threadIdx.x & 31;
     mlp_setup(sm, b.mlp_pack);
     const float thr = reinterpret_cast<const float*>(sm.w + kPackB3)[1];
     MlpThread st;
     unsigned n_scored = 0, n_kept = 0;
-    // Software pipeline over tiles: while the tensor cores run a tile's first
-    // layer, the CTA decodes the next tile's candidates and loads their
-    // features; a tile's kept candidates are written one tile later, when
-    // the atomic that reserved their positions has returned.
-    unsigned pend_m = 0;
-    unsigned long long pend_p0 = 0;
-    int pend_leader = 0;
-    int2 pend = make_int2(0, 0);
-    // decode candidate c = t * 128 + threadIdx.x of task t and compute its features
-    auto load_tile = [&](int64_t t, bool& valid, int& s, int& tt, float* f) {
-        const int64_t base = t * kMlpTile;
-        const int64_t end = t < ntask ? min(base + kMlpTile, total) : base;
-        const int64_t wbase = base + kWarp * w;
-        int ilo = 0;
-        if (lane < 2 && wbase < end) {
-            const int64_t wlast = min(wbase + kWarp, end) - 1;
-            int lo, hi;
-            obj_bounds(b, nobj, total, wbase, wlast, lo, hi);
-            ilo = find_obj(b, off, offlim, lo, hi, lane == 0 ? wbase : wlast);
-        }
-        const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
-        const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
-        const int64_t c = wbase + lane;
-        valid = c < end;
-        s = 0;
-        tt = 0;
+    // entry t * 128 + threadIdx.x of tile t and its features
+    auto load = [&](int64_t t, PfPending& p, float* f) -> bool {
+        const int64_t i = t * kMlpTile + threadIdx.x;
+        const bool valid = t < ntile && i < n;
         if (valid) {
-            s = (i0 == i1) ? i0 : find_obj(b, off, offlim, i0, i1, c);
-            tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
-            (void)IX(s, b.obj[kSG].cap);
-            (void)IX(tt, b.obj[kSG].cap);
-            tl_features(feat_s(b.sgfeat, s), feat_t(b.sgfeat, tt), f);
+            p.e = AT(b.passa, i, b.kept_cap);
+            p.muls = AT(b.passa_muls, i, b.kept_cap);
+            tl_features(feat_s(b.sgfeat, p.e.x), feat_t(b.sgfeat, p.e.y), f);
         } else {
 #pragma unroll
             for (int k = 0; k < kMlpIn; ++k) f[k] = 0.f;
         }
+        return valid;
     };
-    if (threadIdx.x == 0) s_task = (long long)atomicAdd(b.task + kTL, 1ull);
-    __syncthreads();
-    int64_t t = s_task;
-    bool valid;
-    int s, tt;
+    int64_t t = blockIdx.x;
+    PfPending cur, pend;
     float f[kMlpIn];
-    if (t < ntask) load_tile(t, valid, s, tt, f);
-    // s_task is rewritten only after every thread passed the barrier in
-    // mlp_tile_begin, i.e. after every thread has read it
-    __syncthreads();
-    if (threadIdx.x == 0) s_task = (long long)atomicAdd(b.task + kTL, 1ull);
-    while (t < ntask) {
-        mlp_tile_begin(sm, f, st);  // its barrier publishes s_task (the next task)
-        const int64_t tn = s_task;
-        unsigned long long nxt = 0;
-        if (threadIdx.x == 0) nxt = atomicAdd(b.task + kTL, 1ull);
-        bool valid_n;
-        int s_n, tt_n;
-        float f_n[kMlpIn];
-        load_tile(tn, valid_n, s_n, tt_n, f_n);
-        kept_append(b, pend_m, pend_p0, pend_leader, pend);
+    bool valid = load(t, cur, f);
+    while (t < ntile) {
+        mlp_tile_begin(sm, f, st);
+        const int64_t tn = t + gridDim.x;
+        PfPending nxt;
+        float fn[kMlpIn];
+        const bool valid_n = load(tn, nxt, fn);
+        pf_flush(b, pend);
         const float z = mlp_tile_end(sm, st);
         const bool keep = valid && z >= thr;
         n_scored += valid;
         n_kept += keep;
-        pend_m = __ballot_sync(0xffffffffu, keep);
-        if (pend_m) {
-            pend_leader = __ffs(pend_m) - 1;
-            if (lane == pend_leader) pend_p0 = atomicAdd(b.n_kept, (unsigned long long)__popc(pend_m));
+        cur.m = __ballot_sync(0xffffffffu, keep);
+        if (cur.m) {
+            cur.leader = __ffs(cur.m) - 1;
+            if (lane == cur.leader) cur.raw = atomicAdd(b.n_kept2, (unsigned long long)__popc(cur.m));
         }
-        pend = make_int2(s, tt);
-        if (threadIdx.x == 0) s_task = (long long)nxt;
-        t = tn;
+        pend = cur;
+        cur = nxt;
         valid = valid_n;
-        s = s_n;
-        tt = tt_n;
 #pragma unroll
-        for (int k = 0; k < kMlpIn; ++k) f[k] = f_n[k];
+        for (int k = 0; k < kMlpIn; ++k) f[k] = fn[k];
+        t = tn;
     }
-    kept_append(b, pend_m, pend_p0, pend_leader, pend);
+    pf_flush(b, pend);
     n_scored = __reduce_add_sync(0xffffffffu, n_scored);
     n_kept = __reduce_add_sync(0xffffffffu, n_kept);
     if (lane == 0) {
@@ -937,34 +913,12 @@ __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
     mlp_teardown(sm, st);
 }
 
-// The reference's tracklet cuts on the candidates the pre-filter kept:
-// k_tl_exact_a runs phase A on every kept candidate and lists its survivors
-// (at most as many as kept candidates); k_tl_b1 and k_tl_b2 then run phase B
-// on the list as for the plain chain.
-__global__ void __launch_bounds__(kEnumThreads) k_tl_exact_a(BatchDev b) {
-    if (halted(b)) return;
-    const int64_t n = min((int64_t)*b.n_kept, b.kept_cap);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t nwarp = (int64_t)gridDim.x * (kEnumThreads / 32);
-    for (int64_t base = ((int64_t)blockIdx.x * (kEnumThreads / 32) + w) * kWarp; base < n; base += nwarp * kWarp) {
-        const int64_t i = base + lane;
-        int algo = kAlgoNone, s = 0, tt = 0;
-        float cut = 0.f, muls = 0.f;
-        if (i < n) {
-            const int2 p = AT(b.kept, i, b.kept_cap);
-            s = p.x;
-            tt = p.y;
-            algo = tl_phaseA(load_sgv(b.sgpack, s), load_sgv(b.sgpack, tt), cut, muls);
-        }
-        passa_append(b, b.n_passa, algo, s, tt, cut, muls);  // at most n <= kept_cap survivors
-    }
-}
-
-// Phase B1 on a survivor list of phase A (count entries); the candidates
+// Phase B1 on a survivor list of phase A (count entries of list/muls); the candidates
 // through it go to the phase-B2 list, BBBB ones from the front and the others
 // from the back, so that phase B2's warps mostly run one algorithm.  Front
 // and back never meet: together they hold at most count <= kept_cap entries.
-__global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const unsigned long long* count) {
+__global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const int4* __restrict__ list,
+                                                         const float* __restrict__ list_muls, const unsigned long long* count) {
     if (halted(b)) return;
     const int64_t n = min((int64_t)*count, b.kept_cap);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -975,8 +929,8 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const unsign
         int4 p = make_int4(0, 0, kAlgoNone, 0);
         float betaIn = 0.f, dPhi = 0.f, muls = 0.f;
         if (i < n) {
-            p = AT(b.passa, i, b.kept_cap);
-            muls = AT(b.passa_muls, i, b.kept_cap);
+            p = AT(list, i, b.kept_cap);
+            muls = AT(list_muls, i, b.kept_cap);
             pass = tl_phaseB1(p.z, b.sgpack, p.x, p.y, __int_as_float(p.w), betaIn, dPhi);
         }
         const bool front = pass && p.z == kAlgoBBBB;
@@ -997,7 +951,6 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const unsign
             AT(b.pb2, pos, b.kept_cap) = make_float2(betaIn, dPhi);
         }
     }
-    if ((b.flags & kFlagMLP) && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.mlp_stats->passA, (unsigned long long)n);
 }
 
 // Phase B2 on the phase-B2 list (front part, then back part); appends the tracklets.
@@ -1403,21 +1356,22 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, kTL);
     if (h) h->launches += 1;
     if (h && h->timed) rec_event(h->enum_start[kTL], s);
-    if (b.flags & kFlagMLP) {
-        cudaMemsetAsync(b.n_kept, 0, sizeof(unsigned long long), s);
-        cudaMemsetAsync(b.n_passa, 0, sizeof(unsigned long long), s);
+    // enumeration + phase A -> survivor list (-> the pre-filter -> kept list)
+    // -> phase B1 -> phase B2
+    cudaMemsetAsync(b.n_kept, 0, sizeof(unsigned long long), s);
+    k_tl_enum_a<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
+    if (h && h->timed) rec_event(h->tl_mid[0], s);
+    const bool mlp = (b.flags & kFlagMLP) != 0;
+    if (mlp) {
+        cudaMemsetAsync(b.n_kept2, 0, sizeof(unsigned long long), s);
         k_tl_prefilter<<<b.n_sm * 8, kMlpTile, 0, s>>>(b);
-        if (h && h->timed) rec_event(h->tl_mid, s);
-        k_tl_exact_a<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
-    } else {
-        cudaMemsetAsync(b.n_kept, 0, sizeof(unsigned long long), s);
-        k_tl_enum_a<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
-        if (h && h->timed) rec_event(h->tl_mid, s);
     }
+    if (h && h->timed) rec_event(h->tl_mid[1], s);
     cudaMemsetAsync(b.n_pb, 0, 2 * sizeof(unsigned long long), s);
-    k_tl_b1<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, (b.flags & kFlagMLP) ? b.n_passa : b.n_kept);
+    k_tl_b1<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, mlp ? b.kept : b.passa, mlp ? b.kept_muls : b.passa_muls,
+                                                                 mlp ? b.n_kept2 : b.n_kept);
     k_tl_b2<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
-    if (h) h->launches += (b.flags & kFlagMLP) ? 3 : 2;
+    if (h) h->launches += mlp ? 3 : 2;
     if (h && h->timed) rec_event(h->enum_stop[kTL], s);
     k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kTL);
     scan_h(b, b.obj[kTL].mod_cnt, b.n_gm_dev, b.n_gm, s, h);

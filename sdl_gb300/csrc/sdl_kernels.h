@@ -53,12 +53,13 @@ struct BatchDev {
     int enum_grid[kNumStages];
     const unsigned char* mlp_pack; // packed pre-filter weights and threshold (kPackBytes)
     MlpStats* mlp_stats;           // pre-filter counts of the last run
-    int2* kept;                    // (inner, outer) segments of the tracklet candidates the pre-filter kept
-    int64_t kept_cap;
-    unsigned long long* n_kept;    // kept candidates found (can exceed kept_cap: overflow)
-    int4* passa;                   // kept candidates through phase A: (inner, outer, algorithm, cut bits)
-    float* passa_muls;             //   and their multiple-scattering factor (kept_cap entries)
-    unsigned long long* n_passa;
+    int4* passa;                   // tracklet candidates through phase A: (inner, outer, algorithm, cut bits)
+    float* passa_muls;             //   and their multiple-scattering factor
+    int64_t kept_cap;              // entries of each survivor list
+    unsigned long long* n_kept;    // phase-A survivors found (can exceed kept_cap: overflow)
+    int4* kept;                    // the phase-A survivors the pre-filter kept, as passa
+    float* kept_muls;
+    unsigned long long* n_kept2;
     int4* pb;                      // candidates through phase B1: (inner, outer, algorithm, muls bits), BBBB
     float2* pb2;                   //   from the front, the others from the back; and (betaIn, dPhi)
     unsigned long long* n_pb;      // [2]: BBBB entries, other entries (kept_cap in all)
@@ -69,9 +70,9 @@ struct BatchDev {
 // Host-side instrumentation of the launches: events around each stage's
 // candidate-evaluation kernel and a count of kernels launched.
 struct Hooks {
-    cudaEvent_t enum_start[kNumStages];
-    cudaEvent_t enum_stop[kNumStages];
-    cudaEvent_t tl_mid;  // between the pre-filter and the exact tracklet cuts
+    cudaEvent_t enum_start[kNumStages] = {};
+    cudaEvent_t enum_stop[kNumStages] = {};
+    cudaEvent_t tl_mid[2] = {};  // after phase A, after the pre-filter
     bool timed = false;
     int launches = 0;
 };

@@ -67,10 +67,10 @@ __host__ __device__ inline float bf16_round(float f) {
 }
 
 struct MlpStats {
-    unsigned long long scored;   // candidates scored
-    unsigned long long kept;     // logit >= threshold
-    unsigned long long passA;    // kept and through the float cuts (phase B load)
-    unsigned long long timeouts; // tensor-core waits that gave up
+    unsigned long long candidates;  // tracklet candidates
+    unsigned long long scored;      // through the float cuts (phase A) and scored
+    unsigned long long kept;        // logit >= threshold (phase B load)
+    unsigned long long timeouts;    // tensor-core waits that gave up
 };
 
 #if defined(__CUDACC__)

@@ -70,7 +70,7 @@ def pruned_counts(chain: Chain, det, events, thr: float, per_run: int = 16, flag
     chain.upload_detector(det)
     chain.mlp_set_threshold(thr)
     tl = tc = 0
-    st = {"scored": 0, "kept": 0, "passed_float_cuts": 0, "timeouts": 0}
+    st = {"candidates": 0, "scored": 0, "kept": 0, "timeouts": 0}
     for part in chunks(events, per_run):
         chain.set_events(part)
         chain.run(4, flags | FLAG_MLP)
@@ -152,9 +152,9 @@ def evaluate(chain: Chain, det, events, per_run: int = 16, flags: int = 0) -> di
     return {
         "events": len(events), "tc_plain": tc0, "tc_pruned": tc, "tc_recall": tc / tc0 if tc0 else 1.0,
         "tl_plain": tl0, "tl_pruned": tl, "tl_recall": tl / tl0 if tl0 else 1.0,
-        "candidates": st["scored"], "kept": st["kept"], "pruned_fraction": 1.0 - st["kept"] / max(1, st["scored"]),
-        "plain_float_cut_passes": base["passed_float_cuts"], "kept_float_cut_passes": st["passed_float_cuts"],
-        "exact_cut_load_reduction": 1.0 - st["passed_float_cuts"] / max(1, base["passed_float_cuts"]),
+        "candidates": st["candidates"], "scored": st["scored"], "kept": st["kept"],
+        "pruned_fraction": 1.0 - st["kept"] / max(1, st["scored"]),
+        "exact_cut_load_reduction": 1.0 - st["kept"] / max(1, base["kept"]),
     }
 
 
@@ -180,10 +180,9 @@ def fit(chain: Chain, det, train, held, *, neg_keep: float, epochs: int, batch: 
         "neg_keep": neg_keep, "epochs": epochs, "batch": batch, "lr": lr, "pos_weight": pos_weight,
         "loss_first": float(losses[0]), "loss_last": float(losses[-1]), "threshold": thr,
         "tc_recall": rec, "tl_recall": tl_rec, "target": target,
-        "candidates": base["scored"], "plain_float_cut_passes": base["passed_float_cuts"],
-        "kept": st["kept"], "kept_float_cut_passes": st["passed_float_cuts"],
+        "candidates": base["candidates"], "scored": base["scored"], "kept": st["kept"],
         "pruned_fraction": 1.0 - st["kept"] / max(1, st["scored"]),
-        "exact_cut_load_reduction": 1.0 - st["passed_float_cuts"] / max(1, base["passed_float_cuts"]),
+        "exact_cut_load_reduction": 1.0 - st["kept"] / max(1, base["kept"]),
     }
     log(json.dumps(report, sort_keys=True))
     return {"params": params, "threshold": thr, "report": report}
