@@ -154,7 +154,10 @@ int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3);
  * start .. start+n-1 (exhaustive != 0, unary functions) or hashed pseudo-random
  * inputs from `seed`.  out8: inputs where the fast path answered, of those
  * the ones whose float differs from the double evaluation's (must be 0), a
- * flag, and the first differing inputs and results as bit patterns. */
+ * flag, and the first differing inputs and results as bit patterns.
+ * Functions 16 (direction of a point by atan2f) and 17 (asinf) are the
+ * tracklet cuts' single-precision approximations: "differs" there means
+ * more than 2e-6 away from the exact value. */
 int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64_t n, uint64_t seed, uint64_t* out8);
 
 /* Number of kernels one run of the chain launches (as last enqueued). */

@@ -335,6 +335,7 @@ int ensure_buffers(sdlg_ctx* ctx) {
     AL(b.hit_gm, H); AL(b.hit_rank, H); AL(b.mod_hit, n_gm + 1);
     AL(b.hx, H); AL(b.hy, H); AL(b.hz, H); AL(b.hrt, H); AL(b.hphi, H); AL(b.hr3, H);
     AL(b.ha1, H); AL(b.htf, H); AL(b.htd, H); AL(b.ha3, H); AL(b.hidx, H); AL(b.hgm, H);
+    AL(b.hsx, H); AL(b.hsy, H); AL(b.hsz, H);
     const int nf[kNumStages] = {4, 6, 0, 0, 0};
     for (int s = 0; s < kNumStages; ++s) {
         const int64_t C = ctx->cap_obj[s];
@@ -362,7 +363,6 @@ int ensure_buffers(sdlg_ctx* ctx) {
     AL(b.kept_muls, b.kept_cap);
     AL(b.n_kept2, 1);
     AL(b.pb, b.kept_cap);
-    AL(b.pb2, b.kept_cap);
     AL(b.n_pb, 2);
     AL(b.sgpack, ctx->cap_obj[kSG] * PK_N);
     AL(b.sgfeat, ctx->cap_obj[kSG] * kFeatN);
@@ -990,7 +990,7 @@ int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3) {
 int64_t sdlg_last_launches(const sdlg_ctx* ctx) { return ctx ? ctx->launches_per_run : -1; }
 
 int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64_t n, uint64_t seed, uint64_t* out8) {
-    if (!ctx || !out8 || n < 0 || fn < 0 || fn > 15) return SDLG_ERR_ARG;
+    if (!ctx || !out8 || n < 0 || fn < 0 || fn > 17) return SDLG_ERR_ARG;
     cudaSetDevice(ctx->device);
     unsigned long long* d = nullptr;
     CK(cudaMalloc(&d, 8 * sizeof(unsigned long long)));

@@ -367,12 +367,15 @@ __device__ __forceinline__ float dphi_threshold(float rt, float asin_rt1, const 
     return add_dsqrt3(miniSlope, miniMuls, miniPVoff, miniLum);
 }
 
-// MiniDoublet.cc:989-1209.  pix/str are the anchoring and the shifted hit.
-__device__ __forceinline__ void shift_strip(const P3& lo, const P3& up, const ModDev& lm, float& xn, float& yn, float& zn) {
+// MiniDoublet.cc:989-1209 (shiftStripHits), split in two.  Everything up to
+// the shifted anchor point (xa, ya) and the new z depends only on the
+// anchoring hit `pix` and the lower module lm of its pair, so shift_anchor
+// runs once per hit (k_hit_scatter); shift_finish projects onto the strip
+// through the other hit `str` per mini-doublet candidate.  The arithmetic and
+// its order are the reference's.
+__device__ __forceinline__ void shift_anchor(const P3& pix, const ModDev& lm, float& xa, float& ya, float& zn) {
     const bool ps = lm.type == kPS;
     const bool pixLower = lm.ltype == kPixel;
-    const P3& pix = (ps && !pixLower) ? up : lo;
-    const P3& str = (ps && !pixLower) ? lo : up;
     const bool isEndcap = lm.subdet == kEndcap;
     const float angleA = fabsf(f_atan(pix.rt / pix.z));
     const float angleB = isEndcap ? (float)(kPi / 2.) : f_atan(lm.drdz_s);
@@ -390,14 +393,8 @@ __device__ __forceinline__ void shift_strip(const P3& lo, const P3& up, const Mo
     else angleM = two_pi_plus(-absArctanSlope);
     const float dx = drprime * f_sin(angleM);
     const float dy = drprime * f_cos(angleM);
-    const float xa = xp + dx, ya = yp + dy;
-    const float xo = str.x, yo = str.y;
-    if (slope == kSdlInf) { xn = xa; yn = yo; }
-    else if (slope == 0) { xn = xo; yn = ya; }
-    else {
-        xn = (slope * xa + (1.f / slope) * xo - ya + yo) / (slope + (1.f / slope));
-        yn = (xn - xa) * slope + ya;
-    }
+    xa = xp + dx;
+    ya = yp + dy;
     const float absdzprime = fabsf(sep / sAB * f_cos(angleA));
     float abszn;
     // one double operation on two floats rounded to float: the float operation
@@ -405,14 +402,30 @@ __device__ __forceinline__ void shift_strip(const P3& lo, const P3& up, const Mo
     else abszn = fabsf(pix.z) - absdzprime;
     zn = abszn * ((pix.z > 0) ? 1 : -1);
 }
+__device__ __forceinline__ void shift_finish(float xa, float ya, const P3& str, const ModDev& lm, float& xn, float& yn) {
+    const float slope = lm.slope_s;
+    const float xo = str.x, yo = str.y;
+    if (slope == kSdlInf) { xn = xa; yn = yo; }
+    else if (slope == 0) { xn = xo; yn = ya; }
+    else {
+        xn = (slope * xa + (1.f / slope) * xo - ya + yo) / (slope + (1.f / slope));
+        yn = (xn - xa) * slope + ya;
+    }
+}
+// whether the mini-doublets of the pair with lower module lm shift a strip
+// hit, and whether the upper hit anchors (MiniDoublet.cc:60-81)
+__device__ __forceinline__ bool md_shifts(const ModDev& lm) { return lm.subdet == kEndcap || lm.side != kCenter; }
+__device__ __forceinline__ bool md_upper_anchors(const ModDev& lm) { return lm.type == kPS && lm.ltype != kPixel; }
 
 struct MDVals {
     float dz, shiftedDz, dphi, dphichange;
 };
 
 // MiniDoublet.cc:243-447.  pixAsin is asin(min(rt*k, .95)) of the hit that
-// dPhiThreshold reads (the pixel-side hit).
-__device__ __forceinline__ bool md_barrel(const P3& lo, const P3& up, float pixAsin, const ModDev& lm, MDVals& v) {
+// dPhiThreshold reads (the pixel-side hit); sh is shift_anchor's (xa, ya, zn)
+// of the anchoring hit.
+__device__ __forceinline__ bool md_barrel(const P3& lo, const P3& up, float pixAsin, const ModDev& lm, const float* sh,
+                                          MDVals& v) {
     v.dz = lo.z - up.z;
     const float dz = v.dz;
     const float dzCut = lm.type == kPS ? 2.f : 10.f;
@@ -422,8 +435,8 @@ __device__ __forceinline__ bool md_barrel(const P3& lo, const P3& up, float pixA
     const float miniCut = dphi_threshold(0.f, pixAsin, lm, 0.f, 1.f);
     P3 shifted;
     if (lm.side != kCenter) {
-        float xn, yn, zn;
-        shift_strip(lo, up, lm, xn, yn, zn);
+        float xn, yn;
+        shift_finish(sh[0], sh[1], md_upper_anchors(lm) ? lo : up, lm, xn, yn);
         if (lm.ltype == kPixel) { shifted = mk2(xn, yn, up.z); v.dphi = dphi(lo, shifted); }
         else { shifted = mk2(xn, yn, lo.z); v.dphi = dphi(shifted, up); }
     } else {
@@ -442,14 +455,16 @@ __device__ __forceinline__ bool md_barrel(const P3& lo, const P3& up, float pixA
 }
 
 // MiniDoublet.cc:449-684
-__device__ __forceinline__ bool md_endcap(const P3& lo, const P3& up, float pixAsin, const ModDev& lm, MDVals& v) {
+__device__ __forceinline__ bool md_endcap(const P3& lo, const P3& up, float pixAsin, const ModDev& lm, const float* sh,
+                                          MDVals& v) {
     v.dz = lo.z - up.z;
     float dz = v.dz;
     if (!(fabsf(dz) < 10.f)) return false;  // side() is never SubDet::Endcap (MiniDoublet.cc:470)
     const float drtCut = lm.type == kPS ? 2.f : 10.f;
     if (!(fabsf(lo.rt - up.rt) < drtCut)) return false;
-    float xn, yn, zn;
-    shift_strip(lo, up, lm, xn, yn, zn);
+    float xn, yn;
+    const float zn = sh[2];
+    shift_finish(sh[0], sh[1], md_upper_anchors(lm) ? lo : up, lm, xn, yn);
     P3 shifted;
     if (lm.type == kPS && lm.ltype != kPixel) { shifted = mk2(xn, yn, lo.z); v.dphi = dphi(shifted, up); }
     else { shifted = mk2(xn, yn, up.z); v.dphi = dphi(lo, shifted); }
@@ -818,36 +833,96 @@ __device__ __forceinline__ int tl_phaseA(const SGV& S, const SGV& T, float& sdlC
     return kAlgoNone;
 }
 
-// ---- phase B1: the mid-point direction cut and the betaIn cut
-// (Tracklet.cc:1139-1222 BBBB, 1765-1819 BBEE, 2258-2292 EEEE; EEEE has no
-// betaIn cut).  Its code is the same for the three algorithms.  Returns
-// whether the candidate passes, and betaIn and dPhi, which phase B2 reuses.
-// (The records are loaded here from their indices: passing them by reference
-// to an out-of-line function would put them on the stack.)
-static __device__ __noinline__ bool tl_phaseB1(int algo, const float* __restrict__ pack, int s, int t, float sdlCut,
-                                                float& betaIn, float& dPhi) {
-    const SGV S = load_sgv(pack, s);
-    const SGV T = load_sgv(pack, t);
-    const P3 InLo = S.lo(), OutLo = T.lo(), OutUp = T.up();
-    dPhi = dphi(midpoint(InLo, OutLo), sub(OutLo, InLo));
-    if (!(fabsf(dPhi) <= sdlCut)) return false;
-    const P3 axis = sub(OutUp, InLo);  // tl_axis (BBBB) / dr3 (BBEE, EEEE)
-    betaIn = S.dpc - dphi(InLo, axis);  // alphaIn - dphi(InLo, axis)
-    if (algo == kAlgoEEEE) return true;
-    const float sdIn_d = S.urt - S.lrt;
-    const float betaIn_cut = f_asin(fmin_ref((-S.rtseg * 1.f + axis.rt) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdIn_d);
-    return fabsf(betaIn) < betaIn_cut;  // betaInRHmin == betaIn for BBBB and BBEE
+// Phase B1 decides most candidates from single-precision approximations of
+// its two angles: atan2f for the directions and asinf for the betaIn cut's
+// asin, whose errors CUDA documents as at most 3 and 2 ulp.  The exact values
+// are the floats nearest the reference's double evaluations; for angles
+// below pi the two differ by about 1e-6 at most, and the compared quantities
+// (a difference of two directions wrapped into [-pi, pi], minus a float;
+// an asin plus a float) by a few 1e-6.  A comparison is decided from the
+// approximations only when it holds by kB1Margin (about 400 ulp of pi), and
+// only away from the wrap at +-pi; otherwise the exact evaluation decides.
+// The self-check (functions 16 and 17 of k_math_check) bounds both
+// approximation errors by 2e-6 on the GPU itself.
+constexpr float kB1Margin = 1e-4f;
+constexpr float kPiF = 3.14159265f;
+
+// approximate direction of (x, y) (Hit.cc:68-83's phi), or false when the
+// point is at the origin, tiny, huge or not finite
+__device__ __forceinline__ bool phi_approx(float x, float y, float& p) {
+    const float m = fabsf(x) + fabsf(y);
+    if (!(m > 0x1p-60f && m < 0x1p60f)) return false;
+    p = atan2f(y, x);
+    return true;
+}
+// a difference of two directions in [-pi, pi], into [-pi, pi]
+__device__ __forceinline__ float wrap_approx(float d) {
+    return d > kPiF ? d - 2.f * kPiF : (d < -kPiF ? d + 2.f * kPiF : d);
+}
+// 1 when |v| < cut (or <= cut) holds by the margin, 0 when it fails by the
+// margin, -1 when the approximations cannot tell (v or cut not usable)
+__device__ __forceinline__ int clear_within(float v, float cut) {
+    const float a = fabsf(v);
+    if (!(a < 3.f && fabsf(cut) < 3.f)) return -1;
+    if (a > cut + kB1Margin) return 0;
+    if (a < cut - kB1Margin) return 1;
+    return -1;
 }
 
-// ---- phase B2: betaOut, the deltaBeta iterations, the betaOut cut and the
-// deltaBeta cut, on the candidates through phase B1
+// ---- phase B1: the mid-point direction cut and the betaIn cut
+// (Tracklet.cc:1139-1222 BBBB, 1765-1819 BBEE, 2258-2292 EEEE; EEEE has no
+// betaIn cut).  Its code is the same for the three algorithms.
+static __device__ __noinline__ bool tl_phaseB1(int algo, const float* __restrict__ pack, int s, int t, float sdlCut) {
+    const SGV S = load_sgv(pack, s);
+    const SGV T = load_sgv(pack, t);
+    // cut #5: dphi(midpoint(InLo, OutLo), OutLo - InLo) (the same float
+    // operations as midpoint() and sub())
+    float mx = 0.f, my = 0.f;
+    mx += S.lx; my += S.ly;
+    mx += T.lx; my += T.ly;
+    mx /= 2.f; my /= 2.f;
+    const float dx = T.lx - S.lx, dy = T.ly - S.ly;
+    int c5 = -1;
+    float pm, pd;
+    if (phi_approx(mx, my, pm) && phi_approx(dx, dy, pd)) c5 = clear_within(wrap_approx(pd - pm), sdlCut);
+    if (c5 < 0) {
+        const P3 InLo = S.lo(), OutLo = T.lo();
+        const float dPhi = dphi(midpoint(InLo, OutLo), sub(OutLo, InLo));
+        c5 = fabsf(dPhi) <= sdlCut ? 1 : 0;
+    }
+    if (!c5) return false;
+    if (algo == kAlgoEEEE) return true;
+    // betaIn = alphaIn - dphi(InLo, axis), axis = OutUp - InLo (tl_axis / dr3);
+    // betaIn_cut = asin(min((-sdIn_dr + dr) k / ptCut, sinAlphaMax)) + 0.02 / sdIn_d
+    const float ax = T.ux - S.lx, ay = T.uy - S.ly;
+    const float dr = __fsqrt_rn(__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(ay, ay)));  // as mk2()
+    const float sdIn_d = S.urt - S.lrt;
+    const float arg = fmin_ref((-S.rtseg * 1.f + dr) * k2Rinv1GeVf / kPtCut, kSinAlphaMax);
+    int cb = -1;
+    float pa;
+    if (phi_approx(ax, ay, pa) && fabsf(arg) <= kSinAlphaMax) {
+        const float w = wrap_approx(pa - S.lphi);
+        if (fabsf(w) < 3.f) cb = clear_within(S.dpc - w, asinf(arg) + (0.02f / sdIn_d));
+    }
+    if (cb < 0) {
+        const P3 InLo = S.lo();
+        const float betaIn = S.dpc - dphi(InLo, sub(T.up(), InLo));
+        cb = fabsf(betaIn) < f_asin(arg) + (0.02f / sdIn_d) ? 1 : 0;  // betaInRHmin == betaIn here
+    }
+    return cb != 0;
+}
+
+// ---- phase B2: betaIn, betaOut, the deltaBeta iterations, the betaOut cut
+// and the deltaBeta cut, on the candidates through phase B1 (exact values
+// throughout)
 static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict__ pack, int s, int t, float mulsF,
-                                                float betaIn, float dPhi, bool nm1) {
+                                                bool nm1) {
     const SGV S = load_sgv(pack, s);
     const SGV T = load_sgv(pack, t);
     const float pt_betaMax = 7.0f;
     const P3 InLo = S.lo(), InUp = S.up(), OutLo = T.lo(), OutUp = T.up();
     const P3 axis = sub(OutUp, InLo);
+    float betaIn = S.dpc - dphi(InLo, axis);
     const float dr = axis.rt;
     const float sdIn_dr = S.rtseg;
     const float sdIn_d = InUp.rt - InLo.rt;
@@ -868,7 +943,7 @@ static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict
             const P3 loE = edge_point(OutUp.x, OutUp.y, OutUp.z, T.ex, T.ey, false);
             betaOutRHmin = -dphi(hiE, sub(hiE, OutLo)) + dphi(hiE, sub(hiE, InLo));
             betaOutRHmax = -dphi(loE, sub(loE, OutLo)) + dphi(loE, sub(loE, InLo));
-            const float sinDPhi = f_sin(dPhi);
+            const float sinDPhi = f_sin(dphi(midpoint(InLo, OutLo), sub(OutLo, InLo)));
             const float rr = (hiE.rt - loE.rt) * sinDPhi / dr;
             dBetaROut2 = rr * rr;  // the double square of a float is exact: one rounding to float
         } else {
@@ -893,7 +968,7 @@ static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict
         betaOutRHmax = betaOut - sdOut_alphaOut_max + sdOut_alphaOut;
         if (fabsf(betaOutRHmin) > fabsf(betaOutRHmax)) { const float t = betaOutRHmin; betaOutRHmin = betaOutRHmax; betaOutRHmax = t; }
         if (T.flags & F_UP_2S) {
-            const float sinDPhi = f_sin(dPhi);
+            const float sinDPhi = f_sin(dphi(midpoint(InLo, OutLo), sub(OutLo, InLo)));
             const float hrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, true);
             const float lrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, false);
             const float rr = (hrt - lrt) * sinDPhi / dr;
@@ -948,8 +1023,7 @@ static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict
 // phase B in one call (phase B1, then phase B2 on its survivors)
 __device__ __forceinline__ bool tl_phaseB(int algo, const float* __restrict__ pack, int s, int t, float sdlCut, float mulsF,
                                           bool nm1) {
-    float betaIn = 0.f, dPhi = 0.f;
-    return tl_phaseB1(algo, pack, s, t, sdlCut, betaIn, dPhi) && tl_phaseB2(algo, pack, s, t, mulsF, betaIn, dPhi, nm1);
+    return tl_phaseB1(algo, pack, s, t, sdlCut) && tl_phaseB2(algo, pack, s, t, mulsF, nm1);
 }
 
 }  // namespace sdlg

@@ -264,6 +264,16 @@ __global__ void k_hit_scatter(BatchDev b) {
         AT(b.ha3, pos, H(b)) = f_asin(fmin_ref(p.rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax));
         AT(b.hidx, pos, H(b)) = AT(b.in_idx, h, H(b));
         AT(b.hgm, pos, H(b)) = gm;
+        // the strip shift of the mini-doublets this hit anchors
+        const int m = gm % b.geo.n_mod;
+        const ModDev& M = MOD(b, m);
+        const int lmi = M.lower ? m : M.partner;
+        float xa = 0.f, ya = 0.f, zn = 0.f;
+        if (lmi >= 0) {
+            const ModDev& lm = MOD(b, lmi);
+            if (md_shifts(lm) && (md_upper_anchors(lm) != (bool)M.lower)) shift_anchor(p, lm, xa, ya, zn);
+        }
+        AT(b.hsx, pos, H(b)) = xa; AT(b.hsy, pos, H(b)) = ya; AT(b.hsz, pos, H(b)) = zn;
     }
 }
 
@@ -321,9 +331,11 @@ struct MDStage {
         const int64_t lo = AT(b.mod_hit, gm, NG1(b)) + i, up = AT(b.mod_hit, pg, NG1(b)) + j;
         const P3 L = hit(b, lo), U = hit(b, up);
         const float pixAsin = lm.ltype == kPixel ? AT(b.ha1, lo, H(b)) : AT(b.ha1, up, H(b));
+        const int64_t anc = md_upper_anchors(lm) ? up : lo;
+        const float sh[3] = {AT(b.hsx, anc, H(b)), AT(b.hsy, anc, H(b)), AT(b.hsz, anc, H(b))};
         MDVals v;
         v.dz = 0.f; v.shiftedDz = 0.f; v.dphi = 0.f; v.dphichange = 0.f;
-        const bool pass = lm.subdet == kBarrel ? md_barrel(L, U, pixAsin, lm, v) : md_endcap(L, U, pixAsin, lm, v);
+        const bool pass = lm.subdet == kBarrel ? md_barrel(L, U, pixAsin, lm, sh, v) : md_endcap(L, U, pixAsin, lm, sh, v);
         oi = (int)lo; oj = (int)up;
         fv[0] = v.dz; fv[1] = v.shiftedDz; fv[2] = v.dphi; fv[3] = v.dphichange;
         return pass;
@@ -927,11 +939,11 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const int4* 
         const int64_t i = base + lane;
         bool pass = false;
         int4 p = make_int4(0, 0, kAlgoNone, 0);
-        float betaIn = 0.f, dPhi = 0.f, muls = 0.f;
+        float muls = 0.f;
         if (i < n) {
             p = AT(list, i, b.kept_cap);
             muls = AT(list_muls, i, b.kept_cap);
-            pass = tl_phaseB1(p.z, b.sgpack, p.x, p.y, __int_as_float(p.w), betaIn, dPhi);
+            pass = tl_phaseB1(p.z, b.sgpack, p.x, p.y, __int_as_float(p.w));
         }
         const bool front = pass && p.z == kAlgoBBBB;
         const unsigned mf = __ballot_sync(0xffffffffu, front);
@@ -948,7 +960,6 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const int4* 
             const unsigned below = (1u << lane) - 1u;
             const int64_t pos = front ? (int64_t)pf + __popc(mf & below) : b.kept_cap - 1 - ((int64_t)pbk + __popc(mb & below));
             AT(b.pb, pos, b.kept_cap) = make_int4(p.x, p.y, p.z, __float_as_int(muls));
-            AT(b.pb2, pos, b.kept_cap) = make_float2(betaIn, dPhi);
         }
     }
 }
@@ -968,10 +979,9 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b2(BatchDev b) {
         if (i < n) {
             const int64_t k = i < nf ? i : b.kept_cap - 1 - (i - nf);
             const int4 p = AT(b.pb, k, b.kept_cap);
-            const float2 q = AT(b.pb2, k, b.kept_cap);
             s = p.x;
             tt = p.y;
-            pass = tl_phaseB2(p.z, b.sgpack, s, tt, __int_as_float(p.w), q.x, q.y, nm1);
+            pass = tl_phaseB2(p.z, b.sgpack, s, tt, __int_as_float(p.w), nm1);
         }
         append_rec(b, kTL, pass, s, tt, pass ? OG(b, kSG, s) : 0, nullptr);
     }
@@ -1421,7 +1431,7 @@ __global__ void k_math_check(int fn, int exhaustive, unsigned long long start, l
             const unsigned long long h4 = mix64(h3 + 0x632BE59BD9B4E019ull);
             const float sa = (h1 & 1) ? -1.f : 1.f, sb = (h2 & 1) ? -1.f : 1.f;
             switch (fn) {
-                case 1: case 2:  // coordinates: magnitudes 2^-12..2^9, a fraction on axes and diagonals
+                case 1: case 2: case 16:  // coordinates: magnitudes 2^-12..2^9, a fraction on axes and diagonals
                     a = sa * hash_log(h1, -12.f, 9.f);
                     b = sb * hash_log(h2, -12.f, 9.f);
                     if ((h3 & 15) == 0) b = sb * fabsf(a) * (1.f + (float)((h4 >> 40) & 0xff) * 0x1p-20f);
@@ -1485,9 +1495,15 @@ __global__ void k_math_check(int fn, int exhaustive, unsigned long long start, l
             case 13: ok = hypot_fast(a, b, f); if (ok) ref = hypot_d(a, b); break;
             case 14: ok = times15_over_fast(a, b, f); if (ok) ref = times15_over_d(a, b); break;
             case 15: ok = muls_fast(a, b, false, f); if (ok) ref = muls_d(a, b, false); break;
+            case 16: ok = phi_approx(a, b, f); if (ok) ref = phi_of(a, b); break;
+            case 17: ok = fabsf(a) <= kSinAlphaMax; if (ok) { f = asinf(a); ref = f_asin(a); } break;
             default: break;
         }
-        const bool bad = ok && __float_as_uint(f) != __float_as_uint(ref) && !(isnan(f) && isnan(ref));
+        // functions 16 and 17 are the approximations of phase B1: within 2e-6
+        // of the exact value (directions compared modulo 2 pi); the others
+        // must match the double evaluation bit for bit
+        const bool bad = fn >= 16 ? ok && !(fabsf(fn == 16 ? wrap_approx(f - ref) : f - ref) <= 2e-6f)
+                                  : ok && __float_as_uint(f) != __float_as_uint(ref) && !(isnan(f) && isnan(ref));
         const unsigned m_ok = __ballot_sync(__activemask(), ok);
         const unsigned m_bad = __ballot_sync(__activemask(), bad);
         if ((threadIdx.x & 31) == 0) {

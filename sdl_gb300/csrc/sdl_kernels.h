@@ -25,6 +25,7 @@ struct BatchDev {
     int64_t* mod_hit;        // n_gm + 1: counts -> offsets
     // sorted hits (SoA)
     float *hx, *hy, *hz, *hrt, *hphi, *hr3, *ha1, *htf, *htd, *ha3;
+    float *hsx, *hsy, *hsz;  // the strip-shift anchor point of an anchoring hit (shift_anchor)
     int32_t *hidx, *hgm;
     // stages
     Objs obj[kNumStages];
@@ -61,7 +62,7 @@ struct BatchDev {
     float* kept_muls;
     unsigned long long* n_kept2;
     int4* pb;                      // candidates through phase B1: (inner, outer, algorithm, muls bits), BBBB
-    float2* pb2;                   //   from the front, the others from the back; and (betaIn, dPhi)
+                                   //   from the front, the others from the back
     unsigned long long* n_pb;      // [2]: BBBB entries, other entries (kept_cap in all)
     int n_sm;
     unsigned long long* dbg;       // bounds-check record (debug builds): count, line, index, limit

@@ -8,7 +8,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-ASIN, ATAN2, PHI, ADD_SQRT, ADD_SQRT3, PHI_MPI_PI, ADD_PI, PT, MULS, QSQ, SIN, COS, ATAN, HYPOT, T15, MULS1 = range(16)
+(ASIN, ATAN2, PHI, ADD_SQRT, ADD_SQRT3, PHI_MPI_PI, ADD_PI, PT, MULS, QSQ, SIN, COS, ATAN, HYPOT, T15, MULS1,
+ PHI_APPROX, ASIN_APPROX) = range(18)
 
 
 @pytest.fixture(scope="module")
@@ -47,3 +48,15 @@ def test_random_inputs(gpu, fn, n, min_answered):
     r = gpu.math_check(fn, n, seed=12345)
     assert r["mismatches"] == 0, r
     assert r["answered"] >= min_answered * n, (r["answered"], n)
+
+
+def test_phase_b1_approximation_bounds(gpu):
+    """Phase B1 decides from atan2f / asinf when a cut holds or fails by 1e-4;
+    both approximations must stay within 2e-6 of the exact values (asinf on
+    every float of the asin arguments, the directions on 2^28 hashed points)."""
+    n = _bits(0.95) - _bits(2.0 ** -30) + 1
+    for sign in (0, 0x80000000):
+        r = gpu.math_check(ASIN_APPROX, n, start=sign | _bits(2.0 ** -30), exhaustive=True)
+        assert r["mismatches"] == 0 and r["answered"] == n, r
+    r = gpu.math_check(PHI_APPROX, 1 << 28, seed=777)
+    assert r["mismatches"] == 0 and r["answered"] == 1 << 28, r
