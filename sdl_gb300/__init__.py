@@ -191,13 +191,21 @@ class Chain:
         self._ck(lib().sdlg_get_counts(self.h, event, out.ctypes.data))
         return out
 
-    def objects(self, stage: int, event: int = -1) -> np.ndarray:
+    def objects(self, stage: int, event: int = -1, out: np.ndarray | None = None) -> np.ndarray:
+        """Hit-index tuples of a stage's objects (all events: event = -1).
+        `out` (int32, C-contiguous, at least as many rows as objects and the
+        stage's width), e.g. a view of pinned() memory, is filled and its
+        first rows returned; otherwise a new array is."""
         n = ctypes.c_int64()
         self._ck(lib().sdlg_get_objects(self.h, stage, event, None, 0, ctypes.byref(n)))
-        out = np.empty((n.value, WIDTH[stage]), dtype=np.int32)
+        if out is None:
+            out = np.empty((n.value, WIDTH[stage]), dtype=np.int32)
+        elif (out.dtype != np.int32 or out.ndim != 2 or out.shape[1] != WIDTH[stage] or out.shape[0] < n.value
+              or not out.flags.c_contiguous):
+            raise ValueError("out must be a C-contiguous int32 array of shape (>= %d, %d)" % (n.value, WIDTH[stage]))
         if n.value:
             self._ck(lib().sdlg_get_objects(self.h, stage, event, out.ctypes.data, n.value, ctypes.byref(n)))
-        return out
+        return out[:n.value]
 
     def counters(self, event: int = 0) -> np.ndarray:
         out = np.zeros(110, dtype=np.uint32)
