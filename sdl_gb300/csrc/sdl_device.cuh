@@ -733,13 +733,33 @@ __device__ __forceinline__ float dbeta_cut2(float dBetaRes, float dBetaMuls, flo
 }
 
 
+// What phase A reads of the outer segment, from six arrays of one float per
+// segment (consecutive outer segments of a warp's candidates are then read
+// with coalesced loads); the same values as the packed record's fields.
+struct SGOuter {
+    float lrt, lz, ltd, la1, uphi;
+    uint32_t flags;
+};
+__device__ __forceinline__ SGOuter load_sgo(const float* __restrict__ a, int64_t cap, int64_t t) {
+    SGOuter o;
+    o.lrt = __ldg(a + t);
+    o.lz = __ldg(a + cap + t);
+    o.ltd = __ldg(a + 2 * cap + t);
+    o.la1 = __ldg(a + 3 * cap + t);
+    o.uphi = __ldg(a + 4 * cap + t);
+    o.flags = __float_as_uint(__ldg(a + 5 * cap + t));
+    return o;
+}
+
 // Tracklet algorithm ids carried between the two phases
 enum : int { kAlgoNone = 0, kAlgoBBBB = 1, kAlgoBBEE = 2, kAlgoEEEE = 3 };
 
 // ---- phase A: dispatch (Tracklet.cc:144-296) and the cuts that need only
 // float arithmetic and square roots.  Returns the algorithm or kAlgoNone,
 // and the two quantities phase B reuses.
-__device__ __forceinline__ int tl_phaseA(const SGV& S, const SGV& T, float& sdlCut, float& mulsF) {
+// (T: an SGV or an SGOuter, the outer segment)
+template <class TSeg>
+__device__ __forceinline__ int tl_phaseA(const SGV& S, const TSeg& T, float& sdlCut, float& mulsF) {
     const uint32_t fs = S.flags, ft = T.flags;
     const bool b1 = fs & F_LO_B, b2 = fs & F_UP_B, b3 = ft & F_LO_B, b4 = ft & F_UP_B;
     const bool e1 = fs & F_LO_E, e2 = fs & F_UP_E, e3 = ft & F_LO_E, e4 = ft & F_UP_E;

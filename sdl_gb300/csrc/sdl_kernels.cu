@@ -728,6 +728,10 @@ __global__ void k_sg_pack(BatchDev b) {
         v[PK_FLAGS] = __uint_as_float(fl);
         v[PK_G2] = __int_as_float(OG(b, kMD, om));
         v[PK_S0] = v[PK_S1] = v[PK_S2] = v[PK_S3] = 0.f;
+        const int64_t C = b.obj[kSG].cap;
+        const int fo[6] = {PK_LRT, PK_LZ, PK_LTD, PK_LA1, PK_UPHI, PK_FLAGS};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) AT(b.sgouter, k * C + s, 6 * C) = v[fo[k]];
         float4* dst = reinterpret_cast<float4*>(&AT(b.sgpack, s * PK_N, b.obj[kSG].cap * PK_N));
         for (int k = 0; k < PK_N / 4; ++k) dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
         // the pre-filter's feature records (inner role, outer role)
@@ -816,7 +820,7 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_a(BatchDev b) {
                 tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
                 (void)IX(s, b.obj[kSG].cap);
                 (void)IX(tt, b.obj[kSG].cap);
-                algo = tl_phaseA(load_sgv(b.sgpack, s), load_sgv(b.sgpack, tt), cut, muls);
+                algo = tl_phaseA(load_sgv(b.sgpack, s), load_sgo(b.sgouter, b.obj[kSG].cap, tt), cut, muls);
             }
             passa_append(b, b.n_kept, algo, s, tt, cut, muls);
         }
