@@ -527,20 +527,29 @@ struct SGVals {
     float dphi, dphimin, dphimax, dphichange, dphiminchange, dphimaxchange;
 };
 
-// Segment.cc:364-599.  outAsin / outTanf: asin(min(rtOut*k,.95)) of the
-// outer anchor and its float tan.
-__device__ __forceinline__ bool sg_barrel(const MDView& im, const MDView& om, float outAsin, float outTanf, SGVals& v) {
+// Segment.cc:364-599: sdCut of an outer barrel anchor (rtOut, asin term)
+// for inner barrel layer lIn
+__device__ __forceinline__ float sg_barrel_cut(int lIn, float rtOut, float outAsin) {
     const float mulsB[6] = {0.0052f, 0.0038f, 0.0034f, 0.0034f, 0.0032f, 0.0034f};
-    const float sdMuls = mulsB[im.m->layer - 1] * 3.f / kPtCut;
+    const float sdMuls = mulsB[lIn - 1] * 3.f / kPtCut;
+    const float sdPVoff = 0.1f / rtOut;
+    return add_dsqrt(outAsin, sdMuls * sdMuls + sdPVoff * sdPVoff);
+}
+
+// Segment.cc:364-599.  outAsin / outTanf: asin(min(rtOut*k,.95)) of the
+// outer anchor and its float tan; cutPrev: sg_barrel_cut for the barrel
+// layer below the outer one (k_md_pack).
+__device__ __forceinline__ bool sg_barrel(const MDView& im, const MDView& om, float outAsin, float outTanf, float cutPrev,
+                                          SGVals& v) {
     const float rtIn = im.a.rt, rtOut = om.a.rt, zIn = im.a.z, zOut = om.a.z;
     const float sdSlope = outAsin;
-    const float sdPVoff = 0.1f / rtOut;
     const float dzDrtScale = outTanf / sdSlope;
     const float zGeom = im.m->layer <= 2 ? 2.f * kPixelPSZpitch : 2.f * kStrip2SZpitch;
     const float zLo = zIn + (zIn - kDeltaZLum) * (rtOut / rtIn - 1.f) * (zIn > 0.f ? 1.f : dzDrtScale) - zGeom;
     const float zHi = zIn + (zIn + kDeltaZLum) * (rtOut / rtIn - 1.f) * (zIn < 0.f ? 1.f : dzDrtScale) + zGeom;
     if (!(zOut >= zLo && zOut <= zHi)) return false;
-    const float sdCut = add_dsqrt(sdSlope, sdMuls * sdMuls + sdPVoff * sdPVoff);
+    const bool prev = im.m->subdet == kBarrel && im.m->layer + 1 == om.m->layer;
+    const float sdCut = prev ? cutPrev : sg_barrel_cut(im.m->layer, rtOut, outAsin);
     const float deltaPhi = dphi(im.a, om.a);
     if (!(fabsf(deltaPhi) <= sdCut)) return false;
     v.dphichange = dphichange(im.a, om.a);
@@ -549,9 +558,10 @@ __device__ __forceinline__ bool sg_barrel(const MDView& im, const MDView& om, fl
 }
 
 // Segment.cc:601-859.  connected: outer module is in the inner module's
-// connection list (cut #0).
+// connection list (cut #0); phiHi / phiLo: the phi of the outer anchor's
+// strip-edge points (the anchor itself for PS modules; k_md_pack).
 __device__ __forceinline__ bool sg_endcap(const MDView& im, const MDView& om, float outAsin, float outTanf,
-                                          bool connected, const P3& oHi, const P3& oLo, SGVals& v) {
+                                          bool connected, float phiHi, float phiLo, SGVals& v) {
     const ModDev& I = *im.m;
     const bool l2r123 = (I.ring == 1 || I.ring == 2 || I.ring == 3) && I.layer == 2;
     if (!(connected || l2r123)) return false;
@@ -571,8 +581,8 @@ __device__ __forceinline__ bool sg_endcap(const MDView& im, const MDView& om, fl
     const float dPhiPos = dphi(im.a, om.a);
     const float sdCut = sdSlope;
     if (!(fabsf(dPhiPos) <= sdCut)) return false;
-    const float hiP = dphi(im.a, oHi);
-    const float loP = dphi(im.a, oLo);
+    const float hiP = phi_mpi_pi(phiHi - im.a.phi);  // dphi(im.a, oHi)
+    const float loP = phi_mpi_pi(phiLo - im.a.phi);
     const bool hiBigger = iabs(trunc_i32(hiP)) > iabs(trunc_i32(loP));
     v.dphi = dPhiPos;
     v.dphimax = hiBigger ? hiP : loP;

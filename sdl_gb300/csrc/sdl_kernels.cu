@@ -364,6 +364,7 @@ struct MDRec {
     MDView v;
     float a1, tf;  // asin(min(rt*k,.95)) and its float tan, of the anchor hit
     int anc_mod;   // module of the anchor hit
+    float c0, c1;  // barrel: sdCut for the layer below (c0); endcap: strip-edge phis (hi, lo)
 };
 __device__ __forceinline__ MDRec md_rec(const BatchDev& b, int64_t a) {
     const float4* q = reinterpret_cast<const float4*>(&AT(b.mdpack, a * kMdPack, b.obj[kMD].cap * kMdPack));
@@ -374,6 +375,8 @@ __device__ __forceinline__ MDRec md_rec(const BatchDev& b, int64_t a) {
     r.v.dz = r2.x; r.v.shiftedDz = r2.y; r.v.dphi = r2.z; r.v.dphichange = r2.w;
     r.v.m = &MOD(b, __float_as_int(r3.x));
     r.anc_mod = __float_as_int(r3.y);
+    r.c0 = r3.z;
+    r.c1 = r3.w;
     return r;
 }
 
@@ -389,7 +392,21 @@ __global__ void k_md_pack(BatchDev b) {
         q[0] = make_float4(p.x, p.y, p.z, p.rt);
         q[1] = make_float4(p.phi, p.r3, AT(b.ha1, anc, H(b)), AT(b.htf, anc, H(b)));
         q[2] = make_float4(OF(b, kMD, 0, a), OF(b, kMD, 1, a), OF(b, kMD, 2, a), OF(b, kMD, 3, a));
-        q[3] = make_float4(__int_as_float(lm), __int_as_float(AT(b.hgm, anc, H(b)) % n_mod), 0.f, 0.f);
+        // what the segment algorithms compute from this mini-doublet alone as
+        // the outer one: the barrel cut for the layer below, the endcap strip
+        // edges' phi
+        const ModDev& M = MOD(b, lm);
+        const int am = AT(b.hgm, anc, H(b)) % n_mod;
+        float c0 = 0.f, c1 = 0.f;
+        if (M.subdet == kBarrel) {
+            if (M.layer >= 2) c0 = sg_barrel_cut(M.layer - 1, p.rt, AT(b.ha1, anc, H(b)));
+        } else if (M.type == kTwoS) {
+            c0 = strip_edge(p, MOD(b, am), true).phi;
+            c1 = strip_edge(p, MOD(b, am), false).phi;
+        } else {
+            c0 = c1 = p.phi;
+        }
+        q[3] = make_float4(__int_as_float(lm), __int_as_float(am), c0, c1);
     }
 }
 
@@ -404,17 +421,8 @@ __device__ __forceinline__ bool sg_pair(const BatchDev& b, int a, int bmd, bool 
     v.dphi = v.dphimin = v.dphimax = v.dphichange = v.dphiminchange = v.dphimaxchange = 0.f;
     bool pass;
     const bool ob = om.m->subdet == kBarrel;
-    if (ob) {
-        pass = sg_barrel(im, om, orec.a1, orec.tf, v);
-    } else {
-        P3 oHi = om.a, oLo = om.a;
-        if (om.m->type == kTwoS && om.m->subdet == kEndcap) {
-            const ModDev& am = MOD(b, orec.anc_mod);
-            oHi = strip_edge(om.a, am, true);
-            oLo = strip_edge(om.a, am, false);
-        }
-        pass = sg_endcap(im, om, orec.a1, orec.tf, connected, oHi, oLo, v);
-    }
+    if (ob) pass = sg_barrel(im, om, orec.a1, orec.tf, orec.c0, v);
+    else pass = sg_endcap(im, om, orec.a1, orec.tf, connected, orec.c0, orec.c1, v);
     fv[0] = v.dphi; fv[1] = v.dphimin; fv[2] = v.dphimax;
     fv[3] = v.dphichange; fv[4] = v.dphiminchange; fv[5] = v.dphimaxchange;
     return pass;
