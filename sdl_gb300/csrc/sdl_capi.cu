@@ -376,6 +376,9 @@ int ensure_buffers(sdlg_ctx* ctx) {
     for (int s = 0; s < kNumStages; ++s) mx = std::max(mx, ctx->cap_obj[s]);
     b.scan_tmp_cap = mx / 4096 + 16;
     AL(b.scan_tmp, b.scan_tmp_cap);
+    AL(b.joff, ctx->cap_obj[kMD] + 1);
+    AL(b.jcur, ctx->cap_obj[kMD]);
+    AL(b.jidx, std::max(ctx->cap_obj[kSG], ctx->cap_obj[kTL]));
 #undef AL
     CK(cudaMemcpyAsync(b.n_gm_dev, &n_gm, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));

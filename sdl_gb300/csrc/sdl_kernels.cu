@@ -546,32 +546,53 @@ __device__ __forceinline__ int tl_outer_layer(const BatchDev& b, int s, int64_t 
     return layer_object(b, kSG, ev, tl_layer_outer(MOD(b, g1 - ev * n_mod).layer_slot), q);
 }
 
+// The triplets and track candidates are equi-joins on a mini-doublet: the
+// join index lists the objects of stage st (segments, or tracklets) by their
+// key mini-doublet (a segment's inner one; a tracklet's inner segment's inner
+// one), so that each join visits only matching objects (joff: offsets per
+// mini-doublet, jidx: the objects).
+__device__ __forceinline__ int join_key(const BatchDev& b, int st, int64_t o) {
+    return st == kSG ? OI(b, kSG, o) : OI(b, kSG, OI(b, kTL, o));
+}
+__device__ __forceinline__ int64_t join_n(const BatchDev& b, int md) {
+    return AT(b.joff, md + 1, b.obj[kMD].cap + 1) - AT(b.joff, md, b.obj[kMD].cap + 1);
+}
+__device__ __forceinline__ int join_obj(const BatchDev& b, int md, int64_t k) {
+    return AT(b.jidx, AT(b.joff, md, b.obj[kMD].cap + 1) + k, max(b.obj[kSG].cap, b.obj[kTL].cap));
+}
+
+// triplet candidates (Event.cc:524-597 via Triplet.cc:55): candidate q of
+// inner segment s1 is the (q mod n)-th segment starting at its outer
+// mini-doublet; the multiplicity of the outer module in the connection list
+// repeats each, as the reference's nested loops do (k_tp_count)
 struct TPStage {
     static constexpr int kSt = kTP;
     __device__ static bool eval(const BatchDev& b, int s1, int64_t q, int& oi, int& oj, float* fv) {
         const int omd = OJ(b, kSG, s1);
-        const int g2 = OG(b, kMD, omd);
-        const int64_t n2 = OFF(b, kSG, g2 + 1) - OFF(b, kSG, g2);
+        const int64_t n2 = join_n(b, omd);
         if (n2 <= 0) {
 #ifdef SDL_DEVICE_CHECKS
             IX(-2, 0);
 #endif
             return false;
         }
-        const int s2 = (int)(OFF(b, kSG, g2) + q % n2);
-        oi = s1; oj = s2;
+        oi = s1;
+        oj = join_obj(b, omd, q % n2);
         (void)fv;
-        return OI(b, kSG, s2) == omd;  // Triplet.cc:55 via Segment.cc:861-866
+        return true;
     }
     __device__ static int group_of(const BatchDev& b, int s) { return OG(b, kSG, s); }
 };
 
+// track candidates (Event.cc:823-872 via TrackCandidate.cc:161): candidate q
+// of inner tracklet t1 is the q-th tracklet whose inner segment starts at the
+// inner mini-doublet of t1's outer segment; it matches when that segment's
+// outer mini-doublet is the same too
 struct TCStage {
     static constexpr int kSt = kTC;
     __device__ static bool eval(const BatchDev& b, int t1, int64_t q, int& oi, int& oj, float* fv) {
         const int sB = OJ(b, kTL, t1);
-        const int g3 = OG(b, kSG, sB);
-        const int t2 = (int)(OFF(b, kTL, g3) + q);
+        const int t2 = join_obj(b, OI(b, kSG, sB), q);
         const int sC = OI(b, kTL, t2);
         oi = t1; oj = t2;
         (void)fv;
@@ -1220,6 +1241,23 @@ __global__ void k_tl_count_layers(BatchDev b) {
     }
 }
 
+// objects of stage st per key mini-doublet, then their positions
+__global__ void k_join_count(BatchDev b, int st) {
+    if (halted(b)) return;
+    const int64_t n = min(OFF(b, st, b.n_gm), b.obj[st].cap);
+    for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x)
+        atomicAdd((unsigned long long*)&AT(b.joff, join_key(b, st, o), b.obj[kMD].cap + 1), 1ull);
+}
+__global__ void k_join_scatter(BatchDev b, int st) {
+    if (halted(b)) return;
+    const int64_t n = min(OFF(b, st, b.n_gm), b.obj[st].cap);
+    for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x) {
+        const int k = join_key(b, st, o);
+        const int64_t pos = AT(b.joff, k, b.obj[kMD].cap + 1) + atomicAdd(&AT(b.jcur, k, b.obj[kMD].cap), 1);
+        AT(b.jidx, pos, max(b.obj[kSG].cap, b.obj[kTL].cap)) = (int)o;
+    }
+}
+
 __global__ void k_tp_count(BatchDev b) {
     if (halted(b)) return;
     const int n_mod = b.geo.n_mod;
@@ -1232,7 +1270,7 @@ __global__ void k_tp_count(BatchDev b) {
         int mult = 0;
         const int k0 = AT(b.geo.conn_off, m1, NM(b) + 1), k1 = AT(b.geo.conn_off, m1 + 1, NM(b) + 1);
         for (int k = k0; k < k1; ++k) mult += AT(b.geo.conn_idx, k, NC(b)) == m2;
-        AT(b.cand[kTP], s, b.cand_cap[kTP] + 1) = (int64_t)mult * (OFF(b, kSG, g2 + 1) - OFF(b, kSG, g2));
+        AT(b.cand[kTP], s, b.cand_cap[kTP] + 1) = (int64_t)mult * join_n(b, OJ(b, kSG, s));
     }
 }
 
@@ -1247,7 +1285,7 @@ __global__ void k_tc_count(BatchDev b) {
         if (m1.subdet == kBarrel && m1.layer == 1) {
             const int g3 = OG(b, kSG, OJ(b, kTL, t));
             const ModDev& m3 = MOD(b, g3 % n_mod);
-            if (m3.subdet == kBarrel && m3.layer == 3) c = OFF(b, kTL, g3 + 1) - OFF(b, kTL, g3);
+            if (m3.subdet == kBarrel && m3.layer == 3) c = join_n(b, OI(b, kSG, OJ(b, kTL, t)));
         }
         AT(b.cand[kTC], t, b.cand_cap[kTC] + 1) = c;
     }
@@ -1401,13 +1439,25 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     if (h) h->launches += 3;
 }
 
+// the join index of stage st's objects (segments or tracklets), keyed by mini-doublet
+static void join_index(const BatchDev& b, int st, cudaStream_t s, Hooks* h) {
+    cudaMemsetAsync(b.joff, 0, (b.obj[kMD].cap + 1) * sizeof(int64_t), s);
+    cudaMemsetAsync(b.jcur, 0, b.obj[kMD].cap * sizeof(int32_t), s);
+    k_join_count<<<b.n_sm * 8, 256, 0, s>>>(b, st);
+    scan_h(b, b.joff, b.obj[kMD].mod_cnt + b.n_gm, b.obj[kMD].cap, s, h);
+    k_join_scatter<<<b.n_sm * 8, 256, 0, s>>>(b, st);
+    if (h) h->launches += 2;
+}
+
 void launch_tp(const BatchDev& b, cudaStream_t s, Hooks* h) {
+    join_index(b, kSG, s, h);
     k_tp_count<<<b.n_sm * 8, 256, 0, s>>>(b);
     if (h) h->launches += 1;
     enum_and_group<TPStage>(b, s, h);
 }
 
 void launch_tc(const BatchDev& b, cudaStream_t s, Hooks* h) {
+    join_index(b, kTL, s, h);
     k_tc_count<<<b.n_sm * 8, 256, 0, s>>>(b);
     k_tc_cand_counter<<<grid_for(b.n_ev, 128, 1024), 128, 0, s>>>(b);
     if (h) h->launches += 2;

@@ -63,6 +63,11 @@ struct BatchDev {
     int4* kept;                    // the phase-A survivors the pre-filter kept, as passa
     float* kept_muls;
     unsigned long long* n_kept2;
+    // join index (triplets, then track candidates): the segments by their inner
+    // mini-doublet, then the tracklets by their inner segment's inner mini-doublet
+    int64_t* joff;                 // mini-doublet cap + 1: counts -> offsets
+    int32_t* jcur;                 // mini-doublet cap: fill cursors
+    int32_t* jidx;                 // max(segment cap, tracklet cap): object indices
     int4* pb;                      // candidates through phase B1: (inner, outer, algorithm, muls bits), BBBB
                                    //   from the front, the others from the back
     unsigned long long* n_pb;      // [2]: BBBB entries, other entries (kept_cap in all)
