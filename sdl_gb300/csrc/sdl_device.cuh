@@ -944,9 +944,15 @@ static __device__ __noinline__ bool tl_phaseB1(int algo, const float* __restrict
 
 // ---- phase B2: betaIn, betaOut, the deltaBeta iterations, the betaOut cut
 // and the deltaBeta cut, on the candidates through phase B1 (exact values
-// throughout)
+// throughout).  kSet restricts the algorithms compiled in (kB2All, kB2BBBB:
+// BBBB only, kB2Others: BBEE and EEEE), so that a kernel running one group
+// keeps only that code resident.
+enum : int { kB2All = 0, kB2BBBB = 1, kB2Others = 2 };
+template <int kSet>
 static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict__ pack, int s, int t, float mulsF,
                                                 bool nm1) {
+    if (kSet == kB2BBBB) algo = kAlgoBBBB;
+    if (kSet == kB2Others && algo == kAlgoBBBB) return false;
     const SGV S = load_sgv(pack, s);
     const SGV T = load_sgv(pack, t);
     const float pt_betaMax = 7.0f;
@@ -963,7 +969,7 @@ static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict
     float alphaOutReg;
     int lIn, lOut;
     float dBetaROut2 = 0.f;
-    if (algo == kAlgoBBBB) {
+    if (kSet != kB2Others && algo == kAlgoBBBB) {
         // Tracklet.cc:1205-1538
         betaInRHmin = betaIn; betaInRHmax = betaIn;
         betaOut = -T.alphaup + dphi(OutUp, axis);
@@ -987,7 +993,7 @@ static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict
         alphaOutReg = T.dpc;
         lIn = 5;
         lOut = ec2s ? 11 : 5;
-    } else if (algo == kAlgoBBEE) {
+    } else if (kSet != kB2BBBB && algo == kAlgoBBEE) {
         // Tracklet.cc:1765-2016
         const float sdOut_alphaOut = T.alphaup;
         const float sdOut_alphaOut_min = phi_mpi_pi(T.dpminc - T.dpmin);
@@ -1053,7 +1059,7 @@ static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict
 // phase B in one call (phase B1, then phase B2 on its survivors)
 __device__ __forceinline__ bool tl_phaseB(int algo, const float* __restrict__ pack, int s, int t, float sdlCut, float mulsF,
                                           bool nm1) {
-    return tl_phaseB1(algo, pack, s, t, sdlCut) && tl_phaseB2(algo, pack, s, t, mulsF, nm1);
+    return tl_phaseB1(algo, pack, s, t, sdlCut) && tl_phaseB2<kB2All>(algo, pack, s, t, mulsF, nm1);
 }
 
 }  // namespace sdlg

@@ -997,11 +997,13 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const int4* 
     }
 }
 
-// Phase B2 on the phase-B2 list (front part, then back part); appends the tracklets.
+// Phase B2 on one part of the phase-B2 list (kSet kB2BBBB: the front, BBBB
+// entries; kB2Others: the back, BBEE and EEEE entries); appends the tracklets.
+template <int kSet>
 __global__ void __launch_bounds__(kEnumThreads) k_tl_b2(BatchDev b) {
     if (halted(b)) return;
     const int64_t nf = min((int64_t)b.n_pb[0], b.kept_cap);
-    const int64_t n = min(nf + (int64_t)b.n_pb[1], b.kept_cap);
+    const int64_t n = kSet == kB2BBBB ? nf : min((int64_t)b.n_pb[1], b.kept_cap - nf);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const bool nm1 = (b.flags & kFlagTLNm1) != 0;
     const int64_t nwarp = (int64_t)gridDim.x * (kEnumThreads / 32);
@@ -1010,11 +1012,11 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b2(BatchDev b) {
         bool pass = false;
         int s = 0, tt = 0;
         if (i < n) {
-            const int64_t k = i < nf ? i : b.kept_cap - 1 - (i - nf);
+            const int64_t k = kSet == kB2BBBB ? i : b.kept_cap - 1 - i;
             const int4 p = AT(b.pb, k, b.kept_cap);
             s = p.x;
             tt = p.y;
-            pass = tl_phaseB2(p.z, b.sgpack, s, tt, __int_as_float(p.w), nm1);
+            pass = tl_phaseB2<kSet>(p.z, b.sgpack, s, tt, __int_as_float(p.w), nm1);
         }
         append_rec(b, kTL, pass, s, tt, pass ? OG(b, kSG, s) : 0, nullptr);
     }
@@ -1430,8 +1432,9 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     cudaMemsetAsync(b.n_pb, 0, 2 * sizeof(unsigned long long), s);
     k_tl_b1<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, mlp ? b.kept : b.passa, mlp ? b.kept_muls : b.passa_muls,
                                                                  mlp ? b.n_kept2 : b.n_kept);
-    k_tl_b2<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
-    if (h) h->launches += mlp ? 3 : 2;
+    k_tl_b2<kB2BBBB><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
+    k_tl_b2<kB2Others><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
+    if (h) h->launches += mlp ? 4 : 3;
     if (h && h->timed) rec_event(h->enum_stop[kTL], s);
     k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kTL);
     scan_h(b, b.obj[kTL].mod_cnt, b.n_gm_dev, b.n_gm, s, h);
