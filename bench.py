@@ -405,14 +405,24 @@ def main():
                     "tl_kernel_ms": round(statistics.fmean(s_tl), 4)}
 
     # ---- roofline of the dominant kernel of the headline run -----------------
-    # k_tl_prefilter (the network over the phase-A survivor list): algorithmic
-    # bytes = each survivor entry read once (20 B) + each segment's feature
-    # record read once (64 B) + each kept entry written once (20 B); tensor
-    # work = the network's MMAs per scored candidate
+    # k_tl_enum_a (tracklet enumeration + the float cuts, a third of the step):
+    # algorithmic bytes = each segment's record as inner segment (112 B), its
+    # six outer-role fields (24 B) and its candidate offset (8 B) read once +
+    # each phase-A survivor's entry written once (20 B)
     hbm, tflops, src = peaks()
     pf = np.mean(np.array(pf_ms), axis=0)
     fc_mean, pf_mean, ex_mean = float(pf[0]), float(pf[1]), float(pf[2])
     n_sg = int(n_pruned[1])
+    en_bytes = (112 + 24 + 8) * n_sg + 20 * mstats["scored"]
+    en_achieved = en_bytes / (fc_mean * 1e-3) / 1e9
+    tr = ncu_traffic("tl_enum_traffic.json")
+    en_traffic = None
+    if tr and tr.get("traffic_per_algorithmic_byte"):
+        en_traffic = int(en_bytes * float(tr["traffic_per_algorithmic_byte"]))
+    # k_tl_prefilter (the network over the phase-A survivor list): algorithmic
+    # bytes = each survivor entry read once (20 B) + each segment's feature
+    # record read once (64 B) + each kept entry written once (20 B); tensor
+    # work = the network's MMAs per scored candidate
     alg_bytes = 20 * mstats["scored"] + 64 * n_sg + 20 * mstats["kept"]
     achieved = alg_bytes / (pf_mean * 1e-3) / 1e9
     tr = ncu_traffic("tl_prefilter_traffic.json")
@@ -420,15 +430,20 @@ def main():
     if tr and tr.get("traffic_per_algorithmic_byte"):
         traffic = int(alg_bytes * float(tr["traffic_per_algorithmic_byte"]))
     mma_tflops = mstats["scored"] * MLP_FLOPS_PER_CANDIDATE / (pf_mean * 1e-3) / 1e12
-    roofline = {"bound": "hbm", "achieved": round(achieved, 3), "peak": hbm, "unit": "GB/s",
-                "frac": round(achieved / hbm, 6), "traffic": traffic, "peak_source": src,
-                "kernel": "k_tl_prefilter (tensor-core pre-filter of the tracklet candidates through the float cuts)",
-                "kernel_ms": round(pf_mean, 3), "algorithmic_bytes": alg_bytes,
-                "enumeration_float_cuts_ms": round(fc_mean, 3), "double_cuts_ms": round(ex_mean, 3),
-                "tensor": {"achieved": round(mma_tflops, 2), "peak": tflops, "unit": "TFLOP/s",
-                           "frac": round(mma_tflops / tflops, 5), "flops_per_candidate": MLP_FLOPS_PER_CANDIDATE,
-                           "candidates": mstats["scored"]},
-                "note": "latency/FP64-bound candidate evaluation; HBM bytes are small by construction"}
+    roofline = {"bound": "hbm", "achieved": round(en_achieved, 3), "peak": hbm, "unit": "GB/s",
+                "frac": round(en_achieved / hbm, 6), "traffic": en_traffic, "peak_source": src,
+                "kernel": "k_tl_enum_a (tracklet candidate enumeration and the float cuts)",
+                "kernel_ms": round(fc_mean, 3), "algorithmic_bytes": en_bytes,
+                "note": "issue-bound candidate evaluation (profiles/tl_kernels_ncu.md); HBM bytes are small by construction",
+                "prefilter": {"kernel": "k_tl_prefilter (tensor-core pre-filter of the candidates through the float cuts)",
+                              "kernel_ms": round(pf_mean, 3), "algorithmic_bytes": alg_bytes,
+                              "achieved": round(achieved, 3), "peak": hbm, "unit": "GB/s",
+                              "frac": round(achieved / hbm, 6), "traffic": traffic,
+                              "tensor": {"achieved": round(mma_tflops, 2), "peak": tflops, "unit": "TFLOP/s",
+                                         "frac": round(mma_tflops / tflops, 5),
+                                         "flops_per_candidate": MLP_FLOPS_PER_CANDIDATE,
+                                         "candidates": mstats["scored"]}},
+                "double_cuts_ms": round(ex_mean, 3)}
 
     # ---- CPU baseline (rank 0) -----------------------------------------------
     cpu = None
