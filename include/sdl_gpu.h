@@ -157,7 +157,8 @@ int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3);
  * flag, and the first differing inputs and results as bit patterns.
  * Functions 16 (direction of a point by atan2f) and 17 (asinf) are the
  * tracklet cuts' single-precision approximations: "differs" there means
- * more than 2e-6 away from the exact value. */
+ * more than 2e-6 away from the exact value.  Functions 18 and 19 are tan(x)
+ * and tan(x) / x (the hits' tan of their asin angle). */
 int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64_t n, uint64_t seed, uint64_t* out8);
 
 /* Number of kernels one run of the chain launches (as last enqueued). */

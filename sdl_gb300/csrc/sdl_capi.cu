@@ -332,7 +332,7 @@ int ensure_buffers(sdlg_ctx* ctx) {
     float* fx; float* fy; float* fz; int32_t* fi; uint32_t* fd; int64_t* eo;
     AL(fx, H); AL(fy, H); AL(fz, H); AL(fi, H); AL(fd, H); AL(eo, ctx->n_ev + 1);
     b.in_x = fx; b.in_y = fy; b.in_z = fz; b.in_idx = fi; b.in_det = fd; b.ev_off = eo;
-    AL(b.hit_gm, H); AL(b.hit_rank, H); AL(b.mod_hit, n_gm + 1);
+    AL(b.hit_gm, H); AL(b.hit_rank, H); AL(b.hit_perm, H); AL(b.mod_hit, n_gm + 1);
     AL(b.hx, H); AL(b.hy, H); AL(b.hz, H); AL(b.hrt, H); AL(b.hphi, H); AL(b.hr3, H);
     AL(b.ha1, H); AL(b.htf, H); AL(b.htd, H); AL(b.ha3, H); AL(b.hidx, H); AL(b.hgm, H);
     AL(b.hsx, H); AL(b.hsy, H); AL(b.hsz, H);
@@ -994,7 +994,7 @@ int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3) {
 int64_t sdlg_last_launches(const sdlg_ctx* ctx) { return ctx ? ctx->launches_per_run : -1; }
 
 int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64_t n, uint64_t seed, uint64_t* out8) {
-    if (!ctx || !out8 || n < 0 || fn < 0 || fn > 17) return SDLG_ERR_ARG;
+    if (!ctx || !out8 || n < 0 || fn < 0 || fn > 19) return SDLG_ERR_ARG;
     cudaSetDevice(ctx->device);
     unsigned long long* d = nullptr;
     CK(cudaMalloc(&d, 8 * sizeof(unsigned long long)));

@@ -104,6 +104,27 @@ __device__ __forceinline__ bool f_sincos_fast(float x, int shift, float& r) {
     ffm::ff v;
     return ffm::sincos_ff(x, shift, v) && ffm::round_unique_rel(v, r);
 }
+// (float)tan((double)x) and (float)(tan((double)x) / (double)x), the hits'
+// tan of their asin angle (0 < x <= asin(0.95)): sine over cosine in
+// float-float (relative error below 2^-41), answered when the rounding is
+// unique; the double evaluation otherwise
+static __device__ __noinline__ float f_tan_over_d(float x) { return (float)(tan((double)x) / (double)x); }
+__device__ __forceinline__ bool f_tan_fast(float x, bool over_x, float& r) {
+    if (!(x > 0x1p-30f && x < 1.5f)) return false;
+    ffm::ff s, c;
+    if (!ffm::sincos_ff(x, 0, s) || !ffm::sincos_ff(x, 1, c)) return false;
+    ffm::ff t = ffm::div(s, c);
+    if (over_x) t = ffm::div(t, ffm::ff{x, 0.f});
+    return ffm::round_unique_rel(t, r);
+}
+static __device__ __noinline__ float f_tan_ff(float x) {
+    float r;
+    return f_tan_fast(x, false, r) ? r : f_tan(x);
+}
+static __device__ __noinline__ float f_tan_over(float x) {
+    float r;
+    return f_tan_fast(x, true, r) ? r : f_tan_over_d(x);
+}
 static __device__ __noinline__ float f_sin(float x) {
     float r;
     return f_sincos_fast(x, 0, r) ? r : f_sin_d(x);

@@ -247,20 +247,31 @@ __global__ void k_hit_map(BatchDev b) {
     }
 }
 
-__global__ void k_hit_scatter(BatchDev b) {
+// sorted position of every input hit in a known module -> hit_perm
+__global__ void k_hit_perm(BatchDev b) {
     const int64_t n = *b.n_hit;
     for (int64_t h = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; h < n; h += (int64_t)gridDim.x * blockDim.x) {
         const int gm = AT(b.hit_gm, h, H(b));
         if (gm < 0) continue;
-        const int64_t pos = AT(b.mod_hit, gm, NG1(b)) + AT(b.hit_rank, h, H(b));
+        AT(b.hit_perm, AT(b.mod_hit, gm, NG1(b)) + AT(b.hit_rank, h, H(b)), H(b)) = (int)h;
+    }
+}
+
+// the sorted hit arrays, one thread per sorted position (coalesced writes;
+// the input hit is gathered through hit_perm)
+__global__ void k_hit_scatter(BatchDev b) {
+    const int64_t n = min(AT(b.mod_hit, b.n_gm, NG1(b)), *b.n_hit);  // hits in known modules
+    for (int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; pos < n; pos += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t h = AT(b.hit_perm, pos, H(b));
+        const int gm = AT(b.hit_gm, h, H(b));
         const float x = AT(b.in_x, h, H(b)), y = AT(b.in_y, h, H(b)), z = AT(b.in_z, h, H(b));
         const P3 p = mk(x, y, z);
         AT(b.hx, pos, H(b)) = x; AT(b.hy, pos, H(b)) = y; AT(b.hz, pos, H(b)) = z;
         AT(b.hrt, pos, H(b)) = p.rt; AT(b.hphi, pos, H(b)) = p.phi; AT(b.hr3, pos, H(b)) = p.r3;
         const float a1 = f_asin(fmin_ref(p.rt * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
         AT(b.ha1, pos, H(b)) = a1;
-        AT(b.htf, pos, H(b)) = f_tan(a1);
-        AT(b.htd, pos, H(b)) = (float)(tan((double)a1) / (double)a1);
+        AT(b.htf, pos, H(b)) = f_tan_ff(a1);
+        AT(b.htd, pos, H(b)) = f_tan_over(a1);
         AT(b.ha3, pos, H(b)) = f_asin(fmin_ref(p.rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax));
         AT(b.hidx, pos, H(b)) = AT(b.in_idx, h, H(b));
         AT(b.hgm, pos, H(b)) = gm;
@@ -1380,8 +1391,9 @@ void launch_ingest(const BatchDev& b, cudaStream_t s, Hooks* h) {
     const unsigned g = grid_for(b.n_hit_cap, 256, b.n_sm * 16);
     k_hit_map<<<g, 256, 0, s>>>(b);
     scan_h(b, b.mod_hit, b.n_gm_dev, b.n_gm, s, h);
+    k_hit_perm<<<g, 256, 0, s>>>(b);
     k_hit_scatter<<<g, 256, 0, s>>>(b);
-    if (h) h->launches += 2;
+    if (h) h->launches += 3;
 }
 
 void launch_md(const BatchDev& b, cudaStream_t s, Hooks* h) {
@@ -1562,12 +1574,14 @@ __global__ void k_math_check(int fn, int exhaustive, unsigned long long start, l
             case 15: ok = muls_fast(a, b, false, f); if (ok) ref = muls_d(a, b, false); break;
             case 16: ok = phi_approx(a, b, f); if (ok) ref = phi_of(a, b); break;
             case 17: ok = fabsf(a) <= kSinAlphaMax; if (ok) { f = asinf(a); ref = f_asin(a); } break;
+            case 18: ok = f_tan_fast(a, false, f); if (ok) ref = f_tan(a); break;
+            case 19: ok = f_tan_fast(a, true, f); if (ok) ref = f_tan_over_d(a); break;
             default: break;
         }
         // functions 16 and 17 are the approximations of phase B1: within 2e-6
         // of the exact value (directions compared modulo 2 pi); the others
         // must match the double evaluation bit for bit
-        const bool bad = fn >= 16 ? ok && !(fabsf(fn == 16 ? wrap_approx(f - ref) : f - ref) <= 2e-6f)
+        const bool bad = (fn == 16 || fn == 17) ? ok && !(fabsf(fn == 16 ? wrap_approx(f - ref) : f - ref) <= 2e-6f)
                                   : ok && __float_as_uint(f) != __float_as_uint(ref) && !(isnan(f) && isnan(ref));
         const unsigned m_ok = __ballot_sync(__activemask(), ok);
         const unsigned m_bad = __ballot_sync(__activemask(), bad);

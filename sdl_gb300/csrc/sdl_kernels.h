@@ -22,6 +22,7 @@ struct BatchDev {
     // ingest
     int32_t* hit_gm;
     int32_t* hit_rank;
+    int32_t* hit_perm;       // sorted position -> input hit
     int64_t* mod_hit;        // n_gm + 1: counts -> offsets
     // sorted hits (SoA)
     float *hx, *hy, *hz, *hrt, *hphi, *hr3, *ha1, *htf, *htd, *ha3;

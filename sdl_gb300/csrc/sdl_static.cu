@@ -45,7 +45,7 @@ constexpr int64_t kModCnt = kCandMD + kMaxModules + 1;          // kMaxModules +
 constexpr int64_t kScan = kModCnt + kMaxModules + 1;            // kScanTmp
 constexpr int64_t kWords64 = kScan + kScanTmp;
 // 4-byte regions follow the 8-byte ones
-constexpr int64_t kHitArrays = 17;                              // hit_gm, hit_rank and 15 sorted arrays
+constexpr int64_t kHitArrays = 18;                              // hit_gm, hit_rank, hit_perm and 15 sorted arrays
 constexpr int64_t kObjWords = 3 + 4;                            // i, j, g, f[4]
 constexpr int64_t kRecWords = 4 + 4;                            // i, j, g, rank, f[4]
 constexpr int64_t kWords32Raw = kHitArrays * kMaxHits + (kObjWords + kRecWords) * kMaxMD + 110 + 1;
@@ -162,6 +162,7 @@ extern "C" int sdlg_mini_doublets_static(sdlg_ctx* ctx, int64_t n_hits, const fl
     int64_t o = 0;
     b.hit_gm = w32 + o; o += H;
     b.hit_rank = w32 + o; o += H;
+    b.hit_perm = w32 + o; o += H;
     float** hf[13] = {&b.hx, &b.hy, &b.hz, &b.hrt, &b.hphi, &b.hr3, &b.ha1, &b.htf, &b.htd, &b.ha3, &b.hsx, &b.hsy, &b.hsz};
     for (float** f : hf) { *f = f32 + o; o += H; }
     b.hidx = w32 + o; o += H;

@@ -9,7 +9,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 (ASIN, ATAN2, PHI, ADD_SQRT, ADD_SQRT3, PHI_MPI_PI, ADD_PI, PT, MULS, QSQ, SIN, COS, ATAN, HYPOT, T15, MULS1,
- PHI_APPROX, ASIN_APPROX) = range(18)
+ PHI_APPROX, ASIN_APPROX, TAN, TAN_OVER) = range(20)
 
 
 @pytest.fixture(scope="module")
@@ -24,17 +24,20 @@ def _bits(x):
     return struct.unpack("<I", struct.pack("<f", x))[0]
 
 
-@pytest.mark.parametrize("fn,lo,hi,min_answered", [
-    (ASIN, 2.0 ** -30, 0.95, 0.999),        # every float of the std::asin arguments
-    (PHI_MPI_PI, 3.1415927, 9.0, 0.999),    # every float the loop's first step handles
-    (ADD_PI, 2.0 ** -20, 3.1415925, 0.99),  # M_PI + atan2 result
-    (SIN, 2.0 ** -30, 8.0, 0.999),          # every float of the angles the strip shift uses
-    (COS, 2.0 ** -30, 8.0, 0.999),
-    (ATAN, 2.0 ** -40, 2.0 ** 40, 0.999),
+@pytest.mark.parametrize("fn,lo,hi,min_answered,signs", [
+    (ASIN, 2.0 ** -30, 0.95, 0.999, 2),        # every float of the std::asin arguments
+    (PHI_MPI_PI, 3.1415927, 9.0, 0.999, 2),    # every float the loop's first step handles
+    (ADD_PI, 2.0 ** -20, 3.1415925, 0.99, 2),  # M_PI + atan2 result
+    (SIN, 2.0 ** -30, 8.0, 0.999, 2),          # every float of the angles the strip shift uses
+    (COS, 2.0 ** -30, 8.0, 0.999, 2),
+    (ATAN, 2.0 ** -40, 2.0 ** 40, 0.999, 2),
+    # every float of the hits' asin angles asin(min(rt k, 0.95)) for rt above 0.2 cm
+    (TAN, 2.0 ** -10, 1.2533, 0.999, 1),
+    (TAN_OVER, 2.0 ** -10, 1.2533, 0.999, 1),
 ])
-def test_unary_exhaustive(gpu, fn, lo, hi, min_answered):
+def test_unary_exhaustive(gpu, fn, lo, hi, min_answered, signs):
     n = _bits(hi) - _bits(lo) + 1
-    for sign in (0, 0x80000000):
+    for sign in (0, 0x80000000)[:signs]:
         r = gpu.math_check(fn, n, start=sign | _bits(lo), exhaustive=True)
         assert r["mismatches"] == 0, r
         assert r["answered"] >= min_answered * n, (r["answered"], n)
