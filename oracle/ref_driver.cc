@@ -56,7 +56,7 @@ double now() {
 
 int main(int argc, char** argv) {
     if (argc < 6) {
-        std::fprintf(stderr, "usage: %s tilted endcap map hits.bin out.bin [map|layer]\n", argv[0]);
+        std::fprintf(stderr, "usage: %s tilted endcap map hits.bin out.bin [map|layer|nav|tctl|tctp]\n", argv[0]);
         return 2;
     }
     std::string mode = argc > 6 ? argv[6] : "map";
@@ -88,13 +88,24 @@ int main(int argc, char** argv) {
     double t0 = now();
     ev.createMiniDoublets();
     t[0] = now() - t0; t0 = now();
-    if (mode == "layer") ev.createSegments(); else ev.createSegmentsWithModuleMap();
+    // mode tokens: "layer" (createSegments + createTracklets), "nav"
+    // (createTrackletsViaNavigation), "tctl" / "tctp" (createTrackCandidatesFrom
+    // Tracklets / Triplets); the module-map variants otherwise
+    const bool layer = mode.find("layer") != std::string::npos;
+    const bool nav = mode.find("nav") != std::string::npos;
+    const bool tctl = mode.find("tctl") != std::string::npos;
+    const bool tctp = mode.find("tctp") != std::string::npos;
+    if (layer) ev.createSegments(); else ev.createSegmentsWithModuleMap();
     t[1] = now() - t0; t0 = now();
-    if (mode == "layer") ev.createTracklets(); else ev.createTrackletsWithModuleMap();
+    if (layer) ev.createTracklets();
+    else if (nav) ev.createTrackletsViaNavigation();
+    else ev.createTrackletsWithModuleMap();
     t[2] = now() - t0; t0 = now();
     ev.createTriplets();
     t[3] = now() - t0; t0 = now();
-    ev.createTrackCandidates();
+    if (tctp) ev.createTrackCandidatesFromTriplets();
+    else if (tctl) ev.createTrackCandidatesFromTracklets();
+    else ev.createTrackCandidates();
     t[4] = now() - t0;
 
     std::vector<int32_t> md, sg, tl, tp, tc;

@@ -229,6 +229,7 @@ struct Event {
     std::vector<MD> mds;
     std::vector<SG> sgs;
     std::vector<Pair> tls, tps, tcs;
+    std::vector<Pair> tcsTP;  // track candidates built from two triplets (createTrackCandidatesFromTriplets)
     std::vector<int> tcLayer;
     uint32_t cnt[5][2][11];
     int tlMode = 0;  // 0 default, 1 DefaultNm1
@@ -1017,6 +1018,28 @@ struct Event {
         }
     }
 
+    // Event.cc:694-751: inner segment x segments leaving its outer MD x
+    // segments leaving their outer MD (MiniDoublet.cc:40-58: every segment is
+    // listed at its inner MD as outward); counted and stored at the inner
+    // segment's lower module
+    void create_tls_nav(int algo) {
+        std::vector<std::vector<int>> outward(mds.size());
+        for (size_t s = 0; s < sgs.size(); ++s) outward[sgs[s].imd].push_back((int)s);
+        const std::vector<int> lower = lowerMods;
+        for (int m1 : lower) {
+            const ModInfo m1i = mods[m1];
+            for (int si : modSGs[m1])
+                for (int sc : outward[sgs[si].omd])
+                    for (int so : outward[sgs[sc].omd]) {
+                        count(2, 0, m1i);
+                        if (run_tl(si, so, algo)) {
+                            count(2, 1, m1i);
+                            add_tl(si, so, true);
+                        }
+                    }
+        }
+    }
+
     // Event.cc:599-609, 755-790 and Layer.cc:19-24
     void create_tls_layer(int algo) {
         static const int pairs[3][2] = {{1, 3}, {2, 4}, {3, 5}};
@@ -1103,6 +1126,68 @@ struct Event {
         }
     }
 
+    // Event.cc:984-1062 with TrackCandidate.cc:143-226: every module's
+    // tracklets x the tracklets of the modules connected to the module of the
+    // inner segment's outer MD (repeated connections repeat them); pass iff
+    // the inner tracklet's outer segment idx-matches the outer tracklet's
+    // inner segment
+    void create_tcs_from_tls(int algo) {
+        const std::vector<int> lower = lowerMods;
+        for (int m1 : lower) {
+            const ModInfo m1i = mods[m1];
+            for (int a : modTLs[m1]) {
+                const ModInfo& m2 = mods[mds[sgs[tls[a].in].omd].mod];
+                for (uint32_t d3 : geo.connected(m2.detid)) {
+                    if (!has(d3)) continue;
+                    for (int b : modTLs[modIndex.at(d3)]) {
+                        count(4, 0, m1i);
+                        if (algo == 1 || sg_match(tls[a].out, tls[b].in)) {
+                            count(4, 1, m1i);
+                            tcs.push_back({a, b});
+                        }
+                    }
+                }
+            }
+        }
+    }
+
+    // Event.cc:874-982: every module's triplets x the triplets of the modules
+    // connected to the module of the triplet's outermost MD; pass iff the
+    // segment from that MD to the outer triplet's innermost MD passes the
+    // segment algorithm and the tracklet (that segment, the outer triplet's
+    // outer segment) passes the tracklet algorithm.  The trial segment is not
+    // kept.
+    void create_tcs_from_tps(int algo) {
+        const std::vector<int> lower = lowerMods;
+        for (int m1 : lower) {
+            const ModInfo m1i = mods[m1];
+            for (int a : modTPs[m1]) {
+                const int mdA = sgs[tps[a].out].omd;
+                const ModInfo& mo = mods[mds[mdA].mod];
+                for (uint32_t d3 : geo.connected(mo.detid)) {
+                    if (!has(d3)) continue;
+                    for (int b : modTPs[modIndex.at(d3)]) {
+                        count(4, 0, m1i);
+                        SG trial;
+                        if (!run_sg(mdA, sgs[tps[b].in].imd, 0, trial)) continue;
+                        // run_tl reads segments by index; the tracklet algorithm
+                        // is the default one here (Event.cc:947-951)
+                        sgs.push_back(trial);
+                        const int keep = tlMode;
+                        tlMode = 0;
+                        const bool pass = run_tl((int)sgs.size() - 1, tps[b].out, 0);
+                        tlMode = keep;
+                        sgs.pop_back();
+                        if (!pass) continue;
+                        (void)algo;
+                        count(4, 1, m1i);
+                        tcsTP.push_back({a, b});
+                    }
+                }
+            }
+        }
+    }
+
     // ---------------------------------------------------------- output
     void push_md(std::vector<int32_t>& v, int m) const { v.push_back(hits[mds[m].lo].idx); v.push_back(hits[mds[m].up].idx); }
     void push_sg(std::vector<int32_t>& v, int s) const { push_md(v, sgs[s].imd); push_md(v, sgs[s].omd); }
@@ -1114,6 +1199,7 @@ struct Event {
         for (auto& p : tls) push_tl(r.t[2], p);
         for (auto& p : tps) push_tl(r.t[3], p);
         for (auto& p : tcs) { push_tl(r.t[4], tls[p.in]); push_tl(r.t[4], tls[p.out]); }
+        for (auto& p : tcsTP) { push_tl(r.t[4], tps[p.in]); push_tl(r.t[4], tps[p.out]); }
         int k = 0;
         for (int s = 0; s < 5; ++s)
             for (int o = 0; o < 2; ++o)
@@ -1143,7 +1229,9 @@ Result* run_event(const Geo& g, int64_t n, const float* x, const float* y, const
     }
     if (stop_after >= 2) {
         t0 = now();
-        if (mode & 2) ev.create_tls_layer(0); else ev.create_tls_map(0);
+        if (mode & 2) ev.create_tls_layer(0);
+        else if (mode & 32) ev.create_tls_nav(0);
+        else ev.create_tls_map(0);
         r->seconds[2] = now() - t0;
     }
     if (stop_after >= 3) {
@@ -1153,7 +1241,9 @@ Result* run_event(const Geo& g, int64_t n, const float* x, const float* y, const
     }
     if (stop_after >= 4) {
         t0 = now();
-        ev.create_tcs(0);
+        if (mode & 128) ev.create_tcs_from_tps(0);
+        else if (mode & 64) ev.create_tcs_from_tls(0);
+        else ev.create_tcs(0);
         r->seconds[4] = now() - t0;
     }
     ev.emit(*r);

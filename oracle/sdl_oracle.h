@@ -34,7 +34,10 @@ void sdlo_geometry_free(void* geo);
 
 /* mode bit 0: layer-pair segments (createSegments) instead of module map;
  * bit 1: layer-pair tracklets (createTracklets) instead of module map;
- * bit 2: DefaultNm1 tracklet algorithm (no deltaBeta rejection).
+ * bit 2: DefaultNm1 tracklet algorithm (no deltaBeta rejection);
+ * bit 5 (32): tracklets via navigation (createTrackletsViaNavigation);
+ * bit 6 (64): track candidates from tracklets (createTrackCandidatesFromTracklets);
+ * bit 7 (128): track candidates from triplets (createTrackCandidatesFromTriplets).
  * stop_after: last stage to run (0 MD .. 4 TC). */
 void* sdlo_run(const void* geo, int64_t n, const float* x, const float* y, const float* z,
                const int32_t* idx, const uint32_t* detid, int mode, int stop_after);

@@ -35,6 +35,10 @@ CASES = [
     ("pu50_s1", "pu", 1, 50, "map", False),
     ("pu200_s0", "pu", 0, 200, "map", False),
     ("pu200_s1", "pu", 1, 200, "map", False),
+    # createTrackletsViaNavigation, createTrackCandidatesFromTracklets / FromTriplets
+    *[("flat_s0_" + m, "barrel_flat", 0, None, m, True) for m in ("nav", "tctl", "tctp")],
+    *[("pu20_s0_" + m, "pu", 0, 20, m, True) for m in ("nav", "tctl", "tctp")],
+    *[("pu50_s1_" + m, "pu", 1, 50, m, False) for m in ("nav", "tctl", "tctp")],
 ]
 
 

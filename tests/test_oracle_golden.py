@@ -5,7 +5,8 @@ import pytest
 
 from conftest import golden_meta, golden_names, golden_tuples, regenerate
 
-MODE = {"map": 0, "layer": 3}
+# fixture mode -> oracle mode bits (the chain's flag bits)
+MODE = {"map": 0, "layer": 3, "nav": 32, "tctl": 64, "tctp": 128}
 
 
 @pytest.mark.parametrize("name", golden_names())
