@@ -117,8 +117,30 @@ class Event {
         tl_flags_ = SDLG_FLAG_TL_LAYERS | (algo == DefaultNm1_TLAlgo ? SDLG_FLAG_TL_NM1 : 0);
         run(SDLG_STAGE_TL);
     }
+    // Event.cc:694-751: tracklets along the segments that share mini-doublets
+    void createTrackletsViaNavigation(TLAlgo algo = Default_TLAlgo) {
+        require(algo == Default_TLAlgo || algo == DefaultNm1_TLAlgo);
+        tl_flags_ = SDLG_FLAG_TL_NAV | (algo == DefaultNm1_TLAlgo ? SDLG_FLAG_TL_NM1 : 0);
+        run(SDLG_STAGE_TL);
+    }
     void createTriplets(TPAlgo algo = Default_TPAlgo) { require(algo == Default_TPAlgo); run(SDLG_STAGE_TP); }
-    void createTrackCandidates(TCAlgo algo = Default_TCAlgo) { require(algo == Default_TCAlgo); run(SDLG_STAGE_TC); }
+    void createTrackCandidates(TCAlgo algo = Default_TCAlgo) {
+        require(algo == Default_TCAlgo);
+        tc_flags_ = 0;
+        run(SDLG_STAGE_TC);
+    }
+    // Event.cc:984-1062
+    void createTrackCandidatesFromTracklets(TCAlgo algo = Default_TCAlgo) {
+        require(algo == Default_TCAlgo);
+        tc_flags_ = SDLG_FLAG_TC_FROM_TL;
+        run(SDLG_STAGE_TC);
+    }
+    // Event.cc:874-982
+    void createTrackCandidatesFromTriplets(TCAlgo algo = Default_TCAlgo) {
+        require(algo == Default_TCAlgo);
+        tc_flags_ = SDLG_FLAG_TC_FROM_TP;
+        run(SDLG_STAGE_TC);
+    }
 
     // Event.h:302-311
     unsigned int getNumberOfHits() const { return (unsigned int)x_.size(); }
@@ -178,7 +200,7 @@ class Event {
             dirty_ = false;
         }
         // each call re-runs the chain up to `stage` with the variants chosen so far
-        check(sdlg_run(ctx_, stage, sg_flags_ | tl_flags_), "run");
+        check(sdlg_run(ctx_, stage, sg_flags_ | tl_flags_ | tc_flags_), "run");
         ran_ = stage;
         stage_ = stage;
     }
@@ -210,7 +232,7 @@ class Event {
     std::vector<int32_t> idx_;
     std::vector<uint32_t> det_;
     bool dirty_ = false;
-    int sg_flags_ = 0, tl_flags_ = 0;
+    int sg_flags_ = 0, tl_flags_ = 0, tc_flags_ = 0;
     int ran_ = -1;
     int stage_ = -1;
 };

@@ -57,6 +57,12 @@ extern "C" {
 #define SDLG_FLAG_TL_NM1 4   /* tracklets with DefaultNm1_TLAlgo (Algo.h:23-28) */
 #define SDLG_FLAG_NO_GRAPH 8 /* launch stage by stage instead of replaying a CUDA graph */
 #define SDLG_FLAG_MLP 16     /* learned pre-filter ahead of the tracklet cuts (no counterpart in the reference) */
+#define SDLG_FLAG_TL_NAV 32  /* tracklets via navigation: Event::createTrackletsViaNavigation (Event.cc:694-751):
+                                inner segment x segments leaving its outer MD x segments leaving theirs */
+#define SDLG_FLAG_TC_FROM_TL 64  /* track candidates: Event::createTrackCandidatesFromTracklets (Event.cc:984-1062) */
+#define SDLG_FLAG_TC_FROM_TP 128 /* track candidates from two triplets and a trial segment between them:
+                                    Event::createTrackCandidatesFromTriplets (Event.cc:874-982); the objects
+                                    of stage 4 are then pairs of triplets (hit tuples of width 16 as before) */
 
 typedef struct sdlg_ctx sdlg_ctx;
 

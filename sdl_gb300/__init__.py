@@ -32,6 +32,9 @@ FLAG_TL_LAYERS = 2   # Event::createTracklets (layer pairs) instead of createTra
 FLAG_TL_NM1 = 4
 FLAG_NO_GRAPH = 8
 FLAG_MLP = 16        # learned pre-filter ahead of the tracklet cuts
+FLAG_TL_NAV = 32     # Event::createTrackletsViaNavigation instead of createTrackletsWithModuleMap
+FLAG_TC_FROM_TL = 64   # Event::createTrackCandidatesFromTracklets instead of createTrackCandidates
+FLAG_TC_FROM_TP = 128  # Event::createTrackCandidatesFromTriplets instead of createTrackCandidates
 MLP_FEATURES = 12
 MLP_PARAMS = 5057
 

@@ -349,7 +349,7 @@ int ensure_buffers(sdlg_ctx* ctx) {
     b.cand_cap[kSG] = ctx->cap_obj[kMD];
     b.cand_cap[kTL] = ctx->cap_obj[kSG];
     b.cand_cap[kTP] = ctx->cap_obj[kSG];
-    b.cand_cap[kTC] = ctx->cap_obj[kTL];
+    b.cand_cap[kTC] = std::max(ctx->cap_obj[kTL], ctx->cap_obj[kTP]);  // tracklets, or triplets (SDLG_FLAG_TC_FROM_TP)
     for (int s = 0; s < kNumStages; ++s) AL(b.cand[s], b.cand_cap[s] + 1);
     AL(b.conn_pref, std::max<int64_t>(1, ctx->n_ev * (int64_t)ctx->conn_idx.size()));
     AL(b.conn_sum, n_gm);

@@ -662,6 +662,19 @@ __device__ __forceinline__ SGV load_sgv(const float* __restrict__ pack, int64_t 
     return v;
 }
 
+// the same from a record held in registers or local memory
+__device__ __forceinline__ SGV sgv_from(const float* p) {
+    SGV v;
+    v.lx = p[PK_LX]; v.ly = p[PK_LY]; v.lz = p[PK_LZ]; v.lrt = p[PK_LRT];
+    v.lphi = p[PK_LPHI]; v.lr3 = p[PK_LR3]; v.la1 = p[PK_LA1]; v.ltd = p[PK_LTD];
+    v.la3 = p[PK_LA3]; v.lr3z = p[PK_LR3Z]; v.ux = p[PK_UX]; v.uy = p[PK_UY];
+    v.uz = p[PK_UZ]; v.urt = p[PK_URT]; v.uphi = p[PK_UPHI]; v.ur3 = p[PK_UR3];
+    v.dpc = p[PK_DPC]; v.dpmin = p[PK_DPMIN]; v.dpmax = p[PK_DPMAX]; v.dpminc = p[PK_DPMINC];
+    v.dpmaxc = p[PK_DPMAXC]; v.rtseg = p[PK_RTSEG]; v.alphaup = p[PK_ALPHAUP]; v.dphilu = p[PK_DPHILU];
+    v.ex = p[PK_EX]; v.ey = p[PK_EY]; v.flags = __float_as_uint(p[PK_FLAGS]);
+    return v;
+}
+
 // Features of a tracklet candidate for the learned pre-filter (float
 // arithmetic only, no counterpart in the reference): anchor radii and z of
 // the innermost and outermost mini-doublets, the azimuthal opening between
@@ -923,9 +936,7 @@ __device__ __forceinline__ int clear_within(float v, float cut) {
 // ---- phase B1: the mid-point direction cut and the betaIn cut
 // (Tracklet.cc:1139-1222 BBBB, 1765-1819 BBEE, 2258-2292 EEEE; EEEE has no
 // betaIn cut).  Its code is the same for the three algorithms.
-static __device__ __noinline__ bool tl_phaseB1(int algo, const float* __restrict__ pack, int s, int t, float sdlCut) {
-    const SGV S = load_sgv(pack, s);
-    const SGV T = load_sgv(pack, t);
+__device__ __forceinline__ bool tl_phaseB1_sgv(int algo, const SGV& S, const SGV& T, float sdlCut) {
     // cut #5: dphi(midpoint(InLo, OutLo), OutLo - InLo) (the same float
     // operations as midpoint() and sub())
     float mx = 0.f, my = 0.f;
@@ -962,6 +973,9 @@ static __device__ __noinline__ bool tl_phaseB1(int algo, const float* __restrict
     }
     return cb != 0;
 }
+static __device__ __noinline__ bool tl_phaseB1(int algo, const float* __restrict__ pack, int s, int t, float sdlCut) {
+    return tl_phaseB1_sgv(algo, load_sgv(pack, s), load_sgv(pack, t), sdlCut);
+}
 
 // ---- phase B2: betaIn, betaOut, the deltaBeta iterations, the betaOut cut
 // and the deltaBeta cut, on the candidates through phase B1 (exact values
@@ -970,12 +984,9 @@ static __device__ __noinline__ bool tl_phaseB1(int algo, const float* __restrict
 // keeps only that code resident.
 enum : int { kB2All = 0, kB2BBBB = 1, kB2Others = 2 };
 template <int kSet>
-static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict__ pack, int s, int t, float mulsF,
-                                                bool nm1) {
+__device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV& T, float mulsF, bool nm1) {
     if (kSet == kB2BBBB) algo = kAlgoBBBB;
     if (kSet == kB2Others && algo == kAlgoBBBB) return false;
-    const SGV S = load_sgv(pack, s);
-    const SGV T = load_sgv(pack, t);
     const float pt_betaMax = 7.0f;
     const P3 InLo = S.lo(), InUp = S.up(), OutLo = T.lo(), OutUp = T.up();
     const P3 axis = sub(OutUp, InLo);
@@ -1075,6 +1086,11 @@ static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict
     const float dBetaCut2 = dbeta_cut2(dBetaRes, dBetaMuls, dBetaLum2, dBetaROut2, betaInRHmin, betaInRHmax, betaOutRHmin, betaOutRHmax);
     const float dBeta = betaIn - betaOut;
     return (dBeta * dBeta <= dBetaCut2) || nm1;
+}
+template <int kSet>
+static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict__ pack, int s, int t, float mulsF,
+                                                bool nm1) {
+    return tl_phaseB2_sgv<kSet>(algo, load_sgv(pack, s), load_sgv(pack, t), mulsF, nm1);
 }
 
 // phase B in one call (phase B1, then phase B2 on its survivors)

@@ -595,15 +595,18 @@ struct TPStage {
     __device__ static int group_of(const BatchDev& b, int s) { return OG(b, kSG, s); }
 };
 
-// track candidates (Event.cc:823-872 via TrackCandidate.cc:161): candidate q
-// of inner tracklet t1 is the q-th tracklet whose inner segment starts at the
-// inner mini-doublet of t1's outer segment; it matches when that segment's
+// track candidates (Event.cc:823-872, and 984-1062 for
+// createTrackCandidatesFromTracklets, via TrackCandidate.cc:161): candidate q
+// of inner tracklet t1 is the (q mod n)-th of the n tracklets whose inner
+// segment starts at the inner mini-doublet of t1's outer segment (repeated
+// connections repeat them, k_tc_count_tl); it matches when that segment's
 // outer mini-doublet is the same too
 struct TCStage {
     static constexpr int kSt = kTC;
     __device__ static bool eval(const BatchDev& b, int t1, int64_t q, int& oi, int& oj, float* fv) {
         const int sB = OJ(b, kTL, t1);
-        const int t2 = join_obj(b, OI(b, kSG, sB), q);
+        const int mB = OI(b, kSG, sB);
+        const int t2 = join_obj(b, mB, q % join_n(b, mB));  // n > 0 when t1 has candidates
         const int sC = OI(b, kTL, t2);
         oi = t1; oj = t2;
         (void)fv;
@@ -619,7 +622,9 @@ __device__ __forceinline__ int64_t n_inner(const BatchDev& b, int st) {
         case kSG: return min(OFF(b, kMD, b.n_gm), b.obj[kMD].cap);
         case kTL:
         case kTP: return min(OFF(b, kSG, b.n_gm), b.obj[kSG].cap);
-        default: return min(OFF(b, kTL, b.n_gm), b.obj[kTL].cap);
+        default:  // track candidates: tracklets, or triplets (createTrackCandidatesFromTriplets)
+            return (b.flags & kFlagTCFromTP) ? min(OFF(b, kTP, b.n_gm), b.obj[kTP].cap)
+                                             : min(OFF(b, kTL, b.n_gm), b.obj[kTL].cap);
     }
 }
 
@@ -732,42 +737,52 @@ __device__ __forceinline__ void append_rec(const BatchDev& b, int st, bool pass,
 // One packed record per segment for the tracklet stage (the anchors of both
 // mini-doublets, the segment's angles and the per-segment sub-expressions of
 // Tracklet.cc that depend on one segment only).
+// the packed record of the segment from mini-doublet im to mini-doublet om
+// with the segment algorithm's six values f6 (dPhi, dPhiMin, dPhiMax,
+// dPhiChange, dPhiMinChange, dPhiMaxChange)
+__device__ __forceinline__ void sg_pack_record(const BatchDev& b, int im, int om, const float* f6, float* v) {
+    const int n_mod = b.geo.n_mod;
+    const ModDev& ilm = MOD(b, OG(b, kMD, im) % n_mod);
+    const ModDev& olm = MOD(b, OG(b, kMD, om) % n_mod);
+    const int la = md_anchor(ilm, OI(b, kMD, im), OJ(b, kMD, im));
+    const int ua = md_anchor(olm, OI(b, kMD, om), OJ(b, kMD, om));
+    const P3 lo = hit(b, la), up = hit(b, ua);
+    const ModDev& lam = MOD(b, AT(b.hgm, la, H(b)) % n_mod);
+    const ModDev& uam = MOD(b, AT(b.hgm, ua, H(b)) % n_mod);
+    uint32_t fl = 0;
+    fl |= lam.subdet == kBarrel ? F_LO_B : 0u;
+    fl |= lam.subdet == kEndcap ? F_LO_E : 0u;
+    fl |= lam.type == kPS ? F_LO_PS : 0u;
+    fl |= uam.subdet == kBarrel ? F_UP_B : 0u;
+    fl |= uam.subdet == kEndcap ? F_UP_E : 0u;
+    fl |= uam.type == kPS ? F_UP_PS : 0u;
+    fl |= uam.type == kTwoS ? F_UP_2S : 0u;
+    v[PK_LX] = lo.x; v[PK_LY] = lo.y; v[PK_LZ] = lo.z; v[PK_LRT] = lo.rt;
+    v[PK_LPHI] = lo.phi; v[PK_LR3] = lo.r3; v[PK_LA1] = AT(b.ha1, la, H(b)); v[PK_LTD] = AT(b.htd, la, H(b));
+    v[PK_LA3] = AT(b.ha3, la, H(b));
+    v[PK_LR3Z] = __fsqrt_rn(lo.z * lo.z + lo.rt * lo.rt);
+    v[PK_UX] = up.x; v[PK_UY] = up.y; v[PK_UZ] = up.z; v[PK_URT] = up.rt; v[PK_UPHI] = up.phi; v[PK_UR3] = up.r3;
+    v[PK_DPC] = f6[3]; v[PK_DPMIN] = f6[1]; v[PK_DPMAX] = f6[2];
+    v[PK_DPMINC] = f6[4]; v[PK_DPMAXC] = f6[5];
+    v[PK_RTSEG] = rt_of_diff(up, lo);
+    v[PK_ALPHAUP] = dphi(up, sub(up, lo));
+    v[PK_DPHILU] = dphi(lo, up);
+    v[PK_EX] = uam.edge_x; v[PK_EY] = uam.edge_y;
+    v[PK_FLAGS] = __uint_as_float(fl);
+    v[PK_G2] = __int_as_float(OG(b, kMD, om));
+    v[PK_S0] = v[PK_S1] = v[PK_S2] = v[PK_S3] = 0.f;
+}
+
 __global__ void k_sg_pack(BatchDev b) {
     if (halted(b)) return;
-    const int n_mod = b.geo.n_mod;
     const int64_t n = n_inner(b, kTL);
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
-        const int im = OI(b, kSG, s), om = OJ(b, kSG, s);
-        const ModDev& ilm = MOD(b, OG(b, kMD, im) % n_mod);
-        const ModDev& olm = MOD(b, OG(b, kMD, om) % n_mod);
-        const int la = md_anchor(ilm, OI(b, kMD, im), OJ(b, kMD, im));
-        const int ua = md_anchor(olm, OI(b, kMD, om), OJ(b, kMD, om));
-        const P3 lo = hit(b, la), up = hit(b, ua);
-        const ModDev& lam = MOD(b, AT(b.hgm, la, H(b)) % n_mod);
-        const ModDev& uam = MOD(b, AT(b.hgm, ua, H(b)) % n_mod);
-        uint32_t fl = 0;
-        fl |= lam.subdet == kBarrel ? F_LO_B : 0u;
-        fl |= lam.subdet == kEndcap ? F_LO_E : 0u;
-        fl |= lam.type == kPS ? F_LO_PS : 0u;
-        fl |= uam.subdet == kBarrel ? F_UP_B : 0u;
-        fl |= uam.subdet == kEndcap ? F_UP_E : 0u;
-        fl |= uam.type == kPS ? F_UP_PS : 0u;
-        fl |= uam.type == kTwoS ? F_UP_2S : 0u;
+        float f6[6];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) f6[k] = OF(b, kSG, k, s);
         float v[PK_N];
-        v[PK_LX] = lo.x; v[PK_LY] = lo.y; v[PK_LZ] = lo.z; v[PK_LRT] = lo.rt;
-        v[PK_LPHI] = lo.phi; v[PK_LR3] = lo.r3; v[PK_LA1] = AT(b.ha1, la, H(b)); v[PK_LTD] = AT(b.htd, la, H(b));
-        v[PK_LA3] = AT(b.ha3, la, H(b));
-        v[PK_LR3Z] = __fsqrt_rn(lo.z * lo.z + lo.rt * lo.rt);
-        v[PK_UX] = up.x; v[PK_UY] = up.y; v[PK_UZ] = up.z; v[PK_URT] = up.rt; v[PK_UPHI] = up.phi; v[PK_UR3] = up.r3;
-        v[PK_DPC] = OF(b, kSG, 3, s); v[PK_DPMIN] = OF(b, kSG, 1, s); v[PK_DPMAX] = OF(b, kSG, 2, s);
-        v[PK_DPMINC] = OF(b, kSG, 4, s); v[PK_DPMAXC] = OF(b, kSG, 5, s);
-        v[PK_RTSEG] = rt_of_diff(up, lo);
-        v[PK_ALPHAUP] = dphi(up, sub(up, lo));
-        v[PK_DPHILU] = dphi(lo, up);
-        v[PK_EX] = uam.edge_x; v[PK_EY] = uam.edge_y;
-        v[PK_FLAGS] = __uint_as_float(fl);
-        v[PK_G2] = __int_as_float(OG(b, kMD, om));
-        v[PK_S0] = v[PK_S1] = v[PK_S2] = v[PK_S3] = 0.f;
+        sg_pack_record(b, OI(b, kSG, s), OJ(b, kSG, s), f6, v);
+        const uint32_t fl = __float_as_uint(v[PK_FLAGS]);
         const int64_t C = b.obj[kSG].cap;
         const int fo[6] = {PK_LRT, PK_LZ, PK_LTD, PK_LA1, PK_UPHI, PK_FLAGS};
 #pragma unroll
@@ -775,21 +790,80 @@ __global__ void k_sg_pack(BatchDev b) {
         float4* dst = reinterpret_cast<float4*>(&AT(b.sgpack, s * PK_N, b.obj[kSG].cap * PK_N));
         for (int k = 0; k < PK_N / 4; ++k) dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
         // the pre-filter's feature records (inner role, outer role)
-        const float drIn = up.rt - lo.rt;
-        const float slope = (up.z - lo.z) / (fabsf(drIn) > 1e-3f ? drIn : copysignf(1e-3f, drIn));
+        const float lz = v[PK_LZ], lrt = v[PK_LRT], uz = v[PK_UZ], urt = v[PK_URT];
+        const float drIn = urt - lrt;
+        const float slope = (uz - lz) / (fabsf(drIn) > 1e-3f ? drIn : copysignf(1e-3f, drIn));
         const float scode = ((fl & F_LO_E) ? 1.f : 0.f) + ((fl & F_LO_PS) ? 0.25f : 0.f);
         const float tcode = ((fl & F_UP_E) ? 0.5f : 0.f) + ((fl & F_UP_2S) ? 0.125f : 0.f);
         float4* fd = reinterpret_cast<float4*>(&AT(b.sgfeat, s * kFeatN, b.obj[kSG].cap * kFeatN));
-        fd[0] = make_float4(lo.x, lo.y, lo.z, lo.rt);
-        fd[1] = make_float4(lo.phi, v[PK_DPC], slope, scode);
-        fd[2] = make_float4(up.x, up.y, up.z, up.rt);
-        fd[3] = make_float4(up.phi, v[PK_ALPHAUP], tcode, 0.f);
+        fd[0] = make_float4(v[PK_LX], v[PK_LY], lz, lrt);
+        fd[1] = make_float4(v[PK_LPHI], v[PK_DPC], slope, scode);
+        fd[2] = make_float4(v[PK_UX], v[PK_UY], uz, urt);
+        fd[3] = make_float4(v[PK_UPHI], v[PK_ALPHAUP], tcode, 0.f);
     }
 }
 
+// createTrackCandidatesFromTriplets (Event.cc:874-982): candidate q of inner
+// triplet p1 is a triplet p2 of a module connected to the module of p1's
+// outermost MD (connection-list order, as the segment candidates); it passes
+// when the trial segment from that MD to p2's innermost MD passes the segment
+// algorithm and the tracklet (trial segment, p2's outer segment) passes the
+// default tracklet algorithm.  The trial segment is not kept.
+struct TCTPStage {
+    static constexpr int kSt = kTC;
+    __device__ static bool eval(const BatchDev& b, int p1, int64_t q, int& oi, int& oj, float* fv) {
+        const int n_mod = b.geo.n_mod;
+        const int mdA = OJ(b, kSG, OJ(b, kTP, p1));
+        const int gA = OG(b, kMD, mdA);
+        const int ev = gA / n_mod, mA = gA - ev * n_mod;
+        int pref;
+        const int k = conn_entry(b, ev, mA, q, pref);
+        const int g3 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
+        const int p2 = (int)(OFF(b, kTP, g3) + (q - pref));
+        oi = p1;
+        oj = p2;
+        (void)fv;
+        const int mdB = OI(b, kSG, OI(b, kTP, p2));
+        float f6[6];
+        if (!sg_pair(b, mdA, mdB, true, f6)) return false;
+        float v[PK_N];
+        sg_pack_record(b, mdA, mdB, f6, v);
+        const SGV S = sgv_from(v);
+        const int so = OJ(b, kTP, p2);
+        const SGV T = load_sgv(b.sgpack, so);
+        float cut, muls;
+        const int algo = tl_phaseA(S, T, cut, muls);
+        if (algo == kAlgoNone || !tl_phaseB1_sgv(algo, S, T, cut)) return false;
+        return tl_phaseB2_sgv<kB2All>(algo, S, T, muls, false);
+    }
+    __device__ static int group_of(const BatchDev& b, int p) { return OG(b, kTP, p); }
+};
+
 // outer segment of flat tracklet candidate c of inner segment s
-__device__ __forceinline__ int tl_outer_of(const BatchDev& b, bool lay, int s, int64_t q) {
-    return lay ? tl_outer_layer(b, s, q) : tl_outer(b, s, q);
+// tracklet candidate q of inner segment s by navigation (Event.cc:694-751):
+// over the segments leaving s's outer MD, the segments leaving their outer MD
+// (both lists from the join index of segments by inner MD)
+__device__ __forceinline__ int tl_outer_nav(const BatchDev& b, int s, int64_t q) {
+    const int m = OJ(b, kSG, s);
+    const int64_t nc = join_n(b, m);
+    for (int64_t k = 0; k < nc; ++k) {
+        const int mc = OJ(b, kSG, join_obj(b, m, k));
+        const int64_t n = join_n(b, mc);
+        if (q < n) return join_obj(b, mc, q);
+        q -= n;
+    }
+#ifdef SDL_DEVICE_CHECKS
+    IX(-3, 0);
+#endif
+    return 0;  // q is below the candidate count (k_tl_count_nav)
+}
+
+// the tracklet variant of a run: 0 module map, 1 layer pairs, 2 navigation
+__device__ __forceinline__ int tl_variant(const BatchDev& b) {
+    return (b.flags & kFlagTLLayers) ? 1 : ((b.flags & kFlagTLNav) ? 2 : 0);
+}
+__device__ __forceinline__ int tl_outer_of(const BatchDev& b, int var, int s, int64_t q) {
+    return var == 1 ? tl_outer_layer(b, s, q) : (var == 2 ? tl_outer_nav(b, s, q) : tl_outer(b, s, q));
 }
 
 // append the lanes' phase-A survivors to the survivor list at the positions
@@ -835,7 +909,7 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_a(BatchDev b) {
     const int task = b.enum_task[kTL] > 0 ? b.enum_task[kTL] : kTaskDefault;
     const int64_t ntask = (total + task - 1) / task;
     const int lane = threadIdx.x & 31;
-    const bool lay = (b.flags & kFlagTLLayers) != 0;
+    const int lay = tl_variant(b);
     for (;;) {
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(b.task + kTL, 1ull);
@@ -1053,7 +1127,7 @@ __global__ void k_tl_collect(BatchDev b, MlpCollect col) {
     const int64_t* off = b.cand[kTL];
     const int64_t offlim = b.cand_cap[kTL] + 1;
     const int64_t total = AT(off, nobj, offlim);
-    const bool lay = (b.flags & kFlagTLLayers) != 0;
+    const int lay = tl_variant(b);
     const int lane = threadIdx.x & 31;
     for (int64_t c0 = (int64_t)blockIdx.x * blockDim.x; c0 < total; c0 += (int64_t)gridDim.x * blockDim.x) {
         const int64_t c = c0 + threadIdx.x;
@@ -1304,6 +1378,89 @@ __global__ void k_tc_count(BatchDev b) {
     }
 }
 
+// navigation tracklet candidates of every segment (Event.cc:694-751) and the
+// reference's candidate counters
+__global__ void k_tl_count_nav(BatchDev b) {
+    if (halted(b)) return;
+    const int n_mod = b.geo.n_mod;
+    const int64_t n = n_inner(b, kTL);
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s - threadIdx.x < n; s += (int64_t)gridDim.x * blockDim.x) {
+        const bool in = s < n;
+        int64_t c = 0;
+        int ev = 0, slot = 0;
+        if (in) {
+            const int m = OJ(b, kSG, s);
+            const int64_t nc = join_n(b, m);
+            for (int64_t k = 0; k < nc; ++k) c += join_n(b, OJ(b, kSG, join_obj(b, m, k)));
+            AT(b.cand[kTL], s, b.cand_cap[kTL] + 1) = c;
+            const int g1 = OG(b, kSG, s);
+            ev = g1 / n_mod;
+            slot = MOD(b, g1 - ev * n_mod).layer_slot;
+        }
+        const bool act = in && c != 0;
+        warp_add(act ? counter_at(b, ev, kTL, 0, slot) : b.counters, (uint32_t)c, act);
+    }
+}
+
+// createTrackCandidatesFromTracklets (Event.cc:984-1062): the reference's
+// candidates of tracklet t are the tracklets of the modules connected to the
+// module of its inner segment's outer MD (conn_sum over tracklet counts); the
+// matching ones are the tracklets whose inner segment matches t's outer
+// segment, which all lie in the module of that segment's inner MD and come
+// once per occurrence of that module in the connection list.  Layer-pair
+// tracklets are listed by no module (Event.cc:785 via
+// addTrackletToLowerLayer), so after them there are no candidates.
+__global__ void k_tc_count_tl(BatchDev b) {
+    if (halted(b)) return;
+    const int n_mod = b.geo.n_mod;
+    const int64_t n = n_inner(b, kTC);
+    const bool none = (b.flags & kFlagTLLayers) != 0;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t - threadIdx.x < n; t += (int64_t)gridDim.x * blockDim.x) {
+        const bool in = t < n;
+        int64_t cref = 0;
+        int ev = 0, slot = 0;
+        if (in) {
+            const int gA2 = OG(b, kMD, OJ(b, kSG, OI(b, kTL, t)));
+            ev = gA2 / n_mod;
+            const int mA2 = gA2 - ev * n_mod;
+            cref = none ? 0 : AT(b.conn_sum, gA2, b.n_gm);
+            const int mB = OI(b, kSG, OJ(b, kTL, t));
+            const int mB1 = OG(b, kMD, mB) - ev * n_mod;
+            int mult = 0;
+            const int k0 = AT(b.geo.conn_off, mA2, NM(b) + 1), k1 = AT(b.geo.conn_off, mA2 + 1, NM(b) + 1);
+            for (int k = k0; k < k1; ++k) mult += AT(b.geo.conn_idx, k, NC(b)) == mB1;
+            AT(b.cand[kTC], t, b.cand_cap[kTC] + 1) = none ? 0 : (int64_t)mult * join_n(b, mB);
+            slot = MOD(b, OG(b, kTL, t) - ev * n_mod).layer_slot;
+        }
+        const bool act = in && cref != 0;
+        warp_add(act ? counter_at(b, ev, kTC, 0, slot) : b.counters, (uint32_t)cref, act);
+    }
+}
+
+// createTrackCandidatesFromTriplets (Event.cc:874-982): candidates of triplet
+// p = the triplets of the modules connected to the module of its outermost MD
+// (conn_sum over triplet counts), with the reference's candidate counters
+__global__ void k_tc_count_tp(BatchDev b) {
+    if (halted(b)) return;
+    const int n_mod = b.geo.n_mod;
+    const int64_t n = n_inner(b, kTC);
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p - threadIdx.x < n; p += (int64_t)gridDim.x * blockDim.x) {
+        const bool in = p < n;
+        int64_t c = 0;
+        int ev = 0, slot = 0;
+        if (in) {
+            const int gA = OG(b, kMD, OJ(b, kSG, OJ(b, kTP, p)));
+            c = AT(b.conn_sum, gA, b.n_gm);
+            AT(b.cand[kTC], p, b.cand_cap[kTC] + 1) = c;
+            const int g1 = OG(b, kTP, p);
+            ev = g1 / n_mod;
+            slot = MOD(b, g1 - ev * n_mod).layer_slot;
+        }
+        const bool act = in && c != 0;
+        warp_add(act ? counter_at(b, ev, kTC, 0, slot) : b.counters, (uint32_t)c, act);
+    }
+}
+
 // Event.cc:835: track-candidate candidates are barrel-layer-1 x barrel-layer-3 tracklets
 __global__ void k_tc_cand_counter(BatchDev b) {
     for (int ev = blockIdx.x * blockDim.x + threadIdx.x; ev < b.n_ev; ev += gridDim.x * blockDim.x) {
@@ -1334,9 +1491,11 @@ __global__ void k_materialize(BatchDev b, int st, int64_t first, int64_t n, int3
             case kSG: put_sg(b, o, out + 4 * k); break;
             case kTL: put_tl(b, kTL, o, out + 8 * k); break;
             case kTP: put_tl(b, kTP, o, out + 8 * k); break;
-            default:
-                put_tl(b, kTL, OI(b, kTC, o), out + 16 * k);
-                put_tl(b, kTL, OJ(b, kTC, o), out + 16 * k + 8);
+            default: {  // two tracklets, or two triplets (createTrackCandidatesFromTriplets)
+                const int ist = (b.flags & kFlagTCFromTP) ? kTP : kTL;
+                put_tl(b, ist, OI(b, kTC, o), out + 16 * k);
+                put_tl(b, ist, OJ(b, kTC, o), out + 16 * k + 8);
+            }
         }
     }
 }
@@ -1371,7 +1530,7 @@ void enum_and_group(const BatchDev& b, cudaStream_t s, Hooks* h, bool layer_coun
         case kSG: ninner_ptr = b.obj[kMD].mod_cnt + b.n_gm; break;
         case kTL:
         case kTP: ninner_ptr = b.obj[kSG].mod_cnt + b.n_gm; break;
-        default: ninner_ptr = b.obj[kTL].mod_cnt + b.n_gm;
+        default: ninner_ptr = ((b.flags & kFlagTCFromTP) ? b.obj[kTP] : b.obj[kTL]).mod_cnt + b.n_gm;
     }
     scan_h(b, b.cand[st], ninner_ptr, b.cand_cap[st], s, h);
     k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, st);
@@ -1418,13 +1577,29 @@ void launch_sg(const BatchDev& b, cudaStream_t s, Hooks* h) {
     enum_and_group<SGStage>(b, s, h);
 }
 
+// the join index of stage st's objects (segments or tracklets), keyed by mini-doublet
+static void join_index(const BatchDev& b, int st, cudaStream_t s, Hooks* h) {
+    cudaMemsetAsync(b.joff, 0, (b.obj[kMD].cap + 1) * sizeof(int64_t), s);
+    cudaMemsetAsync(b.jcur, 0, b.obj[kMD].cap * sizeof(int32_t), s);
+    k_join_count<<<b.n_sm * 8, 256, 0, s>>>(b, st);
+    scan_h(b, b.joff, b.obj[kMD].mod_cnt + b.n_gm, b.obj[kMD].cap, s, h);
+    k_join_scatter<<<b.n_sm * 8, 256, 0, s>>>(b, st);
+    if (h) h->launches += 2;
+}
+
 void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     // conn sums over segment counts serve the tracklet enumeration and the
     // triplet candidate counters (Event.cc:547-596 loops over the same lists)
     k_sg_pack<<<b.n_sm * 8, 256, 0, s>>>(b);
     k_conn_sum<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kSG, kTP);
-    if (b.flags & kFlagTLLayers) k_tl_count_layers<<<b.n_sm * 8, 256, 0, s>>>(b);
-    else k_tl_count<<<b.n_sm * 8, 256, 0, s>>>(b);
+    if (b.flags & kFlagTLLayers) {
+        k_tl_count_layers<<<b.n_sm * 8, 256, 0, s>>>(b);
+    } else if (b.flags & kFlagTLNav) {
+        join_index(b, kSG, s, h);  // segments by inner MD: the outward lists
+        k_tl_count_nav<<<b.n_sm * 8, 256, 0, s>>>(b);
+    } else {
+        k_tl_count<<<b.n_sm * 8, 256, 0, s>>>(b);
+    }
     if (h) h->launches += 3;
     scan_h(b, b.cand[kTL], b.obj[kSG].mod_cnt + b.n_gm, b.cand_cap[kTL], s, h);
     k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, kTL);
@@ -1454,15 +1629,6 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     if (h) h->launches += 3;
 }
 
-// the join index of stage st's objects (segments or tracklets), keyed by mini-doublet
-static void join_index(const BatchDev& b, int st, cudaStream_t s, Hooks* h) {
-    cudaMemsetAsync(b.joff, 0, (b.obj[kMD].cap + 1) * sizeof(int64_t), s);
-    cudaMemsetAsync(b.jcur, 0, b.obj[kMD].cap * sizeof(int32_t), s);
-    k_join_count<<<b.n_sm * 8, 256, 0, s>>>(b, st);
-    scan_h(b, b.joff, b.obj[kMD].mod_cnt + b.n_gm, b.obj[kMD].cap, s, h);
-    k_join_scatter<<<b.n_sm * 8, 256, 0, s>>>(b, st);
-    if (h) h->launches += 2;
-}
 
 void launch_tp(const BatchDev& b, cudaStream_t s, Hooks* h) {
     join_index(b, kSG, s, h);
@@ -1472,9 +1638,21 @@ void launch_tp(const BatchDev& b, cudaStream_t s, Hooks* h) {
 }
 
 void launch_tc(const BatchDev& b, cudaStream_t s, Hooks* h) {
+    if (b.flags & kFlagTCFromTP) {
+        k_conn_sum<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kTP, -1);
+        k_tc_count_tp<<<b.n_sm * 8, 256, 0, s>>>(b);
+        if (h) h->launches += 2;
+        enum_and_group<TCTPStage>(b, s, h);
+        return;
+    }
     join_index(b, kTL, s, h);
-    k_tc_count<<<b.n_sm * 8, 256, 0, s>>>(b);
-    k_tc_cand_counter<<<grid_for(b.n_ev, 128, 1024), 128, 0, s>>>(b);
+    if (b.flags & kFlagTCFromTL) {
+        k_conn_sum<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kTL, -1);
+        k_tc_count_tl<<<b.n_sm * 8, 256, 0, s>>>(b);
+    } else {
+        k_tc_count<<<b.n_sm * 8, 256, 0, s>>>(b);
+        k_tc_cand_counter<<<grid_for(b.n_ev, 128, 1024), 128, 0, s>>>(b);
+    }
     if (h) h->launches += 2;
     enum_and_group<TCStage>(b, s, h);
 }

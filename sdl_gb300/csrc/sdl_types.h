@@ -58,6 +58,9 @@ enum : int {
     kFlagTLLayers = 2,   // createTracklets: layer-pair tracklets
     kFlagTLNm1 = 4,      // DefaultNm1_TLAlgo
     kFlagMLP = 16,       // learned pre-filter ahead of the tracklet cuts
+    kFlagTLNav = 32,     // createTrackletsViaNavigation
+    kFlagTCFromTL = 64,  // createTrackCandidatesFromTracklets
+    kFlagTCFromTP = 128, // createTrackCandidatesFromTriplets
 };
 
 // Per-stage status word bits

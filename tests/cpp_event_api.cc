@@ -1,8 +1,9 @@
 // Drives the chain through include/sdl_event.hpp exactly as a caller of the
 // reference's SDL::Event would, and prints the object counts per stage.
-//   cpp_event_api <tilted> <endcap> <map> <hits.bin> [layer]
+//   cpp_event_api <tilted> <endcap> <map> <hits.bin> [map|layer|nav|tctl|tctp]
 // "layer" selects createSegments / createTracklets (layer pairs) instead of
-// the module-map variants.
+// the module-map variants, "nav" createTrackletsViaNavigation, "tctl" /
+// "tctp" createTrackCandidatesFromTracklets / FromTriplets.
 // hits.bin: int64 n, float32 x[n], y[n], z[n], int32 idx[n], uint32 detid[n].
 // Exit code 3 when no CUDA device is available.
 #include <cstdio>
@@ -31,13 +32,17 @@ int main(int argc, char** argv) {
         SDL::Event ev;
         for (int64_t i = 0; i < n; ++i) ev.addHitToModule(SDL::Hit(x[i], y[i], z[i], idx[i]), det[i]);
         ev.createMiniDoublets();
-        const bool layer = argc > 5 && std::string(argv[5]) == "layer";
+        const std::string mode = argc > 5 ? argv[5] : "map";
+        const bool layer = mode == "layer";
         if (layer) ev.createSegments();
         else ev.createSegmentsWithModuleMap();
         if (layer) ev.createTracklets();
+        else if (mode == "nav") ev.createTrackletsViaNavigation();
         else ev.createTrackletsWithModuleMap();
         ev.createTriplets();
-        ev.createTrackCandidates();
+        if (mode == "tctl") ev.createTrackCandidatesFromTracklets();
+        else if (mode == "tctp") ev.createTrackCandidatesFromTriplets();
+        else ev.createTrackCandidates();
         std::printf("%u %u %u %u %u %u\n", ev.getNumberOfHits(), ev.getNumberOfMiniDoublets(), ev.getNumberOfSegments(),
                     ev.getNumberOfTracklets(), ev.getNumberOfTriplets(), ev.getNumberOfTrackCandidates());
         const auto tc = ev.getTrackCandidates();

@@ -29,8 +29,10 @@ def run_gpu(gpu, det, events, flags=0):
 
 
 # fixture mode -> chain flags: "layer" fixtures were made with the
-# reference's createSegments + createTracklets (layer pairs)
-FLAGS = {"map": 0, "layer": 3}
+# reference's createSegments + createTracklets (layer pairs); "nav" with
+# createTrackletsViaNavigation; "tctl" / "tctp" with
+# createTrackCandidatesFromTracklets / FromTriplets
+FLAGS = {"map": 0, "layer": 3, "nav": 32, "tctl": 64, "tctp": 128}
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -153,7 +155,7 @@ def test_unknown_module_extends_table(gpu, oracle_lib):
         assert oracle_lib.digest(gpu.objects(s, 0)) == oracle_lib.digest(ref[s])
 
 
-@pytest.mark.parametrize("name", ["flat_s0", "flat_s0_layer"])
+@pytest.mark.parametrize("name", ["flat_s0", "flat_s0_layer", "pu20_s0_nav", "pu20_s0_tctl", "pu20_s0_tctp"])
 def test_cpp_event_api_matches_golden(name, tmp_path, oracle_lib):
     """The reference's call sequence through include/sdl_event.hpp."""
     import os
