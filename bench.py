@@ -356,6 +356,22 @@ def main():
                      "tl_passes_ms": {"enumeration_and_float_cuts": round(float(np.mean([v[0] for v in p_pass])), 3),
                                       "double_cuts": round(float(np.mean([v[2] for v in p_pass])), 3)}}
 
+    # ---- the chain's other variants on the same events (plain chain, shapes
+    # tuned for the module-map chain) ---------------------------------------------
+    from sdl_gb300 import FLAG_TC_FROM_TL, FLAG_TC_FROM_TP, FLAG_TL_NAV
+    variants = {}
+    for vname, vflags in (("tracklets_via_navigation", FLAG_TL_NAV),
+                          ("track_candidates_from_tracklets", FLAG_TC_FROM_TL),
+                          ("track_candidates_from_triplets", FLAG_TC_FROM_TP)):
+        for _ in range(2):
+            ch.run(4, vflags)
+        v_ms, v_stage, _, _ = timed_runs(ch, vflags, 3, flush)
+        v_mean = allmax(pg, statistics.fmean(v_ms))
+        variants[vname] = {"flags": vflags, "value": round(allsum(pg, len(batch)) * 1e3 / v_mean, 3),
+                           "unit": "events/s", "ms_per_step": round(v_mean, 3),
+                           "objects_per_step": [int(v) for v in ch.counts(-1)],
+                           "stage_ms": [round(float(v), 3) for v in np.mean(np.array(v_stage), axis=0)]}
+
     # ---- end to end through the C ABI: pinned host buffers in, track
     # candidates out, for the whole batch each step -----------------------------
     n_hit = int(sum(len(e) for e in batch))
@@ -470,7 +486,7 @@ def main():
                                      "pruned_fraction": round(1.0 - mstats["kept"] / max(1, mstats["scored"]), 4)},
                        "wall_s": round(wall, 3)},
             "tc_recall": round(tc_rec, 5), "tl_recall": round(tl_rec, 5),
-            "plain_batched": plain_batched, "plain_single": plain_single,
+            "plain_batched": plain_batched, "plain_single": plain_single, "variants": variants,
             "e2e": {"value": round(e2e_value, 3), "unit": "events/s", "ms_per_step": round(e2e_mean, 3),
                     "h2d_bytes_per_step": n_hit * 20 + 8 * (len(batch) + 1), "d2h_bytes_per_step": int(statistics.fmean(d2h)),
                     "path": "sdlg_set_events (pinned host) + sdlg_run(SDLG_FLAG_MLP) + sdlg_get_objects(TC, into pinned host memory)"},
