@@ -379,6 +379,9 @@ int ensure_buffers(sdlg_ctx* ctx) {
     AL(b.joff, ctx->cap_obj[kMD] + 1);
     AL(b.jcur, ctx->cap_obj[kMD]);
     AL(b.jidx, std::max(ctx->cap_obj[kSG], ctx->cap_obj[kTL]));
+    AL(b.joff2, ctx->cap_obj[kMD] + 1);
+    AL(b.jcur2, ctx->cap_obj[kMD]);
+    AL(b.jidx2, ctx->cap_obj[kTP]);
 #undef AL
     CK(cudaMemcpyAsync(b.n_gm_dev, &n_gm, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));

@@ -563,7 +563,14 @@ __device__ __forceinline__ int tl_outer_layer(const BatchDev& b, int s, int64_t 
 // one), so that each join visits only matching objects (joff: offsets per
 // mini-doublet, jidx: the objects).
 __device__ __forceinline__ int join_key(const BatchDev& b, int st, int64_t o) {
-    return st == kSG ? OI(b, kSG, o) : OI(b, kSG, OI(b, kTL, o));
+    return st == kSG ? OI(b, kSG, o) : OI(b, kSG, OI(b, st, o));  // tracklets, triplets: inner segment's inner MD
+}
+// the second index (the triplets by their innermost MD)
+__device__ __forceinline__ int64_t join2_n(const BatchDev& b, int md) {
+    return AT(b.joff2, md + 1, b.obj[kMD].cap + 1) - AT(b.joff2, md, b.obj[kMD].cap + 1);
+}
+__device__ __forceinline__ int join2_obj(const BatchDev& b, int md, int64_t k) {
+    return AT(b.jidx2, AT(b.joff2, md, b.obj[kMD].cap + 1) + k, b.obj[kTP].cap);
 }
 __device__ __forceinline__ int64_t join_n(const BatchDev& b, int md) {
     return AT(b.joff, md + 1, b.obj[kMD].cap + 1) - AT(b.joff, md, b.obj[kMD].cap + 1);
@@ -835,6 +842,43 @@ struct TCTPStage {
         const int algo = tl_phaseA(S, T, cut, muls);
         if (algo == kAlgoNone || !tl_phaseB1_sgv(algo, S, T, cut)) return false;
         return tl_phaseB2_sgv<kB2All>(algo, S, T, muls, false);
+    }
+    __device__ static int group_of(const BatchDev& b, int p) { return OG(b, kTP, p); }
+};
+
+// createTrackCandidatesFromTriplets after module-map segments: the trial
+// segment (mdA, mdB) passes the segment algorithm exactly when the segment
+// stage made it, and it made it once per occurrence of mdB's module in the
+// connection list of mdA's module, which is also how often the reference's
+// loop (over that list) reaches each outer triplet starting at mdB.  So the
+// candidates are: the segments leaving p1's outermost MD mdA (the join index)
+// x the triplets starting at each one's outer MD (the second index); the
+// tracklet algorithm then runs on that segment's packed record and p2's outer
+// segment.  Same track candidates as TCTPStage, without the trial segments.
+struct TCTPMapStage {
+    static constexpr int kSt = kTC;
+    __device__ static bool eval(const BatchDev& b, int p1, int64_t q, int& oi, int& oj, float* fv) {
+        const int mdA = OJ(b, kSG, OJ(b, kTP, p1));
+        const int64_t ns = join_n(b, mdA);
+        int sx = 0, p2 = -1;
+        for (int64_t k = 0; k < ns; ++k) {
+            sx = join_obj(b, mdA, k);
+            const int64_t n = join2_n(b, OJ(b, kSG, sx));
+            if (q < n) {
+                p2 = join2_obj(b, OJ(b, kSG, sx), q);
+                break;
+            }
+            q -= n;
+        }
+        oi = p1;
+        oj = p2;
+        (void)fv;
+        if (p2 < 0) return false;  // not reached: q is below the count (k_tc_count_tp)
+        const int so = OJ(b, kTP, p2);
+        float cut, muls;
+        const int algo = tl_phaseA(load_sgv(b.sgpack, sx), load_sgv(b.sgpack, so), cut, muls);
+        if (algo == kAlgoNone || !tl_phaseB1(algo, b.sgpack, sx, so, cut)) return false;
+        return tl_phaseB2<kB2All>(algo, b.sgpack, sx, so, muls, false);
     }
     __device__ static int group_of(const BatchDev& b, int p) { return OG(b, kTP, p); }
 };
@@ -1329,19 +1373,24 @@ __global__ void k_tl_count_layers(BatchDev b) {
 }
 
 // objects of stage st per key mini-doublet, then their positions
-__global__ void k_join_count(BatchDev b, int st) {
+__global__ void k_join_count(BatchDev b, int st, bool second) {
     if (halted(b)) return;
+    int64_t* off = second ? b.joff2 : b.joff;
     const int64_t n = min(OFF(b, st, b.n_gm), b.obj[st].cap);
     for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x)
-        atomicAdd((unsigned long long*)&AT(b.joff, join_key(b, st, o), b.obj[kMD].cap + 1), 1ull);
+        atomicAdd((unsigned long long*)&AT(off, join_key(b, st, o), b.obj[kMD].cap + 1), 1ull);
 }
-__global__ void k_join_scatter(BatchDev b, int st) {
+__global__ void k_join_scatter(BatchDev b, int st, bool second) {
     if (halted(b)) return;
+    const int64_t* off = second ? b.joff2 : b.joff;
+    int32_t* cur = second ? b.jcur2 : b.jcur;
+    int32_t* idx = second ? b.jidx2 : b.jidx;
+    const int64_t cap = second ? b.obj[kTP].cap : max(b.obj[kSG].cap, b.obj[kTL].cap);
     const int64_t n = min(OFF(b, st, b.n_gm), b.obj[st].cap);
     for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x) {
         const int k = join_key(b, st, o);
-        const int64_t pos = AT(b.joff, k, b.obj[kMD].cap + 1) + atomicAdd(&AT(b.jcur, k, b.obj[kMD].cap), 1);
-        AT(b.jidx, pos, max(b.obj[kSG].cap, b.obj[kTL].cap)) = (int)o;
+        const int64_t pos = AT(off, k, b.obj[kMD].cap + 1) + atomicAdd(&AT(cur, k, b.obj[kMD].cap), 1);
+        AT(idx, pos, cap) = (int)o;
     }
 }
 
@@ -1449,9 +1498,15 @@ __global__ void k_tc_count_tp(BatchDev b) {
         int64_t c = 0;
         int ev = 0, slot = 0;
         if (in) {
-            const int gA = OG(b, kMD, OJ(b, kSG, OJ(b, kTP, p)));
-            c = AT(b.conn_sum, gA, b.n_gm);
-            AT(b.cand[kTC], p, b.cand_cap[kTC] + 1) = c;
+            const int mdA = OJ(b, kSG, OJ(b, kTP, p));
+            c = AT(b.conn_sum, OG(b, kMD, mdA), b.n_gm);
+            int64_t e = c;  // the trial-segment enumeration: every reference candidate
+            if (!(b.flags & kFlagSGLayers)) {  // TCTPMapStage: segments leaving mdA x triplets at their outer MD
+                e = 0;
+                const int64_t ns = join_n(b, mdA);
+                for (int64_t k = 0; k < ns; ++k) e += join2_n(b, OJ(b, kSG, join_obj(b, mdA, k)));
+            }
+            AT(b.cand[kTC], p, b.cand_cap[kTC] + 1) = e;
             const int g1 = OG(b, kTP, p);
             ev = g1 / n_mod;
             slot = MOD(b, g1 - ev * n_mod).layer_slot;
@@ -1577,13 +1632,15 @@ void launch_sg(const BatchDev& b, cudaStream_t s, Hooks* h) {
     enum_and_group<SGStage>(b, s, h);
 }
 
-// the join index of stage st's objects (segments or tracklets), keyed by mini-doublet
-static void join_index(const BatchDev& b, int st, cudaStream_t s, Hooks* h) {
-    cudaMemsetAsync(b.joff, 0, (b.obj[kMD].cap + 1) * sizeof(int64_t), s);
-    cudaMemsetAsync(b.jcur, 0, b.obj[kMD].cap * sizeof(int32_t), s);
-    k_join_count<<<b.n_sm * 8, 256, 0, s>>>(b, st);
-    scan_h(b, b.joff, b.obj[kMD].mod_cnt + b.n_gm, b.obj[kMD].cap, s, h);
-    k_join_scatter<<<b.n_sm * 8, 256, 0, s>>>(b, st);
+// the join index of stage st's objects (segments or tracklets), keyed by
+// mini-doublet; second = true builds the second index (triplets)
+static void join_index(const BatchDev& b, int st, cudaStream_t s, Hooks* h, bool second = false) {
+    int64_t* off = second ? b.joff2 : b.joff;
+    cudaMemsetAsync(off, 0, (b.obj[kMD].cap + 1) * sizeof(int64_t), s);
+    cudaMemsetAsync(second ? b.jcur2 : b.jcur, 0, b.obj[kMD].cap * sizeof(int32_t), s);
+    k_join_count<<<b.n_sm * 8, 256, 0, s>>>(b, st, second);
+    scan_h(b, off, b.obj[kMD].mod_cnt + b.n_gm, b.obj[kMD].cap, s, h);
+    k_join_scatter<<<b.n_sm * 8, 256, 0, s>>>(b, st, second);
     if (h) h->launches += 2;
 }
 
@@ -1639,10 +1696,16 @@ void launch_tp(const BatchDev& b, cudaStream_t s, Hooks* h) {
 
 void launch_tc(const BatchDev& b, cudaStream_t s, Hooks* h) {
     if (b.flags & kFlagTCFromTP) {
+        const bool map = !(b.flags & kFlagSGLayers);
+        if (map) {
+            join_index(b, kSG, s, h);        // segments by inner MD
+            join_index(b, kTP, s, h, true);  // triplets by innermost MD
+        }
         k_conn_sum<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kTP, -1);
         k_tc_count_tp<<<b.n_sm * 8, 256, 0, s>>>(b);
         if (h) h->launches += 2;
-        enum_and_group<TCTPStage>(b, s, h);
+        if (map) enum_and_group<TCTPMapStage>(b, s, h);
+        else enum_and_group<TCTPStage>(b, s, h);
         return;
     }
     join_index(b, kTL, s, h);

@@ -69,6 +69,9 @@ struct BatchDev {
     int64_t* joff;                 // mini-doublet cap + 1: counts -> offsets
     int32_t* jcur;                 // mini-doublet cap: fill cursors
     int32_t* jidx;                 // max(segment cap, tracklet cap): object indices
+    int64_t* joff2;                // a second index (createTrackCandidatesFromTriplets: the triplets by their
+    int32_t* jcur2;                //   innermost mini-doublet, beside the segments by inner mini-doublet)
+    int32_t* jidx2;                // triplet cap
     int4* pb;                      // candidates through phase B1: (inner, outer, algorithm, muls bits), BBBB
                                    //   from the front, the others from the back
     unsigned long long* n_pb;      // [2]: BBBB entries, other entries (kept_cap in all)

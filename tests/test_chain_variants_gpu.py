@@ -1,7 +1,9 @@
 """createTrackletsViaNavigation, createTrackCandidatesFromTracklets and
 createTrackCandidatesFromTriplets on the GPU against the CPU restatement
 (mode bits = chain flag bits), objects and counters, on a batch with barrel,
-tilted and endcap hits, an empty event and a PU event; alone and combined."""
+tilted and endcap hits, an empty event and a PU event; alone and combined
+(track candidates from triplets after module-map segments take the
+segment-object path, after layer-pair segments the trial-segment path)."""
 import numpy as np
 import pytest
 
@@ -17,7 +19,7 @@ def gpu():
     return Chain(0)
 
 
-@pytest.mark.parametrize("flags", [32, 64, 128, 32 | 64, 32 | 128, 32 | 4, 3 | 64])
+@pytest.mark.parametrize("flags", [32, 64, 128, 32 | 64, 32 | 128, 32 | 4, 3 | 64, 1 | 128])
 def test_variants_match_oracle(flags, gpu, oracle_lib):
     from sdl_gb300 import synth
     det = synth.detector("full")
