@@ -87,6 +87,18 @@ int sdlg_geometry_upload(sdlg_ctx* ctx, int64_t n_tilted, const uint32_t* t_deti
                          int64_t n_endcap, const uint32_t* e_detid, const float* e_vals, int64_t n_keys,
                          const uint32_t* keys, const int64_t* off, const uint32_t* dst);
 
+/* Binary geometry (no counterpart in the reference): the three tables in one
+ * file that loads without text parsing.  sdlg_geometry_convert parses the
+ * text files (as sdlg_geometry_load_files; any path may be NULL) and writes
+ * the binary file; it needs no context and no device.  Layout (little
+ * endian): "SDLGEO1" and a zero byte; uint64 n, then n x {uint32 detid,
+ * float drdz, float slope} (tilted); uint64 n, then n x {uint32 detid, float
+ * slope lower, float centroid phi} (endcap); uint64 n_keys, then n_keys x
+ * {uint32 detid, uint32 count}, then the uint32 connected detids of all keys
+ * in key order.  Rows are in detid order. */
+int sdlg_geometry_convert(const char* tilted_path, const char* endcap_path, const char* map_path, const char* out_path);
+int sdlg_geometry_load_binary(sdlg_ctx* ctx, const char* path);
+
 /* Number of modules in the device module table. */
 int64_t sdlg_num_modules(const sdlg_ctx* ctx);
 

@@ -60,6 +60,8 @@ def lib():
         L.sdlg_last_error.restype = ctypes.c_char_p
         L.sdlg_geometry_load_files.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
         L.sdlg_geometry_upload.argtypes = [vp, i64, vp, vp, i64, vp, vp, i64, vp, vp, vp]
+        L.sdlg_geometry_convert.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
+        L.sdlg_geometry_load_binary.argtypes = [vp, ctypes.c_char_p]
         L.sdlg_num_modules.argtypes = [vp]
         L.sdlg_num_modules.restype = i64
         L.sdlg_set_events.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp]
@@ -97,6 +99,15 @@ def lib():
     return _LIB
 
 
+def geometry_convert(tilted, endcap, cmap, out_path):
+    """Parse the three geometry text files (any may be None) into one binary
+    file for Chain.load_binary (no device needed)."""
+    enc = lambda p: p.encode() if p else None
+    rc = lib().sdlg_geometry_convert(enc(tilted), enc(endcap), enc(cmap), out_path.encode())
+    if rc != 0:
+        raise SDLError("%d: cannot convert the geometry files" % rc)
+
+
 class Chain:
     """One device context: geometry, a batch of events and their results."""
 
@@ -131,6 +142,10 @@ class Chain:
     def load_files(self, tilted=None, endcap=None, cmap=None):
         enc = lambda p: p.encode() if p else None
         self._ck(lib().sdlg_geometry_load_files(self.h, enc(tilted), enc(endcap), enc(cmap)))
+
+    def load_binary(self, path):
+        """Geometry from a binary file written by :func:`geometry_convert`."""
+        self._ck(lib().sdlg_geometry_load_binary(self.h, path.encode()))
 
     def upload_tables(self, t_id, t_val, e_id, e_val, keys, off, dst):
         arrs = [np.ascontiguousarray(a, dtype=d) for a, d in

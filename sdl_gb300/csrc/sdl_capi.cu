@@ -745,6 +745,88 @@ int sdlg_geometry_load_files(sdlg_ctx* ctx, const char* tilted_path, const char*
     return build_module_table(ctx, {});
 }
 
+// ---- binary geometry: the host tables in one file (format in sdl_gpu.h)
+namespace {
+const char kGeoMagic[8] = {'S', 'D', 'L', 'G', 'E', 'O', '1', 0};
+
+bool write_geometry(const HostGeometry& hg, const char* path) {
+    std::FILE* f = std::fopen(path, "wb");
+    if (!f) return false;
+    bool ok = std::fwrite(kGeoMagic, 1, 8, f) == 8;
+    auto u64 = [&](uint64_t v) { ok = ok && std::fwrite(&v, 8, 1, f) == 1; };
+    auto row = [&](uint32_t d, float a, float c) {
+        ok = ok && std::fwrite(&d, 4, 1, f) == 1 && std::fwrite(&a, 4, 1, f) == 1 && std::fwrite(&c, 4, 1, f) == 1;
+    };
+    u64(hg.tilted.size());
+    for (const auto& kv : hg.tilted) row(kv.first, kv.second.first, kv.second.second);
+    u64(hg.endcap.size());
+    for (const auto& kv : hg.endcap) row(kv.first, kv.second.first, kv.second.second);
+    u64(hg.conn.size());
+    for (const auto& kv : hg.conn) {
+        const uint32_t n = (uint32_t)kv.second.size();
+        ok = ok && std::fwrite(&kv.first, 4, 1, f) == 1 && std::fwrite(&n, 4, 1, f) == 1;
+    }
+    for (const auto& kv : hg.conn)
+        if (!kv.second.empty()) ok = ok && std::fwrite(kv.second.data(), 4, kv.second.size(), f) == kv.second.size();
+    return std::fclose(f) == 0 && ok;
+}
+
+bool read_geometry(const char* path, HostGeometry& hg) {
+    std::FILE* f = std::fopen(path, "rb");
+    if (!f) return false;
+    char magic[8];
+    bool ok = std::fread(magic, 1, 8, f) == 8 && std::memcmp(magic, kGeoMagic, 8) == 0;
+    auto u64 = [&]() {
+        uint64_t v = 0;
+        ok = ok && std::fread(&v, 8, 1, f) == 1 && v < (1ull << 32);
+        return ok ? v : 0ull;
+    };
+    for (int table = 0; table < 2 && ok; ++table) {
+        const uint64_t n = u64();
+        for (uint64_t i = 0; i < n && ok; ++i) {
+            uint32_t d;
+            float a, c;
+            ok = std::fread(&d, 4, 1, f) == 1 && std::fread(&a, 4, 1, f) == 1 && std::fread(&c, 4, 1, f) == 1;
+            if (ok) (table == 0 ? hg.tilted : hg.endcap)[d] = {a, c};
+        }
+    }
+    const uint64_t nk = u64();
+    std::vector<std::pair<uint32_t, uint32_t>> keys;
+    for (uint64_t k = 0; k < nk && ok; ++k) {
+        uint32_t d, n;
+        ok = std::fread(&d, 4, 1, f) == 1 && std::fread(&n, 4, 1, f) == 1;
+        if (ok) keys.push_back({d, n});
+    }
+    for (const auto& kn : keys) {
+        if (!ok) break;
+        std::vector<uint32_t> v(kn.second);
+        ok = kn.second == 0 || std::fread(v.data(), 4, kn.second, f) == kn.second;
+        hg.conn[kn.first] = std::move(v);
+    }
+    std::fclose(f);
+    return ok;
+}
+}  // namespace
+
+int sdlg_geometry_convert(const char* tilted_path, const char* endcap_path, const char* map_path, const char* out_path) {
+    if (!out_path) return SDLG_ERR_ARG;
+    HostGeometry hg;
+    const char* paths[3] = {tilted_path, endcap_path, map_path};
+    for (int k = 0; k < 3; ++k)
+        if (paths[k] && parse_file(paths[k], k, hg) != SDLG_OK) return SDLG_ERR_IO;
+    return write_geometry(hg, out_path) ? SDLG_OK : SDLG_ERR_IO;
+}
+
+int sdlg_geometry_load_binary(sdlg_ctx* ctx, const char* path) {
+    if (!ctx || !path) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    HostGeometry hg;
+    if (!read_geometry(path, hg)) return fail(ctx, SDLG_ERR_IO, "cannot read binary geometry %s", path);
+    ctx->hg = hg;
+    ctx->detids.clear();
+    return build_module_table(ctx, {});
+}
+
 int sdlg_geometry_upload(sdlg_ctx* ctx, int64_t n_tilted, const uint32_t* t_detid, const float* t_vals, int64_t n_endcap,
                          const uint32_t* e_detid, const float* e_vals, int64_t n_keys, const uint32_t* keys,
                          const int64_t* off, const uint32_t* dst) {
