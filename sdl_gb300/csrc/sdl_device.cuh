@@ -206,6 +206,21 @@ static __device__ __noinline__ float muls(float d, float q, bool two) {
     float r;
     return muls_fast(d, q, two, r) ? r : muls_d(d, q, two);
 }
+// muls(d, S.lr3z / rtIn, true) with sqrt(S.lr3z / rtIn) precomputed for the
+// inner segment S (sg_pack_record: the same sqrt_ff, NaN outside muls_fast's
+// range of the quotient); the same arithmetic as muls_fast
+__device__ __forceinline__ bool muls_fast_sq(float d, float sqh, float sql, float& r) {
+    if (!(d >= 0.f && d < 1e4f)) return false;
+    if (!(sqh > 0.f)) return false;  // NaN: the quotient is outside the fast path's range
+    const ffm::ff t = ffm::div(ffm::mul(ffm::ff{0x1.99999ap-3f, -0x1.99999ap-29f}, d), ffm::ff{50.f, 0.f});
+    ffm::ff m = ffm::mul(ffm::sqrt_ff(ffm::add(t, 0.1f)), 0.015f);
+    m = ffm::mul(m, ffm::ff{sqh, sql});
+    return ffm::round_unique_rel(m, r);
+}
+static __device__ __noinline__ float muls_sq(float d, float sqh, float sql, float lr3z, float rtIn) {
+    float r;
+    return muls_fast_sq(d, sqh, sql, r) ? r : muls_d(d, lr3z / rtIn, true);
+}
 
 // (float)((double)head + 0.25 * ((double)t * (double)t)): the square is exact in double
 static __device__ __noinline__ float add_quarter_sq_d(float head, float t) {
@@ -630,7 +645,7 @@ enum SGPackField : int {
     PK_DPC, PK_DPMIN, PK_DPMAX, PK_DPMINC,  // segment dPhiChange, dPhiMin, dPhiMax, dPhiMinChange
     PK_DPMAXC, PK_RTSEG, PK_ALPHAUP, PK_DPHILU,  // dPhiMaxChange, rt of (up - lo), dphi(up, up - lo), dphi(lo, up)
     PK_EX, PK_EY, PK_FLAGS, PK_G2,          // outer anchor module's strip-edge offset; flags; module of the outer MD
-    PK_S0, PK_S1, PK_S2, PK_S3,
+    PK_S0, PK_S1, PK_S2, PK_S3,             // dz/drt and dr3/drt of the segment; sqrt(lr3z/lrt) in float-float
     PK_N
 };
 enum : uint32_t {
@@ -643,6 +658,10 @@ struct SGV {
     float ux, uy, uz, urt, uphi, ur3;
     float dpc, dpmin, dpmax, dpminc, dpmaxc, rtseg, alphaup, dphilu, ex, ey;
     uint32_t flags;
+    // the inner role's per-segment terms (sg_pack_record): (uz - lz) / (urt -
+    // lrt), (ur3 - lr3) / (urt - lrt), and sqrt(lr3z / lrt) in float-float
+    // (NaN outside the multiple-scattering factor's fast-path range)
+    float dzdr, cosh, sqq_hi, sqq_lo;
     __device__ P3 lo() const { P3 p; p.x = lx; p.y = ly; p.z = lz; p.rt = lrt; p.phi = lphi; p.r3 = lr3; return p; }
     __device__ P3 up() const { P3 p; p.x = ux; p.y = uy; p.z = uz; p.rt = urt; p.phi = uphi; p.r3 = ur3; return p; }
 };
@@ -650,7 +669,7 @@ struct SGV {
 __device__ __forceinline__ SGV load_sgv(const float* __restrict__ pack, int64_t s) {
     const float4* q = reinterpret_cast<const float4*>(pack + s * PK_N);
     const float4 a = __ldg(q + 0), c = __ldg(q + 1), d = __ldg(q + 2), e = __ldg(q + 3);
-    const float4 f = __ldg(q + 4), g = __ldg(q + 5), h = __ldg(q + 6);
+    const float4 f = __ldg(q + 4), g = __ldg(q + 5), h = __ldg(q + 6), i = __ldg(q + 7);
     SGV v;
     v.lx = a.x; v.ly = a.y; v.lz = a.z; v.lrt = a.w;
     v.lphi = c.x; v.lr3 = c.y; v.la1 = c.z; v.ltd = c.w;
@@ -659,6 +678,7 @@ __device__ __forceinline__ SGV load_sgv(const float* __restrict__ pack, int64_t 
     v.dpc = f.x; v.dpmin = f.y; v.dpmax = f.z; v.dpminc = f.w;
     v.dpmaxc = g.x; v.rtseg = g.y; v.alphaup = g.z; v.dphilu = g.w;
     v.ex = h.x; v.ey = h.y; v.flags = __float_as_uint(h.z);
+    v.dzdr = i.x; v.cosh = i.y; v.sqq_hi = i.z; v.sqq_lo = i.w;
     return v;
 }
 
@@ -672,6 +692,7 @@ __device__ __forceinline__ SGV sgv_from(const float* p) {
     v.dpc = p[PK_DPC]; v.dpmin = p[PK_DPMIN]; v.dpmax = p[PK_DPMAX]; v.dpminc = p[PK_DPMINC];
     v.dpmaxc = p[PK_DPMAXC]; v.rtseg = p[PK_RTSEG]; v.alphaup = p[PK_ALPHAUP]; v.dphilu = p[PK_DPHILU];
     v.ex = p[PK_EX]; v.ey = p[PK_EY]; v.flags = __float_as_uint(p[PK_FLAGS]);
+    v.dzdr = p[PK_S0]; v.cosh = p[PK_S1]; v.sqq_hi = p[PK_S2]; v.sqq_lo = p[PK_S3];
     return v;
 }
 
@@ -783,6 +804,7 @@ __device__ __forceinline__ float dbeta_cut2(float dBetaRes, float dBetaMuls, flo
 struct SGOuter {
     float lrt, lz, ltd, la1, uphi;
     uint32_t flags;
+    float pvoff;  // 0.1f / lrt
 };
 __device__ __forceinline__ SGOuter load_sgo(const float* __restrict__ a, int64_t cap, int64_t t) {
     SGOuter o;
@@ -792,8 +814,13 @@ __device__ __forceinline__ SGOuter load_sgo(const float* __restrict__ a, int64_t
     o.la1 = __ldg(a + 3 * cap + t);
     o.uphi = __ldg(a + 4 * cap + t);
     o.flags = __float_as_uint(__ldg(a + 5 * cap + t));
+    o.pvoff = __ldg(a + 6 * cap + t);
     return o;
 }
+// the PV-offset term 0.1f / rtOut of the tracklet cuts (Tracklet.cc:1056 and
+// the like), precomputed for an SGOuter
+__device__ __forceinline__ float pv_off(const SGOuter& T) { return T.pvoff; }
+__device__ __forceinline__ float pv_off(const SGV& T) { return 0.1f / T.lrt; }
 
 // Tracklet algorithm ids carried between the two phases
 enum : int { kAlgoNone = 0, kAlgoBBBB = 1, kAlgoBBEE = 2, kAlgoEEEE = 3 };
@@ -817,19 +844,18 @@ __device__ __forceinline__ int tl_phaseA(const SGV& S, const TSeg& T, float& sdl
         const float zHi = zIn + (zIn + kDeltaZLum) * (rtRatio - 1.f) * (zIn < 0.f ? 1.f : dzDrtScale) + (zpitch_InLo + zpitch_OutLo);
         const float zLo = zIn + (zIn - kDeltaZLum) * (rtRatio - 1.f) * (zIn > 0.f ? 1.f : dzDrtScale) - (zpitch_InLo + zpitch_OutLo);
         if (!(zOut >= zLo && zOut <= zHi)) return kAlgoNone;
-        mulsF = muls(rtOut - rtIn, S.lr3z / rtIn, true);
+        mulsF = muls_sq(rtOut - rtIn, S.sqq_hi, S.sqq_lo, S.lr3z, rtIn);
         const float sdlMuls = mulsF * 3.f / kPtCut * 4.f;
-        const float sdlPVoff = 0.1f / rtOut;
+        const float sdlPVoff = pv_off(T);
         sdlCut = add_dsqrt(T.la1, sdlMuls * sdlMuls + sdlPVoff * sdlPVoff);
         if (!(fabsf(phi_mpi_pi(T.uphi - S.uphi)) <= sdlCut)) return kAlgoNone;
         const float drt_OutLo_InLo = rtOut - rtIn;
         const float drt_InSeg = S.urt - S.lrt;
-        const float dz_InSeg = S.uz - S.lz;
-        const float coshEta = (S.ur3 - S.lr3) / drt_InSeg;
+        const float coshEta = S.cosh;  // (S.ur3 - S.lr3) / drt_InSeg
         float dzErr = (zpitch_InLo + zpitch_OutLo) * (zpitch_InLo + zpitch_OutLo) * 2.f;
         dzErr += sdlMuls * sdlMuls * drt_OutLo_InLo * drt_OutLo_InLo / 3.f * coshEta * coshEta;
         dzErr = __fsqrt_rn(dzErr);
-        const float dzMean = dz_InSeg / drt_InSeg * drt_OutLo_InLo;
+        const float dzMean = S.dzdr * drt_OutLo_InLo;  // dz_InSeg / drt_InSeg * drt_OutLo_InLo
         const float zWindow = dzErr / drt_InSeg * drt_OutLo_InLo + (zpitch_InLo + zpitch_OutLo);
         const float zLoPointed = zIn + dzMean * (zIn > 0.f ? 1.f : dzDrtScale) - zWindow;
         const float zHiPointed = zIn + dzMean * (zIn < 0.f ? 1.f : dzDrtScale) + zWindow;
@@ -852,9 +878,9 @@ __device__ __forceinline__ int tl_phaseA(const SGV& S, const TSeg& T, float& sdl
         if (!(rtOut >= rtLo && rtOut <= rtHi)) return kAlgoNone;
         const float kZ = (zOut - zIn) / (S.uz - S.lz);
         if (!(kZ >= 0)) return kAlgoNone;
-        mulsF = muls(rtOut - rtIn, S.lr3z / rtIn, true);
+        mulsF = muls_sq(rtOut - rtIn, S.sqq_hi, S.sqq_lo, S.lr3z, rtIn);
         const float sdlMuls = mulsF * 3.f / kPtCut * 4.f;
-        const float sdlPVoff = 0.1f / rtOut;
+        const float sdlPVoff = pv_off(T);
         sdlCut = add_dsqrt(T.la1, sdlMuls * sdlMuls + sdlPVoff * sdlPVoff);
         if (!(fabsf(phi_mpi_pi(T.uphi - S.uphi)) <= sdlCut)) return kAlgoNone;
         return kAlgoBBEE;
@@ -873,13 +899,13 @@ __device__ __forceinline__ int tl_phaseA(const SGV& S, const TSeg& T, float& sdl
         if (!(rtOut >= rtLo && rtOut <= rtHi)) return kAlgoNone;
         mulsF = muls(rtOut - rtIn, 0.f, false);
         const float sdlMuls = mulsF * 3.f / kPtCut * 4.f;
-        const float sdlPVoff = 0.1f / rtOut;
+        const float sdlPVoff = pv_off(T);
         sdlCut = add_dsqrt(T.la1, sdlMuls * sdlMuls + sdlPVoff * sdlPVoff);
         if (!(fabsf(phi_mpi_pi(T.uphi - S.uphi)) <= sdlCut)) return kAlgoNone;
         if (inPS && (fs & F_UP_PS)) {
             const float drtSDIn = S.urt - S.lrt;
             const float dzSDIn = S.uz - S.lz;
-            const float coshEta = (S.ur3 - S.lr3) / drtSDIn;
+            const float coshEta = S.cosh;  // (S.ur3 - S.lr3) / drtSDIn
             const float dzOutInAbs = fabsf(zOut - zIn);
             const float multDzDr = dzOutInAbs * coshEta / (coshEta * coshEta - 1.f);
             const float kZ = (zOut - zIn) / dzSDIn;

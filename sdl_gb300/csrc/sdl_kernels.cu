@@ -777,7 +777,18 @@ __device__ __forceinline__ void sg_pack_record(const BatchDev& b, int im, int om
     v[PK_EX] = uam.edge_x; v[PK_EY] = uam.edge_y;
     v[PK_FLAGS] = __uint_as_float(fl);
     v[PK_G2] = __int_as_float(OG(b, kMD, om));
-    v[PK_S0] = v[PK_S1] = v[PK_S2] = v[PK_S3] = 0.f;
+    // the inner role's per-segment terms of phase A (the same float
+    // operations as there)
+    v[PK_S0] = (up.z - lo.z) / (up.rt - lo.rt);
+    v[PK_S1] = (up.r3 - lo.r3) / (up.rt - lo.rt);
+    const float q = v[PK_LR3Z] / lo.rt;
+    if (q > 0x1p-60f && q < 0x1p60f) {
+        const ffm::ff sq = ffm::sqrt_ff(ffm::ff{q, 0.f});
+        v[PK_S2] = sq.hi;
+        v[PK_S3] = sq.lo;
+    } else {
+        v[PK_S2] = v[PK_S3] = __int_as_float(0x7fc00000);  // NaN: muls takes its double path
+    }
 }
 
 __global__ void k_sg_pack(BatchDev b) {
@@ -793,7 +804,8 @@ __global__ void k_sg_pack(BatchDev b) {
         const int64_t C = b.obj[kSG].cap;
         const int fo[6] = {PK_LRT, PK_LZ, PK_LTD, PK_LA1, PK_UPHI, PK_FLAGS};
 #pragma unroll
-        for (int k = 0; k < 6; ++k) AT(b.sgouter, k * C + s, 6 * C) = v[fo[k]];
+        for (int k = 0; k < 6; ++k) AT(b.sgouter, k * C + s, 7 * C) = v[fo[k]];
+        AT(b.sgouter, 6 * C + s, 7 * C) = 0.1f / v[PK_LRT];  // the PV-offset term of an outer segment
         float4* dst = reinterpret_cast<float4*>(&AT(b.sgpack, s * PK_N, b.obj[kSG].cap * PK_N));
         for (int k = 0; k < PK_N / 4; ++k) dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
         // the pre-filter's feature records (inner role, outer role)

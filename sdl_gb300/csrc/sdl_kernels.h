@@ -39,8 +39,8 @@ struct BatchDev {
     int32_t* conn_pref;            // n_ev * n_conn
     int64_t* conn_sum;             // n_gm
     float* sgpack;                 // segment cap * PK_N packed records for the tracklet stage
-    float* sgouter;                // segment cap * 6, one array per field: what phase A reads of an outer
-                                   //   segment (lrt, lz, ltd, la1, uphi, flags; see SGOuter)
+    float* sgouter;                // segment cap * 7, one array per field: what phase A reads of an outer
+                                   //   segment (lrt, lz, ltd, la1, uphi, flags, 0.1/lrt; see SGOuter)
     float* sgfeat;                 // segment cap * kFeatN: the pre-filter's per-segment feature records
     float* mdpack;                 // mini-doublet cap * kMdPack: packed records for the segment stage
     uint32_t* counters;            // n_ev * 110
