@@ -305,6 +305,7 @@ int ensure_buffers(sdlg_ctx* ctx) {
     BatchDev& b = ctx->b;
     b = BatchDev{};
     b.geo.n_mod = n_mod;
+    b.geo.n_mod_inv = n_mod > 1 ? UINT64_MAX / (uint64_t)n_mod + 1 : 0;  // ceil(2^64 / n_mod)
     b.geo.n_conn = (int)ctx->conn_idx.size();
     b.geo.detid = ctx->d_detid;
     b.geo.mod = ctx->d_mod;
@@ -1326,6 +1327,7 @@ namespace sdlg {
 bool ctx_geometry(const sdlg_ctx* ctx, Geometry* g, int* device, int* n_sm) {
     if (!ctx || !ctx->have_geo) return false;
     g->n_mod = (int)ctx->detids.size();
+    g->n_mod_inv = g->n_mod > 1 ? UINT64_MAX / (uint64_t)g->n_mod + 1 : 0;  // ceil(2^64 / n_mod)
     g->n_conn = (int)ctx->conn_idx.size();
     g->detid = ctx->d_detid;
     g->mod = ctx->d_mod;

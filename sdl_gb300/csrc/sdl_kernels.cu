@@ -209,6 +209,15 @@ void scan(const BatchDev& bd, int64_t* data, const int64_t* n_ptr, int64_t cap, 
 // array sizes
 __device__ __forceinline__ int64_t H(const BatchDev& b) { return b.n_hit_cap; }
 __device__ __forceinline__ int64_t NG1(const BatchDev& b) { return (int64_t)b.n_gm + 1; }
+// event and module of a global module index g = event * n_mod + module
+// (0 <= g < 2^31): floor(g * ceil(2^64 / n) / 2^64) is floor(g / n) exactly
+// for g and n = n_mod below 2^32 (the rounding-up error is below 2^-32 < 1 / n)
+__device__ __forceinline__ int ev_of(const BatchDev& b, int64_t g) {
+    return b.geo.n_mod == 1 ? (int)g : (int)__umul64hi((unsigned long long)g, b.geo.n_mod_inv);
+}
+__device__ __forceinline__ int mod_of(const BatchDev& b, int64_t g) {
+    return (int)(g - (int64_t)ev_of(b, g) * b.geo.n_mod);
+}
 __device__ __forceinline__ int64_t NM(const BatchDev& b) { return b.geo.n_mod; }
 __device__ __forceinline__ int64_t NC(const BatchDev& b) { return b.geo.n_conn > 0 ? b.geo.n_conn : 1; }
 __device__ __forceinline__ int64_t NCP(const BatchDev& b) {
@@ -276,7 +285,7 @@ __global__ void k_hit_scatter(BatchDev b) {
         AT(b.hidx, pos, H(b)) = AT(b.in_idx, h, H(b));
         AT(b.hgm, pos, H(b)) = gm;
         // the strip shift of the mini-doublets this hit anchors
-        const int m = gm % b.geo.n_mod;
+        const int m = mod_of(b, gm);
         const ModDev& M = MOD(b, m);
         const int lmi = M.lower ? m : M.partner;
         float xa = 0.f, ya = 0.f, zn = 0.f;
@@ -312,7 +321,7 @@ __device__ __forceinline__ int64_t OFF(const BatchDev& b, int st, int64_t g) { r
 
 __device__ __forceinline__ MDView md_view(const BatchDev& b, int a) {
     const int gm = OG(b, kMD, a);
-    const ModDev* lm = &MOD(b, gm % b.geo.n_mod);
+    const ModDev* lm = &MOD(b, mod_of(b, gm));
     MDView v;
     v.m = lm;
     v.a = hit(b, md_anchor(*lm, OI(b, kMD, a), OJ(b, kMD, a)));
@@ -328,7 +337,7 @@ struct MDStage {
     static constexpr int kSt = kMD;
     __device__ static bool eval(const BatchDev& b, int gm, int64_t q, int& oi, int& oj, float* fv) {
         const int n_mod = b.geo.n_mod;
-        const int ev = gm / n_mod;
+        const int ev = ev_of(b, gm);
         const ModDev lm = MOD(b, gm - ev * n_mod);
         const int pg = ev * n_mod + lm.partner;
         const int64_t nu = AT(b.mod_hit, pg + 1, NG1(b)) - AT(b.mod_hit, pg, NG1(b));
@@ -396,7 +405,7 @@ __global__ void k_md_pack(BatchDev b) {
     const int n_mod = b.geo.n_mod;
     const int64_t n = min(OFF(b, kMD, b.n_gm), b.obj[kMD].cap);  // mini-doublets
     for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
-        const int lm = OG(b, kMD, a) % n_mod;
+        const int lm = mod_of(b, OG(b, kMD, a));
         const int anc = md_anchor(MOD(b, lm), OI(b, kMD, a), OJ(b, kMD, a));
         const P3 p = hit(b, anc);
         float4* q = reinterpret_cast<float4*>(&AT(b.mdpack, a * kMdPack, b.obj[kMD].cap * kMdPack));
@@ -407,7 +416,7 @@ __global__ void k_md_pack(BatchDev b) {
         // the outer one: the barrel cut for the layer below, the endcap strip
         // edges' phi
         const ModDev& M = MOD(b, lm);
-        const int am = AT(b.hgm, anc, H(b)) % n_mod;
+        const int am = mod_of(b, AT(b.hgm, anc, H(b)));
         float c0 = 0.f, c1 = 0.f;
         if (M.subdet == kBarrel) {
             if (M.layer >= 2) c0 = sg_barrel_cut(M.layer - 1, p.rt, AT(b.ha1, anc, H(b)));
@@ -446,7 +455,7 @@ struct SGStage {
     __device__ static bool eval(const BatchDev& b, int a, int64_t q, int& oi, int& oj, float* fv) {
         const int n_mod = b.geo.n_mod;
         const int g1 = OG(b, kMD, a);
-        const int ev = g1 / n_mod, m1 = g1 - ev * n_mod;
+        const int ev = ev_of(b, g1), m1 = g1 - ev * n_mod;
         int pref;
         const int k = conn_entry(b, ev, m1, q, pref);
         const int g2 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
@@ -505,7 +514,7 @@ struct SGLayerStage {
     __device__ static bool eval(const BatchDev& b, int a, int64_t q, int& oi, int& oj, float* fv) {
         const int n_mod = b.geo.n_mod;
         const int g1 = OG(b, kMD, a);
-        const int ev = g1 / n_mod, m1 = g1 - ev * n_mod;
+        const int ev = ev_of(b, g1), m1 = g1 - ev * n_mod;
         const int si = MOD(b, m1).layer_slot;
         int bmd = -1;
         for (int k = 0; k < 3; ++k) {
@@ -541,7 +550,7 @@ __device__ __forceinline__ int tl_outer(const BatchDev& b, int s, int64_t q) {
     const int n_mod = b.geo.n_mod;
     // module of the outer mini-doublet, from the packed segment record
     const int g2 = __float_as_int(AT(b.sgpack, (int64_t)s * PK_N + PK_G2, b.obj[kSG].cap * PK_N));
-    const int ev = g2 / n_mod, m2 = g2 - ev * n_mod;
+    const int ev = ev_of(b, g2), m2 = g2 - ev * n_mod;
     int pref;
     const int k = conn_entry(b, ev, m2, q, pref);
     const int g3 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
@@ -553,7 +562,7 @@ __device__ __forceinline__ int tl_outer(const BatchDev& b, int s, int64_t q) {
 __device__ __forceinline__ int tl_outer_layer(const BatchDev& b, int s, int64_t q) {
     const int n_mod = b.geo.n_mod;
     const int g1 = OG(b, kSG, s);
-    const int ev = g1 / n_mod;
+    const int ev = ev_of(b, g1);
     return layer_object(b, kSG, ev, tl_layer_outer(MOD(b, g1 - ev * n_mod).layer_slot), q);
 }
 
@@ -749,13 +758,13 @@ __device__ __forceinline__ void append_rec(const BatchDev& b, int st, bool pass,
 // dPhiChange, dPhiMinChange, dPhiMaxChange)
 __device__ __forceinline__ void sg_pack_record(const BatchDev& b, int im, int om, const float* f6, float* v) {
     const int n_mod = b.geo.n_mod;
-    const ModDev& ilm = MOD(b, OG(b, kMD, im) % n_mod);
-    const ModDev& olm = MOD(b, OG(b, kMD, om) % n_mod);
+    const ModDev& ilm = MOD(b, mod_of(b, OG(b, kMD, im)));
+    const ModDev& olm = MOD(b, mod_of(b, OG(b, kMD, om)));
     const int la = md_anchor(ilm, OI(b, kMD, im), OJ(b, kMD, im));
     const int ua = md_anchor(olm, OI(b, kMD, om), OJ(b, kMD, om));
     const P3 lo = hit(b, la), up = hit(b, ua);
-    const ModDev& lam = MOD(b, AT(b.hgm, la, H(b)) % n_mod);
-    const ModDev& uam = MOD(b, AT(b.hgm, ua, H(b)) % n_mod);
+    const ModDev& lam = MOD(b, mod_of(b, AT(b.hgm, la, H(b))));
+    const ModDev& uam = MOD(b, mod_of(b, AT(b.hgm, ua, H(b))));
     uint32_t fl = 0;
     fl |= lam.subdet == kBarrel ? F_LO_B : 0u;
     fl |= lam.subdet == kEndcap ? F_LO_E : 0u;
@@ -834,7 +843,7 @@ struct TCTPStage {
         const int n_mod = b.geo.n_mod;
         const int mdA = OJ(b, kSG, OJ(b, kTP, p1));
         const int gA = OG(b, kMD, mdA);
-        const int ev = gA / n_mod, mA = gA - ev * n_mod;
+        const int ev = ev_of(b, gA), mA = gA - ev * n_mod;
         int pref;
         const int k = conn_entry(b, ev, mA, q, pref);
         const int g3 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
@@ -1231,7 +1240,7 @@ __global__ void k_obj_counters(BatchDev b, int st) {
         int ev = 0, slot = 0;
         if (in) {
             v = (uint32_t)OFF(b, st, g);
-            ev = (int)(g / n_mod);
+            ev = ev_of(b, g);
             slot = MOD(b, g - (int64_t)ev * n_mod).layer_slot;
         }
         const bool act = in && v != 0;
@@ -1268,7 +1277,7 @@ __global__ void k_md_count(BatchDev b) {
         int64_t c = 0;
         int ev = 0, slot = 0;
         if (in) {
-            ev = (int)(g / n_mod);
+            ev = ev_of(b, g);
             const ModDev& m = MOD(b, g - (int64_t)ev * n_mod);
             if (m.lower && m.partner >= 0) {
                 const int64_t pg = (int64_t)ev * n_mod + m.partner;
@@ -1294,7 +1303,7 @@ __global__ void k_conn_sum(BatchDev b, int src, int cst) {
         int64_t sum = 0, cand = 0;
         int ev = 0, slot = 0;
         if (in) {
-            ev = (int)(g / n_mod);
+            ev = ev_of(b, g);
             const int m = (int)(g - (int64_t)ev * n_mod);
             const int k0 = AT(b.geo.conn_off, m, NM(b) + 1), k1 = AT(b.geo.conn_off, m + 1, NM(b) + 1);
             const int64_t pbase = (int64_t)ev * b.geo.n_conn;
@@ -1333,7 +1342,7 @@ __global__ void k_tl_count(BatchDev b) {
             c = AT(b.conn_sum, g2, b.n_gm);
             AT(b.cand[kTL], s, b.cand_cap[kTL] + 1) = c;
             const int g1 = OG(b, kSG, s);
-            ev = g1 / n_mod;
+            ev = ev_of(b, g1);
             slot = MOD(b, g1 - ev * n_mod).layer_slot;
         }
         const bool act = in && c != 0;
@@ -1349,7 +1358,7 @@ __global__ void k_sg_count_layers(BatchDev b) {
     const int64_t n = n_inner(b, kSG);
     for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
         const int g1 = OG(b, kMD, a);
-        const int ev = g1 / n_mod;
+        const int ev = ev_of(b, g1);
         const int si = MOD(b, g1 - ev * n_mod).layer_slot;
         int64_t c = 0;
         for (int k = 0; k < 3; ++k) {
@@ -1373,7 +1382,7 @@ __global__ void k_tl_count_layers(BatchDev b) {
         int ev = 0, slot = 0;
         if (in) {
             const int g1 = OG(b, kSG, s);
-            ev = g1 / n_mod;
+            ev = ev_of(b, g1);
             slot = MOD(b, g1 - ev * n_mod).layer_slot;
             const int so = tl_layer_outer(slot);
             c = so >= 0 ? layer_count(b, kSG, ev, so) : 0;
@@ -1412,7 +1421,7 @@ __global__ void k_tp_count(BatchDev b) {
     const int64_t n = n_inner(b, kTP);
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
         const int g1 = OG(b, kSG, s);
-        const int ev = g1 / n_mod, m1 = g1 - ev * n_mod;
+        const int ev = ev_of(b, g1), m1 = g1 - ev * n_mod;
         const int g2 = OG(b, kMD, OJ(b, kSG, s));
         const int m2 = g2 - ev * n_mod;
         int mult = 0;
@@ -1429,10 +1438,10 @@ __global__ void k_tc_count(BatchDev b) {
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
         int64_t c = 0;
         const int g1 = OG(b, kTL, t);
-        const ModDev& m1 = MOD(b, g1 % n_mod);
+        const ModDev& m1 = MOD(b, mod_of(b, g1));
         if (m1.subdet == kBarrel && m1.layer == 1) {
             const int g3 = OG(b, kSG, OJ(b, kTL, t));
-            const ModDev& m3 = MOD(b, g3 % n_mod);
+            const ModDev& m3 = MOD(b, mod_of(b, g3));
             if (m3.subdet == kBarrel && m3.layer == 3) c = join_n(b, OI(b, kSG, OJ(b, kTL, t)));
         }
         AT(b.cand[kTC], t, b.cand_cap[kTC] + 1) = c;
@@ -1455,7 +1464,7 @@ __global__ void k_tl_count_nav(BatchDev b) {
             for (int64_t k = 0; k < nc; ++k) c += join_n(b, OJ(b, kSG, join_obj(b, m, k)));
             AT(b.cand[kTL], s, b.cand_cap[kTL] + 1) = c;
             const int g1 = OG(b, kSG, s);
-            ev = g1 / n_mod;
+            ev = ev_of(b, g1);
             slot = MOD(b, g1 - ev * n_mod).layer_slot;
         }
         const bool act = in && c != 0;
@@ -1482,7 +1491,7 @@ __global__ void k_tc_count_tl(BatchDev b) {
         int ev = 0, slot = 0;
         if (in) {
             const int gA2 = OG(b, kMD, OJ(b, kSG, OI(b, kTL, t)));
-            ev = gA2 / n_mod;
+            ev = ev_of(b, gA2);
             const int mA2 = gA2 - ev * n_mod;
             cref = none ? 0 : AT(b.conn_sum, gA2, b.n_gm);
             const int mB = OI(b, kSG, OJ(b, kTL, t));
@@ -1520,7 +1529,7 @@ __global__ void k_tc_count_tp(BatchDev b) {
             }
             AT(b.cand[kTC], p, b.cand_cap[kTC] + 1) = e;
             const int g1 = OG(b, kTP, p);
-            ev = g1 / n_mod;
+            ev = ev_of(b, g1);
             slot = MOD(b, g1 - ev * n_mod).layer_slot;
         }
         const bool act = in && c != 0;

@@ -36,6 +36,7 @@ struct Objs {
 
 struct Geometry {
     int n_mod;
+    uint64_t n_mod_inv;      // ceil(2^64 / n_mod) (n_mod > 1): global module index -> event by a multiply-high
     int n_conn;
     const uint32_t* detid;   // sorted
     const ModDev* mod;
