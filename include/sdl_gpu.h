@@ -138,6 +138,19 @@ int sdlg_get_counts(sdlg_ctx* ctx, int64_t event, int64_t* out5);
  * out (capacity `cap` tuples); *n_out receives the number of tuples. */
 int sdlg_get_objects(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int64_t cap, int64_t* n_out);
 
+/* Debug dump of the tracklets' final cut variables, as the reference records
+ * them in each Tracklet's recovars map (Tracklet.cc:1440-1495 and the same
+ * block of the BBEE and EEEE algorithms): 15 floats per tracklet of the event
+ * (event < 0: all), in the row order of sdlg_get_objects(stage 2):
+ * betaIn, betaInRHmin, betaInRHmax, betaOut, betaOutRHmin, betaOutRHmax,
+ * betaAv, pt_beta, dBeta, dBetaCut2, dBetaLum2, dBetaMuls, dBetaRes, dBetaRIn2,
+ * dBetaROut2.  Recomputed on demand from the last run's segments.  As in the
+ * reference, BBEE tracklets report -999 (their algorithm records none of
+ * these), and values that pass through the reference's float std::asin can
+ * differ from it in the last bit (glibc's asinf is not always correctly
+ * rounded; the cut decisions here use the correctly rounded value). */
+int sdlg_get_tracklet_vars(sdlg_ctx* ctx, int64_t event, float* out, int64_t cap, int64_t* n_out);
+
 /* The reference's per-layer counters for one event (Event.cc:1064-1344):
  * 5 stages x {candidates, objects} x {barrel layers 1-6, endcap layers 1-5}. */
 int sdlg_get_counters(sdlg_ctx* ctx, int64_t event, uint32_t* out110);

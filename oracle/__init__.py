@@ -134,8 +134,10 @@ def read_dump(path):
     return out, cnt, sec
 
 
-def run_reference(det, ev, mode: str = "map", workdir: str | None = None):
-    """Runs the compiled reference (oracle/_ref/ref_driver) on one event."""
+def run_reference(det, ev, mode: str = "map", workdir: str | None = None, tl_vars: bool = False):
+    """Runs the compiled reference (oracle/_ref/ref_driver) on one event;
+    with tl_vars, also returns the tracklets' final recovars (n_tl x 15, rows
+    as the tracklet tuples)."""
     exe = os.path.join(HERE, "_ref", "ref_driver")
     if not os.path.exists(exe):
         raise FileNotFoundError("reference driver not built (make -C oracle ref)")
@@ -143,9 +145,15 @@ def run_reference(det, ev, mode: str = "map", workdir: str | None = None):
         paths = det.write_files(d)
         hb = os.path.join(d, "hits.bin")
         ob = os.path.join(d, "out.bin")
+        vb = os.path.join(d, "vars.bin")
         ev.write_bin(hb)
-        subprocess.run([exe, *paths, hb, ob, mode], check=True, capture_output=True)
-        return read_dump(ob)
+        subprocess.run([exe, *paths, hb, ob, mode] + ([vb] if tl_vars else []), check=True, capture_output=True)
+        res = read_dump(ob)
+        if not tl_vars:
+            return res
+        v = np.fromfile(vb, dtype=np.float32).reshape(-1, 15)
+        assert v.shape[0] == res[0][2].shape[0]
+        return res + (v,)
 
 
 def canon(t: np.ndarray) -> np.ndarray:
@@ -155,6 +163,12 @@ def canon(t: np.ndarray) -> np.ndarray:
         return t
     order = np.lexsort(t.T[::-1])
     return t[order]
+
+
+def canon_order(t: np.ndarray) -> np.ndarray:
+    """The row order canon() applies (to carry per-row data along)."""
+    t = np.ascontiguousarray(t, dtype=np.int32)
+    return np.lexsort(t.T[::-1]) if t.shape[0] else np.zeros(0, dtype=np.int64)
 
 
 def digest(t: np.ndarray) -> str:

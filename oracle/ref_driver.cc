@@ -15,6 +15,7 @@
 // load the three geometry singletons, add hits, then the create* stages.
 #include <chrono>
 #include <cstdint>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -108,11 +109,23 @@ int main(int argc, char** argv) {
     else ev.createTrackCandidates();
     t[4] = now() - t0;
 
+    // the tracklets' final recovars (Tracklet.cc:1440-1495) in tracklet order
+    static const char* const kVars[15] = {"betaIn", "betaInRHmin", "betaInRHmax", "betaOut", "betaOutRHmin",
+                                          "betaOutRHmax", "betaAv", "pt_beta", "dBeta", "dBetaCut2", "dBetaLum2",
+                                          "dBetaMuls", "dBetaRes", "dBetaRIn2", "dBetaROut2"};
+    std::vector<float> tlvars;
     std::vector<int32_t> md, sg, tl, tp, tc;
     for (SDL::Layer* L : ev.getLayerPtrs()) {
         for (auto* o : L->getMiniDoubletPtrs()) pushMD(md, o);
         for (auto* o : L->getSegmentPtrs()) pushSG(sg, o);
-        for (auto* o : L->getTrackletPtrs()) pushTLB(tl, o);
+        for (auto* o : L->getTrackletPtrs()) {
+            pushTLB(tl, o);
+            const auto& rv = o->getRecoVars();
+            for (const char* k : kVars) {
+                auto it = rv.find(k);
+                tlvars.push_back(it == rv.end() ? std::nanf("") : it->second);
+            }
+        }
         for (auto* o : L->getTripletPtrs()) pushTLB(tp, o);
         for (auto* o : L->getTrackCandidatePtrs()) {
             pushTLB(tc, o->innerTrackletBasePtr());
@@ -149,6 +162,12 @@ int main(int argc, char** argv) {
     for (unsigned i = 0; i < 5; ++i) cnt.push_back(ev.getNumberOfTrackCandidatesByLayerEndcap(i));
     fwrite(cnt.data(), 4, cnt.size(), fo);
     fwrite(t, 8, 5, fo);
+    if (argc > 7) {  // optional: the tracklet recovars, 15 floats per tracklet of stage 2
+        FILE* fv = std::fopen(argv[7], "wb");
+        if (!fv) { std::perror("vars"); return 1; }
+        fwrite(tlvars.data(), 4, tlvars.size(), fv);
+        std::fclose(fv);
+    }
     std::fclose(fo);
     std::fprintf(stderr, "ref: hits %lld MD %zu SG %zu TL %zu TP %zu TC %zu | s: %.3f %.3f %.3f %.3f %.3f\n",
                  (long long)n, md.size() / 2, sg.size() / 4, tl.size() / 8, tp.size() / 8, tc.size() / 16,

@@ -35,6 +35,9 @@ FLAG_MLP = 16        # learned pre-filter ahead of the tracklet cuts
 FLAG_TL_NAV = 32     # Event::createTrackletsViaNavigation instead of createTrackletsWithModuleMap
 FLAG_TC_FROM_TL = 64   # Event::createTrackCandidatesFromTracklets instead of createTrackCandidates
 FLAG_TC_FROM_TP = 128  # Event::createTrackCandidatesFromTriplets instead of createTrackCandidates
+# the columns of Chain.tracklet_vars (the reference's Tracklet recovars keys)
+TL_VAR_NAMES = ("betaIn", "betaInRHmin", "betaInRHmax", "betaOut", "betaOutRHmin", "betaOutRHmax", "betaAv", "pt_beta",
+                "dBeta", "dBetaCut2", "dBetaLum2", "dBetaMuls", "dBetaRes", "dBetaRIn2", "dBetaROut2")
 MLP_FEATURES = 12
 MLP_PARAMS = 5057
 
@@ -60,6 +63,7 @@ def lib():
         L.sdlg_last_error.restype = ctypes.c_char_p
         L.sdlg_geometry_load_files.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
         L.sdlg_geometry_upload.argtypes = [vp, i64, vp, vp, i64, vp, vp, i64, vp, vp, vp]
+        L.sdlg_get_tracklet_vars.argtypes = [vp, i64, vp, i64, vp]
         L.sdlg_geometry_convert.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
         L.sdlg_geometry_load_binary.argtypes = [vp, ctypes.c_char_p]
         L.sdlg_num_modules.argtypes = [vp]
@@ -224,6 +228,16 @@ class Chain:
         if n.value:
             self._ck(lib().sdlg_get_objects(self.h, stage, event, out.ctypes.data, n.value, ctypes.byref(n)))
         return out[:n.value]
+
+    def tracklet_vars(self, event: int = -1) -> np.ndarray:
+        """The tracklets' final cut variables (rows as objects(2, event), columns
+        TL_VAR_NAMES), as the reference's Tracklet recovars."""
+        n = ctypes.c_int64()
+        self._ck(lib().sdlg_get_tracklet_vars(self.h, event, None, 0, ctypes.byref(n)))
+        out = np.empty((n.value, len(TL_VAR_NAMES)), dtype=np.float32)
+        if n.value:
+            self._ck(lib().sdlg_get_tracklet_vars(self.h, event, out.ctypes.data, n.value, ctypes.byref(n)))
+        return out
 
     def counters(self, event: int = 0) -> np.ndarray:
         out = np.zeros(110, dtype=np.uint32)

@@ -984,6 +984,26 @@ int sdlg_get_objects(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int6
     return SDLG_OK;
 }
 
+int sdlg_get_tracklet_vars(sdlg_ctx* ctx, int64_t event, float* out, int64_t cap, int64_t* n_out) {
+    if (!ctx || !n_out || cap < 0) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    int64_t first, n;
+    int rc = event_range(ctx, kTL, event, &first, &n);
+    if (rc) return rc;
+    *n_out = n;
+    if (n == 0 || !out) return SDLG_OK;  // a NULL out is a size query
+    if (cap < n) return fail(ctx, SDLG_ERR_ARG, "output capacity %lld < %lld tracklets", (long long)cap, (long long)n);
+    const size_t bytes = (size_t)n * 15 * sizeof(float);
+    float* tmp = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&tmp, bytes, ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "cudaMallocAsync: %s", cudaGetErrorString(e));
+    launch_tl_vars(ctx->b, first, n, tmp, ctx->stream);
+    CK(cudaMemcpyAsync(out, tmp, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(tmp, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SDLG_OK;
+}
+
 int sdlg_get_counters(sdlg_ctx* ctx, int64_t event, uint32_t* out110) {
     if (!ctx || !out110 || event < 0 || event >= ctx->n_ev) return SDLG_ERR_ARG;
     if (!ctx->ran) return fail(ctx, SDLG_ERR_NO_EVENTS, "chain not run");

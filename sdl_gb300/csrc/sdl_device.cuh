@@ -1009,8 +1009,20 @@ static __device__ __noinline__ bool tl_phaseB1(int algo, const float* __restrict
 // BBBB only, kB2Others: BBEE and EEEE), so that a kernel running one group
 // keeps only that code resident.
 enum : int { kB2All = 0, kB2BBBB = 1, kB2Others = 2 };
+// The tracklet's final cut variables as the reference records them
+// (Tracklet.cc:1440-1495 and the same block of the other algorithms), in the
+// order of the kTLVar* names
+enum : int {
+    kTLVarBetaIn, kTLVarBetaInRHmin, kTLVarBetaInRHmax, kTLVarBetaOut, kTLVarBetaOutRHmin, kTLVarBetaOutRHmax,
+    kTLVarBetaAv, kTLVarPtBeta, kTLVarDBeta, kTLVarDBetaCut2, kTLVarDBetaLum2, kTLVarDBetaMuls, kTLVarDBetaRes,
+    kTLVarDBetaRIn2, kTLVarDBetaROut2, kTLVarN
+};
+
+// rec (optional, kTLVarN floats): the final cut variables of a candidate
+// that reaches the deltaBeta cut
 template <int kSet>
-__device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV& T, float mulsF, bool nm1) {
+__device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV& T, float mulsF, bool nm1,
+                                               float* rec = nullptr) {
     if (kSet == kB2BBBB) algo = kAlgoBBBB;
     if (kSet == kB2Others && algo == kAlgoBBBB) return false;
     const float pt_betaMax = 7.0f;
@@ -1111,6 +1123,13 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
     const float dBetaRes = 0.02f / fmin_ref(sdOut_d, sdIn_d);
     const float dBetaCut2 = dbeta_cut2(dBetaRes, dBetaMuls, dBetaLum2, dBetaROut2, betaInRHmin, betaInRHmax, betaOutRHmin, betaOutRHmax);
     const float dBeta = betaIn - betaOut;
+    if (rec) {
+        rec[kTLVarBetaIn] = betaIn; rec[kTLVarBetaInRHmin] = betaInRHmin; rec[kTLVarBetaInRHmax] = betaInRHmax;
+        rec[kTLVarBetaOut] = betaOut; rec[kTLVarBetaOutRHmin] = betaOutRHmin; rec[kTLVarBetaOutRHmax] = betaOutRHmax;
+        rec[kTLVarBetaAv] = betaAv; rec[kTLVarPtBeta] = pt_beta; rec[kTLVarDBeta] = dBeta;
+        rec[kTLVarDBetaCut2] = dBetaCut2; rec[kTLVarDBetaLum2] = dBetaLum2; rec[kTLVarDBetaMuls] = dBetaMuls;
+        rec[kTLVarDBetaRes] = dBetaRes; rec[kTLVarDBetaRIn2] = 0.f; rec[kTLVarDBetaROut2] = dBetaROut2;
+    }
     return (dBeta * dBeta <= dBetaCut2) || nm1;
 }
 template <int kSet>

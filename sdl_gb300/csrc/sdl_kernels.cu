@@ -1872,6 +1872,37 @@ void launch_tl_collect(const BatchDev& b, const MlpCollect& c, cudaStream_t s) {
     k_tl_collect<<<b.n_sm * 8, 256, 0, s>>>(b, c);
 }
 
+// the final cut variables of tracklets [first, first + n) (kTLVarN floats
+// each, NaN for a pair phase A does not accept): phase A for the algorithm
+// and the factors, then phase B2 with its record.  The reference's BBEE
+// algorithm records none of them (Tracklet.cc:1540-2016 only resets them to
+// -999 at its start), so BBEE tracklets report -999 as the reference does.
+__global__ void k_tl_vars(BatchDev b, int64_t first, int64_t n, float* out) {
+    const bool nm1 = (b.flags & kFlagTLNm1) != 0;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t o = first + k;
+        const SGV S = load_sgv(b.sgpack, OI(b, kTL, o));
+        const SGV T = load_sgv(b.sgpack, OJ(b, kTL, o));
+        float cut, muls, rec[kTLVarN];
+#pragma unroll
+        for (int j = 0; j < kTLVarN; ++j) rec[j] = __int_as_float(0x7fc00000);
+        const int algo = tl_phaseA(S, T, cut, muls);
+        if (algo == kAlgoBBEE) {
+#pragma unroll
+            for (int j = 0; j < kTLVarN; ++j) rec[j] = -999.f;
+        } else if (algo != kAlgoNone) {
+            (void)tl_phaseB2_sgv<kB2All>(algo, S, T, muls, nm1, rec);
+        }
+#pragma unroll
+        for (int j = 0; j < kTLVarN; ++j) out[k * kTLVarN + j] = rec[j];
+    }
+}
+
+void launch_tl_vars(const BatchDev& b, int64_t first, int64_t n, float* out, cudaStream_t s) {
+    if (n <= 0) return;
+    k_tl_vars<<<grid_for(n, 128, b.n_sm * 8), 128, 0, s>>>(b, first, n, out);
+}
+
 void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s) {
     if (n <= 0) return;
     k_materialize<<<grid_for(n, 256, b.n_sm * 16), 256, 0, s>>>(b, st, first, n, out);

@@ -109,6 +109,8 @@ void launch_tl_collect(const BatchDev& b, const MlpCollect& c, cudaStream_t s);
 // self-check of the float-float fast paths (out[8]: see k_math_check)
 void launch_math_check(int fn, int exhaustive, unsigned long long start, long long n, unsigned long long seed,
                        unsigned long long* out, int n_sm, cudaStream_t s);
+// final cut variables of tracklets [first, first + n) (15 floats each, the kTLVar* order)
+void launch_tl_vars(const BatchDev& b, int64_t first, int64_t n, float* out, cudaStream_t s);
 // hit-index tuples of stage st for objects [first, first + n) into out (width 2/4/8/8/16)
 void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s);
 

@@ -45,7 +45,7 @@ CASES = [
 def one(case):
     name, wl, seed, pu, mode, full = case
     det, ev = synth.workload_event(wl, seed, pu=pu or 200.0)
-    out, cnt, sec = oracle.run_reference(det, ev, mode=mode)
+    out, cnt, sec, tlv = oracle.run_reference(det, ev, mode=mode, tl_vars=True)
     meta = {
         "name": name, "workload": wl, "seed": seed, "pu": pu, "mode": mode,
         "n_hits": len(ev), "event_fingerprint": ev.fingerprint(), "geometry_fingerprint": det.fingerprint(),
@@ -53,8 +53,10 @@ def one(case):
         "counters": [int(v) for v in cnt], "reference_seconds": [float(s) for s in sec],
     }
     if full:
+        # the tracklets' final recovars, rows in the canonical tracklet order
         np.savez_compressed(os.path.join(HERE, name + ".npz"),
-                            **{oracle.STAGES[s]: oracle.canon(out[s]) for s in range(5)})
+                            **{oracle.STAGES[s]: oracle.canon(out[s]) for s in range(5)},
+                            tl_vars=tlv[oracle.canon_order(out[2])])
     with open(os.path.join(HERE, name + ".json"), "w") as f:
         json.dump(meta, f, indent=1)
     return name, meta["counts"], sum(sec)
