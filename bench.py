@@ -277,6 +277,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--plain-only", action="store_true",
                     help="time only the plain batched chain (a short run to profile its kernels)")
+    ap.add_argument("--mlp-only", action="store_true",
+                    help="time only the pre-filtered batched chain (a short run to profile its kernels)")
     a = ap.parse_args()
     a.warmup = max(a.warmup, 3)
     rank, world, local, pg = dist()
@@ -306,17 +308,23 @@ def main():
     ch.mlp_set_params(params, thr)
     flush = L2Flush(local)
 
-    if a.plain_only:
+    if a.plain_only or a.mlp_only:
+        fl = FLAG_MLP if a.mlp_only else 0
         ch.set_events(batch)
-        tuned_plain = ch.autotune(4, 0)
+        tuned_plain = ch.autotune(4, fl)
         for _ in range(a.warmup):
-            ch.run(4, 0)
-        p_ms, p_stage, _, p_pass = timed_runs(ch, 0, a.steps, flush)
+            ch.run(4, fl)
+        p_ms, p_stage, _, p_pass = timed_runs(ch, fl, a.steps, flush)
         if rank == 0:
-            print(json.dumps({"workload": "plain batched chain, %d events of PU uniform in 150-300" % len(batch),
-                              "ms_per_step": round(statistics.fmean(p_ms), 3), "tuned": tuned_plain,
-                              "stage_ms": [round(float(v), 3) for v in np.mean(np.array(p_stage), axis=0)],
-                              "tl_passes_ms": [round(float(v), 3) for v in np.mean(np.array(p_pass), axis=0)]}))
+            out = {"workload": "%s batched chain, %d events of PU uniform in 150-300"
+                               % ("pre-filtered" if fl else "plain", len(batch)),
+                   "ms_per_step": round(statistics.fmean(p_ms), 3), "tuned": tuned_plain,
+                   "stage_ms": [round(float(v), 3) for v in np.mean(np.array(p_stage), axis=0)],
+                   "tl_passes_ms": [round(float(v), 3) for v in np.mean(np.array(p_pass), axis=0)],
+                   "objects": [int(v) for v in ch.counts(-1)], "global_modules": len(batch) * ch.num_modules}
+            if fl:
+                out["prefilter"] = ch.mlp_stats()
+            print(json.dumps(out))
         ch.close()
         return
 
@@ -421,25 +429,28 @@ def main():
                     "tl_kernel_ms": round(statistics.fmean(s_tl), 4)}
 
     # ---- roofline of the dominant kernel of the headline run -----------------
-    # k_tl_enum_a (tracklet enumeration + the float cuts, a third of the step):
-    # algorithmic bytes = each segment's record as inner segment (112 B), its
-    # six outer-role fields (24 B) and its candidate offset (8 B) read once +
-    # each phase-A survivor's entry written once (20 B)
+    # k_tl_enum_tiles (tracklet enumeration in module-pair tiles + the float
+    # cuts, the largest kernel of the step): algorithmic bytes = each
+    # segment's record as inner segment (112 B), its seven outer-role fields
+    # (28 B) and its entry in the index of segments by outer module (4 B) read
+    # once + each global module's tile offset, segment offset and connection
+    # sum (24 B) read once + each phase-A survivor's entry written once (16 B)
     hbm, tflops, src = peaks()
     pf = np.mean(np.array(pf_ms), axis=0)
     fc_mean, pf_mean, ex_mean = float(pf[0]), float(pf[1]), float(pf[2])
     n_sg = int(n_pruned[1])
-    en_bytes = (112 + 24 + 8) * n_sg + 20 * mstats["scored"]
+    n_gm = len(batch) * ch.num_modules
+    en_bytes = (112 + 28 + 4) * n_sg + 24 * n_gm + 16 * mstats["scored"]
     en_achieved = en_bytes / (fc_mean * 1e-3) / 1e9
     tr = ncu_traffic("tl_enum_traffic.json")
     en_traffic = None
     if tr and tr.get("traffic_per_algorithmic_byte"):
         en_traffic = int(en_bytes * float(tr["traffic_per_algorithmic_byte"]))
     # k_tl_prefilter (the network over the phase-A survivor list): algorithmic
-    # bytes = each survivor entry read once (20 B) + each segment's feature
-    # record read once (64 B) + each kept entry written once (20 B); tensor
+    # bytes = each survivor entry read once (16 B) + each segment's feature
+    # record read once (64 B) + each kept entry written once (16 B); tensor
     # work = the network's MMAs per scored candidate
-    alg_bytes = 20 * mstats["scored"] + 64 * n_sg + 20 * mstats["kept"]
+    alg_bytes = 16 * mstats["scored"] + 64 * n_sg + 16 * mstats["kept"]
     achieved = alg_bytes / (pf_mean * 1e-3) / 1e9
     tr = ncu_traffic("tl_prefilter_traffic.json")
     traffic = None
@@ -448,7 +459,7 @@ def main():
     mma_tflops = mstats["scored"] * MLP_FLOPS_PER_CANDIDATE / (pf_mean * 1e-3) / 1e12
     roofline = {"bound": "hbm", "achieved": round(en_achieved, 3), "peak": hbm, "unit": "GB/s",
                 "frac": round(en_achieved / hbm, 6), "traffic": en_traffic, "peak_source": src,
-                "kernel": "k_tl_enum_a (tracklet candidate enumeration and the float cuts)",
+                "kernel": "k_tl_enum_tiles (tracklet candidate enumeration in module-pair tiles and the float cuts)",
                 "kernel_ms": round(fc_mean, 3), "algorithmic_bytes": en_bytes,
                 "note": "issue-bound candidate evaluation (profiles/tl_kernels_ncu.md); HBM bytes are small by construction",
                 "prefilter": {"kernel": "k_tl_prefilter (tensor-core pre-filter of the candidates through the float cuts)",

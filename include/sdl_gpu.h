@@ -192,6 +192,14 @@ int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3);
  * and tan(x) / x (the hits' tan of their asin angle). */
 int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64_t n, uint64_t seed, uint64_t* out8);
 
+/* Self-check of the tracklet stage's single-precision phase-A decision
+ * (no counterpart in the reference): after a run through the tracklet stage,
+ * every tracklet candidate of the batch is judged both by the fast decision
+ * and by the exact float cuts.  out4: candidates, candidates the fast
+ * decision settled, candidates it left to the exact cuts, and settled
+ * candidates whose decision differs from the exact one (must be 0). */
+int sdlg_tl_phase_a_check(sdlg_ctx* ctx, uint64_t* out4);
+
 /* Number of kernels one run of the chain launches (as last enqueued). */
 int64_t sdlg_last_launches(const sdlg_ctx* ctx);
 

@@ -79,6 +79,7 @@ def lib():
         L.sdlg_last_kernel_times.argtypes = [vp, vp]
         L.sdlg_last_tl_pass_times.argtypes = [vp, vp]
         L.sdlg_math_check.argtypes = [vp, i32, i32, ctypes.c_uint64, i64, ctypes.c_uint64, vp]
+        L.sdlg_tl_phase_a_check.argtypes = [vp, vp]
         L.sdlg_autotune.argtypes = [vp, i32, i32, vp]
         L.sdlg_last_launches.argtypes = [vp]
         L.sdlg_last_launches.restype = i64
@@ -374,6 +375,14 @@ class Chain:
                                        out.ctypes.data))
         return {"answered": int(out[0]), "mismatches": int(out[1]),
                 "first": [int(v) for v in out[3:8]] if out[2] else None}
+
+    def tl_phase_a_check(self) -> dict:
+        """Self-check of the tracklet stage's single-precision phase-A decision
+        over the last run's candidates: how many it settled, how many it left
+        to the exact float cuts, and how many it settled differently (0)."""
+        out = np.zeros(4, dtype=np.uint64)
+        self._ck(lib().sdlg_tl_phase_a_check(self.h, out.ctypes.data))
+        return {"candidates": int(out[0]), "settled": int(out[1]), "exact": int(out[2]), "mismatches": int(out[3])}
 
     def mlp_stats(self) -> dict:
         """Pre-filter counts of the last run with FLAG_MLP: tracklet candidates,

@@ -353,15 +353,14 @@ int ensure_buffers(sdlg_ctx* ctx) {
     b.cand_cap[kTC] = std::max(ctx->cap_obj[kTL], ctx->cap_obj[kTP]);  // tracklets, or triplets (SDLG_FLAG_TC_FROM_TP)
     for (int s = 0; s < kNumStages; ++s) AL(b.cand[s], b.cand_cap[s] + 1);
     AL(b.conn_pref, std::max<int64_t>(1, ctx->n_ev * (int64_t)ctx->conn_idx.size()));
+    AL(b.conn_first, std::max<int64_t>(1, ctx->n_ev * (int64_t)ctx->conn_idx.size()));
     AL(b.conn_sum, n_gm);
     b.bucket_cap = (int64_t)1 << 24;  // covers 2^32 candidates of one stage
     AL(b.bucket, b.bucket_cap);
     b.kept_cap = ctx->cap_kept;
     AL(b.n_kept, 1);
     AL(b.passa, b.kept_cap);
-    AL(b.passa_muls, b.kept_cap);
     AL(b.kept, b.kept_cap);
-    AL(b.kept_muls, b.kept_cap);
     AL(b.n_kept2, 1);
     AL(b.pb, b.kept_cap);
     AL(b.n_pb, 2);
@@ -383,6 +382,12 @@ int ensure_buffers(sdlg_ctx* ctx) {
     AL(b.joff2, ctx->cap_obj[kMD] + 1);
     AL(b.jcur2, ctx->cap_obj[kMD]);
     AL(b.jidx2, ctx->cap_obj[kTP]);
+    AL(b.eoff, n_gm + 1);
+    AL(b.ecur, n_gm);
+    AL(b.eidx, ctx->cap_obj[kSG]);
+    AL(b.toff, n_gm + 1);
+    b.tile_cap = 2 * std::max<int64_t>(ctx->cap_obj[kSG], n_gm);
+    AL(b.tile_gm, b.tile_cap);
 #undef AL
     CK(cudaMemcpyAsync(b.n_gm_dev, &n_gm, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
@@ -1001,6 +1006,24 @@ int sdlg_get_tracklet_vars(sdlg_ctx* ctx, int64_t event, float* out, int64_t cap
     CK(cudaMemcpyAsync(out, tmp, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaFreeAsync(tmp, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return SDLG_OK;
+}
+
+int sdlg_tl_phase_a_check(sdlg_ctx* ctx, uint64_t* out4) {
+    if (!ctx || !out4) return SDLG_ERR_ARG;
+    if (!ctx->ran || ctx->last_stop < kTL) return fail(ctx, SDLG_ERR_ARG, "run the chain through the tracklet stage first");
+    cudaSetDevice(ctx->device);
+    unsigned long long* d = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&d, 4 * sizeof(unsigned long long), ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "cudaMallocAsync: %s", cudaGetErrorString(e));
+    CK(cudaMemsetAsync(d, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    launch_tl_quick_check(ctx->b, d, ctx->stream);
+    CK(cudaGetLastError());
+    unsigned long long h[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(d, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int k = 0; k < 4; ++k) out4[k] = h[k];
     return SDLG_OK;
 }
 

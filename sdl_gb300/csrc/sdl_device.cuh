@@ -923,6 +923,152 @@ __device__ __forceinline__ int tl_phaseA(const SGV& S, const TSeg& T, float& sdl
     return kAlgoNone;
 }
 
+// The two quantities phase A hands to phase B for a candidate it accepts
+// with algorithm algo: the multiple-scattering factor and the width of the
+// phi cut (Tracklet.cc:1049-1057, 1669-1677, 2127-2135), exactly as
+// tl_phaseA computes them.
+template <class TSeg>
+__device__ __forceinline__ void tl_cut_values(int algo, const SGV& S, const TSeg& T, float& sdlCut, float& mulsF) {
+    const float rtIn = S.lrt, rtOut = T.lrt;
+    mulsF = algo == kAlgoEEEE ? muls(rtOut - rtIn, 0.f, false) : muls_sq(rtOut - rtIn, S.sqq_hi, S.sqq_lo, S.lr3z, rtIn);
+    const float sdlMuls = mulsF * 3.f / kPtCut * 4.f;
+    const float sdlPVoff = pv_off(T);
+    sdlCut = add_dsqrt(T.la1, sdlMuls * sdlMuls + sdlPVoff * sdlPVoff);
+}
+
+// ---- phase A's decision alone, from single-precision approximations of the
+// multiple-scattering factor and of the quantities built on it (the phi-cut
+// width, the pointed z window of BBBB, the pointed rt window of EEEE with PS
+// inner modules).  Everything else is the exact float arithmetic of
+// tl_phaseA.  The approximation of the factor, 0.015 sqrt(0.1 + 0.004 d) [x
+// sqrt(q)] with sqrt(u) = u * rsqrtf(u) (rsqrtf: at most 2 ulp), is within
+// 11 * 2^-24 of the exact float, and every quantity compared is then within
+// 2^-24 * 50 * (the sum of the magnitudes of its terms) of its exact value.
+// A comparison is decided here only when it holds by kQuickMargin times that
+// sum (2^-16: over 5 times the bound); otherwise, and for NaNs or the
+// exact functions' fallback ranges, the result is kAlgoUnsure and the caller
+// runs tl_phaseA.  Returns the algorithm, kAlgoNone or kAlgoUnsure.
+constexpr int kAlgoUnsure = -1;
+constexpr float kQuickMargin = 0x1p-16f;
+
+// sdlMuls = mulsF * 3 / ptCut * 4 from the approximate factor (NaN when d is
+// outside the exact function's fast range or sq is NaN)
+__device__ __forceinline__ float sdl_muls_quick(float d, float sq) {
+    if (!(d >= 0.f && d < 1e4f)) return __int_as_float(0x7fc00000);
+    const float u = __fadd_rn(0.1f, __fmul_rn(d, 0.004f));
+    const float m = __fmul_rn(__fmul_rn(0.015f, __fmul_rn(u, rsqrtf(u))), sq);
+    return m * 3.f / kPtCut * 4.f;
+}
+// |dphi| <= la1 + sqrt(sdlMuls^2 + pvoff^2): 1 holds, 0 fails, -1 not decided
+__device__ __forceinline__ int phi_cut_quick(float adphi, float la1, float sdlMuls, float pvoff) {
+    const float y = sdlMuls * sdlMuls + pvoff * pvoff;
+    if (!(y > 0x1p-100f && y < 0x1p100f)) return -1;
+    const float r = __fmul_rn(y, rsqrtf(y));
+    const float c = la1 + r;
+    const float m = kQuickMargin * (fabsf(la1) + r);
+    if (adphi > c + m) return 0;
+    if (adphi < c - m) return 1;
+    return -1;
+}
+// lo <= v <= hi with both bounds within m of their exact values
+__device__ __forceinline__ int window_quick(float v, float lo, float hi, float m) {
+    if (v < lo - m || v > hi + m) return 0;
+    if (v >= lo + m && v <= hi - m) return 1;
+    return -1;
+}
+
+template <class TSeg>
+__device__ __forceinline__ int tl_phaseA_quick(const SGV& S, const TSeg& T) {
+    const uint32_t fs = S.flags, ft = T.flags;
+    const bool b1 = fs & F_LO_B, b2 = fs & F_UP_B, b3 = ft & F_LO_B, b4 = ft & F_UP_B;
+    const bool e1 = fs & F_LO_E, e2 = fs & F_UP_E, e3 = ft & F_LO_E, e4 = ft & F_UP_E;
+    const float rtIn = S.lrt, rtOut = T.lrt, zIn = S.lz, zOut = T.lz;
+    if (b1 && b2 && b3 && (b4 || e4)) {
+        const float zpitch_InLo = (fs & F_LO_PS) ? kPixelPSZpitch : kStrip2SZpitch;
+        const float zpitch_OutLo = (ft & F_LO_PS) ? kPixelPSZpitch : kStrip2SZpitch;
+        const float rtRatio = rtOut / rtIn;
+        const float dzDrtScale = T.ltd;
+        const float zHi = zIn + (zIn + kDeltaZLum) * (rtRatio - 1.f) * (zIn < 0.f ? 1.f : dzDrtScale) + (zpitch_InLo + zpitch_OutLo);
+        const float zLo = zIn + (zIn - kDeltaZLum) * (rtRatio - 1.f) * (zIn > 0.f ? 1.f : dzDrtScale) - (zpitch_InLo + zpitch_OutLo);
+        if (!(zOut >= zLo && zOut <= zHi)) return kAlgoNone;
+        const float sdlMuls = sdl_muls_quick(rtOut - rtIn, S.sqq_hi);
+        const int c3 = phi_cut_quick(fabsf(phi_mpi_pi(T.uphi - S.uphi)), T.la1, sdlMuls, pv_off(T));
+        if (c3 <= 0) return c3 == 0 ? kAlgoNone : kAlgoUnsure;
+        const float drt_OutLo_InLo = rtOut - rtIn;
+        const float drt_InSeg = S.urt - S.lrt;
+        const float coshEta = S.cosh;
+        const float zp = zpitch_InLo + zpitch_OutLo;
+        float dzErr = zp * zp * 2.f;
+        dzErr += sdlMuls * sdlMuls * drt_OutLo_InLo * drt_OutLo_InLo / 3.f * coshEta * coshEta;
+        dzErr = __fsqrt_rn(dzErr);
+        const float dzMean = S.dzdr * drt_OutLo_InLo;
+        const float pw = dzErr / drt_InSeg * drt_OutLo_InLo;
+        const float zWindow = pw + zp;
+        const float mLo = dzMean * (zIn > 0.f ? 1.f : dzDrtScale), mHi = dzMean * (zIn < 0.f ? 1.f : dzDrtScale);
+        const float zLoPointed = zIn + mLo - zWindow;
+        const float zHiPointed = zIn + mHi + zWindow;
+        const float m = kQuickMargin * (fabsf(zIn) + fabsf(mLo) + fabsf(mHi) + 2.f * (fabsf(pw) + zp));
+        const int c2 = window_quick(zOut, zLoPointed, zHiPointed, m);
+        return c2 > 0 ? kAlgoBBBB : (c2 == 0 ? kAlgoNone : kAlgoUnsure);
+    }
+    if (b1 && e3 && e4 && (b2 || e2)) {
+        const float zGeom = ((fs & F_LO_PS) ? kPixelPSZpitch : kStrip2SZpitch) + ((ft & F_LO_PS) ? kPixelPSZpitch : kStrip2SZpitch);
+        const float dzDrtScale = T.ltd;
+        if (!(zIn * zOut > 0)) return kAlgoNone;
+        const float dLum = f_copysign(kDeltaZLum, zIn);
+        const float rtGeom1 = (ft & F_LO_PS) ? kPixelPSZpitch : kStrip2SZpitch;
+        const float zGeom1 = f_copysign(zGeom, zIn);
+        const float rtLo = rtIn * (1.f + (zOut - zIn - zGeom1) / (zIn + zGeom1 + dLum) / dzDrtScale) - rtGeom1;
+        if (!(rtOut >= rtLo)) return kAlgoNone;
+        float zInForHi = zIn - zGeom1 - dLum;
+        if (zInForHi * zIn < 0) zInForHi = f_copysign(0.1f, zIn);
+        const float rtHi = rtIn * (1.f + (zOut - zIn + zGeom1) / zInForHi) + rtGeom1;
+        if (!(rtOut >= rtLo && rtOut <= rtHi)) return kAlgoNone;
+        const float kZ = (zOut - zIn) / (S.uz - S.lz);
+        if (!(kZ >= 0)) return kAlgoNone;
+        const float sdlMuls = sdl_muls_quick(rtOut - rtIn, S.sqq_hi);
+        const int c3 = phi_cut_quick(fabsf(phi_mpi_pi(T.uphi - S.uphi)), T.la1, sdlMuls, pv_off(T));
+        return c3 > 0 ? kAlgoBBEE : (c3 == 0 ? kAlgoNone : kAlgoUnsure);
+    }
+    if (e1 && e2 && e3 && e4) {
+        const float dzDrtScale = T.ltd;
+        if (!(zIn * zOut > 0)) return kAlgoNone;
+        const float dLum = f_copysign(kDeltaZLum, zIn);
+        const bool inPS = fs & F_LO_PS, outPS = ft & F_LO_PS;
+        const float rtGeom = (inPS && outPS) ? 2.f * kPixelPSZpitch : (inPS || outPS) ? (kPixelPSZpitch + kStrip2SZpitch) : 2.f * kStrip2SZpitch;
+        const float dz = zOut - zIn;
+        const float rtLo = rtIn * (1.f + dz / (zIn + dLum) / dzDrtScale) - rtGeom;
+        if (!(rtOut >= rtLo)) return kAlgoNone;
+        const float rtHi = rtIn * (1.f + dz / (zIn - dLum)) + rtGeom;
+        if (!(rtOut >= rtLo && rtOut <= rtHi)) return kAlgoNone;
+        const float sdlMuls = sdl_muls_quick(rtOut - rtIn, 1.f);
+        const int c3 = phi_cut_quick(fabsf(phi_mpi_pi(T.uphi - S.uphi)), T.la1, sdlMuls, pv_off(T));
+        if (c3 <= 0) return c3 == 0 ? kAlgoNone : kAlgoUnsure;
+        if (inPS && (fs & F_UP_PS)) {
+            const float drtSDIn = S.urt - S.lrt;
+            const float dzSDIn = S.uz - S.lz;
+            const float coshEta = S.cosh;
+            const float dzOutInAbs = fabsf(zOut - zIn);
+            const float multDzDr = dzOutInAbs * coshEta / (coshEta * coshEta - 1.f);
+            const float kZ = (zOut - zIn) / dzSDIn;
+            if (!(kZ >= 0)) return kAlgoNone;
+            float drtErr = kPixelPSZpitch * kPixelPSZpitch * 2.f / dzSDIn / dzSDIn * dzOutInAbs * dzOutInAbs;
+            drtErr += sdlMuls * sdlMuls * multDzDr * multDzDr / 3.f * coshEta * coshEta;
+            drtErr = __fsqrt_rn(drtErr);
+            const float drtMean = drtSDIn * dzOutInAbs / fabsf(dzSDIn);
+            const float rtWindow = drtErr + rtGeom;
+            const float mLo = drtMean / dzDrtScale;
+            const float rtLo_point = rtIn + mLo - rtWindow;
+            const float rtHi_point = rtIn + drtMean + rtWindow;
+            const float m = kQuickMargin * (fabsf(rtIn) + fabsf(mLo) + fabsf(drtMean) + 2.f * fabsf(rtWindow));
+            const int c2 = window_quick(rtOut, rtLo_point, rtHi_point, m);
+            return c2 > 0 ? kAlgoEEEE : (c2 == 0 ? kAlgoNone : kAlgoUnsure);
+        }
+        return kAlgoEEEE;
+    }
+    return kAlgoNone;
+}
+
 // Phase B1 decides most candidates from single-precision approximations of
 // its two angles: atan2f for the directions and asinf for the betaIn cut's
 // asin, whose errors CUDA documents as at most 3 and 2 ulp.  The exact values
@@ -1001,6 +1147,19 @@ __device__ __forceinline__ bool tl_phaseB1_sgv(int algo, const SGV& S, const SGV
 }
 static __device__ __noinline__ bool tl_phaseB1(int algo, const float* __restrict__ pack, int s, int t, float sdlCut) {
     return tl_phaseB1_sgv(algo, load_sgv(pack, s), load_sgv(pack, t), sdlCut);
+}
+// phase B1 of a candidate through phase A (tl_phaseA_quick's survivors carry
+// no cut values): the exact phi-cut width and multiple-scattering factor
+// (tl_cut_values), then the cuts; the factor goes on to phase B2
+struct B1Result {
+    bool pass;
+    float muls;
+};
+static __device__ __noinline__ B1Result tl_phaseB1_entry(int algo, const float* __restrict__ pack, int s, int t) {
+    const SGV S = load_sgv(pack, s), T = load_sgv(pack, t);
+    float cut, muls;
+    tl_cut_values(algo, S, T, cut, muls);
+    return B1Result{tl_phaseB1_sgv(algo, S, T, cut), muls};
 }
 
 // ---- phase B2: betaIn, betaOut, the deltaBeta iterations, the betaOut cut

@@ -931,28 +931,52 @@ __device__ __forceinline__ int tl_outer_of(const BatchDev& b, int var, int s, in
     return var == 1 ? tl_outer_layer(b, s, q) : (var == 2 ? tl_outer_nav(b, s, q) : tl_outer(b, s, q));
 }
 
-// append the lanes' phase-A survivors to the survivor list at the positions
-// reserved on `count` (every lane calls it); positions past the list's
-// capacity are not written and flag the overflow (the count keeps growing, so
-// it holds the capacity needed)
-__device__ __forceinline__ void passa_append(const BatchDev& b, unsigned long long* count, int algo, int s, int tt,
-                                             float cut, float muls) {
+// phase A's decision: the single-precision one, and tl_phaseA where that
+// cannot decide (the cut values are computed again in phase B1)
+__device__ __forceinline__ int tl_phase_a_decide(const SGV& S, const SGOuter& T) {
+    int algo = tl_phaseA_quick(S, T);
+    if (algo == kAlgoUnsure) {
+        float cut, muls;
+        algo = tl_phaseA(S, T, cut, muls);
+    }
+    return algo;
+}
+
+// A warp's phase-A survivors, collected in shared memory and appended to
+// the survivor list in batches of up to kPassBuf: one atomic on the list's
+// count per batch instead of one per 32 candidates (atomics on one address
+// serialise at its L2 slice, a few per nanosecond at most).  Positions past
+// the list's capacity are not written and flag the overflow (the count keeps
+// growing, so it holds the capacity needed).  Every lane of the warp calls
+// passbuf_add and passbuf_flush.
+constexpr int kPassBuf = 128;
+struct PassBuf {
+    int4* e;    // this warp's kPassBuf entries in shared memory
+    int n = 0;  // entries held (warp-uniform)
+};
+__device__ __forceinline__ void passbuf_flush(const BatchDev& b, PassBuf& pb) {
+    __syncwarp();
+    const int lane = threadIdx.x & 31;
+    unsigned long long p0 = 0;
+    if (lane == 0 && pb.n) p0 = atomicAdd(b.n_kept, (unsigned long long)pb.n);
+    p0 = __shfl_sync(0xffffffffu, p0, 0);
+    for (int i = lane; i < pb.n; i += kWarp) {
+        const int64_t pos = (int64_t)p0 + i;
+        if (pos < b.kept_cap) AT(b.passa, pos, b.kept_cap) = pb.e[i];
+        else atomicOr(b.status, kStatusOverflowKept);
+    }
+    __syncwarp();
+    pb.n = 0;
+}
+__device__ __forceinline__ void passbuf_add(const BatchDev& b, PassBuf& pb, int algo, int s, int tt) {
     const int lane = threadIdx.x & 31;
     const bool pass = algo != kAlgoNone;
     const unsigned m = __ballot_sync(0xffffffffu, pass);
     if (!m) return;
-    const int leader = __ffs(m) - 1;
-    unsigned long long p0 = 0;
-    if (lane == leader) p0 = atomicAdd(count, (unsigned long long)__popc(m));
-    p0 = __shfl_sync(0xffffffffu, p0, leader);
-    if (!pass) return;
-    const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));
-    if (pos < b.kept_cap) {
-        AT(b.passa, pos, b.kept_cap) = make_int4(s, tt, algo, __float_as_int(cut));
-        AT(b.passa_muls, pos, b.kept_cap) = muls;
-    } else {
-        atomicOr(b.status, kStatusOverflowKept);
-    }
+    const int c = __popc(m);
+    if (pb.n + c > kPassBuf) passbuf_flush(b, pb);
+    if (pass) pb.e[pb.n + __popc(m & ((1u << lane) - 1u))] = make_int4(s, tt, algo, 0);
+    pb.n += c;
 }
 
 constexpr int kMlpWarps = kMlpTile / 32;
@@ -965,6 +989,7 @@ constexpr int kMlpWarps = kMlpTile / 32;
 // resident, and each phase runs on full warps.  The survivor list shares the
 // pre-filter's capacity and overflow handling (its count is n_kept).
 __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_a(BatchDev b) {
+    __shared__ int4 pbuf[kEnumThreads / kWarp][kPassBuf];
     if (halted(b)) return;
     const int64_t nobj = n_inner(b, kTL);
     if (nobj <= 0) return;
@@ -975,6 +1000,7 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_a(BatchDev b) {
     const int64_t ntask = (total + task - 1) / task;
     const int lane = threadIdx.x & 31;
     const int lay = tl_variant(b);
+    PassBuf pb{pbuf[threadIdx.x >> 5]};
     for (;;) {
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(b.task + kTL, 1ull);
@@ -993,17 +1019,172 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_a(BatchDev b) {
         for (int64_t cb = base; cb < end; cb += kWarp) {
             const int64_t c = cb + lane;
             int algo = kAlgoNone, s = 0, tt = 0;
-            float cut = 0.f, muls = 0.f;
             if (c < end) {
                 s = (i0 == i1) ? i0 : find_obj(b, off, offlim, i0, i1, c);
                 tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
                 (void)IX(s, b.obj[kSG].cap);
                 (void)IX(tt, b.obj[kSG].cap);
-                algo = tl_phaseA(load_sgv(b.sgpack, s), load_sgo(b.sgouter, b.obj[kSG].cap, tt), cut, muls);
+                algo = tl_phase_a_decide(load_sgv(b.sgpack, s), load_sgo(b.sgouter, b.obj[kSG].cap, tt));
             }
-            passa_append(b, b.n_kept, algo, s, tt, cut, muls);
+            passbuf_add(b, pb, algo, s, tt);
         }
     }
+    passbuf_flush(b, pb);
+}
+
+// Module-map tracklet candidates in module-pair tiles.  The outer segments of
+// an inner segment are those of the modules connected to the module of its
+// outer mini-doublet (Event.cc:611-693), so all inner segments ending in one
+// module g share one list of outer segments, and g's candidates are the
+// product (segments ending in g) x (segments of g's connected modules, in
+// connection-list order).  A warp task is a tile of that product: up to
+// kTileA inner segments x 32 outer segments.  Each lane decodes and loads its
+// outer segment once per tile, and the inner segments' records are
+// warp-uniform loads.  The candidates, and so the survivor list as a set, are
+// those k_tl_enum_a enumerates.
+constexpr int kTileA = 16;
+
+__device__ __forceinline__ int64_t tl_tile_count(int64_t na, int64_t nb) {
+    return (na > 0 && nb > 0) ? ((na + kTileA - 1) / kTileA) * ((nb + kWarp - 1) / kWarp) : 0;
+}
+
+// tiles per global module (eoff still holds the counts of segments ending there)
+__global__ void k_tl_tile_count(BatchDev b) {
+    if (halted(b)) return;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < b.n_gm; g += (int64_t)gridDim.x * blockDim.x)
+        AT(b.toff, g, NG1(b)) = tl_tile_count(AT(b.eoff, g, NG1(b)), AT(b.conn_sum, g, b.n_gm));
+}
+
+// the segments by the global module of their outer mini-doublet (eoff scanned)
+__global__ void k_sg_end_scatter(BatchDev b) {
+    if (halted(b)) return;
+    const int64_t n = n_inner(b, kTL);
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        const int g2 = OG(b, kMD, OJ(b, kSG, s));
+        const int64_t pos = AT(b.eoff, g2, NG1(b)) + atomicAdd(&AT(b.ecur, g2, b.n_gm), 1);
+        AT(b.eidx, pos, b.obj[kSG].cap) = (int)s;
+    }
+}
+
+// the global module holding tile t: the largest g < n_gm with toff[g] <= t
+// (toff[0] = 0 <= t), by a 32-way search; every lane calls it with the same t
+__device__ __forceinline__ int tile_module(const BatchDev& b, int64_t t) {
+    const int lane = threadIdx.x & 31;
+    int lo = 0, hi = b.n_gm - 1;  // toff[lo] <= t, and the answer is in [lo, hi]
+    while (hi - lo >= kWarp) {
+        const int64_t span = (int64_t)(hi - lo) + 1;
+        const int p = lo + (int)((span * lane) >> 5);  // probes lo = p_0 < p_1 < ... < p_31 <= hi
+        const unsigned m = __ballot_sync(0xffffffffu, AT(b.toff, p, NG1(b)) <= t);
+        const int j = 31 - __clz(m);  // bit 0 is set, and the set bits are a prefix
+        if (j < 31) hi = lo + (int)((span * (j + 1)) >> 5) - 1;
+        lo += (int)((span * j) >> 5);
+    }
+    const int p = lo + lane;
+    const unsigned m = __ballot_sync(0xffffffffu, p <= hi && AT(b.toff, p, NG1(b)) <= t);
+    return lo + 31 - __clz(m);
+}
+
+// tile -> global module map of the module-pair tiles (toff scanned); not
+// built when the tiles exceed its capacity (the enumeration then searches toff)
+__global__ void k_tl_tile_map(BatchDev b) {
+    if (halted(b)) return;
+    const int64_t ntile = AT(b.toff, b.n_gm, NG1(b));
+    if (ntile > b.tile_cap) return;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < b.n_gm; g += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t1 = AT(b.toff, g + 1, NG1(b));
+        for (int64_t t = AT(b.toff, g, NG1(b)); t < t1; ++t) AT(b.tile_gm, t, b.tile_cap) = (int)g;
+    }
+}
+
+// Each warp takes tiles from a shared counter (the next index is fetched
+// while the current tile runs).  Per tile, the loads come in a few dependent
+// rounds: the module (tile map), its offsets and connection-list range, the
+// inner segments' indices with the connection entries' prefix sums and first
+// segments (one entry per lane while the module has at most 32 connections),
+// then the inner segments' records (staged in shared memory, read there as
+// warp-uniform values) with the lanes' outer-segment fields.
+__global__ void __launch_bounds__(kEnumThreads) k_tl_enum_tiles(BatchDev b) {
+    __shared__ __align__(16) float4 srec[kEnumThreads / kWarp][kTileA * (PK_N / 4)];
+    __shared__ int sidx[kEnumThreads / kWarp][kTileA];
+    __shared__ int4 pbuf[kEnumThreads / kWarp][kPassBuf];
+    if (halted(b) || b.n_gm <= 0) return;
+    const int64_t ntile = AT(b.toff, b.n_gm, NG1(b));
+    const bool mapped = ntile <= b.tile_cap;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int n_mod = b.geo.n_mod;
+    const int64_t sgcap = b.obj[kSG].cap;
+    PassBuf pb{pbuf[w]};
+    unsigned long long next = 0;
+    if (lane == 0) next = atomicAdd(b.task + kTL, 1ull);
+    for (;;) {
+        const int64_t t = (int64_t)__shfl_sync(0xffffffffu, next, 0);
+        if (t >= ntile) break;
+        if (lane == 0) next = atomicAdd(b.task + kTL, 1ull);
+        const int g = mapped ? AT(b.tile_gm, t, b.tile_cap) : tile_module(b, t);
+        const int ev = ev_of(b, g), m2 = g - ev * n_mod;
+        const int64_t a0 = AT(b.eoff, g, NG1(b));
+        const int64_t na = AT(b.eoff, g + 1, NG1(b)) - a0;
+        const int64_t nb = AT(b.conn_sum, g, b.n_gm);
+        const int k0 = AT(b.geo.conn_off, m2, NM(b) + 1), k1 = AT(b.geo.conn_off, m2 + 1, NM(b) + 1);
+        const int64_t nbb = (nb + kWarp - 1) / kWarp;
+        const int64_t local = t - AT(b.toff, g, NG1(b));
+        const int64_t ab = local / nbb, bb = local - ab * nbb;
+        const int64_t abase = ab * kTileA;
+        const int nat = (int)min((int64_t)kTileA, na - abase);
+        // this lane's outer segment: entry q of g's outer list
+        const int64_t q0 = bb * kWarp, q = q0 + lane;
+        const bool has = q < nb;
+        const int64_t pbase = (int64_t)ev * b.geo.n_conn;
+        int tt = 0;
+        __syncwarp();  // the previous tile's records have been read
+        if (lane < nat) sidx[w][lane] = AT(b.eidx, a0 + abase + lane, sgcap);
+        if (k1 - k0 <= kWarp) {
+            // connection entry j = k0 + lane: prefix sum and first segment
+            int pj = 0x7fffffff, fj = 0;
+            if (lane < k1 - k0) {
+                pj = AT(b.conn_pref, pbase + k0 + lane, NCP(b));
+                fj = AT(b.conn_first, pbase + k0 + lane, NCP(b));
+            }
+            // the entry of lane L is the last j with pj <= q0 + L (entry 0 has pj = 0)
+            int j = 31 - __clz(__ballot_sync(0xffffffffu, pj <= q0));
+            for (int jj = j + 1; jj < k1 - k0; ++jj) {
+                const int pjj = __shfl_sync(0xffffffffu, pj, jj);
+                if (pjj > q0 + (kWarp - 1)) break;
+                if (pjj <= q) j = jj;
+            }
+            const int pref = __shfl_sync(0xffffffffu, pj, j);
+            const int first = __shfl_sync(0xffffffffu, fj, j);
+            tt = first + (int)(q - pref);
+        } else if (has) {
+            int pref;
+            const int k = conn_entry(b, ev, m2, q, pref);
+            tt = (int)(AT(b.conn_first, pbase + k, NCP(b)) + (q - pref));
+        }
+        SGOuter T{};
+        if (has) {
+            (void)IX(tt, sgcap);
+            T = load_sgo(b.sgouter, sgcap, tt);
+        }
+        __syncwarp();
+        // stage the tile's inner-segment records (nat x 8 float4)
+#pragma unroll
+        for (int r = 0; r < kTileA * (PK_N / 4) / kWarp; ++r) {
+            const int e = lane + r * kWarp;
+            if (e < nat * (PK_N / 4)) {
+                const int sr = sidx[w][e / (PK_N / 4)];
+                (void)IX(sr, sgcap);
+                srec[w][e] = __ldg(reinterpret_cast<const float4*>(b.sgpack + (int64_t)sr * PK_N) + e % (PK_N / 4));
+            }
+        }
+        __syncwarp();
+        for (int r = 0; r < nat; ++r) {
+            const int sr = sidx[w][r];
+            const int algo = has ? tl_phase_a_decide(sgv_from(reinterpret_cast<const float*>(&srec[w][r * (PK_N / 4)])), T)
+                                 : kAlgoNone;
+            passbuf_add(b, pb, algo, sr, tt);
+        }
+    }
+    passbuf_flush(b, pb);
 }
 
 // Learned pre-filter of the tracklet candidates (no counterpart in the
@@ -1023,8 +1204,7 @@ struct PfPending {
     unsigned m = 0u;
     unsigned long long raw = 0ull;
     int leader = 0;
-    int4 e = make_int4(0, 0, 0, 0);  // (inner, outer, algorithm, cut bits)
-    float muls = 0.f;
+    int4 e = make_int4(0, 0, 0, 0);  // (inner, outer, algorithm, 0)
 };
 
 __device__ __forceinline__ void pf_flush(const BatchDev& b, const PfPending& p) {
@@ -1034,7 +1214,6 @@ __device__ __forceinline__ void pf_flush(const BatchDev& b, const PfPending& p) 
     if (!((p.m >> lane) & 1u)) return;
     const int64_t pos = (int64_t)p0 + __popc(p.m & ((1u << lane) - 1u));  // below the list length <= kept_cap
     AT(b.kept, pos, b.kept_cap) = p.e;
-    AT(b.kept_muls, pos, b.kept_cap) = p.muls;
 }
 
 __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
@@ -1059,7 +1238,6 @@ __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
         const bool valid = t < ntile && i < n;
         if (valid) {
             p.e = AT(b.passa, i, b.kept_cap);
-            p.muls = AT(b.passa_muls, i, b.kept_cap);
             tl_features(feat_s(b.sgfeat, p.e.x), feat_t(b.sgfeat, p.e.y), f);
         } else {
 #pragma unroll
@@ -1113,7 +1291,7 @@ __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
 // from the back, so that phase B2's warps mostly run one algorithm.  Front
 // and back never meet: together they hold at most count <= kept_cap entries.
 __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const int4* __restrict__ list,
-                                                         const float* __restrict__ list_muls, const unsigned long long* count) {
+                                                         const unsigned long long* count) {
     if (halted(b)) return;
     const int64_t n = min((int64_t)*count, b.kept_cap);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -1125,8 +1303,9 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const int4* 
         float muls = 0.f;
         if (i < n) {
             p = AT(list, i, b.kept_cap);
-            muls = AT(list_muls, i, b.kept_cap);
-            pass = tl_phaseB1(p.z, b.sgpack, p.x, p.y, __int_as_float(p.w));
+            const B1Result r = tl_phaseB1_entry(p.z, b.sgpack, p.x, p.y);
+            pass = r.pass;
+            muls = r.muls;
         }
         const bool front = pass && p.z == kAlgoBBBB;
         const unsigned mf = __ballot_sync(0xffffffffu, front);
@@ -1230,6 +1409,42 @@ __global__ void k_tl_collect(BatchDev b, MlpCollect col) {
     }
 }
 
+// Self-check of phase A's single-precision decision over the tracklet
+// candidates of the last run: out[0] candidates, out[1] decided by
+// tl_phaseA_quick, out[2] left to tl_phaseA, out[3] decided differently from
+// tl_phaseA (0 when the margins hold).
+__global__ void k_tl_quick_check(BatchDev b, unsigned long long* out) {
+    if (halted(b)) return;
+    const int64_t nobj = n_inner(b, kTL);
+    if (nobj <= 0) return;
+    const int64_t* off = b.cand[kTL];
+    const int64_t offlim = b.cand_cap[kTL] + 1;
+    const int64_t total = AT(off, nobj, offlim);
+    const int lay = tl_variant(b);
+    unsigned long long n[4] = {0ull, 0ull, 0ull, 0ull};
+    for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < total; c += (int64_t)gridDim.x * blockDim.x) {
+        int lo, hi;
+        obj_bounds(b, nobj, total, c, c, lo, hi);
+        const int s = find_obj(b, off, offlim, lo, hi, c);
+        const int tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
+        const SGV S = load_sgv(b.sgpack, s);
+        const SGOuter T = load_sgo(b.sgouter, b.obj[kSG].cap, tt);
+        const int q = tl_phaseA_quick(S, T);
+        float cut, muls;
+        const int e = tl_phaseA(S, T, cut, muls);
+        n[0] += 1;
+        n[1] += q != kAlgoUnsure;
+        n[2] += q == kAlgoUnsure;
+        n[3] += q != kAlgoUnsure && q != e;
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        unsigned long long v = n[k];
+        for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((threadIdx.x & 31) == 0 && v) atomicAdd(out + k, v);
+    }
+}
+
 // per-module object counts of a stage -> layer counters (before the scan)
 __global__ void k_obj_counters(BatchDev b, int st) {
     if (halted(b)) return;
@@ -1311,7 +1526,9 @@ __global__ void k_conn_sum(BatchDev b, int src, int cst) {
             for (int k = k0; k < k1; ++k) {
                 AT(b.conn_pref, pbase + k, NCP(b)) = (int32_t)sum;
                 const int64_t g2 = ebase + AT(b.geo.conn_idx, k, NC(b));
-                sum += OFF(b, src, g2 + 1) - OFF(b, src, g2);
+                const int64_t o2 = OFF(b, src, g2);
+                AT(b.conn_first, pbase + k, NCP(b)) = (int32_t)o2;
+                sum += OFF(b, src, g2 + 1) - o2;
             }
             AT(b.conn_sum, g, b.n_gm) = sum;
             cand = (OFF(b, src, g + 1) - OFF(b, src, g)) * sum;
@@ -1341,6 +1558,7 @@ __global__ void k_tl_count(BatchDev b) {
             const int g2 = OG(b, kMD, OJ(b, kSG, s));
             c = AT(b.conn_sum, g2, b.n_gm);
             AT(b.cand[kTL], s, b.cand_cap[kTL] + 1) = c;
+            atomicAdd((unsigned long long*)&AT(b.eoff, g2, NG1(b)), 1ull);  // segments ending in g2
             const int g1 = OG(b, kSG, s);
             ev = ev_of(b, g1);
             slot = MOD(b, g1 - ev * n_mod).layer_slot;
@@ -1676,17 +1894,30 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
         join_index(b, kSG, s, h);  // segments by inner MD: the outward lists
         k_tl_count_nav<<<b.n_sm * 8, 256, 0, s>>>(b);
     } else {
+        cudaMemsetAsync(b.eoff, 0, (b.n_gm + 1) * sizeof(int64_t), s);
+        cudaMemsetAsync(b.ecur, 0, b.n_gm * sizeof(int32_t), s);
         k_tl_count<<<b.n_sm * 8, 256, 0, s>>>(b);
     }
     if (h) h->launches += 3;
     scan_h(b, b.cand[kTL], b.obj[kSG].mod_cnt + b.n_gm, b.cand_cap[kTL], s, h);
     k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, kTL);
     if (h) h->launches += 1;
+    // module-map candidates: the module-pair tiles (k_tl_enum_tiles)
+    const bool tiles = !(b.flags & (kFlagTLLayers | kFlagTLNav));
+    if (tiles) {
+        k_tl_tile_count<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b);
+        scan_h(b, b.eoff, b.n_gm_dev, b.n_gm, s, h);
+        scan_h(b, b.toff, b.n_gm_dev, b.n_gm, s, h);
+        k_sg_end_scatter<<<b.n_sm * 8, 256, 0, s>>>(b);
+        k_tl_tile_map<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b);
+        if (h) h->launches += 3;
+    }
     if (h && h->timed) rec_event(h->enum_start[kTL], s);
     // enumeration + phase A -> survivor list (-> the pre-filter -> kept list)
     // -> phase B1 -> phase B2
     cudaMemsetAsync(b.n_kept, 0, sizeof(unsigned long long), s);
-    k_tl_enum_a<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
+    if (tiles) k_tl_enum_tiles<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
+    else k_tl_enum_a<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
     if (h && h->timed) rec_event(h->tl_mid[0], s);
     const bool mlp = (b.flags & kFlagMLP) != 0;
     if (mlp) {
@@ -1695,8 +1926,7 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     }
     if (h && h->timed) rec_event(h->tl_mid[1], s);
     cudaMemsetAsync(b.n_pb, 0, 2 * sizeof(unsigned long long), s);
-    k_tl_b1<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, mlp ? b.kept : b.passa, mlp ? b.kept_muls : b.passa_muls,
-                                                                 mlp ? b.n_kept2 : b.n_kept);
+    k_tl_b1<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, mlp ? b.kept : b.passa, mlp ? b.n_kept2 : b.n_kept);
     k_tl_b2<kB2BBBB><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
     k_tl_b2<kB2Others><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
     if (h) h->launches += mlp ? 4 : 3;
@@ -1870,6 +2100,11 @@ void launch_tl_collect(const BatchDev& b, const MlpCollect& c, cudaStream_t s) {
     // the bucket table holds the last stage that ran: rebuild the tracklet one
     k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, kTL);
     k_tl_collect<<<b.n_sm * 8, 256, 0, s>>>(b, c);
+}
+
+void launch_tl_quick_check(const BatchDev& b, unsigned long long* out, cudaStream_t s) {
+    k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, kTL);
+    k_tl_quick_check<<<b.n_sm * 8, 256, 0, s>>>(b, out);
 }
 
 // the final cut variables of tracklets [first, first + n) (kTLVarN floats

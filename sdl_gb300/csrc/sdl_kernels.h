@@ -37,6 +37,7 @@ struct BatchDev {
     int64_t* n_gm_dev;             // device scalar = n_gm
     // connection-list prefix sums of per-module object counts
     int32_t* conn_pref;            // n_ev * n_conn
+    int32_t* conn_first;           // n_ev * n_conn: offset of the entry's module's first object
     int64_t* conn_sum;             // n_gm
     float* sgpack;                 // segment cap * PK_N packed records for the tracklet stage
     float* sgouter;                // segment cap * 7, one array per field: what phase A reads of an outer
@@ -57,12 +58,10 @@ struct BatchDev {
     int enum_grid[kNumStages];
     const unsigned char* mlp_pack; // packed pre-filter weights and threshold (kPackBytes)
     MlpStats* mlp_stats;           // pre-filter counts of the last run
-    int4* passa;                   // tracklet candidates through phase A: (inner, outer, algorithm, cut bits)
-    float* passa_muls;             //   and their multiple-scattering factor
+    int4* passa;                   // tracklet candidates through phase A: (inner, outer, algorithm, 0)
     int64_t kept_cap;              // entries of each survivor list
     unsigned long long* n_kept;    // phase-A survivors found (can exceed kept_cap: overflow)
     int4* kept;                    // the phase-A survivors the pre-filter kept, as passa
-    float* kept_muls;
     unsigned long long* n_kept2;
     // join index (triplets, then track candidates): the segments by their inner
     // mini-doublet, then the tracklets by their inner segment's inner mini-doublet
@@ -72,6 +71,14 @@ struct BatchDev {
     int64_t* joff2;                // a second index (createTrackCandidatesFromTriplets: the triplets by their
     int32_t* jcur2;                //   innermost mini-doublet, beside the segments by inner mini-doublet)
     int32_t* jidx2;                // triplet cap
+    // module-pair tiles of the module-map tracklet candidates: the segments by
+    // the global module of their outer mini-doublet, and the tiles per module
+    int64_t* eoff;                 // n_gm + 1: counts -> offsets
+    int32_t* ecur;                 // n_gm: fill cursors
+    int32_t* eidx;                 // segment cap: segment indices
+    int64_t* toff;                 // n_gm + 1: tile counts -> offsets
+    int32_t* tile_gm;              // tile_cap: the global module of each tile (when the tiles fit)
+    int64_t tile_cap;
     int4* pb;                      // candidates through phase B1: (inner, outer, algorithm, muls bits), BBBB
                                    //   from the front, the others from the back
     unsigned long long* n_pb;      // [2]: BBBB entries, other entries (kept_cap in all)
@@ -109,6 +116,8 @@ void launch_tl_collect(const BatchDev& b, const MlpCollect& c, cudaStream_t s);
 // self-check of the float-float fast paths (out[8]: see k_math_check)
 void launch_math_check(int fn, int exhaustive, unsigned long long start, long long n, unsigned long long seed,
                        unsigned long long* out, int n_sm, cudaStream_t s);
+// self-check of phase A's single-precision decision (out[4]: see k_tl_quick_check)
+void launch_tl_quick_check(const BatchDev& b, unsigned long long* out, cudaStream_t s);
 // final cut variables of tracklets [first, first + n) (15 floats each, the kTLVar* order)
 void launch_tl_vars(const BatchDev& b, int64_t first, int64_t n, float* out, cudaStream_t s);
 // hit-index tuples of stage st for objects [first, first + n) into out (width 2/4/8/8/16)

@@ -1,0 +1,36 @@
+"""The tracklet stage's single-precision phase-A decision (tl_phaseA_quick)
+against the exact float cuts (tl_phaseA) on every tracklet candidate of a
+batch at PU 100, 200 and 300, for the module-map, layer-pair and navigation
+candidate sets: it never settles a candidate differently, and it leaves only
+a small share of them to the exact cuts.  The object sets of the chain that
+uses it are checked against the reference and the oracle elsewhere."""
+import pytest
+
+from test_gpu_parity import run_gpu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    from sdl_gb300 import Chain, build
+    build.build()
+    return Chain(0)
+
+
+@pytest.fixture(scope="module")
+def batch():
+    from sdl_gb300 import synth
+    det = synth.detector("full")
+    return det, [synth.make_event(det, 970 + k, "full", n_pu=n) for k, n in enumerate((3500, 7000, 10500))]
+
+
+@pytest.mark.parametrize("flags", [0, 3, 32])
+def test_phase_a_decision_matches_exact_cuts(gpu, batch, flags):
+    det, events = batch
+    run_gpu(gpu, det, events, flags)
+    r = gpu.tl_phase_a_check()
+    assert r["candidates"] > 1_000_000, r
+    assert r["settled"] + r["exact"] == r["candidates"], r
+    assert r["mismatches"] == 0, r
+    assert r["exact"] <= 1e-3 * r["candidates"], r
