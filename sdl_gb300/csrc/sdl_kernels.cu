@@ -663,9 +663,50 @@ __global__ void k_cand_buckets(BatchDev b, int st) {
     }
 }
 
+// A warp's accepted objects, collected in shared memory and appended to the
+// stage's record list in batches of up to kRecBuf: one atomic on the list's
+// count per batch instead of one per 32 candidates (atomics on one address
+// serialise at its L2 slice), and coalesced record writes.  The ranks within
+// the objects' modules are taken at the flush (atomics on distinct module
+// counters, issued together).  Every lane of the warp calls rec_flush.
+constexpr int kRecBuf = 64;
+template <int kNF>
+struct RecBuf {
+    int (*e)[kRecBuf];  // this warp's [3 + kNF][kRecBuf] words: inner, outer, module, float values
+    int n = 0;          // records held (warp-uniform)
+};
+template <int kNF>
+__device__ __forceinline__ void rec_flush(const BatchDev& b, int st, RecBuf<kNF>& rb) {
+    __syncwarp();
+    const int lane = threadIdx.x & 31;
+    const Recs& R = b.rec[st];
+    const Objs& O = b.obj[st];
+    unsigned long long p0 = 0;
+    if (lane == 0 && rb.n) p0 = atomicAdd((unsigned long long*)(b.n_rec + st), (unsigned long long)rb.n);
+    p0 = __shfl_sync(0xffffffffu, p0, 0);
+    for (int k = lane; k < rb.n; k += kWarp) {
+        const int64_t pos = (int64_t)p0 + k;
+        if (pos < O.cap) {
+            const int g = rb.e[2][k];
+            AT(R.i, pos, O.cap) = rb.e[0][k];
+            AT(R.j, pos, O.cap) = rb.e[1][k];
+            AT(R.g, pos, O.cap) = g;
+            AT(R.rank, pos, O.cap) = (int)atomicAdd((unsigned long long*)&AT(O.mod_cnt, g, NG1(b)), 1ull);
+#pragma unroll
+            for (int q = 0; q < kNF; ++q) AT(R.f, (int64_t)q * O.cap + pos, O.cap * kNF) = __int_as_float(rb.e[3 + q][k]);
+        } else {
+            atomicOr(b.status, 1u << st);
+        }
+    }
+    __syncwarp();
+    rb.n = 0;
+}
+
 template <class F>
 __global__ void __launch_bounds__(kEnumThreads) k_enum(BatchDev b) {
     constexpr int st = F::kSt;
+    constexpr int kNF = st == kMD ? 4 : (st == kSG ? 6 : 0);  // the stage's float values per object
+    __shared__ int rbuf[kEnumThreads / kWarp][3 + kNF][kRecBuf];
     if (halted(b)) return;
     const int64_t nobj = n_inner(b, st);
     if (nobj <= 0) return;
@@ -675,8 +716,7 @@ __global__ void __launch_bounds__(kEnumThreads) k_enum(BatchDev b) {
     const int task = b.enum_task[st] > 0 ? b.enum_task[st] : kTaskDefault;
     const int64_t ntask = (total + task - 1) / task;
     const int lane = threadIdx.x & 31;
-    const Recs& R = b.rec[st];
-    const Objs& O = b.obj[st];
+    RecBuf<kNF> rb{rbuf[threadIdx.x >> 5]};
     for (;;) {
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(b.task + st, 1ull);
@@ -705,25 +745,21 @@ __global__ void __launch_bounds__(kEnumThreads) k_enum(BatchDev b) {
             }
             const unsigned m = __ballot_sync(0xffffffffu, pass);
             if (m) {
-                const int leader = __ffs(m) - 1;
-                unsigned long long p0 = 0;
-                if (lane == leader) p0 = atomicAdd((unsigned long long*)(b.n_rec + st), (unsigned long long)__popc(m));
-                p0 = __shfl_sync(0xffffffffu, p0, leader);
+                const int c = __popc(m);
+                if (rb.n + c > kRecBuf) rec_flush<kNF>(b, st, rb);
                 if (pass) {
-                    const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));
-                    if (pos < O.cap) {
-                        AT(R.i, pos, O.cap) = oi;
-                        AT(R.j, pos, O.cap) = oj;
-                        AT(R.g, pos, O.cap) = g;
-                        AT(R.rank, pos, O.cap) = (int)atomicAdd((unsigned long long*)&AT(O.mod_cnt, g, NG1(b)), 1ull);
-                        for (int k = 0; k < R.nf; ++k) AT(R.f, (int64_t)k * O.cap + pos, O.cap * R.nf) = fv[k];
-                    } else {
-                        atomicOr(b.status, 1u << st);
-                    }
+                    const int k = rb.n + __popc(m & ((1u << lane) - 1u));
+                    rb.e[0][k] = oi;
+                    rb.e[1][k] = oj;
+                    rb.e[2][k] = g;
+#pragma unroll
+                    for (int q = 0; q < kNF; ++q) rb.e[3 + q][k] = __float_as_int(fv[q]);
                 }
+                rb.n += c;
             }
         }
     }
+    rec_flush<kNF>(b, st, rb);
 }
 
 // warp-aggregated append of a survivor of stage st (inner object i, outer j)
