@@ -433,9 +433,7 @@ __global__ void k_md_pack(BatchDev b) {
 // segment algorithm on inner MD a and outer MD bmd (Segment.cc:337-859);
 // `connected`: the outer MD's module is in the inner module's connection list
 // (the endcap algorithm's first requirement, Segment.cc:613-633)
-__device__ __forceinline__ bool sg_pair(const BatchDev& b, int a, int bmd, bool connected, float* fv) {
-    const MDView im = md_rec(b, a).v;
-    const MDRec orec = md_rec(b, bmd);
+__device__ __forceinline__ bool sg_pair_rec(const MDView& im, const MDRec& orec, bool connected, float* fv) {
     const MDView& om = orec.v;
     SGVals v;
     v.dphi = v.dphimin = v.dphimax = v.dphichange = v.dphiminchange = v.dphimaxchange = 0.f;
@@ -446,6 +444,9 @@ __device__ __forceinline__ bool sg_pair(const BatchDev& b, int a, int bmd, bool 
     fv[0] = v.dphi; fv[1] = v.dphimin; fv[2] = v.dphimax;
     fv[3] = v.dphichange; fv[4] = v.dphiminchange; fv[5] = v.dphimaxchange;
     return pass;
+}
+__device__ __forceinline__ bool sg_pair(const BatchDev& b, int a, int bmd, bool connected, float* fv) {
+    return sg_pair_rec(md_rec(b, a).v, md_rec(b, bmd), connected, fv);
 }
 
 // segment candidates along the module map (Event.cc:445-522): candidate q of
@@ -1080,7 +1081,7 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_a(BatchDev b) {
 // those k_tl_enum_a enumerates.
 constexpr int kTileA = 16;
 
-__device__ __forceinline__ int64_t tl_tile_count(int64_t na, int64_t nb) {
+__device__ __forceinline__ int64_t tile_count(int64_t na, int64_t nb) {
     return (na > 0 && nb > 0) ? ((na + kTileA - 1) / kTileA) * ((nb + kWarp - 1) / kWarp) : 0;
 }
 
@@ -1088,7 +1089,7 @@ __device__ __forceinline__ int64_t tl_tile_count(int64_t na, int64_t nb) {
 __global__ void k_tl_tile_count(BatchDev b) {
     if (halted(b)) return;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < b.n_gm; g += (int64_t)gridDim.x * blockDim.x)
-        AT(b.toff, g, NG1(b)) = tl_tile_count(AT(b.eoff, g, NG1(b)), AT(b.conn_sum, g, b.n_gm));
+        AT(b.toff, g, NG1(b)) = tile_count(AT(b.eoff, g, NG1(b)), AT(b.conn_sum, g, b.n_gm));
 }
 
 // the segments by the global module of their outer mini-doublet (eoff scanned)
@@ -1122,7 +1123,7 @@ __device__ __forceinline__ int tile_module(const BatchDev& b, int64_t t) {
 
 // tile -> global module map of the module-pair tiles (toff scanned); not
 // built when the tiles exceed its capacity (the enumeration then searches toff)
-__global__ void k_tl_tile_map(BatchDev b) {
+__global__ void k_tile_map(BatchDev b) {
     if (halted(b)) return;
     const int64_t ntile = AT(b.toff, b.n_gm, NG1(b));
     if (ntile > b.tile_cap) return;
@@ -1130,6 +1131,41 @@ __global__ void k_tl_tile_map(BatchDev b) {
         const int64_t t1 = AT(b.toff, g + 1, NG1(b));
         for (int64_t t = AT(b.toff, g, NG1(b)); t < t1; ++t) AT(b.tile_gm, t, b.tile_cap) = (int)g;
     }
+}
+
+// The outer object of lane q - q0 of a tile whose outer block starts at entry
+// q0 of global module g's outer list (the objects of g's connected modules in
+// connection-list order; module m of event ev, connection entries [k0, k1)),
+// from the entries' prefix sums and first objects (k_conn_sum).  While g has
+// at most 32 connections, lane j loads entry k0 + j and each lane finds its
+// entry among them (the last one whose prefix sum is <= its q); otherwise
+// each lane searches.  Every lane of the warp calls it; lanes with has false
+// get an unspecified value.
+__device__ __forceinline__ int tile_outer(const BatchDev& b, int ev, int m, int k0, int k1, int64_t q0, bool has) {
+    const int lane = threadIdx.x & 31;
+    const int64_t q = q0 + lane;
+    const int64_t pbase = (int64_t)ev * b.geo.n_conn;
+    if (k1 - k0 <= kWarp) {
+        int pj = 0x7fffffff, fj = 0;
+        if (lane < k1 - k0) {
+            pj = AT(b.conn_pref, pbase + k0 + lane, NCP(b));
+            fj = AT(b.conn_first, pbase + k0 + lane, NCP(b));
+        }
+        // entry 0 has prefix sum 0 <= q0
+        int j = 31 - __clz(__ballot_sync(0xffffffffu, pj <= q0));
+        for (int jj = j + 1; jj < k1 - k0; ++jj) {
+            const int pjj = __shfl_sync(0xffffffffu, pj, jj);
+            if (pjj > q0 + (kWarp - 1)) break;
+            if (pjj <= q) j = jj;
+        }
+        const int pref = __shfl_sync(0xffffffffu, pj, j);
+        const int first = __shfl_sync(0xffffffffu, fj, j);
+        return first + (int)(q - pref);
+    }
+    if (!has) return 0;
+    int pref;
+    const int k = conn_entry(b, ev, m, q, pref);
+    return (int)(AT(b.conn_first, pbase + k, NCP(b)) + (q - pref));
 }
 
 // Each warp takes tiles from a shared counter (the next index is fetched
@@ -1168,34 +1204,11 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_tiles(BatchDev b) {
         const int64_t abase = ab * kTileA;
         const int nat = (int)min((int64_t)kTileA, na - abase);
         // this lane's outer segment: entry q of g's outer list
-        const int64_t q0 = bb * kWarp, q = q0 + lane;
-        const bool has = q < nb;
-        const int64_t pbase = (int64_t)ev * b.geo.n_conn;
-        int tt = 0;
+        const int64_t q0 = bb * kWarp;
+        const bool has = q0 + lane < nb;
         __syncwarp();  // the previous tile's records have been read
         if (lane < nat) sidx[w][lane] = AT(b.eidx, a0 + abase + lane, sgcap);
-        if (k1 - k0 <= kWarp) {
-            // connection entry j = k0 + lane: prefix sum and first segment
-            int pj = 0x7fffffff, fj = 0;
-            if (lane < k1 - k0) {
-                pj = AT(b.conn_pref, pbase + k0 + lane, NCP(b));
-                fj = AT(b.conn_first, pbase + k0 + lane, NCP(b));
-            }
-            // the entry of lane L is the last j with pj <= q0 + L (entry 0 has pj = 0)
-            int j = 31 - __clz(__ballot_sync(0xffffffffu, pj <= q0));
-            for (int jj = j + 1; jj < k1 - k0; ++jj) {
-                const int pjj = __shfl_sync(0xffffffffu, pj, jj);
-                if (pjj > q0 + (kWarp - 1)) break;
-                if (pjj <= q) j = jj;
-            }
-            const int pref = __shfl_sync(0xffffffffu, pj, j);
-            const int first = __shfl_sync(0xffffffffu, fj, j);
-            tt = first + (int)(q - pref);
-        } else if (has) {
-            int pref;
-            const int k = conn_entry(b, ev, m2, q, pref);
-            tt = (int)(AT(b.conn_first, pbase + k, NCP(b)) + (q - pref));
-        }
+        const int tt = tile_outer(b, ev, m2, k0, k1, q0, has);
         SGOuter T{};
         if (has) {
             (void)IX(tt, sgcap);
@@ -1945,7 +1958,7 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
         scan_h(b, b.eoff, b.n_gm_dev, b.n_gm, s, h);
         scan_h(b, b.toff, b.n_gm_dev, b.n_gm, s, h);
         k_sg_end_scatter<<<b.n_sm * 8, 256, 0, s>>>(b);
-        k_tl_tile_map<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b);
+        k_tile_map<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b);
         if (h) h->launches += 3;
     }
     if (h && h->timed) rec_event(h->enum_start[kTL], s);
