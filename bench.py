@@ -429,18 +429,19 @@ def main():
                     "tl_kernel_ms": round(statistics.fmean(s_tl), 4)}
 
     # ---- roofline of the dominant kernel of the headline run -----------------
-    # k_tl_enum_tiles (tracklet enumeration in module-pair tiles + the float
-    # cuts, the largest kernel of the step): algorithmic bytes = each
-    # segment's record as inner segment (112 B), its seven outer-role fields
-    # (28 B) and its entry in the index of segments by outer module (4 B) read
-    # once + each global module's tile offset, segment offset and connection
-    # sum (24 B) read once + each phase-A survivor's entry written once (16 B)
+    # k_tl_enum_tiles (tracklet enumeration in module-pair tiles, the float
+    # cuts and the single-precision decision of the first tracklet cuts):
+    # algorithmic bytes = each segment's record as inner segment (112 B), its
+    # eleven outer-role fields (44 B) and its entry in the index of segments by
+    # outer module (4 B) read once + each global module's tile offset, segment
+    # offset and connection sum (24 B) read once + each surviving candidate's
+    # entry written once (16 B)
     hbm, tflops, src = peaks()
     pf = np.mean(np.array(pf_ms), axis=0)
     fc_mean, pf_mean, ex_mean = float(pf[0]), float(pf[1]), float(pf[2])
     n_sg = int(n_pruned[1])
     n_gm = len(batch) * ch.num_modules
-    en_bytes = (112 + 28 + 4) * n_sg + 24 * n_gm + 16 * mstats["scored"]
+    en_bytes = (112 + 44 + 4) * n_sg + 24 * n_gm + 16 * mstats["scored"]
     en_achieved = en_bytes / (fc_mean * 1e-3) / 1e9
     tr = ncu_traffic("tl_enum_traffic.json")
     en_traffic = None
@@ -459,10 +460,11 @@ def main():
     mma_tflops = mstats["scored"] * MLP_FLOPS_PER_CANDIDATE / (pf_mean * 1e-3) / 1e12
     roofline = {"bound": "hbm", "achieved": round(en_achieved, 3), "peak": hbm, "unit": "GB/s",
                 "frac": round(en_achieved / hbm, 6), "traffic": en_traffic, "peak_source": src,
-                "kernel": "k_tl_enum_tiles (tracklet candidate enumeration in module-pair tiles and the float cuts)",
+                "kernel": "k_tl_enum_tiles (tracklet candidate enumeration in module-pair tiles, the float cuts and "
+                          "the single-precision phase-B1 decision)",
                 "kernel_ms": round(fc_mean, 3), "algorithmic_bytes": en_bytes,
                 "note": "issue-bound candidate evaluation (profiles/tl_kernels_ncu.md); HBM bytes are small by construction",
-                "prefilter": {"kernel": "k_tl_prefilter (tensor-core pre-filter of the candidates through the float cuts)",
+                "prefilter": {"kernel": "k_tl_prefilter (tensor-core pre-filter of the candidates through the float cuts and phase B1)",
                               "kernel_ms": round(pf_mean, 3), "algorithmic_bytes": alg_bytes,
                               "achieved": round(achieved, 3), "peak": hbm, "unit": "GB/s",
                               "frac": round(achieved / hbm, 6), "traffic": traffic,
@@ -492,7 +494,7 @@ def main():
                        "stage_ms": {k: round(float(v), 3) for k, v in zip(("ingest", "MD", "SG", "TL", "TP", "TC"), hl_stage)},
                        "prefilter": {"weights": "sdl_gb300/weights/tl_mlp_pu.npz", "threshold": thr,
                                      "trained_on": "%d events, PU 100-300 (seeds 100000+)" % meta.get("train_events", 0),
-                                     "candidates": mstats["candidates"], "scored_after_float_cuts": mstats["scored"],
+                                     "candidates": mstats["candidates"], "scored_after_float_cuts_and_b1": mstats["scored"],
                                      "kept": mstats["kept"],
                                      "pruned_fraction": round(1.0 - mstats["kept"] / max(1, mstats["scored"]), 4)},
                        "wall_s": round(wall, 3)},

@@ -192,12 +192,13 @@ int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3);
  * and tan(x) / x (the hits' tan of their asin angle). */
 int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64_t n, uint64_t seed, uint64_t* out8);
 
-/* Self-check of the tracklet stage's single-precision phase-A decision
- * (no counterpart in the reference): after a run through the tracklet stage,
- * every tracklet candidate of the batch is judged both by the fast decision
- * and by the exact float cuts.  out4: candidates, candidates the fast
- * decision settled, candidates it left to the exact cuts, and settled
- * candidates whose decision differs from the exact one (must be 0). */
+/* Self-check of the tracklet enumeration's single-precision decisions (no
+ * counterpart in the reference): after a run through the tracklet stage,
+ * every tracklet candidate of the batch is judged both by the fast decisions
+ * (the float cuts, then for their survivors the first part of the tracklet
+ * cuts) and by the exact cuts.  out4: candidates, candidates the fast
+ * decisions settled alone, candidates that needed an exact evaluation, and
+ * candidates settled differently from the exact cuts (must be 0). */
 int sdlg_tl_phase_a_check(sdlg_ctx* ctx, uint64_t* out4);
 
 /* Number of kernels one run of the chain launches (as last enqueued). */
@@ -235,9 +236,12 @@ int sdlg_mini_doublets_static(sdlg_ctx* ctx, int64_t n_hits, const float* d_x, c
  * A 12-64-64-1 perceptron (ReLU, BF16 weights and first hidden layer, FP32
  * accumulation) scores every tracklet candidate (inner segment, outer
  * segment) from 12 float features; with SDLG_FLAG_MLP every candidate through
- * the float part of the reference's tracklet cuts is scored, one whose logit
- * is below the threshold is dropped, and the rest of the cuts judge every
- * other one.  The pruned chain's tracklets,
+ * the float part of the reference's tracklet cuts and the first part of the
+ * rest (the direction and betaIn cuts, where their single-precision decision
+ * settles them) is scored, one whose logit is below the threshold is dropped,
+ * and the rest of the cuts judge every other one.  The cuts and the network
+ * judge each candidate on its own, so their order does not change the
+ * result.  The pruned chain's tracklets,
  * triplets and track candidates are therefore subsets of the plain chain's.
  * Inference runs on the tensor cores inside the tracklet kernel; training
  * runs on the GPU with this library's kernels on samples labelled by the
@@ -271,8 +275,9 @@ int sdlg_mlp_gradient(sdlg_ctx* ctx, int64_t n, const float* x, const float* y, 
 /* logits of n feature rows (n x 12) through the tensor-core kernel */
 int sdlg_mlp_score(sdlg_ctx* ctx, int64_t n, const float* x, float* logits);
 /* counts of the last run with SDLG_FLAG_MLP: tracklet candidates, those
- * through the float cuts (scored by the network), those kept (logit at or
- * above the threshold), tensor-core waits that gave up */
+ * through the float cuts and the enumeration's decision of the direction and
+ * betaIn cuts (scored by the network), those kept (logit at or above the
+ * threshold), tensor-core waits that gave up */
 int sdlg_mlp_stats(sdlg_ctx* ctx, int64_t* out4);
 
 /* Pinned host memory for zero-staging transfers. */

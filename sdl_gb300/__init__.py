@@ -377,16 +377,18 @@ class Chain:
                 "first": [int(v) for v in out[3:8]] if out[2] else None}
 
     def tl_phase_a_check(self) -> dict:
-        """Self-check of the tracklet stage's single-precision phase-A decision
-        over the last run's candidates: how many it settled, how many it left
-        to the exact float cuts, and how many it settled differently (0)."""
+        """Self-check of the tracklet enumeration's single-precision decisions
+        (phase A, then phase B1) over the last run's candidates: how many they
+        settled alone, how many needed an exact evaluation, and how many they
+        settled differently from the exact cuts (0)."""
         out = np.zeros(4, dtype=np.uint64)
         self._ck(lib().sdlg_tl_phase_a_check(self.h, out.ctypes.data))
         return {"candidates": int(out[0]), "settled": int(out[1]), "exact": int(out[2]), "mismatches": int(out[3])}
 
     def mlp_stats(self) -> dict:
         """Pre-filter counts of the last run with FLAG_MLP: tracklet candidates,
-        those through the float cuts (scored by the network), those kept."""
+        those through the float cuts and the enumeration's phase-B1 decision
+        (scored by the network), those kept."""
         out = np.zeros(4, dtype=np.int64)
         self._ck(lib().sdlg_mlp_stats(self.h, out.ctypes.data))
         return {"candidates": int(out[0]), "scored": int(out[1]), "kept": int(out[2]), "timeouts": int(out[3])}

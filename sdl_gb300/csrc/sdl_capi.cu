@@ -365,7 +365,7 @@ int ensure_buffers(sdlg_ctx* ctx) {
     AL(b.pb, b.kept_cap);
     AL(b.n_pb, 2);
     AL(b.sgpack, ctx->cap_obj[kSG] * PK_N);
-    AL(b.sgouter, ctx->cap_obj[kSG] * 7);
+    AL(b.sgouter, ctx->cap_obj[kSG] * 11);
     AL(b.sgfeat, ctx->cap_obj[kSG] * kFeatN);
     AL(b.mdpack, ctx->cap_obj[kMD] * kMdPack);
     AL(b.counters, ctx->n_ev * 110);

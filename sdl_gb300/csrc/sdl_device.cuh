@@ -798,7 +798,7 @@ __device__ __forceinline__ float dbeta_cut2(float dBetaRes, float dBetaMuls, flo
 }
 
 
-// What phase A reads of the outer segment, from six arrays of one float per
+// What phase A reads of the outer segment, from arrays of one float per
 // segment (consecutive outer segments of a warp's candidates are then read
 // with coalesced loads); the same values as the packed record's fields.
 struct SGOuter {
@@ -816,6 +816,11 @@ __device__ __forceinline__ SGOuter load_sgo(const float* __restrict__ a, int64_t
     o.flags = __float_as_uint(__ldg(a + 5 * cap + t));
     o.pvoff = __ldg(a + 6 * cap + t);
     return o;
+}
+// the outer segment's anchor points as phase B1 reads them: (lx, ly, ux, uy),
+// arrays 7 to 10 of the same layout
+__device__ __forceinline__ float4 load_sgo_xy(const float* __restrict__ a, int64_t cap, int64_t t) {
+    return make_float4(__ldg(a + 7 * cap + t), __ldg(a + 8 * cap + t), __ldg(a + 9 * cap + t), __ldg(a + 10 * cap + t));
 }
 // the PV-offset term 0.1f / rtOut of the tracklet cuts (Tracklet.cc:1056 and
 // the like), precomputed for an SGOuter
@@ -959,13 +964,17 @@ __device__ __forceinline__ float sdl_muls_quick(float d, float sq) {
     const float m = __fmul_rn(__fmul_rn(0.015f, __fmul_rn(u, rsqrtf(u))), sq);
     return m * 3.f / kPtCut * 4.f;
 }
-// |dphi| <= la1 + sqrt(sdlMuls^2 + pvoff^2): 1 holds, 0 fails, -1 not decided
-__device__ __forceinline__ int phi_cut_quick(float adphi, float la1, float sdlMuls, float pvoff) {
+// |dphi| <= la1 + sqrt(sdlMuls^2 + pvoff^2): 1 holds, 0 fails, -1 not
+// decided.  cut: the approximate width (within 25 * 2^-24 * (|la1| + r) of
+// the exact one, below 3e-6 where it is set), NaN where |la1| + r >= 2.
+__device__ __forceinline__ int phi_cut_quick(float adphi, float la1, float sdlMuls, float pvoff, float& cut) {
+    cut = __int_as_float(0x7fc00000);
     const float y = sdlMuls * sdlMuls + pvoff * pvoff;
     if (!(y > 0x1p-100f && y < 0x1p100f)) return -1;
     const float r = __fmul_rn(y, rsqrtf(y));
     const float c = la1 + r;
     const float m = kQuickMargin * (fabsf(la1) + r);
+    if (fabsf(la1) + r < 2.f) cut = c;
     if (adphi > c + m) return 0;
     if (adphi < c - m) return 1;
     return -1;
@@ -978,7 +987,8 @@ __device__ __forceinline__ int window_quick(float v, float lo, float hi, float m
 }
 
 template <class TSeg>
-__device__ __forceinline__ int tl_phaseA_quick(const SGV& S, const TSeg& T) {
+__device__ __forceinline__ int tl_phaseA_quick(const SGV& S, const TSeg& T, float& cut) {
+    cut = __int_as_float(0x7fc00000);
     const uint32_t fs = S.flags, ft = T.flags;
     const bool b1 = fs & F_LO_B, b2 = fs & F_UP_B, b3 = ft & F_LO_B, b4 = ft & F_UP_B;
     const bool e1 = fs & F_LO_E, e2 = fs & F_UP_E, e3 = ft & F_LO_E, e4 = ft & F_UP_E;
@@ -992,7 +1002,7 @@ __device__ __forceinline__ int tl_phaseA_quick(const SGV& S, const TSeg& T) {
         const float zLo = zIn + (zIn - kDeltaZLum) * (rtRatio - 1.f) * (zIn > 0.f ? 1.f : dzDrtScale) - (zpitch_InLo + zpitch_OutLo);
         if (!(zOut >= zLo && zOut <= zHi)) return kAlgoNone;
         const float sdlMuls = sdl_muls_quick(rtOut - rtIn, S.sqq_hi);
-        const int c3 = phi_cut_quick(fabsf(phi_mpi_pi(T.uphi - S.uphi)), T.la1, sdlMuls, pv_off(T));
+        const int c3 = phi_cut_quick(fabsf(phi_mpi_pi(T.uphi - S.uphi)), T.la1, sdlMuls, pv_off(T), cut);
         if (c3 <= 0) return c3 == 0 ? kAlgoNone : kAlgoUnsure;
         const float drt_OutLo_InLo = rtOut - rtIn;
         const float drt_InSeg = S.urt - S.lrt;
@@ -1027,7 +1037,7 @@ __device__ __forceinline__ int tl_phaseA_quick(const SGV& S, const TSeg& T) {
         const float kZ = (zOut - zIn) / (S.uz - S.lz);
         if (!(kZ >= 0)) return kAlgoNone;
         const float sdlMuls = sdl_muls_quick(rtOut - rtIn, S.sqq_hi);
-        const int c3 = phi_cut_quick(fabsf(phi_mpi_pi(T.uphi - S.uphi)), T.la1, sdlMuls, pv_off(T));
+        const int c3 = phi_cut_quick(fabsf(phi_mpi_pi(T.uphi - S.uphi)), T.la1, sdlMuls, pv_off(T), cut);
         return c3 > 0 ? kAlgoBBEE : (c3 == 0 ? kAlgoNone : kAlgoUnsure);
     }
     if (e1 && e2 && e3 && e4) {
@@ -1042,7 +1052,7 @@ __device__ __forceinline__ int tl_phaseA_quick(const SGV& S, const TSeg& T) {
         const float rtHi = rtIn * (1.f + dz / (zIn - dLum)) + rtGeom;
         if (!(rtOut >= rtLo && rtOut <= rtHi)) return kAlgoNone;
         const float sdlMuls = sdl_muls_quick(rtOut - rtIn, 1.f);
-        const int c3 = phi_cut_quick(fabsf(phi_mpi_pi(T.uphi - S.uphi)), T.la1, sdlMuls, pv_off(T));
+        const int c3 = phi_cut_quick(fabsf(phi_mpi_pi(T.uphi - S.uphi)), T.la1, sdlMuls, pv_off(T), cut);
         if (c3 <= 0) return c3 == 0 ? kAlgoNone : kAlgoUnsure;
         if (inPS && (fs & F_UP_PS)) {
             const float drtSDIn = S.urt - S.lrt;
@@ -1148,6 +1158,50 @@ __device__ __forceinline__ bool tl_phaseB1_sgv(int algo, const SGV& S, const SGV
 static __device__ __noinline__ bool tl_phaseB1(int algo, const float* __restrict__ pack, int s, int t, float sdlCut) {
     return tl_phaseB1_sgv(algo, load_sgv(pack, s), load_sgv(pack, t), sdlCut);
 }
+// Phase B1 from the approximations alone, with an approximate phi-cut width
+// (tl_phaseA_quick's, within 3e-6 of the exact one, or the exact one): the
+// direction approximations are within 2e-6 of the exact angles (functions 16
+// and 17 of the math self-check), so with the width's error every comparison
+// clear_within decides holds by over 9e-5 in exact arithmetic as well, and
+// the result is tl_phaseB1_sgv's.  txy: the outer segment's (lx, ly, ux, uy).
+// 1: passes, 0: fails, -1: left to tl_phaseB1_sgv (NaN width included).
+__device__ __forceinline__ int tl_phaseB1_quick(int algo, const SGV& S, float4 txy, float cut) {
+    float mx = 0.f, my = 0.f;
+    mx += S.lx; my += S.ly;
+    mx += txy.x; my += txy.y;
+    mx /= 2.f; my /= 2.f;
+    const float dx = txy.x - S.lx, dy = txy.y - S.ly;
+    // the angle from the mid-point direction M to D = OutLo - InLo as one
+    // atan2 of (M x D, M . D): within 2^-22 of the exact angle whatever the
+    // lengths (the rounding of the cross and dot products is below 2^-23
+    // |M| |D| each), and within 2e-6 of the reference's difference of the two
+    // directions wrapped into [-pi, pi] away from the wrap
+    if (!(fabsf(mx) + fabsf(my) > 0x1p-40f && fabsf(mx) + fabsf(my) < 0x1p40f && fabsf(dx) + fabsf(dy) > 0x1p-40f &&
+          fabsf(dx) + fabsf(dy) < 0x1p40f))
+        return -1;
+    float v;
+    if (!phi_approx(mx * dx + my * dy, mx * dy - my * dx, v)) return -1;
+    const int c5 = clear_within(v, cut);
+    if (c5 <= 0 || algo == kAlgoEEEE) return c5;
+    const float ax = txy.z - S.lx, ay = txy.w - S.ly;
+    const float dr = __fsqrt_rn(__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(ay, ay)));
+    const float sdIn_d = S.urt - S.lrt;
+    const float arg = fmin_ref((-S.rtseg * 1.f + dr) * k2Rinv1GeVf / kPtCut, kSinAlphaMax);
+    float pa;
+    if (!(phi_approx(ax, ay, pa) && fabsf(arg) <= kSinAlphaMax)) return -1;
+    const float w = wrap_approx(pa - S.lphi);
+    if (!(fabsf(w) < 3.f)) return -1;
+    return clear_within(S.dpc - w, asinf(arg) + (0.02f / sdIn_d));
+}
+
+// the multiple-scattering factor of a candidate whose phase B1 passed already
+static __device__ __noinline__ float tl_muls_entry(int algo, const float* __restrict__ pack, int s, int t) {
+    const float rtIn = __ldg(pack + (int64_t)s * PK_N + PK_LRT), rtOut = __ldg(pack + (int64_t)t * PK_N + PK_LRT);
+    if (algo == kAlgoEEEE) return muls(rtOut - rtIn, 0.f, false);
+    return muls_sq(rtOut - rtIn, __ldg(pack + (int64_t)s * PK_N + PK_S2), __ldg(pack + (int64_t)s * PK_N + PK_S3),
+                   __ldg(pack + (int64_t)s * PK_N + PK_LR3Z), rtIn);
+}
+
 // phase B1 of a candidate through phase A (tl_phaseA_quick's survivors carry
 // no cut values): the exact phi-cut width and multiple-scattering factor
 // (tl_cut_values), then the cuts; the factor goes on to phase B2

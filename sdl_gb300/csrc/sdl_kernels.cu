@@ -848,10 +848,12 @@ __global__ void k_sg_pack(BatchDev b) {
         sg_pack_record(b, OI(b, kSG, s), OJ(b, kSG, s), f6, v);
         const uint32_t fl = __float_as_uint(v[PK_FLAGS]);
         const int64_t C = b.obj[kSG].cap;
-        const int fo[6] = {PK_LRT, PK_LZ, PK_LTD, PK_LA1, PK_UPHI, PK_FLAGS};
+        const int fo[10] = {PK_LRT, PK_LZ, PK_LTD, PK_LA1, PK_UPHI, PK_FLAGS, -1, PK_LX, PK_LY, PK_UX};
 #pragma unroll
-        for (int k = 0; k < 6; ++k) AT(b.sgouter, k * C + s, 7 * C) = v[fo[k]];
-        AT(b.sgouter, 6 * C + s, 7 * C) = 0.1f / v[PK_LRT];  // the PV-offset term of an outer segment
+        for (int k = 0; k < 10; ++k)
+            if (k != 6) AT(b.sgouter, k * C + s, 11 * C) = v[fo[k]];
+        AT(b.sgouter, 6 * C + s, 11 * C) = 0.1f / v[PK_LRT];  // the PV-offset term of an outer segment
+        AT(b.sgouter, 10 * C + s, 11 * C) = v[PK_UY];
         float4* dst = reinterpret_cast<float4*>(&AT(b.sgpack, s * PK_N, b.obj[kSG].cap * PK_N));
         for (int k = 0; k < PK_N / 4; ++k) dst[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
         // the pre-filter's feature records (inner role, outer role)
@@ -968,14 +970,26 @@ __device__ __forceinline__ int tl_outer_of(const BatchDev& b, int var, int s, in
     return var == 1 ? tl_outer_layer(b, s, q) : (var == 2 ? tl_outer_nav(b, s, q) : tl_outer(b, s, q));
 }
 
-// phase A's decision: the single-precision one, and tl_phaseA where that
-// cannot decide (the cut values are computed again in phase B1)
-__device__ __forceinline__ int tl_phase_a_decide(const SGV& S, const SGOuter& T) {
-    int algo = tl_phaseA_quick(S, T);
-    if (algo == kAlgoUnsure) {
-        float cut, muls;
+// Phases A and B1 of a candidate from the single-precision decisions, with
+// tl_phaseA where the first cannot decide: returns the algorithm (kAlgoNone:
+// rejected by phase A or B1) and sets b1 when phase B1 passed already (0:
+// phase B1 is left to k_tl_b1); exact tells whether an exact evaluation was
+// needed.  txy: the outer segment's anchors (load_sgo_xy).  The exact cut
+// values are computed again in phase B1.
+__device__ __forceinline__ int tl_ab1_decide(const SGV& S, const SGOuter& T, float4 txy, int& b1, bool& exact) {
+    float cut;
+    int algo = tl_phaseA_quick(S, T, cut);
+    exact = algo == kAlgoUnsure;
+    if (exact) {
+        float muls;
         algo = tl_phaseA(S, T, cut, muls);
     }
+    b1 = 0;
+    if (algo == kAlgoNone) return algo;
+    const int q = tl_phaseB1_quick(algo, S, txy, cut);
+    if (q == 0) return kAlgoNone;
+    b1 = q > 0;
+    exact = exact || q < 0;
     return algo;
 }
 
@@ -1005,26 +1019,28 @@ __device__ __forceinline__ void passbuf_flush(const BatchDev& b, PassBuf& pb) {
     __syncwarp();
     pb.n = 0;
 }
-__device__ __forceinline__ void passbuf_add(const BatchDev& b, PassBuf& pb, int algo, int s, int tt) {
+__device__ __forceinline__ void passbuf_add(const BatchDev& b, PassBuf& pb, int algo, int s, int tt, int b1) {
     const int lane = threadIdx.x & 31;
     const bool pass = algo != kAlgoNone;
     const unsigned m = __ballot_sync(0xffffffffu, pass);
     if (!m) return;
     const int c = __popc(m);
     if (pb.n + c > kPassBuf) passbuf_flush(b, pb);
-    if (pass) pb.e[pb.n + __popc(m & ((1u << lane) - 1u))] = make_int4(s, tt, algo, 0);
+    if (pass) pb.e[pb.n + __popc(m & ((1u << lane) - 1u))] = make_int4(s, tt, algo, b1);
     pb.n += c;
 }
 
 constexpr int kMlpWarps = kMlpTile / 32;
 
 // Tracklet candidates (Event.cc:611-693 with Tracklet.cc:144-2665) in three
-// kernels: k_tl_enum_a takes tasks of consecutive candidates from a shared
-// counter, runs phase A (the float cuts) on each and lists the survivors;
-// k_tl_b1 and k_tl_b2 run the two parts of phase B on compacted lists and
-// append the tracklets.  Each kernel keeps only its own phase's code
-// resident, and each phase runs on full warps.  The survivor list shares the
-// pre-filter's capacity and overflow handling (its count is n_kept).
+// kernels: the enumeration (k_tl_enum_a here: tasks of consecutive
+// candidates from a shared counter; k_tl_enum_tiles below for the module
+// map) runs phase A (the float cuts) and, for its survivors, the
+// single-precision decision of phase B1 on each candidate and lists the
+// survivors, marking those through phase B1 already; k_tl_b1 and k_tl_b2 run
+// the two parts of phase B on compacted lists and append the tracklets.  The
+// survivor list shares the pre-filter's capacity and overflow handling (its
+// count is n_kept).
 __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_a(BatchDev b) {
     __shared__ int4 pbuf[kEnumThreads / kWarp][kPassBuf];
     if (halted(b)) return;
@@ -1055,15 +1071,17 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_a(BatchDev b) {
         const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
         for (int64_t cb = base; cb < end; cb += kWarp) {
             const int64_t c = cb + lane;
-            int algo = kAlgoNone, s = 0, tt = 0;
+            int algo = kAlgoNone, s = 0, tt = 0, b1 = 0;
             if (c < end) {
                 s = (i0 == i1) ? i0 : find_obj(b, off, offlim, i0, i1, c);
                 tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
                 (void)IX(s, b.obj[kSG].cap);
                 (void)IX(tt, b.obj[kSG].cap);
-                algo = tl_phase_a_decide(load_sgv(b.sgpack, s), load_sgo(b.sgouter, b.obj[kSG].cap, tt));
+                const int64_t C = b.obj[kSG].cap;
+                bool exact;
+                algo = tl_ab1_decide(load_sgv(b.sgpack, s), load_sgo(b.sgouter, C, tt), load_sgo_xy(b.sgouter, C, tt), b1, exact);
             }
-            passbuf_add(b, pb, algo, s, tt);
+            passbuf_add(b, pb, algo, s, tt, b1);
         }
     }
     passbuf_flush(b, pb);
@@ -1175,10 +1193,11 @@ __device__ __forceinline__ int tile_outer(const BatchDev& b, int ev, int m, int 
 // segments (one entry per lane while the module has at most 32 connections),
 // then the inner segments' records (staged in shared memory, read there as
 // warp-uniform values) with the lanes' outer-segment fields.
-__global__ void __launch_bounds__(kEnumThreads) k_tl_enum_tiles(BatchDev b) {
+__global__ void __launch_bounds__(kEnumThreads, 4) k_tl_enum_tiles(BatchDev b) {
     __shared__ __align__(16) float4 srec[kEnumThreads / kWarp][kTileA * (PK_N / 4)];
     __shared__ int sidx[kEnumThreads / kWarp][kTileA];
     __shared__ int4 pbuf[kEnumThreads / kWarp][kPassBuf];
+    __shared__ float4 sxy[kEnumThreads / kWarp][kWarp];  // the lanes' outer anchors (phase B1)
     if (halted(b) || b.n_gm <= 0) return;
     const int64_t ntile = AT(b.toff, b.n_gm, NG1(b));
     const bool mapped = ntile <= b.tile_cap;
@@ -1213,6 +1232,7 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_tiles(BatchDev b) {
         if (has) {
             (void)IX(tt, sgcap);
             T = load_sgo(b.sgouter, sgcap, tt);
+            sxy[w][lane] = load_sgo_xy(b.sgouter, sgcap, tt);
         }
         __syncwarp();
         // stage the tile's inner-segment records (nat x 8 float4)
@@ -1228,20 +1248,25 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_tiles(BatchDev b) {
         __syncwarp();
         for (int r = 0; r < nat; ++r) {
             const int sr = sidx[w][r];
-            const int algo = has ? tl_phase_a_decide(sgv_from(reinterpret_cast<const float*>(&srec[w][r * (PK_N / 4)])), T)
-                                 : kAlgoNone;
-            passbuf_add(b, pb, algo, sr, tt);
+            int algo = kAlgoNone, b1 = 0;
+            if (has) {
+                bool exact;
+                algo = tl_ab1_decide(sgv_from(reinterpret_cast<const float*>(&srec[w][r * (PK_N / 4)])), T, sxy[w][lane], b1,
+                                     exact);
+            }
+            passbuf_add(b, pb, algo, sr, tt, b1);
         }
     }
     passbuf_flush(b, pb);
 }
 
 // Learned pre-filter of the tracklet candidates (no counterpart in the
-// reference).  It scores the phase-A survivor list (n_kept entries) in tiles
-// of 128 entries on the tensor cores; the entries whose logit reaches the
-// threshold go to the kept list (n_kept2 entries), which k_tl_b1 and k_tl_b2
-// judge.  A candidate that fails phase A gives no tracklet, so the tracklets
-// are those of the plain chain among the candidates the network keeps; the
+// reference).  It scores the enumeration's survivor list (n_kept entries:
+// through phase A, and through phase B1 or undecided there) in tiles of 128
+// entries on the tensor cores; the entries whose logit reaches the threshold
+// go to the kept list (n_kept2 entries), which k_tl_b1 and k_tl_b2 judge.  A
+// candidate that fails phase A or B1 gives no tracklet, so the tracklets are
+// those of the plain chain among the candidates the network keeps; the
 // network only sees phase-A survivors, the candidates it was trained on.
 // Each CTA takes every gridDim.x-th tile; while the tensor cores run a
 // tile's first layer, the CTA loads the next tile's entries and features.
@@ -1352,9 +1377,14 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const int4* 
         float muls = 0.f;
         if (i < n) {
             p = AT(list, i, b.kept_cap);
-            const B1Result r = tl_phaseB1_entry(p.z, b.sgpack, p.x, p.y);
-            pass = r.pass;
-            muls = r.muls;
+            if (p.w) {  // phase B1 passed in the enumeration
+                pass = true;
+                muls = tl_muls_entry(p.z, b.sgpack, p.x, p.y);
+            } else {
+                const B1Result r = tl_phaseB1_entry(p.z, b.sgpack, p.x, p.y);
+                pass = r.pass;
+                muls = r.muls;
+            }
         }
         const bool front = pass && p.z == kAlgoBBBB;
         const unsigned mf = __ballot_sync(0xffffffffu, front);
@@ -1458,10 +1488,14 @@ __global__ void k_tl_collect(BatchDev b, MlpCollect col) {
     }
 }
 
-// Self-check of phase A's single-precision decision over the tracklet
-// candidates of the last run: out[0] candidates, out[1] decided by
-// tl_phaseA_quick, out[2] left to tl_phaseA, out[3] decided differently from
-// tl_phaseA (0 when the margins hold).
+// Self-check of the enumeration's single-precision decisions (tl_ab1_decide:
+// phase A, then phase B1 for its survivors) over the tracklet candidates of
+// the last run, against the exact phase A and B1 on the packed records:
+// out[0] candidates, out[1] settled by the approximations alone, out[2] that
+// needed an exact evaluation, out[3] settled wrongly (0 when the margins
+// hold): rejected although both phases pass, accepted with another
+// algorithm or although phase A fails, or marked as through phase B1 although
+// it fails.
 __global__ void k_tl_quick_check(BatchDev b, unsigned long long* out) {
     if (halted(b)) return;
     const int64_t nobj = n_inner(b, kTL);
@@ -1476,15 +1510,19 @@ __global__ void k_tl_quick_check(BatchDev b, unsigned long long* out) {
         obj_bounds(b, nobj, total, c, c, lo, hi);
         const int s = find_obj(b, off, offlim, lo, hi, c);
         const int tt = tl_outer_of(b, lay, s, c - AT(off, s, offlim));
-        const SGV S = load_sgv(b.sgpack, s);
-        const SGOuter T = load_sgo(b.sgouter, b.obj[kSG].cap, tt);
-        const int q = tl_phaseA_quick(S, T);
+        const SGV S = load_sgv(b.sgpack, s), Tv = load_sgv(b.sgpack, tt);
+        const int64_t C = b.obj[kSG].cap;
+        int b1;
+        bool exact;
+        const int q = tl_ab1_decide(S, load_sgo(b.sgouter, C, tt), load_sgo_xy(b.sgouter, C, tt), b1, exact);
         float cut, muls;
-        const int e = tl_phaseA(S, T, cut, muls);
+        const int e = tl_phaseA(S, Tv, cut, muls);
+        const bool eb1 = e != kAlgoNone && tl_phaseB1_sgv(e, S, Tv, cut);
+        const bool bad = q == kAlgoNone ? eb1 : (q != e || (b1 && !eb1));
         n[0] += 1;
-        n[1] += q != kAlgoUnsure;
-        n[2] += q == kAlgoUnsure;
-        n[3] += q != kAlgoUnsure && q != e;
+        n[1] += !exact;
+        n[2] += exact;
+        n[3] += bad;
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {

@@ -40,8 +40,9 @@ struct BatchDev {
     int32_t* conn_first;           // n_ev * n_conn: offset of the entry's module's first object
     int64_t* conn_sum;             // n_gm
     float* sgpack;                 // segment cap * PK_N packed records for the tracklet stage
-    float* sgouter;                // segment cap * 7, one array per field: what phase A reads of an outer
-                                   //   segment (lrt, lz, ltd, la1, uphi, flags, 0.1/lrt; see SGOuter)
+    float* sgouter;                // segment cap * 11, one array per field: what the enumeration reads of an
+                                   //   outer segment (lrt, lz, ltd, la1, uphi, flags, 0.1/lrt: SGOuter;
+                                   //   lx, ly, ux, uy: load_sgo_xy)
     float* sgfeat;                 // segment cap * kFeatN: the pre-filter's per-segment feature records
     float* mdpack;                 // mini-doublet cap * kMdPack: packed records for the segment stage
     uint32_t* counters;            // n_ev * 110
@@ -58,7 +59,8 @@ struct BatchDev {
     int enum_grid[kNumStages];
     const unsigned char* mlp_pack; // packed pre-filter weights and threshold (kPackBytes)
     MlpStats* mlp_stats;           // pre-filter counts of the last run
-    int4* passa;                   // tracklet candidates through phase A: (inner, outer, algorithm, 0)
+    int4* passa;                   // tracklet candidates through phase A: (inner, outer, algorithm, 1 when
+                                   //   phase B1 passed already, else 0)
     int64_t kept_cap;              // entries of each survivor list
     unsigned long long* n_kept;    // phase-A survivors found (can exceed kept_cap: overflow)
     int4* kept;                    // the phase-A survivors the pre-filter kept, as passa

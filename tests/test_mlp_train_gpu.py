@@ -31,8 +31,10 @@ def test_trained_prefilter_recall_and_gain():
     # the pruned chain only ever loses objects, and keeps >= 99.5 % of the track candidates
     assert trained["tc_pruned"] <= trained["tc_plain"] and trained["tl_pruned"] <= trained["tl_plain"]
     assert trained["tc_recall"] >= 0.995
-    # the trained network drops most candidates and most of the exact-cut work ...
-    assert trained["pruned_fraction"] >= 0.6
+    # the trained network drops most of the candidates it scores (those through
+    # the float cuts and the enumeration's direction and betaIn decision) and
+    # most of the exact-cut work ...
+    assert trained["pruned_fraction"] >= 0.5
     assert trained["exact_cut_load_reduction"] >= 0.5
     # ... where the untrained one, at the same recall target, drops little
     assert trained["pruned_fraction"] >= untrained["pruned_fraction"] + 0.3

@@ -1,9 +1,10 @@
-"""The tracklet stage's single-precision phase-A decision (tl_phaseA_quick)
-against the exact float cuts (tl_phaseA) on every tracklet candidate of a
-batch at PU 100, 200 and 300, for the module-map, layer-pair and navigation
-candidate sets: it never settles a candidate differently, and it leaves only
-a small share of them to the exact cuts.  The object sets of the chain that
-uses it are checked against the reference and the oracle elsewhere."""
+"""The tracklet enumeration's single-precision decisions (tl_ab1_decide:
+phase A, then phase B1 for its survivors) against the exact cuts (tl_phaseA,
+tl_phaseB1_sgv) on every tracklet candidate of a batch at PU 100, 200 and
+300, for the module-map, layer-pair and navigation candidate sets: they
+never settle a candidate differently, and they leave only a small share of
+them to the exact cuts.  The object sets of the chain that uses them are
+checked against the reference and the oracle elsewhere."""
 import pytest
 
 from test_gpu_parity import run_gpu
@@ -33,4 +34,4 @@ def test_phase_a_decision_matches_exact_cuts(gpu, batch, flags):
     assert r["candidates"] > 1_000_000, r
     assert r["settled"] + r["exact"] == r["candidates"], r
     assert r["mismatches"] == 0, r
-    assert r["exact"] <= 1e-3 * r["candidates"], r
+    assert r["exact"] <= 1e-2 * r["candidates"], r
