@@ -1364,11 +1364,30 @@ __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
 // through it go to the phase-B2 list, BBBB ones from the front and the others
 // from the back, so that phase B2's warps mostly run one algorithm.  Front
 // and back never meet: together they hold at most count <= kept_cap entries.
+// Each warp collects its BBBB and its other survivors in two shared-memory
+// buffers and appends each with one atomic per batch (as passbuf_add).
+constexpr int kPbBuf = 64;
+__device__ __forceinline__ void pb_flush(const BatchDev& b, int4* buf, int& n, bool front) {
+    __syncwarp();
+    const int lane = threadIdx.x & 31;
+    unsigned long long p0 = 0;
+    if (lane == 0 && n) p0 = atomicAdd(b.n_pb + (front ? 0 : 1), (unsigned long long)n);
+    p0 = __shfl_sync(0xffffffffu, p0, 0);
+    for (int k = lane; k < n; k += kWarp) {
+        const int64_t q = (int64_t)p0 + k;  // below the list length <= kept_cap
+        AT(b.pb, front ? q : b.kept_cap - 1 - q, b.kept_cap) = buf[k];
+    }
+    __syncwarp();
+    n = 0;
+}
+
 __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const int4* __restrict__ list,
                                                          const unsigned long long* count) {
+    __shared__ int4 fbuf[kEnumThreads / kWarp][kPbBuf], bbuf[kEnumThreads / kWarp][kPbBuf];
     if (halted(b)) return;
     const int64_t n = min((int64_t)*count, b.kept_cap);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int nfb = 0, nbb = 0;  // entries held in this warp's buffers
     const int64_t nwarp = (int64_t)gridDim.x * (kEnumThreads / 32);
     for (int64_t base = ((int64_t)blockIdx.x * (kEnumThreads / 32) + w) * kWarp; base < n; base += nwarp * kWarp) {
         const int64_t i = base + lane;
@@ -1390,31 +1409,33 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const int4* 
         const unsigned mf = __ballot_sync(0xffffffffu, front);
         const unsigned mb = __ballot_sync(0xffffffffu, pass && !front);
         if (!(mf | mb)) continue;
-        unsigned long long pf = 0, pbk = 0;
-        if (lane == 0) {
-            if (mf) pf = atomicAdd(b.n_pb, (unsigned long long)__popc(mf));
-            if (mb) pbk = atomicAdd(b.n_pb + 1, (unsigned long long)__popc(mb));
-        }
-        pf = __shfl_sync(0xffffffffu, pf, 0);
-        pbk = __shfl_sync(0xffffffffu, pbk, 0);
+        if (nfb + __popc(mf) > kPbBuf) pb_flush(b, fbuf[w], nfb, true);
+        if (nbb + __popc(mb) > kPbBuf) pb_flush(b, bbuf[w], nbb, false);
         if (pass) {
             const unsigned below = (1u << lane) - 1u;
-            const int64_t pos = front ? (int64_t)pf + __popc(mf & below) : b.kept_cap - 1 - ((int64_t)pbk + __popc(mb & below));
-            AT(b.pb, pos, b.kept_cap) = make_int4(p.x, p.y, p.z, __float_as_int(muls));
+            const int4 e = make_int4(p.x, p.y, p.z, __float_as_int(muls));
+            if (front) fbuf[w][nfb + __popc(mf & below)] = e;
+            else bbuf[w][nbb + __popc(mb & below)] = e;
         }
+        nfb += __popc(mf);
+        nbb += __popc(mb);
     }
+    pb_flush(b, fbuf[w], nfb, true);
+    pb_flush(b, bbuf[w], nbb, false);
 }
 
 // Phase B2 on one part of the phase-B2 list (kSet kB2BBBB: the front, BBBB
 // entries; kB2Others: the back, BBEE and EEEE entries); appends the tracklets.
 template <int kSet>
 __global__ void __launch_bounds__(kEnumThreads) k_tl_b2(BatchDev b) {
+    __shared__ int rbuf[kEnumThreads / kWarp][3][kRecBuf];
     if (halted(b)) return;
     const int64_t nf = min((int64_t)b.n_pb[0], b.kept_cap);
     const int64_t n = kSet == kB2BBBB ? nf : min((int64_t)b.n_pb[1], b.kept_cap - nf);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const bool nm1 = (b.flags & kFlagTLNm1) != 0;
     const int64_t nwarp = (int64_t)gridDim.x * (kEnumThreads / 32);
+    RecBuf<0> rb{rbuf[w]};
     for (int64_t base = ((int64_t)blockIdx.x * (kEnumThreads / 32) + w) * kWarp; base < n; base += nwarp * kWarp) {
         const int64_t i = base + lane;
         bool pass = false;
@@ -1426,8 +1447,18 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b2(BatchDev b) {
             tt = p.y;
             pass = tl_phaseB2<kSet>(p.z, b.sgpack, s, tt, __int_as_float(p.w), nm1);
         }
-        append_rec(b, kTL, pass, s, tt, pass ? OG(b, kSG, s) : 0, nullptr);
+        const unsigned m = __ballot_sync(0xffffffffu, pass);
+        if (!m) continue;
+        if (rb.n + __popc(m) > kRecBuf) rec_flush<0>(b, kTL, rb);
+        if (pass) {
+            const int k = rb.n + __popc(m & ((1u << lane) - 1u));
+            rb.e[0][k] = s;
+            rb.e[1][k] = tt;
+            rb.e[2][k] = OG(b, kSG, s);
+        }
+        rb.n += __popc(m);
     }
+    rec_flush<0>(b, kTL, rb);
 }
 
 __device__ __forceinline__ float hash_unit(unsigned long long c, unsigned long long seed) {
