@@ -388,6 +388,8 @@ int ensure_buffers(sdlg_ctx* ctx) {
     AL(b.toff, n_gm + 1);
     b.tile_cap = 2 * std::max<int64_t>(ctx->cap_obj[kSG], n_gm);
     AL(b.tile_gm, b.tile_cap);
+    b.olist_cap = 4 * std::max<int64_t>(ctx->cap_obj[kSG], n_gm);
+    AL(b.olist, b.olist_cap);
 #undef AL
     CK(cudaMemcpyAsync(b.n_gm_dev, &n_gm, sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));

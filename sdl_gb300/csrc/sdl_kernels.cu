@@ -456,11 +456,16 @@ struct SGStage {
     __device__ static bool eval(const BatchDev& b, int a, int64_t q, int& oi, int& oj, float* fv) {
         const int n_mod = b.geo.n_mod;
         const int g1 = OG(b, kMD, a);
-        const int ev = ev_of(b, g1), m1 = g1 - ev * n_mod;
-        int pref;
-        const int k = conn_entry(b, ev, m1, q, pref);
-        const int g2 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
-        const int bmd = (int)(OFF(b, kMD, g2) + (q - pref));
+        int bmd;
+        if (AT(b.toff, b.n_gm, NG1(b)) <= b.olist_cap) {
+            bmd = AT(b.olist, AT(b.toff, g1, NG1(b)) + q, b.olist_cap);  // k_sg_olist_fill
+        } else {
+            const int ev = ev_of(b, g1), m1 = g1 - ev * n_mod;
+            int pref;
+            const int k = conn_entry(b, ev, m1, q, pref);
+            const int g2 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
+            bmd = (int)(OFF(b, kMD, g2) + (q - pref));
+        }
         oi = a; oj = bmd;
         return sg_pair(b, a, bmd, true, fv);
     }
@@ -1657,6 +1662,33 @@ __global__ void k_conn_sum(BatchDev b, int src, int cst) {
     }
 }
 
+// The outer lists of the segment candidates, written out: for every global
+// module g holding mini-doublets, the mini-doublets of g's connected modules
+// in connection-list order (entry q of g's list at olist[toff[g] + q]), so
+// that a candidate finds its outer mini-doublet with one load.  toff holds
+// the list lengths, then (scanned) the offsets; the lists are not written
+// when they exceed olist_cap (the candidates then search the connection list).
+__global__ void k_sg_olist_count(BatchDev b) {
+    if (halted(b)) return;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < b.n_gm; g += (int64_t)gridDim.x * blockDim.x)
+        AT(b.toff, g, NG1(b)) = OFF(b, kMD, g + 1) > OFF(b, kMD, g) ? AT(b.conn_sum, g, b.n_gm) : 0;
+}
+__global__ void k_sg_olist_fill(BatchDev b) {
+    if (halted(b) || AT(b.toff, b.n_gm, NG1(b)) > b.olist_cap) return;
+    const int n_mod = b.geo.n_mod;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < b.n_gm; g += (int64_t)gridDim.x * blockDim.x) {
+        int64_t o = AT(b.toff, g, NG1(b));
+        if (AT(b.toff, g + 1, NG1(b)) == o) continue;
+        const int ev = ev_of(b, g), m = (int)(g - (int64_t)ev * n_mod);
+        const int k0 = AT(b.geo.conn_off, m, NM(b) + 1), k1 = AT(b.geo.conn_off, m + 1, NM(b) + 1);
+        for (int k = k0; k < k1; ++k) {
+            const int64_t g2 = (int64_t)ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
+            const int64_t e = OFF(b, kMD, g2 + 1);
+            for (int64_t md = OFF(b, kMD, g2); md < e; ++md) AT(b.olist, o++, b.olist_cap) = (int)md;
+        }
+    }
+}
+
 __global__ void k_sg_count(BatchDev b) {
     if (halted(b)) return;
     const int64_t n = n_inner(b, kSG);
@@ -1985,7 +2017,10 @@ void launch_sg(const BatchDev& b, cudaStream_t s, Hooks* h) {
     }
     k_conn_sum<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kMD, kSG);
     k_sg_count<<<b.n_sm * 8, 256, 0, s>>>(b);
-    if (h) h->launches += 2;
+    k_sg_olist_count<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b);
+    scan_h(b, b.toff, b.n_gm_dev, b.n_gm, s, h);
+    k_sg_olist_fill<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b);
+    if (h) h->launches += 4;
     enum_and_group<SGStage>(b, s, h);
 }
 

@@ -81,6 +81,8 @@ struct BatchDev {
     int64_t* toff;                 // n_gm + 1: tile counts -> offsets
     int32_t* tile_gm;              // tile_cap: the global module of each tile (when the tiles fit)
     int64_t tile_cap;
+    int32_t* olist;                // olist_cap: the segment candidates' outer lists (k_sg_olist_fill; offsets in toff)
+    int64_t olist_cap;
     int4* pb;                      // candidates through phase B1: (inner, outer, algorithm, muls bits), BBBB
                                    //   from the front, the others from the back
     unsigned long long* n_pb;      // [2]: BBBB entries, other entries (kept_cap in all)
