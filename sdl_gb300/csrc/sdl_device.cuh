@@ -1008,11 +1008,12 @@ __device__ __forceinline__ int tl_phaseA_quick(const SGV& S, const TSeg& T, floa
         const float drt_InSeg = S.urt - S.lrt;
         const float coshEta = S.cosh;
         const float zp = zpitch_InLo + zpitch_OutLo;
+        // (the two quotients by __fdividef: 2 ulp instead of 0.5, inside the bound)
         float dzErr = zp * zp * 2.f;
-        dzErr += sdlMuls * sdlMuls * drt_OutLo_InLo * drt_OutLo_InLo / 3.f * coshEta * coshEta;
+        dzErr += __fdividef(sdlMuls * sdlMuls * drt_OutLo_InLo * drt_OutLo_InLo, 3.f) * coshEta * coshEta;
         dzErr = __fsqrt_rn(dzErr);
         const float dzMean = S.dzdr * drt_OutLo_InLo;
-        const float pw = dzErr / drt_InSeg * drt_OutLo_InLo;
+        const float pw = __fdividef(dzErr, drt_InSeg) * drt_OutLo_InLo;
         const float zWindow = pw + zp;
         const float mLo = dzMean * (zIn > 0.f ? 1.f : dzDrtScale), mHi = dzMean * (zIn < 0.f ? 1.f : dzDrtScale);
         const float zLoPointed = zIn + mLo - zWindow;
@@ -1190,8 +1191,8 @@ __device__ __forceinline__ int tl_phaseB1_quick(int algo, const SGV& S, float4 t
     float pa;
     if (!(phi_approx(ax, ay, pa) && fabsf(arg) <= kSinAlphaMax)) return -1;
     const float w = wrap_approx(pa - S.lphi);
-    if (!(fabsf(w) < 3.f)) return -1;
-    return clear_within(S.dpc - w, asinf(arg) + (0.02f / sdIn_d));
+    if (!(fabsf(w) < 3.f) || !(fabsf(sdIn_d) > 1e-3f)) return -1;
+    return clear_within(S.dpc - w, asinf(arg) + __fdividef(0.02f, sdIn_d));  // 2 ulp of at most 20
 }
 
 // the multiple-scattering factor of a candidate whose phase B1 passed already
