@@ -575,6 +575,9 @@ __device__ __forceinline__ float sg_barrel_cut(int lIn, float rtOut, float outAs
 // Segment.cc:364-599.  outAsin / outTanf: asin(min(rtOut*k,.95)) of the
 // outer anchor and its float tan; cutPrev: sg_barrel_cut for the barrel
 // layer below the outer one (k_md_pack).
+// kPre: only the first cuts (the z window and the phi cut), for the segment
+// stage's first pass; a candidate they reject fails the whole algorithm
+template <bool kPre = false>
 __device__ __forceinline__ bool sg_barrel(const MDView& im, const MDView& om, float outAsin, float outTanf, float cutPrev,
                                           SGVals& v) {
     const float rtIn = im.a.rt, rtOut = om.a.rt, zIn = im.a.z, zOut = om.a.z;
@@ -588,6 +591,7 @@ __device__ __forceinline__ bool sg_barrel(const MDView& im, const MDView& om, fl
     const float sdCut = prev ? cutPrev : sg_barrel_cut(im.m->layer, rtOut, outAsin);
     const float deltaPhi = dphi(im.a, om.a);
     if (!(fabsf(deltaPhi) <= sdCut)) return false;
+    if (kPre) return true;
     v.dphichange = dphichange(im.a, om.a);
     if (!(fabsf(v.dphichange) <= sdCut)) return false;
     return dalpha_cuts(im, om, v.dphichange);
@@ -596,6 +600,8 @@ __device__ __forceinline__ bool sg_barrel(const MDView& im, const MDView& om, fl
 // Segment.cc:601-859.  connected: outer module is in the inner module's
 // connection list (cut #0); phiHi / phiLo: the phi of the outer anchor's
 // strip-edge points (the anchor itself for PS modules; k_md_pack).
+// kPre: only the first cuts (connection, rt window and phi cut), as sg_barrel
+template <bool kPre = false>
 __device__ __forceinline__ bool sg_endcap(const MDView& im, const MDView& om, float outAsin, float outTanf,
                                           bool connected, float phiHi, float phiLo, SGVals& v) {
     const ModDev& I = *im.m;
@@ -617,6 +623,7 @@ __device__ __forceinline__ bool sg_endcap(const MDView& im, const MDView& om, fl
     const float dPhiPos = dphi(im.a, om.a);
     const float sdCut = sdSlope;
     if (!(fabsf(dPhiPos) <= sdCut)) return false;
+    if (kPre) return true;
     const float hiP = phi_mpi_pi(phiHi - im.a.phi);  // dphi(im.a, oHi)
     const float loP = phi_mpi_pi(phiLo - im.a.phi);
     const bool hiBigger = iabs(trunc_i32(hiP)) > iabs(trunc_i32(loP));

@@ -433,14 +433,15 @@ __global__ void k_md_pack(BatchDev b) {
 // segment algorithm on inner MD a and outer MD bmd (Segment.cc:337-859);
 // `connected`: the outer MD's module is in the inner module's connection list
 // (the endcap algorithm's first requirement, Segment.cc:613-633)
+template <bool kPre = false>
 __device__ __forceinline__ bool sg_pair_rec(const MDView& im, const MDRec& orec, bool connected, float* fv) {
     const MDView& om = orec.v;
     SGVals v;
     v.dphi = v.dphimin = v.dphimax = v.dphichange = v.dphiminchange = v.dphimaxchange = 0.f;
     bool pass;
     const bool ob = om.m->subdet == kBarrel;
-    if (ob) pass = sg_barrel(im, om, orec.a1, orec.tf, orec.c0, v);
-    else pass = sg_endcap(im, om, orec.a1, orec.tf, connected, orec.c0, orec.c1, v);
+    if (ob) pass = sg_barrel<kPre>(im, om, orec.a1, orec.tf, orec.c0, v);
+    else pass = sg_endcap<kPre>(im, om, orec.a1, orec.tf, connected, orec.c0, orec.c1, v);
     fv[0] = v.dphi; fv[1] = v.dphimin; fv[2] = v.dphimax;
     fv[3] = v.dphichange; fv[4] = v.dphiminchange; fv[5] = v.dphimaxchange;
     return pass;
@@ -450,27 +451,18 @@ __device__ __forceinline__ bool sg_pair(const BatchDev& b, int a, int bmd, bool 
 }
 
 // segment candidates along the module map (Event.cc:445-522): candidate q of
-// inner MD a is an MD of a connected module, in connection-list order
-struct SGStage {
-    static constexpr int kSt = kSG;
-    __device__ static bool eval(const BatchDev& b, int a, int64_t q, int& oi, int& oj, float* fv) {
-        const int n_mod = b.geo.n_mod;
-        const int g1 = OG(b, kMD, a);
-        int bmd;
-        if (AT(b.toff, b.n_gm, NG1(b)) <= b.olist_cap) {
-            bmd = AT(b.olist, AT(b.toff, g1, NG1(b)) + q, b.olist_cap);  // k_sg_olist_fill
-        } else {
-            const int ev = ev_of(b, g1), m1 = g1 - ev * n_mod;
-            int pref;
-            const int k = conn_entry(b, ev, m1, q, pref);
-            const int g2 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
-            bmd = (int)(OFF(b, kMD, g2) + (q - pref));
-        }
-        oi = a; oj = bmd;
-        return sg_pair(b, a, bmd, true, fv);
-    }
-    __device__ static int group_of(const BatchDev& b, int a) { return OG(b, kMD, a); }
-};
+// inner MD a is an MD of a connected module, in connection-list order; the
+// outer mini-doublet of candidate q of inner MD a
+__device__ __forceinline__ int sg_outer_md(const BatchDev& b, int a, int64_t q) {
+    const int n_mod = b.geo.n_mod;
+    const int g1 = OG(b, kMD, a);
+    if (AT(b.toff, b.n_gm, NG1(b)) <= b.olist_cap) return AT(b.olist, AT(b.toff, g1, NG1(b)) + q, b.olist_cap);  // k_sg_olist_fill
+    const int ev = ev_of(b, g1), m1 = g1 - ev * n_mod;
+    int pref;
+    const int k = conn_entry(b, ev, m1, q, pref);
+    const int g2 = ev * n_mod + AT(b.geo.conn_idx, k, NC(b));
+    return (int)(OFF(b, kMD, g2) + (q - pref));
+}
 
 // ------------------------------------------------------------------ layer pairs
 // Layer.cc:32-50: the outer layer slots paired with inner slot si (barrel
@@ -1265,6 +1257,92 @@ __global__ void __launch_bounds__(kEnumThreads, 4) k_tl_enum_tiles(BatchDev b) {
     passbuf_flush(b, pb);
 }
 
+// Module-map segment candidates in two passes (Event.cc:445-522 with
+// Segment.cc:337-859): k_sg_enum_a takes tasks of consecutive candidates
+// like k_enum, runs the algorithm's first cuts (sg_pair_rec<true>: the same
+// float code as the whole algorithm up to its phi cut) and lists the
+// survivors in the passa list; k_sg_b runs the whole algorithm on the list on
+// full warps and appends the segments.  The first cuts reject most
+// candidates, so the expensive rest (the direction-change and dAlpha cuts)
+// no longer runs beside idle lanes.
+__global__ void __launch_bounds__(kEnumThreads) k_sg_enum_a(BatchDev b) {
+    __shared__ int4 pbuf[kEnumThreads / kWarp][kPassBuf];
+    if (halted(b)) return;
+    const int64_t nobj = n_inner(b, kSG);
+    if (nobj <= 0) return;
+    const int64_t* off = b.cand[kSG];
+    const int64_t offlim = b.cand_cap[kSG] + 1;
+    const int64_t total = AT(off, nobj, offlim);
+    const int task = b.enum_task[kSG] > 0 ? b.enum_task[kSG] : kTaskDefault;
+    const int64_t ntask = (total + task - 1) / task;
+    const int lane = threadIdx.x & 31;
+    PassBuf pb{pbuf[threadIdx.x >> 5]};
+    for (;;) {
+        unsigned long long t = 0;
+        if (lane == 0) t = atomicAdd(b.task + kSG, 1ull);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if ((int64_t)t >= ntask) break;
+        const int64_t base = (int64_t)t * task;
+        const int64_t end = min(base + task, total);
+        int ilo = 0;
+        if (lane < 2) {
+            int lo, hi;
+            obj_bounds(b, nobj, total, base, end - 1, lo, hi);
+            ilo = find_obj(b, off, offlim, lo, hi, lane == 0 ? base : end - 1);
+        }
+        const int i0 = __shfl_sync(0xffffffffu, ilo, 0);
+        const int i1 = __shfl_sync(0xffffffffu, ilo, 1);
+        for (int64_t cb = base; cb < end; cb += kWarp) {
+            const int64_t c = cb + lane;
+            int a = 0, bmd = 0;
+            bool pass = false;
+            if (c < end) {
+                a = (i0 == i1) ? i0 : find_obj(b, off, offlim, i0, i1, c);
+                bmd = sg_outer_md(b, a, c - AT(off, a, offlim));
+                (void)IX(bmd, b.obj[kMD].cap);
+                float fv[6];
+                pass = sg_pair_rec<true>(md_rec(b, a).v, md_rec(b, bmd), true, fv);
+            }
+            passbuf_add(b, pb, pass ? 1 : kAlgoNone, a, bmd, 0);
+        }
+    }
+    passbuf_flush(b, pb);
+}
+
+__global__ void __launch_bounds__(kEnumThreads) k_sg_b(BatchDev b) {
+    __shared__ int rbuf[kEnumThreads / kWarp][3 + 6][kRecBuf];
+    if (halted(b)) return;
+    const int64_t n = min((int64_t)*b.n_kept, b.kept_cap);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t nwarp = (int64_t)gridDim.x * (kEnumThreads / 32);
+    RecBuf<6> rb{rbuf[w]};
+    for (int64_t base = ((int64_t)blockIdx.x * (kEnumThreads / 32) + w) * kWarp; base < n; base += nwarp * kWarp) {
+        const int64_t i = base + lane;
+        bool pass = false;
+        int a = 0, bmd = 0;
+        float fv[6];
+        if (i < n) {
+            const int4 e = AT(b.passa, i, b.kept_cap);
+            a = e.x;
+            bmd = e.y;
+            pass = sg_pair(b, a, bmd, true, fv);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, pass);
+        if (!m) continue;
+        if (rb.n + __popc(m) > kRecBuf) rec_flush<6>(b, kSG, rb);
+        if (pass) {
+            const int k = rb.n + __popc(m & ((1u << lane) - 1u));
+            rb.e[0][k] = a;
+            rb.e[1][k] = bmd;
+            rb.e[2][k] = OG(b, kMD, a);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) rb.e[3 + q][k] = __float_as_int(fv[q]);
+        }
+        rb.n += __popc(m);
+    }
+    rec_flush<6>(b, kSG, rb);
+}
+
 // Learned pre-filter of the tracklet candidates (no counterpart in the
 // reference).  It scores the enumeration's survivor list (n_kept entries:
 // through phase A, and through phase B1 or undecided there) in tiles of 128
@@ -2020,8 +2098,19 @@ void launch_sg(const BatchDev& b, cudaStream_t s, Hooks* h) {
     k_sg_olist_count<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b);
     scan_h(b, b.toff, b.n_gm_dev, b.n_gm, s, h);
     k_sg_olist_fill<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b);
+    scan_h(b, b.cand[kSG], b.obj[kMD].mod_cnt + b.n_gm, b.cand_cap[kSG], s, h);
+    k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, kSG);
+    if (h) h->launches += 5;
+    // first cuts -> survivor list -> whole algorithm (k_sg_enum_a, k_sg_b)
+    if (h && h->timed) rec_event(h->enum_start[kSG], s);
+    cudaMemsetAsync(b.n_kept, 0, sizeof(unsigned long long), s);
+    k_sg_enum_a<<<b.n_sm * enum_grid(b, kSG), kEnumThreads, 0, s>>>(b);
+    k_sg_b<<<b.n_sm * enum_grid(b, kSG), kEnumThreads, 0, s>>>(b);
+    if (h && h->timed) rec_event(h->enum_stop[kSG], s);
+    k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kSG);
+    scan_h(b, b.obj[kSG].mod_cnt, b.n_gm_dev, b.n_gm, s, h);
+    k_scatter<<<b.n_sm * 8, 256, 0, s>>>(b, kSG);
     if (h) h->launches += 4;
-    enum_and_group<SGStage>(b, s, h);
 }
 
 // the join index of stage st's objects (segments or tracklets), keyed by
