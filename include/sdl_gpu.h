@@ -189,7 +189,9 @@ int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3);
  * Functions 16 (direction of a point by atan2f) and 17 (asinf) are the
  * tracklet cuts' single-precision approximations: "differs" there means
  * more than 2e-6 away from the exact value.  Functions 18 and 19 are tan(x)
- * and tan(x) / x (the hits' tan of their asin angle). */
+ * and tan(x) / x (the hits' tan of their asin angle).  Function 20 is the
+ * polynomial direction of the tracklet enumeration's phase-B1 decision
+ * ("differs": more than 2.5e-6 away). */
 int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64_t n, uint64_t seed, uint64_t* out8);
 
 /* Self-check of the tracklet enumeration's single-precision decisions (no

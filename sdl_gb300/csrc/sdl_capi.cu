@@ -1125,7 +1125,7 @@ int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3) {
 int64_t sdlg_last_launches(const sdlg_ctx* ctx) { return ctx ? ctx->launches_per_run : -1; }
 
 int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64_t n, uint64_t seed, uint64_t* out8) {
-    if (!ctx || !out8 || n < 0 || fn < 0 || fn > 19) return SDLG_ERR_ARG;
+    if (!ctx || !out8 || n < 0 || fn < 0 || fn > 20) return SDLG_ERR_ARG;
     cudaSetDevice(ctx->device);
     unsigned long long* d = nullptr;
     CK(cudaMalloc(&d, 8 * sizeof(unsigned long long)));

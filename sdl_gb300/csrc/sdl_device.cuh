@@ -1109,6 +1109,35 @@ __device__ __forceinline__ bool phi_approx(float x, float y, float& p) {
     p = atan2f(y, x);
     return true;
 }
+// atan(q) for q in [0, 1] as q * P(q^2) with P of degree 5, fitted to atan
+// near-minimax (least squares at Chebyshev nodes, reweighted by the error)
+// and rounded to float: evaluated in float as below, within 1.76e-6 of
+// atan(q) for every float q in [0, 1] (tests/test_atan_approx.py runs them
+// all with these coefficients)
+__device__ constexpr float kAtanP[6] = {0.999977231f, -0.332622826f, 0.193540379f, -0.116426416f, 0.052647233f,
+                                       -0.0117190806f};
+__device__ __forceinline__ float atan01_approx(float q) {
+    const float s = __fmul_rn(q, q);
+    float p = kAtanP[5];
+#pragma unroll
+    for (int k = 4; k >= 0; --k) p = __fadd_rn(__fmul_rn(p, s), kAtanP[k]);
+    return __fmul_rn(q, p);
+}
+// direction of (x, y) from atan01_approx: q = min / max by __fdividef (2 ulp,
+// below 1.2e-7 in q), then pi/2 - r and pi - r in float (constants and
+// roundings below 4.2e-7): within 2.5e-6 of atan2(y, x); false where
+// phi_approx is false
+__device__ __forceinline__ bool phi_fast(float x, float y, float& p) {
+    const float ax = fabsf(x), ay = fabsf(y);
+    const float m = ax + ay;
+    if (!(m > 0x1p-60f && m < 0x1p60f)) return false;
+    float r = atan01_approx(__fdividef(fminf(ax, ay), fmaxf(ax, ay)));
+    if (ay > ax) r = 1.57079637f - r;
+    if (x < 0.f) r = 3.14159274f - r;
+    p = copysignf(r, y);
+    return true;
+}
+
 // a difference of two directions in [-pi, pi], into [-pi, pi]
 __device__ __forceinline__ float wrap_approx(float d) {
     return d > kPiF ? d - 2.f * kPiF : (d < -kPiF ? d + 2.f * kPiF : d);
@@ -1168,10 +1197,10 @@ static __device__ __noinline__ bool tl_phaseB1(int algo, const float* __restrict
 }
 // Phase B1 from the approximations alone, with an approximate phi-cut width
 // (tl_phaseA_quick's, within 3e-6 of the exact one, or the exact one): the
-// direction approximations are within 2e-6 of the exact angles (functions 16
-// and 17 of the math self-check), so with the width's error every comparison
-// clear_within decides holds by over 9e-5 in exact arithmetic as well, and
-// the result is tl_phaseB1_sgv's.  txy: the outer segment's (lx, ly, ux, uy).
+// directions (phi_fast) are within 2.5e-6 of the exact angles and asinf
+// within 2e-6 (functions 20 and 17 of the math self-check), so with the
+// width's error every comparison clear_within decides holds by over 9e-5 in
+// exact arithmetic as well, and the result is tl_phaseB1_sgv's.  txy: the outer segment's (lx, ly, ux, uy).
 // 1: passes, 0: fails, -1: left to tl_phaseB1_sgv (NaN width included).
 __device__ __forceinline__ int tl_phaseB1_quick(int algo, const SGV& S, float4 txy, float cut) {
     float mx = 0.f, my = 0.f;
@@ -1180,15 +1209,15 @@ __device__ __forceinline__ int tl_phaseB1_quick(int algo, const SGV& S, float4 t
     mx /= 2.f; my /= 2.f;
     const float dx = txy.x - S.lx, dy = txy.y - S.ly;
     // the angle from the mid-point direction M to D = OutLo - InLo as one
-    // atan2 of (M x D, M . D): within 2^-22 of the exact angle whatever the
-    // lengths (the rounding of the cross and dot products is below 2^-23
-    // |M| |D| each), and within 2e-6 of the reference's difference of the two
+    // atan2 of (M x D, M . D): the rounding of the cross and dot products
+    // (below 2^-23 |M| |D| each) moves it by under 2^-22 whatever the lengths,
+    // so it is within 4e-6 of the reference's difference of the two
     // directions wrapped into [-pi, pi] away from the wrap
     if (!(fabsf(mx) + fabsf(my) > 0x1p-40f && fabsf(mx) + fabsf(my) < 0x1p40f && fabsf(dx) + fabsf(dy) > 0x1p-40f &&
           fabsf(dx) + fabsf(dy) < 0x1p40f))
         return -1;
     float v;
-    if (!phi_approx(mx * dx + my * dy, mx * dy - my * dx, v)) return -1;
+    if (!phi_fast(mx * dx + my * dy, mx * dy - my * dx, v)) return -1;
     const int c5 = clear_within(v, cut);
     if (c5 <= 0 || algo == kAlgoEEEE) return c5;
     const float ax = txy.z - S.lx, ay = txy.w - S.ly;
@@ -1196,7 +1225,7 @@ __device__ __forceinline__ int tl_phaseB1_quick(int algo, const SGV& S, float4 t
     const float sdIn_d = S.urt - S.lrt;
     const float arg = fmin_ref((-S.rtseg * 1.f + dr) * k2Rinv1GeVf / kPtCut, kSinAlphaMax);
     float pa;
-    if (!(phi_approx(ax, ay, pa) && fabsf(arg) <= kSinAlphaMax)) return -1;
+    if (!(phi_fast(ax, ay, pa) && fabsf(arg) <= kSinAlphaMax)) return -1;
     const float w = wrap_approx(pa - S.lphi);
     if (!(fabsf(w) < 3.f) || !(fabsf(sdIn_d) > 1e-3f)) return -1;
     return clear_within(S.dpc - w, asinf(arg) + __fdividef(0.02f, sdIn_d));  // 2 ulp of at most 20

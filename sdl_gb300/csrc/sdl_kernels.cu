@@ -2242,7 +2242,7 @@ __global__ void k_math_check(int fn, int exhaustive, unsigned long long start, l
             const unsigned long long h4 = mix64(h3 + 0x632BE59BD9B4E019ull);
             const float sa = (h1 & 1) ? -1.f : 1.f, sb = (h2 & 1) ? -1.f : 1.f;
             switch (fn) {
-                case 1: case 2: case 16:  // coordinates: magnitudes 2^-12..2^9, a fraction on axes and diagonals
+                case 1: case 2: case 16: case 20:  // coordinates: magnitudes 2^-12..2^9, a fraction on axes and diagonals
                     a = sa * hash_log(h1, -12.f, 9.f);
                     b = sb * hash_log(h2, -12.f, 9.f);
                     if ((h3 & 15) == 0) b = sb * fabsf(a) * (1.f + (float)((h4 >> 40) & 0xff) * 0x1p-20f);
@@ -2310,13 +2310,16 @@ __global__ void k_math_check(int fn, int exhaustive, unsigned long long start, l
             case 17: ok = fabsf(a) <= kSinAlphaMax; if (ok) { f = asinf(a); ref = f_asin(a); } break;
             case 18: ok = f_tan_fast(a, false, f); if (ok) ref = f_tan(a); break;
             case 19: ok = f_tan_fast(a, true, f); if (ok) ref = f_tan_over_d(a); break;
+            case 20: ok = phi_fast(a, b, f); if (ok) ref = phi_of(a, b); break;
             default: break;
         }
-        // functions 16 and 17 are the approximations of phase B1: within 2e-6
-        // of the exact value (directions compared modulo 2 pi); the others
-        // must match the double evaluation bit for bit
-        const bool bad = (fn == 16 || fn == 17) ? ok && !(fabsf(fn == 16 ? wrap_approx(f - ref) : f - ref) <= 2e-6f)
-                                  : ok && __float_as_uint(f) != __float_as_uint(ref) && !(isnan(f) && isnan(ref));
+        // functions 16, 17 and 20 are the approximations of phase B1: within
+        // 2e-6 (16, 17) and 2.5e-6 (20) of the exact value (directions compared
+        // modulo 2 pi); the others must match the double evaluation bit for bit
+        const bool approx = fn == 16 || fn == 17 || fn == 20;
+        const float tol = fn == 20 ? 2.5e-6f : 2e-6f;
+        const bool bad = approx ? ok && !(fabsf(fn == 17 ? f - ref : wrap_approx(f - ref)) <= tol)
+                                : ok && __float_as_uint(f) != __float_as_uint(ref) && !(isnan(f) && isnan(ref));
         const unsigned m_ok = __ballot_sync(__activemask(), ok);
         const unsigned m_bad = __ballot_sync(__activemask(), bad);
         if ((threadIdx.x & 31) == 0) {

@@ -9,7 +9,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 (ASIN, ATAN2, PHI, ADD_SQRT, ADD_SQRT3, PHI_MPI_PI, ADD_PI, PT, MULS, QSQ, SIN, COS, ATAN, HYPOT, T15, MULS1,
- PHI_APPROX, ASIN_APPROX, TAN, TAN_OVER) = range(20)
+ PHI_APPROX, ASIN_APPROX, TAN, TAN_OVER, PHI_FAST) = range(21)
 
 
 @pytest.fixture(scope="module")
@@ -62,4 +62,7 @@ def test_phase_b1_approximation_bounds(gpu):
         r = gpu.math_check(ASIN_APPROX, n, start=sign | _bits(2.0 ** -30), exhaustive=True)
         assert r["mismatches"] == 0 and r["answered"] == n, r
     r = gpu.math_check(PHI_APPROX, 1 << 28, seed=777)
+    assert r["mismatches"] == 0 and r["answered"] == 1 << 28, r
+    # the enumeration's polynomial direction (phi_fast): within 2.5e-6
+    r = gpu.math_check(PHI_FAST, 1 << 28, seed=778)
     assert r["mismatches"] == 0 and r["answered"] == 1 << 28, r
