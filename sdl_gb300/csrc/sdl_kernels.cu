@@ -319,18 +319,6 @@ __device__ __forceinline__ float OF(const BatchDev& b, int st, int f, int64_t k)
 }
 __device__ __forceinline__ int64_t OFF(const BatchDev& b, int st, int64_t g) { return AT(b.obj[st].mod_cnt, g, NG1(b)); }
 
-__device__ __forceinline__ MDView md_view(const BatchDev& b, int a) {
-    const int gm = OG(b, kMD, a);
-    const ModDev* lm = &MOD(b, mod_of(b, gm));
-    MDView v;
-    v.m = lm;
-    v.a = hit(b, md_anchor(*lm, OI(b, kMD, a), OJ(b, kMD, a)));
-    v.dz = OF(b, kMD, 0, a);
-    v.shiftedDz = OF(b, kMD, 1, a);
-    v.dphi = OF(b, kMD, 2, a);
-    v.dphichange = OF(b, kMD, 3, a);
-    return v;
-}
 
 // ------------------------------------------------------------------ stage functors
 struct MDStage {
@@ -402,7 +390,6 @@ __device__ __forceinline__ MDRec md_rec(const BatchDev& b, int64_t a) {
 
 __global__ void k_md_pack(BatchDev b) {
     if (halted(b)) return;
-    const int n_mod = b.geo.n_mod;
     const int64_t n = min(OFF(b, kMD, b.n_gm), b.obj[kMD].cap);  // mini-doublets
     for (int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; a < n; a += (int64_t)gridDim.x * blockDim.x) {
         const int lm = mod_of(b, OG(b, kMD, a));
@@ -760,29 +747,6 @@ __global__ void __launch_bounds__(kEnumThreads) k_enum(BatchDev b) {
     rec_flush<kNF>(b, st, rb);
 }
 
-// warp-aggregated append of a survivor of stage st (inner object i, outer j)
-__device__ __forceinline__ void append_rec(const BatchDev& b, int st, bool pass, int oi, int oj, int g, const float* fv) {
-    const int lane = threadIdx.x & 31;
-    const unsigned m = __ballot_sync(0xffffffffu, pass);
-    if (!m) return;
-    const Recs& R = b.rec[st];
-    const Objs& O = b.obj[st];
-    const int leader = __ffs(m) - 1;
-    unsigned long long p0 = 0;
-    if (lane == leader) p0 = atomicAdd((unsigned long long*)(b.n_rec + st), (unsigned long long)__popc(m));
-    p0 = __shfl_sync(0xffffffffu, p0, leader);
-    if (!pass) return;
-    const int64_t pos = (int64_t)p0 + __popc(m & ((1u << lane) - 1u));
-    if (pos < O.cap) {
-        AT(R.i, pos, O.cap) = oi;
-        AT(R.j, pos, O.cap) = oj;
-        AT(R.g, pos, O.cap) = g;
-        AT(R.rank, pos, O.cap) = (int)atomicAdd((unsigned long long*)&AT(O.mod_cnt, g, NG1(b)), 1ull);
-        for (int k = 0; k < R.nf; ++k) AT(R.f, (int64_t)k * O.cap + pos, O.cap * R.nf) = fv[k];
-    } else {
-        atomicOr(b.status, 1u << st);
-    }
-}
 
 // One packed record per segment for the tracklet stage (the anchors of both
 // mini-doublets, the segment's angles and the per-segment sub-expressions of
@@ -791,7 +755,6 @@ __device__ __forceinline__ void append_rec(const BatchDev& b, int st, bool pass,
 // with the segment algorithm's six values f6 (dPhi, dPhiMin, dPhiMax,
 // dPhiChange, dPhiMinChange, dPhiMaxChange)
 __device__ __forceinline__ void sg_pack_record(const BatchDev& b, int im, int om, const float* f6, float* v) {
-    const int n_mod = b.geo.n_mod;
     const ModDev& ilm = MOD(b, mod_of(b, OG(b, kMD, im)));
     const ModDev& olm = MOD(b, mod_of(b, OG(b, kMD, om)));
     const int la = md_anchor(ilm, OI(b, kMD, im), OJ(b, kMD, im));
@@ -1026,8 +989,6 @@ __device__ __forceinline__ void passbuf_add(const BatchDev& b, PassBuf& pb, int 
     if (pass) pb.e[pb.n + __popc(m & ((1u << lane) - 1u))] = make_int4(s, tt, algo, b1);
     pb.n += c;
 }
-
-constexpr int kMlpWarps = kMlpTile / 32;
 
 // Tracklet candidates (Event.cc:611-693 with Tracklet.cc:144-2665) in three
 // kernels: the enumeration (k_tl_enum_a here: tasks of consecutive
@@ -1879,7 +1840,6 @@ __global__ void k_tp_count(BatchDev b) {
 
 __global__ void k_tc_count(BatchDev b) {
     if (halted(b)) return;
-    const int n_mod = b.geo.n_mod;
     const int64_t n = n_inner(b, kTC);
     for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
         int64_t c = 0;
