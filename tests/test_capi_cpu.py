@@ -56,3 +56,19 @@ def test_cpp_event_api_builds_and_reports_missing_device(tmp_path):
     ev.write_bin(hb)
     r = subprocess.run([exe, *paths, hb], capture_output=True, text=True)
     assert r.returncode in (0, 3), r.stderr
+
+
+def test_null_context_is_an_argument_error():
+    """Entry points that read results reject a null context with SDLG_ERR_ARG
+    before touching a device (the tracklet debug dump, the decision
+    self-check, the pass timers, the pre-filter counters)."""
+    import sdl_gb300
+    L = sdl_gb300.lib()
+    n = ctypes.c_int64()
+    buf = (ctypes.c_uint64 * 8)()
+    f = (ctypes.c_float * 16)()
+    i = (ctypes.c_int64 * 4)()
+    assert L.sdlg_get_tracklet_vars(None, ctypes.c_int64(0), f, ctypes.c_int64(0), ctypes.byref(n)) == -1
+    assert L.sdlg_tl_phase_a_check(None, buf) == -1
+    assert L.sdlg_last_tl_pass_times(None, f) == -1
+    assert L.sdlg_mlp_stats(None, i) == -1
