@@ -210,14 +210,69 @@ def single_plan(rank, n):
     return [(base + k, 200.0) for k in range(n)]
 
 
-def cpu_sample(events, threads):
+def cpu_sample(events, threads, digests=False):
+    """events/s of the CPU restatement on `threads` host threads; with
+    digests, also each event's object counts, multiset digests and counters
+    (the parity check of the GPU chain on the same events)"""
     import oracle
     from sdl_gb300 import synth
     orc = oracle.Oracle(synth.detector("full"))
     t0 = time.perf_counter()
-    n_tc = orc.run_many(events, threads)
+    if digests:
+        res = orc.run_many_digest(events, threads)
+    else:
+        res = orc.run_many(events, threads)
     dt = time.perf_counter() - t0
-    return len(events) / dt, dt, n_tc
+    return len(events) / dt, dt, res
+
+
+# Algorithmic bytes per unit of each stage (the roofline numerator): inputs
+# read once + outputs written once, with the record widths of the reference's
+# objects as device SoA (hit 20 B as input / 28 B prepared, MD 36 B, SG 28 B,
+# TL / TP / TC 8 B)
+STAGE_BYTES = {
+    "ingest": lambda n: 20 * n["hits"] + 28 * n["hits"],
+    "MD": lambda n: 28 * n["hits"] + 36 * n["MD"],
+    "SG": lambda n: 36 * n["MD"] + 28 * n["SG"],
+    "TL": lambda n: 28 * n["SG"] + 8 * n["TL"],
+    "TP": lambda n: 8 * n["SG"] + 8 * n["TP"],
+    "TC": lambda n: 8 * n["TL"] + 8 * n["TC"],
+}
+STAGE_NAMES = ("ingest", "MD", "SG", "TL", "TP", "TC")
+
+
+def stage_roofline(n_hits, objs, stage_ms, hbm):
+    """Per stage: algorithmic bytes, device ms, achieved GB/s and the fraction
+    of the measured HBM bandwidth."""
+    n = {"hits": int(n_hits), "MD": int(objs[0]), "SG": int(objs[1]), "TL": int(objs[2]), "TP": int(objs[3]),
+         "TC": int(objs[4])}
+    out = {}
+    for k, ms in zip(STAGE_NAMES, stage_ms):
+        b = STAGE_BYTES[k](n)
+        gbs = b / (float(ms) * 1e-3) / 1e9 if ms > 0 else 0.0
+        out[k] = {"bytes": int(b), "ms": round(float(ms), 3), "achieved_gbs": round(gbs, 2),
+                  "frac": round(gbs / hbm, 6)}
+    return out
+
+
+def event_digests(ch, n_ev, keep_tc=False):
+    """Per event of the last run: object counts, multiset digests (the CPU
+    checker's digest) and the per-layer counters; with keep_tc also the track
+    candidates of every event"""
+    import numpy as np
+    from sdl_gb300 import tuples
+    counts = np.array([ch.counts(e) for e in range(n_ev)], dtype=np.int64)
+    digests = np.zeros((n_ev, 5), dtype=np.uint64)
+    tc = None
+    for s in range(5):
+        parts = tuples.split_by_event(ch.objects(s, -1), counts[:, s])
+        for e, p in enumerate(parts):
+            digests[e, s] = tuples.multiset_digest(p)
+        if s == 4 and keep_tc:
+            tc = parts
+        del parts
+    counters = np.array([ch.counters(e) for e in range(n_ev)], dtype=np.uint32)
+    return (counts, digests, counters, tc) if keep_tc else (counts, digests, counters)
 
 
 def run_reference_arm(a, rank, world, pg):
@@ -227,8 +282,11 @@ def run_reference_arm(a, rank, world, pg):
     import oracle
     oracle.build()
     n_ev = max(1, threads)
-    # the first events of the headline workload (same seeds and PU draws)
-    events = make_events(headline_plan(0, 128)[:n_ev], threads)
+    # events spread evenly over the headline batch (same seeds and PU draws);
+    # the whole batch is generated to state how the sample compares with it
+    batch = make_events(headline_plan(0, 128), threads)
+    events = batch[::max(1, len(batch) // n_ev)][:n_ev]
+    batch_mean = sum(len(e) for e in batch) / len(batch)
     for _ in range(a.warmup):
         cpu_sample(events[: max(1, threads // 4)], threads)
     rates, secs = [], []
@@ -238,13 +296,17 @@ def run_reference_arm(a, rank, world, pg):
         secs.append(dt)
     total = sum(secs)
     value = a.steps * n_ev / total
-    sample = ("%d events of the headline workload per step (PU 150-300), plain chain per event (the reference has "
-              "no pre-filter), %d host threads" % (n_ev, threads))
+    hits = int(sum(len(e) for e in events))
+    sample = ("%d events spread evenly over the headline batch per step (PU 150-300; %d hits, %.0f per event against "
+              "%.0f per event in the whole 128-event batch), plain chain per event (the reference has no "
+              "pre-filter), %d host threads" % (n_ev, hits, hits / n_ev, batch_mean, threads))
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "events/s", "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(1e3 * total / a.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "events_per_step": n_ev, "implementation": "CPU restatement of the reference chain (oracle/), multi-threaded"},
+        "config": {"workload": WORKLOAD, "events_per_step": n_ev, "hits_per_step": hits,
+                   "hits_per_s": round(a.steps * hits / total, 1),
+                   "implementation": "CPU restatement of the reference chain (oracle/), multi-threaded"},
         "cpu_baseline": {"value": round(value, 4), "unit": "events/s", "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": round(value, 4), "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -287,14 +349,17 @@ def main():
         return
 
     import numpy as np
-    from sdl_gb300 import synth
+    from sdl_gb300 import synth, tuples
     threads = os.cpu_count() or 1
     # ---- inputs (generated before any CUDA call) ----------------------------
     batch = make_events(headline_plan(rank, a.batch_events), threads)
     single = make_events(single_plan(rank, 4), threads)
-    cpu_events = []
+    # the CPU baseline runs the restatement on the whole batch (about 30 s on
+    # 16 cores) and doubles as the parity check of the plain batched chain on
+    # every event; with fewer than 8 host threads, on every 8th event
+    cpu_pick = []
     if rank == 0 and not a.no_cpu_baseline:
-        cpu_events = batch[:max(1, threads)]
+        cpu_pick = list(range(len(batch))) if threads >= 8 else list(range(0, len(batch), 8))
 
     from __graft_entry__ import build
     build()
@@ -336,6 +401,9 @@ def main():
         ch.run(4, FLAG_MLP)
     n_pruned = ch.counts(-1)
     mstats = ch.mlp_stats()
+    # the pruned chain's track candidates per event (for the exact recall)
+    pruned_ev = [int(ch.counts(e)[4]) for e in range(len(batch))]
+    pruned_tc = tuples.split_by_event(ch.objects(4, -1), pruned_ev)
     clocks = Clocks(local)
     barrier(pg)
     t_wall0 = time.perf_counter()
@@ -355,7 +423,13 @@ def main():
     n_plain = ch.counts(-1)
     p_ms, p_stage, p_tl, p_pass = timed_runs(ch, 0, max(3, a.steps // 4), flush)
     p_mean = allmax(pg, statistics.fmean(p_ms))
-    tc_rec = float(n_pruned[4]) / max(1.0, float(n_plain[4]))
+    # recall of the pruned chain: |pruned & plain| / |plain| over the track
+    # candidate multisets, event by event (the pruned sets must be subsets)
+    g_counts, g_digests, g_counters, plain_tc = event_digests(ch, len(batch), keep_tc=True)
+    tc_common = sum(tuples.multiset_intersection(p, q) for p, q in zip(pruned_tc, plain_tc))
+    tc_rec = tc_common / max(1.0, float(n_plain[4]))
+    tc_outside = int(n_pruned[4]) - tc_common
+    del pruned_tc, plain_tc
     tl_rec = float(n_pruned[2]) / max(1.0, float(n_plain[2]))
     plain_batched = {"value": round(allsum(pg, len(batch)) * 1e3 / p_mean, 3), "unit": "events/s", "tuned": tuned_plain,
                      "ms_per_step": round(p_mean, 3), "objects_per_step": [int(v) for v in n_plain],
@@ -430,40 +504,51 @@ def main():
 
     # ---- roofline of the dominant kernel of the headline run -----------------
     # k_tl_enum_tiles (tracklet enumeration in module-pair tiles, the float
-    # cuts and the single-precision decision of the first tracklet cuts):
-    # algorithmic bytes = each segment's record as inner segment (112 B), its
-    # eleven outer-role fields (44 B) and its entry in the index of segments by
-    # outer module (4 B) read once + each global module's tile offset, segment
-    # offset and connection sum (24 B) read once + each surviving candidate's
-    # entry written once (16 B)
+    # cuts and the single-precision decision of the first tracklet cuts).
+    # Algorithmic bytes = the tracklet stage's input, 28 B per segment read
+    # once (the tracklets, 8 B each, are written by k_tl_b2).  layout_bytes =
+    # what this kernel's own data layout reads and writes once: each
+    # segment's record as inner segment (112 B), its eleven outer-role fields
+    # (44 B) and its entry in the index of segments by outer module (4 B),
+    # each global module's tile offset, segment offset and connection sum
+    # (24 B), each surviving candidate's list entry (16 B).  traffic = DRAM
+    # bytes per layout byte of an ncu capture of the kernel, times this
+    # launch's layout bytes.
     hbm, tflops, src = peaks()
     pf = np.mean(np.array(pf_ms), axis=0)
     fc_mean, pf_mean, ex_mean = float(pf[0]), float(pf[1]), float(pf[2])
     n_sg = int(n_pruned[1])
     n_gm = len(batch) * ch.num_modules
-    en_bytes = (112 + 44 + 4) * n_sg + 24 * n_gm + 16 * mstats["scored"]
-    en_achieved = en_bytes / (fc_mean * 1e-3) / 1e9
+    en_alg = 28 * n_sg
+    en_layout = (112 + 44 + 4) * n_sg + 24 * n_gm + 16 * mstats["scored"]
+    en_achieved = en_alg / (fc_mean * 1e-3) / 1e9
     tr = ncu_traffic("tl_enum_traffic.json")
     en_traffic = None
-    if tr and tr.get("traffic_per_algorithmic_byte"):
-        en_traffic = int(en_bytes * float(tr["traffic_per_algorithmic_byte"]))
-    # k_tl_prefilter (the network over the phase-A survivor list): algorithmic
-    # bytes = each survivor entry read once (16 B) + each segment's feature
-    # record read once (64 B) + each kept entry written once (16 B); tensor
-    # work = the network's MMAs per scored candidate
+    if tr and tr.get("traffic_per_layout_byte"):
+        en_traffic = int(en_layout * float(tr["traffic_per_layout_byte"]))
+    # k_tl_prefilter (the network over the enumeration's survivor list):
+    # algorithmic bytes = each scored entry read once (16 B) + each segment's
+    # feature record read once (64 B) + each kept entry written once (16 B);
+    # tensor work = the network's MMAs per scored candidate
     alg_bytes = 16 * mstats["scored"] + 64 * n_sg + 16 * mstats["kept"]
     achieved = alg_bytes / (pf_mean * 1e-3) / 1e9
     tr = ncu_traffic("tl_prefilter_traffic.json")
     traffic = None
-    if tr and tr.get("traffic_per_algorithmic_byte"):
-        traffic = int(alg_bytes * float(tr["traffic_per_algorithmic_byte"]))
+    if tr and tr.get("traffic_per_layout_byte"):
+        traffic = int(alg_bytes * float(tr["traffic_per_layout_byte"]))
     mma_tflops = mstats["scored"] * MLP_FLOPS_PER_CANDIDATE / (pf_mean * 1e-3) / 1e12
     roofline = {"bound": "hbm", "achieved": round(en_achieved, 3), "peak": hbm, "unit": "GB/s",
                 "frac": round(en_achieved / hbm, 6), "traffic": en_traffic, "peak_source": src,
                 "kernel": "k_tl_enum_tiles (tracklet candidate enumeration in module-pair tiles, the float cuts and "
                           "the single-precision phase-B1 decision)",
-                "kernel_ms": round(fc_mean, 3), "algorithmic_bytes": en_bytes,
-                "note": "issue-bound candidate evaluation (profiles/tl_kernels_ncu.md); HBM bytes are small by construction",
+                "kernel_ms": round(fc_mean, 3), "algorithmic_bytes": en_alg,
+                "algorithmic_bytes_rule": "28 B per segment (the tracklet stage's input, read once)",
+                "layout_bytes": en_layout,
+                "layout_achieved_gbs": round(en_layout / (fc_mean * 1e-3) / 1e9, 3),
+                "candidates": mstats["candidates"],
+                "candidates_per_s": round(mstats["candidates"] / (fc_mean * 1e-3), 1),
+                "note": "issue-bound candidate evaluation (the ncu capture of this kernel shows issue slots, not DRAM, "
+                        "saturated); the algorithmic bytes are small by construction",
                 "prefilter": {"kernel": "k_tl_prefilter (tensor-core pre-filter of the candidates through the float cuts and phase B1)",
                               "kernel_ms": round(pf_mean, 3), "algorithmic_bytes": alg_bytes,
                               "achieved": round(achieved, 3), "peak": hbm, "unit": "GB/s",
@@ -472,15 +557,30 @@ def main():
                                          "frac": round(mma_tflops / tflops, 5),
                                          "flops_per_candidate": MLP_FLOPS_PER_CANDIDATE,
                                          "candidates": mstats["scored"]}},
-                "double_cuts_ms": round(ex_mean, 3)}
+                "double_cuts_ms": round(ex_mean, 3),
+                "stages": stage_roofline(n_hit, n_pruned, hl_stage, hbm)}
+    plain_batched["stage_roofline"] = stage_roofline(n_hit, n_plain, np.mean(np.array(p_stage), axis=0), hbm)
+    plain_batched["hits_per_s"] = round(n_hit * 1e3 / p_mean, 1)
+    plain_single["stage_roofline"] = stage_roofline(len(ev), s_counts, s_st, hbm)
 
     # ---- CPU baseline (rank 0) -----------------------------------------------
     cpu = None
-    if rank == 0 and cpu_events:
-        r, dt, _ = cpu_sample(cpu_events, threads)
+    parity = None
+    if rank == 0 and cpu_pick:
+        cpu_events = [batch[e] for e in cpu_pick]
+        r, dt, (o_counts, o_digests, o_counters) = cpu_sample(cpu_events, threads, digests=True)
+        cpu_hits = sum(len(e) for e in cpu_events)
         cpu = {"value": round(r, 4), "unit": "events/s", "cores": threads, "kind": "port",
-               "sample": "the first %d events of the headline workload (PU 150-300) through the CPU restatement of "
-                         "the reference chain on %d threads (%.1f s)" % (len(cpu_events), threads, dt)}
+               "hits_per_s": round(cpu_hits / dt, 1),
+               "sample": "%d events of the headline workload (PU 150-300, %d hits) through the CPU restatement of "
+                         "the reference chain on %d threads (%.1f s)" % (len(cpu_events), cpu_hits, threads, dt)}
+        bad = [(e, s) for k, e in enumerate(cpu_pick) for s in range(5)
+               if g_counts[e, s] != o_counts[k, s] or g_digests[e, s] != o_digests[k, s]]
+        bad_cnt = [e for k, e in enumerate(cpu_pick) if not np.array_equal(g_counters[e], o_counters[k])]
+        parity = {"events_checked": len(cpu_pick), "stages": 5, "mismatches": len(bad),
+                  "counter_mismatches": len(bad_cnt), "first": bad[:4],
+                  "check": "plain batched chain vs the CPU restatement: per event, the five object multisets "
+                           "(digests of the hit-index tuples), counts and the 110 per-layer counters"}
 
     if rank == 0:
         line = {
@@ -499,11 +599,19 @@ def main():
                                      "pruned_fraction": round(1.0 - mstats["kept"] / max(1, mstats["scored"]), 4)},
                        "wall_s": round(wall, 3)},
             "tc_recall": round(tc_rec, 5), "tl_recall": round(tl_rec, 5),
+            "recall_method": "track candidates: |pruned & plain| / |plain| over the hit-index tuple multisets, event "
+                             "by event; tracklets: count ratio (pruned tracklets are a subset by construction)",
             "plain_batched": plain_batched, "plain_single": plain_single, "variants": variants,
             "e2e": {"value": round(e2e_value, 3), "unit": "events/s", "ms_per_step": round(e2e_mean, 3),
                     "h2d_bytes_per_step": n_hit * 20 + 8 * (len(batch) + 1), "d2h_bytes_per_step": int(statistics.fmean(d2h)),
                     "path": "sdlg_set_events (pinned host) + sdlg_run(SDLG_FLAG_MLP) + sdlg_get_objects(TC, into pinned host memory)"},
-            "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+            "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "tc_outside_plain": tc_outside,
+            "ratios_vs_cpu_baseline": None if not cpu else {
+                "headline_events": round(value / cpu["value"], 2),
+                "plain_batched_events": round(plain_batched["value"] / cpu["value"], 2),
+                "plain_batched_hits": round(plain_batched["hits_per_s"] / cpu["hits_per_s"], 2),
+                "note": "the CPU restatement runs the plain chain; plain against plain is the like-for-like ratio"},
+            "clocks": clk,
             "gpu_launches": int(launches * a.steps),
         }
         print(json.dumps(line), flush=True)

@@ -209,14 +209,15 @@ int64_t sdlg_last_launches(const sdlg_ctx* ctx);
 /* Mini-doublets of one event with no device allocation (no counterpart in
  * the reference, whose only interface is the host class library).  It is for
  * callers that may not allocate device memory while they process events:
- * frameworks that hand out all device memory from their own pool at start-up,
- * code whose stream is being captured into a CUDA graph, plugins whose host
- * owns the allocator.  Inputs (n_hits hits: x, y, z, idx, detid) and outputs
- * are the caller's DEVICE buffers; the stage's working memory is a fixed
- * array inside the library (about 17 MiB, held on every GPU that loads the
- * library until the process exits).  Results: d_pairs receives up to
- * pair_cap (lower idx, upper idx) pairs, *d_count the number of
- * mini-doublets (or, if the array's capacity overflowed, the number needed)
+ * frameworks that hand out all device memory from their own pool at start-up
+ * and forbid allocation afterwards, and plugins whose host owns the
+ * allocator.  Inputs (n_hits hits: x, y, z, idx, detid) and outputs are the
+ * caller's DEVICE buffers; the stage's working memory is a fixed array inside
+ * the library (18,875,496 bytes, about 18 MiB, held on every GPU that loads
+ * the library until the process exits).  Results: d_pairs receives up to
+ * pair_cap (lower idx, upper idx) pairs (the first pair_cap when there are
+ * more), *d_count the number of mini-doublets (or, if the array's capacity
+ * overflowed, the number needed)
  * and *d_status the device status word (0 = clean; bit 0 = more than
  * SDLG_STATIC_MAX_MINI_DOUBLETS mini-doublets, nothing written; bit 8 = hits
  * in modules the geometry does not list, which are skipped).  Asynchronous on

@@ -33,11 +33,12 @@ def _ptr(a, ct):
     return a.ctypes.data_as(ctypes.POINTER(ct))
 
 
-def build(ref: bool = False) -> None:
+def build(ref_dir: str | None = None) -> None:
+    """Build liboracle.so; with ref_dir (the reference's source directory),
+    also the unmodified reference and its driver (oracle/_ref)."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    if ref and os.path.isdir(os.environ.get("SDL_REFDIR", "/root/reference")):
-        subprocess.run(["make", "-s", "-C", HERE, "ref", "-j8",
-                        "REFDIR=" + os.environ.get("SDL_REFDIR", "/root/reference")], check=True)
+    if ref_dir and os.path.isdir(ref_dir):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "-j8", "REFDIR=" + ref_dir], check=True)
 
 
 _LIB = None
@@ -63,6 +64,9 @@ def lib():
         L.sdlo_free.argtypes = [_vp]
         L.sdlo_run_many.restype = _i64
         L.sdlo_run_many.argtypes = [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int]
+        L.sdlo_run_many_digest.restype = _i64
+        L.sdlo_run_many_digest.argtypes = [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
+                                           _vp, _vp, _vp]
         _LIB = L
     return _LIB
 
@@ -114,6 +118,23 @@ class Oracle:
                for k in ("x", "y", "z", "idx", "detid")]
         return int(lib().sdlo_run_many(self.h, len(events), off.ctypes.data, *[a.ctypes.data for a in cat],
                                        mode, n_threads))
+
+    def run_many_digest(self, events, n_threads: int, mode: int = 0):
+        """Whole chains on independent events in parallel threads; returns per
+        event the object counts (n, 5), the order-independent digests of the
+        object multisets (n, 5; sdl_gb300.tuples.multiset_digest) and the
+        per-layer counters (n, 110)."""
+        n = len(events)
+        off = np.zeros(n + 1, dtype=np.int64)
+        off[1:] = np.cumsum([len(e) for e in events])
+        cat = [np.ascontiguousarray(np.concatenate([getattr(e, k) for e in events]))
+               for k in ("x", "y", "z", "idx", "detid")]
+        counts = np.zeros((n, 5), dtype=np.int64)
+        digests = np.zeros((n, 5), dtype=np.uint64)
+        counters = np.zeros((n, 110), dtype=np.uint32)
+        lib().sdlo_run_many_digest(self.h, n, off.ctypes.data, *[a.ctypes.data for a in cat], mode, n_threads,
+                                   counts.ctypes.data, digests.ctypes.data, counters.ctypes.data)
+        return counts, digests, counters
 
 
 def read_dump(path):

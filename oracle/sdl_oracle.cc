@@ -1250,6 +1250,25 @@ Result* run_event(const Geo& g, int64_t n, const float* x, const float* y, const
     return r;
 }
 
+// Order-independent digest of an object list (hit-index tuples of width w):
+// the sum mod 2^64 of one 64-bit mix per row.  sdl_gb300/tuples.py computes
+// the same digest in numpy for the GPU chain's objects.
+inline uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+uint64_t multiset_digest(const std::vector<int32_t>& t, int w) {
+    uint64_t s = 0;
+    for (size_t r = 0; r + w <= t.size(); r += w) {
+        uint64_t h = (uint64_t)w;
+        for (int c = 0; c < w; ++c) h = mix64(h ^ (uint64_t)(uint32_t)t[r + c]);
+        s += h;
+    }
+    return s;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1304,6 +1323,32 @@ int64_t sdlo_run_many(const void* geo, int64_t n_events, const int64_t* ev_off, 
             if (e >= n_events) break;
             int64_t b = ev_off[e], n = ev_off[e + 1] - b;
             Result* r = run_event(*static_cast<const Geo*>(geo), n, x + b, y + b, z + b, idx + b, detid + b, mode, 4);
+            total += (int64_t)r->t[4].size() / 16;
+            delete r;
+        }
+    };
+    std::vector<std::thread> th;
+    for (int i = 0; i < std::max(1, n_threads); ++i) th.emplace_back(work);
+    for (auto& t : th) t.join();
+    return total.load();
+}
+
+int64_t sdlo_run_many_digest(const void* geo, int64_t n_events, const int64_t* ev_off, const float* x, const float* y,
+                             const float* z, const int32_t* idx, const uint32_t* detid, int mode, int n_threads,
+                             int64_t* counts, uint64_t* digests, uint32_t* counters) {
+    static const int w[5] = {2, 4, 8, 8, 16};
+    std::atomic<int64_t> next(0), total(0);
+    auto work = [&]() {
+        for (;;) {
+            int64_t e = next.fetch_add(1);
+            if (e >= n_events) break;
+            int64_t b = ev_off[e], n = ev_off[e + 1] - b;
+            Result* r = run_event(*static_cast<const Geo*>(geo), n, x + b, y + b, z + b, idx + b, detid + b, mode, 4);
+            for (int s = 0; s < 5; ++s) {
+                counts[e * 5 + s] = (int64_t)r->t[s].size() / w[s];
+                digests[e * 5 + s] = multiset_digest(r->t[s], w[s]);
+            }
+            std::memcpy(counters + e * 110, r->counters, 110 * sizeof(uint32_t));
             total += (int64_t)r->t[4].size() / 16;
             delete r;
         }

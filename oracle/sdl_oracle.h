@@ -55,6 +55,15 @@ int64_t sdlo_run_many(const void* geo, int64_t n_events, const int64_t* ev_off, 
                       const float* y, const float* z, const int32_t* idx, const uint32_t* detid,
                       int mode, int n_threads);
 
+/* The same, keeping per event e and stage s the object count
+ * counts[5e+s], an order-independent digest of the object multiset
+ * digests[5e+s] (sum mod 2^64 of a 64-bit mix of each hit-index tuple; the
+ * numpy twin is sdl_gb300/tuples.py) and the 110 per-layer counters
+ * counters[110e..]. */
+int64_t sdlo_run_many_digest(const void* geo, int64_t n_events, const int64_t* ev_off, const float* x,
+                             const float* y, const float* z, const int32_t* idx, const uint32_t* detid,
+                             int mode, int n_threads, int64_t* counts, uint64_t* digests, uint32_t* counters);
+
 #ifdef __cplusplus
 }
 #endif

@@ -5,12 +5,10 @@
 // Some callers cannot allocate device memory while they process events: a
 // framework that hands out all device memory at start-up from its own pool
 // and forbids allocation afterwards (online trigger farms run this way so
-// that a busy node never stalls or fails in the middle of an event), code
-// that runs while its stream is being captured into a CUDA graph, where
-// cudaMalloc is not permitted, and plugins whose host application owns the
-// device allocator.  sdlg_mini_doublets_static serves them: inputs and
-// outputs are the caller's device buffers and everything else comes from the
-// array below.
+// that a busy node never stalls or fails in the middle of an event), and
+// plugins whose host application owns the device allocator.
+// sdlg_mini_doublets_static serves them: inputs and outputs are the caller's
+// device buffers and everything else comes from the array below.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -29,8 +27,9 @@ using namespace sdlg;
 
 namespace {
 
-// Limits of one call; the array size follows from them (about 17 MiB held on
-// every GPU that loads this library, until the process exits).
+// Limits of one call; the array size follows from them (kBytes = 18,875,496
+// bytes, about 18 MiB, held on every GPU that loads this library until the
+// process exits).
 constexpr int64_t kMaxHits = SDLG_STATIC_MAX_HITS;
 constexpr int64_t kMaxModules = SDLG_STATIC_MAX_MODULES;
 constexpr int64_t kMaxMD = SDLG_STATIC_MAX_MINI_DOUBLETS;
@@ -43,14 +42,15 @@ constexpr int64_t kModHit = kEvOff + 2;                         // kMaxModules +
 constexpr int64_t kCandMD = kModHit + kMaxModules + 1;          // kMaxModules + 1
 constexpr int64_t kModCnt = kCandMD + kMaxModules + 1;          // kMaxModules + 1
 constexpr int64_t kScan = kModCnt + kMaxModules + 1;            // kScanTmp
-constexpr int64_t kWords64 = kScan + kScanTmp;
+constexpr int64_t kWords64 = (kScan + kScanTmp + 31) / 32 * 32;  // 256-byte multiple: the 4-byte regions start aligned
 // 4-byte regions follow the 8-byte ones
 constexpr int64_t kHitArrays = 18;                              // hit_gm, hit_rank, hit_perm and 15 sorted arrays
 constexpr int64_t kObjWords = 3 + 4;                            // i, j, g, f[4]
 constexpr int64_t kRecWords = 4 + 4;                            // i, j, g, rank, f[4]
 constexpr int64_t kWords32Raw = kHitArrays * kMaxHits + (kObjWords + kRecWords) * kMaxMD + 110 + 1;
-constexpr int64_t kWords32 = (kWords32Raw + 63) / 64 * 64;  // keeps the 8-byte tail 256-byte aligned
+constexpr int64_t kWords32 = (kWords32Raw + 63) / 64 * 64;  // 256-byte multiple: the 8-byte tail starts aligned
 constexpr int64_t kBytes = kWords64 * 8 + kWords32 * 4 + 8 * (5 + 8);
+static_assert(kBytes == 18875496, "the documented size of the fixed array (include/sdl_gpu.h)");
 
 static __device__ __align__(256) unsigned char g_scratch[kBytes];
 

@@ -2,7 +2,7 @@
 reference chain (oracle/_ref/ref_driver, built from the reference sources with
 `make -C oracle ref`) on seeded synthetic events.
 
-    python tests/golden/make_golden.py [--jobs 8]
+    python tests/golden/make_golden.py --refdir <reference sources> [--jobs 8]
 
 Each fixture records the event and geometry fingerprints (so a consumer can
 confirm it regenerated the same inputs), the per-stage object multisets as
@@ -66,8 +66,12 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--jobs", type=int, default=os.cpu_count())
     ap.add_argument("--only", default=None)
+    ap.add_argument("--refdir", default=os.environ.get("SDL_REFDIR"),
+                    help="the reference's source directory (default: $SDL_REFDIR)")
     a = ap.parse_args()
-    oracle.build(ref=True)
+    if not a.refdir:
+        raise SystemExit("give the reference's source directory: --refdir DIR or SDL_REFDIR")
+    oracle.build(ref_dir=a.refdir)
     cases = [c for c in CASES if a.only is None or c[0] == a.only]
     with ProcessPoolExecutor(a.jobs) as ex:
         for name, counts, secs in ex.map(one, cases):

@@ -1,9 +1,10 @@
 """The allocation-free mini-doublet entry point (sdlg_mini_doublets_static).
 
 It exists for callers that may not allocate device memory while they process
-events (pre-allocated framework pools, stream capture, plugins whose host owns
-the allocator).  Its output must equal the regular entry point's
-(sdlg_set_events + sdlg_run + sdlg_get_objects) exactly, call after call: the
+events (frameworks that hand out all device memory from a pool they allocate
+at start-up, plugins whose host owns the allocator).  Its output must equal
+the regular entry point's (sdlg_set_events + sdlg_run + sdlg_get_objects)
+exactly, call after call: the
 calls share one fixed array, so a later call must not see the earlier one's
 leftovers.  This file is collected last on purpose.
 """
@@ -80,6 +81,12 @@ def test_static_entry_matches_regular_entry_two_calls():
         assert st == 0
         assert n == len(ref)
         assert np.array_equal(oracle.canon(got), oracle.canon(ref))
+        # an output buffer smaller than the result: the full count, a clean
+        # status, and the first pair_cap pairs, all of them mini-doublets
+        few, n_few, st_few = _static_call(ch, rt, ev, cap=5)
+        assert st_few == 0 and n_few == len(ref) and len(few) == min(5, len(ref))
+        ref_rows = set(map(tuple, ref.tolist()))
+        assert all(tuple(r) in ref_rows for r in few.tolist())
     # sizes beyond the fixed array are refused before anything is launched
     with pytest.raises(SDLError):
         ch.mini_doublets_static(131073, 1, 1, 1, 1, 1, 1, 0, 1, 1, None)
