@@ -123,6 +123,17 @@ int sdlg_set_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, cons
  * selects DefaultNm1_TLAlgo, SDLG_FLAG_NO_GRAPH launches without a graph. */
 int sdlg_run(sdlg_ctx* ctx, int stop_after, int flags);
 
+/* Run stages first..last of the chain (0 MD .. 4 TC), one create* call at a
+ * time, as the reference's Event::create* methods do (Event.cc:245-305,
+ * 445-522, 611-693, 524-597, 823-872): when `first` is the stage right
+ * after the last run's final stage, only stages first..last run, on the
+ * objects that run left (so the five create* calls of an event cost one
+ * chain run); otherwise (first == 0, new events, a stage run again) the
+ * chain runs from the hits up to `last`.  `flags` are those of every stage
+ * run so far (the segment variant, the tracklet variant, ...).  Synchronous,
+ * with the capacity growth of sdlg_run (which re-runs from the hits). */
+int sdlg_run_stages(sdlg_ctx* ctx, int first, int last, int flags);
+
 /* Enqueue the same chain on the context stream without waiting (for callers
  * that overlap work or time the device); sdlg_sync() waits and resolves
  * capacity overflows by re-running. */
@@ -137,6 +148,46 @@ int sdlg_get_counts(sdlg_ctx* ctx, int64_t event, int64_t* out5);
 /* Copy the hit-index tuples of one stage of one event (event < 0: all) into
  * out (capacity `cap` tuples); *n_out receives the number of tuples. */
 int sdlg_get_objects(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int64_t cap, int64_t* n_out);
+
+/* The object graph of one event, for the reference's pointer accessors
+ * (Module::getMiniDoubletPtrs ... getTrackletPtrs, Module.h:273-277;
+ * MiniDoublet::lowerHitPtr/upperHitPtr, getDz, getShiftedDz, getDeltaPhi,
+ * getDeltaPhiChange, MiniDoublet.h:73-84; Segment::inner/outerMiniDoubletPtr,
+ * getDeltaPhi, getDeltaPhiMin/Max, getDeltaPhiChange,
+ * getDeltaPhiMin/MaxChange, Segment.h:110-127;
+ * TrackletBase::inner/outerSegmentPtr, TrackletBase.h:49-50;
+ * TrackCandidate::inner/outerTrackletBasePtr, TrackCandidate.h:91-96).
+ * For the n objects of stage `stage` of event `event` (n_out), in the row
+ * order of sdlg_get_objects:
+ *   links[2k], links[2k+1]: the two constituents, as indices into the
+ *     event's list of the stage below: mini-doublet -> the event's hits
+ *     (lower, upper; their position in the order sdlg_set_events got them),
+ *     segment -> mini-doublets (inner, outer), tracklet and triplet ->
+ *     segments (inner, outer), track candidate -> tracklets, or triplets
+ *     after SDLG_FLAG_TC_FROM_TP (inner, outer);
+ *   module[k]: the object's inner lower module (index into
+ *     sdlg_get_module_detids), the module the reference lists it in;
+ *   vals[k*nv + v]: nv = 4 floats per mini-doublet (dz, shiftedDz, deltaPhi,
+ *     deltaPhiChange), 6 per segment (deltaPhi, deltaPhiMin, deltaPhiMax,
+ *     deltaPhiChange, deltaPhiMinChange, deltaPhiMaxChange), none otherwise.
+ * Any output may be NULL (all NULL: a size query); cap is in objects. */
+int sdlg_get_object_links(sdlg_ctx* ctx, int stage, int64_t event, int32_t* links, int32_t* module, float* vals,
+                          int64_t cap, int64_t* n_out);
+
+/* The device module table: the detIds of module indices 0 .. n-1. */
+int sdlg_get_module_detids(const sdlg_ctx* ctx, uint32_t* out, int64_t cap, int64_t* n_out);
+
+/* detId decoding of SDL::Module (Module.cc:159-358; no context or device):
+ * out11 = subdet, side, layer, rod, ring, module, isLower, isInverted,
+ * partnerDetId, moduleType (0 PS, 1 2S), moduleLayerType (0 pixel, 1 strip).
+ * Returns SDLG_ERR_DETID (with out11 filled) when the detId is neither a
+ * barrel layer 1-6 nor an endcap layer 1-5 ring 1-15 module. */
+int sdlg_module_info(uint32_t detid, uint32_t* out11);
+
+/* SDL::Hit's derived quantities (Hit.cc:68-83; no context or device) for n
+ * points: rt, phi, eta, r3 (any output may be NULL). */
+int sdlg_hit_derived(int64_t n, const float* x, const float* y, const float* z, float* rt, float* phi, float* eta,
+                     float* r3);
 
 /* Debug dump of the tracklets' final cut variables, as the reference records
  * them in each Tracklet's recovars map (Tracklet.cc:1440-1495 and the same
@@ -193,6 +244,22 @@ int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3);
  * polynomial direction of the tracklet enumeration's phase-B1 decision
  * ("differs": more than 2.5e-6 away). */
 int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64_t n, uint64_t seed, uint64_t* out8);
+
+/* The host C library's float functions on the device (no counterpart in
+ * the reference, whose std::asin/atan/sin/cos/tan calls on floats are the
+ * host libm's asinf, atanf, sinf, cosf, tanf).  Those are not correctly
+ * rounded, and the cuts see the difference; the chain evaluates the
+ * correctly rounded float and moves it to the host function's value with a
+ * table built from the host's own functions when the first context of the
+ * process is created (a few seconds; about 200 MB on each device).
+ * sdlg_libm_eval: the device's values of function fn (0 asin, 1 atan, 2 sin,
+ * 3 cos, 4 tan) on the n floats whose bit patterns are start_bits ..
+ * start_bits + n - 1, into host memory (the self-check against the host's
+ * functions).  sdlg_libm_stats: out3 = floats tabulated, floats whose host
+ * value is not the correctly rounded one, and those more than one float
+ * away (kept in an exception list); no context or device needed. */
+int sdlg_libm_eval(sdlg_ctx* ctx, int fn, uint32_t start_bits, int64_t n, float* out);
+int sdlg_libm_stats(int fn, uint64_t* out3);
 
 /* Self-check of the tracklet enumeration's single-precision decisions (no
  * counterpart in the reference): after a run through the tracklet stage,

@@ -67,8 +67,37 @@ def lib():
         L.sdlo_run_many_digest.restype = _i64
         L.sdlo_run_many_digest.argtypes = [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
                                            _vp, _vp, _vp]
+        L.sdlo_set_libm.argtypes = [ctypes.c_int]
+        L.sdlo_libm_values.argtypes = [ctypes.c_int, ctypes.c_uint32, _i64, _vp, ctypes.c_int]
+        L.sdlo_libm_counts.argtypes = [_vp, ctypes.c_int]
         _LIB = L
     return _LIB
+
+
+LIBM_GLIBC, LIBM_ROUNDED, LIBM_COUNT = 0, 1, 2
+
+
+def set_libm(mode: int) -> None:
+    """Float libm of the restatement: LIBM_GLIBC (the reference's glibc float
+    functions, default), LIBM_ROUNDED (correctly rounded floats, the GPU
+    chain's arithmetic), LIBM_COUNT (glibc values, counting the calls whose
+    correctly rounded value differs)."""
+    lib().sdlo_set_libm(int(mode))
+
+
+def libm_values(fn: int, start_bits: int, n: int, threads: int = 0) -> np.ndarray:
+    """The host libm's float function fn (0 asin, 1 atan, 2 sin, 3 cos, 4 tan)
+    on n consecutive float bit patterns."""
+    out = np.empty(n, dtype=np.float32)
+    lib().sdlo_libm_values(int(fn), int(start_bits), int(n), out.ctypes.data, int(threads or os.cpu_count() or 1))
+    return out
+
+
+def libm_counts(reset: bool = False):
+    """(calls counted, calls whose glibc and correctly rounded values differ)"""
+    out = np.zeros(2, dtype=np.uint64)
+    lib().sdlo_libm_counts(out.ctypes.data, 1 if reset else 0)
+    return int(out[0]), int(out[1])
 
 
 class Oracle:

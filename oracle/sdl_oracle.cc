@@ -33,6 +33,38 @@ static_assert(sizeof(std::asin(1.0f)) == sizeof(float), "std::asin(float) must b
 
 namespace {
 
+// ---------------------------------------------------------------- float libm
+// The reference's std::asin/atan/sin/cos/tan on floats are glibc's float
+// functions, which are not always correctly rounded; the GPU chain uses the
+// correctly rounded float (the double function rounded once).  A switch
+// (sdlo_set_libm) makes the restatement use either, or the glibc values while
+// counting the calls where the two differ, so that the effect of the libm
+// difference on the objects can be measured.  Default: glibc, as the
+// reference.
+enum { kLibmGlibc = 0, kLibmRounded = 1, kLibmCount = 2 };
+std::atomic<int> g_libm_mode(kLibmGlibc);
+std::atomic<uint64_t> g_libm_calls(0), g_libm_diff(0);
+thread_local int tl_libm = kLibmGlibc;
+thread_local uint64_t tl_calls = 0, tl_diff = 0;
+
+inline float libm_pick(float glibc, double exact) {
+    const float r = (float)exact;
+    if (tl_libm == kLibmRounded) return r;
+    ++tl_calls;
+    if (!(r == glibc) && !(std::isnan(r) && std::isnan(glibc))) ++tl_diff;
+    return glibc;
+}
+inline float f_asin(float x) { return tl_libm == kLibmGlibc ? std::asin(x) : libm_pick(std::asin(x), ::asin((double)x)); }
+inline float f_atan(float x) { return tl_libm == kLibmGlibc ? std::atan(x) : libm_pick(std::atan(x), ::atan((double)x)); }
+inline float f_sin(float x) { return tl_libm == kLibmGlibc ? std::sin(x) : libm_pick(std::sin(x), ::sin((double)x)); }
+inline float f_cos(float x) { return tl_libm == kLibmGlibc ? std::cos(x) : libm_pick(std::cos(x), ::cos((double)x)); }
+inline float f_tan(float x) { return tl_libm == kLibmGlibc ? std::tan(x) : libm_pick(std::tan(x), ::tan((double)x)); }
+// a worker thread takes the process-wide mode and hands back its counts
+struct LibmScope {
+    LibmScope() { tl_libm = g_libm_mode.load(); tl_calls = tl_diff = 0; }
+    ~LibmScope() { g_libm_calls += tl_calls; g_libm_diff += tl_diff; }
+};
+
 constexpr float kSdlInf = 123456789;  // MiniDoublet.cc:3, compared as float
 const double kPi = M_PI;
 
@@ -297,7 +329,7 @@ struct Event {
         const float sinAlphaMax = 0.95;
         const float rt = h.rt;
         const unsigned iL = m.layer - 1;
-        const float miniSlope = std::asin(fmin_ref(rt * k2Rinv1GeVf / ptCut, sinAlphaMax));
+        const float miniSlope = f_asin(fmin_ref(rt * k2Rinv1GeVf / ptCut, sinAlphaMax));
         const float rLay = m.subdet == kBarrel ? rB[iL] : rE[iL];
         const float miniPVoff = 0.1 / rLay;
         const float miniMuls = m.subdet == kBarrel ? mulsB[iL] * 3.f / ptCut : mulsE[iL] * 3.f / ptCut;
@@ -327,23 +359,23 @@ struct Event {
             pix = &lo; str = &up; detid = lm.detid;
         }
         const bool isEndcap = lm.subdet == kEndcap;
-        float angleA = ::fabs((double)std::atan(pix->rt / pix->z));
-        float angleB = isEndcap ? kPi / 2. : (double)std::atan(geo.drdz(detid));
+        float angleA = ::fabs((double)f_atan(pix->rt / pix->z));
+        float angleB = isEndcap ? kPi / 2. : (double)f_atan(geo.drdz(detid));
         float sep = gap_size(lm);
         if (lm.type == kPS && lm.ltype != kPixel) sep *= -1;
-        float drprime = (sep / std::sin(angleA + angleB)) * std::sin(angleA);
+        float drprime = (sep / f_sin(angleA + angleB)) * f_sin(angleA);
         float slope = 0;
         if (lm.subdet == kEndcap) slope = geo.eslope(detid);
         if (lm.subdet == kBarrel) slope = geo.tslope(detid);
-        float absArctanSlope = (slope != kSdlInf) ? ::fabs((double)std::atan(slope)) : kPi / 2;
+        float absArctanSlope = (slope != kSdlInf) ? ::fabs((double)f_atan(slope)) : kPi / 2;
         float xp = pix->x, yp = pix->y;
         float angleM;
         if (xp > 0 && yp > 0) angleM = absArctanSlope;
         else if (xp > 0 && yp < 0) angleM = kPi - absArctanSlope;
         else if (xp < 0 && yp < 0) angleM = kPi + absArctanSlope;
         else angleM = 2 * kPi - absArctanSlope;
-        float dx = drprime * std::sin(angleM);
-        float dy = drprime * std::cos(angleM);
+        float dx = drprime * f_sin(angleM);
+        float dy = drprime * f_cos(angleM);
         float xa = xp + dx, ya = yp + dy;
         float xo = str->x, yo = str->y;
         if (slope == kSdlInf) { xn = xa; yn = yo; }
@@ -352,7 +384,7 @@ struct Event {
             xn = (slope * xa + (1.f / slope) * xo - ya + yo) / (slope + (1.f / slope));
             yn = (xn - xa) * slope + ya;
         }
-        float absdzprime = ::fabs((double)(sep / std::sin(angleA + angleB) * std::cos(angleA)));
+        float absdzprime = ::fabs((double)(sep / f_sin(angleA + angleB) * f_cos(angleA)));
         float abszn;
         if (lm.ltype == kPixel) abszn = ::fabs((double)pix->z) + absdzprime;
         else abszn = ::fabs((double)pix->z) - absdzprime;
@@ -460,7 +492,7 @@ struct Event {
         const P3& ia = hits[imd.anchor].p;
         const P3& oa = hits[omd.anchor].p;
         float segmentDr = ::sqrt(::pow(oa.y - ia.y, 2) + ::pow(oa.x - ia.x, 2));
-        const float dAlpha_Bfield = std::asin(fmin_ref(segmentDr * k2Rinv1GeVf / ptCut, sinAlphaMax));
+        const float dAlpha_Bfield = f_asin(fmin_ref(segmentDr * k2Rinv1GeVf / ptCut, sinAlphaMax));
         const float pitch = 0.15;
         const bool inTilt = im.subdet == kBarrel && im.side != kCenter;
         const bool outTilt = om.subdet == kBarrel && om.side != kCenter;
@@ -508,9 +540,9 @@ struct Event {
         const P3& ia = hits[imd.anchor].p;
         const P3& oa = hits[omd.anchor].p;
         float rtIn = ia.rt, rtOut = oa.rt, zIn = ia.z, zOut = oa.z;
-        const float sdSlope = std::asin(fmin_ref(rtOut * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
+        const float sdSlope = f_asin(fmin_ref(rtOut * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
         const float sdPVoff = 0.1f / rtOut;
-        const float dzDrtScale = std::tan(sdSlope) / sdSlope;
+        const float dzDrtScale = f_tan(sdSlope) / sdSlope;
         const float zGeom = im.layer <= 2 ? 2.f * kPixelPSZpitch : 2.f * kStrip2SZpitch;
         float zLo = zIn + (zIn - kDeltaZLum) * (rtOut / rtIn - 1.f) * (zIn > 0.f ? 1.f : dzDrtScale) - zGeom;
         float zHi = zIn + (zIn + kDeltaZLum) * (rtOut / rtIn - 1.f) * (zIn < 0.f ? 1.f : dzDrtScale) + zGeom;
@@ -540,7 +572,7 @@ struct Event {
         const P3& oHi = out2S ? oah.hi : oa;
         const P3& oLo = out2S ? oah.lo : oa;
         float rtIn = ia.rt, rtOut = oa.rt, zIn = ia.z, zOut = oa.z;
-        const float sdSlope = std::asin(fmin_ref(rtOut * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
+        const float sdSlope = f_asin(fmin_ref(rtOut * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
         const float disks2SMinRadius = 60.f;
         const float rtGeom = (rtIn < disks2SMinRadius && rtOut < disks2SMinRadius) ? (2.f * kPixelPSZpitch)
                            : ((rtIn < disks2SMinRadius || rtOut < disks2SMinRadius) ? (kPixelPSZpitch + kStrip2SZpitch)
@@ -548,7 +580,7 @@ struct Event {
         if (zIn * zOut < 0) return false;
         const float dz = zOut - zIn;
         const float dLum = std::copysign(kDeltaZLum, zIn);
-        const float drtDzScale = sdSlope / std::tan(sdSlope);
+        const float drtDzScale = sdSlope / f_tan(sdSlope);
         float rtLo = fmax_ref(rtIn * (1.f + dz / (zIn + dLum) * drtDzScale) - rtGeom, rtIn - 0.5f * rtGeom);
         float rtHi = rtIn * (zOut - dLum) / (zIn - dLum) + rtGeom;
         if (!(rtOut >= rtLo && rtOut <= rtHi)) return false;
@@ -648,22 +680,22 @@ struct Event {
         const float sinAlphaMax = 0.95;
         if (betaIn * betaOut > 0.f &&
             (std::abs(pt_beta) < 4.f * pt_betaMax || (lIn >= 11 && std::abs(pt_beta) < 8.f * pt_betaMax))) {
-            const float betaInUpd = betaIn + ::copysign((double)std::asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / std::abs(pt_beta), sinAlphaMax)), (double)betaIn);
-            const float betaOutUpd = betaOut + ::copysign((double)std::asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / std::abs(pt_beta), sinAlphaMax)), (double)betaOut);
+            const float betaInUpd = betaIn + ::copysign((double)f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / std::abs(pt_beta), sinAlphaMax)), (double)betaIn);
+            const float betaOutUpd = betaOut + ::copysign((double)f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / std::abs(pt_beta), sinAlphaMax)), (double)betaOut);
             betaAv = 0.5f * (betaInUpd + betaOutUpd);
             pt_beta = dr * k2Rinv1GeVf / ::sin((double)betaAv);
-            betaIn += ::copysign((double)std::asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / std::abs(pt_beta), sinAlphaMax)), (double)betaIn);
-            betaOut += ::copysign((double)std::asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / std::abs(pt_beta), sinAlphaMax)), (double)betaOut);
+            betaIn += ::copysign((double)f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / std::abs(pt_beta), sinAlphaMax)), (double)betaIn);
+            betaOut += ::copysign((double)f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / std::abs(pt_beta), sinAlphaMax)), (double)betaOut);
             betaAv = 0.5f * (betaIn + betaOut);
             pt_beta = dr * k2Rinv1GeVf / ::sin((double)betaAv);
         } else if (lIn < 11 && std::abs(betaOut) < 0.2 * std::abs(betaIn) && std::abs(pt_beta) < 12.f * pt_betaMax) {
             const float pt_betaIn = dr * k2Rinv1GeVf / ::sin((double)betaIn);
-            const float betaInUpd = betaIn + ::copysign((double)std::asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / std::abs(pt_betaIn), sinAlphaMax)), (double)betaIn);
-            const float betaOutUpd = betaOut + ::copysign((double)std::asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / std::abs(pt_betaIn), sinAlphaMax)), (double)betaIn);
+            const float betaInUpd = betaIn + ::copysign((double)f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / std::abs(pt_betaIn), sinAlphaMax)), (double)betaIn);
+            const float betaOutUpd = betaOut + ::copysign((double)f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / std::abs(pt_betaIn), sinAlphaMax)), (double)betaIn);
             betaAv = (std::abs(betaOut) > 0.2f * std::abs(betaIn)) ? (0.5f * (betaInUpd + betaOutUpd)) : betaInUpd;
             pt_beta = dr * k2Rinv1GeVf / ::sin((double)betaAv);
-            betaIn += ::copysign((double)std::asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / std::abs(pt_beta), sinAlphaMax)), (double)betaIn);
-            betaOut += ::copysign((double)std::asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / std::abs(pt_beta), sinAlphaMax)), (double)betaIn);
+            betaIn += ::copysign((double)f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / std::abs(pt_beta), sinAlphaMax)), (double)betaIn);
+            betaOut += ::copysign((double)f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / std::abs(pt_beta), sinAlphaMax)), (double)betaIn);
             betaAv = 0.5f * (betaIn + betaOut);
             pt_beta = dr * k2Rinv1GeVf / ::sin((double)betaAv);
         }
@@ -683,7 +715,7 @@ struct Event {
         const bool isPS_OutLo = q.mOutLo->type == kPS;
         const float rt_InLo = q.inLo->p.rt, rt_OutLo = q.outLo->p.rt;
         const float z_InLo = q.inLo->p.z, z_OutLo = q.outLo->p.z;
-        const float alpha1GeV_OutLo = std::asin(fmin_ref(rt_OutLo * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
+        const float alpha1GeV_OutLo = f_asin(fmin_ref(rt_OutLo * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
         const float rtRatio = rt_OutLo / rt_InLo;
         const float dzDrtScale = ::tan((double)alpha1GeV_OutLo) / alpha1GeV_OutLo;
         const float zpitch_InLo = isPS_InLo ? kPixelPSZpitch : kStrip2SZpitch;
@@ -736,7 +768,7 @@ struct Event {
         const float drt_tl_axis = tl_axis.rt;
         const float corrF = 1.f;
         const float rt_InSeg = sub(hInUp, hInLo).rt;
-        const float betaIn_cut = std::asin(fmin_ref((-rt_InSeg * corrF + drt_tl_axis) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / drt_InSeg);
+        const float betaIn_cut = f_asin(fmin_ref((-rt_InSeg * corrF + drt_tl_axis) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / drt_InSeg);
         if (!(std::abs(betaInRHmin) < betaIn_cut)) return false;
         float betaAv = 0.5f * (betaIn + betaOut);
         float pt_beta = drt_tl_axis * k2Rinv1GeVf / ::sin((double)betaAv);
@@ -752,15 +784,15 @@ struct Event {
         const float dBetaMuls = sdlThetaMulsF * 4.f / fmin_ref(std::abs(pt_beta), pt_betaMax);
         const float sdIn_rt = hInLo.rt, sdOut_rt = hOutLo.rt, sdIn_z = hInLo.z, sdOut_z = hOutLo.z;
         const float alpha_OutLo = q.osg->dphichange;
-        const float alphaInAbsReg = fmax_ref(std::abs(alpha_InLo), std::asin(fmin_ref(sdIn_rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax)));
-        const float alphaOutAbsReg = fmax_ref(std::abs(alpha_OutLo), std::asin(fmin_ref(sdOut_rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax)));
+        const float alphaInAbsReg = fmax_ref(std::abs(alpha_InLo), f_asin(fmin_ref(sdIn_rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax)));
+        const float alphaOutAbsReg = fmax_ref(std::abs(alpha_OutLo), f_asin(fmin_ref(sdOut_rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax)));
         const float dBetaInLum = lIn < 11 ? 0.0f : std::abs(alphaInAbsReg * kDeltaZLum / sdIn_z);
         const float dBetaOutLum = lOut < 11 ? 0.0f : std::abs(alphaOutAbsReg * kDeltaZLum / sdOut_z);
         const float dBetaLum2 = (dBetaInLum + dBetaOutLum) * (dBetaInLum + dBetaOutLum);
-        const float sinDPhi = std::sin(dPhi);
+        const float sinDPhi = f_sin(dPhi);
         const float dBetaRIn2 = 0;
         const float dBetaROut2 = ::pow((double)((hiE.rt - loE.rt) * sinDPhi / drt_tl_axis), 2);
-        const float betaOut_cut = std::asin(fmin_ref(drt_tl_axis * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d) + ::sqrt((double)(dBetaLum2 + dBetaMuls * dBetaMuls));
+        const float betaOut_cut = f_asin(fmin_ref(drt_tl_axis * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d) + ::sqrt((double)(dBetaLum2 + dBetaMuls * dBetaMuls));
         if (!(std::abs(betaOut) < betaOut_cut)) return false;
         const float dBetaRes = 0.02f / fmin_ref(sdOut_d, drt_InSeg);
         const float dBetaCut2 = (dBetaRes * dBetaRes * 2.0f + dBetaMuls * dBetaMuls + dBetaLum2 + dBetaRIn2 + dBetaROut2 +
@@ -773,7 +805,7 @@ struct Event {
         const float pt_betaMax = 7.0f;
         const float zGeom = (q.mInLo->type == kPS ? kPixelPSZpitch : kStrip2SZpitch) + (q.mOutLo->type == kPS ? kPixelPSZpitch : kStrip2SZpitch);
         const float rtIn = q.inLo->p.rt, rtOut = q.outLo->p.rt, zIn = q.inLo->p.z, zOut = q.outLo->p.z;
-        const float sdlSlope = std::asin(fmin_ref(rtOut * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
+        const float sdlSlope = f_asin(fmin_ref(rtOut * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
         const float dzDrtScale = ::tan((double)sdlSlope) / sdlSlope;
         if (!(zIn * zOut > 0)) return false;
         const float dLum = std::copysign(kDeltaZLum, zIn);
@@ -831,7 +863,7 @@ struct Event {
         const float sdIn_d = hInUp.rt - hInLo.rt;
         const float dr = dr3.rt;
         const float corrF = 1.f;
-        const float betaIn_cut = std::asin(fmin_ref((-sdIn_dr * corrF + dr) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdIn_d);
+        const float betaIn_cut = f_asin(fmin_ref((-sdIn_dr * corrF + dr) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdIn_d);
         if (!(std::abs(betaInRHmin) < betaIn_cut)) return false;
         float betaAv = 0.5f * (betaIn + betaOut);
         float pt_beta = dr * k2Rinv1GeVf / ::sin((double)betaAv);
@@ -845,18 +877,18 @@ struct Event {
         betaOutRHmin *= betaOutMMSF; betaOutRHmax *= betaOutMMSF;
         const float dBetaMuls = sdlThetaMulsF * 4.f / fmin_ref(std::abs(pt_beta), pt_betaMax);
         const float sdIn_rt = hInLo.rt, sdOut_rt = hOutLo.rt, sdIn_z = hInLo.z, sdOut_z = hOutLo.z;
-        const float alphaInAbsReg = fmax_ref(std::abs(sdIn_alpha), std::asin(fmin_ref(sdIn_rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax)));
-        const float alphaOutAbsReg = fmax_ref(std::abs(sdOut_alpha), std::asin(fmin_ref(sdOut_rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax)));
+        const float alphaInAbsReg = fmax_ref(std::abs(sdIn_alpha), f_asin(fmin_ref(sdIn_rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax)));
+        const float alphaOutAbsReg = fmax_ref(std::abs(sdOut_alpha), f_asin(fmin_ref(sdOut_rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax)));
         const float dBetaInLum = lIn < 11 ? 0.0f : std::abs(alphaInAbsReg * kDeltaZLum / sdIn_z);
         const float dBetaOutLum = lOut < 11 ? 0.0f : std::abs(alphaOutAbsReg * kDeltaZLum / sdOut_z);
         const float dBetaLum2 = (dBetaInLum + dBetaOutLum) * (dBetaInLum + dBetaOutLum);
-        const float sinDPhi = std::sin(dPhi);
+        const float sinDPhi = f_sin(dPhi);
         const bool out2S = q.mOutUp->type == kTwoS;
         const P3& hiE = out2S ? q.outUp->hi : hOutUp;
         const P3& loE = out2S ? q.outUp->lo : hOutUp;
         const float dBetaRIn2 = 0;
         const float dBetaROut2 = ::pow((double)((hiE.rt - loE.rt) * sinDPhi / dr), 2);
-        const float betaOut_cut = std::asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d) + ::sqrt((double)(dBetaLum2 + dBetaMuls * dBetaMuls));
+        const float betaOut_cut = f_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d) + ::sqrt((double)(dBetaLum2 + dBetaMuls * dBetaMuls));
         if (!(std::abs(betaOut) < betaOut_cut)) return false;
         const float dBetaRes = 0.02f / fmin_ref(sdOut_d, sdIn_d);
         const float dBetaCut2 = (dBetaRes * dBetaRes * 2.0f + dBetaMuls * dBetaMuls + dBetaLum2 + dBetaRIn2 + dBetaROut2 +
@@ -870,7 +902,7 @@ struct Event {
         const float zGeom = (q.mInLo->type == kPS ? kPixelPSZpitch : kStrip2SZpitch) + (q.mOutLo->type == kPS ? kPixelPSZpitch : kStrip2SZpitch);
         (void)zGeom;
         const float rtIn = q.inLo->p.rt, rtOut = q.outLo->p.rt, zIn = q.inLo->p.z, zOut = q.outLo->p.z;
-        const float sdlSlope = std::asin(fmin_ref(rtOut * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
+        const float sdlSlope = f_asin(fmin_ref(rtOut * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
         const float dzDrtScale = ::tan((double)sdlSlope) / sdlSlope;
         if (!(zIn * zOut > 0)) return false;
         const float dLum = std::copysign(kDeltaZLum, zIn);
@@ -950,14 +982,14 @@ struct Event {
         betaOutRHmin *= betaOutMMSF; betaOutRHmax *= betaOutMMSF;
         const float dBetaMuls = sdlThetaMulsF * 4.f / fmin_ref(std::abs(pt_beta), pt_betaMax);
         const float sdIn_rt = hInLo.rt, sdOut_rt = hOutLo.rt, sdIn_z = hInLo.z, sdOut_z = hOutLo.z;
-        const float alphaInAbsReg = fmax_ref(std::abs(sdIn_alpha), std::asin(fmin_ref(sdIn_rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax)));
-        const float alphaOutAbsReg = fmax_ref(std::abs(sdOut_alpha), std::asin(fmin_ref(sdOut_rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax)));
+        const float alphaInAbsReg = fmax_ref(std::abs(sdIn_alpha), f_asin(fmin_ref(sdIn_rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax)));
+        const float alphaOutAbsReg = fmax_ref(std::abs(sdOut_alpha), f_asin(fmin_ref(sdOut_rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax)));
         const float dBetaInLum = lIn < 11 ? 0.0f : std::abs(alphaInAbsReg * kDeltaZLum / sdIn_z);
         const float dBetaOutLum = lOut < 11 ? 0.0f : std::abs(alphaOutAbsReg * kDeltaZLum / sdOut_z);
         const float dBetaLum2 = (dBetaInLum + dBetaOutLum) * (dBetaInLum + dBetaOutLum);
         const float dBetaRIn2 = 0;
         const float dBetaROut2 = 0;
-        const float betaOut_cut = std::asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d) + ::sqrt((double)(dBetaLum2 + dBetaMuls * dBetaMuls));
+        const float betaOut_cut = f_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d) + ::sqrt((double)(dBetaLum2 + dBetaMuls * dBetaMuls));
         if (!(std::abs(betaOut) < betaOut_cut)) return false;
         const float dBetaRes = 0.02f / fmin_ref(sdOut_d, sdIn_d);
         const float dBetaCut2 = (dBetaRes * dBetaRes * 2.0f + dBetaMuls * dBetaMuls + dBetaLum2 + dBetaRIn2 + dBetaROut2 +
@@ -1213,6 +1245,7 @@ double now() {
 
 Result* run_event(const Geo& g, int64_t n, const float* x, const float* y, const float* z, const int32_t* idx,
                   const uint32_t* detid, int mode, int stop_after) {
+    LibmScope libm;
     Result* r = new Result();
     std::memset(r->seconds, 0, sizeof(r->seconds));
     Event ev(g);
@@ -1313,6 +1346,43 @@ void sdlo_counters(const void* res, uint32_t* out110) {
 void sdlo_times(const void* res, double* out5) { std::memcpy(out5, static_cast<const Result*>(res)->seconds, 5 * 8); }
 
 void sdlo_free(void* res) { delete static_cast<Result*>(res); }
+
+void sdlo_libm_values(int fn, uint32_t start_bits, int64_t n, float* out, int n_threads) {
+    auto one = [fn](float x) -> float {
+        switch (fn) {
+            case 0: return std::asin(x);
+            case 1: return std::atan(x);
+            case 2: return std::sin(x);
+            case 3: return std::cos(x);
+            default: return std::tan(x);
+        }
+    };
+    std::atomic<int64_t> next(0);
+    auto work = [&]() {
+        for (;;) {
+            const int64_t k0 = next.fetch_add(1 << 16);
+            if (k0 >= n) break;
+            const int64_t k1 = std::min<int64_t>(n, k0 + (1 << 16));
+            for (int64_t k = k0; k < k1; ++k) {
+                const uint32_t u = start_bits + (uint32_t)k;
+                float x;
+                std::memcpy(&x, &u, 4);
+                out[k] = one(x);
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int i = 0; i < std::max(1, n_threads); ++i) th.emplace_back(work);
+    for (auto& t : th) t.join();
+}
+
+void sdlo_set_libm(int mode) { g_libm_mode = (mode == kLibmRounded || mode == kLibmCount) ? mode : kLibmGlibc; }
+
+void sdlo_libm_counts(uint64_t* out2, int reset) {
+    out2[0] = g_libm_calls.load();
+    out2[1] = g_libm_diff.load();
+    if (reset) g_libm_calls = g_libm_diff = 0;
+}
 
 int64_t sdlo_run_many(const void* geo, int64_t n_events, const int64_t* ev_off, const float* x, const float* y,
                       const float* z, const int32_t* idx, const uint32_t* detid, int mode, int n_threads) {

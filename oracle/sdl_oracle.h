@@ -48,6 +48,19 @@ void sdlo_counters(const void* res, uint32_t* out110);
 void sdlo_times(const void* res, double* out5);
 void sdlo_free(void* res);
 
+/* Float libm used for the reference's std::asin/atan/sin/cos/tan on floats
+ * (process-wide, read at the start of each event): 0 glibc's float functions
+ * (the reference's; the default), 1 the correctly rounded float (the double
+ * function rounded once: the GPU chain's arithmetic), 2 glibc's values while
+ * counting the calls whose correctly rounded value differs.
+ * sdlo_libm_counts: out2 = {calls counted, calls that differ} since the last
+ * reset (mode 2). */
+void sdlo_set_libm(int mode);
+/* The host libm's float function fn (0 asin, 1 atan, 2 sin, 3 cos, 4 tan)
+ * on the n floats with bit patterns start_bits .. start_bits + n - 1. */
+void sdlo_libm_values(int fn, uint32_t start_bits, int64_t n, float* out, int n_threads);
+void sdlo_libm_counts(uint64_t* out2, int reset);
+
 /* Thread-parallel helper for the CPU baseline: runs n_events independent
  * events (CSR over the concatenated hit arrays) on n_threads threads and
  * returns the total number of track candidates. */

@@ -84,6 +84,13 @@ def lib():
         L.sdlg_last_launches.argtypes = [vp]
         L.sdlg_last_launches.restype = i64
         L.sdlg_mini_doublets_static.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
+        L.sdlg_run_stages.argtypes = [vp, i32, i32, i32]
+        L.sdlg_get_object_links.argtypes = [vp, i32, i64, vp, vp, vp, i64, vp]
+        L.sdlg_get_module_detids.argtypes = [vp, vp, i64, vp]
+        L.sdlg_module_info.argtypes = [ctypes.c_uint32, vp]
+        L.sdlg_hit_derived.argtypes = [i64, vp, vp, vp, vp, vp, vp, vp]
+        L.sdlg_libm_eval.argtypes = [vp, i32, ctypes.c_uint32, i64, vp]
+        L.sdlg_libm_stats.argtypes = [i32, vp]
         L.sdlg_host_alloc.argtypes = [vp, i64, ctypes.POINTER(vp)]
         L.sdlg_host_free.argtypes = [vp, vp]
         u64, f32 = ctypes.c_uint64, ctypes.c_float
@@ -102,6 +109,27 @@ def lib():
         L.sdlg_mlp_stats.argtypes = [vp, vp]
         _LIB = L
     return _LIB
+
+
+def module_info(detid: int) -> dict:
+    """SDL::Module's detId decoding (no device needed)."""
+    out = np.zeros(11, dtype=np.uint32)
+    rc = lib().sdlg_module_info(int(detid), out.ctypes.data)
+    keys = ("subdet", "side", "layer", "rod", "ring", "module", "isLower", "isInverted", "partnerDetId",
+            "moduleType", "moduleLayerType")
+    d = {k: int(v) for k, v in zip(keys, out)}
+    d["valid"] = rc == 0
+    return d
+
+
+def hit_derived(x, y, z):
+    """SDL::Hit's derived quantities (rt, phi, eta, r3) of float32 points (no device needed)."""
+    x, y, z = (np.ascontiguousarray(a, dtype=np.float32) for a in (x, y, z))
+    out = [np.empty(len(x), dtype=np.float32) for _ in range(4)]
+    rc = lib().sdlg_hit_derived(len(x), x.ctypes.data, y.ctypes.data, z.ctypes.data, *[o.ctypes.data for o in out])
+    if rc != 0:
+        raise SDLError("%d: sdlg_hit_derived" % rc)
+    return tuple(out)
 
 
 def geometry_convert(tilted, endcap, cmap, out_path):
@@ -202,6 +230,11 @@ class Chain:
     def run(self, stop_after: int = 4, flags: int = 0):
         self._ck(lib().sdlg_run(self.h, stop_after, flags))
 
+    def run_stages(self, first: int, last: int, flags: int = 0):
+        """Stages first..last (one create* call at a time): continues the last
+        run when `first` follows its final stage, else runs from the hits."""
+        self._ck(lib().sdlg_run_stages(self.h, int(first), int(last), int(flags)))
+
     def run_async(self, stop_after: int = 4, flags: int = 0):
         self._ck(lib().sdlg_run_async(self.h, stop_after, flags))
 
@@ -229,6 +262,44 @@ class Chain:
         if n.value:
             self._ck(lib().sdlg_get_objects(self.h, stage, event, out.ctypes.data, n.value, ctypes.byref(n)))
         return out[:n.value]
+
+    def links(self, stage: int, event: int = 0):
+        """The object graph of one event's stage: (constituents n x 2 as
+        indices into the stage below -- hits in input order for
+        mini-doublets --, inner lower module index n, per-object floats
+        n x nv with nv 4 for mini-doublets, 6 for segments, 0 otherwise)."""
+        n = ctypes.c_int64()
+        self._ck(lib().sdlg_get_object_links(self.h, stage, event, None, None, None, 0, ctypes.byref(n)))
+        nv = {0: 4, 1: 6}.get(stage, 0)
+        lk = np.empty((n.value, 2), dtype=np.int32)
+        md = np.empty(n.value, dtype=np.int32)
+        vals = np.empty((n.value, nv), dtype=np.float32)
+        if n.value:
+            self._ck(lib().sdlg_get_object_links(self.h, stage, event, lk.ctypes.data, md.ctypes.data,
+                                                 vals.ctypes.data if nv else None, n.value, ctypes.byref(n)))
+        return lk, md, vals
+
+    def module_detids(self) -> np.ndarray:
+        n = ctypes.c_int64()
+        self._ck(lib().sdlg_get_module_detids(self.h, None, 0, ctypes.byref(n)))
+        out = np.empty(n.value, dtype=np.uint32)
+        self._ck(lib().sdlg_get_module_detids(self.h, out.ctypes.data, n.value, ctypes.byref(n)))
+        return out
+
+    def libm_eval(self, fn: int, start_bits: int, n: int) -> np.ndarray:
+        """The chain's value of the host libm's float function fn (0 asin,
+        1 atan, 2 sin, 3 cos, 4 tan) on n consecutive float bit patterns."""
+        out = np.empty(n, dtype=np.float32)
+        self._ck(lib().sdlg_libm_eval(self.h, int(fn), int(start_bits), int(n), out.ctypes.data))
+        return out
+
+    @staticmethod
+    def libm_stats(fn: int) -> dict:
+        out = np.zeros(3, dtype=np.uint64)
+        rc = lib().sdlg_libm_stats(int(fn), out.ctypes.data)
+        if rc != 0:
+            raise SDLError("%d: sdlg_libm_stats" % rc)
+        return {"tabulated": int(out[0]), "moved": int(out[1]), "exceptions": int(out[2])}
 
     def tracklet_vars(self, event: int = -1) -> np.ndarray:
         """The tracklets' final cut variables (rows as objects(2, event), columns

@@ -441,6 +441,36 @@ void enqueue_chain(sdlg_ctx* ctx, int stop_after) {
     cudaMemcpyAsync(ctx->h_small + kNumStages + 1, b.n_kept, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
 }
 
+// stages first..last only (first >= 1), on the objects the previous run left
+// for the stages below first; no graph
+void enqueue_stages(sdlg_ctx* ctx, int first, int last) {
+    BatchDev& b = ctx->b;
+    cudaStream_t s = ctx->stream;
+    const int64_t n_gm = b.n_gm;
+    const int ns = last - first + 1;
+    record(ctx->ev[0], s);
+    cudaMemsetAsync(b.status, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(b.dbg, 0, 8 * sizeof(unsigned long long), s);
+    cudaMemsetAsync(b.n_rec + first, 0, ns * sizeof(int64_t), s);
+    cudaMemsetAsync(b.task + first, 0, ns * sizeof(unsigned long long), s);
+    // the counters of these stages only: 22 per stage in each event's 110
+    cudaMemset2DAsync(b.counters + first * 22, 110 * sizeof(uint32_t), 0, ns * 22 * sizeof(uint32_t), b.n_ev, s);
+    for (int st = first; st <= last; ++st) cudaMemsetAsync(b.obj[st].mod_cnt, 0, (n_gm + 1) * sizeof(int64_t), s);
+    if (first <= kTL && last >= kTL) cudaMemsetAsync(b.mlp_stats, 0, sizeof(MlpStats), s);
+    Hooks* h = &ctx->hooks;
+    h->timed = true;
+    h->launches = 0;
+    record(ctx->ev[1], s);
+    void (*fns[5])(const BatchDev&, cudaStream_t, Hooks*) = {launch_md, launch_sg, launch_tl, launch_tp, launch_tc};
+    for (int st = 0; st < kNumStages; ++st) {
+        if (st >= first && st <= last) fns[st](b, s, h);
+        record(ctx->ev[2 + st], s);
+    }
+    cudaMemcpyAsync(ctx->h_small, b.n_rec, kNumStages * sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(ctx->h_small + kNumStages, b.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(ctx->h_small + kNumStages + 1, b.n_kept, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+}
+
 #ifdef SDL_DEVICE_CHECKS
 // debug builds: run stage by stage, synchronising after each, and report the
 // first out-of-bounds index the device checks recorded
@@ -688,6 +718,9 @@ int sdlg_create(sdlg_ctx** out, int device) {
     for (int k = 0; k < 2; ++k)
         if (e == cudaSuccess) e = cudaEventCreate(&ctx->hooks.tl_mid[k]);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_small, 16 * sizeof(int64_t));
+    // the host libm's float functions for the cut arithmetic (once per process / device)
+    const char* lm_err = nullptr;
+    if (e == cudaSuccess && libm_setup(device, &lm_err) != 0) e = cudaErrorMemoryAllocation;
     // pre-filter state is small and allocated once, so device pointers captured
     // in the launch graph never change
     auto& M = ctx->mlp;
@@ -939,6 +972,28 @@ int sdlg_run(sdlg_ctx* ctx, int stop_after, int flags) {
     return sdlg_sync(ctx);
 }
 
+int sdlg_run_stages(sdlg_ctx* ctx, int first, int last, int flags) {
+    if (!ctx) return SDLG_ERR_ARG;
+    if (first < 0 || last > 4 || first > last) return fail(ctx, SDLG_ERR_ARG, "stages %d..%d out of range", first, last);
+    // a first stage right after the last run's final stage continues that
+    // run; anything else (no run yet, new events, a stage run again) runs
+    // from the hits
+    if (first == 0 || !ctx->ran || !ctx->buffers_ok || ctx->last_stop != first - 1) return sdlg_run(ctx, last, flags);
+    if ((flags & SDLG_FLAG_MLP) && !ctx->mlp.have) return fail(ctx, SDLG_ERR_ARG, "SDLG_FLAG_MLP without pre-filter parameters");
+    cudaSetDevice(ctx->device);
+    ctx->b.flags = flags;
+    ctx->last_stop = last;
+    ctx->last_flags = flags;
+#ifdef SDL_DEVICE_CHECKS
+    int rc = launch_checked(ctx, last);
+    if (rc) return rc;
+#else
+    enqueue_stages(ctx, first, last);
+    CK(cudaGetLastError());
+#endif
+    return finish(ctx);
+}
+
 static int event_range(sdlg_ctx* ctx, int stage, int64_t event, int64_t* first, int64_t* n) {
     if (!ctx->ran) return fail(ctx, SDLG_ERR_NO_EVENTS, "chain not run");
     if (stage < 0 || stage > ctx->last_stop) return fail(ctx, SDLG_ERR_ARG, "stage %d not run", stage);
@@ -988,6 +1043,116 @@ int sdlg_get_objects(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int6
     CK(cudaMemcpyAsync(out, tmp, bytes, cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaFreeAsync(tmp, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return SDLG_OK;
+}
+
+int sdlg_get_object_links(sdlg_ctx* ctx, int stage, int64_t event, int32_t* links, int32_t* module, float* vals,
+                          int64_t cap, int64_t* n_out) {
+    if (!ctx || !n_out || cap < 0) return SDLG_ERR_ARG;
+    if (event < 0) return fail(ctx, SDLG_ERR_ARG, "object links are per event");
+    cudaSetDevice(ctx->device);
+    int64_t first, n;
+    int rc = event_range(ctx, stage, event, &first, &n);
+    if (rc) return rc;
+    *n_out = n;
+    if (n == 0 || (!links && !module && !vals)) return SDLG_OK;  // a size query
+    if (cap < n) return fail(ctx, SDLG_ERR_ARG, "output capacity %lld < %lld objects", (long long)cap, (long long)n);
+    // the list the constituents index: hits, mini-doublets, segments
+    // (tracklets and triplets), tracklets or triplets (track candidates)
+    int64_t lo_first = ctx->ev_off[event];
+    if (stage != kMD) {
+        const int lower = stage == kSG ? kMD : stage <= kTP ? kSG : ((ctx->b.flags & SDLG_FLAG_TC_FROM_TP) ? kTP : kTL);
+        int64_t nl;
+        rc = event_range(ctx, lower, event, &lo_first, &nl);
+        if (rc) return rc;
+    }
+    const int nf = ctx->b.obj[stage].nf;
+    const size_t b_links = (size_t)n * 2 * sizeof(int32_t), b_mod = (size_t)n * sizeof(int32_t);
+    const size_t b_vals = (size_t)n * nf * sizeof(float);
+    char* tmp = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&tmp, b_links + b_mod + b_vals + 16, ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "cudaMallocAsync: %s", cudaGetErrorString(e));
+    int32_t* d_links = links ? reinterpret_cast<int32_t*>(tmp) : nullptr;
+    int32_t* d_mod = module ? reinterpret_cast<int32_t*>(tmp + b_links) : nullptr;
+    float* d_vals = (vals && nf) ? reinterpret_cast<float*>(tmp + b_links + b_mod) : nullptr;
+    launch_links(ctx->b, stage, first, n, lo_first, event * (int64_t)ctx->detids.size(), d_links, d_mod, d_vals,
+                 ctx->stream);
+    CK(cudaGetLastError());
+    if (d_links) CK(cudaMemcpyAsync(links, d_links, b_links, cudaMemcpyDeviceToHost, ctx->stream));
+    if (d_mod) CK(cudaMemcpyAsync(module, d_mod, b_mod, cudaMemcpyDeviceToHost, ctx->stream));
+    if (d_vals) CK(cudaMemcpyAsync(vals, d_vals, b_vals, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(tmp, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SDLG_OK;
+}
+
+int sdlg_get_module_detids(const sdlg_ctx* ctx, uint32_t* out, int64_t cap, int64_t* n_out) {
+    if (!ctx || !n_out || cap < 0) return SDLG_ERR_ARG;
+    const int64_t n = (int64_t)ctx->detids.size();
+    *n_out = n;
+    if (!out) return SDLG_OK;
+    if (cap < n) return SDLG_ERR_ARG;
+    std::memcpy(out, ctx->detids.data(), n * sizeof(uint32_t));
+    return SDLG_OK;
+}
+
+int sdlg_module_info(uint32_t detid, uint32_t* out11) {
+    if (!out11) return SDLG_ERR_ARG;
+    const Decoded m = decode(detid);
+    const uint32_t v[11] = {m.subdet, m.side, m.layer, m.rod, m.ring, m.module, (uint32_t)m.lower,
+                            (uint32_t)m.inverted, m.partner, m.type, m.ltype};
+    std::memcpy(out11, v, sizeof(v));
+    return valid_module(m) ? SDLG_OK : SDLG_ERR_DETID;
+}
+
+// Hit.cc:68-83 with MathUtil.cc:3-27, in the reference's types: float
+// products and sums, double sqrt and atan2 rounded to float, Phi_mpi_pi's
+// double comparisons, the float acosh (this file is compiled without
+// multiply-add contraction)
+int sdlg_hit_derived(int64_t n, const float* x, const float* y, const float* z, float* rt, float* phi, float* eta,
+                     float* r3) {
+    if (n < 0 || (n > 0 && (!x || !y || !z))) return SDLG_ERR_ARG;
+    for (int64_t i = 0; i < n; ++i) {
+        const float X = x[i], Y = y[i], Z = z[i];
+        const float R3 = (float)std::sqrt((double)(X * X + Y * Y + Z * Z));
+        const float RT = (float)std::sqrt((double)(X * X + Y * Y));
+        float at;
+        if (-X != 0) at = (float)std::atan2((double)-Y, (double)-X);
+        else if (-Y == 0) at = 0.f;
+        else if (-Y > 0) at = (float)(M_PI / 2);
+        else at = (float)(-M_PI / 2);
+        float p = (float)(M_PI + (double)at);
+        if (!std::isnan(p)) {
+            while (p >= M_PI) p = (float)((double)p - 2. * M_PI);
+            while (p < -M_PI) p = (float)((double)p + 2. * M_PI);
+        }
+        if (rt) rt[i] = RT;
+        if (r3) r3[i] = R3;
+        if (phi) phi[i] = p;
+        if (eta) eta[i] = (float)((Z > 0) - (Z < 0)) * std::acosh(R3 / RT);
+    }
+    return SDLG_OK;
+}
+
+int sdlg_libm_eval(sdlg_ctx* ctx, int fn, uint32_t start_bits, int64_t n, float* out) {
+    if (!ctx || !out || n < 0 || fn < 0 || fn >= kLmCount) return SDLG_ERR_ARG;
+    if ((uint64_t)start_bits + (uint64_t)n > (1ull << 32)) return fail(ctx, SDLG_ERR_ARG, "bit patterns past 2^32");
+    cudaSetDevice(ctx->device);
+    if (n == 0) return SDLG_OK;
+    float* d = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&d, n * sizeof(float), ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "cudaMallocAsync: %s", cudaGetErrorString(e));
+    launch_libm_eval(fn, start_bits, n, d, ctx->n_sm, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, d, n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(d, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return SDLG_OK;
+}
+
+int sdlg_libm_stats(int fn, uint64_t* out3) {
+    if (!out3 || fn < 0 || fn >= kLmCount) return SDLG_ERR_ARG;
+    libm_stats(fn, out3);
     return SDLG_OK;
 }
 

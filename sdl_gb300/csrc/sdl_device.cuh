@@ -134,6 +134,70 @@ static __device__ __noinline__ float f_cos(float x) {
     return f_sincos_fast(x, 1, r) ? r : f_cos_d(x);
 }
 
+// ------------------------------------------------------------------ host libm
+// The reference's std::asin/atan/sin/cos/tan on floats are the host libm's
+// float functions (glibc's asinf, atanf, sinf, cosf, tanf), which are not
+// correctly rounded: on glibc 2.39 they differ from the correctly rounded
+// value on 0.4-3 % of the floats, always by one float step, and the cut
+// decisions see it.  The host library tabulates, for every |x| bit pattern
+// in [lo, lo + n), whether its float function returns the correctly rounded
+// value of |x| (code 0), the next float up (1), the next float down (2) or a
+// value kept in a sorted exception list (3); outside [lo, lo + n) it returns
+// the correctly rounded value (checked on every float of each function's
+// domain by the library's self-check).  The functions are odd (asin, atan,
+// sin, tan) or even (cos) in the host libm as well, so |x| indexes the table.
+struct LibmTab {
+    const uint32_t* code;   // 2 bits per float, 16 per word
+    const uint32_t* exc_x;  // exceptions: |x| bit patterns (sorted) and their values
+    const float* exc_v;
+    uint32_t lo, n, n_exc, pad;
+};
+enum { kLmAsin = 0, kLmAtan, kLmSin, kLmCos, kLmTan, kLmCount };
+static __constant__ LibmTab c_libm[kLmCount];
+
+// the host libm's value for |x| (ax), given the correctly rounded value r of ax
+__device__ __forceinline__ float libm_host(int fn, float ax, float r) {
+    const LibmTab& t = c_libm[fn];
+    const uint32_t k = __float_as_uint(ax) - t.lo;
+    if (k >= t.n) return r;
+    const uint32_t c = (__ldg(t.code + (k >> 4)) >> ((k & 15u) * 2u)) & 3u;
+    if (c == 1u) return nextafterf(r, INFINITY);
+    if (c == 2u) return nextafterf(r, -INFINITY);
+    if (c == 3u) {
+        const uint32_t u = __float_as_uint(ax);
+        uint32_t a = 0, b = t.n_exc;
+        while (a < b) {
+            const uint32_t m = (a + b) >> 1;
+            if (__ldg(t.exc_x + m) < u) a = m + 1;
+            else b = m;
+        }
+        if (a < t.n_exc && __ldg(t.exc_x + a) == u) return __ldg(t.exc_v + a);
+    }
+    return r;
+}
+// std::asin, std::atan, std::sin, std::tan (odd) and std::cos (even) of a
+// float, as the host libm computes them
+static __device__ __noinline__ float g_asin(float x) {
+    const float ax = fabsf(x), r = libm_host(kLmAsin, ax, f_asin(ax));
+    return x < 0.f ? -r : r;
+}
+static __device__ __noinline__ float g_atan(float x) {
+    const float ax = fabsf(x), r = libm_host(kLmAtan, ax, f_atan(ax));
+    return x < 0.f ? -r : r;
+}
+static __device__ __noinline__ float g_sin(float x) {
+    const float ax = fabsf(x), r = libm_host(kLmSin, ax, f_sin(ax));
+    return x < 0.f ? -r : r;
+}
+static __device__ __noinline__ float g_cos(float x) {
+    const float ax = fabsf(x);
+    return libm_host(kLmCos, ax, f_cos(ax));
+}
+static __device__ __noinline__ float g_tan(float x) {
+    const float ax = fabsf(x), r = libm_host(kLmTan, ax, f_tan_ff(ax));
+    return x < 0.f ? -r : r;
+}
+
 // (float)(c + (double)a) for the double constants c = M_PI and 2 M_PI (as
 // hi + lo they are 3.6e-15 and 7.1e-15 off; the sum's error is below 2e-13)
 __device__ __forceinline__ bool add_dconst_fast(ffm::ff c, float a, float& r) {
@@ -413,25 +477,25 @@ __device__ __forceinline__ void shift_anchor(const P3& pix, const ModDev& lm, fl
     const bool ps = lm.type == kPS;
     const bool pixLower = lm.ltype == kPixel;
     const bool isEndcap = lm.subdet == kEndcap;
-    const float angleA = fabsf(f_atan(pix.rt / pix.z));
-    const float angleB = isEndcap ? (float)(kPi / 2.) : f_atan(lm.drdz_s);
+    const float angleA = fabsf(g_atan(pix.rt / pix.z));
+    const float angleB = isEndcap ? (float)(kPi / 2.) : g_atan(lm.drdz_s);
     float sep = lm.gap;
     if (ps && !pixLower) sep *= -1;
-    const float sAB = f_sin(angleA + angleB);
-    const float drprime = (sep / sAB) * f_sin(angleA);
+    const float sAB = g_sin(angleA + angleB);
+    const float drprime = (sep / sAB) * g_sin(angleA);
     const float slope = lm.slope_s;
-    const float absArctanSlope = (slope != kSdlInf) ? fabsf(f_atan(slope)) : (float)(kPi / 2);
+    const float absArctanSlope = (slope != kSdlInf) ? fabsf(g_atan(slope)) : (float)(kPi / 2);
     const float xp = pix.x, yp = pix.y;
     float angleM;
     if (xp > 0 && yp > 0) angleM = absArctanSlope;
     else if (xp > 0 && yp < 0) angleM = pi_plus(-absArctanSlope);  // (float)(kPi - (double)a)
     else if (xp < 0 && yp < 0) angleM = pi_plus(absArctanSlope);
     else angleM = two_pi_plus(-absArctanSlope);
-    const float dx = drprime * f_sin(angleM);
-    const float dy = drprime * f_cos(angleM);
+    const float dx = drprime * g_sin(angleM);
+    const float dy = drprime * g_cos(angleM);
     xa = xp + dx;
     ya = yp + dy;
-    const float absdzprime = fabsf(sep / sAB * f_cos(angleA));
+    const float absdzprime = fabsf(sep / sAB * g_cos(angleA));
     float abszn;
     // one double operation on two floats rounded to float: the float operation
     if (pixLower) abszn = fabsf(pix.z) + absdzprime;
@@ -530,7 +594,7 @@ __device__ __forceinline__ void dalpha_threshold(const MDView& im, const MDView&
     const ModDev& O = *om.m;
     const float sdMuls = I.subdet == kBarrel ? mulsB[I.layer - 1] * 3.f / kPtCut : 0.006f * 3.f / kPtCut;
     const float segmentDr = hypot_ref(om.a.y - im.a.y, om.a.x - im.a.x);
-    const float dAlpha_Bfield = f_asin(fmin_ref(segmentDr * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
+    const float dAlpha_Bfield = g_asin(fmin_ref(segmentDr * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
     const bool inTilt = I.subdet == kBarrel && I.side != kCenter;
     const bool outTilt = O.subdet == kBarrel && O.side != kCenter;
     const float iTilt = inTilt ? I.tilt : 0.f;
@@ -776,22 +840,22 @@ __device__ __forceinline__ void delta_beta_iterations(float& betaIn, float& beta
     const float sinAlphaMax = 0.95f;
     if (betaIn * betaOut > 0.f &&
         (fabsf(pt_beta) < 4.f * pt_betaMax || (lIn >= 11 && fabsf(pt_beta) < 8.f * pt_betaMax))) {
-        const float betaInUpd = betaIn + copysignf(f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
-        const float betaOutUpd = betaOut + copysignf(f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaOut);
+        const float betaInUpd = betaIn + copysignf(g_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
+        const float betaOutUpd = betaOut + copysignf(g_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaOut);
         betaAv = 0.5f * (betaInUpd + betaOutUpd);
         pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
-        betaIn = betaIn + copysignf(f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
-        betaOut = betaOut + copysignf(f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaOut);
+        betaIn = betaIn + copysignf(g_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
+        betaOut = betaOut + copysignf(g_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaOut);
         betaAv = 0.5f * (betaIn + betaOut);
         pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
     } else if (lIn < 11 && (double)fabsf(betaOut) < 0.2 * (double)fabsf(betaIn) && fabsf(pt_beta) < 12.f * pt_betaMax) {
         const float pt_betaIn = pt_from(dr * k2Rinv1GeVf, betaIn);
-        const float betaInUpd = betaIn + copysignf(f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), betaIn);
-        const float betaOutUpd = betaOut + copysignf(f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), betaIn);
+        const float betaInUpd = betaIn + copysignf(g_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), betaIn);
+        const float betaOutUpd = betaOut + copysignf(g_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), betaIn);
         betaAv = (fabsf(betaOut) > 0.2f * fabsf(betaIn)) ? (0.5f * (betaInUpd + betaOutUpd)) : betaInUpd;
         pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
-        betaIn = betaIn + copysignf(f_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
-        betaOut = betaOut + copysignf(f_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
+        betaIn = betaIn + copysignf(g_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
+        betaOut = betaOut + copysignf(g_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
         betaAv = 0.5f * (betaIn + betaOut);
         pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
     }
@@ -1188,7 +1252,7 @@ __device__ __forceinline__ bool tl_phaseB1_sgv(int algo, const SGV& S, const SGV
     if (cb < 0) {
         const P3 InLo = S.lo();
         const float betaIn = S.dpc - dphi(InLo, sub(T.up(), InLo));
-        cb = fabsf(betaIn) < f_asin(arg) + (0.02f / sdIn_d) ? 1 : 0;  // betaInRHmin == betaIn here
+        cb = fabsf(betaIn) < g_asin(arg) + (0.02f / sdIn_d) ? 1 : 0;  // betaInRHmin == betaIn here
     }
     return cb != 0;
 }
@@ -1299,7 +1363,7 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
             const P3 loE = edge_point(OutUp.x, OutUp.y, OutUp.z, T.ex, T.ey, false);
             betaOutRHmin = -dphi(hiE, sub(hiE, OutLo)) + dphi(hiE, sub(hiE, InLo));
             betaOutRHmax = -dphi(loE, sub(loE, OutLo)) + dphi(loE, sub(loE, InLo));
-            const float sinDPhi = f_sin(dphi(midpoint(InLo, OutLo), sub(OutLo, InLo)));
+            const float sinDPhi = g_sin(dphi(midpoint(InLo, OutLo), sub(OutLo, InLo)));
             const float rr = (hiE.rt - loE.rt) * sinDPhi / dr;
             dBetaROut2 = rr * rr;  // the double square of a float is exact: one rounding to float
         } else {
@@ -1324,7 +1388,7 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
         betaOutRHmax = betaOut - sdOut_alphaOut_max + sdOut_alphaOut;
         if (fabsf(betaOutRHmin) > fabsf(betaOutRHmax)) { const float t = betaOutRHmin; betaOutRHmin = betaOutRHmax; betaOutRHmax = t; }
         if (T.flags & F_UP_2S) {
-            const float sinDPhi = f_sin(dphi(midpoint(InLo, OutLo), sub(OutLo, InLo)));
+            const float sinDPhi = g_sin(dphi(midpoint(InLo, OutLo), sub(OutLo, InLo)));
             const float hrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, true);
             const float lrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, false);
             const float rr = (hrt - lrt) * sinDPhi / dr;
@@ -1367,7 +1431,7 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
     const float dBetaInLum = lIn < 11 ? 0.0f : fabsf(alphaInAbsReg * kDeltaZLum / InLo.z);
     const float dBetaOutLum = lOut < 11 ? 0.0f : fabsf(alphaOutAbsReg * kDeltaZLum / OutLo.z);
     const float dBetaLum2 = (dBetaInLum + dBetaOutLum) * (dBetaInLum + dBetaOutLum);
-    const float betaOut_cut = add_dsqrt(f_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d),
+    const float betaOut_cut = add_dsqrt(g_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d),
                                         dBetaLum2 + dBetaMuls * dBetaMuls);
     if (!(fabsf(betaOut) < betaOut_cut)) return false;
     const float dBetaRes = 0.02f / fmin_ref(sdOut_d, sdIn_d);

@@ -277,11 +277,11 @@ __global__ void k_hit_scatter(BatchDev b) {
         const P3 p = mk(x, y, z);
         AT(b.hx, pos, H(b)) = x; AT(b.hy, pos, H(b)) = y; AT(b.hz, pos, H(b)) = z;
         AT(b.hrt, pos, H(b)) = p.rt; AT(b.hphi, pos, H(b)) = p.phi; AT(b.hr3, pos, H(b)) = p.r3;
-        const float a1 = f_asin(fmin_ref(p.rt * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
+        const float a1 = g_asin(fmin_ref(p.rt * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
         AT(b.ha1, pos, H(b)) = a1;
-        AT(b.htf, pos, H(b)) = f_tan_ff(a1);
+        AT(b.htf, pos, H(b)) = g_tan(a1);
         AT(b.htd, pos, H(b)) = f_tan_over(a1);
-        AT(b.ha3, pos, H(b)) = f_asin(fmin_ref(p.rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax));
+        AT(b.ha3, pos, H(b)) = g_asin(fmin_ref(p.rt * k2Rinv1GeVf / 3.0f, kSinAlphaMax));
         AT(b.hidx, pos, H(b)) = AT(b.in_idx, h, H(b));
         AT(b.hgm, pos, H(b)) = gm;
         // the strip shift of the mini-doublets this hit anchors
@@ -1982,6 +1982,49 @@ __global__ void k_materialize(BatchDev b, int st, int64_t first, int64_t n, int3
     }
 }
 
+// The object graph of stage st for objects [first, first + n) of one event:
+// constituents as indices into the event's lists of the stage below (hits:
+// their position in the event's input order), the inner lower module within
+// the event, and the floats the stage keeps per object.  lo_first: the
+// event's first object of the stage below (its first input hit for
+// mini-doublets); gm0: the event's first global module.
+__global__ void k_links(BatchDev b, int st, int64_t first, int64_t n, int64_t lo_first, int64_t gm0, int32_t* links,
+                        int32_t* module, float* vals) {
+    const int nf = b.obj[st].nf;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t o = first + k;
+        int64_t a = OI(b, st, o), c = OJ(b, st, o);
+        if (st == kMD) {  // sorted hit positions -> input hits
+            a = AT(b.hit_perm, a, H(b));
+            c = AT(b.hit_perm, c, H(b));
+        }
+        if (links) {
+            links[2 * k] = (int32_t)(a - lo_first);
+            links[2 * k + 1] = (int32_t)(c - lo_first);
+        }
+        if (module) module[k] = (int32_t)(OG(b, st, o) - gm0);
+        if (vals)
+            for (int f = 0; f < nf; ++f) vals[k * nf + f] = OF(b, st, f, o);
+    }
+}
+
+// the host libm's float functions as the chain evaluates them, on the float
+// bit patterns start .. start + n - 1 (the self-check of the libm tables)
+__global__ void k_libm_eval(int fn, uint32_t start, int64_t n, float* out) {
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const float x = __uint_as_float(start + (uint32_t)k);
+        float v;
+        switch (fn) {
+            case kLmAsin: v = g_asin(x); break;
+            case kLmAtan: v = g_atan(x); break;
+            case kLmSin: v = g_sin(x); break;
+            case kLmCos: v = g_cos(x); break;
+            default: v = g_tan(x); break;
+        }
+        out[k] = v;
+    }
+}
+
 unsigned grid_for(int64_t n, int threads, int cap_blocks) {
     int64_t g = (n + threads - 1) / threads;
     if (g < 1) g = 1;
@@ -2341,6 +2384,19 @@ __global__ void k_tl_vars(BatchDev b, int64_t first, int64_t n, float* out) {
 void launch_tl_vars(const BatchDev& b, int64_t first, int64_t n, float* out, cudaStream_t s) {
     if (n <= 0) return;
     k_tl_vars<<<grid_for(n, 128, b.n_sm * 8), 128, 0, s>>>(b, first, n, out);
+}
+
+void launch_links(const BatchDev& b, int st, int64_t first, int64_t n, int64_t lo_first, int64_t gm0, int32_t* links,
+                  int32_t* module, float* vals, cudaStream_t s) {
+    if (n <= 0) return;
+    k_links<<<grid_for(n, 256, b.n_sm * 16), 256, 0, s>>>(b, st, first, n, lo_first, gm0, links, module, vals);
+}
+
+cudaError_t set_libm_tables(const LibmTab* t) { return cudaMemcpyToSymbol(c_libm, t, sizeof(LibmTab) * kLmCount); }
+
+void launch_libm_eval(int fn, uint32_t start, int64_t n, float* out, int n_sm, cudaStream_t s) {
+    if (n <= 0) return;
+    k_libm_eval<<<grid_for(n, 256, n_sm * 16), 256, 0, s>>>(fn, start, n, out);
 }
 
 void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s) {

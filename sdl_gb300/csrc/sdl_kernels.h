@@ -124,6 +124,18 @@ void launch_math_check(int fn, int exhaustive, unsigned long long start, long lo
 void launch_tl_quick_check(const BatchDev& b, unsigned long long* out, cudaStream_t s);
 // final cut variables of tracklets [first, first + n) (15 floats each, the kTLVar* order)
 void launch_tl_vars(const BatchDev& b, int64_t first, int64_t n, float* out, cudaStream_t s);
+// the host libm's float functions on the device (sdl_libm.cu): build the
+// tables once per process, upload them once per device and point this
+// module's kernels at them (call with the device current); the host tables'
+// size, moved entries and exceptions of function fn; the device's values on
+// consecutive float bit patterns; the constant-memory setter
+int libm_setup(int device, const char** err);
+void libm_stats(int fn, uint64_t* out3);
+void launch_libm_eval(int fn, uint32_t start, int64_t n, float* out, int n_sm, cudaStream_t s);
+cudaError_t set_libm_tables(const LibmTab* t);
+// object graph of stage st for objects [first, first + n) of one event (see k_links)
+void launch_links(const BatchDev& b, int st, int64_t first, int64_t n, int64_t lo_first, int64_t gm0, int32_t* links,
+                  int32_t* module, float* vals, cudaStream_t s);
 // hit-index tuples of stage st for objects [first, first + n) into out (width 2/4/8/8/16)
 void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s);
 

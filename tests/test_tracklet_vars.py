@@ -1,9 +1,9 @@
 """Debug dump of the tracklets' final cut variables (sdlg_get_tracklet_vars)
 against the reference's own Tracklet recovars, recorded by the reference
 driver into the golden fixtures: -999 for BBEE tracklets as in the
-reference; bit-identical otherwise, except the last bits of values that go
-through the reference's float std::asin (glibc's asinf is not always
-correctly rounded, the chain uses the correctly rounded value)."""
+reference; bit-identical otherwise, including the values that go through the
+reference's float std::asin (the chain reproduces the host libm's asinf,
+which is not always correctly rounded)."""
 import os
 
 import numpy as np
@@ -41,14 +41,7 @@ def test_tracklet_vars_match_reference(name, oracle_lib):
     # BBEE tracklets: -999 in both (the reference records none of these)
     unset = ref[:, 0] == -999.0
     assert np.array_equal(v[unset], ref[unset])
-    # the others: bit-identical, except values that pass through the
-    # reference's float std::asin (glibc's asinf, not always correctly
-    # rounded) in the deltaBeta iterations: a last-bit difference of betaIn
-    # or betaOut, and what follows from it (dBeta = betaIn - betaOut cancels
-    # most of the magnitude), within 1e-7 + 1e-5 |value|
-    err = np.abs(v[~unset].astype(np.float64) - ref[~unset].astype(np.float64))
-    bound = 1e-7 + 1e-5 * np.abs(ref[~unset].astype(np.float64))
-    assert np.all(err <= bound), (np.max(err / bound), np.argwhere(err > bound)[:5])
+    # the others: bit-identical
     exact_rows = np.all(v.view(np.uint32) == ref.view(np.uint32), axis=1)
-    assert exact_rows.mean() >= 0.95, exact_rows.mean()
+    assert exact_rows.all(), (exact_rows.mean(), np.argwhere(~exact_rows)[:5])
     ch.close()
