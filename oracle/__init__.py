@@ -60,6 +60,7 @@ def lib():
         L.sdlo_count.argtypes = [_vp, ctypes.c_int]
         L.sdlo_copy.argtypes = [_vp, ctypes.c_int, _vp]
         L.sdlo_counters.argtypes = [_vp, _vp]
+        L.sdlo_vals.argtypes = [_vp, ctypes.c_int, _vp]
         L.sdlo_times.argtypes = [_vp, _vp]
         L.sdlo_free.argtypes = [_vp]
         L.sdlo_run_many.restype = _i64
@@ -67,6 +68,9 @@ def lib():
         L.sdlo_run_many_digest.restype = _i64
         L.sdlo_run_many_digest.argtypes = [_vp, _i64, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, ctypes.c_int,
                                            _vp, _vp, _vp]
+        L.sdlo_audit.restype = _i64
+        L.sdlo_audit.argtypes = [_vp, _i64, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp, _i64, _vp]
+        L.sdlo_audit_record_size.restype = ctypes.c_int
         L.sdlo_set_libm.argtypes = [ctypes.c_int]
         L.sdlo_libm_values.argtypes = [ctypes.c_int, ctypes.c_uint32, _i64, _vp, ctypes.c_int]
         L.sdlo_libm_counts.argtypes = [_vp, ctypes.c_int]
@@ -75,6 +79,11 @@ def lib():
 
 
 LIBM_GLIBC, LIBM_ROUNDED, LIBM_COUNT = 0, 1, 2
+
+# one near-cut audit record (sdlo_audit)
+AUDIT_DTYPE = np.dtype([("stage", "<i4"), ("accept_glibc", "<i4"), ("primary", "<i4"), ("pad", "<i4"),
+                        ("tuple", "<i4", (8,)), ("g_value", "<f4"), ("g_lo", "<f4"), ("g_hi", "<f4"),
+                        ("r_value", "<f4"), ("r_lo", "<f4"), ("r_hi", "<f4"), ("where", "S24"), ("cut", "S88")])
 
 
 def set_libm(mode: int) -> None:
@@ -117,8 +126,11 @@ class Oracle:
             lib().sdlo_geometry_free(self.h)
             self.h = None
 
-    def run(self, ev, mode: int = 0, stop_after: int = 4):
-        """Returns (tuples per stage, counters[110], seconds[5])."""
+    def run(self, ev, mode: int = 0, stop_after: int = 4, vals: bool = False):
+        """Returns (tuples per stage, counters[110], seconds[5]); with vals,
+        also the per-object floats of the mini-doublets (n x 4: dz,
+        shiftedDz, dphi, dphichange) and segments (n x 6: dphi, dphimin,
+        dphimax, dphichange, dphiminchange, dphimaxchange) in tuple order."""
         L = lib()
         arrs = [np.ascontiguousarray(a) for a in (ev.x, ev.y, ev.z, ev.idx, ev.detid)]
         r = L.sdlo_run(self.h, len(arrs[0]), *[a.ctypes.data for a in arrs], mode, stop_after)
@@ -134,9 +146,30 @@ class Oracle:
             L.sdlo_counters(r, cnt.ctypes.data)
             sec = np.empty(5, dtype=np.float64)
             L.sdlo_times(r, sec.ctypes.data)
+            vv = []
+            for s, w in ((0, 4), (1, 6)):
+                a = np.zeros((len(out[s]), w), dtype=np.float32)
+                if len(a):
+                    L.sdlo_vals(r, s, a.ctypes.data)
+                vv.append(a)
         finally:
             L.sdlo_free(r)
-        return out, cnt, sec
+        return (out, cnt, sec, vv) if vals else (out, cnt, sec)
+
+    def audit(self, ev, mode: int = 0, cap: int = 4096):
+        """Near-cut audit of one event: the chain with the reference's float
+        libm and with correctly rounded floats.  Returns (records of the
+        objects only one of them makes, AUDIT_DTYPE; summary 5 x 4 per stage:
+        objects with glibc, with rounded floats, primary flips, secondary
+        flips)."""
+        L = lib()
+        assert L.sdlo_audit_record_size() == AUDIT_DTYPE.itemsize
+        arrs = [np.ascontiguousarray(a) for a in (ev.x, ev.y, ev.z, ev.idx, ev.detid)]
+        out = np.zeros(cap, dtype=AUDIT_DTYPE)
+        summ = np.zeros((5, 4), dtype=np.int64)
+        n = L.sdlo_audit(self.h, len(arrs[0]), *[a.ctypes.data for a in arrs], mode, out.ctypes.data, cap,
+                         summ.ctypes.data)
+        return out[:min(n, cap)], summ
 
     def run_many(self, events, n_threads: int, mode: int = 0) -> int:
         """Runs whole chains on independent events in parallel threads;

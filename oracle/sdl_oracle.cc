@@ -9,11 +9,14 @@
 #include "sdl_oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <climits>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <thread>
 #include <unordered_map>
@@ -64,6 +67,25 @@ struct LibmScope {
     LibmScope() { tl_libm = g_libm_mode.load(); tl_calls = tl_diff = 0; }
     ~LibmScope() { g_libm_calls += tl_calls; g_libm_diff += tl_diff; }
 };
+
+// ---------------------------------------------------------------- cut trace
+// Every cut of the algorithms goes through CUT(decision, value, lo, hi): the
+// decision is returned unchanged; with a trace switched on (the near-cut
+// audit, sdlo_audit), the compared value and its bounds are recorded so that
+// a decision can be reported with its distance to the cut.
+struct CutRec {
+    const char* where;  // the algorithm
+    const char* cut;    // the decision as written
+    float value, lo, hi;
+    bool pass;
+};
+thread_local std::vector<CutRec>* tl_trace = nullptr;
+const float kNoBound = INFINITY;
+inline bool cut_rec(bool pass, const char* where, const char* cut, float value, float lo, float hi) {
+    if (tl_trace) tl_trace->push_back({where, cut, value, lo, hi, pass});
+    return pass;
+}
+#define CUT(pass, value, lo, hi) cut_rec((pass), __func__, #pass, (value), (lo), (hi))
 
 constexpr float kSdlInf = 123456789;  // MiniDoublet.cc:3, compared as float
 const double kPi = M_PI;
@@ -246,6 +268,7 @@ struct Pair {
 
 struct Result {
     std::vector<int32_t> t[5];
+    std::vector<float> vals[2];  // per mini-doublet 4 floats, per segment 6, in tuple order
     uint32_t counters[110];
     double seconds[5];
 };
@@ -398,7 +421,7 @@ struct Event {
         const float dzCut = lm.type == kPS ? 2.f : 10.f;
         const float sign = ((dz > 0) - (dz < 0)) * ((lo.z > 0) - (lo.z < 0));
         const float inverted = (iabs(trunc_i32(dz)) > 2) * sign;
-        if (!(std::abs(dz) < dzCut && inverted <= 0)) return false;
+        if (!CUT(std::abs(dz) < dzCut && inverted <= 0, std::abs(dz), -kNoBound, dzCut)) return false;
         const float miniCut = lm.ltype == kPixel ? dphi_threshold(lo, lm) : dphi_threshold(up, lm);
         float xn = 0, yn = 0, zn = 0;
         P3 shifted;
@@ -409,7 +432,7 @@ struct Event {
         } else {
             md.dphi = dphi(lo, up);
         }
-        if (!(std::abs(md.dphi) < miniCut)) return false;
+        if (!CUT(std::abs(md.dphi) < miniCut, std::abs(md.dphi), -kNoBound, miniCut)) return false;
         if (lm.side != kCenter) {
             if (lm.ltype == kPixel)
                 md.dphichange = lo.rt < shifted.rt ? dphichange(lo, shifted) : dphichange(shifted, lo);
@@ -418,7 +441,7 @@ struct Event {
         } else {
             md.dphichange = dphichange(lo, up);
         }
-        return std::abs(md.dphichange) < miniCut;
+        return CUT(std::abs(md.dphichange) < miniCut, std::abs(md.dphichange), -kNoBound, miniCut);
     }
 
     // MiniDoublet.cc:449-684
@@ -426,10 +449,10 @@ struct Event {
         md.dz = lo.z - up.z;
         float dz = md.dz;
         const float dzCut = 10.f;  // side() is never SubDet::Endcap (MiniDoublet.cc:470)
-        if (!(std::abs(dz) < dzCut)) return false;
+        if (!CUT(std::abs(dz) < dzCut, std::abs(dz), -kNoBound, dzCut)) return false;
         const float drtCut = lm.type == kPS ? 2.f : 10.f;
         float drt = std::abs(lo.rt - up.rt);
-        if (!(drt < drtCut)) return false;
+        if (!CUT(drt < drtCut, drt, -kNoBound, drtCut)) return false;
         float xn = 0, yn = 0, zn = 0;
         shift_strip(lo, up, lm, xn, yn, zn);
         P3 shifted;
@@ -446,10 +469,10 @@ struct Event {
         }
         const float miniCut = lm.ltype == kPixel ? dphi_threshold(lo, lm, md.dphi, dz)
                                                  : dphi_threshold(up, lm, md.dphi, dz);
-        if (!(std::abs(md.dphi) < miniCut)) return false;
+        if (!CUT(std::abs(md.dphi) < miniCut, std::abs(md.dphi), -kNoBound, miniCut)) return false;
         float dzFrac = std::abs(dz) / ::fabs((double)lo.z);
         md.dphichange = md.dphi / dzFrac * (1.f + dzFrac);
-        return std::abs(md.dphichange) < miniCut;
+        return CUT(std::abs(md.dphichange) < miniCut, std::abs(md.dphichange), -kNoBound, miniCut);
     }
 
     // Event.cc:245-305
@@ -527,9 +550,9 @@ struct Event {
     bool dalpha_cuts(const MD& imd, const MD& omd, float sg_alpha) const {
         float th[3];
         dalpha_threshold(imd, omd, th);
-        if (!(std::abs(imd.dphichange - sg_alpha) < th[0])) return false;
-        if (!(std::abs(omd.dphichange - sg_alpha) < th[1])) return false;
-        return std::abs(omd.dphichange - imd.dphichange) < th[2];
+        if (!CUT(std::abs(imd.dphichange - sg_alpha) < th[0], std::abs(imd.dphichange - sg_alpha), -kNoBound, th[0])) return false;
+        if (!CUT(std::abs(omd.dphichange - sg_alpha) < th[1], std::abs(omd.dphichange - sg_alpha), -kNoBound, th[1])) return false;
+        return CUT(std::abs(omd.dphichange - imd.dphichange) < th[2], std::abs(omd.dphichange - imd.dphichange), -kNoBound, th[2]);
     }
 
     // Segment.cc:364-599
@@ -546,12 +569,12 @@ struct Event {
         const float zGeom = im.layer <= 2 ? 2.f * kPixelPSZpitch : 2.f * kStrip2SZpitch;
         float zLo = zIn + (zIn - kDeltaZLum) * (rtOut / rtIn - 1.f) * (zIn > 0.f ? 1.f : dzDrtScale) - zGeom;
         float zHi = zIn + (zIn + kDeltaZLum) * (rtOut / rtIn - 1.f) * (zIn < 0.f ? 1.f : dzDrtScale) + zGeom;
-        if (!(zOut >= zLo && zOut <= zHi)) return false;
+        if (!CUT(zOut >= zLo && zOut <= zHi, zOut, zLo, zHi)) return false;
         const float sdCut = sdSlope + ::sqrt((double)(sdMuls * sdMuls + sdPVoff * sdPVoff));
         const float deltaPhi = dphi(ia, oa);
-        if (!(std::abs(deltaPhi) <= sdCut)) return false;
+        if (!CUT(std::abs(deltaPhi) <= sdCut, std::abs(deltaPhi), -kNoBound, sdCut)) return false;
         sg.dphichange = dphichange(ia, oa);
-        if (!(std::abs(sg.dphichange) <= sdCut)) return false;
+        if (!CUT(std::abs(sg.dphichange) <= sdCut, std::abs(sg.dphichange), -kNoBound, sdCut)) return false;
         return dalpha_cuts(imd, omd, sg.dphichange);
     }
 
@@ -563,7 +586,7 @@ struct Event {
         for (uint32_t d : geo.connected(im.detid))
             if (om.detid == d) { found = true; break; }
         bool l2r123 = (im.ring == 1 || im.ring == 2 || im.ring == 3) && im.layer == 2;
-        if (!(found || l2r123)) return false;
+        if (!CUT(found || l2r123, 0.f, -kNoBound, kNoBound)) return false;
         const Hit& iah = hits[imd.anchor];
         const Hit& oah = hits[omd.anchor];
         const P3& ia = iah.p;
@@ -577,13 +600,13 @@ struct Event {
         const float rtGeom = (rtIn < disks2SMinRadius && rtOut < disks2SMinRadius) ? (2.f * kPixelPSZpitch)
                            : ((rtIn < disks2SMinRadius || rtOut < disks2SMinRadius) ? (kPixelPSZpitch + kStrip2SZpitch)
                            : (2.f * kStrip2SZpitch));
-        if (zIn * zOut < 0) return false;
+        if (!CUT(!(zIn * zOut < 0), zIn * zOut, 0.f, kNoBound)) return false;
         const float dz = zOut - zIn;
         const float dLum = std::copysign(kDeltaZLum, zIn);
         const float drtDzScale = sdSlope / f_tan(sdSlope);
         float rtLo = fmax_ref(rtIn * (1.f + dz / (zIn + dLum) * drtDzScale) - rtGeom, rtIn - 0.5f * rtGeom);
         float rtHi = rtIn * (zOut - dLum) / (zIn - dLum) + rtGeom;
-        if (!(rtOut >= rtLo && rtOut <= rtHi)) return false;
+        if (!CUT(rtOut >= rtLo && rtOut <= rtHi, rtOut, rtLo, rtHi)) return false;
         const float dPhiPos = dphi(ia, oa);
         const float sdCut = sdSlope;
         const float hiP = dphi(ia, oHi);
@@ -592,12 +615,12 @@ struct Event {
         sg.dphi = dPhiPos;
         sg.dphimax = hiBigger ? hiP : loP;
         sg.dphimin = hiBigger ? loP : hiP;
-        if (!(std::abs(dPhiPos) <= sdCut)) return false;
+        if (!CUT(std::abs(dPhiPos) <= sdCut, std::abs(dPhiPos), -kNoBound, sdCut)) return false;
         const float dzFrac = dz / zIn;
         sg.dphichange = dPhiPos / dzFrac * (1.f + dzFrac);
         sg.dphiminchange = sg.dphimin / dzFrac * (1.f + dzFrac);
         sg.dphimaxchange = sg.dphimax / dzFrac * (1.f + dzFrac);
-        if (!(std::abs(sg.dphichange) <= sdCut)) return false;
+        if (!CUT(std::abs(sg.dphichange) <= sdCut, std::abs(sg.dphichange), -kNoBound, sdCut)) return false;
         return dalpha_cuts(imd, omd, sg.dphichange);
     }
 
@@ -704,7 +727,7 @@ struct Event {
     // the common tail of the three algorithms: dBeta cut (returns pass)
     bool dbeta_cut(float betaIn, float betaOut, float dBetaCut2) const {
         const float dBeta = betaIn - betaOut;
-        if (!(dBeta * dBeta <= dBetaCut2)) return tlMode == 1;
+        if (!CUT(dBeta * dBeta <= dBetaCut2, dBeta * dBeta, -kNoBound, dBetaCut2)) return tlMode == 1;
         return true;
     }
 
@@ -722,7 +745,7 @@ struct Event {
         const float zpitch_OutLo = isPS_OutLo ? kPixelPSZpitch : kStrip2SZpitch;
         const float zHi = z_InLo + (z_InLo + kDeltaZLum) * (rtRatio - 1.f) * (z_InLo < 0.f ? 1.f : dzDrtScale) + (zpitch_InLo + zpitch_OutLo);
         const float zLo = z_InLo + (z_InLo - kDeltaZLum) * (rtRatio - 1.f) * (z_InLo > 0.f ? 1.f : dzDrtScale) - (zpitch_InLo + zpitch_OutLo);
-        if (!(z_OutLo >= zLo && z_OutLo <= zHi)) return false;
+        if (!CUT(z_OutLo >= zLo && z_OutLo <= zHi, z_OutLo, zLo, zHi)) return false;
         const float drt_OutLo_InLo = rt_OutLo - rt_InLo;
         const float r3_InLo = ::sqrt((double)(z_InLo * z_InLo + rt_InLo * rt_InLo));
         const float drt_InSeg = q.inUp->p.rt - q.inLo->p.rt;
@@ -738,7 +761,7 @@ struct Event {
         const float zWindow = dzErr / drt_InSeg * drt_OutLo_InLo + (zpitch_InLo + zpitch_OutLo);
         const float zLoPointed = z_InLo + dzMean * (z_InLo > 0.f ? 1.f : dzDrtScale) - zWindow;
         const float zHiPointed = z_InLo + dzMean * (z_InLo < 0.f ? 1.f : dzDrtScale) + zWindow;
-        if (!(z_OutLo >= zLoPointed && z_OutLo <= zHiPointed)) return false;
+        if (!CUT(z_OutLo >= zLoPointed && z_OutLo <= zHiPointed, z_OutLo, zLoPointed, zHiPointed)) return false;
         const float sdlPVoff = 0.1f / rt_OutLo;
         const float sdlCut = alpha1GeV_OutLo + ::sqrt((double)(sdlMuls * sdlMuls + sdlPVoff * sdlPVoff));
         const P3& hInUp = q.inUp->p;
@@ -746,10 +769,10 @@ struct Event {
         const P3& hInLo = q.inLo->p;
         const P3& hOutLo = q.outLo->p;
         float deltaPhiPos = dphi(hInUp, hOutUp);
-        if (!(std::abs(deltaPhiPos) <= sdlCut)) return false;
+        if (!CUT(std::abs(deltaPhiPos) <= sdlCut, std::abs(deltaPhiPos), -kNoBound, sdlCut)) return false;
         const P3 mid = midpoint(hInLo, hOutLo);
         const float dPhi = dphi(mid, sub(hOutLo, hInLo));
-        if (!(std::abs(dPhi) <= sdlCut)) return false;
+        if (!CUT(std::abs(dPhi) <= sdlCut, std::abs(dPhi), -kNoBound, sdlCut)) return false;
         const float alpha_InLo = q.isg->dphichange;
         const bool isEC_lastLayer = q.mOutUp->subdet == kEndcap && q.mOutUp->type == kTwoS;
         const P3 hiE = isEC_lastLayer ? strip_edge(hOutUp, q.mOutUp->detid, true) : hOutUp;
@@ -769,7 +792,7 @@ struct Event {
         const float corrF = 1.f;
         const float rt_InSeg = sub(hInUp, hInLo).rt;
         const float betaIn_cut = f_asin(fmin_ref((-rt_InSeg * corrF + drt_tl_axis) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / drt_InSeg);
-        if (!(std::abs(betaInRHmin) < betaIn_cut)) return false;
+        if (!CUT(std::abs(betaInRHmin) < betaIn_cut, std::abs(betaInRHmin), -kNoBound, betaIn_cut)) return false;
         float betaAv = 0.5f * (betaIn + betaOut);
         float pt_beta = drt_tl_axis * k2Rinv1GeVf / ::sin((double)betaAv);
         const int lIn = 5;
@@ -793,7 +816,7 @@ struct Event {
         const float dBetaRIn2 = 0;
         const float dBetaROut2 = ::pow((double)((hiE.rt - loE.rt) * sinDPhi / drt_tl_axis), 2);
         const float betaOut_cut = f_asin(fmin_ref(drt_tl_axis * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d) + ::sqrt((double)(dBetaLum2 + dBetaMuls * dBetaMuls));
-        if (!(std::abs(betaOut) < betaOut_cut)) return false;
+        if (!CUT(std::abs(betaOut) < betaOut_cut, std::abs(betaOut), -kNoBound, betaOut_cut)) return false;
         const float dBetaRes = 0.02f / fmin_ref(sdOut_d, drt_InSeg);
         const float dBetaCut2 = (dBetaRes * dBetaRes * 2.0f + dBetaMuls * dBetaMuls + dBetaLum2 + dBetaRIn2 + dBetaROut2 +
                                  0.25 * ::pow((double)(std::abs(betaInRHmin - betaInRHmax) + std::abs(betaOutRHmin - betaOutRHmax)), 2));
@@ -807,17 +830,17 @@ struct Event {
         const float rtIn = q.inLo->p.rt, rtOut = q.outLo->p.rt, zIn = q.inLo->p.z, zOut = q.outLo->p.z;
         const float sdlSlope = f_asin(fmin_ref(rtOut * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
         const float dzDrtScale = ::tan((double)sdlSlope) / sdlSlope;
-        if (!(zIn * zOut > 0)) return false;
+        if (!CUT(zIn * zOut > 0, zIn * zOut, 0.f, kNoBound)) return false;
         const float dLum = std::copysign(kDeltaZLum, zIn);
         const bool isOutSgInnerMDPS = q.mOutLo->type == kPS;
         const float rtGeom1 = isOutSgInnerMDPS ? kPixelPSZpitch : kStrip2SZpitch;
         const float zGeom1 = std::copysign(zGeom, zIn);
         const float rtLo = rtIn * (1.f + (zOut - zIn - zGeom1) / (zIn + zGeom1 + dLum) / dzDrtScale) - rtGeom1;
-        if (!(rtOut >= rtLo)) return false;
+        if (!CUT(rtOut >= rtLo, rtOut, rtLo, kNoBound)) return false;
         float zInForHi = zIn - zGeom1 - dLum;
         if (zInForHi * zIn < 0) zInForHi = std::copysign(0.1f, zIn);
         const float rtHi = rtIn * (1.f + (zOut - zIn + zGeom1) / zInForHi) + rtGeom1;
-        if (!(rtOut >= rtLo && rtOut <= rtHi)) return false;
+        if (!CUT(rtOut >= rtLo && rtOut <= rtHi, rtOut, rtLo, rtHi)) return false;
         const float rIn = ::sqrt((double)(zIn * zIn + rtIn * rtIn));
         const float drtSDIn = q.inUp->p.rt - q.inLo->p.rt;
         const float dzSDIn = q.inUp->p.z - q.inLo->p.z;
@@ -832,7 +855,7 @@ struct Event {
         const float sdlMuls = sdlThetaMulsF * 3.f / kPtCut * 4.f;
         drtErr += sdlMuls * sdlMuls * multDzDr * multDzDr / 3.f * coshEta * coshEta;
         drtErr = ::sqrt((double)drtErr);
-        if (!(kZ >= 0 && rtOut >= rtLo && rtOut <= rtHi)) return false;
+        if (!CUT(kZ >= 0 && rtOut >= rtLo && rtOut <= rtHi, rtOut, rtLo, rtHi)) return false;
         const float sdlPVoff = 0.1f / rtOut;
         const float sdlCut = sdlSlope + ::sqrt((double)(sdlMuls * sdlMuls + sdlPVoff * sdlPVoff));
         const P3& hInUp = q.inUp->p;
@@ -840,10 +863,10 @@ struct Event {
         const P3& hInLo = q.inLo->p;
         const P3& hOutLo = q.outLo->p;
         float deltaPhiPos = dphi(hInUp, hOutUp);
-        if (!(std::abs(deltaPhiPos) <= sdlCut)) return false;
+        if (!CUT(std::abs(deltaPhiPos) <= sdlCut, std::abs(deltaPhiPos), -kNoBound, sdlCut)) return false;
         const P3 mid = midpoint(hInLo, hOutLo);
         const float dPhi = dphi(mid, sub(hOutLo, hInLo));
-        if (!(std::abs(dPhi) <= sdlCut)) return false;
+        if (!CUT(std::abs(dPhi) <= sdlCut, std::abs(dPhi), -kNoBound, sdlCut)) return false;
         const float sdIn_alpha = q.isg->dphichange;
         const float sdOut_alpha = q.isg->dphichange;  // (sic) Tracklet.cc:1790
         const float sdOut_alphaOut = dphi(hOutUp, sub(hOutUp, hOutLo));
@@ -864,7 +887,7 @@ struct Event {
         const float dr = dr3.rt;
         const float corrF = 1.f;
         const float betaIn_cut = f_asin(fmin_ref((-sdIn_dr * corrF + dr) * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdIn_d);
-        if (!(std::abs(betaInRHmin) < betaIn_cut)) return false;
+        if (!CUT(std::abs(betaInRHmin) < betaIn_cut, std::abs(betaInRHmin), -kNoBound, betaIn_cut)) return false;
         float betaAv = 0.5f * (betaIn + betaOut);
         float pt_beta = dr * k2Rinv1GeVf / ::sin((double)betaAv);
         const int lIn = 5, lOut = 11;
@@ -889,7 +912,7 @@ struct Event {
         const float dBetaRIn2 = 0;
         const float dBetaROut2 = ::pow((double)((hiE.rt - loE.rt) * sinDPhi / dr), 2);
         const float betaOut_cut = f_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d) + ::sqrt((double)(dBetaLum2 + dBetaMuls * dBetaMuls));
-        if (!(std::abs(betaOut) < betaOut_cut)) return false;
+        if (!CUT(std::abs(betaOut) < betaOut_cut, std::abs(betaOut), -kNoBound, betaOut_cut)) return false;
         const float dBetaRes = 0.02f / fmin_ref(sdOut_d, sdIn_d);
         const float dBetaCut2 = (dBetaRes * dBetaRes * 2.0f + dBetaMuls * dBetaMuls + dBetaLum2 + dBetaRIn2 + dBetaROut2 +
                                  0.25 * ::pow((double)(std::abs(betaInRHmin - betaInRHmax) + std::abs(betaOutRHmin - betaOutRHmax)), 2));
@@ -904,7 +927,7 @@ struct Event {
         const float rtIn = q.inLo->p.rt, rtOut = q.outLo->p.rt, zIn = q.inLo->p.z, zOut = q.outLo->p.z;
         const float sdlSlope = f_asin(fmin_ref(rtOut * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
         const float dzDrtScale = ::tan((double)sdlSlope) / sdlSlope;
-        if (!(zIn * zOut > 0)) return false;
+        if (!CUT(zIn * zOut > 0, zIn * zOut, 0.f, kNoBound)) return false;
         const float dLum = std::copysign(kDeltaZLum, zIn);
         const bool isOutSgInnerMDPS = q.mOutLo->type == kPS;
         const bool isInSgInnerMDPS = q.mInLo->type == kPS;
@@ -912,9 +935,9 @@ struct Event {
                            : (isInSgInnerMDPS || isOutSgInnerMDPS) ? (kPixelPSZpitch + kStrip2SZpitch) : 2.f * kStrip2SZpitch;
         const float dz = zOut - zIn;
         const float rtLo = rtIn * (1.f + dz / (zIn + dLum) / dzDrtScale) - rtGeom;
-        if (!(rtOut >= rtLo)) return false;
+        if (!CUT(rtOut >= rtLo, rtOut, rtLo, kNoBound)) return false;
         const float rtHi = rtIn * (1.f + dz / (zIn - dLum)) + rtGeom;
-        if (!(rtOut >= rtLo && rtOut <= rtHi)) return false;
+        if (!CUT(rtOut >= rtLo && rtOut <= rtHi, rtOut, rtLo, rtHi)) return false;
         const bool isInSgOuterMDPS = q.mInUp->type == kPS;
         const float drtSDIn = q.inUp->p.rt - q.inLo->p.rt;
         const float dzSDIn = q.inUp->p.z - q.inLo->p.z;
@@ -933,7 +956,7 @@ struct Event {
         const float rtLo_point = rtIn + drtMean / dzDrtScale - rtWindow;
         const float rtHi_point = rtIn + drtMean + rtWindow;
         if (isInSgInnerMDPS && isInSgOuterMDPS) {
-            if (!(kZ >= 0 && rtOut >= rtLo_point && rtOut <= rtHi_point)) return false;
+            if (!CUT(kZ >= 0 && rtOut >= rtLo_point && rtOut <= rtHi_point, rtOut, rtLo_point, rtHi_point)) return false;
         }
         const float sdlPVoff = 0.1f / rtOut;
         const float sdlCut = sdlSlope + ::sqrt((double)(sdlMuls * sdlMuls + sdlPVoff * sdlPVoff));
@@ -942,10 +965,10 @@ struct Event {
         const P3& hInLo = q.inLo->p;
         const P3& hOutLo = q.outLo->p;
         float deltaPhiPos = dphi(hInUp, hOutUp);
-        if (!(std::abs(deltaPhiPos) <= sdlCut)) return false;
+        if (!CUT(std::abs(deltaPhiPos) <= sdlCut, std::abs(deltaPhiPos), -kNoBound, sdlCut)) return false;
         const P3 mid = midpoint(hInLo, hOutLo);
         const float dPhi = dphi(mid, sub(hOutLo, hInLo));
-        if (!(std::abs(dPhi) <= sdlCut)) return false;
+        if (!CUT(std::abs(dPhi) <= sdlCut, std::abs(dPhi), -kNoBound, sdlCut)) return false;
         const float sdIn_alpha = q.isg->dphichange;
         const float sdOut_alpha = q.isg->dphichange;  // (sic)
         float sdOut_dPhiPos = dphi(hOutLo, hOutUp);
@@ -990,7 +1013,7 @@ struct Event {
         const float dBetaRIn2 = 0;
         const float dBetaROut2 = 0;
         const float betaOut_cut = f_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d) + ::sqrt((double)(dBetaLum2 + dBetaMuls * dBetaMuls));
-        if (!(std::abs(betaOut) < betaOut_cut)) return false;
+        if (!CUT(std::abs(betaOut) < betaOut_cut, std::abs(betaOut), -kNoBound, betaOut_cut)) return false;
         const float dBetaRes = 0.02f / fmin_ref(sdOut_d, sdIn_d);
         const float dBetaCut2 = (dBetaRes * dBetaRes * 2.0f + dBetaMuls * dBetaMuls + dBetaLum2 + dBetaRIn2 + dBetaROut2 +
                                  0.25 * ::pow((double)(std::abs(betaInRHmin - betaInRHmax) + std::abs(betaOutRHmin - betaOutRHmax)), 2));
@@ -1226,8 +1249,16 @@ struct Event {
     void push_tl(std::vector<int32_t>& v, const Pair& p) const { push_sg(v, p.in); push_sg(v, p.out); }
 
     void emit(Result& r) const {
-        for (size_t i = 0; i < mds.size(); ++i) push_md(r.t[0], (int)i);
-        for (size_t i = 0; i < sgs.size(); ++i) push_sg(r.t[1], (int)i);
+        for (size_t i = 0; i < mds.size(); ++i) {
+            push_md(r.t[0], (int)i);
+            const MD& m = mds[i];
+            r.vals[0].insert(r.vals[0].end(), {m.dz, m.shiftedDz, m.dphi, m.dphichange});
+        }
+        for (size_t i = 0; i < sgs.size(); ++i) {
+            push_sg(r.t[1], (int)i);
+            const SG& g = sgs[i];
+            r.vals[1].insert(r.vals[1].end(), {g.dphi, g.dphimin, g.dphimax, g.dphichange, g.dphiminchange, g.dphimaxchange});
+        }
         for (auto& p : tls) push_tl(r.t[2], p);
         for (auto& p : tps) push_tl(r.t[3], p);
         for (auto& p : tcs) { push_tl(r.t[4], tls[p.in]); push_tl(r.t[4], tls[p.out]); }
@@ -1243,12 +1274,11 @@ double now() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
 
-Result* run_event(const Geo& g, int64_t n, const float* x, const float* y, const float* z, const int32_t* idx,
-                  const uint32_t* detid, int mode, int stop_after) {
-    LibmScope libm;
-    Result* r = new Result();
-    std::memset(r->seconds, 0, sizeof(r->seconds));
-    Event ev(g);
+// the chain on one event's hits, with the stage timings in r (may be NULL)
+void run_chain(Event& ev, int64_t n, const float* x, const float* y, const float* z, const int32_t* idx,
+               const uint32_t* detid, int mode, int stop_after, Result* r) {
+    Result dummy;
+    if (!r) r = &dummy;
     ev.tlMode = (mode & 4) ? 1 : 0;
     ev.hits.reserve(n);
     for (int64_t i = 0; i < n; ++i) ev.add_hit(x[i], y[i], z[i], idx[i], detid[i]);
@@ -1279,8 +1309,175 @@ Result* run_event(const Geo& g, int64_t n, const float* x, const float* y, const
         else ev.create_tcs(0);
         r->seconds[4] = now() - t0;
     }
+}
+
+Result* run_event(const Geo& g, int64_t n, const float* x, const float* y, const float* z, const int32_t* idx,
+                  const uint32_t* detid, int mode, int stop_after) {
+    LibmScope libm;
+    Result* r = new Result();
+    std::memset(r->seconds, 0, sizeof(r->seconds));
+    Event ev(g);
+    run_chain(ev, n, x, y, z, idx, detid, mode, stop_after, r);
     ev.emit(*r);
     return r;
+}
+
+// ---------------------------------------------------------------- near-cut audit
+// The chain is run twice on one event, with the reference's float libm
+// (glibc) and with correctly rounded floats; every object that only one of
+// the two runs makes is listed.  A "primary" flip is a candidate whose
+// constituents both runs made but whose cuts decide differently: it is
+// evaluated again in both runs with the cut trace on, and the cut that
+// rejects it in one run is reported with its compared value and bounds in
+// both (the distance to the cut).  A "secondary" flip only follows from a
+// primary one (a missing constituent); triplets and track candidates, which
+// are joins without float cuts, can only flip that way.
+struct AuditRec {
+    int32_t stage, accept_glibc, primary, pad;
+    int32_t tuple[8];
+    float g_value, g_lo, g_hi, r_value, r_lo, r_hi;
+    char where[24];
+    char cut[88];
+};
+
+using Key = std::array<int32_t, 8>;
+
+Key key_of(const std::vector<int32_t>& t, size_t row, int w) {
+    Key k;
+    k.fill(INT32_MIN);
+    for (int c = 0; c < w; ++c) k[c] = t[row * w + c];
+    return k;
+}
+
+std::vector<CutRec> traced(int libm, const std::function<void()>& f) {
+    std::vector<CutRec> t;
+    const int keep = tl_libm;
+    tl_libm = libm;
+    tl_trace = &t;
+    f();
+    tl_trace = nullptr;
+    tl_libm = keep;
+    return t;
+}
+
+void audit_event(const Geo& g, int64_t n, const float* x, const float* y, const float* z, const int32_t* idx,
+                 const uint32_t* detid, int mode, std::vector<AuditRec>& out, int64_t* summary20) {
+    static const int w[3] = {2, 4, 8};
+    Event ev[2] = {Event(g), Event(g)};
+    Result res[2];
+    for (int k = 0; k < 2; ++k) {
+        const int keep = tl_libm;
+        tl_libm = k == 0 ? kLibmGlibc : kLibmRounded;
+        run_chain(ev[k], n, x, y, z, idx, detid, mode, 4, nullptr);
+        tl_libm = keep;
+        ev[k].emit(res[k]);
+    }
+    // object index of each key (first occurrence) per stage and run
+    std::map<Key, std::vector<int>> obj[3][2];
+    for (int k = 0; k < 2; ++k)
+        for (int s = 0; s < 3; ++s) {
+            const size_t nr = res[k].t[s].size() / w[s];
+            for (size_t r = 0; r < nr; ++r) obj[s][k][key_of(res[k].t[s], r, w[s])].push_back((int)r);
+        }
+    for (int s = 0; s < 5; ++s) {
+        summary20[s * 4 + 0] = (int64_t)res[0].t[s].size() / (s == 0 ? 2 : s == 1 ? 4 : s == 4 ? 16 : 8);
+        summary20[s * 4 + 1] = (int64_t)res[1].t[s].size() / (s == 0 ? 2 : s == 1 ? 4 : s == 4 ? 16 : 8);
+    }
+    // triplets and track candidates: secondary flips only (multiset differences)
+    for (int s = 3; s < 5; ++s) {
+        const int ws = s == 4 ? 16 : 8;
+        std::map<std::vector<int32_t>, int64_t> c;
+        for (int k = 0; k < 2; ++k)
+            for (size_t r = 0; r + ws <= res[k].t[s].size(); r += ws)
+                c[std::vector<int32_t>(res[k].t[s].begin() + r, res[k].t[s].begin() + r + ws)] += k == 0 ? 1 : -1;
+        int64_t d = 0;
+        for (auto& kv : c) d += kv.second < 0 ? -kv.second : kv.second;
+        summary20[s * 4 + 2] = 0;
+        summary20[s * 4 + 3] = d;
+    }
+    for (int s = 0; s < 3; ++s) {
+        int64_t prim = 0, sec = 0;
+        for (int k = 0; k < 2; ++k) {
+            const int o = 1 - k;  // the run that lacks the object
+            for (auto& kv : obj[s][k]) {
+                auto it = obj[s][o].find(kv.first);
+                const size_t have = it == obj[s][o].end() ? 0 : it->second.size();
+                if (kv.second.size() <= have) continue;
+                const int64_t extra = (int64_t)(kv.second.size() - have);
+                const Key& K = kv.first;
+                // constituents in the run that lacks it
+                int ci = -1, cj = -1;
+                Event& eo = ev[o];
+                Event& ek = ev[k];
+                const int row = kv.second[0];
+                if (s == 0) {
+                    ci = ek.mds[row].lo;
+                    cj = ek.mds[row].up;
+                } else {
+                    const Key a = [&] { Key q; q.fill(INT32_MIN); for (int c = 0; c < w[s - 1]; ++c) q[c] = K[c]; return q; }();
+                    const Key b = [&] { Key q; q.fill(INT32_MIN); for (int c = 0; c < w[s - 1]; ++c) q[c] = K[w[s - 1] + c]; return q; }();
+                    auto ia = obj[s - 1][o].find(a), ib = obj[s - 1][o].find(b);
+                    if (ia != obj[s - 1][o].end() && ib != obj[s - 1][o].end()) {
+                        ci = ia->second[0];
+                        cj = ib->second[0];
+                    }
+                }
+                if (s > 0 && ci < 0) {
+                    sec += extra;
+                    continue;
+                }
+                prim += extra;
+                // evaluate the candidate in both runs with the trace on
+                std::vector<CutRec> tr[2];
+                for (int m = 0; m < 2; ++m) {
+                    Event& e = ev[m];
+                    const int libm = m == 0 ? kLibmGlibc : kLibmRounded;
+                    if (s == 0) {
+                        const int lh = m == k ? ek.mds[row].lo : ci, uh = m == k ? ek.mds[row].up : cj;
+                        const ModInfo lm = e.mods[e.hits[lh].mod];
+                        tr[m] = traced(libm, [&] {
+                            MD md;
+                            if (lm.subdet == kBarrel) e.md_barrel(e.hits[lh].p, e.hits[uh].p, lm, md);
+                            else e.md_endcap(e.hits[lh].p, e.hits[uh].p, lm, md);
+                        });
+                    } else if (s == 1) {
+                        const int a = m == k ? ek.sgs[row].imd : ci, b = m == k ? ek.sgs[row].omd : cj;
+                        tr[m] = traced(libm, [&] {
+                            SG sg;
+                            e.run_sg(a, b, 0, sg);
+                        });
+                    } else {
+                        const int a = m == k ? ek.tls[row].in : ci, b = m == k ? ek.tls[row].out : cj;
+                        tr[m] = traced(libm, [&] { e.run_tl(a, b, e.tlMode); });
+                    }
+                }
+                AuditRec rec{};
+                rec.stage = s;
+                rec.accept_glibc = k == 0;
+                rec.primary = 1;
+                for (int c = 0; c < 8; ++c) rec.tuple[c] = c < w[s] ? K[c] : -1;
+                // the cut that rejects it in the run that lacks it, and the same cut in the other run
+                const std::vector<CutRec>& rej = tr[o];
+                const CutRec* rc = nullptr;
+                for (const CutRec& c : rej)
+                    if (!c.pass) { rc = &c; break; }
+                if (rc) {
+                    std::snprintf(rec.where, sizeof(rec.where), "%s", rc->where);
+                    std::snprintf(rec.cut, sizeof(rec.cut), "%s", rc->cut);
+                    const CutRec* ac = nullptr;
+                    for (const CutRec& c : tr[k])
+                        if (c.cut == rc->cut) ac = &c;
+                    const CutRec* gc = o == 0 ? rc : ac;
+                    const CutRec* cc = o == 0 ? ac : rc;
+                    if (gc) { rec.g_value = gc->value; rec.g_lo = gc->lo; rec.g_hi = gc->hi; }
+                    if (cc) { rec.r_value = cc->value; rec.r_lo = cc->lo; rec.r_hi = cc->hi; }
+                }
+                out.push_back(rec);
+            }
+        }
+        summary20[s * 4 + 2] = prim;
+        summary20[s * 4 + 3] = sec;
+    }
 }
 
 // Order-independent digest of an object list (hit-index tuples of width w):
@@ -1339,6 +1536,12 @@ void sdlo_copy(const void* res, int stage, int32_t* out) {
     if (!r->t[stage].empty()) std::memcpy(out, r->t[stage].data(), r->t[stage].size() * 4);
 }
 
+void sdlo_vals(const void* res, int stage, float* out) {
+    const Result* r = static_cast<const Result*>(res);
+    if ((stage == 0 || stage == 1) && !r->vals[stage].empty())
+        std::memcpy(out, r->vals[stage].data(), r->vals[stage].size() * sizeof(float));
+}
+
 void sdlo_counters(const void* res, uint32_t* out110) {
     std::memcpy(out110, static_cast<const Result*>(res)->counters, 110 * 4);
 }
@@ -1375,6 +1578,17 @@ void sdlo_libm_values(int fn, uint32_t start_bits, int64_t n, float* out, int n_
     for (int i = 0; i < std::max(1, n_threads); ++i) th.emplace_back(work);
     for (auto& t : th) t.join();
 }
+
+int64_t sdlo_audit(const void* geo, int64_t n, const float* x, const float* y, const float* z, const int32_t* idx,
+                   const uint32_t* detid, int mode, void* out, int64_t cap, int64_t* summary20) {
+    std::vector<AuditRec> recs;
+    audit_event(*static_cast<const Geo*>(geo), n, x, y, z, idx, detid, mode, recs, summary20);
+    const int64_t m = std::min<int64_t>(cap, (int64_t)recs.size());
+    if (m > 0) std::memcpy(out, recs.data(), m * sizeof(AuditRec));
+    return (int64_t)recs.size();
+}
+
+int sdlo_audit_record_size() { return (int)sizeof(AuditRec); }
 
 void sdlo_set_libm(int mode) { g_libm_mode = (mode == kLibmRounded || mode == kLibmCount) ? mode : kLibmGlibc; }
 

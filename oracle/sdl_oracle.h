@@ -45,8 +45,24 @@ int64_t sdlo_count(const void* res, int stage);
 int sdlo_width(int stage);
 void sdlo_copy(const void* res, int stage, int32_t* out);
 void sdlo_counters(const void* res, uint32_t* out110);
+/* per-object floats in tuple order: stage 0 (mini-doublets) dz, shiftedDz,
+ * dphi, dphichange; stage 1 (segments) dphi, dphimin, dphimax, dphichange,
+ * dphiminchange, dphimaxchange */
+void sdlo_vals(const void* res, int stage, float* out);
 void sdlo_times(const void* res, double* out5);
 void sdlo_free(void* res);
+
+/* Near-cut audit of one event: the chain with the reference's float libm
+ * (glibc) and with correctly rounded floats; every object only one of them
+ * makes is written to out (cap records of sdlo_audit_record_size() bytes:
+ * int32 stage, accepted with glibc, primary, pad, tuple[8] (-1 padded),
+ * float value, lo, hi of the rejecting cut with glibc, the same with rounded
+ * floats, char where[24], char cut[88]); summary20 = per stage {objects with
+ * glibc, objects rounded, primary flips, secondary flips}.  Returns the
+ * number of records (may exceed cap). */
+int64_t sdlo_audit(const void* geo, int64_t n, const float* x, const float* y, const float* z, const int32_t* idx,
+                   const uint32_t* detid, int mode, void* out, int64_t cap, int64_t* summary20);
+int sdlo_audit_record_size(void);
 
 /* Float libm used for the reference's std::asin/atan/sin/cos/tan on floats
  * (process-wide, read at the start of each event): 0 glibc's float functions

@@ -155,46 +155,80 @@ struct LibmTab {
 enum { kLmAsin = 0, kLmAtan, kLmSin, kLmCos, kLmTan, kLmCount };
 static __constant__ LibmTab c_libm[kLmCount];
 
-// the host libm's value for |x| (ax), given the correctly rounded value r of ax
-__device__ __forceinline__ float libm_host(int fn, float ax, float r) {
+// The table word of |x| (ax) is loaded first and the correctly rounded value
+// computed while the load is in flight (the float-float paths are inlined;
+// only their rare double fallbacks are calls); libm_pick then moves the value.
+struct LibmWord {
+    uint32_t w, k;
+    bool in;
+};
+__device__ __forceinline__ LibmWord libm_word(int fn, float ax) {
     const LibmTab& t = c_libm[fn];
-    const uint32_t k = __float_as_uint(ax) - t.lo;
-    if (k >= t.n) return r;
-    const uint32_t c = (__ldg(t.code + (k >> 4)) >> ((k & 15u) * 2u)) & 3u;
+    LibmWord r;
+    r.k = __float_as_uint(ax) - t.lo;
+    r.in = r.k < t.n;
+    r.w = r.in ? __ldg(t.code + (r.k >> 4)) : 0u;
+    return r;
+}
+// the host libm's value for |x| (ax), given the correctly rounded value r of ax
+static __device__ __noinline__ float libm_exception(int fn, float ax, float r) {
+    const LibmTab& t = c_libm[fn];
+    const uint32_t u = __float_as_uint(ax);
+    uint32_t a = 0, b = t.n_exc;
+    while (a < b) {
+        const uint32_t m = (a + b) >> 1;
+        if (__ldg(t.exc_x + m) < u) a = m + 1;
+        else b = m;
+    }
+    return (a < t.n_exc && __ldg(t.exc_x + a) == u) ? __ldg(t.exc_v + a) : r;
+}
+__device__ __forceinline__ float libm_pick(int fn, LibmWord lw, float ax, float r) {
+    if (!lw.in) return r;
+    const uint32_t c = (lw.w >> ((lw.k & 15u) * 2u)) & 3u;
     if (c == 1u) return nextafterf(r, INFINITY);
     if (c == 2u) return nextafterf(r, -INFINITY);
-    if (c == 3u) {
-        const uint32_t u = __float_as_uint(ax);
-        uint32_t a = 0, b = t.n_exc;
-        while (a < b) {
-            const uint32_t m = (a + b) >> 1;
-            if (__ldg(t.exc_x + m) < u) a = m + 1;
-            else b = m;
-        }
-        if (a < t.n_exc && __ldg(t.exc_x + a) == u) return __ldg(t.exc_v + a);
-    }
+    if (c == 3u) return libm_exception(fn, ax, r);
     return r;
 }
 // std::asin, std::atan, std::sin, std::tan (odd) and std::cos (even) of a
 // float, as the host libm computes them
 static __device__ __noinline__ float g_asin(float x) {
-    const float ax = fabsf(x), r = libm_host(kLmAsin, ax, f_asin(ax));
+    const float ax = fabsf(x);
+    const LibmWord lw = libm_word(kLmAsin, ax);
+    float r;
+    if (!f_asin_fast(ax, r)) r = f_asin_d(ax);
+    r = libm_pick(kLmAsin, lw, ax, r);
     return x < 0.f ? -r : r;
 }
 static __device__ __noinline__ float g_atan(float x) {
-    const float ax = fabsf(x), r = libm_host(kLmAtan, ax, f_atan(ax));
+    const float ax = fabsf(x);
+    const LibmWord lw = libm_word(kLmAtan, ax);
+    float r;
+    if (!f_atan_fast(ax, r)) r = f_atan_d(ax);
+    r = libm_pick(kLmAtan, lw, ax, r);
     return x < 0.f ? -r : r;
 }
 static __device__ __noinline__ float g_sin(float x) {
-    const float ax = fabsf(x), r = libm_host(kLmSin, ax, f_sin(ax));
+    const float ax = fabsf(x);
+    const LibmWord lw = libm_word(kLmSin, ax);
+    float r;
+    if (!f_sincos_fast(ax, 0, r)) r = f_sin_d(ax);
+    r = libm_pick(kLmSin, lw, ax, r);
     return x < 0.f ? -r : r;
 }
 static __device__ __noinline__ float g_cos(float x) {
     const float ax = fabsf(x);
-    return libm_host(kLmCos, ax, f_cos(ax));
+    const LibmWord lw = libm_word(kLmCos, ax);
+    float r;
+    if (!f_sincos_fast(ax, 1, r)) r = f_cos_d(ax);
+    return libm_pick(kLmCos, lw, ax, r);
 }
 static __device__ __noinline__ float g_tan(float x) {
-    const float ax = fabsf(x), r = libm_host(kLmTan, ax, f_tan_ff(ax));
+    const float ax = fabsf(x);
+    const LibmWord lw = libm_word(kLmTan, ax);
+    float r;
+    if (!f_tan_fast(ax, false, r)) r = f_tan(ax);
+    r = libm_pick(kLmTan, lw, ax, r);
     return x < 0.f ? -r : r;
 }
 
@@ -588,13 +622,15 @@ struct MDView {
 constexpr int kMdPack = 16;  // floats per packed mini-doublet record
 
 // Segment.cc:886-994 (the three thresholds)
-__device__ __forceinline__ void dalpha_threshold(const MDView& im, const MDView& om, float th[3]) {
+// host: the host libm's asin (the reference's), else the correctly rounded one
+__device__ __forceinline__ void dalpha_threshold(const MDView& im, const MDView& om, float th[3], bool host) {
     const float mulsB[6] = {0.0052f, 0.0038f, 0.0034f, 0.0034f, 0.0032f, 0.0034f};
     const ModDev& I = *im.m;
     const ModDev& O = *om.m;
     const float sdMuls = I.subdet == kBarrel ? mulsB[I.layer - 1] * 3.f / kPtCut : 0.006f * 3.f / kPtCut;
     const float segmentDr = hypot_ref(om.a.y - im.a.y, om.a.x - im.a.x);
-    const float dAlpha_Bfield = g_asin(fmin_ref(segmentDr * k2Rinv1GeVf / kPtCut, kSinAlphaMax));
+    const float a = fmin_ref(segmentDr * k2Rinv1GeVf / kPtCut, kSinAlphaMax);
+    const float dAlpha_Bfield = host ? g_asin(a) : f_asin(a);
     const bool inTilt = I.subdet == kBarrel && I.side != kCenter;
     const bool outTilt = O.subdet == kBarrel && O.side != kCenter;
     const float iTilt = inTilt ? I.tilt : 0.f;
@@ -615,12 +651,33 @@ __device__ __forceinline__ void dalpha_threshold(const MDView& im, const MDView&
     th[2] = add_dsqrt3(dAlpha_Bfield, res, sdMuls, 0.f);
 }
 
+// |v - t| small enough that replacing the correctly rounded value of one
+// float libm call behind t by the host libm's (one float step away) could
+// move t across v
+__device__ __forceinline__ bool near_cut(float v, float t, float rel) { return fabsf(v - t) <= fabsf(t) * rel; }
+
+// The three dAlpha cuts are decided with the correctly rounded asin first.
+// The host libm's asin is within one float step of it (dAlpha_Bfield >= 0);
+// each threshold, dAlpha_Bfield + a square root (with dAlpha_Bfield inside it
+// for tilted modules, times a tilt factor below 1) rounded to float, moves
+// by at most three float steps, 2^-21 |t|; a comparison at least 2^-19 |t|
+// from its threshold is therefore the host's decision too, and the rare
+// closer ones are decided again with the host libm's asin.
 __device__ __forceinline__ bool dalpha_cuts(const MDView& im, const MDView& om, float sg_alpha) {
     float th[3];
-    dalpha_threshold(im, om, th);
-    if (!(fabsf(im.dphichange - sg_alpha) < th[0])) return false;
-    if (!(fabsf(om.dphichange - sg_alpha) < th[1])) return false;
-    return fabsf(om.dphichange - im.dphichange) < th[2];
+    dalpha_threshold(im, om, th, false);
+    const float v0 = fabsf(im.dphichange - sg_alpha), v1 = fabsf(om.dphichange - sg_alpha);
+    const float v2 = fabsf(om.dphichange - im.dphichange);
+    const float rel = 0x1p-19f;
+    bool close = near_cut(v0, th[0], rel);
+    if (v0 < th[0]) {
+        close |= near_cut(v1, th[1], rel);
+        if (v1 < th[1]) close |= near_cut(v2, th[2], rel);
+    }
+    if (close) dalpha_threshold(im, om, th, true);
+    if (!(v0 < th[0])) return false;
+    if (!(v1 < th[1])) return false;
+    return v2 < th[2];
 }
 
 struct SGVals {
@@ -835,27 +892,28 @@ __device__ __forceinline__ float edge_rt(float x, float y, float ex, float ey, b
 // Tracklet.cc:3181-3324.  The reference adds the double copysign term to a
 // float and rounds to float; a double sum of two floats rounded to float
 // equals the float sum (53 >= 2*24+2), so the additions are done in float.
+__device__ __forceinline__ float lm_asin(float x, bool host) { return host ? g_asin(x) : f_asin(x); }
 __device__ __forceinline__ void delta_beta_iterations(float& betaIn, float& betaOut, float& betaAv, float& pt_beta, float sdIn_dr,
-                                                      float sdOut_dr, float dr, int lIn, float pt_betaMax) {
+                                                      float sdOut_dr, float dr, int lIn, float pt_betaMax, bool host) {
     const float sinAlphaMax = 0.95f;
     if (betaIn * betaOut > 0.f &&
         (fabsf(pt_beta) < 4.f * pt_betaMax || (lIn >= 11 && fabsf(pt_beta) < 8.f * pt_betaMax))) {
-        const float betaInUpd = betaIn + copysignf(g_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
-        const float betaOutUpd = betaOut + copysignf(g_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaOut);
+        const float betaInUpd = betaIn + copysignf(lm_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax), host), betaIn);
+        const float betaOutUpd = betaOut + copysignf(lm_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax), host), betaOut);
         betaAv = 0.5f * (betaInUpd + betaOutUpd);
         pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
-        betaIn = betaIn + copysignf(g_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
-        betaOut = betaOut + copysignf(g_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaOut);
+        betaIn = betaIn + copysignf(lm_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax), host), betaIn);
+        betaOut = betaOut + copysignf(lm_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax), host), betaOut);
         betaAv = 0.5f * (betaIn + betaOut);
         pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
     } else if (lIn < 11 && (double)fabsf(betaOut) < 0.2 * (double)fabsf(betaIn) && fabsf(pt_beta) < 12.f * pt_betaMax) {
         const float pt_betaIn = pt_from(dr * k2Rinv1GeVf, betaIn);
-        const float betaInUpd = betaIn + copysignf(g_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), betaIn);
-        const float betaOutUpd = betaOut + copysignf(g_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), betaIn);
+        const float betaInUpd = betaIn + copysignf(lm_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax), host), betaIn);
+        const float betaOutUpd = betaOut + copysignf(lm_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax), host), betaIn);
         betaAv = (fabsf(betaOut) > 0.2f * fabsf(betaIn)) ? (0.5f * (betaInUpd + betaOutUpd)) : betaInUpd;
         pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
-        betaIn = betaIn + copysignf(g_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
-        betaOut = betaOut + copysignf(g_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
+        betaIn = betaIn + copysignf(lm_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax), host), betaIn);
+        betaOut = betaOut + copysignf(lm_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax), host), betaIn);
         betaAv = 0.5f * (betaIn + betaOut);
         pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
     }
@@ -1334,9 +1392,12 @@ enum : int {
 
 // rec (optional, kTLVarN floats): the final cut variables of a candidate
 // that reaches the deltaBeta cut
+// host: the host libm's float asin and sin (the reference's), else the
+// correctly rounded ones; close (with host false): set when a final cut is
+// too close to call with the correctly rounded values (see tl_phaseB2)
 template <int kSet>
 __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV& T, float mulsF, bool nm1,
-                                               float* rec = nullptr) {
+                                               float* rec = nullptr, bool host = true, bool* close = nullptr) {
     if (kSet == kB2BBBB) algo = kAlgoBBBB;
     if (kSet == kB2Others && algo == kAlgoBBBB) return false;
     const float pt_betaMax = 7.0f;
@@ -1363,7 +1424,8 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
             const P3 loE = edge_point(OutUp.x, OutUp.y, OutUp.z, T.ex, T.ey, false);
             betaOutRHmin = -dphi(hiE, sub(hiE, OutLo)) + dphi(hiE, sub(hiE, InLo));
             betaOutRHmax = -dphi(loE, sub(loE, OutLo)) + dphi(loE, sub(loE, InLo));
-            const float sinDPhi = g_sin(dphi(midpoint(InLo, OutLo), sub(OutLo, InLo)));
+            const float dPhi = dphi(midpoint(InLo, OutLo), sub(OutLo, InLo));
+            const float sinDPhi = host ? g_sin(dPhi) : f_sin(dPhi);
             const float rr = (hiE.rt - loE.rt) * sinDPhi / dr;
             dBetaROut2 = rr * rr;  // the double square of a float is exact: one rounding to float
         } else {
@@ -1388,7 +1450,8 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
         betaOutRHmax = betaOut - sdOut_alphaOut_max + sdOut_alphaOut;
         if (fabsf(betaOutRHmin) > fabsf(betaOutRHmax)) { const float t = betaOutRHmin; betaOutRHmin = betaOutRHmax; betaOutRHmax = t; }
         if (T.flags & F_UP_2S) {
-            const float sinDPhi = g_sin(dphi(midpoint(InLo, OutLo), sub(OutLo, InLo)));
+            const float dPhi = dphi(midpoint(InLo, OutLo), sub(OutLo, InLo));
+            const float sinDPhi = host ? g_sin(dPhi) : f_sin(dPhi);
             const float hrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, true);
             const float lrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, false);
             const float rr = (hrt - lrt) * sinDPhi / dr;
@@ -1420,7 +1483,7 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
     }
     float betaAv = 0.5f * (betaIn + betaOut);
     float pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
-    delta_beta_iterations(betaIn, betaOut, betaAv, pt_beta, sdIn_dr, sdOut_dr, dr, lIn, pt_betaMax);
+    delta_beta_iterations(betaIn, betaOut, betaAv, pt_beta, sdIn_dr, sdOut_dr, dr, lIn, pt_betaMax, host);
     const float betaInMMSF = (fabsf(betaInRHmin + betaInRHmax) > 0) ? (2.f * betaIn / fabsf(betaInRHmin + betaInRHmax)) : 0.f;
     const float betaOutMMSF = (fabsf(betaOutRHmin + betaOutRHmax) > 0) ? (2.f * betaOut / fabsf(betaOutRHmin + betaOutRHmax)) : 0.f;
     betaInRHmin *= betaInMMSF; betaInRHmax *= betaInMMSF;
@@ -1431,8 +1494,12 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
     const float dBetaInLum = lIn < 11 ? 0.0f : fabsf(alphaInAbsReg * kDeltaZLum / InLo.z);
     const float dBetaOutLum = lOut < 11 ? 0.0f : fabsf(alphaOutAbsReg * kDeltaZLum / OutLo.z);
     const float dBetaLum2 = (dBetaInLum + dBetaOutLum) * (dBetaInLum + dBetaOutLum);
-    const float betaOut_cut = add_dsqrt(g_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d),
+    const float betaOut_cut = add_dsqrt(lm_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax), host) + (0.02f / sdOut_d),
                                         dBetaLum2 + dBetaMuls * dBetaMuls);
+    if (close && fabsf(fabsf(betaOut) - betaOut_cut) <= (fabsf(betaOut) + betaOut_cut) * 0x1p-12f) {
+        *close = true;
+        return false;
+    }
     if (!(fabsf(betaOut) < betaOut_cut)) return false;
     const float dBetaRes = 0.02f / fmin_ref(sdOut_d, sdIn_d);
     const float dBetaCut2 = dbeta_cut2(dBetaRes, dBetaMuls, dBetaLum2, dBetaROut2, betaInRHmin, betaInRHmax, betaOutRHmin, betaOutRHmax);
@@ -1444,12 +1511,29 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
         rec[kTLVarDBetaCut2] = dBetaCut2; rec[kTLVarDBetaLum2] = dBetaLum2; rec[kTLVarDBetaMuls] = dBetaMuls;
         rec[kTLVarDBetaRes] = dBetaRes; rec[kTLVarDBetaRIn2] = 0.f; rec[kTLVarDBetaROut2] = dBetaROut2;
     }
+    if (close && !nm1) {
+        const float sc = fabsf(betaIn) + fabsf(betaOut);
+        if (fabsf(dBeta * dBeta - dBetaCut2) <= (dBetaCut2 + sc * sc) * 0x1p-12f) {
+            *close = true;
+            return false;
+        }
+    }
     return (dBeta * dBeta <= dBetaCut2) || nm1;
 }
+// Phase B2 is evaluated with the correctly rounded float asin and sin first.
+// The host libm's (the reference's) are within one float step of them; through
+// the deltaBeta iterations (sums of same-signed angles, pT from a sine,
+// asin arguments scaled by it, condition numbers below 3) every quantity the
+// final cuts compare moves by less than 2^-18 of the magnitudes involved, so
+// a comparison decided by more than 2^-12 of them is the host's decision as
+// well; the rare closer ones are evaluated again with the host libm.
 template <int kSet>
 static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict__ pack, int s, int t, float mulsF,
                                                 bool nm1) {
-    return tl_phaseB2_sgv<kSet>(algo, load_sgv(pack, s), load_sgv(pack, t), mulsF, nm1);
+    const SGV S = load_sgv(pack, s), T = load_sgv(pack, t);
+    bool close = false;
+    const bool pass = tl_phaseB2_sgv<kSet>(algo, S, T, mulsF, nm1, nullptr, false, &close);
+    return close ? tl_phaseB2_sgv<kSet>(algo, S, T, mulsF, nm1, nullptr, true) : pass;
 }
 
 // phase B in one call (phase B1, then phase B2 on its survivors)
