@@ -204,6 +204,16 @@ def headline_plan(rank, n):
     return [(base + 500 + k, float(p)) for k, p in enumerate(headline_pus(rank, n))]
 
 
+def dense_plan(rank, n):
+    """(seed, PU) of the stated-density batch of a rank: PU uniform in
+    227-474, which gives 110k-230k hits per event with this generator (about
+    485 hits per PU unit), the hit counts the 128-event configuration states"""
+    import numpy as np
+    base = 1000 + 997 * rank
+    pus = np.random.default_rng(4343 + rank).uniform(227.0, 474.0, size=n)
+    return [(base + 300 + k, float(p)) for k, p in enumerate(pus)]
+
+
 def single_plan(rank, n):
     """(seed, PU) of the single-event workload of a rank"""
     base = 1000 + 997 * rank
@@ -337,6 +347,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--batch-events", type=int, default=128)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-dense", action="store_true", help="skip the stated-density batch")
     ap.add_argument("--plain-only", action="store_true",
                     help="time only the plain batched chain (a short run to profile its kernels)")
     ap.add_argument("--mlp-only", action="store_true",
@@ -354,6 +365,7 @@ def main():
     # ---- inputs (generated before any CUDA call) ----------------------------
     batch = make_events(headline_plan(rank, a.batch_events), threads)
     single = make_events(single_plan(rank, 4), threads)
+    dense_batch = [] if (a.no_dense or a.plain_only or a.mlp_only) else make_events(dense_plan(rank, a.batch_events), threads)
     # the CPU baseline runs the restatement on the whole batch (about 30 s on
     # 16 cores) and doubles as the parity check of the plain batched chain on
     # every event; with fewer than 8 host threads, on every 8th event
@@ -453,6 +465,42 @@ def main():
                            "unit": "events/s", "ms_per_step": round(v_mean, 3),
                            "objects_per_step": [int(v) for v in ch.counts(-1)],
                            "stage_ms": [round(float(v), 3) for v in np.mean(np.array(v_stage), axis=0)]}
+
+    # ---- the stated density: 110k-230k hits per event --------------------------
+    # (the headline batch's PU 150-300 gives 73k-146k with this generator);
+    # pre-filtered and plain chain on the same events, exact recall
+    dense = None
+    if dense_batch:
+        nd = len(dense_batch)
+        ch.set_events(dense_batch)
+        for _ in range(2):
+            ch.run(4, FLAG_MLP)
+        dm_ms, dm_stage, _, _ = timed_runs(ch, FLAG_MLP, max(3, a.steps // 4), flush)
+        d_pruned = ch.counts(-1)
+        d_mstats = ch.mlp_stats()
+        d_pr = tuples.split_by_event(ch.objects(4, -1), [int(ch.counts(e)[4]) for e in range(nd)])
+        for _ in range(2):
+            ch.run(4, 0)
+        dp_ms, dp_stage, _, _ = timed_runs(ch, 0, max(3, a.steps // 4), flush)
+        d_plain = ch.counts(-1)
+        d_pl = tuples.split_by_event(ch.objects(4, -1), [int(ch.counts(e)[4]) for e in range(nd)])
+        d_common = sum(tuples.multiset_intersection(p, q) for p, q in zip(d_pr, d_pl))
+        del d_pr, d_pl
+        hits = [len(e) for e in dense_batch]
+        dm_mean = allmax(pg, statistics.fmean(dm_ms))
+        dp_mean = allmax(pg, statistics.fmean(dp_ms))
+        dense = {"workload": "%d events, PU uniform in 227-474 (%d-%d hits per event, mean %.0f)"
+                             % (nd, min(hits), max(hits), statistics.fmean(hits)),
+                 "hits_per_step": int(sum(hits)),
+                 "value": round(allsum(pg, nd) * 1e3 / dm_mean, 3), "unit": "events/s", "ms_per_step": round(dm_mean, 3),
+                 "plain_value": round(allsum(pg, nd) * 1e3 / dp_mean, 3), "plain_ms_per_step": round(dp_mean, 3),
+                 "tc_recall": round(d_common / max(1.0, float(d_plain[4])), 5),
+                 "tl_recall": round(float(d_pruned[2]) / max(1.0, float(d_plain[2])), 5),
+                 "tc_outside_plain": int(d_pruned[4]) - d_common,
+                 "objects_per_step": [int(v) for v in d_pruned], "plain_objects_per_step": [int(v) for v in d_plain],
+                 "prefilter": {k: d_mstats[k] for k in ("candidates", "scored", "kept")},
+                 "stage_ms": {k: round(float(v), 3) for k, v in zip(STAGE_NAMES, np.mean(np.array(dm_stage), axis=0))},
+                 "plain_stage_ms": {k: round(float(v), 3) for k, v in zip(STAGE_NAMES, np.mean(np.array(dp_stage), axis=0))}}
 
     # ---- end to end through the C ABI: pinned host buffers in, track
     # candidates out, for the whole batch each step -----------------------------
@@ -602,6 +650,7 @@ def main():
             "recall_method": "track candidates: |pruned & plain| / |plain| over the hit-index tuple multisets, event "
                              "by event; tracklets: count ratio (pruned tracklets are a subset by construction)",
             "plain_batched": plain_batched, "plain_single": plain_single, "variants": variants,
+            "stated_density": dense,
             "e2e": {"value": round(e2e_value, 3), "unit": "events/s", "ms_per_step": round(e2e_mean, 3),
                     "h2d_bytes_per_step": n_hit * 20 + 8 * (len(batch) + 1), "d2h_bytes_per_step": int(statistics.fmean(d2h)),
                     "path": "sdlg_set_events (pinned host) + sdlg_run(SDLG_FLAG_MLP) + sdlg_get_objects(TC, into pinned host memory)"},

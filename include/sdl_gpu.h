@@ -63,6 +63,10 @@ extern "C" {
 #define SDLG_FLAG_TC_FROM_TP 128 /* track candidates from two triplets and a trial segment between them:
                                     Event::createTrackCandidatesFromTriplets (Event.cc:874-982); the objects
                                     of stage 4 are then pairs of triplets (hit tuples of width 16 as before) */
+#define SDLG_FLAG_TEST_MLP_GIVE_UP 4096 /* self-test of a failure path (no counterpart in the reference): with
+                                    SDLG_FLAG_MLP, the pre-filter's first tensor-core wait in each CTA gives up at
+                                    once, as a wait that ran out of time would; the run fails with SDLG_ERR_CUDA,
+                                    sdlg_mlp_stats counts the waits that gave up, the context stays usable */
 
 typedef struct sdlg_ctx sdlg_ctx;
 
@@ -98,6 +102,47 @@ int sdlg_geometry_upload(sdlg_ctx* ctx, int64_t n_tilted, const uint32_t* t_deti
  * in key order.  Rows are in detid order. */
 int sdlg_geometry_convert(const char* tilted_path, const char* endcap_path, const char* map_path, const char* out_path);
 int sdlg_geometry_load_binary(sdlg_ctx* ctx, const char* path);
+
+/* Starting object capacities (no counterpart in the reference): caps6 =
+ * mini-doublets, segments, tracklets, triplets, track candidates, and
+ * tracklet candidates through the enumeration's cuts; 0 = the default (a
+ * multiple of the batch's hit count).  Capacities grow by themselves when a
+ * run overflows them (the run is repeated), so small values only cost time;
+ * they exist to exercise that path.  Frees the batch buffers: call
+ * sdlg_set_events next.  sdlg_get_capacities: the current ones. */
+int sdlg_set_capacities(sdlg_ctx* ctx, const int64_t* caps6);
+int sdlg_get_capacities(const sdlg_ctx* ctx, int64_t* out6);
+
+/* Straight-line module connection map on the GPU (no counterpart in the
+ * reference, which reads its map from a text file, ModuleConnectionMap.cc:
+ * 18-47; this builds one for a detector of barrel cylinders with modules
+ * tiled in phi and z -- layers 1-3 tilted beyond |z| = flat_zmax_tilted when
+ * has_tilt -- and endcap disks of rings tiled in phi, the detId layout of
+ * Module.cc:159-358).  For every lower module, straight lines from five
+ * vertex positions z0 in [-lum_z, lum_z] through a 3 x 3 grid of its points
+ * (0 and +-98 % of its half extents) are extended to the next barrel layer,
+ * or the first disk when they leave the barrel, or the next disk; each
+ * crossing, also turned by +- the bend of a track of radius radius_1gev
+ * between the two radii, connects the lower module that covers it.  Inputs:
+ * n lower modules with detid, kind (0 flat barrel, 1 tilted barrel, 2
+ * endcap) and 16 doubles of geometry each (centre xyz, in-plane tangential
+ * axis xyz, in-plane long axis xyz, half width, half length, ring inner and
+ * outer radius, centre phi, half phi width, tilt angle).  Output: the map as
+ * CSR in detId order (keys[n_keys], off[n_keys + 1], dst[n_dst], the
+ * connected detIds of each key sorted), the sdlg_geometry_upload layout;
+ * all NULL: a size query.  Runs on CUDA device `device`; needs no context. */
+typedef struct sdlg_line_map_layout {
+    double barrel_r[6];
+    int32_t barrel_nphi[6];
+    double zmax, module_dz, flat_zmax_tilted, lum_z, radius_1gev;
+    int32_t n_tilt_rings, has_tilt, has_endcap;
+    double disk_z[5];
+    int32_t disk_nrings[5];
+    double ec_rmin, ec_rmax;
+} sdlg_line_map_layout;
+int sdlg_build_line_map(int device, const sdlg_line_map_layout* layout, int64_t n, const uint32_t* detid,
+                        const int8_t* kind, const double* geom, int64_t cap_keys, int64_t cap_dst, uint32_t* keys,
+                        int64_t* off, uint32_t* dst, int64_t* n_keys, int64_t* n_dst);
 
 /* Number of modules in the device module table. */
 int64_t sdlg_num_modules(const sdlg_ctx* ctx);
@@ -261,13 +306,15 @@ int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64
 int sdlg_libm_eval(sdlg_ctx* ctx, int fn, uint32_t start_bits, int64_t n, float* out);
 int sdlg_libm_stats(int fn, uint64_t* out3);
 
-/* Self-check of the tracklet enumeration's single-precision decisions (no
- * counterpart in the reference): after a run through the tracklet stage,
- * every tracklet candidate of the batch is judged both by the fast decisions
- * (the float cuts, then for their survivors the first part of the tracklet
- * cuts) and by the exact cuts.  out4: candidates, candidates the fast
- * decisions settled alone, candidates that needed an exact evaluation, and
- * candidates settled differently from the exact cuts (must be 0). */
+/* Self-check of the tracklet stage's fast decisions (no counterpart in the
+ * reference): after a run through the tracklet stage, every tracklet
+ * candidate of the batch is judged both by the fast decisions (the float
+ * cuts, then for their survivors the first part of the tracklet cuts; for
+ * the candidates through those, the final cuts evaluated with correctly
+ * rounded float asin and sin and decided by margin) and by the exact cuts
+ * (with the host libm's float functions).  out4: candidates, candidates the
+ * fast decisions settled alone, candidates that needed an exact evaluation,
+ * and candidates settled differently from the exact cuts (must be 0). */
 int sdlg_tl_phase_a_check(sdlg_ctx* ctx, uint64_t* out4);
 
 /* Number of kernels one run of the chain launches (as last enqueued). */

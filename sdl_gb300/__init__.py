@@ -35,6 +35,7 @@ FLAG_MLP = 16        # learned pre-filter ahead of the tracklet cuts
 FLAG_TL_NAV = 32     # Event::createTrackletsViaNavigation instead of createTrackletsWithModuleMap
 FLAG_TC_FROM_TL = 64   # Event::createTrackCandidatesFromTracklets instead of createTrackCandidates
 FLAG_TC_FROM_TP = 128  # Event::createTrackCandidatesFromTriplets instead of createTrackCandidates
+FLAG_TEST_MLP_GIVE_UP = 4096  # self-test: the pre-filter's first tensor-core wait gives up at once
 # the columns of Chain.tracklet_vars (the reference's Tracklet recovars keys)
 TL_VAR_NAMES = ("betaIn", "betaInRHmin", "betaInRHmax", "betaOut", "betaOutRHmin", "betaOutRHmax", "betaAv", "pt_beta",
                 "dBeta", "dBetaCut2", "dBetaLum2", "dBetaMuls", "dBetaRes", "dBetaRIn2", "dBetaROut2")
@@ -85,6 +86,9 @@ def lib():
         L.sdlg_last_launches.restype = i64
         L.sdlg_mini_doublets_static.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, i64, vp, vp, vp]
         L.sdlg_run_stages.argtypes = [vp, i32, i32, i32]
+        L.sdlg_set_capacities.argtypes = [vp, vp]
+        L.sdlg_build_line_map.argtypes = [i32, vp, i64, vp, vp, vp, i64, i64, vp, vp, vp, vp, vp]
+        L.sdlg_get_capacities.argtypes = [vp, vp]
         L.sdlg_get_object_links.argtypes = [vp, i32, i64, vp, vp, vp, i64, vp]
         L.sdlg_get_module_detids.argtypes = [vp, vp, i64, vp]
         L.sdlg_module_info.argtypes = [ctypes.c_uint32, vp]
@@ -130,6 +134,54 @@ def hit_derived(x, y, z):
     if rc != 0:
         raise SDLError("%d: sdlg_hit_derived" % rc)
     return tuple(out)
+
+
+class LineMapLayout(ctypes.Structure):
+    """sdlg_line_map_layout of include/sdl_gpu.h"""
+    _fields_ = [("barrel_r", ctypes.c_double * 6), ("barrel_nphi", ctypes.c_int32 * 6), ("zmax", ctypes.c_double),
+                ("module_dz", ctypes.c_double), ("flat_zmax_tilted", ctypes.c_double), ("lum_z", ctypes.c_double),
+                ("radius_1gev", ctypes.c_double), ("n_tilt_rings", ctypes.c_int32), ("has_tilt", ctypes.c_int32),
+                ("has_endcap", ctypes.c_int32), ("disk_z", ctypes.c_double * 5), ("disk_nrings", ctypes.c_int32 * 5),
+                ("ec_rmin", ctypes.c_double), ("ec_rmax", ctypes.c_double)]
+
+
+def line_map(det, device: int = 0) -> dict:
+    """The straight-line module connection map of a synthetic detector
+    (sdl_gb300.synth), built on the GPU (sdlg_build_line_map): lower detId ->
+    sorted list of the connected lower detIds."""
+    from . import synth
+    lay = LineMapLayout()
+    for i in range(6):
+        lay.barrel_r[i] = synth.BARREL_R[i]
+        lay.barrel_nphi[i] = det.n_phi(i + 1)
+    lay.zmax, lay.module_dz, lay.flat_zmax_tilted = synth.ZMAX, synth.MOD_DZ, synth.FLAT_ZMAX_TILTED
+    lay.lum_z, lay.radius_1gev = synth.LUM_Z, 1.0 / synth.KR
+    lay.n_tilt_rings, lay.has_tilt, lay.has_endcap = synth.N_TILT_RINGS, int(det.has_tilt), int(det.has_endcap)
+    for i in range(5):
+        lay.disk_z[i] = synth.DISK_Z[i]
+        lay.disk_nrings[i] = synth.DISK_NRINGS[i]
+    lay.ec_rmin, lay.ec_rmax = synth.EC_RMIN, synth.EC_RMAX
+    idx = np.nonzero(det.is_inner)[0]
+    detid = np.ascontiguousarray(det.detid[idx], dtype=np.uint32)
+    kind = np.ascontiguousarray(det.kind[idx], dtype=np.int8)
+    geom = np.ascontiguousarray(np.concatenate(
+        [det.center[idx], det.taxis[idx], det.uaxis[idx]] +
+        [getattr(det, k)[idx][:, None] for k in ("half_t", "half_z", "r0", "r1", "phic", "dphi", "tilt")], axis=1),
+        dtype=np.float64)
+    nk, nd = ctypes.c_int64(), ctypes.c_int64()
+    L = lib()
+    args = (device, ctypes.byref(lay), len(idx), detid.ctypes.data, kind.ctypes.data, geom.ctypes.data)
+    rc = L.sdlg_build_line_map(*args, 0, 0, None, None, None, ctypes.byref(nk), ctypes.byref(nd))
+    if rc != 0:
+        raise SDLError("%d: sdlg_build_line_map" % rc)
+    keys = np.empty(nk.value, np.uint32)
+    off = np.empty(nk.value + 1, np.int64)
+    dst = np.empty(nd.value, np.uint32)
+    rc = L.sdlg_build_line_map(*args, nk.value, nd.value, keys.ctypes.data, off.ctypes.data, dst.ctypes.data,
+                               ctypes.byref(nk), ctypes.byref(nd))
+    if rc != 0:
+        raise SDLError("%d: sdlg_build_line_map" % rc)
+    return {int(k): [int(v) for v in dst[off[i]:off[i + 1]]] for i, k in enumerate(keys)}
 
 
 def geometry_convert(tilted, endcap, cmap, out_path):
@@ -229,6 +281,19 @@ class Chain:
     # running ----------------------------------------------------------------
     def run(self, stop_after: int = 4, flags: int = 0):
         self._ck(lib().sdlg_run(self.h, stop_after, flags))
+
+    def set_capacities(self, caps):
+        """Starting capacities (MD, SG, TL, TP, TC, pre-filter list; 0 = default);
+        frees the batch: call set_events next."""
+        c = np.ascontiguousarray(caps, dtype=np.int64)
+        if c.size != 6:
+            raise ValueError("six capacities")
+        self._ck(lib().sdlg_set_capacities(self.h, c.ctypes.data))
+
+    def capacities(self) -> np.ndarray:
+        out = np.zeros(6, dtype=np.int64)
+        self._ck(lib().sdlg_get_capacities(self.h, out.ctypes.data))
+        return out
 
     def run_stages(self, first: int, last: int, flags: int = 0):
         """Stages first..last (one create* call at a time): continues the last

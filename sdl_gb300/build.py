@@ -9,7 +9,7 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libsdlgpu.so")
-SOURCES = ("sdl_kernels.cu", "sdl_capi.cu", "sdl_static.cu", "sdl_mlp.cu", "sdl_libm.cu")
+SOURCES = ("sdl_kernels.cu", "sdl_capi.cu", "sdl_static.cu", "sdl_mlp.cu", "sdl_libm.cu", "sdl_map.cu")
 # -fmad=false (device) and -ffp-contract=off (host): no multiply-add
 # contraction, the cut arithmetic must round like the reference CPU build;
 # IEEE division and square root are nvcc's defaults.

@@ -133,6 +133,7 @@ struct sdlg_ctx {
     int64_t cap_hit = 0, cap_ev = 0;
     int64_t cap_obj[kNumStages] = {0, 0, 0, 0, 0};
     int64_t cap_kept = 0;  // tracklet candidates the pre-filter may keep per run
+    int64_t cap_init[kNumStages + 1] = {0, 0, 0, 0, 0, 0};  // starting capacities (0: from the hit count)
     int tune_task[kNumStages] = {0, 0, 0, 0, 0};  // tuned launch shapes (0: default)
     int tune_grid[kNumStages] = {0, 0, 0, 0, 0};
     bool buffers_ok = false;
@@ -300,8 +301,9 @@ int ensure_buffers(sdlg_ctx* ctx) {
     ctx->cap_ev = ctx->n_ev;
     const int64_t H = std::max<int64_t>(ctx->cap_hit, 1024);
     const int64_t mult[kNumStages] = {1, 2, 3, 4, 2};
-    for (int s = 0; s < kNumStages; ++s) ctx->cap_obj[s] = std::max<int64_t>(ctx->cap_obj[s], H * mult[s] + 4096);
-    ctx->cap_kept = std::max<int64_t>(ctx->cap_kept, 8 * H + 4096);
+    for (int s = 0; s < kNumStages; ++s)
+        ctx->cap_obj[s] = std::max<int64_t>(ctx->cap_obj[s], ctx->cap_init[s] > 0 ? ctx->cap_init[s] : H * mult[s] + 4096);
+    ctx->cap_kept = std::max<int64_t>(ctx->cap_kept, ctx->cap_init[kNumStages] > 0 ? ctx->cap_init[kNumStages] : 8 * H + 4096);
     BatchDev& b = ctx->b;
     b = BatchDev{};
     b.geo.n_mod = n_mod;
@@ -453,8 +455,17 @@ void enqueue_stages(sdlg_ctx* ctx, int first, int last) {
     cudaMemsetAsync(b.dbg, 0, 8 * sizeof(unsigned long long), s);
     cudaMemsetAsync(b.n_rec + first, 0, ns * sizeof(int64_t), s);
     cudaMemsetAsync(b.task + first, 0, ns * sizeof(unsigned long long), s);
-    // the counters of these stages only: 22 per stage in each event's 110
-    cudaMemset2DAsync(b.counters + first * 22, 110 * sizeof(uint32_t), 0, ns * 22 * sizeof(uint32_t), b.n_ev, s);
+    // the counters these stages write (22 per stage in each event's 110:
+    // candidates, then objects): the triplet candidates are counted by the
+    // tracklet stage (Event.cc:547-596 loops over the segment lists)
+    auto zero_counters = [&](int at, int n) {
+        cudaMemset2DAsync(b.counters + at, 110 * sizeof(uint32_t), 0, n * sizeof(uint32_t), b.n_ev, s);
+    };
+    for (int st = first; st <= last; ++st) {
+        if (st == kTP) zero_counters(kTP * 22 + 11, 11);
+        else zero_counters(st * 22, 22);
+    }
+    if (first <= kTL && last >= kTL) zero_counters(kTP * 22, 11);
     for (int st = first; st <= last; ++st) cudaMemsetAsync(b.obj[st].mod_cnt, 0, (n_gm + 1) * sizeof(int64_t), s);
     if (first <= kTL && last >= kTL) cudaMemsetAsync(b.mlp_stats, 0, sizeof(MlpStats), s);
     Hooks* h = &ctx->hooks;
@@ -551,7 +562,7 @@ int launch(sdlg_ctx* ctx, int stop_after, int flags) {
 
 // wait for a run; grow overflowing capacities and re-run until clean
 int finish(sdlg_ctx* ctx) {
-    for (int attempt = 0; attempt < 8; ++attempt) {
+    for (int attempt = 0; attempt < 16; ++attempt) {  // one overflowing stage per attempt at worst
         CK(cudaStreamSynchronize(ctx->stream));
         const uint32_t status = (uint32_t)(ctx->h_small[kNumStages] & 0xffffffffu);
         if (status & kStatusUnknownModule) {
@@ -970,6 +981,31 @@ int sdlg_run(sdlg_ctx* ctx, int stop_after, int flags) {
     int rc = sdlg_run_async(ctx, stop_after, flags);
     if (rc) return rc;
     return sdlg_sync(ctx);
+}
+
+int sdlg_set_capacities(sdlg_ctx* ctx, const int64_t* caps6) {
+    if (!ctx || !caps6) return SDLG_ERR_ARG;
+    for (int k = 0; k <= kNumStages; ++k)
+        if (caps6[k] < 0) return fail(ctx, SDLG_ERR_ARG, "negative capacity");
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    free_batch(ctx);
+    for (int k = 0; k < kNumStages; ++k) {
+        ctx->cap_init[k] = caps6[k];
+        ctx->cap_obj[k] = caps6[k];
+    }
+    ctx->cap_init[kNumStages] = caps6[kNumStages];
+    ctx->cap_kept = caps6[kNumStages];
+    ctx->n_ev = 0;
+    ctx->ran = false;
+    return SDLG_OK;
+}
+
+int sdlg_get_capacities(const sdlg_ctx* ctx, int64_t* out6) {
+    if (!ctx || !out6) return SDLG_ERR_ARG;
+    for (int k = 0; k < kNumStages; ++k) out6[k] = ctx->cap_obj[k];
+    out6[kNumStages] = ctx->cap_kept;
+    return SDLG_OK;
 }
 
 int sdlg_run_stages(sdlg_ctx* ctx, int first, int last, int flags) {

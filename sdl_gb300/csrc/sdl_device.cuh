@@ -656,6 +656,14 @@ __device__ __forceinline__ void dalpha_threshold(const MDView& im, const MDView&
 // move t across v
 __device__ __forceinline__ bool near_cut(float v, float t, float rel) { return fabsf(v - t) <= fabsf(t) * rel; }
 
+// the three dAlpha cuts with the host libm's asin (the reference's)
+static __device__ __noinline__ bool dalpha_cuts_host(const MDView& im, const MDView& om, float sg_alpha) {
+    float th[3];
+    dalpha_threshold(im, om, th, true);
+    if (!(fabsf(im.dphichange - sg_alpha) < th[0])) return false;
+    if (!(fabsf(om.dphichange - sg_alpha) < th[1])) return false;
+    return fabsf(om.dphichange - im.dphichange) < th[2];
+}
 // The three dAlpha cuts are decided with the correctly rounded asin first.
 // The host libm's asin is within one float step of it (dAlpha_Bfield >= 0);
 // each threshold, dAlpha_Bfield + a square root (with dAlpha_Bfield inside it
@@ -664,19 +672,17 @@ __device__ __forceinline__ bool near_cut(float v, float t, float rel) { return f
 // from its threshold is therefore the host's decision too, and the rare
 // closer ones are decided again with the host libm's asin.
 __device__ __forceinline__ bool dalpha_cuts(const MDView& im, const MDView& om, float sg_alpha) {
+    constexpr float rel = 0x1p-19f;
     float th[3];
     dalpha_threshold(im, om, th, false);
-    const float v0 = fabsf(im.dphichange - sg_alpha), v1 = fabsf(om.dphichange - sg_alpha);
-    const float v2 = fabsf(om.dphichange - im.dphichange);
-    const float rel = 0x1p-19f;
-    bool close = near_cut(v0, th[0], rel);
-    if (v0 < th[0]) {
-        close |= near_cut(v1, th[1], rel);
-        if (v1 < th[1]) close |= near_cut(v2, th[2], rel);
-    }
-    if (close) dalpha_threshold(im, om, th, true);
+    const float v0 = fabsf(im.dphichange - sg_alpha);
+    if (near_cut(v0, th[0], rel)) return dalpha_cuts_host(im, om, sg_alpha);
     if (!(v0 < th[0])) return false;
+    const float v1 = fabsf(om.dphichange - sg_alpha);
+    if (near_cut(v1, th[1], rel)) return dalpha_cuts_host(im, om, sg_alpha);
     if (!(v1 < th[1])) return false;
+    const float v2 = fabsf(om.dphichange - im.dphichange);
+    if (near_cut(v2, th[2], rel)) return dalpha_cuts_host(im, om, sg_alpha);
     return v2 < th[2];
 }
 
@@ -1496,7 +1502,8 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
     const float dBetaLum2 = (dBetaInLum + dBetaOutLum) * (dBetaInLum + dBetaOutLum);
     const float betaOut_cut = add_dsqrt(lm_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax), host) + (0.02f / sdOut_d),
                                         dBetaLum2 + dBetaMuls * dBetaMuls);
-    if (close && fabsf(fabsf(betaOut) - betaOut_cut) <= (fabsf(betaOut) + betaOut_cut) * 0x1p-12f) {
+    const float sc = fabsf(betaIn) + fabsf(betaOut);
+    if (close && fabsf(fabsf(betaOut) - betaOut_cut) <= (sc + betaOut_cut) * 0x1p-10f) {
         *close = true;
         return false;
     }
@@ -1511,29 +1518,40 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
         rec[kTLVarDBetaCut2] = dBetaCut2; rec[kTLVarDBetaLum2] = dBetaLum2; rec[kTLVarDBetaMuls] = dBetaMuls;
         rec[kTLVarDBetaRes] = dBetaRes; rec[kTLVarDBetaRIn2] = 0.f; rec[kTLVarDBetaROut2] = dBetaROut2;
     }
-    if (close && !nm1) {
-        const float sc = fabsf(betaIn) + fabsf(betaOut);
-        if (fabsf(dBeta * dBeta - dBetaCut2) <= (dBetaCut2 + sc * sc) * 0x1p-12f) {
-            *close = true;
-            return false;
-        }
+    const float rh = fabsf(betaInRHmin - betaInRHmax) + fabsf(betaOutRHmin - betaOutRHmax);
+    if (close && !nm1 &&
+        fabsf(dBeta * dBeta - dBetaCut2) <=
+            dBetaCut2 * 0x1p-9f + (fabsf(dBeta) + rh) * sc * 0x1p-10f + sc * sc * 0x1p-20f) {
+        *close = true;
+        return false;
     }
     return (dBeta * dBeta <= dBetaCut2) || nm1;
 }
 // Phase B2 is evaluated with the correctly rounded float asin and sin first.
-// The host libm's (the reference's) are within one float step of them; through
-// the deltaBeta iterations (sums of same-signed angles, pT from a sine,
-// asin arguments scaled by it, condition numbers below 3) every quantity the
-// final cuts compare moves by less than 2^-18 of the magnitudes involved, so
-// a comparison decided by more than 2^-12 of them is the host's decision as
-// well; the rare closer ones are evaluated again with the host libm.
+// The host libm's (the reference's) are within one float step of them.
+// Through the deltaBeta iterations (angles added to angles of the same sign,
+// pT from a sine of their mean, asin arguments scaled by it, asin condition
+// numbers below 2.4 for arguments up to 0.95) betaIn and betaOut move by at
+// most 2^-15 of sc = |betaIn| + |betaOut| (a betaOut that the iteration
+// cancels towards zero included: its asin term is below 3 |betaIn|), pT and
+// the multiple-scattering term by 2^-14 of themselves, so betaOut_cut by
+// 2^-13 and dBetaCut2 by 2^-12 of themselves (and the spread of the scaled
+// RH bounds by 2^-14 sc), dBeta by 2^-14 sc.  A final comparison decided by
+// more than the margins above (at least four times those bounds) is the
+// host's decision as well; the rare closer ones are evaluated again with the
+// host libm.  sdlg_tl_phase_a_check evaluates both on every candidate through
+// phase B1 and counts the decisions that differ.
+template <int kSet>
+static __device__ __noinline__ bool tl_phaseB2_host(int algo, const SGV& S, const SGV& T, float mulsF, bool nm1) {
+    return tl_phaseB2_sgv<kSet>(algo, S, T, mulsF, nm1, nullptr, true);
+}
 template <int kSet>
 static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict__ pack, int s, int t, float mulsF,
                                                 bool nm1) {
     const SGV S = load_sgv(pack, s), T = load_sgv(pack, t);
     bool close = false;
     const bool pass = tl_phaseB2_sgv<kSet>(algo, S, T, mulsF, nm1, nullptr, false, &close);
-    return close ? tl_phaseB2_sgv<kSet>(algo, S, T, mulsF, nm1, nullptr, true) : pass;
+    return close ? tl_phaseB2_host<kSet>(algo, S, T, mulsF, nm1) : pass;
 }
 
 // phase B in one call (phase B1, then phase B2 on its survivors)

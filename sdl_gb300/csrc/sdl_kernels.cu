@@ -1349,6 +1349,7 @@ __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
     mlp_setup(sm, b.mlp_pack);
     const float thr = reinterpret_cast<const float*>(sm.w + kPackB3)[1];
     MlpThread st;
+    if (b.flags & kFlagTestMlpGiveUp) st.polls = 0;
     unsigned n_scored = 0, n_kept = 0;
     // entry t * 128 + threadIdx.x of tile t and its features
     auto load = [&](int64_t t, PfPending& p, float* f) -> bool {
@@ -1593,7 +1594,16 @@ __global__ void k_tl_quick_check(BatchDev b, unsigned long long* out) {
         float cut, muls;
         const int e = tl_phaseA(S, Tv, cut, muls);
         const bool eb1 = e != kAlgoNone && tl_phaseB1_sgv(e, S, Tv, cut);
-        const bool bad = q == kAlgoNone ? eb1 : (q != e || (b1 && !eb1));
+        bool bad = q == kAlgoNone ? eb1 : (q != e || (b1 && !eb1));
+        if (eb1) {
+            // the final cuts: correctly rounded values with margins against the host libm's
+            const bool nm1 = (b.flags & kFlagTLNm1) != 0;
+            bool close = false;
+            const bool cr = tl_phaseB2_sgv<kB2All>(e, S, Tv, muls, nm1, nullptr, false, &close);
+            const bool host = tl_phaseB2_sgv<kB2All>(e, S, Tv, muls, nm1, nullptr, true);
+            exact |= close;
+            bad |= !close && cr != host;
+        }
         n[0] += 1;
         n[1] += !exact;
         n[2] += exact;

@@ -122,11 +122,13 @@ __device__ __forceinline__ uint64_t global_ns() {
     asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
     return t;
 }
-// wait for the mbarrier phase of the given parity, at most ~0.25 s
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity) {
+// wait for the mbarrier phase of the given parity, at most ~0.25 s or
+// max_it polls (0: give up at once, the failure-path self-test)
+constexpr uint32_t kMbarPolls = 1u << 24;
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t max_it = kMbarPolls) {
     const uint32_t a = smem_addr(mbar);
     uint64_t t0 = 0;
-    for (uint32_t it = 0; it < (1u << 24); ++it) {
+    for (uint32_t it = 0; it < max_it; ++it) {
         uint32_t done;
         asm volatile(
             "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}"
@@ -186,7 +188,8 @@ struct __align__(128) MlpSmem {
 struct MlpThread {
     uint32_t phase = 0;
     bool abort = false;
-    bool pending = false;  // an MMA whose completion was not seen may still run
+    bool pending = false;       // an MMA whose completion was not seen may still run
+    uint32_t polls = kMbarPolls;  // poll limit of the next layer wait (0 once: the failure-path self-test)
 };
 
 // copy the packed weights, set up the mbarrier and tensor memory (all 128 threads)
@@ -239,7 +242,9 @@ __device__ __forceinline__ void mlp_layer_sync(MlpSmem& sm, int layer, MlpThread
         }
         tc_commit(&sm.mbar);
     }
-    if (mbar_wait(&sm.mbar, st.phase)) {
+    const uint32_t polls = st.polls;
+    st.polls = kMbarPolls;
+    if (mbar_wait(&sm.mbar, st.phase, polls)) {
         st.phase ^= 1u;
     } else {
         st.abort = true;
@@ -280,7 +285,9 @@ __device__ __forceinline__ void mlp_tile_begin(MlpSmem& sm, const float* x, MlpT
 __device__ __forceinline__ float mlp_tile_end(MlpSmem& sm, MlpThread& st) {
     const int t = threadIdx.x;
     if (!st.abort) {
-        if (mbar_wait(&sm.mbar, st.phase)) {
+        const uint32_t polls = st.polls;
+        st.polls = kMbarPolls;
+        if (mbar_wait(&sm.mbar, st.phase, polls)) {
             st.phase ^= 1u;
         } else {
             st.abort = true;
@@ -289,20 +296,25 @@ __device__ __forceinline__ float mlp_tile_end(MlpSmem& sm, MlpThread& st) {
         tc_fence_after();
     }
     const uint32_t lane_base = sm.tmem + ((uint32_t)(t & ~31) << 16);
+    // tensor memory is read only when the accumulator is known complete; the
+    // skip is warp-uniform (tcgen05.ld is a warp-wide instruction)
+    if (!__any_sync(0xffffffffu, st.abort)) {
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
-        float v[16];
-        tc_ld16(lane_base + 16 * c, v);
-        uint32_t q[8];
+        for (int c = 0; c < 4; ++c) {
+            float v[16];
+            tc_ld16(lane_base + 16 * c, v);
+            uint32_t q[8];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) q[j] = pack_bf16x2_relu(v[2 * j], v[2 * j + 1]);
-        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c, 8)) = make_uint4(q[0], q[1], q[2], q[3]);
-        *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c + 8, 8)) = make_uint4(q[4], q[5], q[6], q[7]);
+            for (int j = 0; j < 8; ++j) q[j] = pack_bf16x2_relu(v[2 * j], v[2 * j + 1]);
+            *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c, 8)) = make_uint4(q[0], q[1], q[2], q[3]);
+            *reinterpret_cast<uint4*>(sm.a2 + cm_offset(t, 16 * c + 8, 8)) = make_uint4(q[4], q[5], q[6], q[7]);
+        }
     }
     mlp_layer_sync(sm, 1, st);
     const float4* b2 = reinterpret_cast<const float4*>(sm.w + kPackB2);
     const float4* w3 = reinterpret_cast<const float4*>(sm.w + kPackW3);
     float z = *reinterpret_cast<const float*>(sm.w + kPackB3);
+    if (__any_sync(0xffffffffu, st.abort)) return z;  // meaningless after an abort
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         float v[16];

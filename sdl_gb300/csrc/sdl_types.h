@@ -62,6 +62,7 @@ enum : int {
     kFlagTLNav = 32,     // createTrackletsViaNavigation
     kFlagTCFromTL = 64,  // createTrackCandidatesFromTracklets
     kFlagTCFromTP = 128, // createTrackCandidatesFromTriplets
+    kFlagTestMlpGiveUp = 4096,  // self-test: the pre-filter's first tensor-core wait of each CTA gives up at once
 };
 
 // Per-stage status word bits

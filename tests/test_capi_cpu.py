@@ -72,3 +72,55 @@ def test_null_context_is_an_argument_error():
     assert L.sdlg_tl_phase_a_check(None, buf) == -1
     assert L.sdlg_last_tl_pass_times(None, f) == -1
     assert L.sdlg_mlp_stats(None, i) == -1
+
+
+def test_module_info_decodes_the_synthetic_detids():
+    """sdlg_module_info (SDL::Module's detId decoding, Module.cc:159-358) on
+    every sensor of the synthetic detector: layer, side, rod / ring, module,
+    lower / upper sensor and partner as the generator laid them out."""
+    import numpy as np
+    from sdl_gb300 import module_info, synth
+    det = synth.detector("full")
+    ids = set(int(d) for d in det.detid)
+    for d, inner in zip(det.detid[::7], det.is_inner[::7]):
+        m = module_info(int(d))
+        assert m["valid"]
+        assert m["isLower"] == int(bool(inner))
+        assert m["partnerDetId"] in ids and module_info(m["partnerDetId"])["partnerDetId"] == int(d)
+        if m["subdet"] == 5:
+            assert m["layer"] == (int(d) >> 20) & 7 and m["side"] == (int(d) >> 18) & 3
+            assert m["moduleType"] == (0 if m["layer"] <= 3 else 1)
+        else:
+            assert m["subdet"] == 4 and m["ring"] == (int(d) >> 12) & 15
+    assert not module_info(0x0123457)["valid"]
+
+
+def test_hit_derived_quantities():
+    """sdlg_hit_derived (Hit.cc:68-83): rt and r3 are float sums of float
+    products under a double square root, phi is Phi_mpi_pi(M_PI + ATan2(-y, -x))."""
+    import math
+    import numpy as np
+    from sdl_gb300 import hit_derived
+    rng = np.random.default_rng(7)
+    x, y, z = (rng.uniform(-120, 120, 1000).astype(np.float32) for _ in range(3))
+    x[:3] = 0
+    y[:2] = 0
+    rt, phi, eta, r3 = hit_derived(x, y, z)
+    for i in range(len(x)):
+        X, Y, Z = np.float32(x[i]), np.float32(y[i]), np.float32(z[i])
+        assert rt[i] == np.float32(math.sqrt(float(X * X + Y * Y)))
+        assert r3[i] == np.float32(math.sqrt(float(X * X + Y * Y + Z * Z)))
+        if X != 0:
+            at = np.float32(math.atan2(float(-Y), float(-X)))
+        else:
+            at = np.float32(0.0 if Y == 0 else (math.pi / 2 if -Y > 0 else -math.pi / 2))
+        p = np.float32(math.pi + float(at))
+        while float(p) >= math.pi:
+            p = np.float32(float(p) - 2 * math.pi)
+        while float(p) < -math.pi:
+            p = np.float32(float(p) + 2 * math.pi)
+        assert phi[i] == p
+        if rt[i] > 0:  # the float acosh of the float quotient r3 / rt
+            ratio = float(np.float32(r3[i]) / np.float32(rt[i]))
+            want = math.copysign(math.acosh(ratio), float(Z)) * (Z != 0)
+            assert abs(float(eta[i]) - want) <= 2e-7 * max(1.0, abs(want))
