@@ -306,15 +306,13 @@ int sdlg_math_check(sdlg_ctx* ctx, int fn, int exhaustive, uint64_t start, int64
 int sdlg_libm_eval(sdlg_ctx* ctx, int fn, uint32_t start_bits, int64_t n, float* out);
 int sdlg_libm_stats(int fn, uint64_t* out3);
 
-/* Self-check of the tracklet stage's fast decisions (no counterpart in the
- * reference): after a run through the tracklet stage, every tracklet
- * candidate of the batch is judged both by the fast decisions (the float
- * cuts, then for their survivors the first part of the tracklet cuts; for
- * the candidates through those, the final cuts evaluated with correctly
- * rounded float asin and sin and decided by margin) and by the exact cuts
- * (with the host libm's float functions).  out4: candidates, candidates the
- * fast decisions settled alone, candidates that needed an exact evaluation,
- * and candidates settled differently from the exact cuts (must be 0). */
+/* Self-check of the tracklet enumeration's single-precision decisions (no
+ * counterpart in the reference): after a run through the tracklet stage,
+ * every tracklet candidate of the batch is judged both by the fast decisions
+ * (the float cuts, then for their survivors the first part of the tracklet
+ * cuts) and by the exact cuts.  out4: candidates, candidates the fast
+ * decisions settled alone, candidates that needed an exact evaluation, and
+ * candidates settled differently from the exact cuts (must be 0). */
 int sdlg_tl_phase_a_check(sdlg_ctx* ctx, uint64_t* out4);
 
 /* Number of kernels one run of the chain launches (as last enqueued). */

@@ -898,28 +898,27 @@ __device__ __forceinline__ float edge_rt(float x, float y, float ex, float ey, b
 // Tracklet.cc:3181-3324.  The reference adds the double copysign term to a
 // float and rounds to float; a double sum of two floats rounded to float
 // equals the float sum (53 >= 2*24+2), so the additions are done in float.
-__device__ __forceinline__ float lm_asin(float x, bool host) { return host ? g_asin(x) : f_asin(x); }
 __device__ __forceinline__ void delta_beta_iterations(float& betaIn, float& betaOut, float& betaAv, float& pt_beta, float sdIn_dr,
-                                                      float sdOut_dr, float dr, int lIn, float pt_betaMax, bool host) {
+                                                      float sdOut_dr, float dr, int lIn, float pt_betaMax) {
     const float sinAlphaMax = 0.95f;
     if (betaIn * betaOut > 0.f &&
         (fabsf(pt_beta) < 4.f * pt_betaMax || (lIn >= 11 && fabsf(pt_beta) < 8.f * pt_betaMax))) {
-        const float betaInUpd = betaIn + copysignf(lm_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax), host), betaIn);
-        const float betaOutUpd = betaOut + copysignf(lm_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax), host), betaOut);
+        const float betaInUpd = betaIn + copysignf(g_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
+        const float betaOutUpd = betaOut + copysignf(g_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaOut);
         betaAv = 0.5f * (betaInUpd + betaOutUpd);
         pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
-        betaIn = betaIn + copysignf(lm_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax), host), betaIn);
-        betaOut = betaOut + copysignf(lm_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax), host), betaOut);
+        betaIn = betaIn + copysignf(g_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
+        betaOut = betaOut + copysignf(g_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaOut);
         betaAv = 0.5f * (betaIn + betaOut);
         pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
     } else if (lIn < 11 && (double)fabsf(betaOut) < 0.2 * (double)fabsf(betaIn) && fabsf(pt_beta) < 12.f * pt_betaMax) {
         const float pt_betaIn = pt_from(dr * k2Rinv1GeVf, betaIn);
-        const float betaInUpd = betaIn + copysignf(lm_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax), host), betaIn);
-        const float betaOutUpd = betaOut + copysignf(lm_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax), host), betaIn);
+        const float betaInUpd = betaIn + copysignf(g_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), betaIn);
+        const float betaOutUpd = betaOut + copysignf(g_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_betaIn), sinAlphaMax)), betaIn);
         betaAv = (fabsf(betaOut) > 0.2f * fabsf(betaIn)) ? (0.5f * (betaInUpd + betaOutUpd)) : betaInUpd;
         pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
-        betaIn = betaIn + copysignf(lm_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax), host), betaIn);
-        betaOut = betaOut + copysignf(lm_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax), host), betaIn);
+        betaIn = betaIn + copysignf(g_asin(fmin_ref(sdIn_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
+        betaOut = betaOut + copysignf(g_asin(fmin_ref(sdOut_dr * k2Rinv1GeVf / fabsf(pt_beta), sinAlphaMax)), betaIn);
         betaAv = 0.5f * (betaIn + betaOut);
         pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
     }
@@ -1398,12 +1397,9 @@ enum : int {
 
 // rec (optional, kTLVarN floats): the final cut variables of a candidate
 // that reaches the deltaBeta cut
-// host: the host libm's float asin and sin (the reference's), else the
-// correctly rounded ones; close (with host false): set when a final cut is
-// too close to call with the correctly rounded values (see tl_phaseB2)
 template <int kSet>
 __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV& T, float mulsF, bool nm1,
-                                               float* rec = nullptr, bool host = true, bool* close = nullptr) {
+                                               float* rec = nullptr) {
     if (kSet == kB2BBBB) algo = kAlgoBBBB;
     if (kSet == kB2Others && algo == kAlgoBBBB) return false;
     const float pt_betaMax = 7.0f;
@@ -1430,8 +1426,7 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
             const P3 loE = edge_point(OutUp.x, OutUp.y, OutUp.z, T.ex, T.ey, false);
             betaOutRHmin = -dphi(hiE, sub(hiE, OutLo)) + dphi(hiE, sub(hiE, InLo));
             betaOutRHmax = -dphi(loE, sub(loE, OutLo)) + dphi(loE, sub(loE, InLo));
-            const float dPhi = dphi(midpoint(InLo, OutLo), sub(OutLo, InLo));
-            const float sinDPhi = host ? g_sin(dPhi) : f_sin(dPhi);
+            const float sinDPhi = g_sin(dphi(midpoint(InLo, OutLo), sub(OutLo, InLo)));
             const float rr = (hiE.rt - loE.rt) * sinDPhi / dr;
             dBetaROut2 = rr * rr;  // the double square of a float is exact: one rounding to float
         } else {
@@ -1456,8 +1451,7 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
         betaOutRHmax = betaOut - sdOut_alphaOut_max + sdOut_alphaOut;
         if (fabsf(betaOutRHmin) > fabsf(betaOutRHmax)) { const float t = betaOutRHmin; betaOutRHmin = betaOutRHmax; betaOutRHmax = t; }
         if (T.flags & F_UP_2S) {
-            const float dPhi = dphi(midpoint(InLo, OutLo), sub(OutLo, InLo));
-            const float sinDPhi = host ? g_sin(dPhi) : f_sin(dPhi);
+            const float sinDPhi = g_sin(dphi(midpoint(InLo, OutLo), sub(OutLo, InLo)));
             const float hrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, true);
             const float lrt = edge_rt(OutUp.x, OutUp.y, T.ex, T.ey, false);
             const float rr = (hrt - lrt) * sinDPhi / dr;
@@ -1489,7 +1483,7 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
     }
     float betaAv = 0.5f * (betaIn + betaOut);
     float pt_beta = pt_from(dr * k2Rinv1GeVf, betaAv);
-    delta_beta_iterations(betaIn, betaOut, betaAv, pt_beta, sdIn_dr, sdOut_dr, dr, lIn, pt_betaMax, host);
+    delta_beta_iterations(betaIn, betaOut, betaAv, pt_beta, sdIn_dr, sdOut_dr, dr, lIn, pt_betaMax);
     const float betaInMMSF = (fabsf(betaInRHmin + betaInRHmax) > 0) ? (2.f * betaIn / fabsf(betaInRHmin + betaInRHmax)) : 0.f;
     const float betaOutMMSF = (fabsf(betaOutRHmin + betaOutRHmax) > 0) ? (2.f * betaOut / fabsf(betaOutRHmin + betaOutRHmax)) : 0.f;
     betaInRHmin *= betaInMMSF; betaInRHmax *= betaInMMSF;
@@ -1500,13 +1494,8 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
     const float dBetaInLum = lIn < 11 ? 0.0f : fabsf(alphaInAbsReg * kDeltaZLum / InLo.z);
     const float dBetaOutLum = lOut < 11 ? 0.0f : fabsf(alphaOutAbsReg * kDeltaZLum / OutLo.z);
     const float dBetaLum2 = (dBetaInLum + dBetaOutLum) * (dBetaInLum + dBetaOutLum);
-    const float betaOut_cut = add_dsqrt(lm_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax), host) + (0.02f / sdOut_d),
+    const float betaOut_cut = add_dsqrt(g_asin(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d),
                                         dBetaLum2 + dBetaMuls * dBetaMuls);
-    const float sc = fabsf(betaIn) + fabsf(betaOut);
-    if (close && fabsf(fabsf(betaOut) - betaOut_cut) <= (sc + betaOut_cut) * 0x1p-10f) {
-        *close = true;
-        return false;
-    }
     if (!(fabsf(betaOut) < betaOut_cut)) return false;
     const float dBetaRes = 0.02f / fmin_ref(sdOut_d, sdIn_d);
     const float dBetaCut2 = dbeta_cut2(dBetaRes, dBetaMuls, dBetaLum2, dBetaROut2, betaInRHmin, betaInRHmax, betaOutRHmin, betaOutRHmax);
@@ -1518,40 +1507,12 @@ __device__ __forceinline__ bool tl_phaseB2_sgv(int algo, const SGV& S, const SGV
         rec[kTLVarDBetaCut2] = dBetaCut2; rec[kTLVarDBetaLum2] = dBetaLum2; rec[kTLVarDBetaMuls] = dBetaMuls;
         rec[kTLVarDBetaRes] = dBetaRes; rec[kTLVarDBetaRIn2] = 0.f; rec[kTLVarDBetaROut2] = dBetaROut2;
     }
-    const float rh = fabsf(betaInRHmin - betaInRHmax) + fabsf(betaOutRHmin - betaOutRHmax);
-    if (close && !nm1 &&
-        fabsf(dBeta * dBeta - dBetaCut2) <=
-            dBetaCut2 * 0x1p-9f + (fabsf(dBeta) + rh) * sc * 0x1p-10f + sc * sc * 0x1p-20f) {
-        *close = true;
-        return false;
-    }
     return (dBeta * dBeta <= dBetaCut2) || nm1;
-}
-// Phase B2 is evaluated with the correctly rounded float asin and sin first.
-// The host libm's (the reference's) are within one float step of them.
-// Through the deltaBeta iterations (angles added to angles of the same sign,
-// pT from a sine of their mean, asin arguments scaled by it, asin condition
-// numbers below 2.4 for arguments up to 0.95) betaIn and betaOut move by at
-// most 2^-15 of sc = |betaIn| + |betaOut| (a betaOut that the iteration
-// cancels towards zero included: its asin term is below 3 |betaIn|), pT and
-// the multiple-scattering term by 2^-14 of themselves, so betaOut_cut by
-// 2^-13 and dBetaCut2 by 2^-12 of themselves (and the spread of the scaled
-// RH bounds by 2^-14 sc), dBeta by 2^-14 sc.  A final comparison decided by
-// more than the margins above (at least four times those bounds) is the
-// host's decision as well; the rare closer ones are evaluated again with the
-// host libm.  sdlg_tl_phase_a_check evaluates both on every candidate through
-// phase B1 and counts the decisions that differ.
-template <int kSet>
-static __device__ __noinline__ bool tl_phaseB2_host(int algo, const SGV& S, const SGV& T, float mulsF, bool nm1) {
-    return tl_phaseB2_sgv<kSet>(algo, S, T, mulsF, nm1, nullptr, true);
 }
 template <int kSet>
 static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict__ pack, int s, int t, float mulsF,
                                                 bool nm1) {
-    const SGV S = load_sgv(pack, s), T = load_sgv(pack, t);
-    bool close = false;
-    const bool pass = tl_phaseB2_sgv<kSet>(algo, S, T, mulsF, nm1, nullptr, false, &close);
-    return close ? tl_phaseB2_host<kSet>(algo, S, T, mulsF, nm1) : pass;
+    return tl_phaseB2_sgv<kSet>(algo, load_sgv(pack, s), load_sgv(pack, t), mulsF, nm1);
 }
 
 // phase B in one call (phase B1, then phase B2 on its survivors)

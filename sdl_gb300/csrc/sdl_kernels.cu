@@ -1351,29 +1351,43 @@ __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
     MlpThread st;
     if (b.flags & kFlagTestMlpGiveUp) st.polls = 0;
     unsigned n_scored = 0, n_kept = 0;
-    // entry t * 128 + threadIdx.x of tile t and its features
-    auto load = [&](int64_t t, PfPending& p, float* f) -> bool {
-        const int64_t i = t * kMlpTile + threadIdx.x;
-        const bool valid = t < ntile && i < n;
-        if (valid) {
-            p.e = AT(b.passa, i, b.kept_cap);
-            tl_features(feat_s(b.sgfeat, p.e.x), feat_t(b.sgfeat, p.e.y), f);
-        } else {
-#pragma unroll
-            for (int k = 0; k < kMlpIn; ++k) f[k] = 0.f;
-        }
+    // Three tiles in the pipeline of each thread: the list entry of tile
+    // t + 2G (G = gridDim.x) is loaded, the two segment records of tile t + G
+    // are loaded with the entry loaded one iteration earlier, and the features
+    // of tile t are computed from the records loaded one iteration earlier,
+    // so that every load has a tile's MMAs and epilogue to complete in.
+    const int64_t G = gridDim.x;
+    auto entry = [&](int64_t tt, int4& e) -> bool {
+        const int64_t i = tt * kMlpTile + threadIdx.x;
+        const bool valid = tt < ntile && i < n;
+        if (valid) e = AT(b.passa, i, b.kept_cap);
         return valid;
     };
     int64_t t = blockIdx.x;
     PfPending cur, pend;
-    float f[kMlpIn];
-    bool valid = load(t, cur, f);
+    int4 e1 = make_int4(0, 0, 0, 0), e2 = make_int4(0, 0, 0, 0);
+    bool valid = entry(t, cur.e);
+    bool v1 = entry(t + G, e1);
+    FeatS rs{};
+    FeatT rt{};
+    if (valid) {
+        rs = feat_s(b.sgfeat, cur.e.x);
+        rt = feat_t(b.sgfeat, cur.e.y);
+    }
     while (t < ntile) {
+        float f[kMlpIn];
+        if (valid) {
+            tl_features(rs, rt, f);
+        } else {
+#pragma unroll
+            for (int k = 0; k < kMlpIn; ++k) f[k] = 0.f;
+        }
         mlp_tile_begin(sm, f, st);
-        const int64_t tn = t + gridDim.x;
-        PfPending nxt;
-        float fn[kMlpIn];
-        const bool valid_n = load(tn, nxt, fn);
+        const bool v2 = entry(t + 2 * G, e2);
+        if (v1) {
+            rs = feat_s(b.sgfeat, e1.x);
+            rt = feat_t(b.sgfeat, e1.y);
+        }
         pf_flush(b, pend);
         const float z = mlp_tile_end(sm, st);
         const bool keep = valid && z >= thr;
@@ -1385,11 +1399,11 @@ __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
             if (lane == cur.leader) cur.raw = atomicAdd(b.n_kept2, (unsigned long long)__popc(cur.m));
         }
         pend = cur;
-        cur = nxt;
-        valid = valid_n;
-#pragma unroll
-        for (int k = 0; k < kMlpIn; ++k) f[k] = fn[k];
-        t = tn;
+        cur.e = e1;
+        valid = v1;
+        e1 = e2;
+        v1 = v2;
+        t += G;
     }
     pf_flush(b, pend);
     n_scored = __reduce_add_sync(0xffffffffu, n_scored);
@@ -1594,16 +1608,7 @@ __global__ void k_tl_quick_check(BatchDev b, unsigned long long* out) {
         float cut, muls;
         const int e = tl_phaseA(S, Tv, cut, muls);
         const bool eb1 = e != kAlgoNone && tl_phaseB1_sgv(e, S, Tv, cut);
-        bool bad = q == kAlgoNone ? eb1 : (q != e || (b1 && !eb1));
-        if (eb1) {
-            // the final cuts: correctly rounded values with margins against the host libm's
-            const bool nm1 = (b.flags & kFlagTLNm1) != 0;
-            bool close = false;
-            const bool cr = tl_phaseB2_sgv<kB2All>(e, S, Tv, muls, nm1, nullptr, false, &close);
-            const bool host = tl_phaseB2_sgv<kB2All>(e, S, Tv, muls, nm1, nullptr, true);
-            exact |= close;
-            bad |= !close && cr != host;
-        }
+        const bool bad = q == kAlgoNone ? eb1 : (q != e || (b1 && !eb1));
         n[0] += 1;
         n[1] += !exact;
         n[2] += exact;

@@ -1,9 +1,7 @@
-"""The tracklet stage's fast decisions (tl_ab1_decide: phase A, then phase
-B1 for its survivors, single precision; then the final cuts of phase B2
-with correctly rounded float asin and sin, decided by margin) against the
-exact cuts (tl_phaseA, tl_phaseB1_sgv, phase B2 with the host libm's float
-functions) on every tracklet candidate of a batch at PU 100, 200 and 300,
-for the module-map, layer-pair, Nm1 and navigation candidate sets: they
+"""The tracklet enumeration's single-precision decisions (tl_ab1_decide:
+phase A, then phase B1 for its survivors) against the exact cuts (tl_phaseA,
+tl_phaseB1_sgv) on every tracklet candidate of a batch at PU 100, 200 and
+300, for the module-map, layer-pair, Nm1 and navigation candidate sets: they
 never settle a candidate differently, and they leave only a small share of
 them to the exact cuts.  The object sets of the chain that uses them are
 checked against the reference and the oracle elsewhere."""
