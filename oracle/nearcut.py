@@ -11,6 +11,9 @@ the host libm (``sdlg_libm_eval``), so these are the decisions on which a
 correctly rounded evaluation would disagree with the reference.
 
     python -m oracle.nearcut --batch headline|config3 [--events N] [--threads T] [--out report.json]
+
+The committed reports, tests/golden/nearcut/headline.json and config3.json, were made with
+--threads 8 and --out set to those paths.
 """
 from __future__ import annotations
 
