@@ -1218,6 +1218,12 @@ __global__ void __launch_bounds__(kEnumThreads, 4) k_tl_enum_tiles(BatchDev b) {
     passbuf_flush(b, pb);
 }
 
+// CTAs per SM the segment second pass is compiled for (register budget)
+#ifndef SDLG_SGB_MIN_BLOCKS
+#define SDLG_SGB_MIN_BLOCKS 1
+#endif
+constexpr int kSgbMinBlocks = SDLG_SGB_MIN_BLOCKS;
+
 // Module-map segment candidates in two passes (Event.cc:445-522 with
 // Segment.cc:337-859): k_sg_enum_a takes tasks of consecutive candidates
 // like k_enum, runs the algorithm's first cuts (sg_pair_rec<true>: the same
@@ -1270,7 +1276,7 @@ __global__ void __launch_bounds__(kEnumThreads) k_sg_enum_a(BatchDev b) {
     passbuf_flush(b, pb);
 }
 
-__global__ void __launch_bounds__(kEnumThreads) k_sg_b(BatchDev b) {
+__global__ void __launch_bounds__(kEnumThreads, kSgbMinBlocks) k_sg_b(BatchDev b) {
     __shared__ int rbuf[kEnumThreads / kWarp][3 + 6][kRecBuf];
     if (halted(b)) return;
     const int64_t n = min((int64_t)*b.n_kept, b.kept_cap);
@@ -1483,10 +1489,16 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const int4* 
     pb_flush(b, bbuf[w], nbb, false);
 }
 
+// CTAs per SM the phase-B2 kernels are compiled for (register budget)
+#ifndef SDLG_B2_MIN_BLOCKS
+#define SDLG_B2_MIN_BLOCKS 1
+#endif
+constexpr int kB2MinBlocks = SDLG_B2_MIN_BLOCKS;
+
 // Phase B2 on one part of the phase-B2 list (kSet kB2BBBB: the front, BBBB
 // entries; kB2Others: the back, BBEE and EEEE entries); appends the tracklets.
 template <int kSet>
-__global__ void __launch_bounds__(kEnumThreads) k_tl_b2(BatchDev b) {
+__global__ void __launch_bounds__(kEnumThreads, kB2MinBlocks) k_tl_b2(BatchDev b) {
     __shared__ int rbuf[kEnumThreads / kWarp][3][kRecBuf];
     if (halted(b)) return;
     const int64_t nf = min((int64_t)b.n_pb[0], b.kept_cap);
