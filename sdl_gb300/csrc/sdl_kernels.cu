@@ -1218,9 +1218,11 @@ __global__ void __launch_bounds__(kEnumThreads, 4) k_tl_enum_tiles(BatchDev b) {
     passbuf_flush(b, pb);
 }
 
-// CTAs per SM the segment second pass is compiled for (register budget)
+// CTAs per SM the segment second pass is compiled for (register budget; 6
+// measured fastest on the 128-event PU 150-300 batch: 8.9 ms against 9.6 ms
+// at 1)
 #ifndef SDLG_SGB_MIN_BLOCKS
-#define SDLG_SGB_MIN_BLOCKS 1
+#define SDLG_SGB_MIN_BLOCKS 6
 #endif
 constexpr int kSgbMinBlocks = SDLG_SGB_MIN_BLOCKS;
 
@@ -1489,9 +1491,11 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const int4* 
     pb_flush(b, bbuf[w], nbb, false);
 }
 
-// CTAs per SM the phase-B2 kernels are compiled for (register budget)
+// CTAs per SM the phase-B2 kernels are compiled for (register budget; 4
+// measured fastest on the 128-event PU 150-300 batch: phase B1+B2 8.1 ms
+// against 9.7 ms at 1, plain chain's B2 54.9 ms against 58.5 ms)
 #ifndef SDLG_B2_MIN_BLOCKS
-#define SDLG_B2_MIN_BLOCKS 1
+#define SDLG_B2_MIN_BLOCKS 4
 #endif
 constexpr int kB2MinBlocks = SDLG_B2_MIN_BLOCKS;
 
