@@ -428,6 +428,59 @@ def main():
     value = allsum(pg, len(batch)) * 1e3 / mean_ms
     hl_stage = np.mean(np.array(stage_ms), axis=0)
 
+    # ---- end to end through the C ABI: pinned host buffers in, track
+    # candidates out, for the whole batch each step (the launch shapes tuned
+    # above for this chain) -----------------------------------------------------
+    n_hit = int(sum(len(e) for e in batch))
+    pin = ch.pinned(n_hit * 20 + 64)
+    evoff = np.zeros(len(batch) + 1, dtype=np.int64)
+    evoff[1:] = np.cumsum([len(e) for e in batch])
+    views = []
+    for k, (attr, dt) in enumerate((("x", np.float32), ("y", np.float32), ("z", np.float32), ("idx", np.int32),
+                                    ("detid", np.uint32))):
+        v = pin[k * n_hit * 4:(k + 1) * n_hit * 4].view(dt)
+        v[:] = np.concatenate([getattr(e, attr) for e in batch])
+        views.append(v)
+    # the result buffers are pinned too (two, used in turn), each sized for
+    # twice the headline run's track candidates
+    n_tc_cap = 2 * int(n_pruned[4]) + 1024
+    tc_outs = [ch.pinned(n_tc_cap * 16 * 4).view(np.int32).reshape(n_tc_cap, 16) for _ in range(2)]
+
+    def e2e_step(k, pipelined):
+        ch.set_events_raw(len(batch), evoff.ctypes.data, *[v.ctypes.data for v in views])
+        ch.run(4, FLAG_MLP)
+        if pipelined:  # the copy of this step's candidates overlaps the next step
+            return ch.objects_async(4, -1, tc_outs[k & 1]) * 64 + 8 * 2
+        return ch.objects(4, -1, out=tc_outs[k & 1]).nbytes + 8 * 2
+
+    # (1) one step after another, each ending when its candidates are in host
+    # memory; L2 flushed before each step
+    e2e_ms, d2h = [], []
+    for k in range(a.warmup + a.steps):
+        flush()
+        t0 = time.perf_counter()
+        nb = e2e_step(k, False)
+        t1 = time.perf_counter()
+        if k >= a.warmup:
+            e2e_ms.append((t1 - t0) * 1e3)
+            d2h.append(nb)
+    e2e_sync_mean = allmax(pg, statistics.fmean(e2e_ms))
+    # (2) the same steps back to back, each step's readback copied while the
+    # next step runs; timed from the first step's inputs to the last step's
+    # candidates in host memory (inputs of 280 MB, above the L2's 129 MB)
+    for k in range(a.warmup):
+        e2e_step(k, True)
+    ch.wait_objects()
+    flush()
+    barrier(pg)
+    t0 = time.perf_counter()
+    d2h_p = [e2e_step(k, True) for k in range(a.steps)]
+    ch.wait_objects()
+    t1 = time.perf_counter()
+    e2e_mean = allmax(pg, (t1 - t0) * 1e3 / a.steps)
+    e2e_value = allsum(pg, len(batch)) * 1e3 / e2e_mean
+    e2e_sync_value = allsum(pg, len(batch)) * 1e3 / e2e_sync_mean
+
     # ---- the plain batched chain on the same events --------------------------
     tuned_plain = ch.autotune(4, 0)
     for _ in range(2):
@@ -501,36 +554,6 @@ def main():
                  "prefilter": {k: d_mstats[k] for k in ("candidates", "scored", "kept")},
                  "stage_ms": {k: round(float(v), 3) for k, v in zip(STAGE_NAMES, np.mean(np.array(dm_stage), axis=0))},
                  "plain_stage_ms": {k: round(float(v), 3) for k, v in zip(STAGE_NAMES, np.mean(np.array(dp_stage), axis=0))}}
-
-    # ---- end to end through the C ABI: pinned host buffers in, track
-    # candidates out, for the whole batch each step -----------------------------
-    n_hit = int(sum(len(e) for e in batch))
-    pin = ch.pinned(n_hit * 20 + 64)
-    evoff = np.zeros(len(batch) + 1, dtype=np.int64)
-    evoff[1:] = np.cumsum([len(e) for e in batch])
-    views = []
-    for k, (attr, dt) in enumerate((("x", np.float32), ("y", np.float32), ("z", np.float32), ("idx", np.int32),
-                                    ("detid", np.uint32))):
-        v = pin[k * n_hit * 4:(k + 1) * n_hit * 4].view(dt)
-        v[:] = np.concatenate([getattr(e, attr) for e in batch])
-        views.append(v)
-    # the result buffer is pinned too, sized for twice the headline run's
-    # track candidates
-    n_tc_cap = 2 * int(n_pruned[4]) + 1024
-    tc_out = ch.pinned(n_tc_cap * 16 * 4).view(np.int32).reshape(n_tc_cap, 16)
-    e2e_ms, d2h = [], []
-    for k in range(a.warmup + a.steps):
-        flush()
-        t0 = time.perf_counter()
-        ch.set_events_raw(len(batch), evoff.ctypes.data, *[v.ctypes.data for v in views])
-        ch.run(4, FLAG_MLP)
-        tc = ch.objects(4, -1, out=tc_out)
-        t1 = time.perf_counter()
-        if k >= a.warmup:
-            e2e_ms.append((t1 - t0) * 1e3)
-            d2h.append(tc.nbytes + 8 * 2)
-    e2e_mean = allmax(pg, statistics.fmean(e2e_ms))
-    e2e_value = allsum(pg, len(batch)) * 1e3 / e2e_mean
 
     # ---- plain chain, one PU200-like event per step --------------------------
     ev = single[0]
@@ -652,8 +675,14 @@ def main():
             "plain_batched": plain_batched, "plain_single": plain_single, "variants": variants,
             "stated_density": dense,
             "e2e": {"value": round(e2e_value, 3), "unit": "events/s", "ms_per_step": round(e2e_mean, 3),
-                    "h2d_bytes_per_step": n_hit * 20 + 8 * (len(batch) + 1), "d2h_bytes_per_step": int(statistics.fmean(d2h)),
-                    "path": "sdlg_set_events (pinned host) + sdlg_run(SDLG_FLAG_MLP) + sdlg_get_objects(TC, into pinned host memory)"},
+                    "h2d_bytes_per_step": n_hit * 20 + 8 * (len(batch) + 1), "d2h_bytes_per_step": int(statistics.fmean(d2h_p)),
+                    "path": "per step: sdlg_set_events (pinned host) + sdlg_run(SDLG_FLAG_MLP) + sdlg_get_objects_async(TC, "
+                            "into pinned host memory); the steps back to back, each step's readback overlapping the next "
+                            "step's run; timed until sdlg_wait_objects returns after the last step",
+                    "unpipelined": {"value": round(e2e_sync_value, 3), "ms_per_step": round(e2e_sync_mean, 3),
+                                    "d2h_bytes_per_step": int(statistics.fmean(d2h)),
+                                    "path": "sdlg_set_events + sdlg_run + sdlg_get_objects (synchronous), "
+                                            "each step timed alone, L2 flushed before it"}},
             "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "tc_outside_plain": tc_outside,
             "ratios_vs_cpu_baseline": None if not cpu else {
                 "headline_events": round(value / cpu["value"], 2),

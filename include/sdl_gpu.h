@@ -194,6 +194,16 @@ int sdlg_get_counts(sdlg_ctx* ctx, int64_t event, int64_t* out5);
  * out (capacity `cap` tuples); *n_out receives the number of tuples. */
 int sdlg_get_objects(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int64_t cap, int64_t* n_out);
 
+/* The same tuples without waiting for the copy: they are written on the
+ * device right away (so the next sdlg_run may follow at once) and copied to
+ * `out` on a second stream while the caller goes on; out must stay valid
+ * and untouched until sdlg_wait_objects() returns, and should be pinned
+ * (sdlg_host_alloc) for the copy to overlap the next run.  *n_out is known
+ * on return.  A later readback of the same context waits for this copy
+ * before it reuses the device buffer. */
+int sdlg_get_objects_async(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int64_t cap, int64_t* n_out);
+int sdlg_wait_objects(sdlg_ctx* ctx);
+
 /* The object graph of one event, for the reference's pointer accessors
  * (Module::getMiniDoubletPtrs ... getTrackletPtrs, Module.h:273-277;
  * MiniDoublet::lowerHitPtr/upperHitPtr, getDz, getShiftedDz, getDeltaPhi,

@@ -75,6 +75,8 @@ def lib():
         L.sdlg_sync.argtypes = [vp]
         L.sdlg_get_counts.argtypes = [vp, i64, vp]
         L.sdlg_get_objects.argtypes = [vp, i32, i64, vp, i64, vp]
+        L.sdlg_get_objects_async.argtypes = [vp, i32, i64, vp, i64, vp]
+        L.sdlg_wait_objects.argtypes = [vp]
         L.sdlg_get_counters.argtypes = [vp, i64, vp]
         L.sdlg_last_times.argtypes = [vp, vp]
         L.sdlg_last_kernel_times.argtypes = [vp, vp]
@@ -207,6 +209,7 @@ class Chain:
 
     def close(self):
         if getattr(self, "h", None):
+            lib().sdlg_wait_objects(self.h)  # no readback may still be writing pinned memory
             for p in self._pinned:
                 lib().sdlg_host_free(self.h, p)
             self._pinned = []
@@ -327,6 +330,23 @@ class Chain:
         if n.value:
             self._ck(lib().sdlg_get_objects(self.h, stage, event, out.ctypes.data, n.value, ctypes.byref(n)))
         return out[:n.value]
+
+    def objects_async(self, stage: int, event: int, out: np.ndarray) -> int:
+        """Start reading a stage's tuples into `out` (int32, C-contiguous,
+        shape (>= n, width); pinned() memory for the copy to overlap the next
+        run) and return n without waiting: `out` holds them once
+        wait_objects() returns."""
+        n = ctypes.c_int64()
+        self._ck(lib().sdlg_get_objects(self.h, stage, event, None, 0, ctypes.byref(n)))
+        if (out.dtype != np.int32 or out.ndim != 2 or out.shape[1] != WIDTH[stage] or out.shape[0] < n.value
+                or not out.flags.c_contiguous):
+            raise ValueError("out must be a C-contiguous int32 array of shape (>= %d, %d)" % (n.value, WIDTH[stage]))
+        self._ck(lib().sdlg_get_objects_async(self.h, stage, event, out.ctypes.data, out.shape[0], ctypes.byref(n)))
+        return n.value
+
+    def wait_objects(self):
+        """Wait for the readback objects_async() started."""
+        self._ck(lib().sdlg_wait_objects(self.h))
 
     def links(self, stage: int, event: int = 0):
         """The object graph of one event's stage: (constituents n x 2 as

@@ -140,6 +140,15 @@ struct sdlg_ctx {
     // pinned staging
     void* pinned = nullptr;
     int64_t pinned_bytes = 0;
+    // device scratch for results on their way to pageable host memory (kept
+    // between calls: allocating a gigabyte afresh costs more than copying it)
+    void* scratch = nullptr;
+    int64_t scratch_bytes = 0;
+    // asynchronous readback: the copy of the scratch to the host runs on its
+    // own stream (ev_mat: the scratch is written; ev_copy: it has been read)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_mat = nullptr, ev_copy = nullptr;
+    bool copy_pending = false;
     int64_t* h_small = nullptr;   // pinned: n_rec[5], status
     // graph
     cudaGraphExec_t graph = nullptr;
@@ -178,6 +187,26 @@ void free_batch(sdlg_ctx* ctx) {
     for (void* p : ctx->allocs) cudaFree(p);
     ctx->allocs.clear();
     ctx->buffers_ok = false;
+}
+
+// ctx->scratch grown to at least `bytes` (with a quarter of headroom)
+int ensure_scratch(sdlg_ctx* ctx, size_t bytes, void** p) {
+    if (ctx->scratch_bytes < (int64_t)bytes) {
+        if (ctx->scratch) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaStreamSynchronize(ctx->copy_stream);
+            ctx->copy_pending = false;
+            cudaFree(ctx->scratch);
+        }
+        ctx->scratch = nullptr;
+        ctx->scratch_bytes = 0;
+        const size_t want = bytes + bytes / 4 + 256;
+        cudaError_t e = cudaMalloc(&ctx->scratch, want);
+        if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CAPACITY, "cudaMalloc(%zu): %s", want, cudaGetErrorString(e));
+        ctx->scratch_bytes = (int64_t)want;
+    }
+    *p = ctx->scratch;
+    return SDLG_OK;
 }
 
 template <class T>
@@ -248,6 +277,16 @@ int build_module_table(sdlg_ctx* ctx, const std::vector<uint32_t>& extra) {
         const float half_pitch_drdz = 0.5f * 0.15f * o.drdz_s;
         const float one_plus = 1.f + o.drdz_s * o.drdz_s;
         o.tilt = (float)((double)half_pitch_drdz / std::sqrt((double)one_plus) / (double)o.gap);
+        // the strip shift's module-only terms (MiniDoublet.cc:1260-1332), with
+        // the host's float functions as the reference calls them
+        o.sh_angle_b = m.subdet == kEndcap ? (float)(M_PI / 2.) : std::atan(o.drdz_s);
+        const float abs_atan_slope = (o.slope_s != kSdlInf) ? std::fabs(std::atan(o.slope_s)) : (float)(M_PI / 2);
+        const float angle_m[4] = {abs_atan_slope, (float)(M_PI - (double)abs_atan_slope),
+                                  (float)(M_PI + (double)abs_atan_slope), (float)(2 * M_PI - (double)abs_atan_slope)};
+        for (int q = 0; q < 4; ++q) {
+            o.sh_sin[q] = std::sin(angle_m[q]);
+            o.sh_cos[q] = std::cos(angle_m[q]);
+        }
     }
     ctx->conn_off.assign(n + 1, 0);
     ctx->conn_idx.clear();
@@ -721,6 +760,9 @@ int sdlg_create(sdlg_ctx** out, int device) {
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_mat, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming);
     for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&ctx->ev[k]);
     for (int k = 0; k < kNumStages && e == cudaSuccess; ++k) {
         e = cudaEventCreate(&ctx->hooks.enum_start[k]);
@@ -761,6 +803,7 @@ int sdlg_destroy(sdlg_ctx* ctx) {
     if (!ctx) return SDLG_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     free_batch(ctx);
     cudaFree(ctx->d_detid); cudaFree(ctx->d_mod); cudaFree(ctx->d_conn_off); cudaFree(ctx->d_conn_idx);
     cudaFree(ctx->d_slot_run);
@@ -770,6 +813,10 @@ int sdlg_destroy(sdlg_ctx* ctx) {
         for (void* p : ps) cudaFree(p);
     }
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
+    if (ctx->scratch) cudaFree(ctx->scratch);
+    if (ctx->ev_mat) cudaEventDestroy(ctx->ev_mat);
+    if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     for (int k = 0; k < 8; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     for (int k = 0; k < kNumStages; ++k) {
@@ -1071,14 +1118,55 @@ int sdlg_get_objects(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int6
     if (cap < n) return fail(ctx, SDLG_ERR_ARG, "output capacity %lld < %lld tuples", (long long)cap, (long long)n);
     static const int width[5] = {2, 4, 8, 8, 16};
     const size_t bytes = (size_t)n * width[stage] * 4;
-    // materialise into the (then unused) staging records of the stage
-    int32_t* tmp = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&tmp, bytes, ctx->stream);
-    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "cudaMallocAsync: %s", cudaGetErrorString(e));
-    launch_materialize(ctx->b, stage, first, n, tmp, ctx->stream);
+    // through the device scratch and one copy (measured on the 1.06 GB of a
+    // 128-event batch's track candidates: 9 ms, against 26 ms for the kernel
+    // writing pinned host memory itself)
+    void* tmp = nullptr;
+    rc = ensure_scratch(ctx, bytes, &tmp);
+    if (rc) return rc;
+    if (ctx->copy_pending) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0));
+    launch_materialize(ctx->b, stage, first, n, static_cast<int32_t*>(tmp), ctx->stream);
+    CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, tmp, bytes, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaFreeAsync(tmp, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
+    return SDLG_OK;
+}
+
+int sdlg_get_objects_async(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int64_t cap, int64_t* n_out) {
+    if (!ctx || !n_out || cap < 0) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    int64_t first, n;
+    int rc = event_range(ctx, stage, event, &first, &n);
+    if (rc) return rc;
+    *n_out = n;
+    if (n == 0 || !out) return SDLG_OK;
+    if (cap < n) return fail(ctx, SDLG_ERR_ARG, "output capacity %lld < %lld tuples", (long long)cap, (long long)n);
+    static const int width[5] = {2, 4, 8, 8, 16};
+    const size_t bytes = (size_t)n * width[stage] * 4;
+    void* tmp = nullptr;
+    rc = ensure_scratch(ctx, bytes, &tmp);
+    if (rc) return rc;
+    // the tuples are written to the scratch on the context stream (after the
+    // run, before the next one) once the previous readback has read it; the
+    // copy to the host then runs on the copy stream, beside the next run
+    if (ctx->copy_pending) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0));
+    launch_materialize(ctx->b, stage, first, n, static_cast<int32_t*>(tmp), ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev_mat, ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_mat, 0));
+    CK(cudaMemcpyAsync(out, tmp, bytes, cudaMemcpyDeviceToHost, ctx->copy_stream));
+    CK(cudaEventRecord(ctx->ev_copy, ctx->copy_stream));
+    ctx->copy_pending = true;
+    return SDLG_OK;
+}
+
+int sdlg_wait_objects(sdlg_ctx* ctx) {
+    if (!ctx) return SDLG_ERR_ARG;
+    cudaSetDevice(ctx->device);
+    if (ctx->copy_pending) {
+        CK(cudaEventSynchronize(ctx->ev_copy));
+        ctx->copy_pending = false;
+    }
     return SDLG_OK;
 }
 
@@ -1105,9 +1193,11 @@ int sdlg_get_object_links(sdlg_ctx* ctx, int stage, int64_t event, int32_t* link
     const int nf = ctx->b.obj[stage].nf;
     const size_t b_links = (size_t)n * 2 * sizeof(int32_t), b_mod = (size_t)n * sizeof(int32_t);
     const size_t b_vals = (size_t)n * nf * sizeof(float);
-    char* tmp = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&tmp, b_links + b_mod + b_vals + 16, ctx->stream);
-    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "cudaMallocAsync: %s", cudaGetErrorString(e));
+    void* vtmp = nullptr;
+    rc = ensure_scratch(ctx, b_links + b_mod + b_vals + 16, &vtmp);
+    if (rc) return rc;
+    char* tmp = static_cast<char*>(vtmp);
+    if (ctx->copy_pending) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0));
     int32_t* d_links = links ? reinterpret_cast<int32_t*>(tmp) : nullptr;
     int32_t* d_mod = module ? reinterpret_cast<int32_t*>(tmp + b_links) : nullptr;
     float* d_vals = (vals && nf) ? reinterpret_cast<float*>(tmp + b_links + b_mod) : nullptr;
@@ -1117,7 +1207,6 @@ int sdlg_get_object_links(sdlg_ctx* ctx, int stage, int64_t event, int32_t* link
     if (d_links) CK(cudaMemcpyAsync(links, d_links, b_links, cudaMemcpyDeviceToHost, ctx->stream));
     if (d_mod) CK(cudaMemcpyAsync(module, d_mod, b_mod, cudaMemcpyDeviceToHost, ctx->stream));
     if (d_vals) CK(cudaMemcpyAsync(vals, d_vals, b_vals, cudaMemcpyDeviceToHost, ctx->stream));
-    CK(cudaFreeAsync(tmp, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     return SDLG_OK;
 }

@@ -42,6 +42,13 @@ struct ModDev {
     float slope_s;       // strip-direction slope of the strip sensor of the pair
     float edge_x, edge_y;  // (float)(2.5*cos(phi_c)), (float)(2.5*sin(phi_c)) of this sensor
     float tilt;          // (float)((double)(0.5f*pitchPS*drdz_s) / sqrt((double)(1.f + drdz_s*drdz_s)) / (double)gap)
+    // the module-only terms of the strip shift (MiniDoublet.cc:1260-1332),
+    // from the host's float functions when the module table is built: angleB
+    // ((float)(pi / 2) for endcap modules, else atanf(drdz_s)) and the sine
+    // and cosine of angleM for the four quadrants of the anchoring hit (x > 0
+    // and y > 0; x > 0 and y < 0; x < 0 and y < 0; any other)
+    float sh_angle_b;
+    float sh_sin[4], sh_cos[4];
 };
 
 // ------------------------------------------------------------------ math
@@ -232,21 +239,6 @@ static __device__ __noinline__ float g_tan(float x) {
     return x < 0.f ? -r : r;
 }
 
-// (float)(c + (double)a) for the double constants c = M_PI and 2 M_PI (as
-// hi + lo they are 3.6e-15 and 7.1e-15 off; the sum's error is below 2e-13)
-__device__ __forceinline__ bool add_dconst_fast(ffm::ff c, float a, float& r) {
-    return ffm::round_unique(ffm::add(c, a), 2e-13f, r);
-}
-static __device__ __noinline__ float pi_plus(float a) {
-    float r;
-    if (add_dconst_fast(ffm::ff{0x1.921fb6p+1f, -0x1.777a5cp-24f}, a, r)) return r;
-    return (float)(kPi + (double)a);
-}
-static __device__ __noinline__ float two_pi_plus(float a) {
-    float r;
-    if (add_dconst_fast(ffm::ff{0x1.921fb6p+2f, -0x1.777a5cp-23f}, a, r)) return r;
-    return (float)(2 * kPi + (double)a);
-}
 
 // (float)sqrt((double)a*a + (double)b*b)
 static __device__ __noinline__ float hypot_d(float a, float b) {
@@ -510,23 +502,18 @@ __device__ __forceinline__ float dphi_threshold(float rt, float asin_rt1, const 
 __device__ __forceinline__ void shift_anchor(const P3& pix, const ModDev& lm, float& xa, float& ya, float& zn) {
     const bool ps = lm.type == kPS;
     const bool pixLower = lm.ltype == kPixel;
-    const bool isEndcap = lm.subdet == kEndcap;
     const float angleA = fabsf(g_atan(pix.rt / pix.z));
-    const float angleB = isEndcap ? (float)(kPi / 2.) : g_atan(lm.drdz_s);
+    const float angleB = lm.sh_angle_b;  // (float)(pi / 2) for endcap modules
     float sep = lm.gap;
     if (ps && !pixLower) sep *= -1;
     const float sAB = g_sin(angleA + angleB);
     const float drprime = (sep / sAB) * g_sin(angleA);
-    const float slope = lm.slope_s;
-    const float absArctanSlope = (slope != kSdlInf) ? fabsf(g_atan(slope)) : (float)(kPi / 2);
+    // angleM: |atan(slope)| (pi / 2 for the "infinite" slope), pi - it, pi +
+    // it, 2 pi - it by quadrant; its sine and cosine come with the module
     const float xp = pix.x, yp = pix.y;
-    float angleM;
-    if (xp > 0 && yp > 0) angleM = absArctanSlope;
-    else if (xp > 0 && yp < 0) angleM = pi_plus(-absArctanSlope);  // (float)(kPi - (double)a)
-    else if (xp < 0 && yp < 0) angleM = pi_plus(absArctanSlope);
-    else angleM = two_pi_plus(-absArctanSlope);
-    const float dx = drprime * g_sin(angleM);
-    const float dy = drprime * g_cos(angleM);
+    const int q = (xp > 0 && yp > 0) ? 0 : (xp > 0 && yp < 0) ? 1 : (xp < 0 && yp < 0) ? 2 : 3;
+    const float dx = drprime * lm.sh_sin[q];
+    const float dy = drprime * lm.sh_cos[q];
     xa = xp + dx;
     ya = yp + dy;
     const float absdzprime = fabsf(sep / sAB * g_cos(angleA));

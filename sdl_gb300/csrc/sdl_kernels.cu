@@ -1996,20 +1996,42 @@ __device__ __forceinline__ void put_tl(const BatchDev& b, int st, int t, int32_t
     put_sg(b, OJ(b, st, t), o + 4);
 }
 
-__global__ void k_materialize(BatchDev b, int st, int64_t first, int64_t n, int32_t* out) {
+// one row of W hit indices, built in registers, stored with 8- or 16-byte
+// stores when the output is 16-byte aligned
+template <int W>
+__device__ __forceinline__ void store_row(int32_t* o, const int32_t* v, bool vec) {
+    if (vec) {
+        if constexpr (W == 2) {
+            *reinterpret_cast<int2*>(o) = make_int2(v[0], v[1]);
+        } else {
+#pragma unroll
+            for (int i = 0; i < W; i += 4) *reinterpret_cast<int4*>(o + i) = make_int4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < W; ++i) o[i] = v[i];
+    }
+}
+
+template <int kSt>
+__global__ void k_materialize(BatchDev b, int64_t first, int64_t n, int32_t* out) {
+    constexpr int W = kSt == kMD ? 2 : kSt == kSG ? 4 : kSt == kTC ? 16 : 8;
+    const bool vec = (reinterpret_cast<uintptr_t>(out) & 15) == 0;
+    const int ist = (b.flags & kFlagTCFromTP) ? kTP : kTL;  // track candidates: two tracklets or two triplets
     for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
         const int o = (int)(first + k);
-        switch (st) {
-            case kMD: put_md(b, o, out + 2 * k); break;
-            case kSG: put_sg(b, o, out + 4 * k); break;
-            case kTL: put_tl(b, kTL, o, out + 8 * k); break;
-            case kTP: put_tl(b, kTP, o, out + 8 * k); break;
-            default: {  // two tracklets, or two triplets (createTrackCandidatesFromTriplets)
-                const int ist = (b.flags & kFlagTCFromTP) ? kTP : kTL;
-                put_tl(b, ist, OI(b, kTC, o), out + 16 * k);
-                put_tl(b, ist, OJ(b, kTC, o), out + 16 * k + 8);
-            }
+        int32_t v[W];
+        if constexpr (kSt == kMD) {
+            put_md(b, o, v);
+        } else if constexpr (kSt == kSG) {
+            put_sg(b, o, v);
+        } else if constexpr (kSt == kTC) {
+            put_tl(b, ist, OI(b, kTC, o), v);
+            put_tl(b, ist, OJ(b, kTC, o), v + 8);
+        } else {
+            put_tl(b, kSt, o, v);
         }
+        store_row<W>(out + (int64_t)W * k, v, vec);
     }
 }
 
@@ -2432,7 +2454,14 @@ void launch_libm_eval(int fn, uint32_t start, int64_t n, float* out, int n_sm, c
 
 void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s) {
     if (n <= 0) return;
-    k_materialize<<<grid_for(n, 256, b.n_sm * 16), 256, 0, s>>>(b, st, first, n, out);
+    const unsigned g = grid_for(n, 256, b.n_sm * 16);
+    switch (st) {
+        case kMD: k_materialize<kMD><<<g, 256, 0, s>>>(b, first, n, out); break;
+        case kSG: k_materialize<kSG><<<g, 256, 0, s>>>(b, first, n, out); break;
+        case kTL: k_materialize<kTL><<<g, 256, 0, s>>>(b, first, n, out); break;
+        case kTP: k_materialize<kTP><<<g, 256, 0, s>>>(b, first, n, out); break;
+        default: k_materialize<kTC><<<g, 256, 0, s>>>(b, first, n, out);
+    }
 }
 
 }  // namespace sdlg

@@ -108,6 +108,52 @@ def test_graph_and_direct_launch_agree(gpu, oracle_lib):
     assert a == b == c
 
 
+def test_objects_into_pinned_memory(gpu, oracle_lib):
+    """sdlg_get_objects into pinned host memory, 16-byte aligned and not,
+    gives the rows it gives into a fresh array."""
+    from sdl_gb300 import synth
+    det, ev = synth.workload_event("pu", 8, pu=60)
+    run_gpu(gpu, det, [ev, ev], 0)
+    width = (2, 4, 8, 8, 16)
+    for s in range(5):
+        want = gpu.objects(s, -1)
+        n = len(want)
+        assert n > 0
+        raw = gpu.pinned(n * width[s] * 4 + 64)
+        for shift in (0, 4, 8):
+            out = raw[shift:shift + n * width[s] * 4].view(np.int32).reshape(n, width[s])
+            got = gpu.objects(s, -1, out=out)
+            assert np.array_equal(got, want), (s, shift)
+        one = gpu.objects(s, 1, out=raw[16:16 + n * width[s] * 4].view(np.int32).reshape(n, width[s]))
+        assert np.array_equal(one, gpu.objects(s, 1))
+    assert oracle_lib.digest(gpu.objects(4, 0)) == oracle_lib.digest(gpu.objects(4, 1))
+
+
+def test_async_readback_overlaps_the_next_run(gpu, oracle_lib):
+    """sdlg_get_objects_async: the tuples of one batch arrive in pinned
+    memory while the next batch is set and run; a synchronous readback right
+    after an asynchronous one waits for it; both batches' objects are right."""
+    from sdl_gb300 import synth
+    det, ev_a = synth.workload_event("pu", 9, pu=80)
+    _, ev_b = synth.workload_event("pu", 10, pu=120)
+    run_gpu(gpu, det, [ev_a, ev_b], 0)
+    want_a = [gpu.objects(s, -1) for s in range(5)]
+    width = (2, 4, 8, 8, 16)
+    bufs = [gpu.pinned(len(w) * width[s] * 4 + 16)[:len(w) * width[s] * 4].view(np.int32).reshape(len(w), width[s])
+            for s, w in enumerate(want_a)]
+    for s in range(5):
+        assert gpu.objects_async(s, -1, bufs[s]) == len(want_a[s])
+    gpu.set_events([ev_b])
+    gpu.run(4, 0)
+    got_b = gpu.objects(4, 0)  # waits for the pending copies first
+    gpu.wait_objects()
+    for s in range(5):
+        assert np.array_equal(bufs[s], want_a[s]), s
+    ref, _, _ = oracle_lib.Oracle(det).run(ev_b)
+    assert oracle_lib.digest(got_b) == oracle_lib.digest(ref[4])
+    gpu.wait_objects()  # nothing pending: returns at once
+
+
 def test_stop_after_stage(gpu, oracle_lib):
     from sdl_gb300 import synth
     det, ev = synth.workload_event("barrel_flat", 5)
