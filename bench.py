@@ -413,6 +413,7 @@ def main():
         ch.run(4, FLAG_MLP)
     n_pruned = ch.counts(-1)
     mstats = ch.mlp_stats()
+    lists = ch.tl_list_counts()
     # the pruned chain's track candidates per event (for the exact recall)
     pruned_ev = [int(ch.counts(e)[4]) for e in range(len(batch))]
     pruned_tc = tuples.split_by_event(ch.objects(4, -1), pruned_ev)
@@ -501,7 +502,8 @@ def main():
                      "stage_ms": [round(float(v), 3) for v in np.mean(np.array(p_stage), axis=0)],
                      "tl_kernel_ms": round(statistics.fmean(p_tl), 3),
                      "tl_passes_ms": {"enumeration_and_float_cuts": round(float(np.mean([v[0] for v in p_pass])), 3),
-                                      "double_cuts": round(float(np.mean([v[2] for v in p_pass])), 3)}}
+                                      "b2_filter": round(float(np.mean([v[2] for v in p_pass])), 3),
+                                      "double_cuts": round(float(np.mean([v[3] for v in p_pass])), 3)}}
 
     # ---- the chain's other variants on the same events (plain chain, shapes
     # tuned for the module-map chain) ---------------------------------------------
@@ -587,11 +589,16 @@ def main():
     # launch's layout bytes.
     hbm, tflops, src = peaks()
     pf = np.mean(np.array(pf_ms), axis=0)
-    fc_mean, pf_mean, ex_mean = float(pf[0]), float(pf[1]), float(pf[2])
+    fc_mean, pf_mean, bf_mean, ex_mean = float(pf[0]), float(pf[1]), float(pf[2]), float(pf[3])
     n_sg = int(n_pruned[1])
     n_gm = len(batch) * ch.num_modules
     en_alg = 28 * n_sg
-    en_layout = (112 + 44 + 4) * n_sg + 24 * n_gm + 16 * mstats["scored"]
+    en_layout = (112 + 44 + 4) * n_sg + 24 * n_gm + 16 * lists["listed"]
+    # k_tl_b2f (phase B2's single-precision filter over the pre-filter's kept
+    # list): each entry read once (16 B), each segment's 128-byte record read
+    # once, each entry it leaves written once (16 B)
+    bf_alg = 16 * lists["kept"] + 128 * n_sg + 16 * lists["filtered"]
+    bf_achieved = bf_alg / (bf_mean * 1e-3) / 1e9
     en_achieved = en_alg / (fc_mean * 1e-3) / 1e9
     tr = ncu_traffic("tl_enum_traffic.json")
     en_traffic = None
@@ -620,7 +627,15 @@ def main():
                 "candidates_per_s": round(mstats["candidates"] / (fc_mean * 1e-3), 1),
                 "note": "issue-bound candidate evaluation (the ncu capture of this kernel shows issue slots, not DRAM, "
                         "saturated); the algorithmic bytes are small by construction",
-                "prefilter": {"kernel": "k_tl_prefilter (tensor-core pre-filter of the candidates through the float cuts and phase B1)",
+                "b2_filter": {"kernel": "k_tl_b2f (phase B2's single-precision decision on the pre-filter's kept "
+                                        "list; rejects only what the exact phase B2 rejects)",
+                              "kernel_ms": round(bf_mean, 3), "algorithmic_bytes": bf_alg,
+                              "achieved": round(bf_achieved, 3), "peak": hbm, "unit": "GB/s",
+                              "frac": round(bf_achieved / hbm, 6), "entries": lists["kept"],
+                              "left": lists["filtered"],
+                              "entries_per_s": round(lists["kept"] / (bf_mean * 1e-3), 1)},
+                "prefilter": {"kernel": "k_tl_prefilter (tensor-core pre-filter of the candidates through the float cuts "
+                                        "and phase B1's decision)",
                               "kernel_ms": round(pf_mean, 3), "algorithmic_bytes": alg_bytes,
                               "achieved": round(achieved, 3), "peak": hbm, "unit": "GB/s",
                               "frac": round(achieved / hbm, 6), "traffic": traffic,
@@ -665,9 +680,11 @@ def main():
                        "stage_ms": {k: round(float(v), 3) for k, v in zip(("ingest", "MD", "SG", "TL", "TP", "TC"), hl_stage)},
                        "prefilter": {"weights": "sdl_gb300/weights/tl_mlp_pu.npz", "threshold": thr,
                                      "trained_on": "%d events, PU 100-300 (seeds 100000+)" % meta.get("train_events", 0),
-                                     "candidates": mstats["candidates"], "scored_after_float_cuts_and_b1": mstats["scored"],
+                                     "candidates": mstats["candidates"],
+                                     "scored_after_float_cuts_and_b1": mstats["scored"],
                                      "kept": mstats["kept"],
-                                     "pruned_fraction": round(1.0 - mstats["kept"] / max(1, mstats["scored"]), 4)},
+                                     "pruned_fraction": round(1.0 - mstats["kept"] / max(1, mstats["scored"]), 4),
+                                     "left_by_b2_filter": lists["filtered"]},
                        "wall_s": round(wall, 3)},
             "tc_recall": round(tc_rec, 5), "tl_recall": round(tl_rec, 5),
             "recall_method": "track candidates: |pruned & plain| / |plain| over the hit-index tuple multisets, event "

@@ -63,6 +63,9 @@ extern "C" {
 #define SDLG_FLAG_TC_FROM_TP 128 /* track candidates from two triplets and a trial segment between them:
                                     Event::createTrackCandidatesFromTriplets (Event.cc:874-982); the objects
                                     of stage 4 are then pairs of triplets (hit tuples of width 16 as before) */
+#define SDLG_FLAG_NO_B2_FILTER 256 /* the exact phases B1 and B2 judge every survivor of the enumeration (or
+                                    * of the pre-filter), without the single-precision phase-B2 filter
+                                    * ahead of them (the same tracklets; no counterpart in the reference) */
 #define SDLG_FLAG_TEST_MLP_GIVE_UP 4096 /* self-test of a failure path (no counterpart in the reference): with
                                     SDLG_FLAG_MLP, the pre-filter's first tensor-core wait in each CTA gives up at
                                     once, as a wait that ran out of time would; the run fails with SDLG_ERR_CUDA,
@@ -276,10 +279,20 @@ int sdlg_last_kernel_times(sdlg_ctx* ctx, float* out5);
 int sdlg_autotune(sdlg_ctx* ctx, int stop_after, int flags, int32_t* out10);
 
 /* Device time (ms) of the last run's tracklet passes (no counterpart in the
- * reference): the enumeration with the float part of the cuts, the
- * pre-filter (0 without SDLG_FLAG_MLP), and the double-precision part of the
- * cuts; zeros for a run that stopped before the tracklets. */
+ * reference): the enumeration with the float part of the cuts, the filters
+ * (with SDLG_FLAG_MLP the pre-filter, then phase B2's single-precision
+ * decision), and the double-precision part of the cuts; zeros for a run that
+ * stopped before the tracklets.  sdlg_last_tl_pass_times4 gives the two
+ * filters apart: enumeration, pre-filter, phase-B2 filter, exact cuts. */
 int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3);
+int sdlg_last_tl_pass_times4(sdlg_ctx* ctx, float* out4);
+
+/* Entries of the last run's tracklet candidate lists (no counterpart in the
+ * reference): the enumeration's phase-A survivors, those the pre-filter kept
+ * (0 without SDLG_FLAG_MLP), and what the single-precision phase-B2 filter
+ * left of the list before it (that list's length without the filter), which
+ * the exact phases judge. */
+int sdlg_last_tl_list_counts(sdlg_ctx* ctx, int64_t* out3);
 
 /* Self-check of the float-float evaluations that stand for the reference's
  * double sub-expressions (no counterpart in the reference).  Function fn
@@ -324,6 +337,17 @@ int sdlg_libm_stats(int fn, uint64_t* out3);
  * decisions settled alone, candidates that needed an exact evaluation, and
  * candidates settled differently from the exact cuts (must be 0). */
 int sdlg_tl_phase_a_check(sdlg_ctx* ctx, uint64_t* out4);
+
+/* Self-check of the single-precision phase-B2 filter (no counterpart in the
+ * reference): after a run through the tracklet stage, every entry of the
+ * enumeration's survivor list is judged by the filter and by the exact phases
+ * B1 and B2.  out10: entries; through exact phase B1; through exact phases B1
+ * and B2; rejected by the filter; rejected by the filter but through the exact
+ * phases (must be 0); rejected by the filter among those through exact phase
+ * B1; the largest |filter value - exact value| / the filter's bound for
+ * deltaBeta, dBetaCut2 and betaOut (as float bits; below 1 when the bounds
+ * hold); entries the filter left before reaching the cuts. */
+int sdlg_tl_b2_filter_check(sdlg_ctx* ctx, uint64_t* out10);
 
 /* Number of kernels one run of the chain launches (as last enqueued). */
 int64_t sdlg_last_launches(const sdlg_ctx* ctx);

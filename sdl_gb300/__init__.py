@@ -35,6 +35,7 @@ FLAG_MLP = 16        # learned pre-filter ahead of the tracklet cuts
 FLAG_TL_NAV = 32     # Event::createTrackletsViaNavigation instead of createTrackletsWithModuleMap
 FLAG_TC_FROM_TL = 64   # Event::createTrackCandidatesFromTracklets instead of createTrackCandidates
 FLAG_TC_FROM_TP = 128  # Event::createTrackCandidatesFromTriplets instead of createTrackCandidates
+FLAG_NO_B2_FILTER = 256  # without the single-precision phase-B2 filter (same tracklets)
 FLAG_TEST_MLP_GIVE_UP = 4096  # self-test: the pre-filter's first tensor-core wait gives up at once
 # the columns of Chain.tracklet_vars (the reference's Tracklet recovars keys)
 TL_VAR_NAMES = ("betaIn", "betaInRHmin", "betaInRHmax", "betaOut", "betaOutRHmin", "betaOutRHmax", "betaAv", "pt_beta",
@@ -81,6 +82,9 @@ def lib():
         L.sdlg_last_times.argtypes = [vp, vp]
         L.sdlg_last_kernel_times.argtypes = [vp, vp]
         L.sdlg_last_tl_pass_times.argtypes = [vp, vp]
+        L.sdlg_last_tl_pass_times4.argtypes = [vp, vp]
+        L.sdlg_tl_b2_filter_check.argtypes = [vp, vp]
+        L.sdlg_last_tl_list_counts.argtypes = [vp, vp]
         L.sdlg_math_check.argtypes = [vp, i32, i32, ctypes.c_uint64, i64, ctypes.c_uint64, vp]
         L.sdlg_tl_phase_a_check.argtypes = [vp, vp]
         L.sdlg_autotune.argtypes = [vp, i32, i32, vp]
@@ -513,10 +517,30 @@ class Chain:
 
     def tl_pass_times(self) -> np.ndarray:
         """Device ms of the last run's tracklet passes: enumeration + float cuts,
-        the pre-filter (0 without FLAG_MLP), the double-precision cuts."""
-        out = np.zeros(3, dtype=np.float32)
-        self._ck(lib().sdlg_last_tl_pass_times(self.h, out.ctypes.data))
+        the pre-filter (0 without FLAG_MLP), the single-precision phase-B2
+        filter, the double-precision cuts."""
+        out = np.zeros(4, dtype=np.float32)
+        self._ck(lib().sdlg_last_tl_pass_times4(self.h, out.ctypes.data))
         return out
+
+    def tl_list_counts(self) -> dict:
+        """Entries of the last run's tracklet candidate lists: phase-A survivors,
+        those the pre-filter kept (0 without FLAG_MLP), and what the phase-B2
+        filter left of the list before it (the exact phases' input)."""
+        out = np.zeros(3, dtype=np.int64)
+        self._ck(lib().sdlg_last_tl_list_counts(self.h, out.ctypes.data))
+        return {"listed": int(out[0]), "kept": int(out[1]), "filtered": int(out[2])}
+
+    def tl_b2_filter_check(self) -> dict:
+        """Self-check of the single-precision phase-B2 filter over the last
+        run's phase-A survivors against the exact phases B1 and B2."""
+        out = np.zeros(10, dtype=np.uint64)
+        self._ck(lib().sdlg_tl_b2_filter_check(self.h, out.ctypes.data))
+        r = out[6:9].astype(np.uint32).view(np.float32)
+        return {"entries": int(out[0]), "b1_pass": int(out[1]), "b2_pass": int(out[2]), "rejected": int(out[3]),
+                "violations": int(out[4]), "rejected_of_b1_pass": int(out[5]),
+                "bound_ratio": {"dbeta": float(r[0]), "cut2": float(r[1]), "betaout": float(r[2])},
+                "undecided_early": int(out[9])}
 
     def autotune(self, stop_after: int = 4, flags: int = 0) -> dict:
         """Pick the fastest launch shape per stage on the current batch (kept for later runs)."""

@@ -403,6 +403,8 @@ int ensure_buffers(sdlg_ctx* ctx) {
     AL(b.passa, b.kept_cap);
     AL(b.kept, b.kept_cap);
     AL(b.n_kept2, 1);
+    AL(b.passf, b.kept_cap);
+    AL(b.n_keptf, 1);
     AL(b.pb, b.kept_cap);
     AL(b.n_pb, 2);
     AL(b.sgpack, ctx->cap_obj[kSG] * PK_N);
@@ -768,7 +770,7 @@ int sdlg_create(sdlg_ctx** out, int device) {
         e = cudaEventCreate(&ctx->hooks.enum_start[k]);
         if (e == cudaSuccess) e = cudaEventCreate(&ctx->hooks.enum_stop[k]);
     }
-    for (int k = 0; k < 2; ++k)
+    for (int k = 0; k < 3; ++k)
         if (e == cudaSuccess) e = cudaEventCreate(&ctx->hooks.tl_mid[k]);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_small, 16 * sizeof(int64_t));
     // the host libm's float functions for the cut arithmetic (once per process / device)
@@ -823,7 +825,7 @@ int sdlg_destroy(sdlg_ctx* ctx) {
         if (ctx->hooks.enum_start[k]) cudaEventDestroy(ctx->hooks.enum_start[k]);
         if (ctx->hooks.enum_stop[k]) cudaEventDestroy(ctx->hooks.enum_stop[k]);
     }
-    for (int k = 0; k < 2; ++k)
+    for (int k = 0; k < 3; ++k)
         if (ctx->hooks.tl_mid[k]) cudaEventDestroy(ctx->hooks.tl_mid[k]);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -1399,16 +1401,65 @@ int sdlg_autotune(sdlg_ctx* ctx, int stop_after, int flags, int32_t* out10) {
     return SDLG_OK;
 }
 
-int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3) {
-    if (!ctx || !out3) return SDLG_ERR_ARG;
+int sdlg_last_tl_pass_times4(sdlg_ctx* ctx, float* out4) {
+    if (!ctx || !out4) return SDLG_ERR_ARG;
     if (!ctx->ran) return fail(ctx, SDLG_ERR_NO_EVENTS, "chain not run");
-    out3[0] = out3[1] = out3[2] = 0.f;
+    out4[0] = out4[1] = out4[2] = out4[3] = 0.f;
     if (ctx->last_stop < kTL) return SDLG_OK;
     cudaSetDevice(ctx->device);
     CK(cudaEventSynchronize(ctx->hooks.enum_stop[kTL]));
-    CK(cudaEventElapsedTime(&out3[0], ctx->hooks.enum_start[kTL], ctx->hooks.tl_mid[0]));
-    CK(cudaEventElapsedTime(&out3[1], ctx->hooks.tl_mid[0], ctx->hooks.tl_mid[1]));
-    CK(cudaEventElapsedTime(&out3[2], ctx->hooks.tl_mid[1], ctx->hooks.enum_stop[kTL]));
+    CK(cudaEventElapsedTime(&out4[0], ctx->hooks.enum_start[kTL], ctx->hooks.tl_mid[0]));
+    CK(cudaEventElapsedTime(&out4[1], ctx->hooks.tl_mid[0], ctx->hooks.tl_mid[1]));
+    CK(cudaEventElapsedTime(&out4[2], ctx->hooks.tl_mid[1], ctx->hooks.tl_mid[2]));
+    CK(cudaEventElapsedTime(&out4[3], ctx->hooks.tl_mid[2], ctx->hooks.enum_stop[kTL]));
+    return SDLG_OK;
+}
+
+int sdlg_last_tl_pass_times(sdlg_ctx* ctx, float* out3) {
+    if (!out3) return SDLG_ERR_ARG;
+    float t[4];
+    const int rc = sdlg_last_tl_pass_times4(ctx, t);
+    if (rc) return rc;
+    out3[0] = t[0];
+    out3[1] = t[1] + t[2];
+    out3[2] = t[3];
+    return SDLG_OK;
+}
+
+int sdlg_last_tl_list_counts(sdlg_ctx* ctx, int64_t* out3) {
+    if (!ctx || !out3) return SDLG_ERR_ARG;
+    if (!ctx->ran) return fail(ctx, SDLG_ERR_NO_EVENTS, "chain not run");
+    out3[0] = out3[1] = out3[2] = 0;
+    if (ctx->last_stop < kTL) return SDLG_OK;
+    cudaSetDevice(ctx->device);
+    unsigned long long h[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(&h[0], ctx->b.n_kept, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(&h[1], ctx->b.n_keptf, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(&h[2], ctx->b.n_kept2, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const bool filt = !(ctx->last_flags & (SDLG_FLAG_TL_NM1 | SDLG_FLAG_NO_B2_FILTER));
+    const bool mlp = (ctx->last_flags & SDLG_FLAG_MLP) != 0;
+    out3[0] = (int64_t)h[0];
+    out3[1] = mlp ? (int64_t)h[2] : 0;
+    out3[2] = filt ? (int64_t)h[1] : out3[mlp ? 1 : 0];
+    return SDLG_OK;
+}
+
+int sdlg_tl_b2_filter_check(sdlg_ctx* ctx, uint64_t* out10) {
+    if (!ctx || !out10) return SDLG_ERR_ARG;
+    if (!ctx->ran || ctx->last_stop < kTL) return fail(ctx, SDLG_ERR_ARG, "run the chain through the tracklet stage first");
+    cudaSetDevice(ctx->device);
+    unsigned long long* d = nullptr;
+    cudaError_t e = cudaMallocAsync((void**)&d, 10 * sizeof(unsigned long long), ctx->stream);
+    if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "cudaMallocAsync: %s", cudaGetErrorString(e));
+    CK(cudaMemsetAsync(d, 0, 10 * sizeof(unsigned long long), ctx->stream));
+    launch_tl_b2q_check(ctx->b, d, ctx->stream);
+    CK(cudaGetLastError());
+    unsigned long long h[10];
+    CK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(d, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int k = 0; k < 10; ++k) out10[k] = h[k];
     return SDLG_OK;
 }
 

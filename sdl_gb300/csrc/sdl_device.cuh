@@ -1502,6 +1502,314 @@ static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict
     return tl_phaseB2_sgv<kSet>(algo, load_sgv(pack, s), load_sgv(pack, t), mulsF, nm1);
 }
 
+// ---- Phase B2's decision from single-precision approximations: a filter
+// ahead of the exact phases B1 and B2 (no counterpart in the reference).  The
+// directions come from atan2f and the deltaBeta iterations' functions from
+// asinf and __sinf (CUDA: at most 3 and 2 ulp, and 2^-21.41 absolute on
+// [-pi, pi]) instead of the host libm and the double sub-expressions; every
+// other input is the exact code's own float (the packed segment fields, dr,
+// sdOut_d, the luminous-region terms, dBetaRes, the alpha terms of the BBEE
+// and EEEE algorithms).  Each compared quantity carries a bound on its
+// distance to the exact value, propagated through the iterations with the
+// derivatives of asin and 1/sin, and every bound is taken kB2qSafety times at
+// the decisions: a candidate is rejected only when a cut fails by more than
+// that, and a branch condition within its bound, a non-finite value or an
+// angle too close to the wrap at +-pi leaves it to the exact phases.  So the
+// tracklets do not change; the filter only spares the exact phases the
+// candidates that certainly fail.  Returns 0 (phase B2 rejects the candidate)
+// or 1 (not decided here); with kDefer, 2 for the entries whose evaluation
+// takes the long branches (BBEE and EEEE, and BBBB with a 2S endcap outer
+// anchor, about one entry in six), which a second pass evaluates on full
+// warps instead of holding a warp of the common case for one lane.
+constexpr float kB2qSafety = 4.f;
+constexpr float kB2qDir = 2e-6f;  // a direction difference from atan2f: 3 ulp of pi, the exact value's rounding, the wrap
+constexpr float kB2qSin = 4e-7f;  // __sinf on [-pi, pi]: absolute error below 2^-21.41 (CUDA)
+__device__ __forceinline__ float ulp_of(float x) { return fabsf(x) * 0x1p-23f + 0x1p-126f; }
+// (the bounds' own arithmetic uses __fdividef and rsqrtf, within 2 and 2 ulp,
+// and widens its results by a relative 1e-6; the few quantities the exact
+// code computes with the same float operations keep IEEE division)
+
+// the exact code's dphi(a, b) = phi_mpi_pi(b - a) of two directions in
+// [-pi, pi] (one of them approximate); false near the wrap at +-pi
+__device__ __forceinline__ bool dphi_q(float a, float b, float& d) {
+    float v = b - a;
+    if (v >= kPiF) v -= 2.f * kPiF;
+    else if (v < -kPiF) v += 2.f * kPiF;
+    d = v;
+    return fabsf(fabsf(v) - kPiF) > 1e-4f;
+}
+
+// pt = D / sin(b) (approximate) and bounds [lo, hi] of |D / sin(b')| over
+// every b' within e of b
+__device__ __forceinline__ float pt_range(float D, float b, float e, float& lo, float& hi) {
+    const float sb = __sinf(b), s = fabsf(sb);  // |b| <= pi here
+    const float es = e + kB2qSin + 2.f * ulp_of(s) + 1e-30f;
+    lo = __fdividef(D, s + es) * (1.f - 1e-6f);
+    hi = s > es ? __fdividef(D, s - es) * (1.f + 1e-6f) : __int_as_float(0x7f800000);
+    return __fdividef(D, sb);
+}
+// 1: |pt| < c for every pt in [lo, hi]; 0: for none; -1: not decided
+__device__ __forceinline__ int pt_below(float lo, float hi, float c) { return hi < c ? 1 : (lo >= c ? 0 : -1); }
+
+// one update of the deltaBeta iterations, asin(min(a / |pt|, 0.95)) with a =
+// sd_dr * k, for |pt| = p (approximate) within [lo, hi]: value and bound
+__device__ __forceinline__ float b2q_update(float a, float p, float lo, float hi, float& e) {
+    const float arg = fmin_ref(__fdividef(a, fabsf(p)), kSinAlphaMax);
+    const float alo = fmin_ref(__fdividef(a, hi) * (1.f - 1e-6f), kSinAlphaMax);
+    const float ahi = fmin_ref(__fdividef(a, lo) * (1.f + 1e-6f), kSinAlphaMax);
+    const float earg = fmaxf(ahi - arg, arg - alo) + 2.f * ulp_of(arg);
+    const float v = asinf(arg);
+    // asin' <= 1 / sqrt(1 - 0.95^2) = 3.2026 on [0, 0.95]
+    const float slope = rsqrtf(fmaxf(1.f - ahi * ahi, 0.0975f)) * (1.f + 1e-6f);
+    e = earg * slope + 3.f * ulp_of(v);
+    return v;
+}
+
+// the filter's values and bounds (for the self-check)
+struct B2Quick {
+    float dbeta, e_dbeta, cut2, e_cut2, bout, e_bout, bout_cut, e_bout_cut;
+    bool complete;  // the function reached the cuts
+};
+
+template <bool kDefer = false>
+__device__ __forceinline__ int tl_b2_quick(int algo, const SGV& S, const SGV& T, B2Quick* q = nullptr) {
+    constexpr float K = kB2qSafety;
+    const float pt_betaMax = 7.0f;
+    if (q) q->complete = false;
+    if (kDefer && (algo != kAlgoBBBB || ((T.flags & F_UP_E) && (T.flags & F_UP_2S)))) return 2;
+    // axis = OutUp - InLo: the float differences and IEEE square root of sub()
+    const float ax = T.ux - S.lx, ay = T.uy - S.ly;
+    const float dr = __fsqrt_rn(__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(ay, ay)));
+    if (!(dr > 1e-3f && dr < 1e5f)) return 1;
+    const float axphi = atan2f(ay, ax);
+    float d;
+    if (!dphi_q(S.lphi, axphi, d)) return 1;
+    const float betaIn0 = S.dpc - d;
+    const float eIn = kB2qDir + ulp_of(betaIn0);
+    const float sdIn_dr = S.rtseg, sdOut_dr = T.rtseg;
+    const float sdIn_d = S.urt - S.lrt, sdOut_d = T.urt - T.lrt;
+    const float alphaIn = S.dpc;
+    if (!dphi_q(T.uphi, axphi, d)) return 1;
+    float betaOut0, eOut, inMin, inMax, outMin, outMax, eInRH, eOutRH, alphaOutReg;
+    float dBetaROut2 = 0.f, eROut2 = 0.f;
+    int lIn, lOut;
+    // (rt - rt') * sin(dPhi(midpoint(InLo, OutLo), OutLo - InLo)) / dr with an
+    // approximate sine: value of the square and its bound
+    auto rout2 = [&](float drt, float& e2) -> bool {
+        const float mx = (0.f + S.lx + T.lx) / 2.f, my = (0.f + S.ly + T.ly) / 2.f;
+        float dm;
+        if (!dphi_q(atan2f(my, mx), atan2f(T.ly - S.ly, T.lx - S.lx), dm)) return false;
+        const float sd = __sinf(dm);
+        const float rr = __fdividef(drt * sd, dr);
+        // (both directions approximate)
+        const float err = __fdividef(fabsf(drt), dr) * (2.f * kB2qDir + kB2qSin + 2.f * ulp_of(sd)) * (1.f + 1e-6f) +
+                          4.f * ulp_of(rr);
+        dBetaROut2 = rr * rr;
+        e2 = 2.f * fabsf(rr) * err + err * err + ulp_of(dBetaROut2);
+        return true;
+    };
+    if (algo == kAlgoBBBB) {
+        // Tracklet.cc:1205-1538
+        betaOut0 = -T.alphaup + d;
+        eOut = kB2qDir + ulp_of(betaOut0);
+        inMin = inMax = betaIn0;
+        eInRH = eIn;
+        const bool ec2s = (T.flags & F_UP_E) && (T.flags & F_UP_2S);
+        if (ec2s) {
+            // the strip-edge points of the outer anchor (edge_point's float sums)
+            const float hx = T.ux + T.ex, hy = T.uy + T.ey, lx = T.ux + -T.ex, ly = T.uy + -T.ey;
+            const float hphi = atan2f(hy, hx), lphi = atan2f(ly, lx);
+            float d1, d2, d3, d4;
+            if (!dphi_q(hphi, atan2f(hy - T.ly, hx - T.lx), d1) || !dphi_q(hphi, atan2f(hy - S.ly, hx - S.lx), d2) ||
+                !dphi_q(lphi, atan2f(ly - T.ly, lx - T.lx), d3) || !dphi_q(lphi, atan2f(ly - S.ly, lx - S.lx), d4))
+                return 1;
+            outMin = -d1 + d2;
+            outMax = -d3 + d4;
+            eOutRH = 4.f * kB2qDir + ulp_of(outMin) + ulp_of(outMax);
+            const float hrt = __fsqrt_rn(__fadd_rn(__fmul_rn(hx, hx), __fmul_rn(hy, hy)));
+            const float lrt = __fsqrt_rn(__fadd_rn(__fmul_rn(lx, lx), __fmul_rn(ly, ly)));
+            if (!rout2(hrt - lrt, eROut2)) return 1;
+        } else {
+            outMin = outMax = betaOut0;
+            eOutRH = eOut;
+        }
+        alphaOutReg = T.dpc;
+        lIn = 5;
+        lOut = ec2s ? 11 : 5;
+    } else if (algo == kAlgoBBEE) {
+        // Tracklet.cc:1765-2016 (the alpha terms are the exact code's floats)
+        const float aOut = T.alphaup;
+        const float aMin = phi_mpi_pi(T.dpminc - T.dpmin), aMax = phi_mpi_pi(T.dpmaxc - T.dpmax);
+        betaOut0 = -aOut + d;
+        eOut = kB2qDir + ulp_of(betaOut0);
+        inMin = inMax = betaIn0;
+        eInRH = eIn;
+        outMin = betaOut0 - aMin + aOut;
+        outMax = betaOut0 - aMax + aOut;
+        eOutRH = eOut + 2.f * ulp_of(fabsf(outMin) + fabsf(outMax) + fabsf(aOut));
+        if (T.flags & F_UP_2S) {
+            const float hrt = edge_rt(T.ux, T.uy, T.ex, T.ey, true), lrt = edge_rt(T.ux, T.uy, T.ex, T.ey, false);
+            if (!rout2(hrt - lrt, eROut2)) return 1;
+        }
+        alphaOutReg = S.dpc;
+        lIn = 5;
+        lOut = 11;
+    } else if (algo == kAlgoEEEE) {
+        // Tracklet.cc:2220-2665
+        const float dPhiPos = T.dphilu;
+        const float aOutMin = phi_mpi_pi(T.dpminc - dPhiPos), aOutMax = phi_mpi_pi(T.dpmaxc - dPhiPos);
+        const float aOut = phi_mpi_pi(T.dpc - dPhiPos);
+        betaOut0 = -aOut + d;
+        eOut = kB2qDir + ulp_of(betaOut0);
+        inMin = betaIn0 + S.dpminc - alphaIn;
+        inMax = betaIn0 + S.dpmaxc - alphaIn;
+        eInRH = eIn + 2.f * ulp_of(fabsf(inMin) + fabsf(inMax) + fabsf(alphaIn));
+        outMin = betaOut0 - aOutMin + aOut;
+        outMax = betaOut0 - aOutMax + aOut;
+        eOutRH = eOut + 2.f * ulp_of(fabsf(outMin) + fabsf(outMax) + fabsf(aOut));
+        alphaOutReg = S.dpc;
+        lIn = 11;
+        lOut = 13;
+    } else {
+        return 1;
+    }
+    // ---- the deltaBeta iterations (Tracklet.cc:3181-3324) with bounds
+    const float D = dr * k2Rinv1GeVf;
+    const float aIn = sdIn_dr * k2Rinv1GeVf, aOut = sdOut_dr * k2Rinv1GeVf;
+    float betaIn = betaIn0, betaOut = betaOut0, eBi = eIn, eBo = eOut;
+    if (!(fabsf(betaIn) < 1.5f && fabsf(betaOut) < 1.5f)) return 1;  // keeps every pt_range argument within pi
+    float betaAv = 0.5f * (betaIn + betaOut);
+    float eAv = 0.5f * (eBi + eBo) + ulp_of(betaAv);
+    float lo, hi;
+    float pt = pt_range(D, betaAv, K * eAv, lo, hi);
+    const int ptc = pt_below(lo, hi, (lIn >= 11 ? 8.f : 4.f) * pt_betaMax);
+    const int same = (fabsf(betaIn) > K * eBi && fabsf(betaOut) > K * eBo) ? ((betaIn > 0.f) == (betaOut > 0.f)) : -1;
+    int mode;  // 1, 2 or 0 (no update)
+    if (same == 1 && ptc == 1) mode = 1;
+    else if (same == 0 || ptc == 0) mode = 0;
+    else return 1;
+    if (mode == 0 && lIn < 11) {
+        // (double)|betaOut| < 0.2 (double)|betaIn| && |pt| < 12 pt_betaMax
+        const float slack = 1e-7f * fabsf(betaIn);
+        const int small = (fabsf(betaOut) + K * eBo < 0.2f * (fabsf(betaIn) - K * eBi) - slack)
+                              ? 1
+                              : ((fabsf(betaOut) - K * eBo > 0.2f * (fabsf(betaIn) + K * eBi) + slack) ? 0 : -1);
+        const int ptc2 = pt_below(lo, hi, 12.f * pt_betaMax);
+        if (small == 1 && ptc2 == 1) mode = 2;
+        else if (!(small == 0 || ptc2 == 0)) return 1;
+    }
+    if (mode == 1) {
+        float e1, e2;
+        const float uIn = b2q_update(aIn, pt, lo, hi, e1), uOut = b2q_update(aOut, pt, lo, hi, e2);
+        const float bIn1 = betaIn + copysignf(uIn, betaIn), bOut1 = betaOut + copysignf(uOut, betaOut);
+        const float av1 = 0.5f * (bIn1 + bOut1);
+        const float eAv1 = 0.5f * (eBi + e1 + eBo + e2) + ulp_of(bIn1) + ulp_of(bOut1) + ulp_of(av1);
+        float lo1, hi1;
+        const float p1 = pt_range(D, av1, K * eAv1, lo1, hi1);
+        const float vIn = b2q_update(aIn, p1, lo1, hi1, e1), vOut = b2q_update(aOut, p1, lo1, hi1, e2);
+        betaIn = betaIn + copysignf(vIn, betaIn);
+        betaOut = betaOut + copysignf(vOut, betaOut);
+        eBi = eBi + e1 + ulp_of(betaIn);
+        eBo = eBo + e2 + ulp_of(betaOut);
+    } else if (mode == 2) {
+        // the sign of betaIn is certain here (|betaIn| > 5 |betaOut| + the bounds)
+        float loI, hiI;
+        const float pI = pt_range(D, betaIn, K * eBi, loI, hiI);
+        float e1, e2;
+        const float uIn = b2q_update(aIn, pI, loI, hiI, e1);
+        // |betaOut| > 0.2f |betaIn| is false here, so betaAv = betaInUpd (betaOutUpd is unused)
+        const float av1 = betaIn + copysignf(uIn, betaIn);
+        const float eAv1 = eBi + e1 + ulp_of(av1);
+        float lo1, hi1;
+        const float p1 = pt_range(D, av1, K * eAv1, lo1, hi1);
+        const float vIn = b2q_update(aIn, p1, lo1, hi1, e1), vOut = b2q_update(aOut, p1, lo1, hi1, e2);
+        betaIn = betaIn + copysignf(vIn, betaIn);
+        betaOut = betaOut + copysignf(vOut, betaIn);
+        eBi = eBi + e1 + ulp_of(betaIn);
+        eBo = eBo + e2 + ulp_of(betaOut);
+    }
+    if (mode != 0) {
+        betaAv = 0.5f * (betaIn + betaOut);
+        eAv = 0.5f * (eBi + eBo) + ulp_of(betaAv);
+        pt = pt_range(D, betaAv, K * eAv, lo, hi);
+    }
+    // ---- the cut values
+    // betaRH * (2 beta / |RHmin + RHmax|): the spread |RHmin - RHmax| scaled
+    auto spread = [&](float mn, float mx, float eRH, float beta, float eBeta, float& e) -> bool {
+        if (mn == mx) {  // the same float in both codes: the difference is 0
+            e = 0.f;
+            return true;
+        }
+        const float sum = fabsf(mn + mx), eSum = 2.f * eRH + ulp_of(sum);
+        if (!(sum > 2.f * K * eSum)) return false;
+        const float m = 2.f * beta / sum;
+        const float eM = __fdividef(2.f * eBeta + fabsf(m) * eSum, sum - K * eSum) * (1.f + 1e-6f) + 2.f * ulp_of(m);
+        const float s = fabsf(mn * m - mx * m);
+        const float eD = 2.f * eRH;
+        e = fabsf(mn - mx) * eM + fabsf(m) * eD + eD * eM + 3.f * ulp_of(fabsf(mn * m) + fabsf(mx * m));
+        return s == s;
+    };
+    float eTin, eTout;
+    if (!spread(inMin, inMax, eInRH, betaIn, eBi, eTin) || !spread(outMin, outMax, eOutRH, betaOut, eBo, eTout)) return 1;
+    float tIn = 0.f, tOut = 0.f;
+    if (inMin != inMax) {
+        const float m = 2.f * betaIn / fabsf(inMin + inMax);
+        tIn = fabsf(inMin * m - inMax * m);
+    }
+    if (outMin != outMax) {
+        const float m = 2.f * betaOut / fabsf(outMin + outMax);
+        tOut = fabsf(outMin * m - outMax * m);
+    }
+    const float t = tIn + tOut, eT = eTin + eTout + ulp_of(t);
+    // the multiple-scattering factor: phase A's approximation (relative 11 * 2^-24)
+    const float dd = T.lrt - S.lrt;
+    if (!(dd >= 0.f && dd < 1e4f)) return 1;
+    const float u = __fadd_rn(0.1f, __fmul_rn(dd, 0.004f));
+    const float mulsF = __fmul_rn(__fmul_rn(0.015f, __fmul_rn(u, rsqrtf(u))), algo == kAlgoEEEE ? 1.f : S.sqq_hi);
+    const float rMuls = 2e-6f;
+    const float ptm = fmin_ref(fabsf(pt), pt_betaMax);
+    const float ptmLo = fminf(lo, pt_betaMax), ptmHi = fminf(hi, pt_betaMax);
+    if (!(ptmLo > 0.f)) return 1;
+    const float rPt = __fdividef(fmaxf(ptmHi - ptm, ptm - ptmLo) + ulp_of(ptm), ptmLo) * (1.f + 1e-6f);
+    const float dBetaMuls = __fdividef(mulsF * 4.f, ptm);
+    const float eMuls = dBetaMuls * (K * rMuls + rPt) * (1.f + K * rMuls + rPt) + 4.f * ulp_of(dBetaMuls);
+    // the luminous-region terms and dBetaRes: the exact code's floats
+    const float alphaInAbsReg = fmax_ref(fabsf(alphaIn), S.la3);
+    const float alphaOutAbsReg = fmax_ref(fabsf(alphaOutReg), T.la3);
+    const float dBetaInLum = lIn < 11 ? 0.0f : fabsf(alphaInAbsReg * kDeltaZLum / S.lz);
+    const float dBetaOutLum = lOut < 11 ? 0.0f : fabsf(alphaOutAbsReg * kDeltaZLum / T.lz);
+    const float dBetaLum2 = (dBetaInLum + dBetaOutLum) * (dBetaInLum + dBetaOutLum);
+    const float ey = 2.f * dBetaMuls * eMuls + eMuls * eMuls;
+    // betaOut_cut = asin(min(dr k / ptCut, 0.95)) + 0.02 / sdOut_d + sqrt(dBetaLum2 + dBetaMuls^2)
+    const float x = asinf(fmin_ref(dr * k2Rinv1GeVf / kPtCut, kSinAlphaMax)) + (0.02f / sdOut_d);
+    const float ex = 3.f * ulp_of(1.3f) + ulp_of(x);
+    const float y = dBetaLum2 + dBetaMuls * dBetaMuls;
+    const float eY = ey + 2.f * ulp_of(y);
+    const float sy = y > 0.f ? y * rsqrtf(y) : 0.f;
+    const float eS = (y > 2.f * K * eY ? __fdividef(K * eY, sy) : sqrtf(K * eY)) * (1.f + 1e-6f);
+    const float boutCut = x + sy;
+    const float eBoutCut = K * ex + eS + 2.f * ulp_of(boutCut) + 4.f * ulp_of(sy);
+    const float dBetaRes = 0.02f / fmin_ref(sdOut_d, sdIn_d);
+    const float head = dBetaRes * dBetaRes * 2.0f + dBetaMuls * dBetaMuls + dBetaLum2 + dBetaROut2;
+    const float eHead = ey + eROut2 + 5.f * ulp_of(head);
+    const float cut2 = head + 0.25f * t * t;
+    const float eCut2 = eHead + 0.5f * t * eT + 0.25f * eT * eT + 3.f * ulp_of(cut2);
+    const float dBeta = betaIn - betaOut;
+    const float eD = eBi + eBo + ulp_of(dBeta);
+    if (q) {
+        q->dbeta = dBeta; q->e_dbeta = eD; q->cut2 = cut2; q->e_cut2 = eCut2;
+        q->bout = betaOut; q->e_bout = eBo; q->bout_cut = boutCut; q->e_bout_cut = eBoutCut;
+        q->complete = true;
+    }
+    if (!(dBeta == dBeta && cut2 == cut2 && boutCut == boutCut && betaOut == betaOut)) return 1;
+    // betaOut cut: rejected when |betaOut| >= betaOut_cut
+    if (fabsf(betaOut) - K * eBo >= boutCut + K * eBoutCut) return 0;
+    // deltaBeta cut: rejected when dBeta^2 > dBetaCut2 (the square rounded to float)
+    const float lowD = fabsf(dBeta) - K * eD;
+    if (lowD > 0.f && lowD * lowD * (1.f - 0x1p-21f) > cut2 + K * eCut2) return 0;
+    return 1;
+}
+
 // phase B in one call (phase B1, then phase B2 on its survivors)
 __device__ __forceinline__ bool tl_phaseB(int algo, const float* __restrict__ pack, int s, int t, float sdlCut, float mulsF,
                                           bool nm1) {

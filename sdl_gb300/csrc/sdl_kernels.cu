@@ -1427,6 +1427,110 @@ __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
     mlp_teardown(sm, st);
 }
 
+// Phase B2's single-precision decision (tl_b2_quick, no counterpart in the
+// reference) on a survivor list (in / n_in: the enumeration's, or the
+// pre-filter's kept list): the entries it cannot reject go to the filtered
+// list (n_keptf entries, same format), which phase B1 reads.  Exact phase B2
+// passes about one in thirteen of the enumeration's entries, so the filter
+// spares the exact phases (float-float arithmetic and the host libm's
+// functions) most of their work; the tracklets do not change.  Each warp
+// takes blocks of 32 consecutive entries (one tile's survivors are
+// consecutive, so their segment records are shared in L1) and appends its
+// kept entries in batches.  Pass 1 (kDefer) evaluates the common case and
+// appends the entries of the long branches to the deferred list (the phase-B2
+// list pb, unused until phase B1, with its first count); pass 2 evaluates the
+// deferred list.
+template <bool kDefer>
+__global__ void __launch_bounds__(kEnumThreads) k_tl_b2f(BatchDev b, const int4* __restrict__ in,
+                                                        const unsigned long long* n_in) {
+    __shared__ int4 fbuf[kEnumThreads / kWarp][kPassBuf];
+    __shared__ int4 dbuf[kDefer ? kEnumThreads / kWarp : 1][kPassBuf];
+    if (halted(b)) return;
+    const int64_t n = min((int64_t)*n_in, b.kept_cap);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int4* buf = fbuf[w];
+    int4* dfr = dbuf[kDefer ? w : 0];
+    int nb = 0, nd = 0;
+    // p0 + n <= n_in <= kept_cap: neither list can overflow
+    auto flush = [&](int4* list, unsigned long long* cnt, int4* from, int& m) {
+        __syncwarp();
+        unsigned long long p0 = 0;
+        if (lane == 0 && m) p0 = atomicAdd(cnt, (unsigned long long)m);
+        p0 = __shfl_sync(0xffffffffu, p0, 0);
+        for (int i = lane; i < m; i += kWarp) AT(list, (int64_t)p0 + i, b.kept_cap) = from[i];
+        __syncwarp();
+        m = 0;
+    };
+    const int64_t warps = (int64_t)gridDim.x * (kEnumThreads / kWarp);
+    for (int64_t base = ((int64_t)blockIdx.x * (kEnumThreads / kWarp) + w) * kWarp; base < n; base += warps * kWarp) {
+        const int64_t i = base + lane;
+        int r = 0;
+        int4 e = make_int4(0, 0, 0, 0);
+        if (i < n) {
+            e = AT(in, i, b.kept_cap);
+            (void)IX(e.x, b.obj[kSG].cap);
+            (void)IX(e.y, b.obj[kSG].cap);
+            r = tl_b2_quick<kDefer>(e.z, load_sgv(b.sgpack, e.x), load_sgv(b.sgpack, e.y));
+        }
+        const unsigned lt = (1u << lane) - 1u;
+        const unsigned m = __ballot_sync(0xffffffffu, r == 1);
+        if (nb + __popc(m) > kPassBuf) flush(b.passf, b.n_keptf, buf, nb);
+        if (r == 1) buf[nb + __popc(m & lt)] = e;
+        nb += __popc(m);
+        if (kDefer) {
+            const unsigned md = __ballot_sync(0xffffffffu, r == 2);
+            if (nd + __popc(md) > kPassBuf) flush(b.pb, b.n_pb, dfr, nd);
+            if (r == 2) dfr[nd + __popc(md & lt)] = e;
+            nd += __popc(md);
+        }
+    }
+    flush(b.passf, b.n_keptf, buf, nb);
+    if (kDefer) flush(b.pb, b.n_pb, dfr, nd);
+}
+
+// Self-check of tl_b2_quick (no counterpart in the reference): every entry of
+// the last run's phase-A survivor list judged by the filter and by the exact
+// phases B1 and B2.  out[10]: entries; through exact phase B1; through exact
+// phases B1 and B2; rejected by the filter; rejected by the filter but
+// through the exact phases (must be 0); rejected by the filter among those
+// through exact phase B1; the largest |filter value - exact value| / the
+// filter's bound for deltaBeta, dBetaCut2 and betaOut (float bits; below 1
+// when the bounds hold); entries the filter left before reaching the cuts.
+__global__ void __launch_bounds__(256) k_tl_b2q_check(BatchDev b, unsigned long long* out) {
+    const int64_t n = min((int64_t)*b.n_kept, b.kept_cap);
+    unsigned long long c[6] = {0, 0, 0, 0, 0, 0}, inc = 0;
+    float rmax[3] = {0.f, 0.f, 0.f};
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int4 e = AT(b.passa, i, b.kept_cap);
+        (void)IX(e.x, b.obj[kSG].cap);
+        (void)IX(e.y, b.obj[kSG].cap);
+        const SGV S = load_sgv(b.sgpack, e.x), T = load_sgv(b.sgpack, e.y);
+        float cut, muls;
+        tl_cut_values(e.z, S, T, cut, muls);
+        const bool p1 = tl_phaseB1_sgv(e.z, S, T, cut);
+        float rec[kTLVarN];
+        rec[kTLVarDBeta] = __int_as_float(0x7fc00000);
+        const bool p2 = p1 && tl_phaseB2_sgv<kB2All>(e.z, S, T, muls, false, rec);
+        B2Quick q;
+        const int f = tl_b2_quick(e.z, S, T, &q);
+        c[0] += 1;
+        c[1] += p1;
+        c[2] += p2;
+        c[3] += f == 0;
+        c[4] += f == 0 && p2;
+        c[5] += f == 0 && p1;
+        inc += f != 0 && !q.complete;
+        if (p1 && q.complete && rec[kTLVarDBeta] == rec[kTLVarDBeta]) {
+            rmax[0] = fmaxf(rmax[0], fabsf(q.dbeta - rec[kTLVarDBeta]) / q.e_dbeta);
+            rmax[1] = fmaxf(rmax[1], fabsf(q.cut2 - rec[kTLVarDBetaCut2]) / q.e_cut2);
+            rmax[2] = fmaxf(rmax[2], fabsf(q.bout - rec[kTLVarBetaOut]) / q.e_bout);
+        }
+    }
+    for (int k = 0; k < 6; ++k) atomicAdd(out + k, c[k]);
+    for (int k = 0; k < 3; ++k) atomicMax(out + 6 + k, (unsigned long long)__float_as_uint(rmax[k]));
+    atomicAdd(out + 9, inc);
+}
+
 // Phase B1 on a survivor list of phase A (count entries of list/muls); the candidates
 // through it go to the phase-B2 list, BBBB ones from the front and the others
 // from the back, so that phase B2's warps mostly run one algorithm.  Front
@@ -2217,17 +2321,34 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     if (tiles) k_tl_enum_tiles<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
     else k_tl_enum_a<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
     if (h && h->timed) rec_event(h->tl_mid[0], s);
+    // the list phase B1 reads: the enumeration's, the pre-filter's kept
+    // entries, then what phase B2's single-precision filter leaves of it (not
+    // with DefaultNm1, whose phase B2 keeps what fails the deltaBeta cut)
+    int4* list = b.passa;
+    unsigned long long* count = b.n_kept;
     const bool mlp = (b.flags & kFlagMLP) != 0;
     if (mlp) {
         cudaMemsetAsync(b.n_kept2, 0, sizeof(unsigned long long), s);
         k_tl_prefilter<<<b.n_sm * 8, kMlpTile, 0, s>>>(b);
+        list = b.kept;
+        count = b.n_kept2;
     }
     if (h && h->timed) rec_event(h->tl_mid[1], s);
+    const bool filt = !(b.flags & (kFlagTLNm1 | kFlagNoB2Filter));
+    if (filt) {
+        cudaMemsetAsync(b.n_keptf, 0, sizeof(unsigned long long), s);
+        cudaMemsetAsync(b.n_pb, 0, sizeof(unsigned long long), s);
+        k_tl_b2f<true><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, list, count);
+        k_tl_b2f<false><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, b.pb, b.n_pb);
+        list = b.passf;
+        count = b.n_keptf;
+    }
+    if (h && h->timed) rec_event(h->tl_mid[2], s);
     cudaMemsetAsync(b.n_pb, 0, 2 * sizeof(unsigned long long), s);
-    k_tl_b1<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, mlp ? b.kept : b.passa, mlp ? b.n_kept2 : b.n_kept);
+    k_tl_b1<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, list, count);
     k_tl_b2<kB2BBBB><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
     k_tl_b2<kB2Others><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
-    if (h) h->launches += mlp ? 4 : 3;
+    if (h) h->launches += 3 + (mlp ? 1 : 0) + (filt ? 2 : 0);
     if (h && h->timed) rec_event(h->enum_stop[kTL], s);
     k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kTL);
     scan_h(b, b.obj[kTL].mod_cnt, b.n_gm_dev, b.n_gm, s, h);
@@ -2401,6 +2522,10 @@ void launch_tl_collect(const BatchDev& b, const MlpCollect& c, cudaStream_t s) {
     // the bucket table holds the last stage that ran: rebuild the tracklet one
     k_cand_buckets<<<b.n_sm * 8, 256, 0, s>>>(b, kTL);
     k_tl_collect<<<b.n_sm * 8, 256, 0, s>>>(b, c);
+}
+
+void launch_tl_b2q_check(const BatchDev& b, unsigned long long* out, cudaStream_t s) {
+    k_tl_b2q_check<<<b.n_sm * 8, 256, 0, s>>>(b, out);
 }
 
 void launch_tl_quick_check(const BatchDev& b, unsigned long long* out, cudaStream_t s) {

@@ -65,6 +65,9 @@ struct BatchDev {
     unsigned long long* n_kept;    // phase-A survivors found (can exceed kept_cap: overflow)
     int4* kept;                    // the phase-A survivors the pre-filter kept, as passa
     unsigned long long* n_kept2;
+    int4* passf;                   // what phase B2's single-precision decision (tl_b2_quick) left of
+                                   //   the enumeration's or the pre-filter's list, as passa
+    unsigned long long* n_keptf;
     // join index (triplets, then track candidates): the segments by their inner
     // mini-doublet, then the tracklets by their inner segment's inner mini-doublet
     int64_t* joff;                 // mini-doublet cap + 1: counts -> offsets
@@ -95,7 +98,7 @@ struct BatchDev {
 struct Hooks {
     cudaEvent_t enum_start[kNumStages] = {};
     cudaEvent_t enum_stop[kNumStages] = {};
-    cudaEvent_t tl_mid[2] = {};  // after phase A, after the pre-filter
+    cudaEvent_t tl_mid[3] = {};  // after phase A, after the pre-filter, after the B2 filter
     bool timed = false;
     int launches = 0;
 };
@@ -121,6 +124,7 @@ void launch_tl_collect(const BatchDev& b, const MlpCollect& c, cudaStream_t s);
 void launch_math_check(int fn, int exhaustive, unsigned long long start, long long n, unsigned long long seed,
                        unsigned long long* out, int n_sm, cudaStream_t s);
 // self-check of phase A's single-precision decision (out[4]: see k_tl_quick_check)
+void launch_tl_b2q_check(const BatchDev& b, unsigned long long* out, cudaStream_t s);
 void launch_tl_quick_check(const BatchDev& b, unsigned long long* out, cudaStream_t s);
 // final cut variables of tracklets [first, first + n) (15 floats each, the kTLVar* order)
 void launch_tl_vars(const BatchDev& b, int64_t first, int64_t n, float* out, cudaStream_t s);

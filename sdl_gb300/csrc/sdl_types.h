@@ -62,6 +62,7 @@ enum : int {
     kFlagTLNav = 32,     // createTrackletsViaNavigation
     kFlagTCFromTL = 64,  // createTrackCandidatesFromTracklets
     kFlagTCFromTP = 128, // createTrackCandidatesFromTriplets
+    kFlagNoB2Filter = 256,  // phase B2's single-precision filter off
     kFlagTestMlpGiveUp = 4096,  // self-test: the pre-filter's first tensor-core wait of each CTA gives up at once
 };
 

@@ -35,3 +35,47 @@ def test_phase_a_decision_matches_exact_cuts(gpu, batch, flags):
     assert r["settled"] + r["exact"] == r["candidates"], r
     assert r["mismatches"] == 0, r
     assert r["exact"] <= 1e-2 * r["candidates"], r
+
+
+@pytest.mark.parametrize("flags", [0, 3, 32])
+def test_b2_filter_rejects_only_what_exact_phase_b2_rejects(gpu, batch, flags):
+    """The single-precision phase-B2 filter (tl_b2_quick) against the exact
+    phases B1 and B2 on every phase-A survivor: it never rejects a candidate
+    the exact phases accept, its bounds on deltaBeta, dBetaCut2 and betaOut
+    hold (largest error / bound below 1; the decisions use four times the
+    bounds), and it rejects most of what the exact phases reject."""
+    det, events = batch
+    run_gpu(gpu, det, events, flags)
+    r = gpu.tl_b2_filter_check()
+    print(r)
+    assert r["entries"] > 1_000_000, r
+    assert r["violations"] == 0, r
+    assert all(v < 1.0 for v in r["bound_ratio"].values()), r
+    failing = r["entries"] - r["b2_pass"]
+    assert r["rejected"] >= 0.6 * failing, r
+    lists = gpu.tl_list_counts()
+    assert lists["listed"] == r["entries"] and lists["filtered"] == r["entries"] - r["rejected"], (lists, r)
+
+
+@pytest.mark.parametrize("flags", [0, 3, 32, 64])
+def test_b2_filter_changes_no_object(gpu, batch, flags):
+    """The chain with and without the phase-B2 filter (SDLG_FLAG_NO_B2_FILTER):
+    the same objects and counters in every event, with and without the
+    learned pre-filter."""
+    import bench
+    from sdl_gb300 import FLAG_MLP, FLAG_NO_B2_FILTER, mlp
+    import oracle
+    det, events = batch
+    params, thr, _ = mlp.load(bench.MLP_WEIGHTS)
+    gpu.upload_detector(det)
+    gpu.mlp_set_params(params, thr)
+    gpu.set_events(events)
+    for extra in (0, FLAG_MLP):
+        got = []
+        for off in (0, FLAG_NO_B2_FILTER):
+            gpu.run(4, flags | extra | off)
+            got.append(([[oracle.digest(gpu.objects(s, e)) for s in range(5)] for e in range(len(events))],
+                        [gpu.counters(e).tolist() for e in range(len(events))]))
+        assert got[0] == got[1], (flags, extra)
+        last = gpu.tl_list_counts()  # the last run had the filter off
+        assert last["filtered"] == (last["kept"] if extra else last["listed"])
