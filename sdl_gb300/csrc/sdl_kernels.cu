@@ -1427,67 +1427,6 @@ __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
     mlp_teardown(sm, st);
 }
 
-// Phase B2's single-precision decision (tl_b2_quick, no counterpart in the
-// reference) on a survivor list (in / n_in: the enumeration's, or the
-// pre-filter's kept list): the entries it cannot reject go to the filtered
-// list (n_keptf entries, same format), which phase B1 reads.  Exact phase B2
-// passes about one in thirteen of the enumeration's entries, so the filter
-// spares the exact phases (float-float arithmetic and the host libm's
-// functions) most of their work; the tracklets do not change.  Each warp
-// takes blocks of 32 consecutive entries (one tile's survivors are
-// consecutive, so their segment records are shared in L1) and appends its
-// kept entries in batches.  Pass 1 (kDefer) evaluates the common case and
-// appends the entries of the long branches to the deferred list (the phase-B2
-// list pb, unused until phase B1, with its first count); pass 2 evaluates the
-// deferred list.
-template <bool kDefer>
-__global__ void __launch_bounds__(kEnumThreads) k_tl_b2f(BatchDev b, const int4* __restrict__ in,
-                                                        const unsigned long long* n_in) {
-    __shared__ int4 fbuf[kEnumThreads / kWarp][kPassBuf];
-    __shared__ int4 dbuf[kDefer ? kEnumThreads / kWarp : 1][kPassBuf];
-    if (halted(b)) return;
-    const int64_t n = min((int64_t)*n_in, b.kept_cap);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int4* buf = fbuf[w];
-    int4* dfr = dbuf[kDefer ? w : 0];
-    int nb = 0, nd = 0;
-    // p0 + n <= n_in <= kept_cap: neither list can overflow
-    auto flush = [&](int4* list, unsigned long long* cnt, int4* from, int& m) {
-        __syncwarp();
-        unsigned long long p0 = 0;
-        if (lane == 0 && m) p0 = atomicAdd(cnt, (unsigned long long)m);
-        p0 = __shfl_sync(0xffffffffu, p0, 0);
-        for (int i = lane; i < m; i += kWarp) AT(list, (int64_t)p0 + i, b.kept_cap) = from[i];
-        __syncwarp();
-        m = 0;
-    };
-    const int64_t warps = (int64_t)gridDim.x * (kEnumThreads / kWarp);
-    for (int64_t base = ((int64_t)blockIdx.x * (kEnumThreads / kWarp) + w) * kWarp; base < n; base += warps * kWarp) {
-        const int64_t i = base + lane;
-        int r = 0;
-        int4 e = make_int4(0, 0, 0, 0);
-        if (i < n) {
-            e = AT(in, i, b.kept_cap);
-            (void)IX(e.x, b.obj[kSG].cap);
-            (void)IX(e.y, b.obj[kSG].cap);
-            r = tl_b2_quick<kDefer>(e.z, load_sgv(b.sgpack, e.x), load_sgv(b.sgpack, e.y));
-        }
-        const unsigned lt = (1u << lane) - 1u;
-        const unsigned m = __ballot_sync(0xffffffffu, r == 1);
-        if (nb + __popc(m) > kPassBuf) flush(b.passf, b.n_keptf, buf, nb);
-        if (r == 1) buf[nb + __popc(m & lt)] = e;
-        nb += __popc(m);
-        if (kDefer) {
-            const unsigned md = __ballot_sync(0xffffffffu, r == 2);
-            if (nd + __popc(md) > kPassBuf) flush(b.pb, b.n_pb, dfr, nd);
-            if (r == 2) dfr[nd + __popc(md & lt)] = e;
-            nd += __popc(md);
-        }
-    }
-    flush(b.passf, b.n_keptf, buf, nb);
-    if (kDefer) flush(b.pb, b.n_pb, dfr, nd);
-}
-
 // Self-check of tl_b2_quick (no counterpart in the reference): every entry of
 // the last run's phase-A survivor list judged by the filter and by the exact
 // phases B1 and B2.  out[10]: entries; through exact phase B1; through exact
@@ -1550,6 +1489,85 @@ __device__ __forceinline__ void pb_flush(const BatchDev& b, int4* buf, int& n, b
     }
     __syncwarp();
     n = 0;
+}
+
+// Phase B2's single-precision decision (tl_b2_quick, no counterpart in the
+// reference) on a survivor list (in / n_in: the enumeration's, or the
+// pre-filter's kept list): the entries it cannot reject go to the filtered
+// list (n_keptf entries, same format), which phase B1 reads.  Exact phase B2
+// passes about one in thirteen of the enumeration's entries, so the filter
+// spares the exact phases (float-float arithmetic and the host libm's
+// functions) most of their work; the tracklets do not change.  Each warp
+// takes blocks of 32 consecutive entries (one tile's survivors are
+// consecutive, so their segment records are shared in L1) and appends its
+// kept entries in batches.  Pass 0 evaluates the common case (BBBB without a
+// 2S endcap outer anchor) and defers the entries of the long branches to the
+// phase-B2 list pb (unused until phase B1): BBEE entries to its front, EEEE
+// and the 2S endcap BBBB entries to its back; passes 1 and 2 evaluate the
+// front and the back, so that each pass's warps mostly run one branch.
+template <int kPass>
+__global__ void __launch_bounds__(kEnumThreads) k_tl_b2f(BatchDev b, const int4* __restrict__ in,
+                                                        const unsigned long long* n_in) {
+    constexpr bool kDefer = kPass == 0;
+    __shared__ int4 fbuf[kEnumThreads / kWarp][kPassBuf];
+    __shared__ int4 dbuf[kDefer ? kEnumThreads / kWarp : 1][2][kPbBuf];
+    if (halted(b)) return;
+    int64_t n;
+    if (kPass == 0) {
+        n = min((int64_t)*n_in, b.kept_cap);
+    } else {
+        const int64_t nf = min((int64_t)b.n_pb[0], b.kept_cap);
+        n = kPass == 1 ? nf : min((int64_t)b.n_pb[1], b.kept_cap - nf);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int4* buf = fbuf[w];
+    int4* dfront = dbuf[kDefer ? w : 0][0];
+    int4* dback = dbuf[kDefer ? w : 0][1];
+    int nb = 0, nf = 0, nk = 0;
+    // p0 + nb <= the input length <= kept_cap: the filtered list cannot overflow
+    auto flush = [&]() {
+        __syncwarp();
+        unsigned long long p0 = 0;
+        if (lane == 0 && nb) p0 = atomicAdd(b.n_keptf, (unsigned long long)nb);
+        p0 = __shfl_sync(0xffffffffu, p0, 0);
+        for (int i = lane; i < nb; i += kWarp) AT(b.passf, (int64_t)p0 + i, b.kept_cap) = buf[i];
+        __syncwarp();
+        nb = 0;
+    };
+    const int64_t warps = (int64_t)gridDim.x * (kEnumThreads / kWarp);
+    for (int64_t base = ((int64_t)blockIdx.x * (kEnumThreads / kWarp) + w) * kWarp; base < n; base += warps * kWarp) {
+        const int64_t i = base + lane;
+        int r = 0;
+        int4 e = make_int4(0, 0, 0, 0);
+        if (i < n) {
+            e = kPass == 0 ? AT(in, i, b.kept_cap) : AT(b.pb, kPass == 1 ? i : b.kept_cap - 1 - i, b.kept_cap);
+            (void)IX(e.x, b.obj[kSG].cap);
+            (void)IX(e.y, b.obj[kSG].cap);
+            r = tl_b2_quick<kDefer>(e.z, load_sgv(b.sgpack, e.x), load_sgv(b.sgpack, e.y));
+        }
+        const unsigned lt = (1u << lane) - 1u;
+        const unsigned m = __ballot_sync(0xffffffffu, r == 1);
+        if (nb + __popc(m) > kPassBuf) flush();
+        if (r == 1) buf[nb + __popc(m & lt)] = e;
+        nb += __popc(m);
+        if (kDefer) {
+            // (the deferred entries fit: together at most the input length <= kept_cap)
+            const bool front = e.z == kAlgoBBEE;
+            const unsigned mf = __ballot_sync(0xffffffffu, r == 2 && front);
+            const unsigned mk = __ballot_sync(0xffffffffu, r == 2 && !front);
+            if (nf + __popc(mf) > kPbBuf) pb_flush(b, dfront, nf, true);
+            if (nk + __popc(mk) > kPbBuf) pb_flush(b, dback, nk, false);
+            if (r == 2 && front) dfront[nf + __popc(mf & lt)] = e;
+            if (r == 2 && !front) dback[nk + __popc(mk & lt)] = e;
+            nf += __popc(mf);
+            nk += __popc(mk);
+        }
+    }
+    flush();
+    if (kDefer) {
+        pb_flush(b, dfront, nf, true);
+        pb_flush(b, dback, nk, false);
+    }
 }
 
 __global__ void __launch_bounds__(kEnumThreads) k_tl_b1(BatchDev b, const int4* __restrict__ list,
@@ -2337,9 +2355,10 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     const bool filt = !(b.flags & (kFlagTLNm1 | kFlagNoB2Filter));
     if (filt) {
         cudaMemsetAsync(b.n_keptf, 0, sizeof(unsigned long long), s);
-        cudaMemsetAsync(b.n_pb, 0, sizeof(unsigned long long), s);
-        k_tl_b2f<true><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, list, count);
-        k_tl_b2f<false><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, b.pb, b.n_pb);
+        cudaMemsetAsync(b.n_pb, 0, 2 * sizeof(unsigned long long), s);
+        k_tl_b2f<0><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, list, count);
+        k_tl_b2f<1><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, nullptr, nullptr);
+        k_tl_b2f<2><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, nullptr, nullptr);
         list = b.passf;
         count = b.n_keptf;
     }
@@ -2348,7 +2367,7 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     k_tl_b1<<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b, list, count);
     k_tl_b2<kB2BBBB><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
     k_tl_b2<kB2Others><<<b.n_sm * enum_grid(b, kTL), kEnumThreads, 0, s>>>(b);
-    if (h) h->launches += 3 + (mlp ? 1 : 0) + (filt ? 2 : 0);
+    if (h) h->launches += 3 + (mlp ? 1 : 0) + (filt ? 3 : 0);
     if (h && h->timed) rec_event(h->enum_stop[kTL], s);
     k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kTL);
     scan_h(b, b.obj[kTL].mod_cnt, b.n_gm_dev, b.n_gm, s, h);
