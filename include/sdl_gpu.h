@@ -370,8 +370,7 @@ int64_t sdlg_last_launches(const sdlg_ctx* ctx);
  * `stream` (NULL: the context's stream); the geometry must be loaded.
  * Limits: n_hits <= SDLG_STATIC_MAX_HITS and at most SDLG_STATIC_MAX_MODULES
  * modules, else SDLG_ERR_CAPACITY.  The first call on a device looks up the
- * array's device address; make that first call before any stream capture.
- * All calls share the one array: calls that overlap on the GPU (different
+ * array's device address.  All calls share the one array: calls that overlap on the GPU (different
  * streams, contexts or threads without ordering) race and corrupt each
  * other's results. */
 #define SDLG_STATIC_MAX_HITS 131072
