@@ -1069,9 +1069,10 @@ __device__ __forceinline__ void tl_cut_values(int algo, const SGV& S, const TSeg
 // tl_phaseA.  The approximation of the factor, 0.015 sqrt(0.1 + 0.004 d) [x
 // sqrt(q)] with sqrt(u) = u * rsqrtf(u) (rsqrtf: at most 2 ulp), is within
 // 11 * 2^-24 of the exact float, and every quantity compared is then within
-// 2^-24 * 50 * (the sum of the magnitudes of its terms) of its exact value.
+// 2^-24 * 53 * (the sum of the magnitudes of its terms) of its exact value
+// (3 of the 53 from the pointed windows' square roots as u * rsqrtf(u)).
 // A comparison is decided here only when it holds by kQuickMargin times that
-// sum (2^-16: over 5 times the bound); otherwise, and for NaNs or the
+// sum (2^-16: over 4.8 times the bound); otherwise, and for NaNs or the
 // exact functions' fallback ranges, the result is kAlgoUnsure and the caller
 // runs tl_phaseA.  Returns the algorithm, kAlgoNone or kAlgoUnsure.
 constexpr int kAlgoUnsure = -1;
@@ -1132,7 +1133,7 @@ __device__ __forceinline__ int tl_phaseA_quick(const SGV& S, const TSeg& T, floa
         // (the two quotients by __fdividef: 2 ulp instead of 0.5, inside the bound)
         float dzErr = zp * zp * 2.f;
         dzErr += __fdividef(sdlMuls * sdlMuls * drt_OutLo_InLo * drt_OutLo_InLo, 3.f) * coshEta * coshEta;
-        dzErr = __fsqrt_rn(dzErr);
+        dzErr = dzErr * rsqrtf(dzErr);  // (>= 2 zp^2 > 0; 3 ulp, inside the margin)
         const float dzMean = S.dzdr * drt_OutLo_InLo;
         const float pw = __fdividef(dzErr, drt_InSeg) * drt_OutLo_InLo;
         const float zWindow = pw + zp;
@@ -1186,7 +1187,7 @@ __device__ __forceinline__ int tl_phaseA_quick(const SGV& S, const TSeg& T, floa
             if (!(kZ >= 0)) return kAlgoNone;
             float drtErr = kPixelPSZpitch * kPixelPSZpitch * 2.f / dzSDIn / dzSDIn * dzOutInAbs * dzOutInAbs;
             drtErr += sdlMuls * sdlMuls * multDzDr * multDzDr / 3.f * coshEta * coshEta;
-            drtErr = __fsqrt_rn(drtErr);
+            drtErr = drtErr * rsqrtf(drtErr);  // (3 ulp, inside the margin; NaN for 0: undecided)
             const float drtMean = drtSDIn * dzOutInAbs / fabsf(dzSDIn);
             const float rtWindow = drtErr + rtGeom;
             const float mLo = drtMean / dzDrtScale;
@@ -1335,7 +1336,8 @@ __device__ __forceinline__ int tl_phaseB1_quick(int algo, const SGV& S, float4 t
     const int c5 = clear_within(v, cut);
     if (c5 <= 0 || algo == kAlgoEEEE) return c5;
     const float ax = txy.z - S.lx, ay = txy.w - S.ly;
-    const float dr = __fsqrt_rn(__fadd_rn(__fmul_rn(ax, ax), __fmul_rn(ay, ay)));
+    const float dr2 = __fadd_rn(__fmul_rn(ax, ax), __fmul_rn(ay, ay));
+    const float dr = dr2 * rsqrtf(dr2);  // (3 ulp: a few 1e-7 on the angle, far inside kB1Margin; NaN for 0: undecided)
     const float sdIn_d = S.urt - S.lrt;
     const float arg = fmin_ref((-S.rtseg * 1.f + dr) * k2Rinv1GeVf / kPtCut, kSinAlphaMax);
     float pa;

@@ -5,7 +5,9 @@ and 110 per-layer counters must be identical.
 
 * configuration 3: 64 events of uneven size, PU drawn uniformly in 50-250;
 * configuration 5: the benchmark's headline batch, 128 events of PU drawn
-  uniformly in 150-300 (the same seeds and PU draws as bench.py).
+  uniformly in 150-300 (the same seeds and PU draws as bench.py);
+* the stated density: 128 events of PU drawn uniformly in 227-474, 110k-229k
+  hits per event (bench.py's stated_density batch).
 
 Also: the pre-filtered chain's track candidates are a subset of the plain
 chain's (exact multiset intersection, not a count ratio) on a batch of
@@ -82,6 +84,13 @@ def test_config5_headline_batch_matches_oracle(oracle_lib):
     n, hits, objs = check_batch(bench.headline_plan(0, 128), oracle_lib)
     assert n == 128
     print("config 5: %d events, %d hits, objects %s identical" % (n, hits, objs.tolist()))
+
+
+def test_stated_density_batch_matches_oracle(oracle_lib):
+    import bench
+    n, hits, objs = check_batch(bench.dense_plan(0, 128), oracle_lib)
+    assert n == 128 and hits > 128 * 150000
+    print("stated density: %d events, %d hits, objects %s identical" % (n, hits, objs.tolist()))
 
 
 def test_prefiltered_track_candidates_are_a_subset():
