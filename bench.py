@@ -214,6 +214,15 @@ def dense_plan(rank, n):
     return [(base + 300 + k, float(p)) for k, p in enumerate(pus)]
 
 
+def uneven_plan(rank, n):
+    """(seed, PU) of the batch of uneven events of a rank: PU uniform in
+    50-250 (the 64-event plain batched configuration: 30k-121k hits per event
+    with this generator, 4.79M in all)"""
+    import numpy as np
+    pus = np.random.default_rng(3303 + rank).uniform(50.0, 250.0, size=n)
+    return [(30000 + 997 * rank + k, float(p)) for k, p in enumerate(pus)]
+
+
 def single_plan(rank, n):
     """(seed, PU) of the single-event workload of a rank"""
     base = 1000 + 997 * rank
@@ -366,6 +375,7 @@ def main():
     batch = make_events(headline_plan(rank, a.batch_events), threads)
     single = make_events(single_plan(rank, 4), threads)
     dense_batch = [] if (a.no_dense or a.plain_only or a.mlp_only) else make_events(dense_plan(rank, a.batch_events), threads)
+    uneven_batch = [] if (a.plain_only or a.mlp_only) else make_events(uneven_plan(rank, 64), threads)
     # the CPU baseline runs the restatement on the whole batch (about 30 s on
     # 16 cores) and doubles as the parity check of the plain batched chain on
     # every event; with fewer than 8 host threads, on every 8th event
@@ -557,6 +567,26 @@ def main():
                  "stage_ms": {k: round(float(v), 3) for k, v in zip(STAGE_NAMES, np.mean(np.array(dm_stage), axis=0))},
                  "plain_stage_ms": {k: round(float(v), 3) for k, v in zip(STAGE_NAMES, np.mean(np.array(dp_stage), axis=0))}}
 
+    # ---- the plain batched chain on 64 events of uneven size (PU 50-250) ------
+    uneven = None
+    if uneven_batch:
+        nu = len(uneven_batch)
+        ch.set_events(uneven_batch)
+        ch.run(4, 0)
+        tuned_uneven = ch.autotune(4, 0)
+        for _ in range(2):
+            ch.run(4, 0)
+        u_ms, u_stage, _, _ = timed_runs(ch, 0, max(3, a.steps // 4), flush)
+        u_mean = allmax(pg, statistics.fmean(u_ms))
+        hits_u = [len(e) for e in uneven_batch]
+        uneven = {"workload": "plain batched chain, %d events of uneven size, PU uniform in 50-250 (%d-%d hits per "
+                              "event)" % (nu, min(hits_u), max(hits_u)),
+                  "value": round(allsum(pg, nu) * 1e3 / u_mean, 3), "unit": "events/s", "ms_per_step": round(u_mean, 3),
+                  "hits_per_step": int(sum(hits_u)), "hits_per_s": round(sum(hits_u) * 1e3 / u_mean, 1),
+                  "objects_per_step": [int(v) for v in ch.counts(-1)], "tuned": tuned_uneven,
+                  "stage_ms": {k: round(float(v), 3) for k, v in zip(STAGE_NAMES, np.mean(np.array(u_stage), axis=0))},
+                  "parity": "tests/test_batch_parity_gpu.py: every event against the CPU restatement"}
+
     # ---- plain chain, one PU200-like event per step --------------------------
     ev = single[0]
     ch.set_events([ev])
@@ -690,7 +720,7 @@ def main():
             "recall_method": "track candidates: |pruned & plain| / |plain| over the hit-index tuple multisets, event "
                              "by event; tracklets: count ratio (pruned tracklets are a subset by construction)",
             "plain_batched": plain_batched, "plain_single": plain_single, "variants": variants,
-            "stated_density": dense,
+            "stated_density": dense, "batched_uneven": uneven,
             "e2e": {"value": round(e2e_value, 3), "unit": "events/s", "ms_per_step": round(e2e_mean, 3),
                     "h2d_bytes_per_step": n_hit * 20 + 8 * (len(batch) + 1), "d2h_bytes_per_step": int(statistics.fmean(d2h_p)),
                     "path": "per step: sdlg_set_events (pinned host) + sdlg_run(SDLG_FLAG_MLP) + sdlg_get_objects_async(TC, "

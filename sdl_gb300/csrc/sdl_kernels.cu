@@ -420,15 +420,18 @@ __global__ void k_md_pack(BatchDev b) {
 // segment algorithm on inner MD a and outer MD bmd (Segment.cc:337-859);
 // `connected`: the outer MD's module is in the inner module's connection list
 // (the endcap algorithm's first requirement, Segment.cc:613-633)
-template <bool kPre = false>
+// kOuter: 0 either algorithm, 1 only the barrel one (outer MD in the barrel),
+// 2 only the endcap one (a kernel compiled for one keeps the other's code out
+// of its instruction caches); a candidate of the other kind fails
+template <bool kPre = false, int kOuter = 0>
 __device__ __forceinline__ bool sg_pair_rec(const MDView& im, const MDRec& orec, bool connected, float* fv) {
     const MDView& om = orec.v;
     SGVals v;
     v.dphi = v.dphimin = v.dphimax = v.dphichange = v.dphiminchange = v.dphimaxchange = 0.f;
-    bool pass;
+    bool pass = false;
     const bool ob = om.m->subdet == kBarrel;
-    if (ob) pass = sg_barrel<kPre>(im, om, orec.a1, orec.tf, orec.c0, v);
-    else pass = sg_endcap<kPre>(im, om, orec.a1, orec.tf, connected, orec.c0, orec.c1, v);
+    if (kOuter != 2 && ob) pass = sg_barrel<kPre>(im, om, orec.a1, orec.tf, orec.c0, v);
+    else if (kOuter != 1 && !ob) pass = sg_endcap<kPre>(im, om, orec.a1, orec.tf, connected, orec.c0, orec.c1, v);
     fv[0] = v.dphi; fv[1] = v.dphimin; fv[2] = v.dphimax;
     fv[3] = v.dphichange; fv[4] = v.dphiminchange; fv[5] = v.dphimaxchange;
     return pass;
@@ -961,6 +964,7 @@ __device__ __forceinline__ int tl_ab1_decide(const SGV& S, const SGOuter& T, flo
 // growing, so it holds the capacity needed).  Every lane of the warp calls
 // passbuf_add and passbuf_flush.
 constexpr int kPassBuf = 128;
+constexpr int kPbBuf = 64;  // the phase-B2 (and segment first-pass) list's per-warp buffers
 struct PassBuf {
     int4* e;    // this warp's kPassBuf entries in shared memory
     int n = 0;  // entries held (warp-uniform)
@@ -1234,8 +1238,36 @@ constexpr int kSgbMinBlocks = SDLG_SGB_MIN_BLOCKS;
 // full warps and appends the segments.  The first cuts reject most
 // candidates, so the expensive rest (the direction-change and dAlpha cuts)
 // no longer runs beside idle lanes.
+// A warp's segment first-pass survivors appended to the spare list pb:
+// candidates with a barrel outer MD at its front (count n_pb[0]), the others
+// at its back (n_pb[1]), so that the second pass runs each algorithm in its
+// own kernel.  n_kept counts both and reserves their room: a batch that would
+// take the two parts past kept_cap is not written and flags the overflow (the
+// count keeps growing, so it holds the capacity needed).
+__device__ __forceinline__ void sg_list_flush(const BatchDev& b, int4* buf, int& n, bool front) {
+    __syncwarp();
+    const int lane = threadIdx.x & 31;
+    unsigned long long p0 = 0;
+    int ok = 1;
+    if (lane == 0 && n) {
+        const unsigned long long tot = atomicAdd(b.n_kept, (unsigned long long)n);
+        ok = tot + (unsigned long long)n <= (unsigned long long)b.kept_cap;
+        if (ok) p0 = atomicAdd(b.n_pb + (front ? 0 : 1), (unsigned long long)n);
+        else atomicOr(b.status, kStatusOverflowKept);
+    }
+    p0 = __shfl_sync(0xffffffffu, p0, 0);
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (ok)
+        for (int k = lane; k < n; k += kWarp) {
+            const int64_t q = (int64_t)p0 + k;
+            AT(b.pb, front ? q : b.kept_cap - 1 - q, b.kept_cap) = buf[k];
+        }
+    __syncwarp();
+    n = 0;
+}
+
 __global__ void __launch_bounds__(kEnumThreads) k_sg_enum_a(BatchDev b) {
-    __shared__ int4 pbuf[kEnumThreads / kWarp][kPassBuf];
+    __shared__ int4 sbuf[kEnumThreads / kWarp][2][kPbBuf];
     if (halted(b)) return;
     const int64_t nobj = n_inner(b, kSG);
     if (nobj <= 0) return;
@@ -1245,7 +1277,9 @@ __global__ void __launch_bounds__(kEnumThreads) k_sg_enum_a(BatchDev b) {
     const int task = b.enum_task[kSG] > 0 ? b.enum_task[kSG] : kTaskDefault;
     const int64_t ntask = (total + task - 1) / task;
     const int lane = threadIdx.x & 31;
-    PassBuf pb{pbuf[threadIdx.x >> 5]};
+    int4* fb = sbuf[threadIdx.x >> 5][0];
+    int4* bb = sbuf[threadIdx.x >> 5][1];
+    int nf = 0, nb = 0;
     for (;;) {
         unsigned long long t = 0;
         if (lane == 0) t = atomicAdd(b.task + kSG, 1ull);
@@ -1264,24 +1298,37 @@ __global__ void __launch_bounds__(kEnumThreads) k_sg_enum_a(BatchDev b) {
         for (int64_t cb = base; cb < end; cb += kWarp) {
             const int64_t c = cb + lane;
             int a = 0, bmd = 0;
-            bool pass = false;
+            bool pass = false, ob = false;
             if (c < end) {
                 a = (i0 == i1) ? i0 : find_obj(b, off, offlim, i0, i1, c);
                 bmd = sg_outer_md(b, a, c - AT(off, a, offlim));
                 (void)IX(bmd, b.obj[kMD].cap);
                 float fv[6];
-                pass = sg_pair_rec<true>(md_rec(b, a).v, md_rec(b, bmd), true, fv);
+                const MDRec orec = md_rec(b, bmd);
+                ob = orec.v.m->subdet == kBarrel;
+                pass = sg_pair_rec<true>(md_rec(b, a).v, orec, true, fv);
             }
-            passbuf_add(b, pb, pass ? 1 : kAlgoNone, a, bmd, 0);
+            const unsigned lt = (1u << lane) - 1u;
+            const unsigned mf = __ballot_sync(0xffffffffu, pass && ob), mb = __ballot_sync(0xffffffffu, pass && !ob);
+            if (nf + __popc(mf) > kPbBuf) sg_list_flush(b, fb, nf, true);
+            if (nb + __popc(mb) > kPbBuf) sg_list_flush(b, bb, nb, false);
+            if (pass && ob) fb[nf + __popc(mf & lt)] = make_int4(a, bmd, 1, 0);
+            if (pass && !ob) bb[nb + __popc(mb & lt)] = make_int4(a, bmd, 2, 0);
+            nf += __popc(mf);
+            nb += __popc(mb);
         }
     }
-    passbuf_flush(b, pb);
+    sg_list_flush(b, fb, nf, true);
+    sg_list_flush(b, bb, nb, false);
 }
 
+template <int kOuter>
 __global__ void __launch_bounds__(kEnumThreads, kSgbMinBlocks) k_sg_b(BatchDev b) {
     __shared__ int rbuf[kEnumThreads / kWarp][3 + 6][kRecBuf];
     if (halted(b)) return;
-    const int64_t n = min((int64_t)*b.n_kept, b.kept_cap);
+    // kOuter 1: the barrel part of the first pass's list (front), 2: the endcap part (back)
+    const int64_t nfront = min((int64_t)b.n_pb[0], b.kept_cap);
+    const int64_t n = kOuter == 1 ? nfront : min((int64_t)b.n_pb[1], b.kept_cap - nfront);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int64_t nwarp = (int64_t)gridDim.x * (kEnumThreads / 32);
     RecBuf<6> rb{rbuf[w]};
@@ -1291,10 +1338,10 @@ __global__ void __launch_bounds__(kEnumThreads, kSgbMinBlocks) k_sg_b(BatchDev b
         int a = 0, bmd = 0;
         float fv[6];
         if (i < n) {
-            const int4 e = AT(b.passa, i, b.kept_cap);
+            const int4 e = AT(b.pb, kOuter == 1 ? i : b.kept_cap - 1 - i, b.kept_cap);
             a = e.x;
             bmd = e.y;
-            pass = sg_pair(b, a, bmd, true, fv);
+            pass = sg_pair_rec<false, kOuter>(md_rec(b, a).v, md_rec(b, bmd), true, fv);
         }
         const unsigned m = __ballot_sync(0xffffffffu, pass);
         if (!m) continue;
@@ -1476,7 +1523,6 @@ __global__ void __launch_bounds__(256) k_tl_b2q_check(BatchDev b, unsigned long 
 // and back never meet: together they hold at most count <= kept_cap entries.
 // Each warp collects its BBBB and its other survivors in two shared-memory
 // buffers and appends each with one atomic per batch (as passbuf_add).
-constexpr int kPbBuf = 64;
 __device__ __forceinline__ void pb_flush(const BatchDev& b, int4* buf, int& n, bool front) {
     __syncwarp();
     const int lane = threadIdx.x & 31;
@@ -2282,13 +2328,15 @@ void launch_sg(const BatchDev& b, cudaStream_t s, Hooks* h) {
     // first cuts -> survivor list -> whole algorithm (k_sg_enum_a, k_sg_b)
     if (h && h->timed) rec_event(h->enum_start[kSG], s);
     cudaMemsetAsync(b.n_kept, 0, sizeof(unsigned long long), s);
+    cudaMemsetAsync(b.n_pb, 0, 2 * sizeof(unsigned long long), s);
     k_sg_enum_a<<<b.n_sm * enum_grid(b, kSG), kEnumThreads, 0, s>>>(b);
-    k_sg_b<<<b.n_sm * enum_grid(b, kSG), kEnumThreads, 0, s>>>(b);
+    k_sg_b<1><<<b.n_sm * enum_grid(b, kSG), kEnumThreads, 0, s>>>(b);
+    k_sg_b<2><<<b.n_sm * enum_grid(b, kSG), kEnumThreads, 0, s>>>(b);
     if (h && h->timed) rec_event(h->enum_stop[kSG], s);
     k_obj_counters<<<grid_for(b.n_gm, 256, b.n_sm * 16), 256, 0, s>>>(b, kSG);
     scan_h(b, b.obj[kSG].mod_cnt, b.n_gm_dev, b.n_gm, s, h);
     k_scatter<<<b.n_sm * 8, 256, 0, s>>>(b, kSG);
-    if (h) h->launches += 4;
+    if (h) h->launches += 5;
 }
 
 // the join index of stage st's objects (segments or tracklets), keyed by

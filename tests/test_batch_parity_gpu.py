@@ -34,8 +34,8 @@ def make_events(plan):
 
 
 def config3_plan(n=64):
-    rng = np.random.default_rng(3303)
-    return [(30000 + k, float(p)) for k, p in enumerate(rng.uniform(50.0, 250.0, size=n))]
+    import bench
+    return bench.uneven_plan(0, n)
 
 
 def gpu_digests(ch, n_ev):
