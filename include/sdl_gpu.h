@@ -290,8 +290,9 @@ int sdlg_last_tl_pass_times4(sdlg_ctx* ctx, float* out4);
 /* Entries of the last run's tracklet candidate lists (no counterpart in the
  * reference): the enumeration's phase-A survivors, those the pre-filter kept
  * (0 without SDLG_FLAG_MLP), and what the single-precision phase-B2 filter
- * left of the list before it (that list's length without the filter), which
- * the exact phases judge. */
+ * left of the list before it for the exact phases to judge (that list's length
+ * without the filter; the entries the filter found through phase B2 are
+ * tracklets already and not counted). */
 int sdlg_last_tl_list_counts(sdlg_ctx* ctx, int64_t* out3);
 
 /* Self-check of the float-float evaluations that stand for the reference's
@@ -341,13 +342,15 @@ int sdlg_tl_phase_a_check(sdlg_ctx* ctx, uint64_t* out4);
 /* Self-check of the single-precision phase-B2 filter (no counterpart in the
  * reference): after a run through the tracklet stage, every entry of the
  * enumeration's survivor list is judged by the filter and by the exact phases
- * B1 and B2.  out10: entries; through exact phase B1; through exact phases B1
+ * B1 and B2.  out12: entries; through exact phase B1; through exact phases B1
  * and B2; rejected by the filter; rejected by the filter but through the exact
  * phases (must be 0); rejected by the filter among those through exact phase
  * B1; the largest |filter value - exact value| / the filter's bound for
  * deltaBeta, dBetaCut2 and betaOut (as float bits; below 1 when the bounds
- * hold); entries the filter left before reaching the cuts. */
-int sdlg_tl_b2_filter_check(sdlg_ctx* ctx, uint64_t* out10);
+ * hold); entries the filter left before reaching the cuts; entries the filter
+ * finds through phase B2; of those, entries through exact phase B1 but not
+ * through exact phase B2 (must be 0). */
+int sdlg_tl_b2_filter_check(sdlg_ctx* ctx, uint64_t* out12);
 
 /* Number of kernels one run of the chain launches (as last enqueued). */
 int64_t sdlg_last_launches(const sdlg_ctx* ctx);

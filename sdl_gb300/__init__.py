@@ -534,13 +534,13 @@ class Chain:
     def tl_b2_filter_check(self) -> dict:
         """Self-check of the single-precision phase-B2 filter over the last
         run's phase-A survivors against the exact phases B1 and B2."""
-        out = np.zeros(10, dtype=np.uint64)
+        out = np.zeros(12, dtype=np.uint64)
         self._ck(lib().sdlg_tl_b2_filter_check(self.h, out.ctypes.data))
         r = out[6:9].astype(np.uint32).view(np.float32)
         return {"entries": int(out[0]), "b1_pass": int(out[1]), "b2_pass": int(out[2]), "rejected": int(out[3]),
                 "violations": int(out[4]), "rejected_of_b1_pass": int(out[5]),
                 "bound_ratio": {"dbeta": float(r[0]), "cut2": float(r[1]), "betaout": float(r[2])},
-                "undecided_early": int(out[9])}
+                "undecided_early": int(out[9]), "accepted": int(out[10]), "accept_violations": int(out[11])}
 
     def autotune(self, stop_after: int = 4, flags: int = 0) -> dict:
         """Pick the fastest launch shape per stage on the current batch (kept for later runs)."""

@@ -1445,21 +1445,21 @@ int sdlg_last_tl_list_counts(sdlg_ctx* ctx, int64_t* out3) {
     return SDLG_OK;
 }
 
-int sdlg_tl_b2_filter_check(sdlg_ctx* ctx, uint64_t* out10) {
-    if (!ctx || !out10) return SDLG_ERR_ARG;
+int sdlg_tl_b2_filter_check(sdlg_ctx* ctx, uint64_t* out12) {
+    if (!ctx || !out12) return SDLG_ERR_ARG;
     if (!ctx->ran || ctx->last_stop < kTL) return fail(ctx, SDLG_ERR_ARG, "run the chain through the tracklet stage first");
     cudaSetDevice(ctx->device);
     unsigned long long* d = nullptr;
-    cudaError_t e = cudaMallocAsync((void**)&d, 10 * sizeof(unsigned long long), ctx->stream);
+    cudaError_t e = cudaMallocAsync((void**)&d, 12 * sizeof(unsigned long long), ctx->stream);
     if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "cudaMallocAsync: %s", cudaGetErrorString(e));
-    CK(cudaMemsetAsync(d, 0, 10 * sizeof(unsigned long long), ctx->stream));
+    CK(cudaMemsetAsync(d, 0, 12 * sizeof(unsigned long long), ctx->stream));
     launch_tl_b2q_check(ctx->b, d, ctx->stream);
     CK(cudaGetLastError());
-    unsigned long long h[10];
+    unsigned long long h[12];
     CK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaFreeAsync(d, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    for (int k = 0; k < 10; ++k) out10[k] = h[k];
+    for (int k = 0; k < 12; ++k) out12[k] = h[k];
     return SDLG_OK;
 }
 

@@ -1518,8 +1518,10 @@ static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict
 // that, and a branch condition within its bound, a non-finite value or an
 // angle too close to the wrap at +-pi leaves it to the exact phases.  So the
 // tracklets do not change; the filter only spares the exact phases the
-// candidates that certainly fail.  Returns 0 (phase B2 rejects the candidate)
-// or 1 (not decided here); with kDefer, 2 for the entries whose evaluation
+// candidates that certainly fail.  Returns 0 (phase B2 rejects the candidate),
+// 3 (phase B2 accepts it: both cuts hold by more than their bounds, so the
+// exact phase need not run), or 1 (not decided here); with kDefer, 2 for the
+// entries whose evaluation
 // takes the long branches (BBEE and EEEE, and BBBB with a 2S endcap outer
 // anchor, about one entry in six), which a second pass evaluates on full
 // warps instead of holding a warp of the common case for one lane.
@@ -1809,6 +1811,12 @@ __device__ __forceinline__ int tl_b2_quick(int algo, const SGV& S, const SGV& T,
     // deltaBeta cut: rejected when dBeta^2 > dBetaCut2 (the square rounded to float)
     const float lowD = fabsf(dBeta) - K * eD;
     if (lowD > 0.f && lowD * lowD * (1.f - 0x1p-21f) > cut2 + K * eCut2) return 0;
+    // both cuts hold: |betaOut| < betaOut_cut and dBeta^2 <= dBetaCut2 for the exact
+    // values (the comparisons' own roundings are ulps, far below the bounds)
+    const float hiO = fabsf(betaOut) + K * eBo, hiD = fabsf(dBeta) + K * eD;
+    if (hiO + ulp_of(hiO) < boutCut - K * eBoutCut - ulp_of(boutCut) &&
+        hiD * hiD * (1.f + 0x1p-21f) < cut2 - K * eCut2 - ulp_of(cut2))
+        return 3;
     return 1;
 }
 

@@ -1481,10 +1481,12 @@ __global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
 // through the exact phases (must be 0); rejected by the filter among those
 // through exact phase B1; the largest |filter value - exact value| / the
 // filter's bound for deltaBeta, dBetaCut2 and betaOut (float bits; below 1
-// when the bounds hold); entries the filter left before reaching the cuts.
+// when the bounds hold); entries the filter left before reaching the cuts;
+// entries it finds through phase B2; of those, entries through exact phase B1
+// but not exact phase B2 (must be 0).
 __global__ void __launch_bounds__(256) k_tl_b2q_check(BatchDev b, unsigned long long* out) {
     const int64_t n = min((int64_t)*b.n_kept, b.kept_cap);
-    unsigned long long c[6] = {0, 0, 0, 0, 0, 0}, inc = 0;
+    unsigned long long c[6] = {0, 0, 0, 0, 0, 0}, inc = 0, acc = 0, acc_bad = 0;
     float rmax[3] = {0.f, 0.f, 0.f};
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int4 e = AT(b.passa, i, b.kept_cap);
@@ -1506,6 +1508,8 @@ __global__ void __launch_bounds__(256) k_tl_b2q_check(BatchDev b, unsigned long 
         c[4] += f == 0 && p2;
         c[5] += f == 0 && p1;
         inc += f != 0 && !q.complete;
+        acc += f == 3;
+        acc_bad += f == 3 && p1 && !p2;
         if (p1 && q.complete && rec[kTLVarDBeta] == rec[kTLVarDBeta]) {
             rmax[0] = fmaxf(rmax[0], fabsf(q.dbeta - rec[kTLVarDBeta]) / q.e_dbeta);
             rmax[1] = fmaxf(rmax[1], fabsf(q.cut2 - rec[kTLVarDBetaCut2]) / q.e_cut2);
@@ -1515,6 +1519,8 @@ __global__ void __launch_bounds__(256) k_tl_b2q_check(BatchDev b, unsigned long 
     for (int k = 0; k < 6; ++k) atomicAdd(out + k, c[k]);
     for (int k = 0; k < 3; ++k) atomicMax(out + 6 + k, (unsigned long long)__float_as_uint(rmax[k]));
     atomicAdd(out + 9, inc);
+    atomicAdd(out + 10, acc);
+    atomicAdd(out + 11, acc_bad);
 }
 
 // Phase B1 on a survivor list of phase A (count entries of list/muls); the candidates
@@ -1550,13 +1556,17 @@ __device__ __forceinline__ void pb_flush(const BatchDev& b, int4* buf, int& n, b
 // 2S endcap outer anchor) and defers the entries of the long branches to the
 // phase-B2 list pb (unused until phase B1): BBEE entries to its front, EEEE
 // and the 2S endcap BBBB entries to its back; passes 1 and 2 evaluate the
-// front and the back, so that each pass's warps mostly run one branch.
+// front and the back, so that each pass's warps mostly run one branch.  An
+// entry the filter finds through phase B2 by more than its bounds, whose
+// phase B1 the enumeration decided already (passed), is a tracklet: it is
+// appended here as k_tl_b2 would, and the exact phases skip it.
 template <int kPass>
 __global__ void __launch_bounds__(kEnumThreads) k_tl_b2f(BatchDev b, const int4* __restrict__ in,
                                                         const unsigned long long* n_in) {
     constexpr bool kDefer = kPass == 0;
     __shared__ int4 fbuf[kEnumThreads / kWarp][kPassBuf];
     __shared__ int4 dbuf[kDefer ? kEnumThreads / kWarp : 1][2][kPbBuf];
+    __shared__ int tbuf[kEnumThreads / kWarp][3][kRecBuf];
     if (halted(b)) return;
     int64_t n;
     if (kPass == 0) {
@@ -1569,6 +1579,7 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b2f(BatchDev b, const int4*
     int4* buf = fbuf[w];
     int4* dfront = dbuf[kDefer ? w : 0][0];
     int4* dback = dbuf[kDefer ? w : 0][1];
+    RecBuf<0> tl{tbuf[w]};
     int nb = 0, nf = 0, nk = 0;
     // p0 + nb <= the input length <= kept_cap: the filtered list cannot overflow
     auto flush = [&]() {
@@ -1590,8 +1601,20 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b2f(BatchDev b, const int4*
             (void)IX(e.x, b.obj[kSG].cap);
             (void)IX(e.y, b.obj[kSG].cap);
             r = tl_b2_quick<kDefer>(e.z, load_sgv(b.sgpack, e.x), load_sgv(b.sgpack, e.y));
+            if (r == 3) r = e.w ? 4 : 1;  // (phase B1 undecided: both exact phases run)
         }
         const unsigned lt = (1u << lane) - 1u;
+        const unsigned mt = __ballot_sync(0xffffffffu, r == 4);
+        if (mt) {
+            if (tl.n + __popc(mt) > kRecBuf) rec_flush<0>(b, kTL, tl);
+            if (r == 4) {
+                const int k = tl.n + __popc(mt & lt);
+                tl.e[0][k] = e.x;
+                tl.e[1][k] = e.y;
+                tl.e[2][k] = OG(b, kSG, e.x);
+            }
+            tl.n += __popc(mt);
+        }
         const unsigned m = __ballot_sync(0xffffffffu, r == 1);
         if (nb + __popc(m) > kPassBuf) flush();
         if (r == 1) buf[nb + __popc(m & lt)] = e;
@@ -1610,6 +1633,7 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_b2f(BatchDev b, const int4*
         }
     }
     flush();
+    rec_flush<0>(b, kTL, tl);
     if (kDefer) {
         pb_flush(b, dfront, nf, true);
         pb_flush(b, dback, nk, false);
