@@ -542,6 +542,27 @@ struct MDVals {
     float dz, shiftedDz, dphi, dphichange;
 };
 
+// ---- single-precision directions with error bounds, for decisions that only
+// reject (or accept) by more than the bound and leave the rest to the exact
+// code: a direction difference with one direction from atan2f is within
+// kB2qDir of the exact float (3 ulp of pi for atan2f, the exact value's own
+// rounding, the subtraction and the wrap at +-pi), and the decisions take
+// kB2qSafety times their bounds.
+constexpr float kPiF = 3.14159265f;
+constexpr float kB2qSafety = 4.f;
+constexpr float kB2qDir = 2e-6f;  // a direction difference from atan2f: 3 ulp of pi, the exact value's rounding, the wrap
+constexpr float kB2qSin = 4e-7f;  // __sinf on [-pi, pi]: absolute error below 2^-21.41 (CUDA)
+__device__ __forceinline__ float ulp_of(float x) { return fabsf(x) * 0x1p-23f + 0x1p-126f; }
+// the exact code's dphi(a, b) = phi_mpi_pi(b - a) of two directions in
+// [-pi, pi] (one of them approximate); false near the wrap at +-pi
+__device__ __forceinline__ bool dphi_q(float a, float b, float& d) {
+    float v = b - a;
+    if (v >= kPiF) v -= 2.f * kPiF;
+    else if (v < -kPiF) v += 2.f * kPiF;
+    d = v;
+    return fabsf(fabsf(v) - kPiF) > 1e-4f;
+}
+
 // MiniDoublet.cc:243-447.  pixAsin is asin(min(rt*k, .95)) of the hit that
 // dPhiThreshold reads (the pixel-side hit); sh is shift_anchor's (xa, ya, zn)
 // of the anchoring hit.
@@ -564,14 +585,19 @@ __device__ __forceinline__ bool md_barrel(const P3& lo, const P3& up, float pixA
         v.dphi = dphi(lo, up);
     }
     if (!(fabsf(v.dphi) < miniCut)) return false;
+    // the two points of the direction change (dphichange(a, b): the direction of
+    // b - a against a's), as the reference picks them
+    const P3* a = &lo;
+    const P3* b = &up;
     if (lm.side != kCenter) {
-        if (lm.ltype == kPixel)
-            v.dphichange = lo.rt < shifted.rt ? dphichange(lo, shifted) : dphichange(shifted, lo);
-        else
-            v.dphichange = shifted.rt < up.rt ? dphichange(shifted, up) : dphichange(up, shifted);
-    } else {
-        v.dphichange = dphichange(lo, up);
+        if (lm.ltype == kPixel) { a = lo.rt < shifted.rt ? &lo : &shifted; b = lo.rt < shifted.rt ? &shifted : &lo; }
+        else { a = shifted.rt < up.rt ? &shifted : &up; b = shifted.rt < up.rt ? &up : &shifted; }
     }
+    // most candidates fail this cut: the direction of b - a from atan2f (a's
+    // direction is exact) rejects those clearly outside it before the exact one
+    float q;
+    if (dphi_q(a->phi, atan2f(b->y - a->y, b->x - a->x), q) && fabsf(q) >= miniCut + kB2qSafety * kB2qDir) return false;
+    v.dphichange = dphichange(*a, *b);
     return fabsf(v.dphichange) < miniCut;
 }
 
@@ -1214,7 +1240,6 @@ __device__ __forceinline__ int tl_phaseA_quick(const SGV& S, const TSeg& T, floa
 // The self-check (functions 16 and 17 of k_math_check) bounds both
 // approximation errors by 2e-6 on the GPU itself.
 constexpr float kB1Margin = 1e-4f;
-constexpr float kPiF = 3.14159265f;
 
 // approximate direction of (x, y) (Hit.cc:68-83's phi), or false when the
 // point is at the origin, tiny, huge or not finite
@@ -1525,23 +1550,10 @@ static __device__ __noinline__ bool tl_phaseB2(int algo, const float* __restrict
 // takes the long branches (BBEE and EEEE, and BBBB with a 2S endcap outer
 // anchor, about one entry in six), which a second pass evaluates on full
 // warps instead of holding a warp of the common case for one lane.
-constexpr float kB2qSafety = 4.f;
-constexpr float kB2qDir = 2e-6f;  // a direction difference from atan2f: 3 ulp of pi, the exact value's rounding, the wrap
-constexpr float kB2qSin = 4e-7f;  // __sinf on [-pi, pi]: absolute error below 2^-21.41 (CUDA)
-__device__ __forceinline__ float ulp_of(float x) { return fabsf(x) * 0x1p-23f + 0x1p-126f; }
 // (the bounds' own arithmetic uses __fdividef and rsqrtf, within 2 and 2 ulp,
 // and widens its results by a relative 1e-6; the few quantities the exact
 // code computes with the same float operations keep IEEE division)
 
-// the exact code's dphi(a, b) = phi_mpi_pi(b - a) of two directions in
-// [-pi, pi] (one of them approximate); false near the wrap at +-pi
-__device__ __forceinline__ bool dphi_q(float a, float b, float& d) {
-    float v = b - a;
-    if (v >= kPiF) v -= 2.f * kPiF;
-    else if (v < -kPiF) v += 2.f * kPiF;
-    d = v;
-    return fabsf(fabsf(v) - kPiF) > 1e-4f;
-}
 
 // pt = D / sin(b) (approximate) and bounds [lo, hi] of |D / sin(b')| over
 // every b' within e of b
