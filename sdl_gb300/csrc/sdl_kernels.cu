@@ -1059,7 +1059,14 @@ __global__ void __launch_bounds__(kEnumThreads) k_tl_enum_a(BatchDev b) {
 // outer segment once per tile, and the inner segments' records are
 // warp-uniform loads.  The candidates, and so the survivor list as a set, are
 // those k_tl_enum_a enumerates.
-constexpr int kTileA = 16;
+#ifndef SDLG_TILE_A
+#define SDLG_TILE_A 24
+#endif
+// inner segments per module-pair tile (a multiple of 4, at most 32); 24
+// measured fastest on the 128-event PU 150-300 batch (enumeration 14.47 ms,
+// against 14.82 at 16 and 14.60 at 32)
+constexpr int kTileA = SDLG_TILE_A;
+static_assert(kTileA % 4 == 0 && kTileA <= 32, "tile rows");
 
 __device__ __forceinline__ int64_t tile_count(int64_t na, int64_t nb) {
     return (na > 0 && nb > 0) ? ((na + kTileA - 1) / kTileA) * ((nb + kWarp - 1) / kWarp) : 0;
@@ -1155,7 +1162,12 @@ __device__ __forceinline__ int tile_outer(const BatchDev& b, int ev, int m, int 
 // segments (one entry per lane while the module has at most 32 connections),
 // then the inner segments' records (staged in shared memory, read there as
 // warp-uniform values) with the lanes' outer-segment fields.
-__global__ void __launch_bounds__(kEnumThreads, 4) k_tl_enum_tiles(BatchDev b) {
+// CTAs per SM the module-pair enumeration is compiled for (register budget;
+// 3, with 78 registers and no spill, measured 15.7 against 14.5 ms)
+#ifndef SDLG_ENUM_MIN_BLOCKS
+#define SDLG_ENUM_MIN_BLOCKS 4
+#endif
+__global__ void __launch_bounds__(kEnumThreads, SDLG_ENUM_MIN_BLOCKS) k_tl_enum_tiles(BatchDev b) {
     __shared__ __align__(16) float4 srec[kEnumThreads / kWarp][kTileA * (PK_N / 4)];
     __shared__ int sidx[kEnumThreads / kWarp][kTileA];
     __shared__ int4 pbuf[kEnumThreads / kWarp][kPassBuf];
