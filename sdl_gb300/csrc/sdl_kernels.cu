@@ -1234,11 +1234,12 @@ __global__ void __launch_bounds__(kEnumThreads, SDLG_ENUM_MIN_BLOCKS) k_tl_enum_
     passbuf_flush(b, pb);
 }
 
-// CTAs per SM the segment second pass is compiled for (register budget; 6
-// measured fastest on the 128-event PU 150-300 batch: 8.9 ms against 9.6 ms
-// at 1)
+// CTAs per SM the segment second pass is compiled for (register budget: 64
+// registers and no spill at 4, 40 and about 100 bytes of spills at 6).  With
+// the pass split by algorithm, 4 measured fastest on the 128-event PU 150-300
+// batch: segment stage 7.21 ms against 7.23 at 5 and 7.57 at 6
 #ifndef SDLG_SGB_MIN_BLOCKS
-#define SDLG_SGB_MIN_BLOCKS 6
+#define SDLG_SGB_MIN_BLOCKS 4
 #endif
 constexpr int kSgbMinBlocks = SDLG_SGB_MIN_BLOCKS;
 
@@ -1401,7 +1402,10 @@ __device__ __forceinline__ void pf_flush(const BatchDev& b, const PfPending& p) 
     AT(b.kept, pos, b.kept_cap) = p.e;
 }
 
-__global__ void __launch_bounds__(kMlpTile, 8) k_tl_prefilter(BatchDev b) {
+// CTAs per SM: shared memory (33.4 KB per CTA) leaves room for 6; 6 and 8
+// CTAs measured the same before the second layer took b2 into its MMA
+constexpr int kPfCtasPerSm = 6;
+__global__ void __launch_bounds__(kMlpTile, kPfCtasPerSm) k_tl_prefilter(BatchDev b) {
     __shared__ MlpSmem sm;
     if (halted(b)) return;
     const int64_t n = min((int64_t)*b.n_kept, b.kept_cap);
@@ -2431,7 +2435,7 @@ void launch_tl(const BatchDev& b, cudaStream_t s, Hooks* h) {
     const bool mlp = (b.flags & kFlagMLP) != 0;
     if (mlp) {
         cudaMemsetAsync(b.n_kept2, 0, sizeof(unsigned long long), s);
-        k_tl_prefilter<<<b.n_sm * 8, kMlpTile, 0, s>>>(b);
+        k_tl_prefilter<<<b.n_sm * kPfCtasPerSm, kMlpTile, 0, s>>>(b);
         list = b.kept;
         count = b.n_kept2;
     }

@@ -9,8 +9,8 @@ namespace sdlg {
 
 namespace {
 
-// FP32 parameters -> packed BF16 tiles [W1 b1], W2 and the FP32 tail
-// (BF16-rounded b2 and w3, b3, threshold)
+// FP32 parameters -> packed BF16 tiles [W1 b1], W2, b2 and the FP32 tail
+// (BF16-rounded w3, b3, threshold)
 __global__ void k_mlp_pack(const float* __restrict__ p, unsigned char* __restrict__ pack, float thr) {
     for (int e = threadIdx.x; e < kMlpHid * kMlpK1; e += blockDim.x) {
         const int n = e / kMlpK1, k = e % kMlpK1;
@@ -21,10 +21,11 @@ __global__ void k_mlp_pack(const float* __restrict__ p, unsigned char* __restric
         const int n = e / kMlpK2, k = e % kMlpK2;
         *reinterpret_cast<uint16_t*>(pack + kPackW2 + cm_offset(n, k, 8)) = bf16_bits(p[kMlpW2 + n * kMlpHid + k]);
     }
-    for (int n = threadIdx.x; n < kMlpHid; n += blockDim.x) {
-        reinterpret_cast<float*>(pack + kPackB2)[n] = bf16_round(p[kMlpB2 + n]);
-        reinterpret_cast<float*>(pack + kPackW3)[n] = bf16_round(p[kMlpW3 + n]);
+    for (int e = threadIdx.x; e < kMlpHid * 16; e += blockDim.x) {
+        const int n = e / 16, k = e % 16;
+        *reinterpret_cast<uint16_t*>(pack + kPackB2 + cm_offset(n, k, 2)) = k == 0 ? bf16_bits(p[kMlpB2 + n]) : (uint16_t)0;
     }
+    for (int n = threadIdx.x; n < kMlpHid; n += blockDim.x) reinterpret_cast<float*>(pack + kPackW3)[n] = bf16_round(p[kMlpW3 + n]);
     if (threadIdx.x == 0) {
         float* tail = reinterpret_cast<float*>(pack + kPackB3);
         tail[0] = p[kMlpB3];

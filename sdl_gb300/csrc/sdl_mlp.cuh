@@ -8,8 +8,8 @@
 // Numerics (shared by inference and training): features, W1, b1, W2, b2,
 // w3 and the first hidden layer are rounded to BF16; every sum accumulates in
 // FP32; b3 and the output layer's sum are FP32.  The bias b1 rides in the
-// first MMA as the weight of a constant 13th input; b2 is added to the
-// second MMA's FP32 result.  Inference uses the tensor cores
+// first MMA as the weight of a constant 13th input, b2 in the second as the
+// weight of a constant 65th one (K = 80).  Inference uses the tensor cores
 // (tcgen05.mma kind::f16, one 128-candidate tile per MMA, FP32 accumulators
 // in tensor memory); training uses CUDA-core kernels.
 #pragma once
@@ -35,14 +35,15 @@ constexpr int kMlpParams = kMlpB3 + 1;  // 5057
 
 // Packed inference weights, copied into shared memory by every CTA: [W1 b1]
 // (64 x 16) and W2 (64 x 64) in BF16 in the tensor cores' K-major
-// core-matrix layout, the BF16-rounded b2 and w3 and b3 in FP32, then the
-// threshold.
+// core-matrix layout, b2 as a 64 x 16 BF16 tile of the same layout (column 0,
+// the weight of the constant input; zeros elsewhere), the BF16-rounded w3 and
+// b3 in FP32, then the threshold.
 constexpr int kPackW1 = 0;                                  // 64 x 16 bf16
 constexpr int kPackW2 = kPackW1 + kMlpHid * kMlpK1 * 2;     // 64 x 64 bf16
-constexpr int kPackB2 = kPackW2 + kMlpHid * kMlpK2 * 2;
-constexpr int kPackW3 = kPackB2 + kMlpHid * 4;
+constexpr int kPackB2 = kPackW2 + kMlpHid * kMlpK2 * 2;     // 64 x 16 bf16
+constexpr int kPackW3 = kPackB2 + kMlpHid * 16 * 2;
 constexpr int kPackB3 = kPackW3 + kMlpHid * 4;
-constexpr int kPackBytes = kPackB3 + 16;                    // 10768, a multiple of 16
+constexpr int kPackBytes = kPackB3 + 16;                    // 12560, a multiple of 16
 
 // Byte offset of element (row, k) of a K-major BF16 tile without swizzling:
 // 8-row x 16-byte core matrices, `kgroups` of them along K per 8-row group
@@ -154,6 +155,29 @@ __device__ __forceinline__ uint32_t pack_bf16x2_relu(float lo, float hi) {
     return d;
 }
 
+// packed FP32 pairs (lo in the low word): the sm_100-family fma.f32x2, one
+// instruction for two lanes of arithmetic, each rounded to nearest like the
+// scalar form
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float2 f2_unpack(uint64_t v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ uint64_t f2_relu(uint64_t v) {
+    const float2 p = f2_unpack(v);
+    return f2_pack(fmaxf(p.x, 0.f), fmaxf(p.y, 0.f));
+}
+
 // 16 consecutive FP32 columns of this thread's tensor-memory lane
 __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
     uint32_t r[16];
@@ -178,6 +202,9 @@ struct __align__(128) MlpSmem {
     // are consumed before the layer overwrites them, and the layer before the
     // next tile's features)
     alignas(128) unsigned char a2[kMlpTile * kMlpK2 * 2];
+    // the second layer's constant input, K = 64-79 of its A operand: 1 in
+    // column 0 of every row, zeros after it (2 k-groups per 8-row group)
+    alignas(128) unsigned char aone[kMlpTile * 16 * 2];
     alignas(8) uint64_t mbar;
     uint32_t tmem;       // base address of 64 tensor-memory columns (both layers' accumulators)
 };
@@ -197,6 +224,8 @@ __device__ __forceinline__ void mlp_setup(MlpSmem& sm, const unsigned char* __re
     const uint4* src = reinterpret_cast<const uint4*>(pack);
     uint4* dst = reinterpret_cast<uint4*>(sm.w);
     for (int k = threadIdx.x; k < kPackBytes / 16; k += blockDim.x) dst[k] = __ldg(src + k);
+    *reinterpret_cast<uint4*>(sm.aone + cm_offset(threadIdx.x, 0, 2)) = make_uint4(0x3f80u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4*>(sm.aone + cm_offset(threadIdx.x, 8, 2)) = make_uint4(0u, 0u, 0u, 0u);
     if (threadIdx.x == 0) mbar_init(&sm.mbar);
     if (threadIdx.x < 32) tc_alloc(&sm.tmem, 64);
     fence_async_smem();
@@ -239,6 +268,8 @@ __device__ __forceinline__ void mlp_layer_sync(MlpSmem& sm, int layer, MlpThread
             for (int kc = 0; kc < kMlpK2 / 16; ++kc)
                 tc_mma(sm.tmem, smem_desc(a2 + 256 * kc, 128, 1024), smem_desc(w + kPackW2 + 256 * kc, 128, 1024),
                        kIdescBf16M128N64, kc > 0 ? 1u : 0u);
+            // + b2, the weight of the constant input
+            tc_mma(sm.tmem, smem_desc(smem_addr(sm.aone), 128, 256), smem_desc(w + kPackB2, 128, 256), kIdescBf16M128N64, 1u);
         }
         tc_commit(&sm.mbar);
     }
@@ -311,24 +342,25 @@ __device__ __forceinline__ float mlp_tile_end(MlpSmem& sm, MlpThread& st) {
         }
     }
     mlp_layer_sync(sm, 1, st);
-    const float4* b2 = reinterpret_cast<const float4*>(sm.w + kPackB2);
-    const float4* w3 = reinterpret_cast<const float4*>(sm.w + kPackW3);
-    float z = *reinterpret_cast<const float*>(sm.w + kPackB3);
-    if (__any_sync(0xffffffffu, st.abort)) return z;  // meaningless after an abort
+    const float b3 = *reinterpret_cast<const float*>(sm.w + kPackB3);
+    if (__any_sync(0xffffffffu, st.abort)) return b3;  // meaningless after an abort
+    // output layer on packed FP32 pairs (units 2j and 2j+1 side by side): two
+    // partial sums, over the even and the odd units, then b3 + even + odd
+    const ulonglong2* w3 = reinterpret_cast<const ulonglong2*>(sm.w + kPackW3);
+    uint64_t zz = 0ull;  // (0.f, 0.f)
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
         float v[16];
         tc_ld16(lane_base + 16 * c, v);
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const float4 w = w3[4 * c + j], bb = b2[4 * c + j];
-            z = __fmaf_rn(w.x, fmaxf(__fadd_rn(v[4 * j], bb.x), 0.f), z);
-            z = __fmaf_rn(w.y, fmaxf(__fadd_rn(v[4 * j + 1], bb.y), 0.f), z);
-            z = __fmaf_rn(w.z, fmaxf(__fadd_rn(v[4 * j + 2], bb.z), 0.f), z);
-            z = __fmaf_rn(w.w, fmaxf(__fadd_rn(v[4 * j + 3], bb.w), 0.f), z);
+            const ulonglong2 w = w3[4 * c + j];
+            zz = f2_fma(w.x, f2_relu(f2_pack(v[4 * j], v[4 * j + 1])), zz);
+            zz = f2_fma(w.y, f2_relu(f2_pack(v[4 * j + 2], v[4 * j + 3])), zz);
         }
     }
-    return z;
+    const float2 s = f2_unpack(zz);
+    return __fadd_rn(__fadd_rn(b3, s.x), s.y);
 }
 
 // One tile: thread t scores the features x of its candidate and gets the logit.
