@@ -197,13 +197,15 @@ int sdlg_get_counts(sdlg_ctx* ctx, int64_t event, int64_t* out5);
  * out (capacity `cap` tuples); *n_out receives the number of tuples. */
 int sdlg_get_objects(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int64_t cap, int64_t* n_out);
 
-/* The same tuples without waiting for the copy: they are written on the
- * device right away (so the next sdlg_run may follow at once) and copied to
- * `out` on a second stream while the caller goes on; out must stay valid
- * and untouched until sdlg_wait_objects() returns, and should be pinned
- * (sdlg_host_alloc) for the copy to overlap the next run.  *n_out is known
- * on return.  A later readback of the same context waits for this copy
- * before it reuses the device buffer. */
+/* The same tuples without waiting for the copy: a kernel on a second stream
+ * writes them into a device buffer once the run is complete, and the copy to
+ * `out` follows on that stream while the caller goes on (the next
+ * sdlg_set_events may follow at once; the next run starts once the kernel
+ * has read the objects).  out must stay valid and untouched until
+ * sdlg_wait_objects() returns, and should be pinned (sdlg_host_alloc) for the
+ * copy to overlap the next run.  *n_out is known on return.  A later
+ * readback of the same context waits for this copy before it reuses the
+ * device buffer. */
 int sdlg_get_objects_async(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int64_t cap, int64_t* n_out);
 int sdlg_wait_objects(sdlg_ctx* ctx);
 

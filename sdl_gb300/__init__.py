@@ -339,7 +339,9 @@ class Chain:
         """Start reading a stage's tuples into `out` (int32, C-contiguous,
         shape (>= n, width); pinned() memory for the copy to overlap the next
         run) and return n without waiting: `out` holds them once
-        wait_objects() returns."""
+        wait_objects() returns.  The tuples are gathered and copied on a
+        second stream; the next set_events may follow at once, and the next
+        run starts once they are gathered."""
         n = ctypes.c_int64()
         self._ck(lib().sdlg_get_objects(self.h, stage, event, None, 0, ctypes.byref(n)))
         if (out.dtype != np.int32 or out.ndim != 2 or out.shape[1] != WIDTH[stage] or out.shape[0] < n.value

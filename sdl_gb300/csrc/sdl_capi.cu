@@ -144,11 +144,13 @@ struct sdlg_ctx {
     // between calls: allocating a gigabyte afresh costs more than copying it)
     void* scratch = nullptr;
     int64_t scratch_bytes = 0;
-    // asynchronous readback: the copy of the scratch to the host runs on its
-    // own stream (ev_mat: the scratch is written; ev_copy: it has been read)
+    // asynchronous readback on its own stream: the kernel that writes the
+    // tuples into the scratch, then the copy to the host (ev_mat: the run that
+    // made the objects is complete; ev_read: the objects have been read, so a
+    // new run may overwrite them; ev_copy: the scratch has been copied)
     cudaStream_t copy_stream = nullptr;
-    cudaEvent_t ev_mat = nullptr, ev_copy = nullptr;
-    bool copy_pending = false;
+    cudaEvent_t ev_mat = nullptr, ev_read = nullptr, ev_copy = nullptr;
+    bool copy_pending = false, read_pending = false;
     int64_t* h_small = nullptr;   // pinned: n_rec[5], status
     // graph
     cudaGraphExec_t graph = nullptr;
@@ -179,7 +181,19 @@ int fail(sdlg_ctx* c, int code, const char* fmt, ...) {
         if (e_ != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
 
+// a new run (or freed buffers) must not overwrite objects that an
+// asynchronous readback still reads: its kernel runs on the copy stream
+void wait_readback(sdlg_ctx* ctx) {
+    if (!ctx->read_pending) return;
+    cudaStreamWaitEvent(ctx->stream, ctx->ev_read, 0);
+    ctx->read_pending = false;
+}
+
 void free_batch(sdlg_ctx* ctx) {
+    if (ctx->read_pending) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        ctx->read_pending = false;
+    }
     if (ctx->graph) {
         cudaGraphExecDestroy(ctx->graph);
         ctx->graph = nullptr;
@@ -196,6 +210,7 @@ int ensure_scratch(sdlg_ctx* ctx, size_t bytes, void** p) {
             cudaStreamSynchronize(ctx->stream);
             cudaStreamSynchronize(ctx->copy_stream);
             ctx->copy_pending = false;
+            ctx->read_pending = false;
             cudaFree(ctx->scratch);
         }
         ctx->scratch = nullptr;
@@ -573,6 +588,7 @@ int launch_checked(sdlg_ctx* ctx, int stop_after) {
 int launch(sdlg_ctx* ctx, int stop_after, int flags) {
     ctx->b.flags = flags;
     ctx->ran = true;
+    wait_readback(ctx);
 #ifdef SDL_DEVICE_CHECKS
     return launch_checked(ctx, stop_after);
 #endif
@@ -764,6 +780,7 @@ int sdlg_create(sdlg_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_mat, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_read, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming);
     for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&ctx->ev[k]);
     for (int k = 0; k < kNumStages && e == cudaSuccess; ++k) {
@@ -817,6 +834,7 @@ int sdlg_destroy(sdlg_ctx* ctx) {
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
     if (ctx->scratch) cudaFree(ctx->scratch);
     if (ctx->ev_mat) cudaEventDestroy(ctx->ev_mat);
+    if (ctx->ev_read) cudaEventDestroy(ctx->ev_read);
     if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
@@ -1069,6 +1087,7 @@ int sdlg_run_stages(sdlg_ctx* ctx, int first, int last, int flags) {
     ctx->b.flags = flags;
     ctx->last_stop = last;
     ctx->last_flags = flags;
+    wait_readback(ctx);
 #ifdef SDL_DEVICE_CHECKS
     int rc = launch_checked(ctx, last);
     if (rc) return rc;
@@ -1148,14 +1167,17 @@ int sdlg_get_objects_async(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out
     void* tmp = nullptr;
     rc = ensure_scratch(ctx, bytes, &tmp);
     if (rc) return rc;
-    // the tuples are written to the scratch on the context stream (after the
-    // run, before the next one) once the previous readback has read it; the
-    // copy to the host then runs on the copy stream, beside the next run
-    if (ctx->copy_pending) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0));
-    launch_materialize(ctx->b, stage, first, n, static_cast<int32_t*>(tmp), ctx->stream);
-    CK(cudaGetLastError());
+    // the tuples are written to the scratch on the copy stream, after the run
+    // that made them (ev_mat) and after the previous readback's copy (stream
+    // order), then copied to the host there; the next run waits for the
+    // kernel alone (ev_read, wait_readback), so that the kernel overlaps the
+    // next batch's input copy and the copy overlaps the next run
     CK(cudaEventRecord(ctx->ev_mat, ctx->stream));
     CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_mat, 0));
+    launch_materialize(ctx->b, stage, first, n, static_cast<int32_t*>(tmp), ctx->copy_stream);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ctx->ev_read, ctx->copy_stream));
+    ctx->read_pending = true;
     CK(cudaMemcpyAsync(out, tmp, bytes, cudaMemcpyDeviceToHost, ctx->copy_stream));
     CK(cudaEventRecord(ctx->ev_copy, ctx->copy_stream));
     ctx->copy_pending = true;

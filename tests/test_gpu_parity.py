@@ -154,6 +154,29 @@ def test_async_readback_overlaps_the_next_run(gpu, oracle_lib):
     gpu.wait_objects()  # nothing pending: returns at once
 
 
+def test_async_readback_before_a_run_on_the_same_buffers(gpu, oracle_lib):
+    """The asynchronous readback's gathering kernel runs on the copy stream:
+    a next batch of the same shape (no reallocation) set and run right after
+    it must not overwrite the objects before they are gathered."""
+    from sdl_gb300 import synth
+    det, ev_a = synth.workload_event("pu", 11, pu=100)
+    _, ev_b = synth.workload_event("pu", 12, pu=100)
+    run_gpu(gpu, det, [ev_a, ev_b], 0)
+    want = [gpu.objects(s, -1) for s in range(5)]
+    width = (2, 4, 8, 8, 16)
+    bufs = [gpu.pinned(len(w) * width[s] * 4 + 16)[:len(w) * width[s] * 4].view(np.int32).reshape(len(w), width[s])
+            for s, w in enumerate(want)]
+    for s in range(5):
+        assert gpu.objects_async(s, -1, bufs[s]) == len(want[s])
+    gpu.set_events([ev_b, ev_a])  # the same events and hits: the buffers stay
+    gpu.run(4, 0)
+    gpu.wait_objects()
+    for s in range(5):
+        assert np.array_equal(bufs[s], want[s]), s
+    ref, _, _ = oracle_lib.Oracle(det).run(ev_b)
+    assert oracle_lib.digest(gpu.objects(4, 0)) == oracle_lib.digest(ref[4])
+
+
 def test_stop_after_stage(gpu, oracle_lib):
     from sdl_gb300 import synth
     det, ev = synth.workload_event("barrel_flat", 5)
