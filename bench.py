@@ -457,12 +457,28 @@ def main():
     n_tc_cap = 2 * int(n_pruned[4]) + 1024
     tc_outs = [ch.pinned(n_tc_cap * 16 * 4).view(np.int32).reshape(n_tc_cap, 16) for _ in range(2)]
 
-    def e2e_step(k, pipelined):
-        ch.set_events_raw(len(batch), evoff.ctypes.data, *[v.ctypes.data for v in views])
+    in_ptrs = (len(batch), evoff.ctypes.data, *[v.ctypes.data for v in views])
+
+    def e2e_step(k):
+        ch.set_events_raw(*in_ptrs)
         ch.run(4, FLAG_MLP)
-        if pipelined:  # the copy of this step's candidates overlaps the next step
-            return ch.objects_async(4, -1, tc_outs[k & 1]) * 64 + 8 * 2
         return ch.objects(4, -1, out=tc_outs[k & 1]).nbytes + 8 * 2
+
+    def e2e_stream(n):
+        """n steps streamed: the first step's inputs by sdlg_set_events, every
+        later step's staged during the step before it (sdlg_stage_events);
+        each step's candidates gathered and copied out while the next step
+        runs (sdlg_get_objects_async); returns the bytes read per step"""
+        ch.set_events_raw(*in_ptrs)
+        out = []
+        for k in range(n):
+            ch.run_async(4, FLAG_MLP)
+            if k + 1 < n:
+                ch.stage_events_raw(*in_ptrs)
+            ch.sync()
+            out.append(ch.objects_async(4, -1, tc_outs[k & 1]) * 64 + 8 * 2)
+        ch.wait_objects()
+        return out
 
     # (1) one step after another, each ending when its candidates are in host
     # memory; L2 flushed before each step
@@ -470,23 +486,21 @@ def main():
     for k in range(a.warmup + a.steps):
         flush()
         t0 = time.perf_counter()
-        nb = e2e_step(k, False)
+        nb = e2e_step(k)
         t1 = time.perf_counter()
         if k >= a.warmup:
             e2e_ms.append((t1 - t0) * 1e3)
             d2h.append(nb)
     e2e_sync_mean = allmax(pg, statistics.fmean(e2e_ms))
-    # (2) the same steps back to back, each step's readback copied while the
-    # next step runs; timed from the first step's inputs to the last step's
-    # candidates in host memory (inputs of 280 MB, above the L2's 129 MB)
-    for k in range(a.warmup):
-        e2e_step(k, True)
-    ch.wait_objects()
+    # (2) the same steps streamed: each step's inputs copied in during the
+    # step before it and its candidates copied out during the step after it;
+    # timed from the first step's inputs to the last step's candidates in
+    # host memory (inputs of 280 MB, above the L2's 129 MB)
+    e2e_stream(a.warmup)
     flush()
     barrier(pg)
     t0 = time.perf_counter()
-    d2h_p = [e2e_step(k, True) for k in range(a.steps)]
-    ch.wait_objects()
+    d2h_p = e2e_stream(a.steps)
     t1 = time.perf_counter()
     e2e_mean = allmax(pg, (t1 - t0) * 1e3 / a.steps)
     e2e_value = allsum(pg, len(batch)) * 1e3 / e2e_mean
@@ -723,9 +737,11 @@ def main():
             "stated_density": dense, "batched_uneven": uneven,
             "e2e": {"value": round(e2e_value, 3), "unit": "events/s", "ms_per_step": round(e2e_mean, 3),
                     "h2d_bytes_per_step": n_hit * 20 + 8 * (len(batch) + 1), "d2h_bytes_per_step": int(statistics.fmean(d2h_p)),
-                    "path": "per step: sdlg_set_events (pinned host) + sdlg_run(SDLG_FLAG_MLP) + sdlg_get_objects_async(TC, "
-                            "into pinned host memory); the steps back to back, each step's readback overlapping the next "
-                            "step's run; timed until sdlg_wait_objects returns after the last step",
+                    "path": "streamed steps from pinned host memory: the first step's inputs by sdlg_set_events, each "
+                            "later step's by sdlg_stage_events during the step before it; per step sdlg_run_async("
+                            "SDLG_FLAG_MLP) + sdlg_sync + sdlg_get_objects_async(TC, into pinned host memory), the "
+                            "readback overlapping the next step's run; timed from the first inputs until "
+                            "sdlg_wait_objects returns after the last step",
                     "unpipelined": {"value": round(e2e_sync_value, 3), "ms_per_step": round(e2e_sync_mean, 3),
                                     "d2h_bytes_per_step": int(statistics.fmean(d2h)),
                                     "path": "sdlg_set_events + sdlg_run + sdlg_get_objects (synchronous), "

@@ -159,6 +159,21 @@ int64_t sdlg_num_modules(const sdlg_ctx* ctx);
 int sdlg_set_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, const float* x, const float* y,
                     const float* z, const int32_t* idx, const uint32_t* detid);
 
+/* The next batch (arguments as sdlg_set_events; no counterpart in the
+ * reference), copied to the device while a run of the current batch may
+ * still be going: on its own stream into a device staging area, returning
+ * once the host buffers have been read.  The next run from the hits
+ * (sdlg_run, sdlg_run_async, sdlg_autotune, sdlg_run_stages from stage 0)
+ * first copies it into the batch buffers on the device and takes it as its
+ * events; until then the current batch's results stay readable.  A batch
+ * whose event count differs from the current one, or whose hits exceed the
+ * buffers, waits on the host and takes sdlg_set_events' path at that run.
+ * sdlg_set_events drops a staged batch.  The streaming pattern: set the
+ * first batch, then per batch sdlg_run_async, sdlg_stage_events of the next
+ * one, sdlg_sync, sdlg_get_objects_async. */
+int sdlg_stage_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, const float* x, const float* y,
+                      const float* z, const int32_t* idx, const uint32_t* detid);
+
 /* Run the chain createMiniDoublets -> createSegmentsWithModuleMap ->
  * createTrackletsWithModuleMap -> createTriplets -> createTrackCandidates
  * (Event.cc:245-305, 445-522, 611-693, 524-597, 823-872) on every event of
@@ -197,15 +212,15 @@ int sdlg_get_counts(sdlg_ctx* ctx, int64_t event, int64_t* out5);
  * out (capacity `cap` tuples); *n_out receives the number of tuples. */
 int sdlg_get_objects(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int64_t cap, int64_t* n_out);
 
-/* The same tuples without waiting for the copy: a kernel on a second stream
- * writes them into a device buffer once the run is complete, and the copy to
- * `out` follows on that stream while the caller goes on (the next
- * sdlg_set_events may follow at once; the next run starts once the kernel
- * has read the objects).  out must stay valid and untouched until
+/* The same tuples without waiting for the copy: a kernel on a gather stream
+ * writes them into one of two device buffers (used in turn) once the run is
+ * complete, and the copy to `out` follows on a copy stream while the caller
+ * goes on (the next sdlg_set_events or sdlg_stage_events may follow at once;
+ * the next run starts once the kernel has read the objects, without waiting
+ * for the copy).  out must stay valid and untouched until
  * sdlg_wait_objects() returns, and should be pinned (sdlg_host_alloc) for the
  * copy to overlap the next run.  *n_out is known on return.  A later
- * readback of the same context waits for this copy before it reuses the
- * device buffer. */
+ * readback into the same device buffer waits for this copy first. */
 int sdlg_get_objects_async(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int64_t cap, int64_t* n_out);
 int sdlg_wait_objects(sdlg_ctx* ctx);
 

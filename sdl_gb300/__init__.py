@@ -71,6 +71,7 @@ def lib():
         L.sdlg_num_modules.argtypes = [vp]
         L.sdlg_num_modules.restype = i64
         L.sdlg_set_events.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp]
+        L.sdlg_stage_events.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp]
         L.sdlg_run.argtypes = [vp, i32, i32]
         L.sdlg_run_async.argtypes = [vp, i32, i32]
         L.sdlg_sync.argtypes = [vp]
@@ -264,9 +265,8 @@ class Chain:
         self._pinned.append(p)
         return np.ctypeslib.as_array((ctypes.c_uint8 * nbytes).from_address(p.value))
 
-    def set_events(self, events=None, *, ev_off=None, x=None, y=None, z=None, idx=None, detid=None):
-        """Either a list of objects with x/y/z/idx/detid arrays, or the
-        concatenated arrays with ev_off (int64, n_events + 1)."""
+    @staticmethod
+    def _event_arrays(events, ev_off, x, y, z, idx, detid):
         if events is not None:
             ev_off = np.zeros(len(events) + 1, dtype=np.int64)
             ev_off[1:] = np.cumsum([len(e.x) for e in events])
@@ -278,15 +278,41 @@ class Chain:
         ev_off = np.ascontiguousarray(ev_off, dtype=np.int64)
         arrs = [np.ascontiguousarray(a, dtype=d) for a, d in
                 ((x, np.float32), (y, np.float32), (z, np.float32), (idx, np.int32), (detid, np.uint32))]
+        return ev_off, arrs
+
+    def set_events(self, events=None, *, ev_off=None, x=None, y=None, z=None, idx=None, detid=None):
+        """Either a list of objects with x/y/z/idx/detid arrays, or the
+        concatenated arrays with ev_off (int64, n_events + 1)."""
+        ev_off, arrs = self._event_arrays(events, ev_off, x, y, z, idx, detid)
         self._ck(lib().sdlg_set_events(self.h, len(ev_off) - 1, ev_off.ctypes.data, *[a.ctypes.data for a in arrs]))
         self.n_events = len(ev_off) - 1
+        self._staged = None
 
     def set_events_raw(self, n_events, ev_off_ptr, x_ptr, y_ptr, z_ptr, idx_ptr, det_ptr):
         self._ck(lib().sdlg_set_events(self.h, n_events, ev_off_ptr, x_ptr, y_ptr, z_ptr, idx_ptr, det_ptr))
         self.n_events = n_events
+        self._staged = None
+
+    def stage_events(self, events=None, *, ev_off=None, x=None, y=None, z=None, idx=None, detid=None):
+        """The next batch (arguments as set_events), copied to the device
+        while a run may still be going; the next run from the hits
+        (run, run_async, autotune) takes it as its events."""
+        ev_off, arrs = self._event_arrays(events, ev_off, x, y, z, idx, detid)
+        self._ck(lib().sdlg_stage_events(self.h, len(ev_off) - 1, ev_off.ctypes.data, *[a.ctypes.data for a in arrs]))
+        self._staged = len(ev_off) - 1
+
+    def stage_events_raw(self, n_events, ev_off_ptr, x_ptr, y_ptr, z_ptr, idx_ptr, det_ptr):
+        self._ck(lib().sdlg_stage_events(self.h, n_events, ev_off_ptr, x_ptr, y_ptr, z_ptr, idx_ptr, det_ptr))
+        self._staged = n_events
+
+    def _take_staged(self):
+        if getattr(self, "_staged", None) is not None:
+            self.n_events = self._staged
+            self._staged = None
 
     # running ----------------------------------------------------------------
     def run(self, stop_after: int = 4, flags: int = 0):
+        self._take_staged()
         self._ck(lib().sdlg_run(self.h, stop_after, flags))
 
     def set_capacities(self, caps):
@@ -305,9 +331,12 @@ class Chain:
     def run_stages(self, first: int, last: int, flags: int = 0):
         """Stages first..last (one create* call at a time): continues the last
         run when `first` follows its final stage, else runs from the hits."""
+        if int(first) == 0:
+            self._take_staged()
         self._ck(lib().sdlg_run_stages(self.h, int(first), int(last), int(flags)))
 
     def run_async(self, stop_after: int = 4, flags: int = 0):
+        self._take_staged()
         self._ck(lib().sdlg_run_async(self.h, stop_after, flags))
 
     def sync(self):
@@ -547,6 +576,7 @@ class Chain:
     def autotune(self, stop_after: int = 4, flags: int = 0) -> dict:
         """Pick the fastest launch shape per stage on the current batch (kept for later runs)."""
         out = np.zeros(10, dtype=np.int32)
+        self._take_staged()
         self._ck(lib().sdlg_autotune(self.h, int(stop_after), int(flags), out.ctypes.data))
         return {"task": [int(v) for v in out[:5]], "ctas_per_sm": [int(v) for v in out[5:]]}
 

@@ -140,18 +140,42 @@ struct sdlg_ctx {
     // pinned staging
     void* pinned = nullptr;
     int64_t pinned_bytes = 0;
-    // device scratch for results on their way to pageable host memory (kept
-    // between calls: allocating a gigabyte afresh costs more than copying it)
-    void* scratch = nullptr;
-    int64_t scratch_bytes = 0;
-    // asynchronous readback on its own stream: the kernel that writes the
-    // tuples into the scratch, then the copy to the host (ev_mat: the run that
-    // made the objects is complete; ev_read: the objects have been read, so a
-    // new run may overwrite them; ev_copy: the scratch has been copied)
-    cudaStream_t copy_stream = nullptr;
-    cudaEvent_t ev_mat = nullptr, ev_read = nullptr, ev_copy = nullptr;
-    bool copy_pending = false, read_pending = false;
+    // device scratch for results on their way to host memory, two buffers
+    // (kept between calls: allocating a gigabyte afresh costs more than
+    // copying it); the synchronous readbacks use the first
+    void* scratch[2] = {nullptr, nullptr};
+    int64_t scratch_bytes[2] = {0, 0};
+    // asynchronous readback: a kernel on the gather stream writes the tuples
+    // into the next scratch buffer once the run that made the objects is
+    // complete (ev_mat) and that buffer's previous copy has read it
+    // (ev_copy[k]), then the copy stream copies them to the host.  ev_read:
+    // the objects have been read, so a new run may overwrite them.  The
+    // gathering never waits behind the previous readback's copy.
+    cudaStream_t copy_stream = nullptr, gather_stream = nullptr;
+    cudaEvent_t ev_mat = nullptr, ev_read = nullptr, ev_copy[2] = {nullptr, nullptr};
+    bool copy_pending[2] = {false, false}, read_pending = false;
+    int next_scratch = 0;
     int64_t* h_small = nullptr;   // pinned: n_rec[5], status
+    // the next batch, copied to the device while a run may still be going
+    // (sdlg_stage_events) and installed by the next run from the hits: one
+    // device allocation of x, y, z, idx, detid (hits each) and the offsets
+    // (events + 1), copied on its own stream (ev_in: the copy is done;
+    // ev_used: the install's copies have read it); a batch that does not fit
+    // the current buffers waits on the host (host_*) for the next run
+    struct {
+        char* dev = nullptr;
+        int64_t hits = 0, evs = 0;  // capacity of dev
+        int64_t* h_off = nullptr;   // pinned offsets on their way to dev
+        int64_t h_off_cap = 0;
+        int64_t n_ev = 0, n_hit = 0;
+        std::vector<int64_t> ev_off;
+        bool pending = false, on_host = false, used_pending = false;
+        std::vector<float> host_f[3];
+        std::vector<int32_t> host_idx;
+        std::vector<uint32_t> host_det;
+        cudaStream_t stream = nullptr;
+        cudaEvent_t ev_in = nullptr, ev_used = nullptr;
+    } stage;
     // graph
     cudaGraphExec_t graph = nullptr;
     int graph_stop = -1, graph_flags = -1;
@@ -181,6 +205,9 @@ int fail(sdlg_ctx* c, int code, const char* fmt, ...) {
         if (e_ != cudaSuccess) return fail(ctx, SDLG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
 
+int set_events_impl(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, const float* x, const float* y, const float* z,
+                    const int32_t* idx, const uint32_t* detid);
+
 // a new run (or freed buffers) must not overwrite objects that an
 // asynchronous readback still reads: its kernel runs on the copy stream
 void wait_readback(sdlg_ctx* ctx) {
@@ -191,7 +218,7 @@ void wait_readback(sdlg_ctx* ctx) {
 
 void free_batch(sdlg_ctx* ctx) {
     if (ctx->read_pending) {
-        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamSynchronize(ctx->gather_stream);
         ctx->read_pending = false;
     }
     if (ctx->graph) {
@@ -203,24 +230,25 @@ void free_batch(sdlg_ctx* ctx) {
     ctx->buffers_ok = false;
 }
 
-// ctx->scratch grown to at least `bytes` (with a quarter of headroom)
-int ensure_scratch(sdlg_ctx* ctx, size_t bytes, void** p) {
-    if (ctx->scratch_bytes < (int64_t)bytes) {
-        if (ctx->scratch) {
+// ctx->scratch[k] grown to at least `bytes` (with a quarter of headroom)
+int ensure_scratch(sdlg_ctx* ctx, int k, size_t bytes, void** p) {
+    if (ctx->scratch_bytes[k] < (int64_t)bytes) {
+        if (ctx->scratch[k]) {
             cudaStreamSynchronize(ctx->stream);
+            cudaStreamSynchronize(ctx->gather_stream);
             cudaStreamSynchronize(ctx->copy_stream);
-            ctx->copy_pending = false;
+            ctx->copy_pending[0] = ctx->copy_pending[1] = false;
             ctx->read_pending = false;
-            cudaFree(ctx->scratch);
+            cudaFree(ctx->scratch[k]);
         }
-        ctx->scratch = nullptr;
-        ctx->scratch_bytes = 0;
+        ctx->scratch[k] = nullptr;
+        ctx->scratch_bytes[k] = 0;
         const size_t want = bytes + bytes / 4 + 256;
-        cudaError_t e = cudaMalloc(&ctx->scratch, want);
+        cudaError_t e = cudaMalloc(&ctx->scratch[k], want);
         if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CAPACITY, "cudaMalloc(%zu): %s", want, cudaGetErrorString(e));
-        ctx->scratch_bytes = (int64_t)want;
+        ctx->scratch_bytes[k] = (int64_t)want;
     }
-    *p = ctx->scratch;
+    *p = ctx->scratch[k];
     return SDLG_OK;
 }
 
@@ -639,7 +667,7 @@ int finish(sdlg_ctx* ctx) {
             const std::vector<int64_t> off = ctx->ev_off;
             int rc = build_module_table(ctx, hd);
             if (rc) return rc;
-            rc = sdlg_set_events(ctx, ctx->n_ev, off.data(), keep[0].data(), keep[1].data(), keep[2].data(), ki.data(), hd.data());
+            rc = set_events_impl(ctx, ctx->n_ev, off.data(), keep[0].data(), keep[1].data(), keep[2].data(), ki.data(), hd.data());
             if (rc) return rc;
             rc = launch(ctx, ctx->last_stop, ctx->last_flags);
             if (rc) return rc;
@@ -674,7 +702,7 @@ int finish(sdlg_ctx* ctx) {
         CK(cudaMemcpy(z.data(), ctx->b.in_z, ctx->n_hit * 4, cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(idx.data(), ctx->b.in_idx, ctx->n_hit * 4, cudaMemcpyDeviceToHost));
         CK(cudaMemcpy(det.data(), ctx->b.in_det, ctx->n_hit * 4, cudaMemcpyDeviceToHost));
-        int rc = sdlg_set_events(ctx, ctx->n_ev, off.data(), x.data(), y.data(), z.data(), idx.data(), det.data());
+        int rc = set_events_impl(ctx, ctx->n_ev, off.data(), x.data(), y.data(), z.data(), idx.data(), det.data());
         if (rc) return rc;
         rc = launch(ctx, ctx->last_stop, ctx->last_flags);
         if (rc) return rc;
@@ -779,9 +807,13 @@ int sdlg_create(sdlg_ctx** out, int device) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->n_sm, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->gather_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stage.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->stage.ev_in, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->stage.ev_used, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_mat, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_read, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&ctx->ev_copy[k], cudaEventDisableTiming);
     for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreate(&ctx->ev[k]);
     for (int k = 0; k < kNumStages && e == cudaSuccess; ++k) {
         e = cudaEventCreate(&ctx->hooks.enum_start[k]);
@@ -822,8 +854,15 @@ int sdlg_destroy(sdlg_ctx* ctx) {
     if (!ctx) return SDLG_ERR_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->gather_stream) cudaStreamSynchronize(ctx->gather_stream);
     if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    if (ctx->stage.stream) cudaStreamSynchronize(ctx->stage.stream);
     free_batch(ctx);
+    if (ctx->stage.dev) cudaFree(ctx->stage.dev);
+    if (ctx->stage.h_off) cudaFreeHost(ctx->stage.h_off);
+    if (ctx->stage.ev_in) cudaEventDestroy(ctx->stage.ev_in);
+    if (ctx->stage.ev_used) cudaEventDestroy(ctx->stage.ev_used);
+    if (ctx->stage.stream) cudaStreamDestroy(ctx->stage.stream);
     cudaFree(ctx->d_detid); cudaFree(ctx->d_mod); cudaFree(ctx->d_conn_off); cudaFree(ctx->d_conn_idx);
     cudaFree(ctx->d_slot_run);
     {
@@ -832,11 +871,14 @@ int sdlg_destroy(sdlg_ctx* ctx) {
         for (void* p : ps) cudaFree(p);
     }
     if (ctx->pinned) cudaFreeHost(ctx->pinned);
-    if (ctx->scratch) cudaFree(ctx->scratch);
+    for (int k = 0; k < 2; ++k)
+        if (ctx->scratch[k]) cudaFree(ctx->scratch[k]);
     if (ctx->ev_mat) cudaEventDestroy(ctx->ev_mat);
     if (ctx->ev_read) cudaEventDestroy(ctx->ev_read);
-    if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
+    for (int k = 0; k < 2; ++k)
+        if (ctx->ev_copy[k]) cudaEventDestroy(ctx->ev_copy[k]);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    if (ctx->gather_stream) cudaStreamDestroy(ctx->gather_stream);
     if (ctx->h_small) cudaFreeHost(ctx->h_small);
     for (int k = 0; k < 8; ++k) if (ctx->ev[k]) cudaEventDestroy(ctx->ev[k]);
     for (int k = 0; k < kNumStages; ++k) {
@@ -967,17 +1009,35 @@ int sdlg_geometry_upload(sdlg_ctx* ctx, int64_t n_tilted, const uint32_t* t_deti
 
 int64_t sdlg_num_modules(const sdlg_ctx* ctx) { return ctx ? (int64_t)ctx->detids.size() : -1; }
 
-int sdlg_set_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, const float* x, const float* y, const float* z,
-                    const int32_t* idx, const uint32_t* detid) {
+}  // extern "C"
+
+namespace {
+
+// the checks of sdlg_set_events and sdlg_stage_events; n: the batch's hits
+int check_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, const float* x, const float* y, const float* z,
+                 const int32_t* idx, const uint32_t* detid, int64_t* n_out) {
     if (!ctx || n_events <= 0 || !ev_off) return SDLG_ERR_ARG;
     if (!ctx->have_geo) return fail(ctx, SDLG_ERR_NO_GEOMETRY, "no geometry loaded");
-    cudaSetDevice(ctx->device);
     if (ev_off[0] != 0) return fail(ctx, SDLG_ERR_ARG, "ev_off[0] must be 0");
     for (int64_t e = 0; e < n_events; ++e)
         if (ev_off[e + 1] < ev_off[e]) return fail(ctx, SDLG_ERR_ARG, "event offsets not monotone");
     const int64_t n = ev_off[n_events];
     if (n > 0 && (!x || !y || !z || !idx || !detid)) return fail(ctx, SDLG_ERR_ARG, "null hit array");
     if (n > INT32_MAX / 4) return fail(ctx, SDLG_ERR_ARG, "too many hits in one batch");
+    *n_out = n;
+    return SDLG_OK;
+}
+
+// the staged device batch's layout: x, y, z, idx, detid (S.hits each), then
+// the offsets (S.evs + 1) and the hit count, 256-byte aligned
+size_t stage_off_pos(int64_t hits) { return ((size_t)hits * 20 + 255) / 256 * 256; }
+
+int set_events_impl(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, const float* x, const float* y, const float* z,
+                    const int32_t* idx, const uint32_t* detid) {
+    int64_t n = 0;
+    int rc0 = check_events(ctx, n_events, ev_off, x, y, z, idx, detid, &n);
+    if (rc0) return rc0;
+    cudaSetDevice(ctx->device);
     // wait for any run still reading the inputs
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->n_ev = n_events;
@@ -1025,8 +1085,174 @@ int sdlg_set_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, cons
     return SDLG_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int sdlg_set_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, const float* x, const float* y, const float* z,
+                    const int32_t* idx, const uint32_t* detid) {
+    if (!ctx) return SDLG_ERR_ARG;
+    // these events replace a staged batch
+    auto& S = ctx->stage;
+    S.pending = false;
+    S.on_host = false;
+    for (auto& v : S.host_f) std::vector<float>().swap(v);
+    std::vector<int32_t>().swap(S.host_idx);
+    std::vector<uint32_t>().swap(S.host_det);
+    return set_events_impl(ctx, n_events, ev_off, x, y, z, idx, detid);
+}
+
+int sdlg_stage_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, const float* x, const float* y, const float* z,
+                      const int32_t* idx, const uint32_t* detid) {
+    int64_t n = 0;
+    int rc = check_events(ctx, n_events, ev_off, x, y, z, idx, detid, &n);
+    if (rc) return rc;
+    cudaSetDevice(ctx->device);
+    auto& S = ctx->stage;
+    // the previous staging's copy may still read the pinned offsets
+    CK(cudaStreamSynchronize(S.stream));
+    S.pending = false;
+    S.on_host = false;
+    S.n_ev = n_events;
+    S.n_hit = n;
+    S.ev_off.assign(ev_off, ev_off + n_events + 1);
+    if (!(ctx->buffers_ok && n_events == ctx->cap_ev && n <= ctx->cap_hit)) {
+        // the batch needs other buffers: it waits on the host, and the next
+        // run reallocates and uploads it (sdlg_set_events' path)
+        S.host_f[0].assign(x, x + n);
+        S.host_f[1].assign(y, y + n);
+        S.host_f[2].assign(z, z + n);
+        S.host_idx.assign(idx, idx + n);
+        S.host_det.assign(detid, detid + n);
+        S.on_host = true;
+        S.pending = true;
+        return SDLG_OK;
+    }
+    for (auto& v : S.host_f) std::vector<float>().swap(v);
+    std::vector<int32_t>().swap(S.host_idx);
+    std::vector<uint32_t>().swap(S.host_det);
+    if (S.hits < ctx->cap_hit || S.evs < ctx->cap_ev) {
+        // an install may still read the old allocation
+        if (S.used_pending) CK(cudaEventSynchronize(S.ev_used));
+        S.used_pending = false;
+        if (S.dev) cudaFree(S.dev);
+        S.dev = nullptr;
+        S.hits = S.evs = 0;
+        const size_t bytes = stage_off_pos(ctx->cap_hit) + (size_t)(ctx->cap_ev + 2) * sizeof(int64_t);
+        cudaError_t e = cudaMalloc(&S.dev, bytes);
+        if (e != cudaSuccess) return fail(ctx, SDLG_ERR_CAPACITY, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+        S.hits = ctx->cap_hit;
+        S.evs = ctx->cap_ev;
+    }
+    if (S.h_off_cap < n_events + 2) {
+        if (S.h_off) cudaFreeHost(S.h_off);
+        S.h_off = nullptr;
+        S.h_off_cap = 0;
+        CK(cudaMallocHost((void**)&S.h_off, (n_events + 2) * sizeof(int64_t)));
+        S.h_off_cap = n_events + 2;
+    }
+    std::memcpy(S.h_off, ev_off, (n_events + 1) * sizeof(int64_t));
+    S.h_off[n_events + 1] = n;
+    // the previous install's copies out of the staging come first
+    if (S.used_pending) CK(cudaStreamWaitEvent(S.stream, S.ev_used, 0));
+    const void* src[5] = {x, y, z, idx, detid};
+    const size_t bytes = (size_t)n * 4;
+    bool all_pinned = true;
+    for (int k = 0; k < 5 && n > 0; ++k) {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, src[k]) != cudaSuccess || a.type != cudaMemoryTypeHost) {
+            cudaGetLastError();
+            all_pinned = false;
+        }
+    }
+    if (n > 0 && !all_pinned) {
+        // through the pinned host staging (free: its users wait for their copies)
+        if (ctx->pinned_bytes < (int64_t)(bytes * 5)) {
+            if (ctx->pinned) cudaFreeHost(ctx->pinned);
+            ctx->pinned = nullptr;
+            ctx->pinned_bytes = 0;
+            CK(cudaMallocHost(&ctx->pinned, bytes * 5));
+            ctx->pinned_bytes = (int64_t)bytes * 5;
+        }
+        char* p = static_cast<char*>(ctx->pinned);
+        for (int k = 0; k < 5; ++k) {
+            std::memcpy(p + k * bytes, src[k], bytes);
+            src[k] = p + k * bytes;
+        }
+    }
+    for (int k = 0; k < 5 && n > 0; ++k)
+        CK(cudaMemcpyAsync(S.dev + (size_t)k * S.hits * 4, src[k], bytes, cudaMemcpyHostToDevice, S.stream));
+    CK(cudaMemcpyAsync(S.dev + stage_off_pos(S.hits), S.h_off, (n_events + 2) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                       S.stream));
+    CK(cudaEventRecord(S.ev_in, S.stream));
+    // the caller's buffers are read when this returns
+    CK(cudaEventSynchronize(S.ev_in));
+    S.pending = true;
+    return SDLG_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// the staged batch becomes the context's events, at the start of a run from
+// the hits: copies from the staging into the batch buffers on the context
+// stream (after the staging's own copy), or sdlg_set_events' path for a
+// batch that waits on the host or no longer fits
+int install_staged(sdlg_ctx* ctx) {
+    auto& S = ctx->stage;
+    if (!S.pending) return SDLG_OK;
+    S.pending = false;
+    if (!S.on_host && !(ctx->buffers_ok && S.n_ev == ctx->cap_ev && S.n_hit <= ctx->cap_hit)) {
+        // the buffers changed since the batch was staged: back through the host
+        CK(cudaStreamSynchronize(S.stream));
+        const size_t bytes = (size_t)S.n_hit * 4;
+        S.host_f[0].resize(S.n_hit); S.host_f[1].resize(S.n_hit); S.host_f[2].resize(S.n_hit);
+        S.host_idx.resize(S.n_hit); S.host_det.resize(S.n_hit);
+        void* dst[5] = {S.host_f[0].data(), S.host_f[1].data(), S.host_f[2].data(), S.host_idx.data(), S.host_det.data()};
+        for (int k = 0; k < 5 && S.n_hit > 0; ++k)
+            CK(cudaMemcpy(dst[k], S.dev + (size_t)k * S.hits * 4, bytes, cudaMemcpyDeviceToHost));
+        S.on_host = true;
+    }
+    if (S.on_host) {
+        S.on_host = false;
+        const int rc = set_events_impl(ctx, S.n_ev, S.ev_off.data(), S.host_f[0].data(), S.host_f[1].data(),
+                                       S.host_f[2].data(), S.host_idx.data(), S.host_det.data());
+        for (auto& v : S.host_f) std::vector<float>().swap(v);
+        std::vector<int32_t>().swap(S.host_idx);
+        std::vector<uint32_t>().swap(S.host_det);
+        return rc;
+    }
+    BatchDev& b = ctx->b;
+    cudaStream_t s = ctx->stream;
+    CK(cudaStreamWaitEvent(s, S.ev_in, 0));
+    void* dstp[5] = {(void*)b.in_x, (void*)b.in_y, (void*)b.in_z, (void*)b.in_idx, (void*)b.in_det};
+    for (int k = 0; k < 5 && S.n_hit > 0; ++k)
+        CK(cudaMemcpyAsync(dstp[k], S.dev + (size_t)k * S.hits * 4, (size_t)S.n_hit * 4, cudaMemcpyDeviceToDevice, s));
+    const char* offs = S.dev + stage_off_pos(S.hits);
+    CK(cudaMemcpyAsync(const_cast<int64_t*>(b.ev_off), offs, (S.n_ev + 1) * sizeof(int64_t), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(const_cast<int64_t*>(b.n_hit), offs + (S.n_ev + 1) * sizeof(int64_t), sizeof(int64_t),
+                       cudaMemcpyDeviceToDevice, s));
+    CK(cudaEventRecord(S.ev_used, s));
+    S.used_pending = true;
+    ctx->n_ev = S.n_ev;
+    ctx->n_hit = S.n_hit;
+    ctx->ev_off = S.ev_off;
+    ctx->ran = false;
+    return SDLG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int sdlg_run_async(sdlg_ctx* ctx, int stop_after, int flags) {
     if (!ctx) return SDLG_ERR_ARG;
+    if (ctx->stage.pending) {
+        cudaSetDevice(ctx->device);
+        const int rc = install_staged(ctx);
+        if (rc) return rc;
+    }
     if (!ctx->have_geo) return fail(ctx, SDLG_ERR_NO_GEOMETRY, "no geometry loaded");
     if (!ctx->buffers_ok || ctx->n_ev <= 0) return fail(ctx, SDLG_ERR_NO_EVENTS, "no events set");
     if (stop_after < 0 || stop_after > 4) return fail(ctx, SDLG_ERR_ARG, "stop_after out of range");
@@ -1143,9 +1369,9 @@ int sdlg_get_objects(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out, int6
     // 128-event batch's track candidates: 9 ms, against 26 ms for the kernel
     // writing pinned host memory itself)
     void* tmp = nullptr;
-    rc = ensure_scratch(ctx, bytes, &tmp);
+    rc = ensure_scratch(ctx, 0, bytes, &tmp);
     if (rc) return rc;
-    if (ctx->copy_pending) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0));
+    if (ctx->copy_pending[0]) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copy[0], 0));
     launch_materialize(ctx->b, stage, first, n, static_cast<int32_t*>(tmp), ctx->stream);
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, tmp, bytes, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1164,32 +1390,39 @@ int sdlg_get_objects_async(sdlg_ctx* ctx, int stage, int64_t event, int32_t* out
     if (cap < n) return fail(ctx, SDLG_ERR_ARG, "output capacity %lld < %lld tuples", (long long)cap, (long long)n);
     static const int width[5] = {2, 4, 8, 8, 16};
     const size_t bytes = (size_t)n * width[stage] * 4;
+    const int kb = ctx->next_scratch;
     void* tmp = nullptr;
-    rc = ensure_scratch(ctx, bytes, &tmp);
+    rc = ensure_scratch(ctx, kb, bytes, &tmp);
     if (rc) return rc;
-    // the tuples are written to the scratch on the copy stream, after the run
-    // that made them (ev_mat) and after the previous readback's copy (stream
-    // order), then copied to the host there; the next run waits for the
-    // kernel alone (ev_read, wait_readback), so that the kernel overlaps the
-    // next batch's input copy and the copy overlaps the next run
+    ctx->next_scratch ^= 1;
+    // the tuples are written into scratch buffer kb on the gather stream,
+    // after the run that made them (ev_mat) and after kb's previous copy, two
+    // readbacks ago; the copy stream then copies them to the host.  The next
+    // run waits for the kernel alone (ev_read, wait_readback), so that the
+    // kernel overlaps the next batch's input copy and the copy overlaps the
+    // next run
     CK(cudaEventRecord(ctx->ev_mat, ctx->stream));
-    CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_mat, 0));
-    launch_materialize(ctx->b, stage, first, n, static_cast<int32_t*>(tmp), ctx->copy_stream);
+    CK(cudaStreamWaitEvent(ctx->gather_stream, ctx->ev_mat, 0));
+    if (ctx->copy_pending[kb]) CK(cudaStreamWaitEvent(ctx->gather_stream, ctx->ev_copy[kb], 0));
+    launch_materialize(ctx->b, stage, first, n, static_cast<int32_t*>(tmp), ctx->gather_stream);
     CK(cudaGetLastError());
-    CK(cudaEventRecord(ctx->ev_read, ctx->copy_stream));
+    CK(cudaEventRecord(ctx->ev_read, ctx->gather_stream));
     ctx->read_pending = true;
+    CK(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_read, 0));
     CK(cudaMemcpyAsync(out, tmp, bytes, cudaMemcpyDeviceToHost, ctx->copy_stream));
-    CK(cudaEventRecord(ctx->ev_copy, ctx->copy_stream));
-    ctx->copy_pending = true;
+    CK(cudaEventRecord(ctx->ev_copy[kb], ctx->copy_stream));
+    ctx->copy_pending[kb] = true;
     return SDLG_OK;
 }
 
 int sdlg_wait_objects(sdlg_ctx* ctx) {
     if (!ctx) return SDLG_ERR_ARG;
     cudaSetDevice(ctx->device);
-    if (ctx->copy_pending) {
-        CK(cudaEventSynchronize(ctx->ev_copy));
-        ctx->copy_pending = false;
+    for (int k = 0; k < 2; ++k) {
+        if (ctx->copy_pending[k]) {
+            CK(cudaEventSynchronize(ctx->ev_copy[k]));
+            ctx->copy_pending[k] = false;
+        }
     }
     return SDLG_OK;
 }
@@ -1218,10 +1451,10 @@ int sdlg_get_object_links(sdlg_ctx* ctx, int stage, int64_t event, int32_t* link
     const size_t b_links = (size_t)n * 2 * sizeof(int32_t), b_mod = (size_t)n * sizeof(int32_t);
     const size_t b_vals = (size_t)n * nf * sizeof(float);
     void* vtmp = nullptr;
-    rc = ensure_scratch(ctx, b_links + b_mod + b_vals + 16, &vtmp);
+    rc = ensure_scratch(ctx, 0, b_links + b_mod + b_vals + 16, &vtmp);
     if (rc) return rc;
     char* tmp = static_cast<char*>(vtmp);
-    if (ctx->copy_pending) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0));
+    if (ctx->copy_pending[0]) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_copy[0], 0));
     int32_t* d_links = links ? reinterpret_cast<int32_t*>(tmp) : nullptr;
     int32_t* d_mod = module ? reinterpret_cast<int32_t*>(tmp + b_links) : nullptr;
     float* d_vals = (vals && nf) ? reinterpret_cast<float*>(tmp + b_links + b_mod) : nullptr;

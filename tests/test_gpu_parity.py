@@ -177,6 +177,42 @@ def test_async_readback_before_a_run_on_the_same_buffers(gpu, oracle_lib):
     assert oracle_lib.digest(gpu.objects(4, 0)) == oracle_lib.digest(ref[4])
 
 
+def test_staged_batches(gpu, oracle_lib):
+    """sdlg_stage_events: the next batch copied while the current one runs,
+    taken by the next run; the current batch's results stay readable until
+    then; a batch with another event count waits on the host; set_events
+    drops a staged batch.  Every run's objects against the restatement."""
+    from sdl_gb300 import synth
+    det, e1 = synth.workload_event("pu", 21, pu=60)
+    evs = [e1] + [synth.workload_event("pu", 22 + k, pu=60)[1] for k in range(4)]
+    orc = oracle_lib.Oracle(det)
+    want = [[oracle_lib.digest(o) for o in orc.run(e)[0]] for e in evs]
+
+    def check(batch):
+        for k, e in enumerate(batch):
+            got = [oracle_lib.digest(gpu.objects(s, k)) for s in range(5)]
+            assert got == want[e], (batch, k)
+
+    gpu.upload_detector(det)
+    gpu.set_events([evs[0], evs[1]])
+    gpu.run_async(4, 0)
+    gpu.stage_events([evs[2], evs[3]])  # overlaps the run
+    gpu.sync()
+    check([0, 1])  # still the current batch
+    gpu.run(4, 0)
+    check([2, 3])
+    gpu.stage_events([evs[4], evs[0], evs[1]])  # three events: through the host
+    check([2, 3])
+    gpu.run(4, 0)
+    check([4, 0, 1])
+    gpu.stage_events([evs[3], evs[2], evs[4]])
+    gpu.set_events([evs[1], evs[4], evs[0]])  # drops the staged batch
+    gpu.run(4, 0)
+    check([1, 4, 0])
+    gpu.run(4, 0)  # nothing staged: the same batch again
+    check([1, 4, 0])
+
+
 def test_stop_after_stage(gpu, oracle_lib):
     from sdl_gb300 import synth
     det, ev = synth.workload_event("barrel_flat", 5)
