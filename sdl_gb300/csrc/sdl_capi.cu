@@ -1028,9 +1028,11 @@ int check_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, const f
     return SDLG_OK;
 }
 
-// the staged device batch's layout: x, y, z, idx, detid (S.hits each), then
-// the offsets (S.evs + 1) and the hit count, 256-byte aligned
-size_t stage_off_pos(int64_t hits) { return ((size_t)hits * 20 + 255) / 256 * 256; }
+// the staged device batch's layout: x, y, z, idx, detid (S.hits each, every
+// array 16-byte aligned), then the offsets (S.evs + 1) and the hit count,
+// 256-byte aligned
+size_t stage_stride(int64_t hits) { return (size_t)((hits + 3) / 4) * 16; }
+size_t stage_off_pos(int64_t hits) { return (5 * stage_stride(hits) + 255) / 256 * 256; }
 
 int set_events_impl(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, const float* x, const float* y, const float* z,
                     const int32_t* idx, const uint32_t* detid) {
@@ -1181,7 +1183,7 @@ int sdlg_stage_events(sdlg_ctx* ctx, int64_t n_events, const int64_t* ev_off, co
         }
     }
     for (int k = 0; k < 5 && n > 0; ++k)
-        CK(cudaMemcpyAsync(S.dev + (size_t)k * S.hits * 4, src[k], bytes, cudaMemcpyHostToDevice, S.stream));
+        CK(cudaMemcpyAsync(S.dev + k * stage_stride(S.hits), src[k], bytes, cudaMemcpyHostToDevice, S.stream));
     CK(cudaMemcpyAsync(S.dev + stage_off_pos(S.hits), S.h_off, (n_events + 2) * sizeof(int64_t), cudaMemcpyHostToDevice,
                        S.stream));
     CK(cudaEventRecord(S.ev_in, S.stream));
@@ -1211,7 +1213,7 @@ int install_staged(sdlg_ctx* ctx) {
         S.host_idx.resize(S.n_hit); S.host_det.resize(S.n_hit);
         void* dst[5] = {S.host_f[0].data(), S.host_f[1].data(), S.host_f[2].data(), S.host_idx.data(), S.host_det.data()};
         for (int k = 0; k < 5 && S.n_hit > 0; ++k)
-            CK(cudaMemcpy(dst[k], S.dev + (size_t)k * S.hits * 4, bytes, cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(dst[k], S.dev + k * stage_stride(S.hits), bytes, cudaMemcpyDeviceToHost));
         S.on_host = true;
     }
     if (S.on_host) {
@@ -1226,13 +1228,25 @@ int install_staged(sdlg_ctx* ctx) {
     BatchDev& b = ctx->b;
     cudaStream_t s = ctx->stream;
     CK(cudaStreamWaitEvent(s, S.ev_in, 0));
+    // one copy kernel on the SMs: the copy engines may still be busy with the
+    // previous batch's readback
     void* dstp[5] = {(void*)b.in_x, (void*)b.in_y, (void*)b.in_z, (void*)b.in_idx, (void*)b.in_det};
-    for (int k = 0; k < 5 && S.n_hit > 0; ++k)
-        CK(cudaMemcpyAsync(dstp[k], S.dev + (size_t)k * S.hits * 4, (size_t)S.n_hit * 4, cudaMemcpyDeviceToDevice, s));
     const char* offs = S.dev + stage_off_pos(S.hits);
-    CK(cudaMemcpyAsync(const_cast<int64_t*>(b.ev_off), offs, (S.n_ev + 1) * sizeof(int64_t), cudaMemcpyDeviceToDevice, s));
-    CK(cudaMemcpyAsync(const_cast<int64_t*>(b.n_hit), offs + (S.n_ev + 1) * sizeof(int64_t), sizeof(int64_t),
-                       cudaMemcpyDeviceToDevice, s));
+    CopyJobs j{};
+    for (int k = 0; k < 5; ++k) {
+        j.src[k] = reinterpret_cast<const uint32_t*>(S.dev + k * stage_stride(S.hits));
+        j.dst[k] = static_cast<uint32_t*>(dstp[k]);
+        j.n[k] = S.n_hit;
+    }
+    j.src[5] = reinterpret_cast<const uint32_t*>(offs);
+    j.dst[5] = reinterpret_cast<uint32_t*>(const_cast<int64_t*>(b.ev_off));
+    j.n[5] = (S.n_ev + 1) * 2;
+    j.src[6] = reinterpret_cast<const uint32_t*>(offs + (S.n_ev + 1) * sizeof(int64_t));
+    j.dst[6] = reinterpret_cast<uint32_t*>(const_cast<int64_t*>(b.n_hit));
+    j.n[6] = 2;
+    j.count = 7;
+    launch_copy_words(j, ctx->n_sm, s);
+    CK(cudaGetLastError());
     CK(cudaEventRecord(S.ev_used, s));
     S.used_pending = true;
     ctx->n_ev = S.n_ev;

@@ -2330,6 +2330,27 @@ void enum_and_group(const BatchDev& b, cudaStream_t s, Hooks* h, bool layer_coun
     if (h) h->launches += layer_counters ? 3 : 2;
 }
 
+// device-to-device copies of 4-byte words (job blockIdx.y), 16 bytes at a
+// time where both buffers are 16-byte aligned
+__global__ void __launch_bounds__(256) k_copy_words(CopyJobs j) {
+    const int q = blockIdx.y;
+    if (q >= j.count) return;
+    const uint32_t* __restrict__ src = j.src[q];
+    uint32_t* __restrict__ dst = j.dst[q];
+    const int64_t n = j.n[q];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t done = 0;
+    if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0) {
+        const int64_t n4 = n / 4;
+        const uint4* s4 = reinterpret_cast<const uint4*>(src);
+        uint4* d4 = reinterpret_cast<uint4*>(dst);
+        for (int64_t i = t; i < n4; i += stride) d4[i] = __ldg(s4 + i);
+        done = n4 * 4;
+    }
+    for (int64_t i = done + t; i < n; i += stride) dst[i] = __ldg(src + i);
+}
+
 }  // namespace
 
 void launch_ingest(const BatchDev& b, cudaStream_t s, Hooks* h) {
@@ -2682,6 +2703,11 @@ cudaError_t set_libm_tables(const LibmTab* t) { return cudaMemcpyToSymbol(c_libm
 void launch_libm_eval(int fn, uint32_t start, int64_t n, float* out, int n_sm, cudaStream_t s) {
     if (n <= 0) return;
     k_libm_eval<<<grid_for(n, 256, n_sm * 16), 256, 0, s>>>(fn, start, n, out);
+}
+
+void launch_copy_words(const CopyJobs& j, int n_sm, cudaStream_t s) {
+    if (j.count <= 0) return;
+    k_copy_words<<<dim3((unsigned)(n_sm * 2), (unsigned)j.count), 256, 0, s>>>(j);
 }
 
 void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s) {

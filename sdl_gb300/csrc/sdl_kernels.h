@@ -143,4 +143,15 @@ void launch_links(const BatchDev& b, int st, int64_t first, int64_t n, int64_t l
 // hit-index tuples of stage st for objects [first, first + n) into out (width 2/4/8/8/16)
 void launch_materialize(const BatchDev& b, int st, int64_t first, int64_t n, int32_t* out, cudaStream_t s);
 
+// device-to-device copies of 4-byte words on the SMs, one kernel for up to
+// kCopyJobs buffers (the copy engines may be busy with readbacks)
+constexpr int kCopyJobs = 8;
+struct CopyJobs {
+    const uint32_t* src[kCopyJobs];
+    uint32_t* dst[kCopyJobs];
+    int64_t n[kCopyJobs];  // words
+    int count;
+};
+void launch_copy_words(const CopyJobs& j, int n_sm, cudaStream_t s);
+
 }  // namespace sdlg
